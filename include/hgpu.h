@@ -1,0 +1,235 @@
+/*
+ * hgpu.h — C ABI of the GB300 HorseIR builtin library (libhgpu.so).
+ *
+ * libhgpu is a link-time drop-in for the builtin ("primitive") library of
+ * HorsePower's HorseIR engine: it exports the same `I pfnXxx(V z, V x, ...)`
+ * entry points over the same `V0` value node, so the interpreter
+ * (src/horseir/v3/translator/interpreter.cc:42-60,278-294) and generated C
+ * code (src/horseir/v3/translator/compiler.cc:338-368) can link against it in
+ * place of libcore.a (src/horseir/v3/make.sh:30-43).
+ *
+ * Every declaration below cites the reference interface it replaces.  Paths
+ * are relative to the HorsePower source tree.  Entry points prefixed `hgpu`
+ * are extensions with no counterpart in the reference (device residency,
+ * timing, fused chains, batched plans, serving).
+ *
+ * Conventions kept from the reference (src/horseir/v3/backend/h_primitive.cc:6-14):
+ *   - z is allocated by the caller; the callee fills it (initV semantics).
+ *   - return 0 on success or an E_* code; outputs may alias inputs.
+ *   - vectors of length <= 1 store their element inline in the node
+ *     (src/horseir/v3/backend/h_memory.cc:182-196).
+ *
+ * GB300 additions:
+ *   - Vector payloads (`g`) may live in host memory or in HBM.  Inputs are
+ *     accepted from either; outputs are placed according to the residency
+ *     mode (hgpuSetResidency), HBM by default.  Node structs and list/dict
+ *     node arrays always live in host memory so host code can walk them.
+ *   - Device failures never exit(): they return E_DEVICE-class codes >= 100.
+ */
+#ifndef HGPU_H
+#define HGPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+#ifndef __cplusplus
+#include <stdbool.h>
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Scalar typedefs: src/horseir/v3/backend/common.h:9-22 */
+typedef bool      B;
+typedef char      C, *S, *G;
+typedef int8_t    J;
+typedef int16_t   H;
+typedef int32_t   I, M, D, U, W, T;
+typedef long long L, Q, Z;
+typedef float     F;
+typedef double    E;
+typedef struct { F real, imag; } X;
+struct hgpu_enum_s;   /* reference Y0 (common.h:23); enums are outside the path */
+struct hgpu_table_s;  /* reference A0 (common.h:25); tables are outside the path */
+
+/* Value node: field order and union members of src/horseir/v3/backend/common.h:31-55.
+ * sizeof(V0) == 32 on LP64. */
+typedef struct NodeValue {
+    L len; G g; I typ;
+    union {
+        B b; J j; H h; I i32; L i64; F f32; E f64; C c; Q q; S s;
+        M m; D d; Z z; U u; W w; T t; X x;
+        struct hgpu_enum_s *y; struct hgpu_table_s *a;
+        struct NodeValue *g2;
+    };
+} V0, *V;
+
+/* Type codes: src/horseir/v3/backend/h_type.h:1-23 */
+#define H_B 0
+#define H_J 1
+#define H_H 2
+#define H_I 3
+#define H_L 4
+#define H_F 5
+#define H_E 6
+#define H_X 7
+#define H_C 8
+#define H_Q 9
+#define H_S 10
+#define H_M 11
+#define H_D 12
+#define H_Z 13
+#define H_U 14
+#define H_W 15
+#define H_T 16
+#define H_G 17
+#define H_N 18
+#define H_Y 19
+#define H_A 90
+#define H_K 91
+#define H_V 93
+
+/* Error codes: src/horseir/v3/backend/h_system.h:128-142 */
+#define E_DOMAIN          1
+#define E_GENERAL         2
+#define E_INDEX           3
+#define E_DIV_ZERO        4
+#define E_LENGTH          5
+#define E_TYPE            6
+#define E_NULL_VALUE      7
+#define E_LIKE_PATTERN    8
+#define E_MATCH           9
+#define E_ENUM_INDEX      10
+#define E_RAZE_LIST       11
+#define E_UNKNOWN         12
+#define E_TABLE_NOT_FOUND 50
+#define E_COL_NOT_FOUND   51
+#define E_NOT_IMPL        99
+/* Extensions (no counterpart in the reference, which exit()s instead:
+ * h_memory.cc:110,448, h_hash_v3.cc:27,259). */
+#define E_DEVICE          100  /* a CUDA call failed; the library stays usable if the context does */
+#define E_DEVICE_OOM      101  /* device or pinned-host arena exhausted */
+#define E_DEVICE_TIMEOUT  102  /* a bounded device-side wait gave up (look-back, work queue) */
+#define E_NO_DEVICE       103  /* no CUDA device / library not initialised */
+#define E_ADMISSION       104  /* serving loop refused a request (footprint larger than the pool) */
+#define E_CANCELLED       105  /* serving loop request cancelled before it ran */
+
+/* ---------------- memory / values (src/horseir/v3/backend/h_memory.h:21-45) -------------- */
+/* initBackend: src/horseir/v3/global.cc:26-35 (arena + symbols + cores).  Also creates the
+ * CUDA context, library stream and arenas; safe to call more than once. */
+void initBackend(void);
+V    allocNode(void);                       /* h_memory.cc:160-162 */
+V    initV(V x, I typ, L len);              /* h_memory.cc:182-196 (payload in the output arena) */
+L    getHeapOffset(void);                   /* h_memory.cc:155-157 */
+L    setHeapOffset(L cur);                  /* h_memory.cc:159-161 (rewinds device + host arenas) */
+L    getTypeSize(I typ, L len);             /* h_memory.cc:124-153 */
+/* Symbols: src/horseir/v3/backend/h_symbol.h:38-56 (interning used by @join_index's op list) */
+L    getSymbol(S name);
+S    getSymbolStr(L x);
+
+/* ---------------- builtins on the accelerated path ---------------- */
+/* Stream compaction */
+I pfnCompress(V z, V x, V y);   /* h_primitive.cc:1479-1521 (@compress) */
+I pfnWhere   (V z, V x);        /* h_primitive.cc:728-762  (@where) */
+/* Elementwise compare (h_primitive.cc:1073-1200; float compares use eps=1e-13, h_system.cc:9) */
+I pfnCompare(V z, V x, V y, I op);
+I pfnLt (V z, V x, V y);
+I pfnLeq(V z, V x, V y);
+I pfnGt (V z, V x, V y);
+I pfnGeq(V z, V x, V y);
+I pfnEq (V z, V x, V y);
+I pfnNeq(V z, V x, V y);
+/* Elementwise arithmetic (h_primitive.cc:1227-1309) */
+I pfnArith(V z, V x, V y, I op);
+I pfnPlus (V z, V x, V y);
+I pfnMinus(V z, V x, V y);
+I pfnMul  (V z, V x, V y);
+I pfnDiv  (V z, V x, V y);
+/* Elementwise logic (h_primitive.cc:1315-1357, functions h_system.cc:898-916) */
+I pfnAnd (V z, V x, V y);
+I pfnNand(V z, V x, V y);
+I pfnOr  (V z, V x, V y);
+I pfnNor (V z, V x, V y);
+I pfnXor (V z, V x, V y);
+I pfnNot (V z, V x);            /* h_primitive.cc:606-615 */
+/* Reductions (h_primitive.cc:764-847) */
+I pfnSum(V z, V x);
+I pfnAvg(V z, V x);
+I pfnReduce(V z, V x, I op);
+I pfnMin(V z, V x);
+I pfnMax(V z, V x);
+I pfnLen(V z, V x);             /* h_primitive.cc:656-662 */
+/* Gather / search */
+I pfnIndex  (V z, V x, V y);    /* h_primitive.cc:43-94 */
+I pfnIndexOf(V z, V x, V y);    /* h_primitive.cc:1523-1579 */
+I pfnMember (V z, V y, V x);    /* h_primitive.cc:2287-2336 (note argument order) */
+I pfnJoinIndex(V z, V x, V y, V f); /* h_primitive.cc:2122-2155 */
+/* Grouping and ordering */
+I pfnGroup    (V z, V x);       /* h_primitive.cc:993-999 */
+I pfnGroupTrie(V z, V x);       /* h_primitive.cc:2656-2681 */
+I pfnGroupBasic(V z, V x);      /* h_primitive.cc:1002-1057 */
+I pfnOrderBy  (V z, V x, V y);  /* h_primitive.cc:1769-1816 */
+/* List plumbing used by the segmented-reduction chain (each_right @index -> each @sum -> raze) */
+I pfnList (V z, L n, V x[]);    /* h_primitive.cc:32-36 */
+I pfnKeys (V z, V x);           /* h_primitive.cc:191-203 */
+I pfnValues(V z, V x);          /* h_primitive.cc:205-217 */
+I pfnEach     (V z, V x, I (*foo)(V, V));        /* h_primitive.cc:1818-1832 */
+I pfnEachRight(V z, V x, V y, I (*foo)(V, V, V)); /* h_primitive.cc:1882-1904 */
+I pfnRaze (V z, V x);           /* h_primitive.cc:935-955 */
+
+/* ---------------- fused segmented reductions ----------------
+ * GB300 counterparts of the peephole functions the pattern pass emits for
+ * raze(each(@sum|@avg|@min|@max|@len, each_right(@index, x, groups)))
+ * (src/horseir/v3/optimizer/pattern.cc:63-105 FP1/2/5/6/7, emitter :180-219),
+ * same (V z, V x, V y) convention: x = column, y = list of i64 index vectors
+ * (the values of a @group dict), z = one aggregate per group.  Aggregation
+ * semantics follow the interpreter (pfnSum/pfnAvg/pfnReduce per group). */
+I hgpuGroupSum(V z, V x, V y);
+I hgpuGroupAvg(V z, V x, V y);
+I hgpuGroupMin(V z, V x, V y);
+I hgpuGroupMax(V z, V x, V y);
+I hgpuGroupLen(V z, V x, V y);
+
+/* ---------------- fused chains ----------------
+ * GB300 counterpart of the fused loops emitted by the loop-fusion passes
+ * (src/horseir/v3/optimizer/autofusion.cc:770-935 genCodeAuto,
+ *  elementwise.cc:239-281 genCodeElem, pattern.cc:482-520 genPatternCompress),
+ * called with the same `(V z, V *x)` / `(V *z, V x, V *y)` conventions.
+ * A chain is described by a small text program (grammar in fused.cu) and
+ * compiled once into a single kernel. */
+typedef struct hgpu_chain_s *hgpuChain;
+I hgpuChainCreate(hgpuChain *out, const char *program);
+I hgpuChainRun(hgpuChain c, V z, V *x);           /* autofusion-style: inputs x[0..n) -> z */
+I hgpuChainDestroy(hgpuChain c);
+/* Multi-column compress sharing one mask: pattern.cc:452-520 (V *z, V x, V *y) */
+I hgpuCompressMany(V *z, V x, V *y, L n);
+
+/* ---------------- runtime extensions ---------------- */
+#define HGPU_RESIDENT_DEVICE 0   /* outputs stay in HBM (default) */
+#define HGPU_RESIDENT_HOST   1   /* outputs are copied to pinned host memory on return */
+I    hgpuInit(L device_arena_bytes, L host_arena_bytes);
+I    hgpuSetResidency(I mode);
+I    hgpuGetResidency(void);
+/* Deep copies: device->host (result usable by plain host code) and host->device. */
+I    hgpuToHost(V z, V x);
+I    hgpuToDevice(V z, V x);
+I    hgpuIsDevice(V x);               /* 1 when x's payload lives in HBM */
+I    hgpuSync(void);                  /* wait for the library stream; returns sticky device errors */
+void*hgpuStream(void);                /* the cudaStream_t every kernel is launched on */
+const char *hgpuLastError(void);      /* text of the last error (thread-local) */
+/* Deterministic reductions: 1 (default) = fixed-order tile tree, bit-exact run to run. */
+I    hgpuSetReduceMode(I mode);
+/* Kernel timing on the library stream (CUDA events around each launch when enabled). */
+I    hgpuProfile(I enable);
+I    hgpuProfileReset(void);
+/* Returns the number of distinct kernels recorded; fills names/ms/launches up to cap. */
+I    hgpuProfileRead(I cap, const char **names, double *total_ms, L *launches);
+L    hgpuLaunchCount(void);           /* kernels launched by this library since load */
+/* Event timer on the library stream */
+I    hgpuTimerStart(void);
+double hgpuTimerStop(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HGPU_H */

@@ -1,0 +1,221 @@
+"""Golden-vector cases for the HorseIR builtins on the accelerated path.
+
+Each case is a builtin name plus its arguments, built from seeded numpy
+inputs.  `make_golden.py` runs every case through the reference's own
+builtin library (compiled from its sources) and stores inputs and outputs in
+`golden.npz`; the tests replay the stored inputs through the oracle port
+(CPU suite) and through libhgpu (GPU suite) and compare.
+
+Argument encoding (so a fixture can be rebuilt without this module):
+  ("vec", array, typ) | ("scalar", value, typ) | ("sym", name) | ("list", [args]) | ("bools", array)
+Case flags:
+  tol        relative tolerance for float outputs (0 = bit-exact)
+  canonical  compare a @group / @order result up to the order of tied rows
+             (reference paths built on its unstable quicksort)
+  error      the case is expected to return this E_* code
+"""
+import numpy as np
+
+H_B, H_J, H_H, H_I, H_L, H_F, H_E, H_C, H_D = 0, 1, 2, 3, 4, 5, 6, 8, 12
+
+
+def V(a, typ):
+    return ("vec", np.asarray(a), typ)
+
+
+def S(v, typ):
+    return ("scalar", v, typ)
+
+
+def Ls(*items):
+    return ("list", list(items))
+
+
+def build_cases():
+    rng = np.random.default_rng(20261203)
+    cases = []
+
+    def add(name, fn, *args, tol=0.0, canonical=False, error=0):
+        cases.append(dict(name=name, fn=fn, args=list(args), tol=tol, canonical=canonical, error=error))
+
+    # ---- reference documentation examples (docs/mkdocs/docs/horseir/builtin/*.md)
+    add("doc_compress", "pfnCompress", V([1, 1, 0], H_B), V([53, 11, 12], H_I))
+    add("doc_group", "pfnGroup", V([-1, 3, 2, 3], H_I))
+    add("doc_order", "pfnOrderBy", V([32, 12, 7, 78, 23, 45], H_I), V([1], H_B))
+
+    # ---- @compress / @where (h_primitive.cc:1479-1521, :728-762)
+    n = 20000
+    for dens, tag in [(0.3, "r30"), (0.018, "sparse"), (0.0, "none"), (1.0, "all")]:
+        m = rng.random(n) < dens
+        for typ, dt in [(H_B, np.bool_), (H_J, np.int8), (H_H, np.int16), (H_I, np.int32),
+                        (H_L, np.int64), (H_F, np.float32), (H_E, np.float64), (H_C, np.int8)]:
+            vals = (rng.integers(-100, 100, n) if dt not in (np.float32, np.float64)
+                    else rng.standard_normal(n)).astype(dt)
+            add(f"compress_{tag}_{typ}", "pfnCompress", V(m, H_B), V(vals, typ))
+        add(f"where_{tag}", "pfnWhere", V(m, H_B))
+    add("compress_empty", "pfnCompress", V(np.zeros(0, bool), H_B), V(np.zeros(0, np.float64), H_E))
+    add("compress_one", "pfnCompress", V([True], H_B), V([2.5], H_E))
+    add("compress_len_mismatch", "pfnCompress", V([True, False], H_B), V([1, 2, 3], H_I), error=5)
+    add("compress_not_bool", "pfnCompress", V([1, 0], H_I), V([1, 2], H_I), error=1)
+    add("where_small", "pfnWhere", V(rng.random(500) < 0.5, H_B))
+    add("where_odd", "pfnWhere", V(rng.random(12345) < 0.5, H_B))
+
+    # ---- compares (h_primitive.cc:1073-1200, eps 1e-13)
+    xi = rng.integers(-60, 60, n).astype(np.int32)
+    xe = np.round(rng.standard_normal(n), 2)
+    xe[:50] = 0.05 + np.array([0, 1e-14, -1e-14, 5e-14, -5e-14, 2e-13, -2e-13, 1e-12, -1e-12, 0] * 5)
+    xe[50] = np.nan
+    for op in ["pfnLt", "pfnLeq", "pfnGt", "pfnGeq", "pfnEq", "pfnNeq"]:
+        add(f"{op}_i32_s", op, V(xi, H_I), S(24, H_I))
+        add(f"{op}_f64_s", op, V(xe, H_E), S(0.05, H_E))
+        add(f"{op}_s_f64", op, S(0.05, H_E), V(xe, H_E))
+        add(f"{op}_i32_f64", op, V(xi, H_I), V(xe * 30, H_E))
+        add(f"{op}_j_h", op, V(rng.integers(-5, 5, 300).astype(np.int8), H_J),
+            V(rng.integers(-5, 5, 300).astype(np.int16), H_H))
+        add(f"{op}_date_s", op, V(rng.integers(8000, 10526, 3000).astype(np.int32), H_D), S(8766, H_D))
+        add(f"{op}_char", op, V(rng.integers(0, 120, 300).astype(np.int8), H_C),
+            V(rng.integers(0, 120, 300).astype(np.int8), H_C))
+        add(f"{op}_f32_s", op, V(rng.standard_normal(500).astype(np.float32), H_F), S(0.25, H_F))
+    add("cmp_len_mismatch", "pfnLt", V([1, 2, 3], H_I), V([1, 2], H_I), error=5)
+    add("cmp_type", "pfnLt", V([1, 2], H_I), V([1, 2], H_D), error=6)
+
+    # ---- arithmetic (h_primitive.cc:1227-1309)
+    a32 = rng.integers(-2 ** 31, 2 ** 31 - 1, 3000, dtype=np.int64).astype(np.int32)
+    b32 = rng.integers(-2 ** 31, 2 ** 31 - 1, 3000, dtype=np.int64).astype(np.int32)
+    b32[b32 == 0] = 7
+    for op in ["pfnPlus", "pfnMinus", "pfnMul", "pfnDiv"]:
+        add(f"{op}_i32", op, V(a32, H_I), V(b32, H_I))
+        add(f"{op}_f64", op, V(rng.standard_normal(3000), H_E), V(rng.standard_normal(3000) + 3, H_E))
+        add(f"{op}_i32_f64_s", op, V(a32, H_I), S(1.5, H_E))
+        add(f"{op}_s_i64", op, S(7, H_L), V(b32.astype(np.int64), H_L))
+        add(f"{op}_j", op, V(rng.integers(-128, 127, 500).astype(np.int8), H_J),
+            V(rng.integers(1, 127, 500).astype(np.int8), H_J))
+        add(f"{op}_b", op, V(rng.random(200) < 0.5, H_B), V(np.ones(200, bool), H_B))
+        add(f"{op}_f32", op, V(rng.standard_normal(500).astype(np.float32), H_F),
+            V((rng.standard_normal(500) + 4).astype(np.float32), H_F))
+    add("div_zero", "pfnDiv", V([1, 2, 3], H_I), V([1, 0, 3], H_I), error=4)
+    add("div_zero_f", "pfnDiv", V([1.0, 2.0], H_E), V([1.0, 0.0], H_E), error=4)
+    add("mul_q6", "pfnMul", V(np.round(rng.uniform(900, 105000, 4000) * 3 / 100, 2), H_E),
+        V(rng.integers(0, 11, 4000) / 100.0, H_E))
+
+    # ---- logic (h_primitive.cc:1315-1357)
+    ba, bb = rng.random(5000) < 0.5, rng.random(5000) < 0.5
+    for op in ["pfnAnd", "pfnNand", "pfnOr", "pfnNor", "pfnXor"]:
+        add(f"{op}_vv", op, V(ba, H_B), V(bb, H_B))
+        add(f"{op}_vs", op, V(ba, H_B), S(True, H_B))
+    add("not", "pfnNot", V(ba, H_B))
+
+    # ---- reductions (h_primitive.cc:764-847)
+    for typ, arr in [(H_B, rng.random(9000) < 0.5), (H_J, rng.integers(-128, 127, 9000).astype(np.int8)),
+                     (H_H, rng.integers(-30000, 30000, 9000).astype(np.int16)),
+                     (H_I, rng.integers(-2 ** 31, 2 ** 31 - 1, 9000, dtype=np.int64).astype(np.int32)),
+                     (H_L, rng.integers(-2 ** 62, 2 ** 62, 9000, dtype=np.int64)),
+                     (H_E, rng.uniform(0, 1e5, 9000)), (H_F, rng.uniform(0, 10, 9000).astype(np.float32))]:
+        tol = 1e-12 if typ == H_E else (1e-5 if typ == H_F else 0.0)
+        add(f"sum_{typ}", "pfnSum", V(arr, typ), tol=tol)
+        add(f"avg_{typ}", "pfnAvg", V(arr, typ), tol=tol if tol else 1e-15)
+        if typ != H_F:
+            add(f"min_{typ}", "pfnMin", V(arr, typ))
+            add(f"max_{typ}", "pfnMax", V(arr, typ))
+    for typ, dt in [(H_I, np.int32), (H_E, np.float64), (H_F, np.float32)]:
+        add(f"min_empty_{typ}", "pfnMin", V(np.zeros(0, dt), typ))
+        add(f"max_empty_{typ}", "pfnMax", V(np.zeros(0, dt), typ))
+        add(f"sum_empty_{typ}", "pfnSum", V(np.zeros(0, dt), typ))
+    add("sum_one", "pfnSum", V([3.25], H_E))
+    add("len", "pfnLen", V(xe, H_E))
+
+    # ---- gather (h_primitive.cc:43-94)
+    src = {H_E: rng.standard_normal(7000), H_I: rng.integers(-99, 99, 7000).astype(np.int32),
+           H_C: rng.integers(0, 120, 7000).astype(np.int8), H_B: rng.random(7000) < 0.5,
+           H_L: rng.integers(-2 ** 40, 2 ** 40, 7000, dtype=np.int64)}
+    idx = rng.integers(0, 7000, 9000).astype(np.int64)
+    for typ, arr in src.items():
+        add(f"index_{typ}", "pfnIndex", V(arr, typ), V(idx, H_L))
+    add("index_oob", "pfnIndex", V(src[H_E], H_E), V([1, 7000], H_L), error=3)
+    add("index_scalar", "pfnIndex", V(src[H_I], H_I), S(5, H_L))
+
+    # ---- index_of (h_primitive.cc:1523-1579)
+    x = rng.permutation(30000)[:8000].astype(np.int32)
+    add("index_of_i32", "pfnIndexOf", V(x, H_I), V(rng.integers(0, 30000, 12000).astype(np.int32), H_I))
+    dup = rng.integers(0, 500, 4000).astype(np.int64)
+    add("index_of_i64_dup", "pfnIndexOf", V(dup, H_L), V(rng.integers(0, 700, 5000).astype(np.int64), H_L))
+    asc = np.sort(rng.integers(0, 5000, 3000)).astype(np.int32)
+    add("index_of_sorted", "pfnIndexOf", V(asc, H_I), V(rng.integers(-10, 5010, 4000).astype(np.int32), H_I))
+    add("index_of_desc", "pfnIndexOf", V(asc[::-1].copy(), H_I), V(rng.integers(0, 5000, 4000).astype(np.int32), H_I))
+    add("index_of_const", "pfnIndexOf", V(np.full(50, 7, np.int64), H_L), V([7, 8, 7], H_L))
+    fx = np.round(rng.standard_normal(3000), 3)
+    add("index_of_f64", "pfnIndexOf", V(fx, H_E), V(np.round(rng.standard_normal(3000), 3), H_E))
+    add("index_of_bool", "pfnIndexOf", V(rng.random(100) < 0.7, H_B), V(rng.random(50) < 0.5, H_B))
+    add("index_of_mixed", "pfnIndexOf", V(rng.integers(0, 100, 300).astype(np.int16), H_H),
+        V(rng.integers(0, 120, 400).astype(np.int32), H_I))
+
+    # ---- member (h_primitive.cc:2287-2336): pfnMember(z, probe, set)
+    add("member_i32", "pfnMember", V(rng.integers(0, 3000, 9000).astype(np.int32), H_I),
+        V(rng.integers(0, 3000, 1500).astype(np.int32), H_I))
+    add("member_i64_small2", "pfnMember", V(rng.integers(0, 5, 400).astype(np.int64), H_L), V([1, 3], H_L))
+    add("member_i64_small1", "pfnMember", V(rng.integers(0, 5, 400).astype(np.int64), H_L), V([4], H_L))
+    add("member_f64", "pfnMember", V(np.round(rng.standard_normal(3000), 2), H_E),
+        V(np.round(rng.standard_normal(800), 2), H_E))
+    add("member_bool", "pfnMember", V(rng.random(100) < 0.5, H_B), V([True, True], H_B))
+    add("member_mixed", "pfnMember", V(rng.integers(0, 100, 300).astype(np.int32), H_I),
+        V(rng.integers(0, 100, 40).astype(np.int64), H_L))
+
+    # ---- join_index (h_primitive.cc:2122-2155; hash v3 for i32 keys)
+    pk = rng.permutation(40000).astype(np.int32)[:9000]
+    fk = rng.integers(0, 40000, 30000).astype(np.int32)
+    add("join_pk_fk", "pfnJoinIndex", V(pk, H_I), V(fk, H_I), ("sym", "eq"))
+    add("join_fk_pk_swapped", "pfnJoinIndex", V(fk, H_I), V(pk, H_I), ("sym", "eq"))
+    bdup = rng.integers(0, 300, 2000).astype(np.int32)
+    add("join_dup_build", "pfnJoinIndex", V(bdup, H_I), V(rng.integers(0, 400, 5000).astype(np.int32), H_I), ("sym", "eq"))
+    add("join_equal_len", "pfnJoinIndex", V(rng.integers(0, 50, 1000).astype(np.int32), H_I),
+        V(rng.integers(0, 50, 1000).astype(np.int32), H_I), ("sym", "eq"))
+    add("join_linear_small", "pfnJoinIndex", V([5, 3, 5, 9], H_I), V(rng.integers(0, 10, 500).astype(np.int32), H_I), ("sym", "eq"))
+    add("join_linear_neq", "pfnJoinIndex", V([5, 3], H_I), V(rng.integers(0, 10, 50).astype(np.int32), H_I), ("sym", "neq"))
+    add("join_linear_f64", "pfnJoinIndex", V([0.5, 0.25, 0.5], H_E), V(rng.integers(0, 4, 60) / 4.0, H_E), ("sym", "eq"))
+    add("join_no_match", "pfnJoinIndex", V(np.arange(100, 200, dtype=np.int32), H_I), V(np.arange(0, 50, dtype=np.int32), H_I), ("sym", "eq"))
+    add("join_mixed_types", "pfnJoinIndex", V(rng.permutation(500).astype(np.int16)[:200], H_H),
+        V(rng.integers(0, 500, 900).astype(np.int32), H_I), ("sym", "eq"))
+
+    # ---- group (h_primitive.cc:993-1057, 2656-2681)
+    add("group_i32", "pfnGroup", V(rng.integers(0, 700, 10000).astype(np.int32), H_I))
+    add("group_i32_neg", "pfnGroup", V(rng.integers(-300, 300, 6000).astype(np.int32), H_I))
+    add("group_i64_small", "pfnGroup", V(rng.integers(-1000, 1000, 6000).astype(np.int64), H_L))
+    add("group_i64_wide", "pfnGroup", V(rng.integers(0, 5, 4000).astype(np.int64) * (2 ** 33) + rng.integers(0, 3, 4000), H_L))
+    add("group_i64_mixed_hi", "pfnGroup", V(np.array([-1, 4294967295, 5, -1, 4294967295, 7, 2 ** 40, -1], np.int64), H_L))
+    add("group_sorted", "pfnGroup", V(np.sort(rng.integers(0, 90, 3000)).astype(np.int32), H_I))
+    add("group_trie", "pfnGroup", Ls(V(rng.integers(0, 3, 12000).astype(np.int8), H_C), V(rng.integers(0, 2, 12000).astype(np.int8), H_C)))
+    add("group_list_ii", "pfnGroup", Ls(V(rng.integers(0, 20, 5000).astype(np.int32), H_I), V(rng.integers(0, 20, 5000).astype(np.int32), H_I)))
+    add("group_list_li", "pfnGroup", Ls(V(rng.integers(-30, 30, 5000).astype(np.int64), H_L), V(rng.integers(-5, 5, 5000).astype(np.int32), H_I)))
+    add("group_list_jj", "pfnGroup", Ls(V(rng.integers(0, 3, 5000).astype(np.int8), H_J), V(rng.integers(0, 2, 5000).astype(np.int8), H_J)), canonical=True)
+    add("group_f64", "pfnGroup", V(np.round(rng.standard_normal(3000), 1), H_E), canonical=True)
+    add("group_char", "pfnGroup", V(rng.integers(0, 60, 3000).astype(np.int8), H_C))
+    add("group_empty", "pfnGroup", V(np.zeros(0, np.int32), H_I))
+
+    # ---- order (h_primitive.cc:1769-1816)
+    oi = rng.integers(-50, 50, 6000).astype(np.int32)
+    add("order_i32_asc", "pfnOrderBy", V(oi, H_I), V([1], H_B))
+    add("order_i32_desc", "pfnOrderBy", V(oi, H_I), V([0], H_B))
+    ol = rng.integers(0, 3000, 6000).astype(np.int64)
+    add("order_i64_asc", "pfnOrderBy", V(ol, H_L), V([1], H_B))
+    add("order_i64_desc", "pfnOrderBy", V(ol, H_L), V([0], H_B))
+    add("order_case1", "pfnOrderBy", Ls(V(rng.integers(0, 40, 5000).astype(np.int32), H_I), V(rng.integers(-20, 20, 5000).astype(np.int32), H_I)), V([1, 1], H_B))
+    add("order_case1_desc", "pfnOrderBy", Ls(V(rng.integers(0, 40, 5000).astype(np.int32), H_I), V(rng.integers(0, 20, 5000).astype(np.int32), H_I)), V([0, 0], H_B))
+    k2 = rng.integers(0, 200, 8000).astype(np.int64)
+    s2 = rng.integers(0, 2 ** 20, 8000).astype(np.int32)
+    add("order_list_li_asc", "pfnOrderBy", Ls(V(k2, H_L), V(s2, H_I)), V([1, 1], H_B))
+    add("order_list_li_mixed", "pfnOrderBy", Ls(V(k2, H_L), V(s2, H_I)), V([1, 0], H_B))
+    add("order_list_li_desc", "pfnOrderBy", Ls(V(k2, H_L), V(s2, H_I)), V([0, 1], H_B))
+    add("order_list_sorted_desc", "pfnOrderBy", Ls(V(np.sort(k2), H_L), V(s2, H_I)), V([0, 1], H_B))
+    add("order_list_3col", "pfnOrderBy", Ls(V(rng.integers(0, 5, 3000).astype(np.int32), H_I), V(rng.integers(0, 5, 3000).astype(np.int64), H_L),
+                                            V(rng.integers(0, 50, 3000).astype(np.int32), H_I)), V([1, 0, 1], H_B))
+    add("order_f64", "pfnOrderBy", V(np.round(rng.standard_normal(3000), 1), H_E), V([1], H_B), canonical=True)
+    add("order_char", "pfnOrderBy", V(rng.integers(0, 100, 3000).astype(np.int8), H_C), V([1], H_B))
+    add("order_char_small", "pfnOrderBy", V([5, 3, 9, 3, 1], H_C), V([1], H_B))
+
+    # ---- segmented reductions through each_right/each/raze (h_primitive.cc:1818-1904, 935-955)
+    gk = rng.integers(0, 40, 5000).astype(np.int32)
+    cases.append(dict(name="group_sum_chain", fn="@chain_group_agg", args=[V(gk, H_I), V(rng.uniform(0, 1e5, 5000), H_E)],
+                      tol=1e-12, canonical=False, error=0))
+    cases.append(dict(name="group_sum_chain_i32", fn="@chain_group_agg", args=[V(gk, H_I), V(rng.integers(-1000, 1000, 5000).astype(np.int32), H_I)],
+                      tol=0.0, canonical=False, error=0))
+    return cases
