@@ -1,0 +1,342 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 HorseIR builtin library.
+
+Workload (one "step"): the join + low-cardinality group-by query on seeded
+synthetic tables -- a 59,986,052-row fact table joined to a 15,000,000-row
+dimension filtered on a 365-day date window, the matches grouped on two
+1-byte columns (6 groups) with sum/avg/count aggregates -- run as the
+interpreter's sequence of builtin calls through libhgpu's C ABI.
+
+  value   fact rows / s with the tables resident in HBM
+  e2e     the same through the public API from pinned host buffers: the
+          step's input columns are copied host->device and the six result
+          vectors read back inside the timed region
+  roofline  the kernel with the largest device time in the timed region:
+          algorithmic bytes (inputs read once + outputs written once) / its
+          CUDA-event time, against the measured HBM copy bandwidth
+  cpu_baseline  the CPU oracle port (a restatement of the reference's
+          builtins, OpenMP like the reference) on a bounded sample
+
+`--impl reference` runs the same query through the CPU oracle port on all
+host cores instead (the reference library itself cannot be built where its
+sources are absent).  Multi-GPU: every rank runs its own replica (weak
+scaling, no collective on the data path).
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+from horsepower_gb300 import data as D  # noqa: E402
+from horsepower_gb300 import plans as P  # noqa: E402
+from horsepower_gb300.abi import Builtins, V0  # noqa: E402
+
+ESIZE = {3: 4, 6: 8, 8: 1, 1: 1, 4: 8, 0: 1}
+METRIC = "GB/s & rows/s per builtin; batched q/s and p99 vs plain per-op launches"
+WORKLOAD = ("join + group-by: fact 59,986,052 x dim 15,000,000 (365-day filter), "
+            "join_index, 5 gathers, group on (flag,status) -> 6 groups, sum/avg/count")
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", os.environ.get("LOCAL_RANK", "0")],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init(n_gpus):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return rank, ws, dist
+    return 0, 1, None
+
+
+def barrier_max(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def algorithmic_bytes(F, Dn, Dp, M, G):
+    """Per-kernel compulsory bytes of one step (inputs read once + outputs
+    written once), by kernel name; hash tables and sort passes not counted."""
+    return {
+        "compare": 2 * (4 + 1) * Dn,                          # two date compares over the dimension
+        "logic": 3 * Dn,                                      # and of the two masks
+        "compact": (1 + 4) * Dn + 4 * Dp,                     # compress pk by the mask
+        "hash_build": 4 * Dp,                                 # build keys
+        "join_probe": 4 * F + 16 * M,                         # probe keys in, index pairs out
+        "gather": 5 * 8 * M + 2 * 2 * M + 3 * 16 * M + 2 * 8 * G * 2,  # row ids + values in, values out
+        "onesweep": 2 * 2 * M,                                # group key bytes (2 x 1 byte) in
+        "widen": 8 * M,
+        "seg_chunk": 3 * (8 + 8) * M,                         # rows + values of three aggregates
+        "seg_small": 3 * (8 + 8) * M,
+    }
+
+
+def run_gb300(args, rank, ws, dist):
+    import horsepower_gb300
+    gpu = horsepower_gb300.load()
+    Lb = gpu.lib
+    Lb.hgpuTimerStop.restype = C.c_double
+    Lb.hgpuLaunchCount.restype = C.c_longlong
+    Lb.hgpuProfileRead.restype = C.c_int32
+    Lb.hgpuProfileRead.argtypes = [C.c_int32, C.POINTER(C.c_char_p), C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+    Lb.initV.restype = C.c_void_p
+    Lb.initV.argtypes = [C.c_void_p, C.c_int32, C.c_longlong]
+    Lb.getHeapOffset.restype = C.c_longlong
+    Lb.setHeapOffset.argtypes = [C.c_longlong]
+
+    F, Dn = args.fact, args.dim
+    dim, fact = D.join_tables(F, Dn, seed=1 + rank)
+    # device-resident copies of the tables
+    host = {}
+    dev = {}
+    for tab, cols, types in (("dim", dim, P.DIM_TYPES), ("fact", fact, P.FACT_TYPES)):
+        for k, v in cols.items():
+            hv = gpu.vec(v, types[k])
+            dv = V0()
+            rc = Lb.hgpuToDevice(C.byref(dv), C.byref(hv))
+            assert rc == 0, rc
+            host[(tab, k)] = hv
+            dev[(tab, k)] = dv
+    Lb.hgpuSync()
+    ddim = {k: dev[("dim", k)] for k in dim}
+    dfact = {k: dev[("fact", k)] for k in fact}
+
+    def step(d_, f_):
+        mark = Lb.getHeapOffset()
+        out = P.join_group(gpu, d_, f_)
+        Lb.hgpuSync()
+        Lb.setHeapOffset(mark)
+        return out
+
+    for _ in range(args.warmup):
+        step(ddim, dfact)
+    # shapes of one step, for the algorithmic bytes
+    mark = Lb.getHeapOffset()
+    res = P.join_group(gpu, ddim, dfact)
+    res_np = [gpu.to_py(r) for r in res]
+    Lb.setHeapOffset(mark)
+    M = int(res_np[5].sum())
+    sel = ((dim["date"] >= D.WIN_LO) & (dim["date"] < D.WIN_HI))
+    Dp = int(sel.sum())
+    G = len(res_np[0])
+
+    # ---- timed region (device resident)
+    clocks = Clocks()
+    if dist:
+        dist.barrier()
+    Lb.hgpuSync()
+    Lb.hgpuProfileReset()
+    Lb.hgpuProfile(1)
+    launches0 = Lb.hgpuLaunchCount()
+    clocks.start()
+    Lb.hgpuTimerStart()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step(ddim, dfact)
+    ms = Lb.hgpuTimerStop()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    launches = Lb.hgpuLaunchCount() - launches0
+    Lb.hgpuProfile(0)
+    cap = 128
+    names = (C.c_char_p * cap)()
+    tot = (C.c_double * cap)()
+    cnt = (C.c_longlong * cap)()
+    nk = Lb.hgpuProfileRead(cap, names, tot, cnt)
+    kernels = sorted(((names[i].decode(), tot[i], cnt[i]) for i in range(min(nk, cap))), key=lambda r: -r[1])
+    ms = barrier_max(dist, ms)
+    step_ms = ms / args.steps
+
+    # ---- e2e: host (pinned) buffers -> device inside the timed region, results back
+    pinned = {}
+    for key, hv in host.items():
+        pv = V0()
+        Lb.initV(C.byref(pv), hv.typ, hv.len)  # caller allocation: pinned host arena
+        C.memmove(pv.g, hv.g, hv.len * ESIZE[hv.typ])
+        pinned[key] = pv
+    h2d = sum(v.len * ESIZE[v.typ] for v in pinned.values())
+
+    def e2e_step():
+        mark = Lb.getHeapOffset()
+        dv = {}
+        for key, pv in pinned.items():
+            z = V0()
+            Lb.hgpuToDevice(C.byref(z), C.byref(pv))
+            dv[key] = z
+        out = P.join_group(gpu, {k: dv[("dim", k)] for k in dim}, {k: dv[("fact", k)] for k in fact})
+        vals = [gpu.to_py(o) for o in out]
+        Lb.setHeapOffset(mark)
+        return vals
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    if dist:
+        dist.barrier()
+    Lb.hgpuSync()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals = e2e_step()
+    e2e_s = barrier_max(dist, time.perf_counter() - t0)
+    d2h = sum(v.nbytes for v in vals)
+
+    out = dict(rows_per_step=F, step_ms=step_ms, wall_s=wall, launches=launches, kernels=kernels,
+               clocks=clk, e2e_rows_s=ws * F * args.steps / e2e_s, e2e_ms=1000 * e2e_s / args.steps,
+               h2d=h2d, d2h=d2h, shapes=dict(F=F, D=Dn, Dp=Dp, M=M, G=G), result=[v.tolist() for v in res_np])
+    return out
+
+
+def cpu_sample(args):
+    """The oracle port on a bounded sample of the workload (fact and dim scaled by 1/10)."""
+    ora = Builtins(os.path.join(ROOT, "oracle", "_build", "liboracle.so"), "oracle")
+    F, Dn = args.fact // args.cpu_scale, args.dim // args.cpu_scale
+    dim, fact = D.join_tables(F, Dn, seed=101)
+    hd, hf = P.host_nodes(ora, dim, P.DIM_TYPES), P.host_nodes(ora, fact, P.FACT_TYPES)
+    times = []
+    for _ in range(args.cpu_reps):
+        mark = ora.lib.getHeapOffset()
+        t0 = time.perf_counter()
+        P.join_group(ora, hd, hf)
+        times.append(time.perf_counter() - t0)
+        ora.lib.setHeapOffset(mark)
+    t = statistics.median(times)
+    return dict(value=F / t, unit="rows/s", cores=os.cpu_count(), kind="port",
+                sample=f"fact {F:,} x dim {Dn:,} rows (1/{args.cpu_scale} of the workload), median of {len(times)}")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--fact", type=int, default=59_986_052)
+    ap.add_argument("--dim", type=int, default=15_000_000)
+    ap.add_argument("--cpu-scale", type=int, default=10)
+    ap.add_argument("--cpu-reps", type=int, default=3)
+    args = ap.parse_args()
+    rank, ws, dist = dist_init(args.gpus)
+
+    if args.impl == "reference":
+        os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+        if rank != 0:
+            return
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
+        cb = cpu_sample(args)
+        print(json.dumps({"metric": METRIC, "value": cb["value"], "unit": "rows/s", "n_gpus": args.gpus,
+                          "steps": args.cpu_reps, "warmup": 0, "ms_per_step": 1000 * (args.fact // args.cpu_scale) / cb["value"],
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
+                          "data": "synthetic (seeded)", "impl": "reference",
+                          "config": {"workload": WORKLOAD, "sample": cb["sample"]},
+                          "cpu_baseline": cb,
+                          "e2e": {"value": cb["value"], "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+
+    r = run_gb300(args, rank, ws, dist)
+    if rank != 0:
+        return
+    hbm, src = peaks()
+    sh = r["shapes"]
+    alg = algorithmic_bytes(sh["F"], sh["D"], sh["Dp"], sh["M"], sh["G"])
+    top = r["kernels"][0]
+    per_step_ms = {k: t / args.steps for k, t, _ in r["kernels"]}
+    tb = alg.get(top[0])
+    achieved = (tb / (top[1] / args.steps / 1000) / 1e9) if tb else None
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get(top[0])
+    builtins = {}
+    for k, t, n in r["kernels"]:
+        b = alg.get(k)
+        builtins[k] = {"ms_per_step": round(t / args.steps, 4), "launches_per_step": n / args.steps,
+                       "gbs": round(b / (t / args.steps / 1000) / 1e9, 1) if b else None}
+    cpu = cpu_sample(args)
+    value = ws * sh["F"] / (r["step_ms"] / 1000)
+    line = {
+        "metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["step_ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32+f64", "data": "synthetic (seeded, reference-shaped)",
+        "config": {"workload": WORKLOAD, "fact_rows": sh["F"], "dim_rows": sh["D"], "dim_selected": sh["Dp"],
+                   "matches": sh["M"], "groups": sh["G"], "l2": "inputs larger than L2 (1.9 GB per step)",
+                   "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": r["e2e_rows_s"], "unit": "rows/s", "h2d_bytes_per_step": r["h2d"],
+                "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"]},
+        "roofline": {"bound": "hbm", "kernel": top[0], "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": (achieved / hbm) if achieved else None, "peak_source": src,
+                     "traffic": traffic, "algorithmic_bytes_per_step": tb},
+        "cpu_baseline": cpu,
+        "gpu_launches": r["launches"],
+        "clocks": r["clocks"],
+        "kernels_ms_per_step": {k: round(v, 4) for k, v in per_step_ms.items()},
+        "builtins": builtins,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -79,20 +79,13 @@ class Builtins:
             if hasattr(L, f):
                 getattr(L, f).restype = C.c_int32
                 getattr(L, f).argtypes = [PV, PV, PV]
-        L.pfnJoinIndex.restype = C.c_int32
-        L.pfnJoinIndex.argtypes = [PV, PV, PV, PV]
-        L.pfnCompare.restype = C.c_int32
-        L.pfnCompare.argtypes = [PV, PV, PV, C.c_int32]
-        L.pfnArith.restype = C.c_int32
-        L.pfnArith.argtypes = [PV, PV, PV, C.c_int32]
-        L.pfnReduce.restype = C.c_int32
-        L.pfnReduce.argtypes = [PV, PV, C.c_int32]
-        L.pfnList.restype = C.c_int32
-        L.pfnList.argtypes = [PV, C.c_longlong, C.POINTER(PV)]
-        L.pfnEach.restype = C.c_int32
-        L.pfnEach.argtypes = [PV, PV, C.c_void_p]
-        L.pfnEachRight.restype = C.c_int32
-        L.pfnEachRight.argtypes = [PV, PV, PV, C.c_void_p]
+        for f, at in [("pfnJoinIndex", [PV, PV, PV, PV]), ("pfnCompare", [PV, PV, PV, C.c_int32]),
+                      ("pfnArith", [PV, PV, PV, C.c_int32]), ("pfnReduce", [PV, PV, C.c_int32]),
+                      ("pfnList", [PV, C.c_longlong, C.POINTER(PV)]), ("pfnEach", [PV, PV, C.c_void_p]),
+                      ("pfnEachRight", [PV, PV, PV, C.c_void_p])]:
+            if hasattr(L, f):
+                getattr(L, f).restype = C.c_int32
+                getattr(L, f).argtypes = at
         L.getSymbol.restype = C.c_longlong
         L.getSymbol.argtypes = [C.c_char_p]
         L.getHeapOffset.restype = C.c_longlong

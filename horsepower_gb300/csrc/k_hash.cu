@@ -1,0 +1,682 @@
+// Hash-based builtins: @index_of, @member, @join_index.
+//
+// Reference (src/horseir/v3/backend):
+//   pfnIndexOf  h_primitive.cc:1523-1579 — first row of x holding y[i], else
+//               len(x).  A monotone (or constant) i32/i64 x takes the
+//               recursive binary search of searchOrdered (h_system.cc:715-745),
+//               which returns whatever matching row the recursion lands on
+//               and misses on descending x; that recursion is reproduced.
+//               Bool uses lib_index_of_B (h_libs.cc:309-314), whose flag
+//               table maps `true` to row 0 always.
+//   pfnMember   h_primitive.cc:2287-2336 (z, probe, set) — sets of <= 2
+//               elements compare directly, larger sets hash.
+//   pfnJoinIndex h_primitive.cc:2122-2155 + lib_join_radix_hash_v3
+//               (h_hash_v3.cc:230-260): the shorter side is built; for each
+//               probe row in order every matching build row in order is
+//               emitted; builds of < 10 rows use the linear join, which keeps
+//               only the first match (h_libs.cc:1542-1575).
+//
+// GB300 design: open-addressing tables in HBM (linear probing, murmur3
+// finaliser, capacity = next power of two >= n / load factor).  Slots hold
+// the key and the minimum row (atomicMin), plus a count for joins.  The join
+// probe is one pass over the probe side: a tile of 4096 probe rows looks up
+// its keys, takes its output offset from a decoupled look-back and writes the
+// (build row, probe row) pairs with ballot/popc compaction.  Keys with
+// duplicate build rows use a count / scan / write path over a CSR of build
+// rows sorted per slot.
+#include "dev_common.cuh"
+
+namespace hg {
+
+I scan_exclusive(const unsigned* in, long long n, unsigned long long* out, unsigned long long* total_h);
+
+static double g_load_factor = 0.5;  // autotuned 0.5 - 0.8
+void set_hash_load_factor(double f) { g_load_factor = f < 0.25 ? 0.25 : (f > 0.9 ? 0.9 : f); }
+
+__device__ __forceinline__ unsigned long long fmix64(unsigned long long k) {
+    k ^= k >> 33; k *= 0xff51afd7ed558ccdULL; k ^= k >> 33; k *= 0xc4ceb9fe1a85ec53ULL; k ^= k >> 33;
+    return k;
+}
+__device__ __forceinline__ unsigned fmix32(unsigned h) {
+    h ^= h >> 16; h *= 0x85ebca6bu; h ^= h >> 13; h *= 0xc2b2ae35u; h ^= h >> 16;
+    return h;
+}
+template <typename K>
+__device__ __forceinline__ unsigned long long hash_key(K k) {
+    if constexpr (sizeof(K) == 4) return fmix32((unsigned)k);
+    else return fmix64((unsigned long long)k);
+}
+
+// key bits of element i of a vector already promoted to `typ`; false for NaN
+template <typename K>
+__device__ __forceinline__ bool key_at(const void* p, int typ, long long i, K* k) {
+    switch (typ) {
+    case H_J: *k = (K)(long long)((const int8_t*)p)[i]; return true;
+    case H_H: *k = (K)(long long)((const int16_t*)p)[i]; return true;
+    case H_I: *k = (K)(long long)((const int32_t*)p)[i]; return true;
+    case H_L: *k = (K)((const long long*)p)[i]; return true;
+    case H_F: { float f = ((const float*)p)[i]; if (f != f) return false; *k = (K)__float_as_uint(f); return true; }
+    case H_E: { double f = ((const double*)p)[i]; if (f != f) return false; *k = (K)__double_as_longlong(f); return true; }
+    default: *k = (K)((const bool*)p)[i]; return true;
+    }
+}
+
+template <typename K>
+struct Table {
+    K* keys;            // EMPTY = all ones
+    unsigned* row;      // minimum row per slot (0xffffffff = none)
+    unsigned* cnt;      // rows per slot (joins), may be null
+    unsigned* special;  // [0] = min row, [1] = count for the key equal to EMPTY
+    unsigned long long mask;
+};
+
+template <typename K>
+__device__ __forceinline__ void table_insert(Table<K> t, K k, unsigned r, unsigned* derr) {
+    const K EMPTY = (K)~(K)0;
+    if (k == EMPTY) {
+        atomicMin(&t.special[0], r);
+        atomicAdd(&t.special[1], 1u);
+        return;
+    }
+    unsigned long long h = hash_key<K>(k) & t.mask;
+    for (unsigned long long p = 0; p <= t.mask; p++) {
+        K cur = t.keys[h];
+        if (cur == EMPTY) {
+            K prev;
+            if constexpr (sizeof(K) == 4) prev = (K)atomicCAS((unsigned*)&t.keys[h], (unsigned)EMPTY, (unsigned)k);
+            else prev = (K)atomicCAS((unsigned long long*)&t.keys[h], (unsigned long long)EMPTY, (unsigned long long)k);
+            cur = (prev == EMPTY) ? k : prev;
+        }
+        if (cur == k) {
+            atomicMin(&t.row[h], r);
+            if (t.cnt) atomicAdd(&t.cnt[h], 1u);
+            return;
+        }
+        h = (h + 1) & t.mask;
+    }
+    flag_error(derr, DERR_CAPACITY);
+}
+
+// slot of k or -1; EMPTY keys map to slot -2 (the special slot) when present
+template <typename K>
+__device__ __forceinline__ long long table_find(const Table<K>& t, K k) {
+    const K EMPTY = (K)~(K)0;
+    if (k == EMPTY) return t.special[1] ? -2 : -1;
+    unsigned long long h = hash_key<K>(k) & t.mask;
+    for (unsigned long long p = 0; p <= t.mask; p++) {
+        K cur = t.keys[h];
+        if (cur == k) return (long long)h;
+        if (cur == EMPTY) return -1;
+        h = (h + 1) & t.mask;
+    }
+    return -1;
+}
+
+template <typename K>
+__global__ void k_build(Table<K> t, const void* __restrict__ x, int typ, long long n, unsigned* derr) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        K k;
+        if (key_at<K>(x, typ, i, &k)) table_insert<K>(t, k, (unsigned)i, derr);
+    }
+}
+
+template <typename K>
+static I table_create(Table<K>* t, long long n, bool with_count) {
+    unsigned long long cap = 16;
+    while ((double)cap * g_load_factor < (double)n) cap <<= 1;
+    t->mask = cap - 1;
+    t->keys = (K*)salloc(cap * sizeof(K));
+    t->row = (unsigned*)salloc(cap * 4);
+    t->cnt = with_count ? (unsigned*)salloc(cap * 4) : nullptr;
+    t->special = (unsigned*)salloc(16);
+    if (!t->keys || !t->row || (with_count && !t->cnt) || !t->special) return E_DEVICE_OOM;
+    HG_CU(cudaMemsetAsync(t->keys, 0xff, cap * sizeof(K), g_stream));
+    HG_CU(cudaMemsetAsync(t->row, 0xff, cap * 4, g_stream));
+    if (with_count) HG_CU(cudaMemsetAsync(t->cnt, 0, cap * 4, g_stream));
+    unsigned init[4] = {0xffffffffu, 0, 0, 0};
+    HG_CU(cudaMemcpyAsync(t->special, init, 16, cudaMemcpyHostToDevice, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));  // `init` is a host stack buffer
+    return 0;
+}
+
+template <typename K>
+static I table_build(Table<K>* t, const void* x, int typ, long long n, bool with_count) {
+    HG_CHECK(table_create<K>(t, n, with_count));
+    if (n > 0) {
+        unsigned grid = grid_for(n, 256);
+        if (grid > (unsigned)g_sms * 16) grid = g_sms * 16;
+        HG_LAUNCH("hash_build", grid, 256, 0, k_build<K>, *t, x, typ, n, g_derr);
+        HG_CHECK(last_launch_error());
+    }
+    return 0;
+}
+
+static bool key64(I typ) { return typ == H_L || typ == H_E; }
+
+// ------------------------------------------------------------------ index_of
+template <typename K>
+__global__ void k_index_of(Table<K> t, const void* __restrict__ y, int typ, long long n, long long lenX,
+                           long long* __restrict__ z) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        K k;
+        long long r = lenX;
+        if (key_at<K>(y, typ, i, &k)) {
+            long long s = table_find<K>(t, k);
+            if (s >= 0) r = t.row[s];
+            else if (s == -2) r = t.special[0];
+        }
+        z[i] = r;
+    }
+}
+
+// has_up / has_down over adjacent pairs (isOrdered, h_system.cc:678-698)
+template <typename T>
+__global__ void k_order_flags(const T* __restrict__ x, long long n, unsigned* flags) {
+    bool up = false, down = false;
+    for (long long i = 1 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        T a = x[i - 1], b = x[i];
+        up |= b > a;
+        down |= b < a;
+    }
+    if (__any_sync(0xffffffffu, up) && lane_id() == 0) atomicOr(flags, 1u);
+    if (__any_sync(0xffffffffu, down) && lane_id() == 0) atomicOr(flags, 2u);
+}
+
+// binarySearch_I/L (h_system.cc:715-729) and searchOrdered (:731-745)
+template <typename T>
+__global__ void k_search_ordered(const T* __restrict__ x, long long lenX, const void* __restrict__ y, int ytyp,
+                                 long long n, long long* __restrict__ z) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        long long v;
+        switch (ytyp) {
+        case H_B: v = ((const bool*)y)[i]; break;
+        case H_J: v = ((const int8_t*)y)[i]; break;
+        case H_H: v = ((const int16_t*)y)[i]; break;
+        case H_I: v = ((const int32_t*)y)[i]; break;
+        default: v = ((const long long*)y)[i]; break;
+        }
+        long long r = lenX;
+        if (lenX > 0) {
+            long long lo = 0, hi = lenX;
+            for (;;) {
+                long long mid = (lo + hi) >> 1;
+                long long xm = (long long)x[mid];
+                if (xm == v) { r = mid; break; }
+                if (lo == mid) break;
+                if (xm > v) hi = mid; else lo = mid;
+            }
+        }
+        z[i] = r;
+    }
+}
+
+__global__ void k_first_false(const bool* __restrict__ x, long long n, unsigned long long* first) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        if (!x[i]) atomicMin(first, (unsigned long long)i);
+}
+__global__ void k_index_of_bool(const bool* __restrict__ y, long long n, const unsigned long long* first,
+                                long long lenX, long long* __restrict__ z) {
+    long long f = (*first == ~0ull) ? lenX : (long long)*first;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        z[i] = y[i] ? 0 : f;
+}
+
+static unsigned grid_cap(long long n) {
+    unsigned g = grid_for(n, 256);
+    return g > (unsigned)g_sms * 16 ? (unsigned)g_sms * 16 : g;
+}
+
+// ------------------------------------------------------------------ member
+template <typename K>
+__global__ void k_member(Table<K> t, const void* __restrict__ y, int typ, long long n, bool* __restrict__ z) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        K k;
+        bool r = false;
+        if (key_at<K>(y, typ, i, &k)) r = table_find<K>(t, k) != -1;
+        z[i] = r;
+    }
+}
+
+// sets of one or two elements: direct == compares (lib_member_fast1/2, h_libs.cc:900-945)
+template <typename T>
+__global__ void k_member_small(const T* __restrict__ y, long long n, T a, T b, int m, bool* __restrict__ z) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        T v = y[i];
+        z[i] = (m >= 1 && v == a) || (m >= 2 && v == b);
+    }
+}
+__global__ void k_member_bool(const bool* __restrict__ x, long long nx, const bool* __restrict__ y, long long n,
+                              unsigned* seen, bool* __restrict__ z, int phase) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (phase ? n : nx); i += (long long)gridDim.x * blockDim.x) {
+        if (phase == 0) atomicOr(seen, x[i] ? 2u : 1u);
+        else z[i] = (*seen & (y[i] ? 2u : 1u)) != 0;
+    }
+}
+
+// ------------------------------------------------------------------ join
+constexpr int JT_THREADS = 256, JT_TILE = 4096;
+
+// mode 0: hash table with unique build keys; mode 1: linear scan of a build
+// side of < 10 rows keeping the first match (eq = op 4, neq = op 5)
+struct LinearBuild {
+    long long k[10];
+    int n;
+    int eq;
+};
+
+template <typename K>
+__global__ void __launch_bounds__(JT_THREADS) k_join_probe(Table<K> t, LinearBuild lin, int mode,
+                                                           const void* __restrict__ y, int ytyp, long long n,
+                                                           long long* __restrict__ zb, long long* __restrict__ zp,
+                                                           unsigned long long* status, unsigned* ticket,
+                                                           unsigned long long* total, unsigned* derr) {
+    __shared__ unsigned warp_tot[8];
+    __shared__ unsigned long long tile_off;
+    __shared__ long long tile_id;
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) tile_id = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const long long t0 = tile_id, base = t0 * JT_TILE + (long long)warp * 512;
+    long long hit[16];
+    unsigned cnt = 0;
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        long long i = base + k * 32 + lane;
+        long long r = -1;
+        K key;
+        if (i < n && key_at<K>(y, ytyp, i, &key)) {
+            if (mode == 0) {
+                long long s = table_find<K>(t, key);
+                if (s >= 0) r = t.row[s];
+                else if (s == -2) r = t.special[0];
+            } else {
+                for (int j = 0; j < lin.n; j++) {
+                    bool m = lin.eq ? ((K)lin.k[j] == key) : ((K)lin.k[j] != key);
+                    if (m) { r = j; break; }
+                }
+            }
+        }
+        hit[k] = r;
+        cnt += __popc(__ballot_sync(0xffffffffu, r >= 0));
+    }
+    if (lane == 0) warp_tot[warp] = cnt;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned v = lane < 8 ? warp_tot[lane] : 0;
+        unsigned agg = warp_sum(v);
+        unsigned long long excl = lookback_exclusive(status, t0, agg, derr);
+        if (lane == 0) {
+            tile_off = excl;
+            if ((t0 + 1) * JT_TILE >= n) *total = excl + agg;
+        }
+    }
+    __syncthreads();
+    unsigned long long off = tile_off;
+    for (unsigned w = 0; w < warp; w++) off += warp_tot[w];
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        bool sel = hit[k] >= 0;
+        unsigned bal = __ballot_sync(0xffffffffu, sel);
+        if (sel) {
+            long long o = (long long)off + __popc(bal & lanemask_lt());
+            zb[o] = hit[k];
+            zp[o] = base + k * 32 + lane;
+        }
+        off += __popc(bal);
+    }
+}
+
+// duplicate build keys: CSR of build rows per slot, filled then sorted per slot
+template <typename K>
+__global__ void k_csr_fill(Table<K> t, const void* __restrict__ x, int typ, long long n,
+                           const unsigned long long* __restrict__ start, unsigned* fillc, unsigned* rows) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        K k;
+        if (!key_at<K>(x, typ, i, &k)) continue;
+        long long s = table_find<K>(t, k);
+        long long slot = s >= 0 ? s : (long long)(t.mask + 1);  // special slot stored last
+        unsigned p = atomicAdd(&fillc[slot], 1u);
+        rows[start[slot] + p] = (unsigned)i;
+    }
+}
+__global__ void k_csr_sort(const unsigned long long* __restrict__ start, const unsigned* __restrict__ cnt,
+                           long long nslots, unsigned* rows) {
+    for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < nslots; s += (long long)gridDim.x * blockDim.x) {
+        unsigned c = cnt[s];
+        if (c < 2) continue;
+        unsigned* r = rows + start[s];
+        for (unsigned a = 1; a < c; a++) {  // insertion sort: per-slot lists are short
+            unsigned v = r[a];
+            long long b = (long long)a - 1;
+            while (b >= 0 && r[b] > v) { r[b + 1] = r[b]; b--; }
+            r[b + 1] = v;
+        }
+    }
+}
+template <typename K>
+__global__ void k_join_count(Table<K> t, const void* __restrict__ y, int ytyp, long long n,
+                             unsigned* __restrict__ c, unsigned* __restrict__ slot) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        K k;
+        unsigned cc = 0, ss = 0;
+        if (key_at<K>(y, ytyp, i, &k)) {
+            long long s = table_find<K>(t, k);
+            if (s >= 0) { cc = t.cnt[s]; ss = (unsigned)s; }
+            else if (s == -2) { cc = t.special[1]; ss = (unsigned)(t.mask + 1); }
+        }
+        c[i] = cc;
+        slot[i] = ss;
+    }
+}
+__global__ void k_join_write(const unsigned* __restrict__ c, const unsigned* __restrict__ slot,
+                             const unsigned long long* __restrict__ off, long long n,
+                             const unsigned long long* __restrict__ start, const unsigned* __restrict__ rows,
+                             long long* __restrict__ zb, long long* __restrict__ zp) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        unsigned cc = c[i];
+        unsigned long long o = off[i], s0 = start[slot[i]];
+        for (unsigned q = 0; q < cc; q++) { zb[o + q] = rows[s0 + q]; zp[o + q] = i; }
+    }
+}
+__global__ void k_max_u32(const unsigned* __restrict__ a, long long n, unsigned* out) {
+    unsigned m = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        m = max(m, a[i]);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane_id() == 0) atomicMax(out, m);
+}
+
+// Writes the two i64 index vectors of a join into z (a 2-element list).
+static I join_outputs(V z, long long m, long long** zb, long long** zp) {
+    HG_CHECK(init_list(z, H_G, 2));
+    V0* e = host_nodes(z);
+    void *b, *p;
+    HG_CHECK(alloc_out(&e[0], H_L, m, &b));
+    HG_CHECK(alloc_out(&e[1], H_L, m, &p));
+    *zb = (long long*)b;
+    *zp = (long long*)p;
+    return 0;
+}
+
+// Probe in one pass with compaction; build rows and probe rows land in
+// scratch, then move into exact-size outputs.
+template <typename K>
+static I join_probe_unique(V z, const Table<K>& t, const LinearBuild& lin, int mode, const void* py, I ytyp,
+                           long long ny) {
+    long long ntiles = (ny + JT_TILE - 1) / JT_TILE;
+    long long* sb = (long long*)salloc((size_t)(ny > 0 ? ny : 1) * 8);
+    long long* sp = (long long*)salloc((size_t)(ny > 0 ? ny : 1) * 8);
+    char* s = (char*)salloc(ntiles * 8 + 64);
+    if (!sb || !sp || !s) return E_DEVICE_OOM;
+    unsigned long long m = 0;
+    if (ntiles > 0) {
+        HG_CU(cudaMemsetAsync(s, 0, ntiles * 8 + 64, g_stream));
+        unsigned long long* total = (unsigned long long*)(s + ntiles * 8 + 8);
+        HG_LAUNCH("join_probe", (unsigned)ntiles, JT_THREADS, 0, k_join_probe<K>, t, lin, mode, py, (int)ytyp, ny,
+                  sb, sp, (unsigned long long*)s, (unsigned*)(s + ntiles * 8), total, g_derr);
+        HG_CHECK(last_launch_error());
+        HG_CU(cudaMemcpyAsync(&m, total, 8, cudaMemcpyDeviceToHost, g_stream));
+        HG_CHECK(check_device_errors());
+    }
+    long long *zb, *zp;
+    HG_CHECK(join_outputs(z, (long long)m, &zb, &zp));
+    V0* e = host_nodes(z);
+    if (m > 0) {
+        HG_CU(cudaMemcpyAsync(zb, sb, m * 8, cudaMemcpyDeviceToDevice, g_stream));
+        HG_CU(cudaMemcpyAsync(zp, sp, m * 8, cudaMemcpyDeviceToDevice, g_stream));
+    }
+    HG_CHECK(finish_out(&e[0], zb));
+    HG_CHECK(finish_out(&e[1], zp));
+    return 0;
+}
+
+template <typename K>
+static I join_hash(V z, const void* px, I typ, long long nx, const void* py, long long ny) {
+    Table<K> t;
+    HG_CHECK(table_build<K>(&t, px, typ, nx, true));
+    unsigned long long nslots = t.mask + 2;  // + the special slot
+    unsigned* maxc = (unsigned*)salloc(16);
+    if (!maxc) return E_DEVICE_OOM;
+    HG_CU(cudaMemsetAsync(maxc, 0, 16, g_stream));
+    HG_LAUNCH("max_u32", grid_cap(t.mask + 1), 256, 0, k_max_u32, t.cnt, (long long)(t.mask + 1), maxc);
+    HG_LAUNCH("max_u32", 1, 32, 0, k_max_u32, t.special + 1, 1LL, maxc);
+    unsigned mx = 0;
+    HG_CU(cudaMemcpyAsync(&mx, maxc, 4, cudaMemcpyDeviceToHost, g_stream));
+    HG_CHECK(check_device_errors());
+    if (mx <= 1) {
+        LinearBuild lin{};
+        return join_probe_unique<K>(z, t, lin, 0, py, typ, ny);
+    }
+    // duplicate build keys: CSR of build rows per slot (special slot last)
+    unsigned* cnt_all = (unsigned*)salloc(nslots * 4);
+    unsigned long long* start = (unsigned long long*)salloc(nslots * 8);
+    unsigned* fillc = (unsigned*)salloc(nslots * 4);
+    unsigned* rows = (unsigned*)salloc((size_t)(nx > 0 ? nx : 1) * 4);
+    if (!cnt_all || !start || !fillc || !rows) return E_DEVICE_OOM;
+    HG_CU(cudaMemcpyAsync(cnt_all, t.cnt, (t.mask + 1) * 4, cudaMemcpyDeviceToDevice, g_stream));
+    HG_CU(cudaMemcpyAsync(cnt_all + t.mask + 1, t.special + 1, 4, cudaMemcpyDeviceToDevice, g_stream));
+    HG_CU(cudaMemsetAsync(fillc, 0, nslots * 4, g_stream));
+    unsigned long long tot = 0;
+    HG_CHECK(scan_exclusive(cnt_all, (long long)nslots, start, &tot));
+    HG_LAUNCH("csr_fill", grid_cap(nx), 256, 0, k_csr_fill<K>, t, px, (int)typ, nx, start, fillc, rows);
+    HG_LAUNCH("csr_sort", grid_cap((long long)nslots), 256, 0, k_csr_sort, start, cnt_all, (long long)nslots, rows);
+    unsigned* c = (unsigned*)salloc((size_t)(ny > 0 ? ny : 1) * 4);
+    unsigned* slot = (unsigned*)salloc((size_t)(ny > 0 ? ny : 1) * 4);
+    unsigned long long* off = (unsigned long long*)salloc((size_t)(ny > 0 ? ny : 1) * 8);
+    if (!c || !slot || !off) return E_DEVICE_OOM;
+    HG_LAUNCH("join_count", grid_cap(ny), 256, 0, k_join_count<K>, t, py, (int)typ, ny, c, slot);
+    unsigned long long m = 0;
+    HG_CHECK(scan_exclusive(c, ny, off, &m));
+    long long *zb, *zp;
+    HG_CHECK(join_outputs(z, (long long)m, &zb, &zp));
+    V0* e = host_nodes(z);
+    long long *wb = zb, *wp = zp;
+    if (m <= 1) {  // one-element outputs are inline: write to scratch first
+        wb = (long long*)salloc(16);
+        wp = (long long*)salloc(16);
+    }
+    if (m > 0) HG_LAUNCH("join_write", grid_cap(ny), 256, 0, k_join_write, c, slot, off, ny, start, rows, wb, wp);
+    HG_CHECK(last_launch_error());
+    HG_CHECK(finish_out(&e[0], wb));
+    HG_CHECK(finish_out(&e[1], wp));
+    return check_device_errors();
+}
+
+static void swap2(V z) {
+    V0* e = host_nodes(z);
+    V0 a = e[0], b = e[1];
+    e[0] = b;
+    e[1] = a;
+    if (is_inline(&a)) e[1].g = (G)&e[1].b;
+    if (is_inline(&b)) e[0].g = (G)&e[0].b;
+}
+
+// pfnJoinIndexSingle (h_primitive.cc:1944-2040) for eq/neq over real types
+static I join_single(V z, V x, V y, V f) {
+    const char* name = getSymbolStr(f->q);
+    int op = !strcmp(name, "lt") ? 0 : !strcmp(name, "leq") ? 1 : !strcmp(name, "gt") ? 2 : !strcmp(name, "geq") ? 3
+           : !strcmp(name, "eq") ? 4 : !strcmp(name, "neq") ? 5 : -1;
+    if (op < 0) return E_DOMAIN;
+    if (!(is_real(x->typ) && is_real(y->typ)))
+        return x->typ == y->typ ? set_error(E_NOT_IMPL, "join on this type is outside the path") : E_TYPE;
+    if (op != 4 && op != 5) return set_error(E_NOT_IMPL, "non-equi single-column join is outside the path");
+    I typ = x->typ > y->typ ? x->typ : y->typ;
+    if (typ != H_H && typ != H_I && typ != H_L && typ != H_F && typ != H_E) return E_NOT_IMPL;
+    const void *px, *py;
+    long long nx = x->len, ny = y->len;
+    if (nx >= 10) {  // NUM_JOIN_LINEAR (common.h:152)
+        if (op != 4) return set_error(E_NOT_IMPL, "hash join supports @eq only (as the reference)");
+        if (typ != H_I && typ != H_L) return set_error(E_NOT_IMPL, "hash join keys must be i32 or i64");
+        HG_CHECK(promote_to(x, typ, &px));
+        HG_CHECK(promote_to(y, typ, &py));
+        if (typ == H_I) return join_hash<unsigned>(z, px, typ, nx, py, ny);
+        return join_hash<unsigned long long>(z, px, typ, nx, py, ny);
+    }
+    if (typ != H_I && typ != H_L && typ != H_E) return set_error(E_NOT_IMPL, "linear join supports i32/i64/f64 keys");
+    HG_CHECK(promote_to(y, typ, &py));
+    // build side (< 10 rows) read on the host and passed by value
+    LinearBuild lin{};
+    lin.n = (int)nx;
+    lin.eq = op == 4;
+    if (nx > 0) {
+        const void* pxd;
+        HG_CHECK(promote_to(x, typ, &pxd));
+        HG_CU(cudaMemcpyAsync(lin.k, pxd, nx * 8 / (typ == H_I ? 2 : 1), cudaMemcpyDefault, g_stream));
+        HG_CU(cudaStreamSynchronize(g_stream));
+        if (typ == H_I) {
+            int tmp[10];
+            memcpy(tmp, lin.k, nx * 4);
+            for (int i = 0; i < nx; i++) lin.k[i] = tmp[i];
+        }
+    }
+    Table<unsigned long long> none{};
+    if (typ == H_I) {
+        Table<unsigned> n32{};
+        for (int i = 0; i < lin.n; i++) lin.k[i] = (long long)(unsigned)(int)lin.k[i];
+        return join_probe_unique<unsigned>(z, n32, lin, 1, py, typ, ny);
+    }
+    return join_probe_unique<unsigned long long>(z, none, lin, 1, py, typ, ny);
+}
+
+}  // namespace hg
+
+using namespace hg;
+
+extern "C" {
+
+I pfnIndexOf(V z, V x, V y) {
+    HG_CHECK(ensure_init());
+    ScratchScope ss;
+    if (!(is_real(x->typ) && is_real(y->typ)))
+        return x->typ == y->typ ? set_error(E_NOT_IMPL, "index_of on this type is outside the path") : E_TYPE;
+    long long lenX = x->len, n = y->len;
+    void* dz;
+    if ((x->typ == H_I || x->typ == H_L)) {
+        const void* px;
+        HG_CHECK(in_ptr(x, &px));
+        unsigned* flags = (unsigned*)salloc(16);
+        if (!flags) return E_DEVICE_OOM;
+        HG_CU(cudaMemsetAsync(flags, 0, 4, g_stream));
+        if (lenX > 1) {
+            if (x->typ == H_I) HG_LAUNCH("order_flags", grid_cap(lenX), 256, 0, k_order_flags<int32_t>, (const int32_t*)px, lenX, flags);
+            else HG_LAUNCH("order_flags", grid_cap(lenX), 256, 0, k_order_flags<long long>, (const long long*)px, lenX, flags);
+        }
+        unsigned fl = 0;
+        HG_CU(cudaMemcpyAsync(&fl, flags, 4, cudaMemcpyDeviceToHost, g_stream));
+        HG_CU(cudaStreamSynchronize(g_stream));
+        if (fl != 3) {  // monotone or constant: searchOrdered
+            const void* py;
+            HG_CHECK(in_ptr(y, &py));
+            HG_CHECK(alloc_out(z, H_L, n, &dz));
+            if (n > 0) {
+                if (x->typ == H_I) HG_LAUNCH("search_ordered", grid_cap(n), 256, 0, k_search_ordered<int32_t>, (const int32_t*)px, lenX, py, (int)y->typ, n, (long long*)dz);
+                else HG_LAUNCH("search_ordered", grid_cap(n), 256, 0, k_search_ordered<long long>, (const long long*)px, lenX, py, (int)y->typ, n, (long long*)dz);
+            }
+            HG_CHECK(last_launch_error());
+            return finish_out(z, dz);
+        }
+    }
+    I typ = x->typ > y->typ ? x->typ : y->typ;
+    const void *px, *py;
+    HG_CHECK(promote_to(x, typ, &px));
+    HG_CHECK(promote_to(y, typ, &py));
+    HG_CHECK(alloc_out(z, H_L, n, &dz));
+    if (typ == H_B) {
+        unsigned long long* first = (unsigned long long*)salloc(16);
+        if (!first) return E_DEVICE_OOM;
+        HG_CU(cudaMemsetAsync(first, 0xff, 8, g_stream));
+        if (lenX > 0) HG_LAUNCH("first_false", grid_cap(lenX), 256, 0, k_first_false, (const bool*)px, lenX, first);
+        if (n > 0) HG_LAUNCH("index_of_bool", grid_cap(n), 256, 0, k_index_of_bool, (const bool*)py, n, first, lenX, (long long*)dz);
+        HG_CHECK(last_launch_error());
+        return finish_out(z, dz);
+    }
+    if (key64(typ)) {
+        Table<unsigned long long> t;
+        HG_CHECK(table_build<unsigned long long>(&t, px, typ, lenX, false));
+        if (n > 0) HG_LAUNCH("index_of", grid_cap(n), 256, 0, k_index_of<unsigned long long>, t, py, (int)typ, n, lenX, (long long*)dz);
+    } else {
+        Table<unsigned> t;
+        HG_CHECK(table_build<unsigned>(&t, px, typ, lenX, false));
+        if (n > 0) HG_LAUNCH("index_of", grid_cap(n), 256, 0, k_index_of<unsigned>, t, py, (int)typ, n, lenX, (long long*)dz);
+    }
+    HG_CHECK(last_launch_error());
+    HG_CHECK(check_device_errors());
+    return finish_out(z, dz);
+}
+
+I pfnMember(V z, V y, V x) {
+    HG_CHECK(ensure_init());
+    ScratchScope ss;
+    long long n = y->len, nx = x->len;
+    void* dz;
+    if (is_real(x->typ) && is_real(y->typ)) {
+        I typ = x->typ > y->typ ? x->typ : y->typ;
+        if (typ == H_J) return set_error(E_NOT_IMPL, "member on i8 (the reference has no i8 case)");
+        const void *px, *py;
+        HG_CHECK(promote_to(x, typ, &px));
+        HG_CHECK(promote_to(y, typ, &py));
+        HG_CHECK(alloc_out(z, H_B, n, &dz));
+        if (typ == H_B) {
+            unsigned* seen = (unsigned*)salloc(16);
+            if (!seen) return E_DEVICE_OOM;
+            HG_CU(cudaMemsetAsync(seen, 0, 4, g_stream));
+            if (nx > 0) HG_LAUNCH("member_bool", grid_cap(nx), 256, 0, k_member_bool, (const bool*)px, nx, (const bool*)py, n, seen, (bool*)dz, 0);
+            if (n > 0) HG_LAUNCH("member_bool", grid_cap(n), 256, 0, k_member_bool, (const bool*)px, nx, (const bool*)py, n, seen, (bool*)dz, 1);
+        } else if (nx <= 2) {
+            uint64_t a = 0, b = 0;
+            if (nx >= 1) HG_CU(cudaMemcpyAsync(&a, px, esize(typ), cudaMemcpyDefault, g_stream));
+            if (nx >= 2) HG_CU(cudaMemcpyAsync(&b, (const char*)px + esize(typ), esize(typ), cudaMemcpyDefault, g_stream));
+            HG_CU(cudaStreamSynchronize(g_stream));
+            int m = (int)nx;
+            if (n > 0) switch (typ) {
+            case H_H: HG_LAUNCH("member_small", grid_cap(n), 256, 0, k_member_small<int16_t>, (const int16_t*)py, n, *(int16_t*)&a, *(int16_t*)&b, m, (bool*)dz); break;
+            case H_I: HG_LAUNCH("member_small", grid_cap(n), 256, 0, k_member_small<int32_t>, (const int32_t*)py, n, *(int32_t*)&a, *(int32_t*)&b, m, (bool*)dz); break;
+            case H_L: HG_LAUNCH("member_small", grid_cap(n), 256, 0, k_member_small<long long>, (const long long*)py, n, *(long long*)&a, *(long long*)&b, m, (bool*)dz); break;
+            case H_F: HG_LAUNCH("member_small", grid_cap(n), 256, 0, k_member_small<float>, (const float*)py, n, *(float*)&a, *(float*)&b, m, (bool*)dz); break;
+            default: HG_LAUNCH("member_small", grid_cap(n), 256, 0, k_member_small<double>, (const double*)py, n, *(double*)&a, *(double*)&b, m, (bool*)dz); break;
+            }
+        } else if (key64(typ)) {
+            Table<unsigned long long> t;
+            HG_CHECK(table_build<unsigned long long>(&t, px, typ, nx, false));
+            if (n > 0) HG_LAUNCH("member", grid_cap(n), 256, 0, k_member<unsigned long long>, t, py, (int)typ, n, (bool*)dz);
+        } else {
+            Table<unsigned> t;
+            HG_CHECK(table_build<unsigned>(&t, px, typ, nx, false));
+            if (n > 0) HG_LAUNCH("member", grid_cap(n), 256, 0, k_member<unsigned>, t, py, (int)typ, n, (bool*)dz);
+        }
+        HG_CHECK(last_launch_error());
+        HG_CHECK(check_device_errors());
+        return finish_out(z, dz);
+    }
+    if (x->typ == y->typ && x->typ == H_C) {  // lib_member_C (h_libs.cc:989-995): bytes as a 256-entry set
+        const void *px, *py;
+        HG_CHECK(in_ptr(x, &px));
+        HG_CHECK(in_ptr(y, &py));
+        HG_CHECK(alloc_out(z, H_B, n, &dz));
+        Table<unsigned> t;
+        HG_CHECK(table_build<unsigned>(&t, px, H_J, nx, false));
+        if (n > 0) HG_LAUNCH("member", grid_cap(n), 256, 0, k_member<unsigned>, t, py, (int)H_J, n, (bool*)dz);
+        HG_CHECK(last_launch_error());
+        HG_CHECK(check_device_errors());
+        return finish_out(z, dz);
+    }
+    if (x->typ == y->typ) return set_error(E_NOT_IMPL, "member on this type is outside the path");
+    return E_DOMAIN;
+}
+
+I pfnJoinIndex(V z, V x, V y, V f) {
+    HG_CHECK(ensure_init());
+    ScratchScope ss;
+    if (f->len == 1) {
+        if (x->len > y->len) {
+            HG_CHECK(join_single(z, y, x, f));
+            swap2(z);
+            return 0;
+        }
+        return join_single(z, x, y, f);
+    }
+    if (f->len > 1) return set_error(E_NOT_IMPL, "multi-column join is outside the current path");
+    return E_DOMAIN;
+}
+
+}  // extern "C"

@@ -1,0 +1,544 @@
+// Segmented aggregation: the interpreter chain
+//     raze(each(@sum|@avg|@min|@max|@len, each_right(@index, x, groups)))
+// (h_primitive.cc:1818-1904 each/each_right, :935-955 raze, per-group
+// pfnIndex :43-94 and pfnSum/pfnAvg/pfnReduce/pfnLen :656-847) and its fused
+// form, the peephole functions of the pattern pass (optimizer/pattern.cc:
+// 63-105 FP1/2/5/6/7, emitter :180-219), exported as hgpuGroupSum & co.
+//
+// Per-group semantics follow the interpreter (ints sum in i64, avg in f64,
+// min/max keep the type, empty groups give the pfnReduce sentinels).  Every
+// group is reduced with the fixed-order tile tree of dev_common.cuh, so the
+// chain and the fused entry points are bit-identical to each other and to a
+// plain @sum of the gathered vector.
+//
+// GB300 layout: the rows of all groups are one device array with group
+// starts (the @group output), so a group is a contiguous segment.  Groups of
+// up to 4096 rows are reduced by one warp each; longer groups are split into
+// 4096-row chunks reduced by one CTA each, and their chunk partials are
+// reduced again the same way.
+#include <limits>
+#include <vector>
+
+#include "dev_common.cuh"
+
+namespace hg {
+
+I scan_exclusive(const unsigned* in, long long n, unsigned long long* out, unsigned long long* total_h);
+I compact_rows(const uint8_t* mask, long long n, long long* out, long long* count);
+
+enum { AG_SUM = 0, AG_AVG = 1, AG_MIN = 2, AG_MAX = 3, AG_LEN = 4 };
+enum { OP_SUM = 0, OP_MIN = 1, OP_MAX = 2 };
+
+template <typename A, int OP>
+__device__ __forceinline__ A sop(A a, A b) {
+    if constexpr (OP == OP_SUM) {
+        if constexpr (std::is_same<A, double>::value) return __dadd_rn(a, b);
+        else if constexpr (std::is_same<A, float>::value) return __fadd_rn(a, b);
+        else return (A)((unsigned long long)a + (unsigned long long)b);
+    } else if constexpr (OP == OP_MIN) return (a < b) ? a : b;
+    else return (a > b) ? a : b;
+}
+template <typename A, int OP>
+__device__ __forceinline__ A swarp(A v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = sop<A, OP>(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// element j of segment [s, e): x[rows[s+j]] (gather) or vals[s+j]
+template <typename T, bool GATHER>
+__device__ __forceinline__ T seg_elem(const T* __restrict__ src, const long long* __restrict__ rows, long long nx,
+                                      long long k, bool& bad) {
+    if constexpr (GATHER) {
+        long long r = rows[k];
+        if (r < 0 || r >= nx) { bad = true; return T(0); }
+        return src[r];
+    } else {
+        return src[k];
+    }
+}
+
+// one warp per segment of at most 4096 elements (longer segments are skipped)
+template <typename T, typename A, int OP, bool GATHER>
+__global__ void k_seg_small(const T* __restrict__ src, const long long* __restrict__ rows, long long nx,
+                            const long long* __restrict__ starts, long long ng, long long total, A ident,
+                            A* __restrict__ out, unsigned* derr) {
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    bool bad = false;
+    for (long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ng; g += warps) {
+        const long long s = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total, m = e - s;
+        if (m > TILE_SUM) continue;
+        const unsigned lane = lane_id();
+        A ws[8];
+#pragma unroll
+        for (int v = 0; v < 8; v++) ws[v] = ident;
+        for (int v = 0; v < 8 && v * 32 < m; v++) {  // virtual warp v of the 256-lane tile
+            A acc = ident;
+            for (int k = 0; k < 16; k++) {
+                long long j = (long long)k * 256 + v * 32 + lane;
+                if (j >= m) break;
+                acc = sop<A, OP>(acc, (A)seg_elem<T, GATHER>(src, rows, nx, s + j, bad));
+            }
+            ws[v] = swarp<A, OP>(acc);
+        }
+        if (lane == 0) {
+            A w01 = sop<A, OP>(ws[0], ws[1]), w23 = sop<A, OP>(ws[2], ws[3]);
+            A w45 = sop<A, OP>(ws[4], ws[5]), w67 = sop<A, OP>(ws[6], ws[7]);
+            out[g] = sop<A, OP>(sop<A, OP>(w01, w23), sop<A, OP>(w45, w67));
+        }
+    }
+    if (bad) flag_error(derr, DERR_INDEX);
+}
+
+// one CTA per 4096-element chunk of the long segments
+template <typename T, typename A, int OP, bool GATHER>
+__global__ void __launch_bounds__(256) k_seg_chunk(const T* __restrict__ src, const long long* __restrict__ rows,
+                                                   long long nx, const long long* __restrict__ starts, long long ng,
+                                                   long long total, const long long* __restrict__ big,
+                                                   const unsigned long long* __restrict__ chunk0, long long nbig,
+                                                   A ident, A* __restrict__ part, unsigned* derr) {
+    __shared__ A ws[8];
+    const long long c = blockIdx.x;
+    long long lo = 0, hi = nbig - 1;  // the long segment owning chunk c
+    while (lo < hi) {
+        long long mid = (lo + hi + 1) >> 1;
+        if ((long long)chunk0[mid] <= c) lo = mid; else hi = mid - 1;
+    }
+    const long long g = big[lo];
+    const long long s = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total;
+    const long long base = s + (c - (long long)chunk0[lo]) * TILE_SUM;
+    bool bad = false;
+    A acc = ident;
+#pragma unroll 4
+    for (int k = 0; k < 16; k++) {
+        long long j = base + k * 256 + threadIdx.x;
+        if (j < e) acc = sop<A, OP>(acc, (A)seg_elem<T, GATHER>(src, rows, nx, j, bad));
+    }
+    acc = swarp<A, OP>(acc);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        A w01 = sop<A, OP>(ws[0], ws[1]), w23 = sop<A, OP>(ws[2], ws[3]);
+        A w45 = sop<A, OP>(ws[4], ws[5]), w67 = sop<A, OP>(ws[6], ws[7]);
+        part[c] = sop<A, OP>(sop<A, OP>(w01, w23), sop<A, OP>(w45, w67));
+    }
+    if (bad) flag_error(derr, DERR_INDEX);
+}
+
+__global__ void k_big_flags(const long long* __restrict__ starts, long long ng, long long total, uint8_t* __restrict__ f,
+                            unsigned* __restrict__ nch) {
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x) {
+        long long m = ((g + 1 < ng) ? starts[g + 1] : total) - starts[g];
+        f[g] = m > TILE_SUM;
+        if (nch) nch[g] = 0;
+    }
+}
+__global__ void k_big_chunks(const long long* __restrict__ starts, long long ng, long long total,
+                             const long long* __restrict__ big, long long nbig, unsigned* __restrict__ nch) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nbig; k += (long long)gridDim.x * blockDim.x) {
+        long long g = big[k];
+        long long m = ((g + 1 < ng) ? starts[g + 1] : total) - starts[g];
+        nch[k] = (unsigned)((m + TILE_SUM - 1) / TILE_SUM);
+    }
+}
+template <typename A>
+__global__ void k_scatter_big(const A* __restrict__ r, const long long* __restrict__ big, long long nbig, A* __restrict__ out) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nbig; k += (long long)gridDim.x * blockDim.x)
+        out[big[k]] = r[k];
+}
+__global__ void k_u64_to_i64(const unsigned long long* __restrict__ a, long long n, long long* __restrict__ b) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = (long long)a[i];
+}
+
+static unsigned gcap(long long n, int per = 256) {
+    unsigned g = grid_for(n, per);
+    return g > (unsigned)g_sms * 32 ? (unsigned)g_sms * 32 : g;
+}
+
+// Reduces every segment of (src via rows | src) into out[ng] (device).
+template <typename T, typename A, int OP, bool GATHER>
+static I seg_reduce(const T* src, const long long* rows, long long nx, const long long* starts, long long ng,
+                    long long total, A ident, A* out) {
+    if (ng == 0) return 0;
+    HG_LAUNCH("seg_small", gcap(ng * 32), 256, 0, (k_seg_small<T, A, OP, GATHER>), src, rows, nx, starts, ng, total,
+              ident, out, g_derr);
+    // long segments
+    uint8_t* f = (uint8_t*)salloc((size_t)ng);
+    long long* big = (long long*)salloc((size_t)ng * 8);
+    if (!f || !big) return E_DEVICE_OOM;
+    HG_LAUNCH("seg_flags", gcap(ng), 256, 0, k_big_flags, starts, ng, total, f, (unsigned*)nullptr);
+    long long nbig = 0;
+    HG_CHECK(compact_rows(f, ng, big, &nbig));
+    if (nbig == 0) return last_launch_error();
+    unsigned* nch = (unsigned*)salloc((size_t)nbig * 4);
+    unsigned long long* c0 = (unsigned long long*)salloc((size_t)nbig * 8);
+    if (!nch || !c0) return E_DEVICE_OOM;
+    HG_LAUNCH("seg_chunks", gcap(nbig), 256, 0, k_big_chunks, starts, ng, total, big, nbig, nch);
+    unsigned long long nchunks = 0;
+    HG_CHECK(scan_exclusive(nch, nbig, c0, &nchunks));
+    A* part = (A*)salloc((size_t)nchunks * sizeof(A));
+    A* res = (A*)salloc((size_t)nbig * sizeof(A));
+    long long* pstarts = (long long*)salloc((size_t)nbig * 8);
+    if (!part || !res || !pstarts) return E_DEVICE_OOM;
+    HG_LAUNCH("seg_chunk", (unsigned)nchunks, 256, 0, (k_seg_chunk<T, A, OP, GATHER>), src, rows, nx, starts, ng,
+              total, big, c0, nbig, ident, part, g_derr);
+    HG_LAUNCH("u64_to_i64", gcap(nbig), 256, 0, k_u64_to_i64, c0, nbig, pstarts);
+    // partials of each long segment are reduced by the same procedure
+    HG_CHECK((seg_reduce<A, A, OP, false>(part, nullptr, 0, pstarts, nbig, (long long)nchunks, ident, res)));
+    HG_LAUNCH("scatter_big", gcap(nbig), 256, 0, k_scatter_big<A>, res, big, nbig, out);
+    return last_launch_error();
+}
+
+// ---------------------------------------------------------- finishing steps
+template <typename A>
+__global__ void k_avg_seg(const A* __restrict__ s, const long long* __restrict__ starts, long long ng, long long total,
+                          void* __restrict__ out) {
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x) {
+        long long m = ((g + 1 < ng) ? starts[g + 1] : total) - starts[g];
+        if constexpr (std::is_same<A, long long>::value) ((double*)out)[g] = __ddiv_rn((double)s[g] * 1.0, (double)m);
+        else if constexpr (std::is_same<A, float>::value) ((float*)out)[g] = __fdiv_rn(s[g], (float)m);
+        else ((double*)out)[g] = __ddiv_rn(s[g], (double)m);
+    }
+}
+__global__ void k_len_seg(const long long* __restrict__ starts, long long ng, long long total, long long* __restrict__ out) {
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x)
+        out[g] = ((g + 1 < ng) ? starts[g + 1] : total) - starts[g];
+}
+// empty groups in min/max: the pfnReduce sentinel (ints become i64)
+template <typename T>
+__global__ void k_minmax_fix(const T* __restrict__ r, const long long* __restrict__ starts, long long ng, long long total,
+                             int op, int to_long, void* __restrict__ out) {
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x) {
+        long long m = ((g + 1 < ng) ? starts[g + 1] : total) - starts[g];
+        if (to_long) ((long long*)out)[g] = m ? (long long)r[g] : (op == AG_MIN ? LLONG_MAX : LLONG_MIN);
+        else if constexpr (std::is_same<T, float>::value) ((float*)out)[g] = m ? r[g] : (op == AG_MIN ? 3.402823466e+38f : 1.175494351e-38f);
+        else if constexpr (std::is_same<T, double>::value) ((double*)out)[g] = m ? r[g] : (op == AG_MIN ? 1.7976931348623157e308 : 2.2250738585072014e-308);
+        else ((T*)out)[g] = r[g];
+    }
+}
+__global__ void k_any_empty(const long long* __restrict__ starts, long long ng, long long total, unsigned* flag) {
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x)
+        if (((g + 1 < ng) ? starts[g + 1] : total) == starts[g]) atomicOr(flag, 1u);
+}
+
+// Aggregates segments of x: result vector (device) of ng values, type in *typ.
+template <typename T, bool GATHER>
+static I agg_typed(int ag, I xt, const T* src, const long long* rows, long long nx, const long long* starts, long long ng,
+                   long long total, void** out, I* typ) {
+    constexpr bool isF = std::is_same<T, float>::value, isE = std::is_same<T, double>::value;
+    using SA = typename std::conditional<isF, float, typename std::conditional<isE, double, long long>::type>::type;
+    if (ag == AG_LEN) {
+        *typ = H_L;
+        *out = salloc((size_t)(ng > 0 ? ng : 1) * 8);
+        if (!*out) return E_DEVICE_OOM;
+        if (ng > 0) HG_LAUNCH("len_seg", gcap(ng), 256, 0, k_len_seg, starts, ng, total, (long long*)*out);
+        return last_launch_error();
+    }
+    if (ag == AG_SUM || ag == AG_AVG) {
+        SA* s = (SA*)salloc((size_t)(ng > 0 ? ng : 1) * sizeof(SA));
+        if (!s) return E_DEVICE_OOM;
+        HG_CHECK((seg_reduce<T, SA, OP_SUM, GATHER>(src, rows, nx, starts, ng, total, (SA)0, s)));
+        if (ag == AG_SUM) {
+            *typ = isF ? H_F : (isE ? H_E : H_L);
+            *out = s;
+            return 0;
+        }
+        *typ = isF ? H_F : H_E;
+        *out = salloc((size_t)(ng > 0 ? ng : 1) * 8);
+        if (!*out) return E_DEVICE_OOM;
+        if (ng > 0) HG_LAUNCH("avg_seg", gcap(ng), 256, 0, k_avg_seg<SA>, s, starts, ng, total, *out);
+        return last_launch_error();
+    }
+    // min / max
+    T* r = (T*)salloc((size_t)(ng > 0 ? ng : 1) * sizeof(T));
+    if (!r) return E_DEVICE_OOM;
+    T identity;
+    if (ag == AG_MIN) identity = std::numeric_limits<T>::has_infinity ? std::numeric_limits<T>::infinity() : std::numeric_limits<T>::max();
+    else identity = std::numeric_limits<T>::has_infinity ? -std::numeric_limits<T>::infinity() : std::numeric_limits<T>::lowest();
+    if (ag == AG_MIN) HG_CHECK((seg_reduce<T, T, OP_MIN, GATHER>(src, rows, nx, starts, ng, total, identity, r)));
+    else HG_CHECK((seg_reduce<T, T, OP_MAX, GATHER>(src, rows, nx, starts, ng, total, identity, r)));
+    unsigned* fl = (unsigned*)salloc(16);
+    if (!fl) return E_DEVICE_OOM;
+    HG_CU(cudaMemsetAsync(fl, 0, 4, g_stream));
+    if (ng > 0) HG_LAUNCH("any_empty", gcap(ng), 256, 0, k_any_empty, starts, ng, total, fl);
+    unsigned h = 0;
+    HG_CU(cudaMemcpyAsync(&h, fl, 4, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));
+    bool to_long = h && is_int(xt);
+    *typ = to_long ? H_L : xt;
+    *out = salloc((size_t)(ng > 0 ? ng : 1) * (to_long ? 8 : sizeof(T)));
+    if (!*out) return E_DEVICE_OOM;
+    if (ng > 0) HG_LAUNCH("minmax_fix", gcap(ng), 256, 0, k_minmax_fix<T>, r, starts, ng, total, ag, to_long ? 1 : 0, *out);
+    return last_launch_error();
+}
+
+template <bool GATHER>
+static I agg_dispatch(int ag, I xt, const void* src, const long long* rows, long long nx, const long long* starts,
+                      long long ng, long long total, void** out, I* typ) {
+    switch (xt) {
+    case H_B: return agg_typed<bool, GATHER>(ag, xt, (const bool*)src, rows, nx, starts, ng, total, out, typ);
+    case H_J: return agg_typed<int8_t, GATHER>(ag, xt, (const int8_t*)src, rows, nx, starts, ng, total, out, typ);
+    case H_H: return agg_typed<int16_t, GATHER>(ag, xt, (const int16_t*)src, rows, nx, starts, ng, total, out, typ);
+    case H_I: return agg_typed<int32_t, GATHER>(ag, xt, (const int32_t*)src, rows, nx, starts, ng, total, out, typ);
+    case H_L: return agg_typed<long long, GATHER>(ag, xt, (const long long*)src, rows, nx, starts, ng, total, out, typ);
+    case H_F: return agg_typed<float, GATHER>(ag, xt, (const float*)src, rows, nx, starts, ng, total, out, typ);
+    case H_E: return agg_typed<double, GATHER>(ag, xt, (const double*)src, rows, nx, starts, ng, total, out, typ);
+    default: return E_DOMAIN;
+    }
+}
+
+// ------------------------------------------------ lists -> contiguous segments
+__global__ void k_node_lens(const V0* __restrict__ nodes, long long ng, unsigned* __restrict__ lens) {
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x)
+        lens[g] = (unsigned)nodes[g].len;
+}
+// copies each element's payload (es bytes per item) to data + off[g]; an
+// inline element's payload sits in the node itself
+__global__ void k_node_copy(const V0* __restrict__ nodes, long long ng, const unsigned long long* __restrict__ off,
+                            int es, char* __restrict__ data) {
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ng; g += warps) {
+        const V0& v = nodes[g];
+        const char* src = (v.len <= 1) ? (const char*)&v.b : (const char*)v.g;
+        long long nb = v.len * es;
+        for (long long b = lane_id(); b < nb; b += 32) data[off[g] * es + b] = src[b];
+    }
+}
+__global__ void k_offsets_i64(const unsigned long long* __restrict__ a, long long n, long long* __restrict__ b) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = (long long)a[i];
+}
+
+// Segments of a list whose elements all have type `typ`.  Lists built by this
+// library are found in the registry; any other list is read through its
+// nodes (copied to pinned memory first when the caller's node array is
+// pageable).  Payloads must be device-readable.
+static I list_segments(V y, I typ, const long long** starts, long long* total, const void** data) {
+    long long ng = y->len;
+    const ListInfo* li = find_list(host_nodes(y), ng);
+    if (li && li->kind == LIST_SEGMENTS && li->typ == typ) {
+        *starts = li->starts;
+        *total = li->total;
+        *data = li->data;
+        return 0;
+    }
+    const V0* nodes = host_nodes(y);
+    int es = esize(typ);
+    for (long long g = 0; g < ng; g++) {
+        if (nodes[g].typ != typ) return set_error(E_TYPE, "list element %lld has type %d, expected %d", g, nodes[g].typ, typ);
+        if (nodes[g].len > 1 && !is_device_ptr(nodes[g].g))
+            return set_error(E_NOT_IMPL, "list element %lld lives in pageable host memory; stage it with hgpuToDevice", g);
+    }
+    if (!is_device_ptr(nodes)) {
+        V0* pin = (V0*)halloc((size_t)(ng > 0 ? ng : 1) * sizeof(V0));
+        if (!pin) return E_DEVICE_OOM;
+        memcpy(pin, nodes, (size_t)ng * sizeof(V0));
+        nodes = pin;
+    }
+    unsigned* lens = (unsigned*)salloc((size_t)(ng > 0 ? ng : 1) * 4);
+    unsigned long long* off = (unsigned long long*)salloc((size_t)(ng > 0 ? ng : 1) * 8);
+    long long* st = (long long*)salloc((size_t)(ng > 0 ? ng : 1) * 8);
+    if (!lens || !off || !st) return E_DEVICE_OOM;
+    unsigned long long tot = 0;
+    if (ng > 0) {
+        HG_LAUNCH("node_lens", gcap(ng), 256, 0, k_node_lens, nodes, ng, lens);
+        HG_CHECK(scan_exclusive(lens, ng, off, &tot));
+    }
+    char* d = (char*)salloc((size_t)(tot > 0 ? tot : 1) * es);
+    if (!d) return E_DEVICE_OOM;
+    if (ng > 0) {
+        HG_LAUNCH("node_copy", gcap(ng * 32), 256, 0, k_node_copy, nodes, ng, off, es, d);
+        HG_LAUNCH("offsets", gcap(ng), 256, 0, k_offsets_i64, off, ng, st);
+    }
+    *starts = st;
+    *total = (long long)tot;
+    *data = d;
+    return last_launch_error();
+}
+
+// writes ng one-element nodes holding vals[g] (es bytes) into a pinned node array
+__global__ void k_scalar_nodes(const char* __restrict__ vals, long long ng, int es, I typ, V0* __restrict__ nodes) {
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x) {
+        V0 v;
+        v.len = 1;
+        v.typ = typ;
+        v.i64 = 0;
+        for (int b = 0; b < es; b++) ((char*)&v.b)[b] = vals[g * es + b];
+        v.g = (G)&nodes[g].b;
+        nodes[g] = v;
+    }
+}
+// segment nodes over a contiguous payload (inline when one element)
+__global__ void k_segment_nodes(const char* __restrict__ data, const long long* __restrict__ starts, long long ng,
+                                long long total, int es, I typ, V0* __restrict__ nodes) {
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x) {
+        long long s = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total;
+        V0 v;
+        v.len = e - s;
+        v.typ = typ;
+        v.i64 = 0;
+        if (e - s == 1) {
+            for (int b = 0; b < es; b++) ((char*)&v.b)[b] = data[s * es + b];
+            v.g = (G)&nodes[g].b;
+        } else {
+            v.g = (G)(data + s * es);
+        }
+        nodes[g] = v;
+    }
+}
+
+static I group_agg(V z, V x, V y, int ag) {
+    HG_CHECK(ensure_init());
+    ScratchScope ss;
+    if (y->typ != H_G) return E_DOMAIN;
+    if (!is_real(x->typ)) return E_DOMAIN;
+    const long long* starts;
+    long long total;
+    const void* rows;
+    HG_CHECK(list_segments(y, H_L, &starts, &total, &rows));
+    const void* px;
+    HG_CHECK(in_ptr(x, &px));
+    void* res;
+    I typ;
+    HG_CHECK(agg_dispatch<true>(ag, x->typ, px, (const long long*)rows, x->len, starts, y->len, total, &res, &typ));
+    HG_CHECK(check_device_errors());
+    void* dz;
+    HG_CHECK(alloc_out(z, typ, y->len, &dz));
+    if (y->len > 0) HG_CU(cudaMemcpyAsync(dz, res, (size_t)y->len * esize(typ), cudaMemcpyDeviceToDevice, g_stream));
+    return finish_out(z, dz);
+}
+
+}  // namespace hg
+
+using namespace hg;
+
+extern "C" {
+
+I hgpuGroupSum(V z, V x, V y) { return group_agg(z, x, y, AG_SUM); }
+I hgpuGroupAvg(V z, V x, V y) { return group_agg(z, x, y, AG_AVG); }
+I hgpuGroupMin(V z, V x, V y) { return group_agg(z, x, y, AG_MIN); }
+I hgpuGroupMax(V z, V x, V y) { return group_agg(z, x, y, AG_MAX); }
+I hgpuGroupLen(V z, V x, V y) { return group_agg(z, x, y, AG_LEN); }
+
+// pfnEachRight: h_primitive.cc:1882-1904.  With @index over a list of i64 row
+// vectors all groups are gathered in one kernel into one contiguous payload.
+I pfnEachRight(V z, V x, V y, I (*foo)(V, V, V)) {
+    HG_CHECK(ensure_init());
+    if (y->typ != H_G) return foo(z, x, y);
+    long long ng = y->len;
+    if (foo == pfnIndex && is_basic(x->typ) && ng > 0) {
+        bool all_long = true;
+        const V0* nodes = host_nodes(y);
+        const ListInfo* li = find_list(nodes, ng);
+        if (!li) for (long long g = 0; g < ng && all_long; g++) all_long = nodes[g].typ == H_L;
+        if (all_long) {
+            ScratchScope ss;
+            const long long* starts;
+            long long total;
+            const void* rows;
+            HG_CHECK(list_segments(y, H_L, &starts, &total, &rows));
+            const void* px;
+            HG_CHECK(in_ptr(x, &px));
+            int es = esize(x->typ);
+            char* data = (char*)dalloc((size_t)(total > 0 ? total : 1) * es);
+            long long* keep = (long long*)dalloc((size_t)ng * 8);
+            if (!data || !keep) return E_DEVICE_OOM;
+            HG_CHECK(gather_into(px, x->len, es, rows, H_L, data, total));
+            HG_CHECK(check_device_errors());
+            HG_CU(cudaMemcpyAsync(keep, starts, (size_t)ng * 8, cudaMemcpyDeviceToDevice, g_stream));
+            HG_CHECK(init_list(z, H_G, ng));
+            HG_LAUNCH("segment_nodes", gcap(ng), 256, 0, k_segment_nodes, data, keep, ng, total, es, x->typ, host_nodes(z));
+            HG_CHECK(last_launch_error());
+            HG_CHECK(sync());
+            register_list({host_nodes(z), ng, LIST_SEGMENTS, x->typ, keep, total, data});
+            return apply_residency(z);
+        }
+    }
+    HG_CHECK(init_list(z, H_G, ng));
+    for (long long i = 0; i < ng; i++) HG_CHECK(foo(host_nodes(z) + i, x, host_nodes(y) + i));
+    return 0;
+}
+
+// pfnEach: h_primitive.cc:1818-1832.  @sum/@avg/@min/@max/@len over a list of
+// vectors run as one segmented reduction; other functions are applied per element.
+I pfnEach(V z, V x, I (*foo)(V, V)) {
+    HG_CHECK(ensure_init());
+    if (x->typ != H_G) return E_DOMAIN;
+    long long ng = x->len;
+    int ag = foo == pfnSum ? AG_SUM : foo == pfnAvg ? AG_AVG : foo == pfnMin ? AG_MIN : foo == pfnMax ? AG_MAX
+           : foo == pfnLen ? AG_LEN : -1;
+    if (ag >= 0 && ng > 0) {
+        const V0* nodes = host_nodes(x);
+        I t = nodes[0].typ;
+        bool same = is_real(t);
+        const ListInfo* li = find_list(nodes, ng);
+        if (!li) for (long long g = 1; g < ng && same; g++) same = nodes[g].typ == t;
+        else same = same && li->typ == t && li->kind == LIST_SEGMENTS;
+        if (same) {
+            ScratchScope ss;
+            const long long* starts;
+            long long total;
+            const void* vals;
+            HG_CHECK(list_segments(x, t, &starts, &total, &vals));
+            void* res;
+            I typ;
+            HG_CHECK(agg_dispatch<false>(ag, t, vals, nullptr, 0, starts, ng, total, &res, &typ));
+            int es = esize(typ);
+            char* keep = (char*)dalloc((size_t)ng * es);
+            if (!keep) return E_DEVICE_OOM;
+            HG_CU(cudaMemcpyAsync(keep, res, (size_t)ng * es, cudaMemcpyDeviceToDevice, g_stream));
+            HG_CHECK(init_list(z, H_G, ng));
+            HG_LAUNCH("scalar_nodes", gcap(ng), 256, 0, k_scalar_nodes, keep, ng, es, typ, host_nodes(z));
+            HG_CHECK(last_launch_error());
+            HG_CHECK(sync());
+            register_list({host_nodes(z), ng, LIST_SCALARS, typ, nullptr, ng, keep});
+            return apply_residency(z);
+        }
+    }
+    HG_CHECK(init_list(z, H_G, ng));
+    for (long long i = 0; i < ng; i++) HG_CHECK(foo(host_nodes(z) + i, host_nodes(x) + i));
+    return 0;
+}
+
+// pfnRaze: h_primitive.cc:935-955 — the elements' common type, concatenated.
+I pfnRaze(V z, V x) {
+    HG_CHECK(ensure_init());
+    ScratchScope ss;
+    if (x->typ != H_G) {
+        if (is_basic(x->typ)) { *z = *x; if (is_inline(x)) z->g = (G)&z->b; return 0; }
+        return E_DOMAIN;
+    }
+    long long ng = x->len;
+    if (ng == 0) return set_error(E_RAZE_LIST, "an empty list cannot be razed");
+    const V0* nodes = host_nodes(x);
+    const ListInfo* li = find_list(nodes, ng);
+    if (li && li->kind == LIST_SCALARS) {  // one value per element, already contiguous on the device
+        void* dz;
+        HG_CHECK(alloc_out(z, li->typ, ng, &dz));
+        HG_CU(cudaMemcpyAsync(dz, li->data, (size_t)ng * esize(li->typ), cudaMemcpyDeviceToDevice, g_stream));
+        return finish_out(z, dz);
+    }
+    I typ = -1;
+    for (long long g = 0; g < ng; g++) {
+        I t = nodes[g].typ;
+        if (!is_basic(t)) return set_error(E_NOT_IMPL, "raze of nested lists");
+        if (typ == -1) typ = t;
+        else if (typ != t) {
+            if (is_real(typ) && is_real(t)) typ = t > typ ? t : typ;
+            else return E_RAZE_LIST;
+        }
+    }
+    for (long long g = 0; g < ng; g++)
+        if (nodes[g].typ != typ) return set_error(E_NOT_IMPL, "raze with type promotion across elements");
+    const long long* starts;
+    long long total;
+    const void* data;
+    HG_CHECK(list_segments(x, typ, &starts, &total, &data));
+    void* dz;
+    HG_CHECK(alloc_out(z, typ, total, &dz));
+    if (total > 0) HG_CU(cudaMemcpyAsync(dz, data, (size_t)total * esize(typ), cudaMemcpyDeviceToDevice, g_stream));
+    return finish_out(z, dz);
+}
+
+}  // extern "C"

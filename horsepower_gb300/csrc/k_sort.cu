@@ -1,0 +1,891 @@
+// Stable LSD radix sort, @group and @order.
+//
+// Reference orderings reproduced (src/horseir/v3/backend/h_libs.cc):
+//   lib_radixsort_core_int  :1184-1207  4 stable passes over the unsigned
+//                           bytes of the 32-bit pattern (negatives after positives)
+//   lib_radixsort_core_long :1243-1274  32 bits unless some key has
+//                           (key >> 32) > 0, then 64
+//   lib_radixsort_int/long  :1215-1293  descending = ascending reversed
+//   checkOrderCase1         :1912-1940  two i32 columns, one direction: pack
+//                           ((i64)x0 << 32) | (i64)x1 (x1 sign-extended)
+//   lib_quicksort_list      :637-697    lists of i32/i64 columns: stable merge
+//                           sort per column, recursing on runs of equal values
+//                           = stable lexicographic order
+//   lib_group_by_normal_*   :1295-1403  groups = runs of equal adjacent values
+//                           in radix order; key = first row of the run
+//   pfnGroupTrie            h_primitive.cc:2656-2681  counting on (c0<<8)+c1
+//
+// Any stable sort by the same key yields the same permutation, so the GPU
+// sorts only the key bits that vary (found with one OR/AND reduction) and
+// packs multi-column integer keys into one u64 after range compression.
+//
+// Radix kernel: onesweep-style LSD (Adinets & Merrill 2022).  One histogram
+// pass gives every digit's global bucket base for all passes; each pass
+// then ranks a 4096-key tile with warp-level __match_any_sync (warps own
+// contiguous sub-ranges, so ranks are stable), resolves per-digit tile
+// offsets with a decoupled look-back (one thread per digit, bounded spin),
+// and scatters keys and row ids.
+#include <cstring>
+#include <vector>
+
+#include "dev_common.cuh"
+
+namespace hg {
+
+I compact_rows(const uint8_t* mask, long long n, long long* out, long long* count);
+I scan_exclusive(const unsigned* in, long long n, unsigned long long* out, unsigned long long* total_h);
+
+constexpr int RS_THREADS = 256, RS_ITEMS = 16, RS_TILE = RS_THREADS * RS_ITEMS;
+static int g_digit_bits = 8;  // autotuned 4..8
+void set_radix_digit_bits(int b) { g_digit_bits = b < 4 ? 4 : (b > 8 ? 8 : b); }
+
+template <typename K>
+__global__ void k_key_bits(const K* __restrict__ k, long long n, unsigned long long* orv, unsigned long long* andv) {
+    unsigned long long o = 0, a = ~0ull;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        o |= (unsigned long long)k[i];
+        a &= (unsigned long long)k[i];
+    }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+        o |= __shfl_xor_sync(0xffffffffu, o, s);
+        a &= __shfl_xor_sync(0xffffffffu, a, s);
+    }
+    if (lane_id() == 0) { atomicOr(orv, o); atomicAnd(andv, a); }
+}
+
+template <typename K>
+__global__ void k_radix_hist(const K* __restrict__ k, long long n, int lo, int bits, int npass,
+                             unsigned long long* __restrict__ hist) {
+    __shared__ unsigned sh[8][256];
+    for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) (&sh[0][0])[i] = 0;
+    __syncthreads();
+    const unsigned dmask = (1u << bits) - 1;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        unsigned long long v = (unsigned long long)k[i];
+        for (int p = 0; p < npass; p++) atomicAdd(&sh[p][(unsigned)(v >> (lo + p * bits)) & dmask], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < npass * 256; i += blockDim.x)
+        if ((&sh[0][0])[i]) atomicAdd(&hist[i], (unsigned long long)(&sh[0][0])[i]);
+}
+
+// exclusive scan of each pass's 256 bins (one block per pass)
+__global__ void k_bucket_base(const unsigned long long* __restrict__ hist, unsigned long long* __restrict__ base) {
+    __shared__ unsigned long long s[256];
+    const int p = blockIdx.x, d = threadIdx.x;
+    s[d] = hist[p * 256 + d];
+    __syncthreads();
+    if (d == 0) {
+        unsigned long long acc = 0;
+        for (int i = 0; i < 256; i++) { unsigned long long v = s[i]; s[i] = acc; acc += v; }
+    }
+    __syncthreads();
+    base[p * 256 + d] = s[d];
+}
+
+template <typename K, bool FIRST>
+__global__ void __launch_bounds__(RS_THREADS) k_onesweep(const K* __restrict__ kin, const unsigned* __restrict__ vin,
+                                                         K* __restrict__ kout, unsigned* __restrict__ vout, long long n,
+                                                         int shift, int bits, const unsigned long long* __restrict__ bucket,
+                                                         unsigned long long* status, unsigned* ticket, unsigned* derr) {
+    __shared__ unsigned whist[8][256];
+    __shared__ unsigned long long dbase[256];
+    __shared__ long long tile_id;
+    for (int i = threadIdx.x; i < 8 * 256; i += RS_THREADS) (&whist[0][0])[i] = 0;
+    if (threadIdx.x == 0) tile_id = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const long long t = tile_id;
+    const unsigned lane = lane_id(), w = threadIdx.x >> 5;
+    const long long wbase = t * RS_TILE + (long long)w * (32 * RS_ITEMS);
+    const unsigned dmask = (1u << bits) - 1;
+    K key[RS_ITEMS];
+    unsigned val[RS_ITEMS], dig[RS_ITEMS], rank[RS_ITEMS];
+#pragma unroll
+    for (int k = 0; k < RS_ITEMS; k++) {
+        long long i = wbase + k * 32 + lane;
+        bool valid = i < n;
+        key[k] = valid ? kin[i] : K(0);
+        val[k] = FIRST ? (unsigned)i : (valid ? vin[i] : 0u);
+        unsigned d = valid ? ((unsigned)((unsigned long long)key[k] >> shift) & dmask) : 0xffffffffu;
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        int leader = __ffs(peers) - 1;
+        unsigned pre = 0;
+        if ((int)lane == leader && valid) {
+            pre = whist[w][d];
+            whist[w][d] = pre + __popc(peers);
+        }
+        pre = __shfl_sync(0xffffffffu, pre, leader);
+        rank[k] = pre + __popc(peers & lanemask_lt());
+        dig[k] = d;
+        __syncwarp();
+    }
+    __syncthreads();
+    {
+        const int d = threadIdx.x;  // one thread per digit
+        unsigned c = 0;
+        for (int ww = 0; ww < 8; ww++) { unsigned h = whist[ww][d]; whist[ww][d] = c; c += h; }
+        unsigned long long* st = status + (size_t)t * 256 + d;
+        unsigned long long excl = 0;
+        if (d <= (int)dmask) {
+            if (t == 0) st_release(st, LB_INC | c);
+            else {
+                st_release(st, LB_AGG | c);
+                long long j = t - 1, spins = 0;
+                while (j >= 0) {
+                    unsigned long long s = ld_acquire(status + (size_t)j * 256 + d);
+                    unsigned long long f = s >> 62;
+                    if (f == 0) {
+                        if (++spins > SPIN_LIMIT) { flag_error(derr, DERR_TIMEOUT); break; }
+                        continue;
+                    }
+                    excl += s & LB_MASK;
+                    if (f == 2) break;
+                    j--;
+                }
+                st_release(st, LB_INC | (excl + c));
+            }
+        }
+        dbase[d] = bucket[d] + excl;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < RS_ITEMS; k++) {
+        long long i = wbase + k * 32 + lane;
+        if (i < n) {
+            unsigned d = dig[k];
+            unsigned long long pos = dbase[d] + whist[w][d] + rank[k];
+            kout[pos] = key[k];
+            vout[pos] = val[k];
+        }
+    }
+}
+
+__global__ void k_iota(unsigned* v, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        v[i] = (unsigned)i;
+}
+
+// Stable sort of keys[0..n) (row ids travel along).  On return *kres/*vres
+// point to the sorted keys and row ids (scratch).  When no key bit varies
+// the result is the identity permutation.
+template <typename K>
+I radix_sort(const K* keys, long long n, const K** kres, const unsigned** vres, const unsigned* init_vals = nullptr) {
+    unsigned long long* red = (unsigned long long*)salloc(16);
+    if (!red) return E_DEVICE_OOM;
+    unsigned long long init[2] = {0, ~0ull};
+    HG_CU(cudaMemcpyAsync(red, init, 16, cudaMemcpyHostToDevice, g_stream));
+    unsigned grid = grid_for(n, 256);
+    if (grid > (unsigned)g_sms * 8) grid = g_sms * 8;
+    HG_LAUNCH("key_bits", grid, 256, 0, k_key_bits<K>, keys, n, red, red + 1);
+    unsigned long long hb[2];
+    HG_CU(cudaMemcpyAsync(hb, red, 16, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));
+    unsigned long long vary = hb[0] ^ hb[1];
+    unsigned* vid = (unsigned*)salloc((size_t)(n > 0 ? n : 1) * 4);
+    if (!vid) return E_DEVICE_OOM;
+    if (vary == 0 || n <= 1) {
+        // all keys equal: identity order
+        K* kcopy = (K*)salloc((size_t)(n > 0 ? n : 1) * sizeof(K));
+        if (!kcopy) return E_DEVICE_OOM;
+        if (n > 0) HG_CU(cudaMemcpyAsync(kcopy, keys, n * sizeof(K), cudaMemcpyDeviceToDevice, g_stream));
+        if (n > 0) {
+            if (init_vals) HG_CU(cudaMemcpyAsync(vid, init_vals, n * 4, cudaMemcpyDeviceToDevice, g_stream));
+            else HG_LAUNCH("iota", grid, 256, 0, k_iota, vid, n);
+        }
+        *kres = kcopy;
+        *vres = vid;
+        return last_launch_error();
+    }
+    int lo = __builtin_ctzll(vary), hi = 64 - __builtin_clzll(vary);
+    int bits = g_digit_bits;
+    int npass = (hi - lo + bits - 1) / bits;
+    if (npass > 8) { bits = 8; npass = (hi - lo + 7) / 8; }
+    unsigned long long* hist = (unsigned long long*)salloc((size_t)npass * 256 * 8 * 2);
+    if (!hist) return E_DEVICE_OOM;
+    unsigned long long* bucket = hist + npass * 256;
+    HG_CU(cudaMemsetAsync(hist, 0, (size_t)npass * 256 * 8, g_stream));
+    HG_LAUNCH("radix_hist", grid, 256, 0, k_radix_hist<K>, keys, n, lo, bits, npass, hist);
+    HG_LAUNCH("bucket_base", npass, 256, 0, k_bucket_base, hist, bucket);
+    long long ntiles = (n + RS_TILE - 1) / RS_TILE;
+    K* kb[2] = {(K*)salloc(n * sizeof(K)), (K*)salloc(n * sizeof(K))};
+    unsigned* vb[2] = {vid, (unsigned*)salloc(n * 4)};
+    char* st = (char*)salloc((size_t)ntiles * 256 * 8 + 64);
+    if (!kb[0] || !kb[1] || !vb[1] || !st) return E_DEVICE_OOM;
+    const K* kin = keys;
+    const unsigned* vin = init_vals;
+    for (int p = 0; p < npass; p++) {
+        HG_CU(cudaMemsetAsync(st, 0, (size_t)ntiles * 256 * 8 + 64, g_stream));
+        K* ko = kb[p & 1];
+        unsigned* vo = vb[p & 1];
+        unsigned* ticket = (unsigned*)(st + (size_t)ntiles * 256 * 8);
+        if (p == 0 && !init_vals)
+            HG_LAUNCH("onesweep", (unsigned)ntiles, RS_THREADS, 0, (k_onesweep<K, true>), kin, vin, ko, vo, n,
+                      lo + p * bits, bits, bucket + p * 256, (unsigned long long*)st, ticket, g_derr);
+        else
+            HG_LAUNCH("onesweep", (unsigned)ntiles, RS_THREADS, 0, (k_onesweep<K, false>), kin, vin, ko, vo, n,
+                      lo + p * bits, bits, bucket + p * 256, (unsigned long long*)st, ticket, g_derr);
+        kin = ko;
+        vin = vo;
+    }
+    HG_CHECK(last_launch_error());
+    *kres = kin;
+    *vres = vin;
+    return 0;
+}
+
+
+// ---------------------------------------------------------------- sort keys
+enum KeyXf : int {
+    XF_RAW32 = 0,   // (u32)(i32)v: the reference's 32-bit pattern
+    XF_LOW32 = 1,   // low 32 bits of an i64
+    XF_RAW64 = 2,   // (u64)v
+    XF_UBYTE = 3,   // (u8)v
+    XF_RANGE = 4,   // (u64)(v - lo), or (u64)(hi - v) when descending
+    XF_FLOAT = 5,   // order-preserving float bits (-0.0 taken as +0.0), complemented when descending
+    XF_CASE1 = 6,   // ((i64)x0 << 32) | (i64)x1 over columns 0 and 1
+};
+constexpr int KMAXC = 4;
+struct KeySpec {
+    const void* col[KMAXC];
+    int typ[KMAXC];
+    int xf[KMAXC];
+    int shift[KMAXC];
+    long long lo[KMAXC], hi[KMAXC];
+    int desc[KMAXC];
+    int ncol;
+};
+
+__device__ __forceinline__ long long ival(const void* p, int typ, long long i) {
+    switch (typ) {
+    case H_B: return ((const bool*)p)[i];
+    case H_J: case H_C: return ((const int8_t*)p)[i];
+    case H_H: return ((const int16_t*)p)[i];
+    case H_I: case H_M: case H_D: case H_U: case H_W: case H_T: return ((const int32_t*)p)[i];
+    default: return ((const long long*)p)[i];
+    }
+}
+__device__ __forceinline__ double fval(const void* p, int typ, long long i) {
+    return typ == H_F ? (double)((const float*)p)[i] : ((const double*)p)[i];
+}
+
+template <typename K>
+__global__ void k_make_keys(KeySpec s, long long n, K* __restrict__ out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        unsigned long long key = 0;
+        for (int c = 0; c < s.ncol; c++) {
+            unsigned long long u;
+            switch (s.xf[c]) {
+            case XF_RAW32: u = (unsigned)(int)ival(s.col[c], s.typ[c], i); break;
+            case XF_LOW32: u = (unsigned)(unsigned long long)ival(s.col[c], s.typ[c], i); break;
+            case XF_RAW64: u = (unsigned long long)ival(s.col[c], s.typ[c], i); break;
+            case XF_UBYTE: u = (uint8_t)ival(s.col[c], s.typ[c], i); break;
+            case XF_RANGE: {
+                long long v = ival(s.col[c], s.typ[c], i);
+                u = s.desc[c] ? (unsigned long long)(s.hi[c] - v) : (unsigned long long)(v - s.lo[c]);
+            } break;
+            case XF_FLOAT: {
+                double f = fval(s.col[c], s.typ[c], i);
+                if (f == 0.0) f = 0.0;
+                unsigned long long b = (unsigned long long)__double_as_longlong(f);
+                b = (b >> 63) ? ~b : (b | (1ull << 63));
+                u = s.desc[c] ? ~b : b;
+            } break;
+            default: {  // XF_CASE1
+                long long a = ival(s.col[0], s.typ[0], i), b = ival(s.col[1], s.typ[1], i);
+                u = ((unsigned long long)a << 32) | (unsigned long long)b;
+                c = s.ncol;
+            } break;
+            }
+            key |= u << s.shift[c < KMAXC ? c : 0];
+        }
+        out[i] = (K)key;
+    }
+}
+
+__global__ void k_minmax_i64(const void* p, int typ, long long n, long long* mn, long long* mx) {
+    long long a = LLONG_MAX, b = LLONG_MIN;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        long long v = ival(p, typ, i);
+        a = v < a ? v : a;
+        b = v > b ? v : b;
+    }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+        long long o = __shfl_xor_sync(0xffffffffu, a, s); a = o < a ? o : a;
+        long long q = __shfl_xor_sync(0xffffffffu, b, s); b = q > b ? q : b;
+    }
+    if (lane_id() == 0) { atomicMin(mn, a); atomicMax(mx, b); }
+}
+__global__ void k_any_high(const long long* __restrict__ x, long long n, unsigned* flag) {
+    bool any = false;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        any |= (x[i] >> 32) > 0;
+    if (__any_sync(0xffffffffu, any) && lane_id() == 0) atomicOr(flag, 1u);
+}
+
+// ------------------------------------------------------------- permutations
+__global__ void k_widen(const unsigned* __restrict__ v, long long n, long long* __restrict__ out, int reverse) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = reverse ? (long long)v[n - 1 - i] : (long long)v[i];
+}
+
+// group boundary flags: row i starts a group when its key differs from row i-1
+template <typename K>
+__global__ void k_bound_keys(const K* __restrict__ k, long long n, uint8_t* __restrict__ f) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        f[i] = (i == 0) || (k[i] != k[i - 1]);
+}
+// ... or when any column value differs between the rows perm[i-1] and perm[i]
+// (equality as the reference's comparator: == on values)
+struct ColSet {
+    const void* col[KMAXC];
+    int typ[KMAXC];
+    int ncol;
+};
+__global__ void k_bound_cols(ColSet c, const unsigned* __restrict__ perm, long long n, uint8_t* __restrict__ f) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        bool b = i == 0;
+        if (!b) {
+            long long a = perm[i - 1], q = perm[i];
+            for (int j = 0; j < c.ncol && !b; j++) {
+                if (c.typ[j] == H_F || c.typ[j] == H_E) b = fval(c.col[j], c.typ[j], a) != fval(c.col[j], c.typ[j], q);
+                else b = ival(c.col[j], c.typ[j], a) != ival(c.col[j], c.typ[j], q);
+            }
+        }
+        f[i] = b;
+    }
+}
+
+// keys[g] = perm[start[g]]; node g = group g's rows (inline when one row)
+__global__ void k_group_nodes(const long long* __restrict__ starts, long long ng, long long n,
+                              const long long* __restrict__ perm, long long* __restrict__ keys, V0* __restrict__ nodes) {
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x) {
+        long long s = starts[g], e = (g + 1 < ng) ? starts[g + 1] : n;
+        long long first = perm[s];
+        if (keys) keys[g] = first;
+        V0 v;
+        v.len = e - s;
+        v.typ = H_L;
+        if (e - s == 1) {
+            v.i64 = first;
+            v.g = (G)&nodes[g].b;
+        } else {
+            v.i64 = 0;
+            v.g = (G)(perm + s);
+        }
+        nodes[g] = v;
+    }
+}
+
+// the reference's char sort of fewer than ten rows (h_libs.cc:388-390):
+// all-pairs exchange on a[rtn[i]] > a[rtn[j]], which leaves them descending
+__global__ void k_char_small(const int8_t* __restrict__ a, long long n, unsigned* __restrict__ perm) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    unsigned r[10];
+    for (long long i = 0; i < n; i++) r[i] = (unsigned)i;
+    for (long long i = 0; i < n; i++)
+        for (long long j = 0; j < n; j++)
+            if (a[r[i]] > a[r[j]]) { unsigned t = r[i]; r[i] = r[j]; r[j] = t; }
+    for (long long i = 0; i < n; i++) perm[i] = r[i];
+}
+
+static unsigned gcap(long long n) {
+    unsigned g = grid_for(n, 256);
+    return g > (unsigned)g_sms * 16 ? (unsigned)g_sms * 16 : g;
+}
+
+// ----------------------------------------------- descending list orders
+// lib_quicksort_list (h_libs.cc:637-697) first asks lib_order_by_sorted
+// (:604-617) whether the range is already in order; for a descending column
+// a range that is ascending (non-decreasing with one strict step) is
+// reversed instead of sorted, which reverses its ties.  Within every run the
+// rows are therefore in ascending or descending row order; one bit per row
+// (dirbit) tracks which, and the final order is the lexicographic key order
+// with fully tied rows in their run's row order.
+__global__ void k_updown(const void* __restrict__ col, int typ, const unsigned* __restrict__ perm,
+                         const unsigned* __restrict__ rid, long long n, unsigned* __restrict__ flags) {
+    for (long long i = 1 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        unsigned r0 = rid ? rid[i - 1] : 0, r1 = rid ? rid[i] : 0;
+        if (r0 != r1) continue;
+        long long a = ival(col, typ, perm ? perm[i - 1] : i - 1), b = ival(col, typ, perm ? perm[i] : i);
+        if (b > a) atomicOr(&flags[r1], 1u);
+        if (b < a) atomicOr(&flags[r1], 2u);
+    }
+}
+// a run whose values are non-decreasing (with a strict step) in its current
+// order is reversed: flip the direction bit of its rows
+__global__ void k_flip(const unsigned* __restrict__ perm, const unsigned* __restrict__ rid, long long n,
+                       const unsigned* __restrict__ flags, uint8_t* __restrict__ dirbit) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        unsigned r = perm ? perm[i] : (unsigned)i;
+        unsigned f = flags[rid ? rid[i] : 0];
+        bool up = f & 1u, down = f & 2u;
+        bool rev = dirbit[r] ? (!up && down) : (!down && up);
+        if (rev) dirbit[r] ^= 1;
+    }
+}
+__global__ void k_run_ids(const uint8_t* __restrict__ bflag, long long n, unsigned* __restrict__ one) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        one[i] = (i > 0 && bflag[i]) ? 1u : 0u;
+}
+__global__ void k_add_u32(unsigned* __restrict__ a, const unsigned* __restrict__ b, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        a[i] += b[i];
+}
+__global__ void k_u64_to_u32(const unsigned long long* __restrict__ a, long long n, unsigned* __restrict__ b) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = (unsigned)a[i];
+}
+__global__ void k_tiebreak(const uint8_t* __restrict__ dirbit, long long n, unsigned* __restrict__ tb, unsigned* any) {
+    bool f = false;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        tb[i] = dirbit[i] ? (unsigned)(n - 1 - i) : (unsigned)i;
+        f |= dirbit[i] != 0;
+    }
+    if (__any_sync(0xffffffffu, f) && lane_id() == 0) atomicOr(any, 1u);
+}
+template <typename K>
+__global__ void k_gather_keys(const K* __restrict__ k, const unsigned* __restrict__ perm, long long n, K* __restrict__ out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = k[perm[i]];
+}
+
+// ------------------------------------------------------------- sort drivers
+struct SortResult {
+    const unsigned* perm;   // row ids in sorted order (scratch)
+    const void* keys;       // sorted keys (scratch), null for the small-char path
+    int key64;
+    bool key_injective;     // equal keys <=> equal rows (boundary test on keys)
+};
+
+static I sort_by_spec(const KeySpec& s, long long n, int total_bits, SortResult* r) {
+    r->key64 = total_bits > 32;
+    if (r->key64) {
+        unsigned long long* k = (unsigned long long*)salloc((size_t)(n > 0 ? n : 1) * 8);
+        if (!k) return E_DEVICE_OOM;
+        if (n > 0) HG_LAUNCH("make_keys", gcap(n), 256, 0, k_make_keys<unsigned long long>, s, n, k);
+        const unsigned long long* ks;
+        HG_CHECK(radix_sort<unsigned long long>(k, n, &ks, &r->perm));
+        r->keys = ks;
+    } else {
+        unsigned* k = (unsigned*)salloc((size_t)(n > 0 ? n : 1) * 4);
+        if (!k) return E_DEVICE_OOM;
+        if (n > 0) HG_LAUNCH("make_keys", gcap(n), 256, 0, k_make_keys<unsigned>, s, n, k);
+        const unsigned* ks;
+        HG_CHECK(radix_sort<unsigned>(k, n, &ks, &r->perm));
+        r->keys = ks;
+    }
+    return last_launch_error();
+}
+
+static int bits_for(unsigned long long range) { return range == 0 ? 1 : 64 - __builtin_clzll(range); }
+
+static I col_minmax(const void* p, I typ, long long n, long long* mn, long long* mx) {
+    long long* d = (long long*)salloc(16);
+    if (!d) return E_DEVICE_OOM;
+    long long init[2] = {LLONG_MAX, LLONG_MIN};
+    HG_CU(cudaMemcpyAsync(d, init, 16, cudaMemcpyHostToDevice, g_stream));
+    if (n > 0) HG_LAUNCH("minmax", gcap(n), 256, 0, k_minmax_i64, p, (int)typ, n, d, d + 1);
+    long long h[2];
+    HG_CU(cudaMemcpyAsync(h, d, 16, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));
+    *mn = h[0];
+    *mx = h[1];
+    return 0;
+}
+
+// Single-column keys following the reference's radix rules (i32 / i64).
+static I sort_int_column(V x, const void* p, long long n, SortResult* r) {
+    KeySpec s{};
+    s.ncol = 1;
+    s.col[0] = p;
+    s.typ[0] = x->typ;
+    s.shift[0] = 0;
+    if (x->typ == H_I) {
+        s.xf[0] = XF_RAW32;
+        r->key_injective = true;
+        return sort_by_spec(s, n, 32, r);
+    }
+    unsigned* flag = (unsigned*)salloc(16);
+    if (!flag) return E_DEVICE_OOM;
+    HG_CU(cudaMemsetAsync(flag, 0, 4, g_stream));
+    if (n > 0) HG_LAUNCH("any_high", gcap(n), 256, 0, k_any_high, (const long long*)p, n, flag);
+    unsigned f = 0;
+    HG_CU(cudaMemcpyAsync(&f, flag, 4, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));
+    s.xf[0] = f ? XF_RAW64 : XF_LOW32;
+    r->key_injective = f != 0;
+    return sort_by_spec(s, n, f ? 64 : 32, r);
+}
+
+// Key spec for the stable lexicographic order of integer / float columns
+// (ascending unless desc[c]); integer columns are range-compressed and all
+// columns packed into one key of *bits bits.
+static I column_spec(int ncol, V* cols, const void** ptrs, const B* asc, long long n, KeySpec* s, int* bits) {
+    if (ncol > KMAXC) return set_error(E_NOT_IMPL, "ordering by more than %d columns", KMAXC);
+    memset(s, 0, sizeof *s);
+    s->ncol = ncol;
+    int shift = 0;
+    for (int c = ncol - 1; c >= 0; c--) {
+        int width;
+        s->col[c] = ptrs[c];
+        s->typ[c] = cols[c]->typ;
+        s->desc[c] = asc ? !asc[c] : 0;
+        if (cols[c]->typ == H_F || cols[c]->typ == H_E) {
+            s->xf[c] = XF_FLOAT;
+            width = 64;
+        } else {
+            long long mn, mx;
+            HG_CHECK(col_minmax(ptrs[c], cols[c]->typ, n, &mn, &mx));
+            s->xf[c] = XF_RANGE;
+            s->lo[c] = mn;
+            s->hi[c] = mx;
+            width = n > 0 ? bits_for((unsigned long long)mx - (unsigned long long)mn) : 1;
+        }
+        s->shift[c] = shift;
+        shift += width;
+    }
+    if (shift > 64) return set_error(E_NOT_IMPL, "packed order key wider than 64 bits");
+    *bits = shift;
+    return 0;
+}
+
+static I sort_columns(int ncol, V* cols, const void** ptrs, const B* asc, long long n, SortResult* r) {
+    KeySpec s;
+    int bits;
+    HG_CHECK(column_spec(ncol, cols, ptrs, asc, n, &s, &bits));
+    r->key_injective = true;
+    return sort_by_spec(s, n, bits, r);
+}
+
+// Multi-column @order with descending columns, as lib_quicksort_list does it
+// (see k_updown above).
+template <typename K>
+static I final_order(const KeySpec& s, long long n, const uint8_t* dirbit, SortResult* r) {
+    K* k = (K*)salloc((size_t)n * sizeof(K));
+    unsigned* tb = (unsigned*)salloc((size_t)n * 4);
+    unsigned* any = (unsigned*)salloc(16);
+    if (!k || !tb || !any) return E_DEVICE_OOM;
+    HG_LAUNCH("make_keys", gcap(n), 256, 0, k_make_keys<K>, s, n, k);
+    HG_CU(cudaMemsetAsync(any, 0, 4, g_stream));
+    HG_LAUNCH("tiebreak", gcap(n), 256, 0, k_tiebreak, dirbit, n, tb, any);
+    unsigned h = 0;
+    HG_CU(cudaMemcpyAsync(&h, any, 4, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));
+    const K* ks;
+    if (!h) {  // no range was reversed: ties stay in row order
+        HG_CHECK(radix_sort<K>(k, n, &ks, &r->perm));
+    } else {  // ties of reversed runs in descending row order: sort by tiebreak first
+        const unsigned* tk;
+        const unsigned* pt;
+        HG_CHECK(radix_sort<unsigned>(tb, n, &tk, &pt));
+        K* kg = (K*)salloc((size_t)n * sizeof(K));
+        if (!kg) return E_DEVICE_OOM;
+        HG_LAUNCH("gather_keys", gcap(n), 256, 0, k_gather_keys<K>, k, pt, n, kg);
+        HG_CHECK(radix_sort<K>(kg, n, &ks, &r->perm, pt));
+    }
+    r->keys = ks;
+    r->key64 = sizeof(K) == 8;
+    r->key_injective = true;
+    return last_launch_error();
+}
+
+static I order_columns_exact(int nc, V* cols, const void** ptrs, const B* asc, long long n, SortResult* r) {
+    uint8_t* dirbit = (uint8_t*)salloc((size_t)(n > 0 ? n : 1));
+    unsigned* flags = (unsigned*)salloc((size_t)(n > 0 ? n : 1) * 4 + 16);
+    if (!dirbit || !flags) return E_DEVICE_OOM;
+    HG_CU(cudaMemsetAsync(dirbit, 0, (size_t)(n > 0 ? n : 1), g_stream));
+    if (n > 1 && !asc[0]) {  // level 0: the whole range in row order
+        HG_CU(cudaMemsetAsync(flags, 0, 4, g_stream));
+        HG_LAUNCH("updown", gcap(n), 256, 0, k_updown, ptrs[0], (int)cols[0]->typ, (const unsigned*)nullptr,
+                  (const unsigned*)nullptr, n, flags);
+        HG_LAUNCH("flip", gcap(n), 256, 0, k_flip, (const unsigned*)nullptr, (const unsigned*)nullptr, n, flags, dirbit);
+    }
+    for (int c = 1; c < nc && n > 1; c++) {
+        if (asc[c]) continue;
+        // runs of equal columns 0..c-1, rows in ascending row order within each run
+        SortResult pr{};
+        HG_CHECK(sort_columns(c, cols, ptrs, nullptr, n, &pr));
+        uint8_t* bf = (uint8_t*)salloc((size_t)n);
+        unsigned* one = (unsigned*)salloc((size_t)n * 4);
+        unsigned long long* ex = (unsigned long long*)salloc((size_t)n * 8);
+        unsigned* rid = (unsigned*)salloc((size_t)n * 4);
+        if (!bf || !one || !ex || !rid) return E_DEVICE_OOM;
+        if (pr.key64) HG_LAUNCH("bound_keys", gcap(n), 256, 0, k_bound_keys<unsigned long long>, (const unsigned long long*)pr.keys, n, bf);
+        else HG_LAUNCH("bound_keys", gcap(n), 256, 0, k_bound_keys<unsigned>, (const unsigned*)pr.keys, n, bf);
+        HG_LAUNCH("run_ids", gcap(n), 256, 0, k_run_ids, bf, n, one);
+        unsigned long long nb = 0;
+        HG_CHECK(scan_exclusive(one, n, ex, &nb));
+        HG_LAUNCH("run_ids", gcap(n), 256, 0, k_u64_to_u32, ex, n, rid);
+        HG_LAUNCH("run_ids", gcap(n), 256, 0, k_add_u32, rid, one, n);
+        HG_CU(cudaMemsetAsync(flags, 0, (size_t)(nb + 1) * 4, g_stream));
+        HG_LAUNCH("updown", gcap(n), 256, 0, k_updown, ptrs[c], (int)cols[c]->typ, pr.perm, rid, n, flags);
+        HG_LAUNCH("flip", gcap(n), 256, 0, k_flip, pr.perm, rid, n, flags, dirbit);
+    }
+    KeySpec s;
+    int bits;
+    HG_CHECK(column_spec(nc, cols, ptrs, asc, n, &s, &bits));
+    if (n == 0) { r->perm = nullptr; r->keys = nullptr; return 0; }
+    if (bits > 32) return final_order<unsigned long long>(s, n, dirbit, r);
+    return final_order<unsigned>(s, n, dirbit, r);
+}
+
+// Builds the @group dict from a sorted permutation.
+static I group_dict(V z, const SortResult& r, long long n, const ColSet* cols) {
+    uint8_t* flags = (uint8_t*)salloc((size_t)(n > 0 ? n : 1));
+    long long* starts = (long long*)salloc((size_t)(n > 0 ? n : 1) * 8);
+    if (!flags || !starts) return E_DEVICE_OOM;
+    if (n > 0) {
+        if (cols) HG_LAUNCH("bound_cols", gcap(n), 256, 0, k_bound_cols, *cols, r.perm, n, flags);
+        else if (r.key64) HG_LAUNCH("bound_keys", gcap(n), 256, 0, k_bound_keys<unsigned long long>, (const unsigned long long*)r.keys, n, flags);
+        else HG_LAUNCH("bound_keys", gcap(n), 256, 0, k_bound_keys<unsigned>, (const unsigned*)r.keys, n, flags);
+    }
+    long long G = 0;
+    HG_CHECK(compact_rows(flags, n, starts, &G));
+    {  // group starts stay in the output arena: aggregations over this dict reuse them
+        long long* keep = (long long*)dalloc((size_t)(G > 0 ? G : 1) * 8);
+        if (!keep) return E_DEVICE_OOM;
+        if (G > 0) HG_CU(cudaMemcpyAsync(keep, starts, (size_t)G * 8, cudaMemcpyDeviceToDevice, g_stream));
+        starts = keep;
+    }
+    HG_CHECK(init_list(z, H_N, 2));
+    V0* kv = host_nodes(z);
+    // permutation as i64 (the rows of every group, concatenated)
+    long long* perm = nullptr;
+    if (n > 0) {
+        perm = (long long*)dalloc((size_t)n * 8);
+        if (!perm) return E_DEVICE_OOM;
+        HG_LAUNCH("widen", gcap(n), 256, 0, k_widen, r.perm, n, perm, 0);
+    }
+    void* dkeys;
+    HG_CHECK(alloc_out(&kv[0], H_L, G, &dkeys));
+    HG_CHECK(init_list(&kv[1], H_G, G));
+    if (G > 0)
+        HG_LAUNCH("group_nodes", gcap(G), 256, 0, k_group_nodes, starts, G, n, perm, (long long*)dkeys,
+                  host_nodes(&kv[1]));
+    HG_CHECK(last_launch_error());
+    HG_CHECK(finish_out(&kv[0], dkeys));
+    HG_CHECK(sync());  // the node array is written by the kernel
+    if (G > 0) register_list({host_nodes(&kv[1]), G, LIST_SEGMENTS, H_L, starts, n, perm});
+    return apply_residency(z);
+}
+
+static I order_output(V z, const SortResult& r, long long n, bool reverse) {
+    void* d;
+    HG_CHECK(alloc_out(z, H_L, n, &d));
+    if (n > 0) HG_LAUNCH("widen", gcap(n), 256, 0, k_widen, r.perm, n, (long long*)d, reverse ? 1 : 0);
+    HG_CHECK(last_launch_error());
+    return finish_out(z, d);
+}
+
+static bool list_of_basic(V x) {
+    if (x->typ != H_G) return false;
+    for (L i = 0; i < x->len; i++)
+        if (!is_basic(host_nodes(x)[i].typ)) return false;
+    return true;
+}
+
+// sort of one char column as lib_quicksort_char (h_libs.cc:386-407)
+static I sort_char(const void* p, long long n, SortResult* r) {
+    if (n < 10) {
+        unsigned* perm = (unsigned*)salloc(64);
+        if (!perm) return E_DEVICE_OOM;
+        if (n > 0) HG_LAUNCH("char_small", 1, 32, 0, k_char_small, (const int8_t*)p, n, perm);
+        r->perm = perm;
+        r->keys = nullptr;
+        r->key64 = 0;
+        r->key_injective = false;
+        return last_launch_error();
+    }
+    KeySpec s{};
+    s.ncol = 1; s.col[0] = p; s.typ[0] = H_C; s.xf[0] = XF_UBYTE;
+    r->key_injective = true;
+    return sort_by_spec(s, n, 8, r);
+}
+
+}  // namespace hg
+
+using namespace hg;
+
+extern "C" {
+
+I pfnGroupTrie(V z, V x) {
+    HG_CHECK(ensure_init());
+    ScratchScope ss;
+    V0* c = host_nodes(x);
+    long long n = c[0].len;
+    const void *p0, *p1;
+    HG_CHECK(in_ptr(&c[0], &p0));
+    HG_CHECK(in_ptr(&c[1], &p1));
+    KeySpec s{};
+    s.ncol = 2;
+    s.col[0] = p0; s.typ[0] = H_C; s.xf[0] = XF_UBYTE; s.shift[0] = 8;
+    s.col[1] = p1; s.typ[1] = H_C; s.xf[1] = XF_UBYTE; s.shift[1] = 0;
+    SortResult r{};
+    r.key_injective = true;
+    HG_CHECK(sort_by_spec(s, n, 16, &r));
+    return group_dict(z, r, n, nullptr);
+}
+
+I pfnGroupBasic(V z, V x) {
+    HG_CHECK(ensure_init());
+    ScratchScope ss;
+    SortResult r{};
+    if (x->typ == H_I || x->typ == H_L) {
+        const void* p;
+        HG_CHECK(in_ptr(x, &p));
+        HG_CHECK(sort_int_column(x, p, x->len, &r));
+        if (r.key_injective) return group_dict(z, r, x->len, nullptr);
+        ColSet cs{};
+        cs.ncol = 1; cs.col[0] = p; cs.typ[0] = x->typ;
+        return group_dict(z, r, x->len, &cs);
+    }
+    if (x->typ == H_G) {
+        if (!list_of_basic(x)) return E_DOMAIN;
+        int nc = (int)x->len;
+        if (nc == 0) return group_dict(z, r, 0, nullptr);
+        if (nc > KMAXC) return set_error(E_NOT_IMPL, "group by more than %d columns", KMAXC);
+        V0* c = host_nodes(x);
+        long long n = c[0].len;
+        V cols[KMAXC];
+        const void* ptrs[KMAXC];
+        ColSet cs{};
+        cs.ncol = nc;
+        for (int i = 0; i < nc; i++) {
+            if (c[i].len != n) return set_error(E_LENGTH, "group: columns of different lengths");
+            cols[i] = &c[i];
+            HG_CHECK(in_ptr(&c[i], &ptrs[i]));
+            cs.col[i] = ptrs[i];
+            cs.typ[i] = c[i].typ;
+            if (!(is_real(c[i].typ) || c[i].typ == H_C || is_dtime(c[i].typ)))
+                return set_error(E_NOT_IMPL, "group on symbol/string columns is outside the path");
+        }
+        if (nc == 2 && c[0].typ == H_I && c[1].typ == H_I) {  // pfnOrderBy -> checkOrderCase1
+            KeySpec s{};
+            s.ncol = 2;
+            s.col[0] = ptrs[0]; s.typ[0] = H_I; s.xf[0] = XF_CASE1;
+            s.col[1] = ptrs[1]; s.typ[1] = H_I;
+            // 32 or 64 bits as lib_radixsort_long decides on the packed keys
+            unsigned long long* k = (unsigned long long*)salloc((size_t)(n > 0 ? n : 1) * 8);
+            if (!k) return E_DEVICE_OOM;
+            if (n > 0) HG_LAUNCH("make_keys", gcap(n), 256, 0, k_make_keys<unsigned long long>, s, n, k);
+            V0 tmp{};
+            tmp.typ = H_L; tmp.len = n; tmp.g = (G)k;
+            HG_CHECK(sort_int_column(&tmp, k, n, &r));
+            return group_dict(z, r, n, &cs);
+        }
+        HG_CHECK(sort_columns(nc, cols, ptrs, nullptr, n, &r));
+        return group_dict(z, r, n, &cs);
+    }
+    if (x->typ == H_C) {
+        const void* p;
+        HG_CHECK(in_ptr(x, &p));
+        HG_CHECK(sort_char(p, x->len, &r));
+        ColSet cs{};
+        cs.ncol = 1; cs.col[0] = p; cs.typ[0] = H_C;
+        return group_dict(z, r, x->len, &cs);
+    }
+    if (is_real(x->typ) || is_dtime(x->typ)) {  // the reference uses its quicksort here: same partition
+        const void* p;
+        HG_CHECK(in_ptr(x, &p));
+        V cols[1] = {x};
+        const void* ptrs[1] = {p};
+        HG_CHECK(sort_columns(1, cols, ptrs, nullptr, x->len, &r));
+        ColSet cs{};
+        cs.ncol = 1; cs.col[0] = p; cs.typ[0] = x->typ;
+        return group_dict(z, r, x->len, &cs);
+    }
+    return set_error(E_NOT_IMPL, "group on this type is outside the path");
+}
+
+I pfnGroup(V z, V x) {
+    if (x->typ == H_G && x->len == 2) {
+        V0* c = host_nodes(x);
+        if (c[0].typ == H_C && c[1].typ == H_C && c[0].len == c[1].len) return pfnGroupTrie(z, x);
+    }
+    return pfnGroupBasic(z, x);
+}
+
+static I order_basic(V z, V x, V y) {
+    if (!(is_basic(x->typ) && y->typ == H_B && y->len == 1)) return 1;  // lib_order_basic returns 1
+    uint64_t b;
+    HG_CHECK(read_elem0(y, &b));
+    bool asc = (b & 1) != 0;
+    long long n = x->len;
+    const void* p;
+    HG_CHECK(in_ptr(x, &p));
+    SortResult r{};
+    if (x->typ == H_I || x->typ == H_L) {
+        HG_CHECK(sort_int_column(x, p, n, &r));
+        return order_output(z, r, n, !asc);
+    }
+    if (x->typ == H_C) {
+        if (!asc) return set_error(E_NOT_IMPL, "descending char order (the reference indexes past the range)");
+        HG_CHECK(sort_char(p, n, &r));
+        return order_output(z, r, n, false);
+    }
+    if (is_real(x->typ) || is_dtime(x->typ)) {
+        V cols[1] = {x};
+        const void* ptrs[1] = {p};
+        B d[1] = {asc};
+        HG_CHECK(sort_columns(1, cols, ptrs, d, n, &r));
+        return order_output(z, r, n, false);
+    }
+    return set_error(E_NOT_IMPL, "order on this type is outside the path");
+}
+
+I pfnOrderBy(V z, V x, V y) {
+    HG_CHECK(ensure_init());
+    ScratchScope ss;
+    if (x->typ == H_G && y->typ == H_B && x->len == y->len) {
+        if (!list_of_basic(x)) return E_DOMAIN;
+        int nc = (int)x->len;
+        V0* c = host_nodes(x);
+        const void* pb;
+        HG_CHECK(in_ptr(y, &pb));
+        B dir[KMAXC + 1];
+        if (nc > KMAXC) return set_error(E_NOT_IMPL, "order by more than %d columns", KMAXC);
+        if (nc > 0) {
+            HG_CU(cudaMemcpyAsync(dir, pb, nc, cudaMemcpyDefault, g_stream));
+            HG_CU(cudaStreamSynchronize(g_stream));
+        }
+        long long n = nc ? c[0].len : 0;
+        SortResult r{};
+        if (nc == 2 && c[0].typ == H_I && c[1].typ == H_I && dir[0] == dir[1]) {  // checkOrderCase1
+            const void *p0, *p1;
+            HG_CHECK(in_ptr(&c[0], &p0));
+            HG_CHECK(in_ptr(&c[1], &p1));
+            KeySpec s{};
+            s.ncol = 2;
+            s.col[0] = p0; s.typ[0] = H_I; s.xf[0] = XF_CASE1;
+            s.col[1] = p1; s.typ[1] = H_I;
+            unsigned long long* k = (unsigned long long*)salloc((size_t)(n > 0 ? n : 1) * 8);
+            if (!k) return E_DEVICE_OOM;
+            if (n > 0) HG_LAUNCH("make_keys", gcap(n), 256, 0, k_make_keys<unsigned long long>, s, n, k);
+            V0 tmp{};
+            tmp.typ = H_L; tmp.len = n; tmp.g = (G)k;
+            HG_CHECK(sort_int_column(&tmp, k, n, &r));
+            return order_output(z, r, n, !dir[0]);
+        }
+        if (nc == 1) return order_basic(z, &c[0], y);
+        V cols[KMAXC];
+        const void* ptrs[KMAXC];
+        for (int i = 0; i < nc; i++) {
+            if (c[i].len != n) return E_LENGTH;
+            if (!(is_int(c[i].typ) || is_dtime(c[i].typ)))
+                return set_error(E_NOT_IMPL, "multi-column order on non-integer columns (the reference uses its quicksort)");
+            cols[i] = &c[i];
+            HG_CHECK(in_ptr(&c[i], &ptrs[i]));
+        }
+        bool all_asc = true;
+        for (int i = 0; i < nc; i++) all_asc = all_asc && dir[i];
+        if (all_asc) HG_CHECK(sort_columns(nc, cols, ptrs, dir, n, &r));
+        else HG_CHECK(order_columns_exact(nc, cols, ptrs, dir, n, &r));
+        return order_output(z, r, n, false);
+    }
+    I rc = order_basic(z, x, y);
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,566 @@
+// libhgpu runtime: initialisation, arenas, residency, staging, errors,
+// launch accounting and the value/symbol entry points of the C ABI.
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "hgpu_internal.cuh"
+
+namespace hg {
+
+cudaStream_t g_stream = nullptr;
+int g_sms = 0;
+unsigned* g_derr = nullptr;
+int g_reduce_mode = 1;
+static int g_residency = HGPU_RESIDENT_DEVICE;
+static bool g_inited = false;
+static std::mutex g_init_mu;
+static long long g_launches = 0;
+
+// ------------------------------------------------------------------ errors
+static thread_local char t_err[512];
+
+I set_error(I code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(t_err, sizeof t_err, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+I cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+    const char* base = strrchr(file, '/');
+    set_error(e == cudaErrorMemoryAllocation ? E_DEVICE_OOM : E_DEVICE, "%s failed: %s (%s:%d)", what,
+              cudaGetErrorString(e), base ? base + 1 : file, line);
+    return e == cudaErrorMemoryAllocation ? E_DEVICE_OOM : E_DEVICE;
+}
+
+// ------------------------------------------------------------------ arenas
+// A bump arena over a list of chunks.  A mark is (chunk index, cursor).
+struct Arena {
+    struct Chunk { char* base; size_t cap, cur; };
+    std::vector<Chunk> chunks;
+    size_t cur_chunk = 0;
+    size_t chunk_bytes;
+    bool host;
+    size_t last_off = 0, last_bytes = 0;  // last allocation (for shrinking)
+    long long last_chunk = -1;
+
+    Arena(size_t cb, bool h) : chunk_bytes(cb), host(h) {}
+
+    void* alloc(size_t bytes) {
+        size_t need = (bytes + 255) & ~(size_t)255;
+        if (need == 0) need = 256;
+        for (;;) {
+            if (cur_chunk < chunks.size()) {
+                Chunk& c = chunks[cur_chunk];
+                if (c.cur + need <= c.cap) {
+                    void* p = c.base + c.cur;
+                    last_chunk = (long long)cur_chunk; last_off = c.cur; last_bytes = need;
+                    c.cur += need;
+                    return p;
+                }
+                if (cur_chunk + 1 < chunks.size()) {
+                    // skip to the next chunk only if the request fits there
+                    if (chunks[cur_chunk + 1].cap >= need) { cur_chunk++; chunks[cur_chunk].cur = 0; continue; }
+                    // otherwise drop the smaller tail chunks and grow a larger one
+                    for (size_t k = cur_chunk + 1; k < chunks.size(); k++) free_chunk(chunks[k]);
+                    chunks.resize(cur_chunk + 1);
+                }
+            }
+            size_t cap = need > chunk_bytes ? need : chunk_bytes;
+            char* base = nullptr;
+            cudaError_t e = host ? cudaHostAlloc((void**)&base, cap, cudaHostAllocPortable | cudaHostAllocMapped)
+                                 : cudaMalloc((void**)&base, cap);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                set_error(E_DEVICE_OOM, "%s arena: cannot allocate %zu bytes (%s)", host ? "host" : "device", cap,
+                          cudaGetErrorString(e));
+                return nullptr;
+            }
+            chunks.push_back({base, cap, 0});
+            cur_chunk = chunks.size() - 1;
+        }
+    }
+    void free_chunk(Chunk& c) {
+        cudaStreamSynchronize(g_stream);  // queued work may still use the chunk
+        if (host) cudaFreeHost(c.base); else cudaFree(c.base);
+    }
+    long long mark() const {
+        if (chunks.empty()) return 0;
+        return ((long long)cur_chunk << 40) | (long long)chunks[cur_chunk].cur;
+    }
+    void rewind(long long m) {
+        size_t c = (size_t)(m >> 40), off = (size_t)(m & ((1LL << 40) - 1));
+        if (chunks.empty()) return;
+        if (c >= chunks.size()) return;
+        cur_chunk = c;
+        chunks[c].cur = off;
+        last_chunk = -1;
+    }
+    bool shrink(void* p, size_t new_bytes) {
+        if (last_chunk < 0) return false;
+        Chunk& c = chunks[(size_t)last_chunk];
+        if ((char*)p != c.base + last_off || (size_t)last_chunk != cur_chunk) return false;
+        size_t need = (new_bytes + 255) & ~(size_t)255;
+        if (need == 0) need = 256;
+        if (need > last_bytes) return false;
+        c.cur = last_off + need;
+        last_bytes = need;
+        return true;
+    }
+    bool contains(const void* p) const {
+        for (auto& c : chunks)
+            if ((const char*)p >= c.base && (const char*)p < c.base + c.cap) return true;
+        return false;
+    }
+};
+
+static size_t env_mb(const char* name, size_t dflt_mb) {
+    const char* s = getenv(name);
+    return (size_t)(s ? atoll(s) : (long long)dflt_mb) << 20;
+}
+static Arena* g_out = nullptr;      // output arena (device)
+static Arena* g_scratch = nullptr;  // scratch arena (device)
+static Arena* g_host = nullptr;     // pinned host arena
+
+// heap-offset tokens: token -> (output mark, host mark)
+static std::vector<std::pair<long long, long long>> g_marks;
+
+I ensure_init() {
+    if (g_inited) return 0;
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    if (g_inited) return 0;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return set_error(E_NO_DEVICE, "libhgpu: no CUDA device (%s)", cudaGetErrorString(e));
+    }
+    HG_CU(cudaSetDevice(0));
+    HG_CU(cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, 0));
+    HG_CU(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+    HG_CU(cudaMalloc((void**)&g_derr, 256));
+    HG_CU(cudaMemset(g_derr, 0, 256));
+    if (!g_out) g_out = new Arena(env_mb("HGPU_DEVICE_CHUNK_MB", 4096), false);
+    if (!g_scratch) g_scratch = new Arena(env_mb("HGPU_SCRATCH_CHUNK_MB", 4096), false);
+    if (!g_host) g_host = new Arena(env_mb("HGPU_HOST_CHUNK_MB", 256), true);
+    g_marks.clear();
+    g_marks.push_back({0, 0});
+    g_inited = true;
+    return 0;
+}
+
+I sync() {
+    HG_CU(cudaStreamSynchronize(g_stream));
+    return 0;
+}
+
+void* dalloc(size_t bytes) { return g_out->alloc(bytes); }
+bool dshrink(void* p, size_t new_bytes) { return g_out->shrink(p, new_bytes); }
+long long out_mark() { return g_out->mark(); }
+void out_rewind(long long m) { g_out->rewind(m); }
+void* salloc(size_t bytes) { return g_scratch->alloc(bytes); }
+void* halloc(size_t bytes) { return g_host->alloc(bytes); }
+ScratchScope::ScratchScope() : mark(g_scratch ? g_scratch->mark() : 0) {}
+ScratchScope::~ScratchScope() {
+    if (g_scratch) g_scratch->rewind(mark);
+}
+
+bool is_device_ptr(const void* p) {
+    if (!p) return true;
+    if (g_out->contains(p) || g_scratch->contains(p) || g_host->contains(p)) return true;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged || a.type == cudaMemoryTypeHost;
+}
+
+int esize(I t) {
+    switch (t) {
+    case H_B: case H_J: case H_C: return 1;
+    case H_H: return 2;
+    case H_I: case H_F: case H_M: case H_D: case H_U: case H_W: case H_T: return 4;
+    case H_L: case H_E: case H_Q: case H_Z: case H_S: case H_X: case H_Y: return 8;
+    default: return 8;
+    }
+}
+
+I in_ptr(V x, const void** p) {
+    size_t nb = (size_t)x->len * esize(x->typ);
+    if (x->len == 0) { *p = nullptr; return 0; }
+    if (!is_inline(x) && is_device_ptr(x->g)) { *p = x->g; return 0; }
+    void* d = salloc(nb);
+    if (!d) return E_DEVICE_OOM;
+    HG_CU(cudaMemcpyAsync(d, x->g, nb, cudaMemcpyHostToDevice, g_stream));
+    *p = d;
+    return 0;
+}
+
+I read_elem0(V x, uint64_t* bits) {
+    *bits = 0;
+    if (x->len < 1) return E_LENGTH;
+    int es = esize(x->typ);
+    if (is_inline(x) || !is_device_ptr(x->g) || g_host->contains(x->g)) {
+        memcpy(bits, x->g, es);
+        return 0;
+    }
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, x->g) == cudaSuccess && a.type == cudaMemoryTypeHost) {
+        memcpy(bits, x->g, es);
+        return 0;
+    }
+    cudaGetLastError();
+    HG_CU(cudaMemcpyAsync(bits, x->g, es, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));
+    return 0;
+}
+
+I alloc_out(V z, I typ, L len, void** dptr) {
+    z->typ = typ;
+    z->len = len;
+    if (len > 1) {
+        void* d = dalloc((size_t)len * esize(typ));
+        if (!d) return E_DEVICE_OOM;
+        z->g = (G)d;
+        *dptr = d;
+    } else {
+        z->g = (G)&z->b;
+        z->i64 = 0;
+        void* d = salloc(16);
+        if (!d) return E_DEVICE_OOM;
+        *dptr = d;
+    }
+    return 0;
+}
+
+I finish_out(V z, void* dptr) {
+    if (z->len == 1 && is_basic(z->typ)) {
+        HG_CU(cudaMemcpyAsync(&z->b, dptr, esize(z->typ), cudaMemcpyDeviceToHost, g_stream));
+        HG_CU(cudaStreamSynchronize(g_stream));
+        z->g = (G)&z->b;
+    }
+    return apply_residency(z);
+}
+
+I init_list(V z, I typ, L n) {
+    z->typ = typ;
+    z->len = n;
+    z->g = (G)halloc((size_t)(n > 0 ? n : 1) * sizeof(V0));
+    if (!z->g) return E_DEVICE_OOM;
+    return 0;
+}
+
+V0* host_nodes(V x) { return (V0*)x->g; }
+
+static I to_host_rec(V z, V x, bool in_place) {
+    if (x->typ == H_G || x->typ == H_N) {
+        V0* src = (V0*)x->g;
+        if (!in_place) {
+            V0 hdr = *x;
+            HG_CHECK(init_list(z, hdr.typ, hdr.len));
+            for (L i = 0; i < hdr.len; i++) HG_CHECK(to_host_rec((V0*)z->g + i, src + i, false));
+        } else {
+            for (L i = 0; i < x->len; i++) HG_CHECK(to_host_rec(src + i, src + i, true));
+        }
+        return 0;
+    }
+    if (!is_basic(x->typ)) return set_error(E_NOT_IMPL, "hgpuToHost: type %d", x->typ);
+    V0 hdr = *x;
+    if (z != x) *z = hdr;
+    if (is_inline(x)) {
+        z->g = (G)&z->b;
+        return 0;
+    }
+    if (hdr.len <= 1) {  // a one-element vector stored out of line
+        uint64_t bits = 0;
+        if (hdr.len == 1) HG_CHECK(read_elem0(&hdr, &bits));
+        z->i64 = (L)bits;
+        z->g = (G)&z->b;
+        return 0;
+    }
+    size_t nb = (size_t)hdr.len * esize(hdr.typ);
+    if (g_host->contains(hdr.g)) { z->g = hdr.g; return 0; }
+    void* h = g_host->alloc(nb);
+    if (!h) return E_DEVICE_OOM;
+    HG_CU(cudaMemcpyAsync(h, hdr.g, nb, cudaMemcpyDefault, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));
+    z->g = (G)h;
+    return 0;
+}
+
+I apply_residency(V z) {
+    if (g_residency != HGPU_RESIDENT_HOST) return 0;
+    return to_host_rec(z, z, true);
+}
+
+// ----------------------------------------------------------- list registry
+static std::vector<ListInfo> g_lists;
+void register_list(const ListInfo& g) {
+    if (g_lists.size() > 256) g_lists.erase(g_lists.begin());
+    g_lists.push_back(g);
+}
+const ListInfo* find_list(const V0* nodes, long long ng) {
+    for (size_t i = g_lists.size(); i-- > 0;)
+        if (g_lists[i].nodes == nodes && g_lists[i].ng == ng) return &g_lists[i];
+    return nullptr;
+}
+
+// ------------------------------------------------------------ device errors
+I check_device_errors() {
+    unsigned h = 0;
+    HG_CU(cudaMemcpyAsync(&h, g_derr, sizeof h, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));
+    if (!h) return 0;
+    HG_CU(cudaMemsetAsync(g_derr, 0, sizeof h, g_stream));
+    if (h & DERR_TIMEOUT) return set_error(E_DEVICE_TIMEOUT, "a device-side wait exceeded its iteration limit");
+    if (h & DERR_CAPACITY) return set_error(E_DEVICE_OOM, "a device hash table or buffer ran out of capacity");
+    if (h & DERR_INDEX) return set_error(E_INDEX, "index out of range");
+    if (h & DERR_DIVZERO) return set_error(E_DIV_ZERO, "division by zero");
+    return set_error(E_DEVICE, "device error flags 0x%x", h);
+}
+
+// ---------------------------------------------------------------- profiling
+static bool g_prof = false;
+struct ProfRec { const char* name; cudaEvent_t e0, e1; };
+static std::vector<ProfRec> g_recs;
+static std::vector<cudaEvent_t> g_event_pool;
+static std::vector<std::string> g_prof_names;
+
+static cudaEvent_t get_event() {
+    if (!g_event_pool.empty()) {
+        cudaEvent_t e = g_event_pool.back();
+        g_event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+LaunchScope::LaunchScope(const char* n) : name(n), e0(nullptr), e1(nullptr), on(g_prof) {
+    g_launches++;
+    if (on) {
+        e0 = get_event();
+        e1 = get_event();
+        cudaEventRecord(e0, g_stream);
+    }
+}
+LaunchScope::~LaunchScope() {
+    if (on) {
+        cudaEventRecord(e1, g_stream);
+        g_recs.push_back({name, e0, e1});
+    }
+}
+
+I last_launch_error() {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch", __FILE__, __LINE__);
+    return 0;
+}
+
+}  // namespace hg
+
+using namespace hg;
+
+// ======================================================================
+// C ABI
+// ======================================================================
+extern "C" {
+
+void initBackend(void) { ensure_init(); }
+
+I hgpuInit(L device_arena_bytes, L host_arena_bytes) {
+    HG_CHECK(ensure_init());
+    if (device_arena_bytes > 0) { void* p = dalloc((size_t)device_arena_bytes); if (!p) return E_DEVICE_OOM; }
+    if (host_arena_bytes > 0) { void* p = g_host->alloc((size_t)host_arena_bytes); if (!p) return E_DEVICE_OOM; }
+    setHeapOffset(0);
+    return 0;
+}
+
+V allocNode(void) {
+    if (ensure_init()) return nullptr;
+    V x = (V)halloc(sizeof(V0));
+    if (x) memset(x, 0, sizeof(V0));
+    return x;
+}
+
+// Caller-facing allocation (literals, interpreter temporaries): payloads go
+// to the pinned host arena, which host code can fill and kernels can read.
+V initV(V x, I typ, L len) {
+    if (ensure_init()) return nullptr;
+    x->typ = typ;
+    x->len = len;
+    if (is_basic(typ)) x->g = (len > 1) ? (G)halloc((size_t)getTypeSize(typ, len)) : (G)&x->b;
+    else x->g = (G)halloc((size_t)(len > 0 ? len : 1) * sizeof(V0));
+    return x;
+}
+
+L getHeapOffset(void) {
+    if (ensure_init()) return 0;
+    g_marks.push_back({g_out->mark(), g_host->mark()});
+    return (L)(g_marks.size() - 1);
+}
+
+L setHeapOffset(L cur) {
+    if (ensure_init()) return cur;
+    if (cur < 0 || (size_t)cur >= g_marks.size()) return cur;
+    // work already queued may still read the region being released
+    cudaStreamSynchronize(g_stream);
+    g_out->rewind(g_marks[(size_t)cur].first);
+    g_host->rewind(g_marks[(size_t)cur].second);
+    g_lists.clear();  // their node arrays and payloads are released
+    g_marks.resize((size_t)cur + 1);
+    return cur;
+}
+
+L getTypeSize(I typ, L len) {
+    if (typ == H_G || typ == H_N || typ == H_A || typ == H_K || typ == H_V) return (L)sizeof(V0) * len;
+    return (L)esize(typ) * len + (typ == H_C ? 1 : 0);
+}
+
+static std::unordered_map<std::string, L>* g_sym_ids;
+static std::vector<std::string>* g_sym_names;
+L getSymbol(S name) {
+    if (!g_sym_ids) { g_sym_ids = new std::unordered_map<std::string, L>(); g_sym_names = new std::vector<std::string>(); }
+    auto it = g_sym_ids->find(name);
+    if (it != g_sym_ids->end()) return it->second;
+    L id = (L)g_sym_names->size();
+    g_sym_names->push_back(name);
+    (*g_sym_ids)[name] = id;
+    return id;
+}
+S getSymbolStr(L x) {
+    if (!g_sym_names || x < 0 || (size_t)x >= g_sym_names->size()) return (S) "";
+    return (S)(*g_sym_names)[(size_t)x].c_str();
+}
+
+I hgpuSetResidency(I mode) {
+    if (mode != HGPU_RESIDENT_DEVICE && mode != HGPU_RESIDENT_HOST) return E_DOMAIN;
+    g_residency = mode;
+    return 0;
+}
+I hgpuGetResidency(void) { return g_residency; }
+
+I hgpuToHost(V z, V x) {
+    HG_CHECK(ensure_init());
+    return to_host_rec(z, x, false);
+}
+
+static I to_device_rec(V z, V x) {
+    if (x->typ == H_G || x->typ == H_N) {
+        V0 hdr = *x;
+        HG_CHECK(init_list(z, hdr.typ, hdr.len));
+        for (L i = 0; i < hdr.len; i++) HG_CHECK(to_device_rec((V0*)z->g + i, (V0*)hdr.g + i));
+        return 0;
+    }
+    if (!is_basic(x->typ)) return set_error(E_NOT_IMPL, "hgpuToDevice: type %d", x->typ);
+    V0 hdr = *x;
+    *z = hdr;
+    if (hdr.len <= 1) {
+        uint64_t bits = 0;
+        if (hdr.len == 1) HG_CHECK(read_elem0(&hdr, &bits));
+        z->i64 = (L)bits;
+        z->g = (G)&z->b;
+        return 0;
+    }
+    size_t nb = (size_t)hdr.len * esize(hdr.typ);
+    void* d = dalloc(nb);
+    if (!d) return E_DEVICE_OOM;
+    HG_CU(cudaMemcpyAsync(d, hdr.g, nb, cudaMemcpyDefault, g_stream));
+    z->g = (G)d;
+    return 0;
+}
+
+I hgpuToDevice(V z, V x) {
+    HG_CHECK(ensure_init());
+    return to_device_rec(z, x);
+}
+
+I hgpuIsDevice(V x) {
+    if (ensure_init()) return 0;
+    if (!is_basic(x->typ) || is_inline(x)) return 0;
+    if (g_host->contains(x->g)) return 0;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, x->g) != cudaSuccess) { cudaGetLastError(); return 0; }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+I hgpuSync(void) {
+    HG_CHECK(ensure_init());
+    HG_CU(cudaStreamSynchronize(g_stream));
+    return check_device_errors();
+}
+
+void* hgpuStream(void) {
+    if (ensure_init()) return nullptr;
+    return (void*)g_stream;
+}
+
+const char* hgpuLastError(void) { return t_err; }
+
+I hgpuSetReduceMode(I mode) {
+    if (mode != 0 && mode != 1) return E_DOMAIN;
+    g_reduce_mode = mode;
+    return 0;
+}
+
+I hgpuProfile(I enable) {
+    g_prof = enable != 0;
+    return 0;
+}
+
+I hgpuProfileReset(void) {
+    if (g_stream) cudaStreamSynchronize(g_stream);
+    for (auto& r : g_recs) { g_event_pool.push_back(r.e0); g_event_pool.push_back(r.e1); }
+    g_recs.clear();
+    return 0;
+}
+
+I hgpuProfileRead(I cap, const char** names, double* total_ms, L* launches) {
+    if (g_stream) cudaStreamSynchronize(g_stream);
+    std::vector<std::pair<const char*, std::pair<double, L>>> acc;
+    for (auto& r : g_recs) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, r.e0, r.e1);
+        size_t k = 0;
+        for (; k < acc.size(); k++)
+            if (!strcmp(acc[k].first, r.name)) break;
+        if (k == acc.size()) acc.push_back({r.name, {0.0, 0}});
+        acc[k].second.first += ms;
+        acc[k].second.second += 1;
+    }
+    for (size_t k = 0; k < acc.size() && (I)k < cap; k++) {
+        if (names) names[k] = acc[k].first;
+        if (total_ms) total_ms[k] = acc[k].second.first;
+        if (launches) launches[k] = acc[k].second.second;
+    }
+    return (I)acc.size();
+}
+
+L hgpuLaunchCount(void) { return g_launches; }
+
+static cudaEvent_t g_t0 = nullptr, g_t1 = nullptr;
+I hgpuTimerStart(void) {
+    HG_CHECK(ensure_init());
+    if (!g_t0) { cudaEventCreate(&g_t0); cudaEventCreate(&g_t1); }
+    HG_CU(cudaEventRecord(g_t0, g_stream));
+    return 0;
+}
+double hgpuTimerStop(void) {
+    if (!g_t0) return -1.0;
+    cudaEventRecord(g_t1, g_stream);
+    cudaEventSynchronize(g_t1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, g_t0, g_t1);
+    return ms;
+}
+
+}  // extern "C"

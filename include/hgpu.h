@@ -200,6 +200,7 @@ I hgpuGroupLen(V z, V x, V y);
 typedef struct hgpu_chain_s *hgpuChain;
 I hgpuChainCreate(hgpuChain *out, const char *program);
 I hgpuChainRun(hgpuChain c, V z, V *x);           /* autofusion-style: inputs x[0..n) -> z */
+I hgpuChainRunMany(hgpuChain c, V *z, V *x);      /* compress sinks: one output node per expression */
 I hgpuChainDestroy(hgpuChain c);
 /* Multi-column compress sharing one mask: pattern.cc:452-520 (V *z, V x, V *y) */
 I hgpuCompressMany(V *z, V x, V *y, L n);

@@ -889,3 +889,40 @@ I hgpuCompressMany(V *z, V x, V *y, L n) {
     for (L k = 0; k < n; k++) CHECKE(pfnCompress(z[k], x, y[k]));
     R 0;
 }
+
+/* ------------------------------------------------ fixed-order tile tree sum */
+/* Restatement of libhgpu's deterministic summation order, for bit-exact
+ * checks of its f64/f32 sums (the reference's own order depends on the
+ * OpenMP thread count, so against it sums agree within a tolerance only):
+ * chunks of 4096 elements; lane t (0..255) adds e[t], e[t+256], ... from
+ * +0.0; each 32-lane group folds by a xor butterfly (offsets 16,8,4,2,1);
+ * the 8 group sums combine as ((w0+w1)+(w2+w3))+((w4+w5)+(w6+w7)); chunk
+ * partials are reduced again the same way until one value is left. */
+static E tile_tree_f64(const E *x, L n) {
+    E lanes[256], ws[8];
+    for (int t = 0; t < 256; t++) {
+        E acc = 0.0;
+        for (int k = 0; k < 16; k++) { L j = (L)k * 256 + t; if (j < n) acc = acc + x[j]; }
+        lanes[t] = acc;
+    }
+    for (int w = 0; w < 8; w++) {
+        E v[32];
+        for (int l = 0; l < 32; l++) v[l] = lanes[w * 32 + l];
+        for (int o = 16; o > 0; o >>= 1) {
+            E nv[32];
+            for (int l = 0; l < 32; l++) nv[l] = v[l] + v[l ^ o];
+            memcpy(v, nv, sizeof v);
+        }
+        ws[w] = v[0];
+    }
+    return ((ws[0] + ws[1]) + (ws[2] + ws[3])) + ((ws[4] + ws[5]) + (ws[6] + ws[7]));
+}
+E hgoTreeSumF64(const E *x, L n) {
+    if (n <= 4096) return tile_tree_f64(x, n);
+    L m = (n + 4095) / 4096;
+    E *p = malloc(sizeof(E) * m);
+    for (L c = 0; c < m; c++) p[c] = tile_tree_f64(x + c * 4096, (n - c * 4096) < 4096 ? (n - c * 4096) : 4096);
+    E r = hgoTreeSumF64(p, m);
+    free(p);
+    return r;
+}

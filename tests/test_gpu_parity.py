@@ -1,0 +1,240 @@
+"""GPU parity against the oracle port on seeded inputs larger than the golden
+fixtures, plus determinism and size-independent properties.
+
+Bar: bit-exact for integer, index, boolean and permutation outputs; f64 sums
+within a relative tolerance of 1e-12 of the oracle (whose OpenMP order, like
+the reference's, depends on the thread count) and bit-exact against the
+oracle's restatement of the library's fixed summation order.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from horsepower_gb300.abi import Builtins, H_B, H_C, H_E, H_I, H_L
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+RTOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def libs():
+    import subprocess
+    import horsepower_gb300
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
+    ora = Builtins(os.path.join(ROOT, "oracle", "_build", "liboracle.so"), "oracle")
+    ora.lib.hgoTreeSumF64.restype = C.c_double
+    ora.lib.hgoTreeSumF64.argtypes = [C.c_void_p, C.c_longlong]
+    return horsepower_gb300.load(), ora
+
+
+def both(libs, fn, mk):
+    out = []
+    for L in libs:
+        z = L.call(fn, *mk(L))
+        out.append(L.to_py(z))
+        L.free_inputs()
+    return out
+
+
+def same(a, b):
+    if isinstance(a, np.ndarray):
+        return a.dtype == b.dtype and np.array_equal(a, b, equal_nan=a.dtype.kind == "f")
+    if isinstance(a, tuple):
+        return all(same(p, q) for p, q in zip(a[1:], b[1:]))
+    return len(a) == len(b) and all(same(p, q) for p, q in zip(a, b))
+
+
+@pytest.mark.parametrize("dens", [0.0, 0.018, 0.5, 1.0])
+@pytest.mark.parametrize("typ,dt", [(H_E, np.float64), (H_I, np.int32), (H_B, np.bool_), (H_C, np.int8)])
+def test_compress_large(libs, dens, typ, dt):
+    rng = np.random.default_rng(11)
+    n = 6_001_215
+    m = rng.random(n) < dens
+    v = rng.integers(-100, 100, n).astype(dt) if typ != H_E else rng.standard_normal(n)
+    a, b = both(libs, "pfnCompress", lambda L: (L.vec(m, H_B), L.vec(v, typ)))
+    assert same(a, b)
+
+
+def test_where_large(libs):
+    rng = np.random.default_rng(12)
+    m = rng.random(10_000_001) < 0.3
+    a, b = both(libs, "pfnWhere", lambda L: (L.vec(m, H_B),))
+    assert same(a, b)
+
+
+@pytest.mark.parametrize("fn", ["pfnLt", "pfnGeq", "pfnEq", "pfnMul", "pfnMinus", "pfnDiv", "pfnAnd"])
+def test_elementwise_large(libs, fn):
+    rng = np.random.default_rng(13)
+    n = 5_000_003
+    if fn == "pfnAnd":
+        x, y, tx, ty = rng.random(n) < 0.5, rng.random(n) < 0.5, H_B, H_B
+    else:
+        x, y, tx, ty = np.round(rng.standard_normal(n), 3), rng.integers(1, 9, n).astype(np.int32), H_E, H_I
+    a, b = both(libs, fn, lambda L: (L.vec(x, tx), L.vec(y, ty)))
+    assert same(a, b)
+
+
+def test_sum_deterministic_and_within_tolerance(libs):
+    gpu, ora = libs
+    rng = np.random.default_rng(14)
+    x = rng.uniform(0, 1e5, 20_000_000)
+    r1 = gpu.to_py(gpu.call("pfnSum", gpu.vec(x, H_E)))[0]
+    r2 = gpu.to_py(gpu.call("pfnSum", gpu.vec(x, H_E)))[0]
+    assert r1 == r2, "fixed-order sum is not reproducible"
+    fixed = ora.lib.hgoTreeSumF64(x.ctypes.data, x.size)
+    assert r1 == fixed, f"GPU sum {r1!r} != oracle restatement of the fixed order {fixed!r}"
+    ref = ora.to_py(ora.call("pfnSum", ora.vec(x, H_E)))[0]
+    assert abs(r1 - ref) <= RTOL * abs(ref)
+    gpu.free_inputs()
+    ora.free_inputs()
+
+
+@pytest.mark.parametrize("fn", ["pfnMin", "pfnMax", "pfnSum", "pfnAvg"])
+def test_int_reductions_large(libs, fn):
+    rng = np.random.default_rng(15)
+    x = rng.integers(-2 ** 31, 2 ** 31 - 1, 9_000_001, dtype=np.int64).astype(np.int32)
+    a, b = both(libs, fn, lambda L: (L.vec(x, H_I),))
+    assert same(a, b) if fn != "pfnAvg" else abs(a[0] - b[0]) <= 1e-15 * abs(b[0])
+
+
+def test_gather_large(libs):
+    rng = np.random.default_rng(16)
+    x = rng.standard_normal(3_000_000)
+    idx = rng.integers(0, x.size, 8_000_000).astype(np.int64)
+    a, b = both(libs, "pfnIndex", lambda L: (L.vec(x, H_E), L.vec(idx, H_L)))
+    assert same(a, b)
+
+
+def test_join_pk_fk(libs):
+    rng = np.random.default_rng(17)
+    D = 3_000_000
+    pk = rng.permutation(D).astype(np.int32)
+    keep = rng.random(D) < 0.15
+    fk = rng.integers(0, D, 12_000_000).astype(np.int32)
+    a, b = both(libs, "pfnJoinIndex", lambda L: (L.vec(pk[keep], H_I), L.vec(fk, H_I), L.sym("eq")))
+    assert same(a, b)
+
+
+def test_join_duplicates(libs):
+    rng = np.random.default_rng(18)
+    x = rng.integers(0, 20000, 200_000).astype(np.int32)
+    y = rng.integers(0, 30000, 400_000).astype(np.int32)
+    a, b = both(libs, "pfnJoinIndex", lambda L: (L.vec(x, H_I), L.vec(y, H_I), L.sym("eq")))
+    assert same(a, b)
+
+
+def test_index_of_and_member(libs):
+    rng = np.random.default_rng(19)
+    x = rng.permutation(4_000_000).astype(np.int64)[:1_000_000]
+    y = rng.integers(0, 4_000_000, 5_000_000).astype(np.int64)
+    a, b = both(libs, "pfnIndexOf", lambda L: (L.vec(x, H_L), L.vec(y, H_L)))
+    assert same(a, b)
+    a, b = both(libs, "pfnMember", lambda L: (L.vec(y, H_L), L.vec(x, H_L)))
+    assert same(a, b)
+
+
+@pytest.mark.parametrize("kind", ["i32", "i64_zipf", "trie", "list_li"])
+def test_group_large(libs, kind):
+    rng = np.random.default_rng(20)
+    n = 3_000_000
+    if kind == "i32":
+        mk = lambda L: (L.vec(rng_a, H_I),)  # noqa: E731
+        rng_a = rng.integers(-1000, 100000, n).astype(np.int32)
+    elif kind == "i64_zipf":
+        rng_a = np.minimum(rng.zipf(1.1, n), 1_000_000).astype(np.int64)
+        mk = lambda L: (L.vec(rng_a, H_L),)  # noqa: E731
+    elif kind == "trie":
+        f, s = rng.integers(0, 3, n).astype(np.int8), rng.integers(0, 2, n).astype(np.int8)
+        mk = lambda L: (L.list([L.vec(f, H_C), L.vec(s, H_C)]),)  # noqa: E731
+    else:
+        k, s = rng.integers(0, 5000, n).astype(np.int64), rng.integers(-3, 3, n).astype(np.int32)
+        mk = lambda L: (L.list([L.vec(k, H_L), L.vec(s, H_I)]),)  # noqa: E731
+    a, b = both(libs, "pfnGroup", mk)
+    assert np.array_equal(a[1], b[1])
+    assert len(a[2]) == len(b[2]) and all(np.array_equal(p, q) for p, q in zip(a[2], b[2]))
+
+
+def test_order_key_sec(libs):
+    rng = np.random.default_rng(21)
+    n = 2_000_000
+    key = np.minimum(rng.zipf(1.1, n), 10_000_000).astype(np.int64)
+    sec = rng.integers(0, 2 ** 20 + 1, n).astype(np.int32)
+    a, b = both(libs, "pfnOrderBy", lambda L: (L.list([L.vec(key, H_L), L.vec(sec, H_I)]), L.vec(np.array([1, 1], bool), H_B)))
+    assert same(a, b)
+
+
+@pytest.mark.parametrize("agg", ["hgpuGroupSum", "hgpuGroupAvg", "hgpuGroupMin", "hgpuGroupMax", "hgpuGroupLen"])
+def test_group_aggregates_large(libs, agg):
+    gpu, ora = libs
+    rng = np.random.default_rng(22)
+    n = 2_000_000
+    key = np.minimum(rng.zipf(1.1, n), 200_000).astype(np.int64)
+    pay = rng.uniform(0, 1e5, n)
+    outs = []
+    for L in libs:
+        g = L.call("pfnGroup", L.vec(key, H_L))
+        vals = L.call("pfnValues", g)
+        outs.append(L.to_py(L.call(agg, L.vec(pay, H_E), vals)))
+    a, b = outs
+    assert a.dtype == b.dtype and a.shape == b.shape
+    if agg in ("hgpuGroupSum", "hgpuGroupAvg"):
+        assert np.allclose(a, b, rtol=RTOL, atol=0)
+    else:
+        assert np.array_equal(a, b)
+    for L in libs:
+        L.free_inputs()
+
+
+def test_chain_equals_fused(libs):
+    gpu, _ = libs
+    rng = np.random.default_rng(23)
+    key = rng.integers(0, 50_000, 1_000_000).astype(np.int32)
+    pay = rng.uniform(0, 1e5, 1_000_000)
+    g = gpu.call("pfnGroup", gpu.vec(key, H_I))
+    vals = gpu.call("pfnValues", g)
+    x = gpu.vec(pay, H_E)
+    fused = gpu.to_py(gpu.call("hgpuGroupSum", x, vals))
+    t = gpu.call("pfnEachRight", x, vals, gpu.fn_ptr("pfnIndex"))
+    e = gpu.call("pfnEach", t, gpu.fn_ptr("pfnSum"))
+    chain = gpu.to_py(gpu.call("pfnRaze", e))
+    assert np.array_equal(fused, chain), "fused and chained group sums differ"
+    gpu.free_inputs()
+
+
+def test_fused_q6_chain(libs):
+    """The q6 chain fused into one kernel equals the interpreter's plain
+    builtin sequence (oracle) within 1e-12, and is reproducible."""
+    from horsepower_gb300 import data as D, plans as P
+    gpu, ora = libs
+    t = D.filter_table()
+    plain = ora.to_py(P.filter_aggregate(ora, P.host_nodes(ora, t, P.FILTER_TYPES)))[0]
+    nodes = P.host_nodes(gpu, t, P.FILTER_TYPES)
+    ch = P.Chain(gpu, P.Q6_CHAIN.format(lo=D.WIN_LO, hi=D.WIN_HI))
+    f1 = gpu.to_py(ch.run([nodes["shipdate"], nodes["qty"], nodes["disc"], nodes["price"]]))[0]
+    f2 = gpu.to_py(ch.run([nodes["shipdate"], nodes["qty"], nodes["disc"], nodes["price"]]))[0]
+    assert f1 == f2
+    assert abs(f1 - plain) <= RTOL * abs(plain), (f1, plain)
+    gplain = gpu.to_py(P.filter_aggregate(gpu, nodes))[0]
+    assert abs(gplain - plain) <= RTOL * abs(plain)
+    gpu.free_inputs()
+    ora.free_inputs()
+
+
+def test_join_group_pipeline(libs):
+    """The join + group-by query at 1/10 scale: GPU vs oracle."""
+    from horsepower_gb300 import data as D, plans as P
+    gpu, ora = libs
+    dim, fact = D.join_tables(6_000_000, 1_500_000, seed=5)
+    outs = []
+    for L in libs:
+        r = P.join_group(L, P.host_nodes(L, dim, P.DIM_TYPES), P.host_nodes(L, fact, P.FACT_TYPES))
+        outs.append([L.to_py(v) for v in r])
+        L.free_inputs()
+    a, b = outs
+    for k in (0, 1, 5):
+        assert np.array_equal(a[k], b[k])
+    for k in (2, 3, 4):
+        assert np.allclose(a[k], b[k], rtol=RTOL, atol=0)
