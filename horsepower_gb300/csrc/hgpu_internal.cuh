@@ -129,9 +129,24 @@ struct ListInfo {
     const long long* starts;  // device, ng entries (LIST_SEGMENTS)
     long long total;          // sum of lengths (LIST_SEGMENTS)
     const void* data;         // device payload
+    int group_rows;           // 1: @group row lists (a permutation of 0..total-1, no empty group)
+    // cached split of the segments longer than one reduction tile (output arena)
+    int planned;
+    long long nbig;
+    unsigned long long nchunks;
+    const long long* big;
+    const unsigned long long* chunk0;
+    const long long* pstarts;
 };
 void register_list(const ListInfo& g);
-const ListInfo* find_list(const V0* nodes, long long ng);
+ListInfo* find_list(const V0* nodes, long long ng);
+
+// Index vectors produced by this library carry a known value range: every
+// element of the i64 vector at `data` (length len) lies in [0, bound).  An
+// @index with such a vector cannot go out of range when bound <= len(x), so
+// it needs no synchronous bounds check.
+void register_bound(const void* data, long long len, long long bound);
+bool known_in_range(const void* data, long long len, long long limit);
 
 // reduction mode (1 = fixed-order deterministic tile tree)
 extern int g_reduce_mode;

@@ -205,6 +205,7 @@ I pfnWhere(V z, V x) {
     }
     dshrink(d, (size_t)cnt * 8);
     z->g = (G)d;
+    register_bound(d, cnt, n);
     return apply_residency(z);
 }
 

@@ -357,8 +357,8 @@ static I compile_chain(hgpu_chain_s* c, const std::vector<int>& types, std::shar
     if (!nv) return set_error(E_NOT_IMPL, "chain compilation needs libnvrtc, which could not be opened");
     nvrtcProgram_t prog;
     if (nv->create(&prog, src.c_str(), "chain.cu", 0, nullptr, nullptr)) return set_error(E_DEVICE, "nvrtcCreateProgram failed");
-    const char* opts[] = {"--gpu-architecture=sm_103a", "-default-device", "-std=c++17", "-O3", "--fmad=false"};
-    int rc = nv->compile(prog, 5, opts);
+    const char* opts[] = {"--gpu-architecture=sm_103a", "-default-device", "-std=c++17", "--fmad=false"};
+    int rc = nv->compile(prog, 4, opts);
     if (rc) {
         size_t ls = 0;
         nv->logsize(prog, &ls);

@@ -81,8 +81,10 @@ I pfnIndex(V z, V x, V y) {
         void* dz;
         HG_CHECK(alloc_out(z, x->typ, y->len, &dz));
         HG_CHECK(gather_into(px, x->len, esize(x->typ), py, y->typ, dz, y->len));
-        I e = check_device_errors();
-        if (e) { out_rewind(mark); return e; }
+        if (!(y->typ == H_L && known_in_range(y->g, y->len, x->len))) {
+            I e = check_device_errors();
+            if (e) { out_rewind(mark); return e; }
+        }
         return finish_out(z, dz);
     }
     if (x->typ == H_G) {  // list indexed by one integer: alias the element (h_primitive.cc:74-88)

@@ -61,55 +61,132 @@ __device__ __forceinline__ bool key_at(const void* p, int typ, long long i, K* k
     }
 }
 
+// Slots.  32-bit keys: one u64 per slot = (key << 32) | row, so a probe is a
+// single 8-byte read and an insert a CAS followed, for a repeated key, by an
+// atomicMin on the packed word (same key bits: the minimum is the minimum row).
+// EMPTY (all ones) cannot collide with a real entry because rows are < 2^32-1.
+// 64-bit keys: 16-byte slots {key, row} read with one vector load; the key
+// equal to EMPTY lives in a side slot.
 template <typename K>
 struct Table {
-    K* keys;            // EMPTY = all ones
-    unsigned* row;      // minimum row per slot (0xffffffff = none)
-    unsigned* cnt;      // rows per slot (joins), may be null
-    unsigned* special;  // [0] = min row, [1] = count for the key equal to EMPTY
-    unsigned long long mask;
+    void* slots;
+    unsigned* cnt;      // rows per slot (duplicate-key joins only), may be null
+    unsigned* special;  // 64-bit keys: [0] min row, [1] count of the key equal to EMPTY
+    unsigned* flags;    // [0] = a key was inserted twice
+    unsigned long long cap;  // slots; the home slot is (hash32 * cap) >> 32
 };
 
 template <typename K>
+__device__ __forceinline__ unsigned long long home_slot(K k, unsigned long long cap) {
+    unsigned long long h = hash_key<K>(k);
+    unsigned h32 = sizeof(K) == 4 ? (unsigned)h : (unsigned)(h >> 32);
+    return ((unsigned long long)h32 * cap) >> 32;
+}
+__device__ __forceinline__ unsigned long long next_slot(unsigned long long h, unsigned long long cap) {
+    return (h + 1 == cap) ? 0 : h + 1;
+}
+
+template <typename K>
 __device__ __forceinline__ void table_insert(Table<K> t, K k, unsigned r, unsigned* derr) {
-    const K EMPTY = (K)~(K)0;
-    if (k == EMPTY) {
-        atomicMin(&t.special[0], r);
-        atomicAdd(&t.special[1], 1u);
-        return;
-    }
-    unsigned long long h = hash_key<K>(k) & t.mask;
-    for (unsigned long long p = 0; p <= t.mask; p++) {
-        K cur = t.keys[h];
-        if (cur == EMPTY) {
-            K prev;
-            if constexpr (sizeof(K) == 4) prev = (K)atomicCAS((unsigned*)&t.keys[h], (unsigned)EMPTY, (unsigned)k);
-            else prev = (K)atomicCAS((unsigned long long*)&t.keys[h], (unsigned long long)EMPTY, (unsigned long long)k);
-            cur = (prev == EMPTY) ? k : prev;
+    unsigned long long h = home_slot<K>(k, t.cap);
+    if constexpr (sizeof(K) == 4) {
+        unsigned long long* sl = (unsigned long long*)t.slots;
+        const unsigned long long mine = ((unsigned long long)k << 32) | r;
+        for (unsigned long long p = 0; p < t.cap; p++) {
+            unsigned long long cur = sl[h];
+            if (cur == ~0ull) {
+                cur = atomicCAS(&sl[h], ~0ull, mine);
+                if (cur == ~0ull) return;
+            }
+            if ((unsigned)(cur >> 32) == (unsigned)k) {
+                atomicMin(&sl[h], mine);
+                atomicOr(t.flags, 1u);
+                return;
+            }
+            h = next_slot(h, t.cap);
         }
-        if (cur == k) {
-            atomicMin(&t.row[h], r);
-            if (t.cnt) atomicAdd(&t.cnt[h], 1u);
+    } else {
+        if (k == ~0ull) {
+            if (atomicAdd(&t.special[1], 1u)) atomicOr(t.flags, 1u);
+            atomicMin(&t.special[0], r);
             return;
         }
-        h = (h + 1) & t.mask;
+        ulonglong2* sl = (ulonglong2*)t.slots;
+        for (unsigned long long p = 0; p < t.cap; p++) {
+            unsigned long long cur = sl[h].x;
+            if (cur == ~0ull) {
+                cur = atomicCAS(&sl[h].x, ~0ull, (unsigned long long)k);
+                if (cur == ~0ull) { atomicMin(&sl[h].y, (unsigned long long)r); return; }
+            }
+            if (cur == (unsigned long long)k) {
+                atomicMin(&sl[h].y, (unsigned long long)r);
+                atomicOr(t.flags, 1u);
+                return;
+            }
+            h = next_slot(h, t.cap);
+        }
     }
     flag_error(derr, DERR_CAPACITY);
 }
 
-// slot of k or -1; EMPTY keys map to slot -2 (the special slot) when present
-template <typename K>
-__device__ __forceinline__ long long table_find(const Table<K>& t, K k) {
-    const K EMPTY = (K)~(K)0;
-    if (k == EMPTY) return t.special[1] ? -2 : -1;
-    unsigned long long h = hash_key<K>(k) & t.mask;
-    for (unsigned long long p = 0; p <= t.mask; p++) {
-        K cur = t.keys[h];
-        if (cur == k) return (long long)h;
-        if (cur == EMPTY) return -1;
-        h = (h + 1) & t.mask;
+// Looks up N keys at once: all first-slot reads are issued before any is
+// examined, so a lane keeps N table reads in flight.  slot[j] = slot index
+// (-2 for the 64-bit side slot, -1 if absent), row[j] = minimum row
+// (0xffffffff if absent).
+template <typename K, int N>
+__device__ __forceinline__ void table_find_n(const Table<K>& t, const K* key, const bool* valid, long long* slot,
+                                             unsigned* row) {
+    unsigned long long h[N];
+    if constexpr (sizeof(K) == 4) {
+        const unsigned long long* sl = (const unsigned long long*)t.slots;
+        unsigned long long s[N];
+#pragma unroll
+        for (int j = 0; j < N; j++) { h[j] = home_slot<K>(key[j], t.cap); s[j] = valid[j] ? __ldg(sl + h[j]) : ~0ull; }
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            slot[j] = -1; row[j] = 0xffffffffu;
+            if (!valid[j]) continue;
+            for (unsigned long long p = 0; p < t.cap; p++) {
+                if (s[j] == ~0ull) break;
+                if ((unsigned)(s[j] >> 32) == (unsigned)key[j]) { slot[j] = (long long)h[j]; row[j] = (unsigned)s[j]; break; }
+                h[j] = next_slot(h[j], t.cap);
+                s[j] = __ldg(sl + h[j]);
+            }
+        }
+    } else {
+        const ulonglong2* sl = (const ulonglong2*)t.slots;
+        ulonglong2 s[N];
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            h[j] = home_slot<K>(key[j], t.cap);
+            s[j] = (valid[j] && key[j] != ~0ull) ? __ldg(sl + h[j]) : make_ulonglong2(~0ull, ~0ull);
+        }
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            slot[j] = -1; row[j] = 0xffffffffu;
+            if (!valid[j]) continue;
+            if (key[j] == ~0ull) {
+                if (t.special[1]) { slot[j] = -2; row[j] = t.special[0]; }
+                continue;
+            }
+            for (unsigned long long p = 0; p < t.cap; p++) {
+                if (s[j].x == ~0ull) break;
+                if (s[j].x == (unsigned long long)key[j]) { slot[j] = (long long)h[j]; row[j] = (unsigned)s[j].y; break; }
+                h[j] = next_slot(h[j], t.cap);
+                s[j] = __ldg(sl + h[j]);
+            }
+        }
     }
-    return -1;
+}
+
+template <typename K>
+__device__ __forceinline__ long long table_find(const Table<K>& t, K k, long long* row) {
+    bool v = true;
+    long long s;
+    unsigned r;
+    table_find_n<K, 1>(t, &k, &v, &s, &r);
+    *row = (long long)r;
+    return s;
 }
 
 template <typename K>
@@ -122,20 +199,19 @@ __global__ void k_build(Table<K> t, const void* __restrict__ x, int typ, long lo
 
 template <typename K>
 static I table_create(Table<K>* t, long long n, bool with_count) {
-    unsigned long long cap = 16;
-    while ((double)cap * g_load_factor < (double)n) cap <<= 1;
-    t->mask = cap - 1;
-    t->keys = (K*)salloc(cap * sizeof(K));
-    t->row = (unsigned*)salloc(cap * 4);
+    unsigned long long cap = (unsigned long long)((double)n / g_load_factor) + 16;
+    if (cap > 0xffffffffull) cap = 0xffffffffull;
+    const size_t ss = sizeof(K) == 4 ? 8 : 16;
+    t->cap = cap;
+    t->slots = salloc(cap * ss);
     t->cnt = with_count ? (unsigned*)salloc(cap * 4) : nullptr;
-    t->special = (unsigned*)salloc(16);
-    if (!t->keys || !t->row || (with_count && !t->cnt) || !t->special) return E_DEVICE_OOM;
-    HG_CU(cudaMemsetAsync(t->keys, 0xff, cap * sizeof(K), g_stream));
-    HG_CU(cudaMemsetAsync(t->row, 0xff, cap * 4, g_stream));
+    t->special = (unsigned*)salloc(32);
+    if (!t->slots || (with_count && !t->cnt) || !t->special) return E_DEVICE_OOM;
+    t->flags = t->special + 2;
+    HG_CU(cudaMemsetAsync(t->slots, 0xff, cap * ss, g_stream));
     if (with_count) HG_CU(cudaMemsetAsync(t->cnt, 0, cap * 4, g_stream));
-    unsigned init[4] = {0xffffffffu, 0, 0, 0};
-    HG_CU(cudaMemcpyAsync(t->special, init, 16, cudaMemcpyHostToDevice, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));  // `init` is a host stack buffer
+    HG_CU(cudaMemsetAsync(t->special, 0xff, 4, g_stream));
+    HG_CU(cudaMemsetAsync(t->special + 1, 0, 12, g_stream));
     return 0;
 }
 
@@ -161,9 +237,8 @@ __global__ void k_index_of(Table<K> t, const void* __restrict__ y, int typ, long
         K k;
         long long r = lenX;
         if (key_at<K>(y, typ, i, &k)) {
-            long long s = table_find<K>(t, k);
-            if (s >= 0) r = t.row[s];
-            else if (s == -2) r = t.special[0];
+            long long row;
+            if (table_find<K>(t, k, &row) != -1) r = row;
         }
         z[i] = r;
     }
@@ -232,7 +307,8 @@ __global__ void k_member(Table<K> t, const void* __restrict__ y, int typ, long l
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         K k;
         bool r = false;
-        if (key_at<K>(y, typ, i, &k)) r = table_find<K>(t, k) != -1;
+        long long row;
+        if (key_at<K>(y, typ, i, &k)) r = table_find<K>(t, k, &row) != -1;
         z[i] = r;
     }
 }
@@ -265,11 +341,20 @@ struct LinearBuild {
 };
 
 template <typename K>
-__global__ void __launch_bounds__(JT_THREADS) k_join_probe(Table<K> t, LinearBuild lin, int mode,
-                                                           const void* __restrict__ y, int ytyp, long long n,
-                                                           long long* __restrict__ zb, long long* __restrict__ zp,
-                                                           unsigned long long* status, unsigned* ticket,
-                                                           unsigned long long* total, unsigned* derr) {
+__device__ __forceinline__ bool key_stream(const void* p, int typ, long long i, K* k) {
+    switch (typ) {  // streaming loads: the probe column is read once, keep the table in L2
+    case H_I: *k = (K)(long long)__ldcs((const int*)p + i); return true;
+    case H_L: *k = (K)__ldcs((const long long*)p + i); return true;
+    default: return key_at<K>(p, typ, i, k);
+    }
+}
+
+template <typename K>
+__global__ void __launch_bounds__(JT_THREADS, 4) k_join_probe(Table<K> t, LinearBuild lin, int mode,
+                                                              const void* __restrict__ y, int ytyp, long long n,
+                                                              long long* __restrict__ zb, long long* __restrict__ zp,
+                                                              unsigned long long* status, unsigned* ticket,
+                                                              unsigned long long* total, unsigned* derr) {
     __shared__ unsigned warp_tot[8];
     __shared__ unsigned long long tile_off;
     __shared__ long long tile_id;
@@ -277,28 +362,38 @@ __global__ void __launch_bounds__(JT_THREADS) k_join_probe(Table<K> t, LinearBui
     if (threadIdx.x == 0) tile_id = atomicAdd(ticket, 1u);
     __syncthreads();
     const long long t0 = tile_id, base = t0 * JT_TILE + (long long)warp * 512;
-    long long hit[16];
+    unsigned hit[16];  // build row of each of the lane's 16 probe rows, 0xffffffff if none
     unsigned cnt = 0;
 #pragma unroll
-    for (int k = 0; k < 16; k++) {
-        long long i = base + k * 32 + lane;
-        long long r = -1;
-        K key;
-        if (i < n && key_at<K>(y, ytyp, i, &key)) {
-            if (mode == 0) {
-                long long s = table_find<K>(t, key);
-                if (s >= 0) r = t.row[s];
-                else if (s == -2) r = t.special[0];
-            } else {
-                for (int j = 0; j < lin.n; j++) {
-                    bool m = lin.eq ? ((K)lin.k[j] == key) : ((K)lin.k[j] != key);
-                    if (m) { r = j; break; }
+    for (int h8 = 0; h8 < 16; h8 += 8) {
+        K key[8];
+        bool valid[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            long long i = base + (h8 + k) * 32 + lane;
+            valid[k] = i < n && key_stream<K>(y, ytyp, i, &key[k]);
+        }
+        if (mode == 0) {
+            long long slot[8];
+            unsigned r8[8];
+            table_find_n<K, 8>(t, key, valid, slot, r8);
+#pragma unroll
+            for (int k = 0; k < 8; k++) hit[h8 + k] = r8[k];
+        } else {
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                unsigned r = 0xffffffffu;
+#pragma unroll
+                for (int j = 9; j >= 0; j--) {  // first match wins: scan backwards, keep the last hit
+                    bool m = lin.eq ? ((K)lin.k[j] == key[k]) : ((K)lin.k[j] != key[k]);
+                    if (valid[k] && j < lin.n && m) r = (unsigned)j;
                 }
+                hit[h8 + k] = r;
             }
         }
-        hit[k] = r;
-        cnt += __popc(__ballot_sync(0xffffffffu, r >= 0));
     }
+#pragma unroll
+    for (int k = 0; k < 16; k++) cnt += __popc(__ballot_sync(0xffffffffu, hit[k] != 0xffffffffu));
     if (lane == 0) warp_tot[warp] = cnt;
     __syncthreads();
     if (warp == 0) {
@@ -315,12 +410,12 @@ __global__ void __launch_bounds__(JT_THREADS) k_join_probe(Table<K> t, LinearBui
     for (unsigned w = 0; w < warp; w++) off += warp_tot[w];
 #pragma unroll
     for (int k = 0; k < 16; k++) {
-        bool sel = hit[k] >= 0;
+        bool sel = hit[k] != 0xffffffffu;
         unsigned bal = __ballot_sync(0xffffffffu, sel);
         if (sel) {
             long long o = (long long)off + __popc(bal & lanemask_lt());
-            zb[o] = hit[k];
-            zp[o] = base + k * 32 + lane;
+            __stcs(zb + o, (long long)hit[k]);
+            __stcs(zp + o, base + k * 32 + lane);
         }
         off += __popc(bal);
     }
@@ -333,10 +428,21 @@ __global__ void k_csr_fill(Table<K> t, const void* __restrict__ x, int typ, long
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         K k;
         if (!key_at<K>(x, typ, i, &k)) continue;
-        long long s = table_find<K>(t, k);
-        long long slot = s >= 0 ? s : (long long)(t.mask + 1);  // special slot stored last
+        long long row;
+        long long s = table_find<K>(t, k, &row);
+        long long slot = s >= 0 ? s : (long long)t.cap;  // special slot stored last
         unsigned p = atomicAdd(&fillc[slot], 1u);
         rows[start[slot] + p] = (unsigned)i;
+    }
+}
+template <typename K>
+__global__ void k_slot_counts(Table<K> t, const void* __restrict__ x, int typ, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        K k;
+        if (!key_at<K>(x, typ, i, &k)) continue;
+        long long row;
+        long long s = table_find<K>(t, k, &row);
+        if (s >= 0) atomicAdd(&t.cnt[s], 1u);
     }
 }
 __global__ void k_csr_sort(const unsigned long long* __restrict__ start, const unsigned* __restrict__ cnt,
@@ -360,9 +466,10 @@ __global__ void k_join_count(Table<K> t, const void* __restrict__ y, int ytyp, l
         K k;
         unsigned cc = 0, ss = 0;
         if (key_at<K>(y, ytyp, i, &k)) {
-            long long s = table_find<K>(t, k);
+            long long row;
+            long long s = table_find<K>(t, k, &row);
             if (s >= 0) { cc = t.cnt[s]; ss = (unsigned)s; }
-            else if (s == -2) { cc = t.special[1]; ss = (unsigned)(t.mask + 1); }
+            else if (s == -2) { cc = t.special[1]; ss = (unsigned)t.cap; }
         }
         c[i] = cc;
         slot[i] = ss;
@@ -377,13 +484,6 @@ __global__ void k_join_write(const unsigned* __restrict__ c, const unsigned* __r
         unsigned long long o = off[i], s0 = start[slot[i]];
         for (unsigned q = 0; q < cc; q++) { zb[o + q] = rows[s0 + q]; zp[o + q] = i; }
     }
-}
-__global__ void k_max_u32(const unsigned* __restrict__ a, long long n, unsigned* out) {
-    unsigned m = 0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        m = max(m, a[i]);
-    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (lane_id() == 0) atomicMax(out, m);
 }
 
 // Writes the two i64 index vectors of a join into z (a 2-element list).
@@ -402,7 +502,7 @@ static I join_outputs(V z, long long m, long long** zb, long long** zp) {
 // scratch, then move into exact-size outputs.
 template <typename K>
 static I join_probe_unique(V z, const Table<K>& t, const LinearBuild& lin, int mode, const void* py, I ytyp,
-                           long long ny) {
+                           long long ny, long long nbuild) {
     long long ntiles = (ny + JT_TILE - 1) / JT_TILE;
     long long* sb = (long long*)salloc((size_t)(ny > 0 ? ny : 1) * 8);
     long long* sp = (long long*)salloc((size_t)(ny > 0 ? ny : 1) * 8);
@@ -427,6 +527,8 @@ static I join_probe_unique(V z, const Table<K>& t, const LinearBuild& lin, int m
     }
     HG_CHECK(finish_out(&e[0], zb));
     HG_CHECK(finish_out(&e[1], zp));
+    register_bound(e[0].g, e[0].len, nbuild);
+    register_bound(e[1].g, e[1].len, ny);
     return 0;
 }
 
@@ -434,27 +536,23 @@ template <typename K>
 static I join_hash(V z, const void* px, I typ, long long nx, const void* py, long long ny) {
     Table<K> t;
     HG_CHECK(table_build<K>(&t, px, typ, nx, true));
-    unsigned long long nslots = t.mask + 2;  // + the special slot
-    unsigned* maxc = (unsigned*)salloc(16);
-    if (!maxc) return E_DEVICE_OOM;
-    HG_CU(cudaMemsetAsync(maxc, 0, 16, g_stream));
-    HG_LAUNCH("max_u32", grid_cap(t.mask + 1), 256, 0, k_max_u32, t.cnt, (long long)(t.mask + 1), maxc);
-    HG_LAUNCH("max_u32", 1, 32, 0, k_max_u32, t.special + 1, 1LL, maxc);
-    unsigned mx = 0;
-    HG_CU(cudaMemcpyAsync(&mx, maxc, 4, cudaMemcpyDeviceToHost, g_stream));
+    unsigned long long nslots = t.cap + 1;  // + the side slot of 64-bit keys
+    unsigned dup = 0;
+    HG_CU(cudaMemcpyAsync(&dup, t.flags, 4, cudaMemcpyDeviceToHost, g_stream));
     HG_CHECK(check_device_errors());
-    if (mx <= 1) {
+    if (!dup) {
         LinearBuild lin{};
-        return join_probe_unique<K>(z, t, lin, 0, py, typ, ny);
+        return join_probe_unique<K>(z, t, lin, 0, py, typ, ny, nx);
     }
+    if (nx > 0) HG_LAUNCH("slot_counts", grid_cap(nx), 256, 0, k_slot_counts<K>, t, px, (int)typ, nx);
     // duplicate build keys: CSR of build rows per slot (special slot last)
     unsigned* cnt_all = (unsigned*)salloc(nslots * 4);
     unsigned long long* start = (unsigned long long*)salloc(nslots * 8);
     unsigned* fillc = (unsigned*)salloc(nslots * 4);
     unsigned* rows = (unsigned*)salloc((size_t)(nx > 0 ? nx : 1) * 4);
     if (!cnt_all || !start || !fillc || !rows) return E_DEVICE_OOM;
-    HG_CU(cudaMemcpyAsync(cnt_all, t.cnt, (t.mask + 1) * 4, cudaMemcpyDeviceToDevice, g_stream));
-    HG_CU(cudaMemcpyAsync(cnt_all + t.mask + 1, t.special + 1, 4, cudaMemcpyDeviceToDevice, g_stream));
+    HG_CU(cudaMemcpyAsync(cnt_all, t.cnt, t.cap * 4, cudaMemcpyDeviceToDevice, g_stream));
+    HG_CU(cudaMemcpyAsync(cnt_all + t.cap, t.special + 1, 4, cudaMemcpyDeviceToDevice, g_stream));
     HG_CU(cudaMemsetAsync(fillc, 0, nslots * 4, g_stream));
     unsigned long long tot = 0;
     HG_CHECK(scan_exclusive(cnt_all, (long long)nslots, start, &tot));
@@ -479,6 +577,8 @@ static I join_hash(V z, const void* px, I typ, long long nx, const void* py, lon
     HG_CHECK(last_launch_error());
     HG_CHECK(finish_out(&e[0], wb));
     HG_CHECK(finish_out(&e[1], wp));
+    register_bound(e[0].g, e[0].len, nx);
+    register_bound(e[1].g, e[1].len, ny);
     return check_device_errors();
 }
 
@@ -533,9 +633,9 @@ static I join_single(V z, V x, V y, V f) {
     if (typ == H_I) {
         Table<unsigned> n32{};
         for (int i = 0; i < lin.n; i++) lin.k[i] = (long long)(unsigned)(int)lin.k[i];
-        return join_probe_unique<unsigned>(z, n32, lin, 1, py, typ, ny);
+        return join_probe_unique<unsigned>(z, n32, lin, 1, py, typ, ny, nx);
     }
-    return join_probe_unique<unsigned long long>(z, none, lin, 1, py, typ, ny);
+    return join_probe_unique<unsigned long long>(z, none, lin, 1, py, typ, ny, nx);
 }
 
 }  // namespace hg

@@ -109,10 +109,33 @@ __global__ void __launch_bounds__(256) k_seg_chunk(const T* __restrict__ src, co
     const long long base = s + (c - (long long)chunk0[lo]) * TILE_SUM;
     bool bad = false;
     A acc = ident;
-#pragma unroll 4
+    T v[16];
+    // all 16 loads of the lane are issued before the fixed-order accumulation
+    if constexpr (GATHER) {
+        long long r[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            long long j = base + k * 256 + threadIdx.x;
+            r[k] = j < e ? __ldg(rows + j) : 0;
+        }
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            long long j = base + k * 256 + threadIdx.x;
+            bool ok = r[k] >= 0 && r[k] < nx;
+            if (j < e && !ok) bad = true;
+            v[k] = (j < e && ok) ? src[r[k]] : T(0);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            long long j = base + k * 256 + threadIdx.x;
+            v[k] = j < e ? src[j] : T(0);
+        }
+    }
+#pragma unroll
     for (int k = 0; k < 16; k++) {
         long long j = base + k * 256 + threadIdx.x;
-        if (j < e) acc = sop<A, OP>(acc, (A)seg_elem<T, GATHER>(src, rows, nx, j, bad));
+        if (j < e) acc = sop<A, OP>(acc, (A)v[k]);
     }
     acc = swarp<A, OP>(acc);
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
@@ -156,34 +179,45 @@ static unsigned gcap(long long n, int per = 256) {
     return g > (unsigned)g_sms * 32 ? (unsigned)g_sms * 32 : g;
 }
 
-// Reduces every segment of (src via rows | src) into out[ng] (device).
+// Reduces every segment of (src via rows | src) into out[ng] (device).  When
+// `li` is given, the split of the long segments is computed once per list
+// and kept with it.
 template <typename T, typename A, int OP, bool GATHER>
 static I seg_reduce(const T* src, const long long* rows, long long nx, const long long* starts, long long ng,
-                    long long total, A ident, A* out) {
+                    long long total, A ident, A* out, ListInfo* li = nullptr) {
     if (ng == 0) return 0;
     HG_LAUNCH("seg_small", gcap(ng * 32), 256, 0, (k_seg_small<T, A, OP, GATHER>), src, rows, nx, starts, ng, total,
               ident, out, g_derr);
-    // long segments
-    uint8_t* f = (uint8_t*)salloc((size_t)ng);
-    long long* big = (long long*)salloc((size_t)ng * 8);
-    if (!f || !big) return E_DEVICE_OOM;
-    HG_LAUNCH("seg_flags", gcap(ng), 256, 0, k_big_flags, starts, ng, total, f, (unsigned*)nullptr);
     long long nbig = 0;
-    HG_CHECK(compact_rows(f, ng, big, &nbig));
-    if (nbig == 0) return last_launch_error();
-    unsigned* nch = (unsigned*)salloc((size_t)nbig * 4);
-    unsigned long long* c0 = (unsigned long long*)salloc((size_t)nbig * 8);
-    if (!nch || !c0) return E_DEVICE_OOM;
-    HG_LAUNCH("seg_chunks", gcap(nbig), 256, 0, k_big_chunks, starts, ng, total, big, nbig, nch);
     unsigned long long nchunks = 0;
-    HG_CHECK(scan_exclusive(nch, nbig, c0, &nchunks));
+    const long long *big, *pstarts;
+    const unsigned long long* c0;
+    if (li && li->planned) {
+        nbig = li->nbig; nchunks = li->nchunks; big = li->big; c0 = li->chunk0; pstarts = li->pstarts;
+    } else {
+        uint8_t* f = (uint8_t*)salloc((size_t)ng);
+        long long* bigs = (long long*)(li ? dalloc((size_t)ng * 8) : salloc((size_t)ng * 8));
+        if (!f || !bigs) return E_DEVICE_OOM;
+        HG_LAUNCH("seg_flags", gcap(ng), 256, 0, k_big_flags, starts, ng, total, f, (unsigned*)nullptr);
+        HG_CHECK(compact_rows(f, ng, bigs, &nbig));
+        unsigned* nch = (unsigned*)salloc((size_t)(nbig > 0 ? nbig : 1) * 4);
+        unsigned long long* c0s = (unsigned long long*)(li ? dalloc((size_t)(nbig > 0 ? nbig : 1) * 8) : salloc((size_t)(nbig > 0 ? nbig : 1) * 8));
+        long long* ps = (long long*)(li ? dalloc((size_t)(nbig > 0 ? nbig : 1) * 8) : salloc((size_t)(nbig > 0 ? nbig : 1) * 8));
+        if (!nch || !c0s || !ps) return E_DEVICE_OOM;
+        if (nbig > 0) {
+            HG_LAUNCH("seg_chunks", gcap(nbig), 256, 0, k_big_chunks, starts, ng, total, bigs, nbig, nch);
+            HG_CHECK(scan_exclusive(nch, nbig, c0s, &nchunks));
+            HG_LAUNCH("u64_to_i64", gcap(nbig), 256, 0, k_u64_to_i64, c0s, nbig, ps);
+        }
+        big = bigs; c0 = c0s; pstarts = ps;
+        if (li) { li->planned = 1; li->nbig = nbig; li->nchunks = nchunks; li->big = bigs; li->chunk0 = c0s; li->pstarts = ps; }
+    }
+    if (nbig == 0) return last_launch_error();
     A* part = (A*)salloc((size_t)nchunks * sizeof(A));
     A* res = (A*)salloc((size_t)nbig * sizeof(A));
-    long long* pstarts = (long long*)salloc((size_t)nbig * 8);
-    if (!part || !res || !pstarts) return E_DEVICE_OOM;
+    if (!part || !res) return E_DEVICE_OOM;
     HG_LAUNCH("seg_chunk", (unsigned)nchunks, 256, 0, (k_seg_chunk<T, A, OP, GATHER>), src, rows, nx, starts, ng,
               total, big, c0, nbig, ident, part, g_derr);
-    HG_LAUNCH("u64_to_i64", gcap(nbig), 256, 0, k_u64_to_i64, c0, nbig, pstarts);
     // partials of each long segment are reduced by the same procedure
     HG_CHECK((seg_reduce<A, A, OP, false>(part, nullptr, 0, pstarts, nbig, (long long)nchunks, ident, res)));
     HG_LAUNCH("scatter_big", gcap(nbig), 256, 0, k_scatter_big<A>, res, big, nbig, out);
@@ -225,7 +259,7 @@ __global__ void k_any_empty(const long long* __restrict__ starts, long long ng, 
 // Aggregates segments of x: result vector (device) of ng values, type in *typ.
 template <typename T, bool GATHER>
 static I agg_typed(int ag, I xt, const T* src, const long long* rows, long long nx, const long long* starts, long long ng,
-                   long long total, void** out, I* typ) {
+                   long long total, void** out, I* typ, ListInfo* li) {
     constexpr bool isF = std::is_same<T, float>::value, isE = std::is_same<T, double>::value;
     using SA = typename std::conditional<isF, float, typename std::conditional<isE, double, long long>::type>::type;
     if (ag == AG_LEN) {
@@ -238,7 +272,7 @@ static I agg_typed(int ag, I xt, const T* src, const long long* rows, long long 
     if (ag == AG_SUM || ag == AG_AVG) {
         SA* s = (SA*)salloc((size_t)(ng > 0 ? ng : 1) * sizeof(SA));
         if (!s) return E_DEVICE_OOM;
-        HG_CHECK((seg_reduce<T, SA, OP_SUM, GATHER>(src, rows, nx, starts, ng, total, (SA)0, s)));
+        HG_CHECK((seg_reduce<T, SA, OP_SUM, GATHER>(src, rows, nx, starts, ng, total, (SA)0, s, li)));
         if (ag == AG_SUM) {
             *typ = isF ? H_F : (isE ? H_E : H_L);
             *out = s;
@@ -256,15 +290,17 @@ static I agg_typed(int ag, I xt, const T* src, const long long* rows, long long 
     T identity;
     if (ag == AG_MIN) identity = std::numeric_limits<T>::has_infinity ? std::numeric_limits<T>::infinity() : std::numeric_limits<T>::max();
     else identity = std::numeric_limits<T>::has_infinity ? -std::numeric_limits<T>::infinity() : std::numeric_limits<T>::lowest();
-    if (ag == AG_MIN) HG_CHECK((seg_reduce<T, T, OP_MIN, GATHER>(src, rows, nx, starts, ng, total, identity, r)));
-    else HG_CHECK((seg_reduce<T, T, OP_MAX, GATHER>(src, rows, nx, starts, ng, total, identity, r)));
-    unsigned* fl = (unsigned*)salloc(16);
-    if (!fl) return E_DEVICE_OOM;
-    HG_CU(cudaMemsetAsync(fl, 0, 4, g_stream));
-    if (ng > 0) HG_LAUNCH("any_empty", gcap(ng), 256, 0, k_any_empty, starts, ng, total, fl);
+    if (ag == AG_MIN) HG_CHECK((seg_reduce<T, T, OP_MIN, GATHER>(src, rows, nx, starts, ng, total, identity, r, li)));
+    else HG_CHECK((seg_reduce<T, T, OP_MAX, GATHER>(src, rows, nx, starts, ng, total, identity, r, li)));
     unsigned h = 0;
-    HG_CU(cudaMemcpyAsync(&h, fl, 4, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    if (!(li && li->group_rows)) {  // @group never yields an empty group
+        unsigned* fl = (unsigned*)salloc(16);
+        if (!fl) return E_DEVICE_OOM;
+        HG_CU(cudaMemsetAsync(fl, 0, 4, g_stream));
+        if (ng > 0) HG_LAUNCH("any_empty", gcap(ng), 256, 0, k_any_empty, starts, ng, total, fl);
+        HG_CU(cudaMemcpyAsync(&h, fl, 4, cudaMemcpyDeviceToHost, g_stream));
+        HG_CU(cudaStreamSynchronize(g_stream));
+    }
     bool to_long = h && is_int(xt);
     *typ = to_long ? H_L : xt;
     *out = salloc((size_t)(ng > 0 ? ng : 1) * (to_long ? 8 : sizeof(T)));
@@ -275,15 +311,15 @@ static I agg_typed(int ag, I xt, const T* src, const long long* rows, long long 
 
 template <bool GATHER>
 static I agg_dispatch(int ag, I xt, const void* src, const long long* rows, long long nx, const long long* starts,
-                      long long ng, long long total, void** out, I* typ) {
+                      long long ng, long long total, void** out, I* typ, ListInfo* li) {
     switch (xt) {
-    case H_B: return agg_typed<bool, GATHER>(ag, xt, (const bool*)src, rows, nx, starts, ng, total, out, typ);
-    case H_J: return agg_typed<int8_t, GATHER>(ag, xt, (const int8_t*)src, rows, nx, starts, ng, total, out, typ);
-    case H_H: return agg_typed<int16_t, GATHER>(ag, xt, (const int16_t*)src, rows, nx, starts, ng, total, out, typ);
-    case H_I: return agg_typed<int32_t, GATHER>(ag, xt, (const int32_t*)src, rows, nx, starts, ng, total, out, typ);
-    case H_L: return agg_typed<long long, GATHER>(ag, xt, (const long long*)src, rows, nx, starts, ng, total, out, typ);
-    case H_F: return agg_typed<float, GATHER>(ag, xt, (const float*)src, rows, nx, starts, ng, total, out, typ);
-    case H_E: return agg_typed<double, GATHER>(ag, xt, (const double*)src, rows, nx, starts, ng, total, out, typ);
+    case H_B: return agg_typed<bool, GATHER>(ag, xt, (const bool*)src, rows, nx, starts, ng, total, out, typ, li);
+    case H_J: return agg_typed<int8_t, GATHER>(ag, xt, (const int8_t*)src, rows, nx, starts, ng, total, out, typ, li);
+    case H_H: return agg_typed<int16_t, GATHER>(ag, xt, (const int16_t*)src, rows, nx, starts, ng, total, out, typ, li);
+    case H_I: return agg_typed<int32_t, GATHER>(ag, xt, (const int32_t*)src, rows, nx, starts, ng, total, out, typ, li);
+    case H_L: return agg_typed<long long, GATHER>(ag, xt, (const long long*)src, rows, nx, starts, ng, total, out, typ, li);
+    case H_F: return agg_typed<float, GATHER>(ag, xt, (const float*)src, rows, nx, starts, ng, total, out, typ, li);
+    case H_E: return agg_typed<double, GATHER>(ag, xt, (const double*)src, rows, nx, starts, ng, total, out, typ, li);
     default: return E_DOMAIN;
     }
 }
@@ -314,13 +350,16 @@ __global__ void k_offsets_i64(const unsigned long long* __restrict__ a, long lon
 // library are found in the registry; any other list is read through its
 // nodes (copied to pinned memory first when the caller's node array is
 // pageable).  Payloads must be device-readable.
-static I list_segments(V y, I typ, const long long** starts, long long* total, const void** data) {
+static I list_segments(V y, I typ, const long long** starts, long long* total, const void** data,
+                       ListInfo** info = nullptr) {
     long long ng = y->len;
-    const ListInfo* li = find_list(host_nodes(y), ng);
+    ListInfo* li = find_list(host_nodes(y), ng);
+    if (info) *info = nullptr;
     if (li && li->kind == LIST_SEGMENTS && li->typ == typ) {
         *starts = li->starts;
         *total = li->total;
         *data = li->data;
+        if (info) *info = li;
         return 0;
     }
     const V0* nodes = host_nodes(y);
@@ -396,13 +435,14 @@ static I group_agg(V z, V x, V y, int ag) {
     const long long* starts;
     long long total;
     const void* rows;
-    HG_CHECK(list_segments(y, H_L, &starts, &total, &rows));
+    ListInfo* li;
+    HG_CHECK(list_segments(y, H_L, &starts, &total, &rows, &li));
     const void* px;
     HG_CHECK(in_ptr(x, &px));
     void* res;
     I typ;
-    HG_CHECK(agg_dispatch<true>(ag, x->typ, px, (const long long*)rows, x->len, starts, y->len, total, &res, &typ));
-    HG_CHECK(check_device_errors());
+    HG_CHECK(agg_dispatch<true>(ag, x->typ, px, (const long long*)rows, x->len, starts, y->len, total, &res, &typ, li));
+    if (!(li && li->group_rows && x->len >= total)) HG_CHECK(check_device_errors());  // rows of @group are in range
     void* dz;
     HG_CHECK(alloc_out(z, typ, y->len, &dz));
     if (y->len > 0) HG_CU(cudaMemcpyAsync(dz, res, (size_t)y->len * esize(typ), cudaMemcpyDeviceToDevice, g_stream));
@@ -451,7 +491,7 @@ I pfnEachRight(V z, V x, V y, I (*foo)(V, V, V)) {
             HG_LAUNCH("segment_nodes", gcap(ng), 256, 0, k_segment_nodes, data, keep, ng, total, es, x->typ, host_nodes(z));
             HG_CHECK(last_launch_error());
             HG_CHECK(sync());
-            register_list({host_nodes(z), ng, LIST_SEGMENTS, x->typ, keep, total, data});
+            register_list({host_nodes(z), ng, LIST_SEGMENTS, x->typ, keep, total, data, 0, 0, 0, 0, nullptr, nullptr, nullptr});
             return apply_residency(z);
         }
     }
@@ -483,7 +523,8 @@ I pfnEach(V z, V x, I (*foo)(V, V)) {
             HG_CHECK(list_segments(x, t, &starts, &total, &vals));
             void* res;
             I typ;
-            HG_CHECK(agg_dispatch<false>(ag, t, vals, nullptr, 0, starts, ng, total, &res, &typ));
+            ListInfo* lk = find_list(host_nodes(x), ng);
+            HG_CHECK(agg_dispatch<false>(ag, t, vals, nullptr, 0, starts, ng, total, &res, &typ, lk));
             int es = esize(typ);
             char* keep = (char*)dalloc((size_t)ng * es);
             if (!keep) return E_DEVICE_OOM;
@@ -492,7 +533,7 @@ I pfnEach(V z, V x, I (*foo)(V, V)) {
             HG_LAUNCH("scalar_nodes", gcap(ng), 256, 0, k_scalar_nodes, keep, ng, es, typ, host_nodes(z));
             HG_CHECK(last_launch_error());
             HG_CHECK(sync());
-            register_list({host_nodes(z), ng, LIST_SCALARS, typ, nullptr, ng, keep});
+            register_list({host_nodes(z), ng, LIST_SCALARS, typ, nullptr, ng, keep, 0, 0, 0, 0, nullptr, nullptr, nullptr});
             return apply_residency(z);
         }
     }

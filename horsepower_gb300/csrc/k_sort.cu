@@ -161,6 +161,21 @@ __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const K* __restrict__ k
     }
 }
 
+// keeps only the bits set in `mask`, packed to the bottom in order
+template <typename K>
+__global__ void k_squeeze(const K* __restrict__ k, long long n, unsigned long long mask, K* __restrict__ out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        unsigned long long v = (unsigned long long)k[i], r = 0, m = mask;
+        int o = 0;
+        while (m) {
+            int b = __ffsll((long long)m) - 1;
+            r |= ((v >> b) & 1ull) << o++;
+            m &= m - 1;
+        }
+        out[i] = (K)r;
+    }
+}
+
 __global__ void k_iota(unsigned* v, long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         v[i] = (unsigned)i;
@@ -200,6 +215,18 @@ I radix_sort(const K* keys, long long n, const K** kres, const unsigned** vres, 
     int lo = __builtin_ctzll(vary), hi = 64 - __builtin_clzll(vary);
     int bits = g_digit_bits;
     int npass = (hi - lo + bits - 1) / bits;
+    int nvar = __builtin_popcountll(vary);
+    if ((nvar + bits - 1) / bits < npass) {
+        // bits that never change inside the range: squeeze them out (order
+        // preserving, injective) and sort the shorter keys
+        K* sq = (K*)salloc((size_t)n * sizeof(K));
+        if (!sq) return E_DEVICE_OOM;
+        HG_LAUNCH("squeeze_keys", grid, 256, 0, k_squeeze<K>, keys, n, vary, sq);
+        keys = sq;
+        lo = 0;
+        hi = nvar;
+        npass = (nvar + bits - 1) / bits;
+    }
     if (npass > 8) { bits = 8; npass = (hi - lo + 7) / 8; }
     unsigned long long* hist = (unsigned long long*)salloc((size_t)npass * 256 * 8 * 2);
     if (!hist) return E_DEVICE_OOM;
@@ -666,8 +693,9 @@ static I group_dict(V z, const SortResult& r, long long n, const ColSet* cols) {
                   host_nodes(&kv[1]));
     HG_CHECK(last_launch_error());
     HG_CHECK(finish_out(&kv[0], dkeys));
+    register_bound(kv[0].g, kv[0].len, n);
     HG_CHECK(sync());  // the node array is written by the kernel
-    if (G > 0) register_list({host_nodes(&kv[1]), G, LIST_SEGMENTS, H_L, starts, n, perm});
+    if (G > 0) register_list({host_nodes(&kv[1]), G, LIST_SEGMENTS, H_L, starts, n, perm, 1, 0, 0, 0, nullptr, nullptr, nullptr});
     return apply_residency(z);
 }
 
@@ -676,6 +704,7 @@ static I order_output(V z, const SortResult& r, long long n, bool reverse) {
     HG_CHECK(alloc_out(z, H_L, n, &d));
     if (n > 0) HG_LAUNCH("widen", gcap(n), 256, 0, k_widen, r.perm, n, (long long*)d, reverse ? 1 : 0);
     HG_CHECK(last_launch_error());
+    register_bound(d, n, n);
     return finish_out(z, d);
 }
 

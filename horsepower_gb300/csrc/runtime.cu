@@ -307,10 +307,23 @@ void register_list(const ListInfo& g) {
     if (g_lists.size() > 256) g_lists.erase(g_lists.begin());
     g_lists.push_back(g);
 }
-const ListInfo* find_list(const V0* nodes, long long ng) {
+ListInfo* find_list(const V0* nodes, long long ng) {
     for (size_t i = g_lists.size(); i-- > 0;)
         if (g_lists[i].nodes == nodes && g_lists[i].ng == ng) return &g_lists[i];
     return nullptr;
+}
+
+struct Bound { const void* data; long long len, bound; };
+static std::vector<Bound> g_bounds;
+void register_bound(const void* data, long long len, long long bound) {
+    if (!data || len <= 1) return;
+    if (g_bounds.size() > 256) g_bounds.erase(g_bounds.begin());
+    g_bounds.push_back({data, len, bound});
+}
+bool known_in_range(const void* data, long long len, long long limit) {
+    for (size_t i = g_bounds.size(); i-- > 0;)
+        if (g_bounds[i].data == data && g_bounds[i].len == len) return g_bounds[i].bound <= limit;
+    return false;
 }
 
 // ------------------------------------------------------------ device errors
@@ -417,6 +430,7 @@ L setHeapOffset(L cur) {
     g_out->rewind(g_marks[(size_t)cur].first);
     g_host->rewind(g_marks[(size_t)cur].second);
     g_lists.clear();  // their node arrays and payloads are released
+    g_bounds.clear();
     g_marks.resize((size_t)cur + 1);
     return cur;
 }
