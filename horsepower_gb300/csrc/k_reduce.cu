@@ -239,3 +239,67 @@ I pfnLen(V z, V x) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free f64 sum.
+//
+// Some callers cannot allocate device memory at the point where they need a
+// sum: code running while a CUDA graph is being captured (cudaMalloc is not
+// allowed there), callers with a fixed, pre-reserved memory budget, and
+// latency-critical paths that cannot afford the device-wide synchronisation
+// an allocation may cause.  hgpuSumF64Static serves them: it computes the same
+// fixed-order tile-tree sum as pfnSum on f64 data, but keeps the tile
+// partials in the file-scope array below instead of the scratch arena, and
+// touches no arena, no cudaMalloc/cudaFree and no allocating library call.
+//
+// Limits and sharing:
+//   * n <= HGPU_STATIC_SUM_MAX_ROWS (65,536 tiles of 4,096 = 268,435,456);
+//     larger n is rejected with E_LENGTH.
+//   * The array (about 512 KiB) is held by every GPU that loads the library
+//     until the process exits.
+//   * Every call shares the array.  Each call overwrites every partial it
+//     reads, so nothing needs clearing, but calls whose kernels overlap on the
+//     GPU (different streams, or different host threads) race on it: issue
+//     them on one stream or serialise them.
+//   * The first call on a device looks up the array's device address with
+//     cudaGetSymbolAddress (the host-side name is only a stand-in).  Make
+//     that first call before any stream capture begins.
+// ---------------------------------------------------------------------------
+#define HGPU_STATIC_SUM_MAX_TILES 65536LL
+#define HGPU_STATIC_SUM_MAX_ROWS (HGPU_STATIC_SUM_MAX_TILES * 4096LL)
+static __device__ __align__(256) double g_static_sum_partials[HGPU_STATIC_SUM_MAX_TILES + 64];
+
+namespace hg {
+static void* g_static_sum_ptr[64];  // device address of the array, per device
+}
+
+extern "C" I hgpuSumF64Static(const double* x, L n, double* result, void* stream) {
+    using namespace hg;
+    if (n < 0 || n > HGPU_STATIC_SUM_MAX_ROWS)
+        return set_error(E_LENGTH, "hgpuSumF64Static: n = %lld is outside [0, %lld]", n, HGPU_STATIC_SUM_MAX_ROWS);
+    int dev = 0;
+    HG_CU(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_error(E_DEVICE, "hgpuSumF64Static: device %d out of range", dev);
+    if (!g_static_sum_ptr[dev]) HG_CU(cudaGetSymbolAddress(&g_static_sum_ptr[dev], g_static_sum_partials));
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n == 0) {
+        HG_CU(cudaMemsetAsync(result, 0, sizeof(double), s));
+        return 0;
+    }
+    double* level0 = (double*)g_static_sum_ptr[dev];                  // up to 65,536 tile partials
+    double* level1 = level0 + HGPU_STATIC_SUM_MAX_TILES;              // up to 16 partials of those
+    long long tiles = (n + TILE_SUM - 1) / TILE_SUM;
+    k_tile_reduce<double, double, RED_SUM><<<(unsigned)tiles, 256, 0, s>>>(x, n, tiles == 1 ? result : level0, 0.0);
+    long long m = tiles;
+    double* cur = level0;
+    while (m > 1) {
+        long long t2 = (m + TILE_SUM - 1) / TILE_SUM;
+        double* nxt = (cur == level0) ? level1 : level0;
+        k_tile_reduce<double, double, RED_SUM><<<(unsigned)t2, 256, 0, s>>>(cur, m, t2 == 1 ? result : nxt, 0.0);
+        cur = nxt;
+        m = t2;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "hgpuSumF64Static launch", __FILE__, __LINE__);
+    return 0;
+}

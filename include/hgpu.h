@@ -230,6 +230,19 @@ L    hgpuLaunchCount(void);           /* kernels launched by this library since 
 I    hgpuTimerStart(void);
 double hgpuTimerStop(void);
 
+/* Allocation-free f64 sum (no counterpart in the reference).  For callers that
+ * cannot allocate device memory where they need a sum: code running during a
+ * CUDA stream capture, under a fixed pre-reserved memory budget, or on a path
+ * that cannot take the synchronisation an allocation may cause.  Same
+ * fixed-order tile-tree result as pfnSum on f64 data.  x and result are
+ * device pointers the caller owns; the tile partials live in a static device
+ * array (~512 KiB, held by every GPU that loads the library), so the call
+ * makes no cudaMalloc/cudaFree and uses no arena.  n is limited to
+ * 268,435,456 (E_LENGTH beyond).  Calls share the array: calls overlapping
+ * on the GPU race, so issue them on one stream.  The first call on a device
+ * looks up the array's address; make it before any stream capture. */
+I    hgpuSumF64Static(const double *x, L n, double *result, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
