@@ -250,6 +250,74 @@ def run_gb300(args, rank, ws, dist):
     return out
 
 
+def run_batched(args):
+    """256 independent join + group-by plans over device-resident synthetic
+    tables (fact rows log-uniform in [1e4, 2e7], dim = fact / 4, seed
+    3000 + p): hgpuBatchJoinGroup against the same plans one at a time
+    through the builtins.  Returns the JSON line."""
+    import horsepower_gb300
+    from horsepower_gb300 import batch as B
+    gpu = horsepower_gb300.load()
+    Lb = gpu.lib
+    Lb.hgpuTimerStop.restype = C.c_double
+    Lb.hgpuLaunchCount.restype = C.c_longlong
+    Lb.getHeapOffset.restype = C.c_longlong
+    Lb.setHeapOffset.argtypes = [C.c_longlong]
+    sizes = B.log_uniform_sizes(args.plans, 10_000, args.max_fact, seed=3000)
+    tabs = [B.synth_tables(gpu, 3000 + p, int(n), max(1, int(n) // 4)) for p, n in enumerate(sizes)]
+    plans = [B.make_plan(d, f) for d, f in tabs]
+    total_rows = int(sizes.sum())
+
+    def batched():
+        mark = Lb.getHeapOffset()
+        r = B.run_batch(gpu, plans)
+        Lb.setHeapOffset(mark)
+        return r
+
+    def one_at_a_time():
+        out = []
+        for d, f in tabs:
+            mark = Lb.getHeapOffset()
+            r = P.join_group(gpu, d, f)
+            out.append([gpu.to_py(v) for v in r])
+            Lb.setHeapOffset(mark)
+        return out
+
+    for _ in range(args.warmup):
+        got = batched()
+    ref = one_at_a_time()
+    exact = all(np.array_equal(g[k], np.asarray(w[k]).astype(g[k].dtype)) for g, w in zip(got, ref) for k in range(6))
+    clocks = Clocks()
+    Lb.hgpuSync()
+    l0 = Lb.hgpuLaunchCount()
+    clocks.start()
+    Lb.hgpuTimerStart()
+    for _ in range(args.steps):
+        batched()
+    ms_b = Lb.hgpuTimerStop() / args.steps
+    clk = clocks.stop()
+    launches = (Lb.hgpuLaunchCount() - l0) // args.steps
+    Lb.hgpuSync()
+    t_plain = []
+    for _ in range(max(1, min(args.steps, 3))):
+        Lb.hgpuTimerStart()
+        one_at_a_time()
+        t_plain.append(Lb.hgpuTimerStop())
+    ms_p = statistics.median(t_plain)
+    n = len(plans)
+    return {
+        "metric": "batched join + group-by plans: queries/s", "value": n / (ms_b / 1000), "unit": "queries/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_b, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64", "data": "synthetic (seeded, on device)",
+        "config": {"workload": f"{n} join + group-by plans, fact rows log-uniform [1e4, {args.max_fact:.0e}], "
+                               f"dim = fact/4, {total_rows:,} fact rows in all", "l2": "inputs larger than L2"},
+        "plain_one_at_a_time": {"value": n / (ms_p / 1000), "unit": "queries/s", "ms": ms_p},
+        "speedup_vs_plain": ms_p / ms_b, "bit_exact_vs_plain": bool(exact),
+        "fact_rows_per_s": total_rows / (ms_b / 1000),
+        "gpu_launches": int(launches), "clocks": clk,
+    }
+
+
 def cpu_sample(args):
     """The oracle port on a bounded sample of the workload (fact and dim scaled by 1/10)."""
     ora = Builtins(os.path.join(ROOT, "oracle", "_build", "liboracle.so"), "oracle")
@@ -278,8 +346,16 @@ def main():
     ap.add_argument("--dim", type=int, default=15_000_000)
     ap.add_argument("--cpu-scale", type=int, default=10)
     ap.add_argument("--cpu-reps", type=int, default=3)
+    ap.add_argument("--workload", default="join_group", choices=["join_group", "batched"])
+    ap.add_argument("--plans", type=int, default=256)
+    ap.add_argument("--max-fact", type=int, default=20_000_000)
     args = ap.parse_args()
     rank, ws, dist = dist_init(args.gpus)
+    if args.workload == "batched" and args.impl == "gb300":
+        line = run_batched(args)
+        if rank == 0:
+            print(json.dumps(line))
+        return
 
     if args.impl == "reference":
         os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))

@@ -1,0 +1,669 @@
+// Batched filter-join-aggregate plans (many independent queries, one set of
+// launches).
+//
+// Each plan is the join + group-by query the interpreter runs as
+//   d = (dim.date >= lo) & (dim.date < hi); pk2 = compress(d, dim.pk)
+//   j = join_index(eq, pk2, fact.fk); fi = j[1]
+//   flag' status' qty' price' disc' = index(fact.col, fi)
+//   g = group(list(flag', status'))                      (pfnGroupTrie)
+//   sum(qty'), avg(price'), sum(disc'), count per group  (hgpuGroup*)
+// and hgpuBatchJoinGroup runs every stage for all plans in one launch:
+// tiles never straddle two plans, and each plan's look-back stops at its
+// first tile, so every plan sees exactly the computation the plain builtins
+// perform on it alone: the matched fact rows in row order, the groups'
+// stable order by (flag<<8 | status), and per group the same fixed-order
+// tile-tree sums (the same seg_sum kernels).  Results are therefore
+// bit-identical to running the plans one at a time through the builtins.
+//
+// The batched kernels cover plans with unique dimension keys whose range is
+// at most 64x the dimension (direct presence bitmaps), a compressed key
+// column no longer than the fact table, and at most 256 groups.  Any other
+// plan of the batch runs through the builtins one call at a time
+// (plan_through_builtins), so every result is still the builtins' own.
+#include <algorithm>
+#include <climits>
+#include <cstring>
+#include <vector>
+
+#include "dev_common.cuh"
+
+namespace hg {
+
+I scan_exclusive(const unsigned* in, long long n, unsigned long long* out, unsigned long long* total_h);
+I seg_sum_f64(const double* src, const long long* rows, long long nx, const long long* starts, long long ng,
+              long long total, double* out);
+
+constexpr int BT = 4096;  // rows per tile
+
+struct DPlan {
+    const int* pk;
+    const int* date;
+    long long nd;
+    const int* fk;
+    const int8_t* flag;
+    const int8_t* status;
+    const double* qty;
+    const double* price;
+    const double* disc;
+    long long nf;
+    int lo, hi;
+    long long kmin, kmax;      // pk range
+    unsigned* bitmap;          // pk presence, bit (pk - kmin)
+    long long fact_off;        // fact-row offset of the plan's region in the fi buffer
+    unsigned* codebits;        // 65536-bit presence of group codes
+    unsigned short* dense;     // code -> dense group id (65536 entries)
+};
+
+// plan of a tile: tile_first[p] = first tile of plan p, tile_first[np] = total tiles
+__device__ __forceinline__ int plan_of_tile(const long long* tile_first, int np, long long t) {
+    int lo = 0, hi = np - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (tile_first[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// decoupled look-back restricted to the tiles [first, t) of one plan
+__device__ __forceinline__ unsigned long long lookback_seg(unsigned long long* status, long long t, long long first,
+                                                          unsigned long long agg, unsigned* derr) {
+    const unsigned lane = lane_id();
+    if (t == first) {
+        if (lane == 0) st_release(&status[t], LB_INC | agg);
+        return 0;
+    }
+    if (lane == 0) st_release(&status[t], LB_AGG | agg);
+    unsigned long long excl = 0;
+    long long base = t - 1, spins = 0;
+    for (;;) {
+        long long j = base - (long long)lane;
+        unsigned long long s = (j >= first) ? ld_acquire(&status[j]) : LB_INC;
+        unsigned flag = (unsigned)(s >> 62);
+        unsigned inc = __ballot_sync(0xffffffffu, flag == 2);
+        unsigned notready = __ballot_sync(0xffffffffu, flag == 0);
+        int stop = inc ? __ffs(inc) - 1 : 31;
+        unsigned upto = stop == 31 ? 0xffffffffu : ((1u << (stop + 1)) - 1u);
+        if (notready & upto) {
+            if (++spins > SPIN_LIMIT) { if (lane == 0) flag_error(derr, DERR_TIMEOUT); break; }
+            continue;
+        }
+        unsigned long long v = ((int)lane <= stop && j >= first) ? (s & LB_MASK) : 0;
+        excl += warp_sum(v);
+        if (inc) break;
+        base -= 32;
+    }
+    if (lane == 0) st_release(&status[t], LB_INC | (excl + agg));
+    return excl;
+}
+
+// ---------------------------------------------------------------- stage 0/1
+__global__ void k_b_minmax(const DPlan* __restrict__ P, const long long* __restrict__ tile_first, int np,
+                           long long* __restrict__ mm) {
+    const long long t = blockIdx.x;
+    const int p = plan_of_tile(tile_first, np, t);
+    const long long r0 = (t - tile_first[p]) * BT;
+    long long a = LLONG_MAX, b = LLONG_MIN;
+    for (long long i = r0 + threadIdx.x; i < r0 + BT && i < P[p].nd; i += blockDim.x) {
+        long long v = P[p].pk[i];
+        a = v < a ? v : a;
+        b = v > b ? v : b;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        long long q = __shfl_xor_sync(0xffffffffu, a, o); a = q < a ? q : a;
+        long long r = __shfl_xor_sync(0xffffffffu, b, o); b = r > b ? r : b;
+    }
+    if (lane_id() == 0) { atomicMin(&mm[2 * p], a); atomicMax(&mm[2 * p + 1], b); }
+}
+
+// dimension rows inside the date window set their key's presence bit; nsel
+// counts them (the length of the compressed key column)
+__global__ void k_b_build(const DPlan* __restrict__ P, const long long* __restrict__ tile_first, int np,
+                          unsigned* __restrict__ dup, unsigned long long* __restrict__ nsel) {
+    const long long t = blockIdx.x;
+    const int p = plan_of_tile(tile_first, np, t);
+    const DPlan& q = P[p];
+    const long long r0 = (t - tile_first[p]) * BT;
+    unsigned cnt = 0;
+    for (long long i = r0 + threadIdx.x; i < r0 + BT && i < q.nd; i += blockDim.x) {
+        int d = q.date[i];
+        long long b = (long long)q.pk[i] - q.kmin;
+        if (d >= q.lo && d < q.hi && b >= 0 && b <= q.kmax - q.kmin) {
+            unsigned bit = 1u << (b & 31);
+            unsigned old = atomicOr(&q.bitmap[b >> 5], bit);
+            if (old & bit) atomicOr(&dup[p], 1u);
+            cnt++;
+        }
+    }
+    cnt = warp_sum(cnt);
+    if (lane_id() == 0 && cnt) atomicAdd(&nsel[p], (unsigned long long)cnt);
+}
+
+// ---------------------------------------------------------------- stage 2
+// probe: matched fact rows of each plan, compacted in row order
+__global__ void __launch_bounds__(256) k_b_probe(const DPlan* __restrict__ P, const long long* __restrict__ tile_first,
+                                                 int np, unsigned* __restrict__ fi, unsigned long long* status,
+                                                 unsigned* ticket, unsigned long long* __restrict__ mcount,
+                                                 unsigned* derr) {
+    __shared__ unsigned warp_tot[8];
+    __shared__ unsigned long long tile_off;
+    __shared__ long long tile_id;
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) tile_id = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const long long t = tile_id;
+    const int p = plan_of_tile(tile_first, np, t);
+    const DPlan& q = P[p];
+    const long long first = tile_first[p];
+    const long long base = (t - first) * BT + (long long)warp * 512;
+    unsigned hits = 0;  // bit k: round k matched
+    unsigned cnt = 0;
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        long long i = base + k * 32 + lane;
+        bool m = false;
+        if (i < q.nf) {
+            long long v = (long long)__ldcs(q.fk + i);
+            if (v >= q.kmin && v <= q.kmax) {
+                long long b = v - q.kmin;
+                m = (__ldg(q.bitmap + (b >> 5)) >> (b & 31)) & 1u;
+            }
+        }
+        hits |= (unsigned)m << k;
+        cnt += __popc(__ballot_sync(0xffffffffu, m));
+    }
+    if (lane == 0) warp_tot[warp] = cnt;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned v = lane < 8 ? warp_tot[lane] : 0;
+        unsigned agg = warp_sum(v);
+        unsigned long long excl = lookback_seg(status, t, first, agg, derr);
+        if (lane == 0) {
+            tile_off = excl;
+            if ((t - first + 1) * BT >= q.nf) mcount[p] = excl + agg;  // the plan's last tile
+        }
+    }
+    __syncthreads();
+    unsigned long long off = tile_off;
+    for (unsigned w = 0; w < warp; w++) off += warp_tot[w];
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        bool sel = (hits >> k) & 1u;
+        unsigned bal = __ballot_sync(0xffffffffu, sel);
+        if (sel) fi[q.fact_off + off + __popc(bal & lanemask_lt())] = (unsigned)(base + k * 32 + lane);
+        off += __popc(bal);
+    }
+}
+
+// exclusive prefix of the per-plan match counts (one block)
+__global__ void k_b_offsets(const unsigned long long* __restrict__ mcount, int np, long long* __restrict__ moff) {
+    if (threadIdx.x == 0) {
+        long long acc = 0;
+        for (int p = 0; p < np; p++) { moff[p] = acc; acc += (long long)mcount[p]; }
+        moff[np] = acc;
+    }
+}
+
+// ---------------------------------------------------------------- stage 3
+// gather the matched rows' columns into contiguous per-plan vectors, and
+// record which group codes occur
+__global__ void k_b_gather(const DPlan* __restrict__ P, const long long* __restrict__ tile_first, int np,
+                           const unsigned* __restrict__ fi, const unsigned long long* __restrict__ mcount,
+                           const long long* __restrict__ moff, unsigned* __restrict__ code, double* __restrict__ qty,
+                           double* __restrict__ price, double* __restrict__ disc) {
+    const long long t = blockIdx.x;
+    const int p = plan_of_tile(tile_first, np, t);
+    const DPlan& q = P[p];
+    const long long r0 = (t - tile_first[p]) * BT;
+    const long long m = (long long)mcount[p], o = moff[p];
+    for (long long i = r0 + threadIdx.x; i < r0 + BT && i < m; i += blockDim.x) {
+        unsigned r = fi[q.fact_off + i];
+        unsigned c = ((unsigned)(uint8_t)q.flag[r] << 8) | (unsigned)(uint8_t)q.status[r];
+        code[o + i] = c;
+        qty[o + i] = q.qty[r];
+        price[o + i] = q.price[r];
+        disc[o + i] = q.disc[r];
+        unsigned peers = __match_any_sync(__activemask(), c);
+        if ((int)lane_id() == __ffs(peers) - 1) atomicOr(&q.codebits[c >> 5], 1u << (c & 31));
+    }
+}
+
+// code -> dense group id (ascending codes), one block per plan
+__global__ void k_b_dense(const DPlan* __restrict__ P, unsigned* __restrict__ ngroups, unsigned* __restrict__ codes) {
+    const int p = blockIdx.x;
+    const DPlan& q = P[p];
+    __shared__ unsigned wsum[8];
+    // 2048 words, 8 per thread
+    unsigned c[8], tot = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) { c[k] = __popc(q.codebits[threadIdx.x * 8 + k]); tot += c[k]; }
+    unsigned inc = warp_incl_scan(tot);
+    if (lane_id() == 31) wsum[threadIdx.x >> 5] = inc;
+    __syncthreads();
+    unsigned before = 0;
+    for (unsigned w = 0; w < (threadIdx.x >> 5); w++) before += wsum[w];
+    unsigned id = before + inc - tot;
+    for (int k = 0; k < 8; k++) {
+        unsigned word = q.codebits[threadIdx.x * 8 + k];
+        for (int b = 0; b < 32; b++) {
+            unsigned cd = (threadIdx.x * 8 + k) * 32 + b;
+            if ((word >> b) & 1u) {
+                if (id < 256) codes[p * 256 + id] = cd;
+                q.dense[cd] = (unsigned short)id++;
+            }
+        }
+    }
+    if (threadIdx.x == 255) ngroups[p] = id;
+}
+
+// ---------------------------------------------------------------- stage 4
+// per-plan histograms of the dense group ids
+__global__ void k_b_hist(const DPlan* __restrict__ P, const long long* __restrict__ tile_first, int np,
+                         const unsigned long long* __restrict__ mcount, const long long* __restrict__ moff,
+                         const unsigned* __restrict__ code, unsigned* __restrict__ hist) {
+    __shared__ unsigned h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const long long t = blockIdx.x;
+    const int p = plan_of_tile(tile_first, np, t);
+    const long long r0 = (t - tile_first[p]) * BT, m = (long long)mcount[p], o = moff[p];
+    for (long long i = r0 + threadIdx.x; i < r0 + BT && i < m; i += blockDim.x)
+        atomicAdd(&h[P[p].dense[code[o + i]] & 255], 1u);
+    __syncthreads();
+    if (h[threadIdx.x]) atomicAdd(&hist[p * 256 + threadIdx.x], h[threadIdx.x]);
+}
+
+__global__ void k_b_bucket(const unsigned* __restrict__ hist, unsigned* __restrict__ bucket) {
+    __shared__ unsigned s[256];
+    const int p = blockIdx.x, d = threadIdx.x;
+    s[d] = hist[p * 256 + d];
+    __syncthreads();
+    if (d == 0) {
+        unsigned acc = 0;
+        for (int i = 0; i < 256; i++) { unsigned v = s[i]; s[i] = acc; acc += v; }
+    }
+    __syncthreads();
+    bucket[p * 256 + d] = s[d];
+}
+
+// one stable counting pass over the dense ids of each plan (the onesweep rank
+// and per-digit look-back, restricted to the plan's tiles); writes, in group
+// order, the global positions of the matched rows
+__global__ void __launch_bounds__(256) k_b_sort(const DPlan* __restrict__ P, const long long* __restrict__ tile_first,
+                                                int np, const unsigned long long* __restrict__ mcount,
+                                                const long long* __restrict__ moff, const unsigned* __restrict__ code,
+                                                const unsigned* __restrict__ bucket, long long* __restrict__ rows,
+                                                unsigned long long* status, unsigned* ticket, unsigned* derr) {
+    __shared__ unsigned whist[8][256];
+    __shared__ unsigned long long dbase[256];
+    __shared__ long long tile_id;
+    for (int i = threadIdx.x; i < 8 * 256; i += 256) (&whist[0][0])[i] = 0;
+    if (threadIdx.x == 0) tile_id = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const long long t = tile_id;
+    const int p = plan_of_tile(tile_first, np, t);
+    const long long first = tile_first[p], m = (long long)mcount[p], o = moff[p];
+    const unsigned lane = lane_id(), w = threadIdx.x >> 5;
+    const long long wbase = (t - first) * BT + (long long)w * 512;
+    unsigned rd[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        long long i = wbase + k * 32 + lane;
+        bool valid = i < m;
+        unsigned d = valid ? (P[p].dense[code[o + i]] & 255u) : 0xffffffffu;
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        int leader = __ffs(peers) - 1;
+        unsigned pre = 0;
+        if ((int)lane == leader && valid) { pre = whist[w][d]; whist[w][d] = pre + __popc(peers); }
+        pre = __shfl_sync(0xffffffffu, pre, leader);
+        rd[k] = ((d & 0xffffu) << 16) | (pre + __popc(peers & lanemask_lt()));
+        __syncwarp();
+    }
+    __syncthreads();
+    {
+        const int d = threadIdx.x;
+        unsigned c = 0;
+        for (int ww = 0; ww < 8; ww++) { unsigned h = whist[ww][d]; whist[ww][d] = c; c += h; }
+        unsigned long long* st = status + (size_t)t * 256 + d;
+        unsigned long long excl = 0;
+        if (t == first) st_release(st, LB_INC | c);
+        else {
+            st_release(st, LB_AGG | c);
+            long long j = t - 1, spins = 0;
+            while (j >= first) {
+                unsigned long long s = ld_acquire(status + (size_t)j * 256 + d);
+                unsigned long long f = s >> 62;
+                if (f == 0) {
+                    if (++spins > SPIN_LIMIT) { flag_error(derr, DERR_TIMEOUT); break; }
+                    continue;
+                }
+                excl += s & LB_MASK;
+                if (f == 2) break;
+                j--;
+            }
+            st_release(st, LB_INC | (excl + c));
+        }
+        dbase[d] = (unsigned long long)o + bucket[p * 256 + d] + excl;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        long long i = wbase + k * 32 + lane;
+        if (i < m) {
+            unsigned d = rd[k] >> 16;
+            rows[dbase[d] + whist[w][d] + (rd[k] & 0xffffu)] = o + i;
+        }
+    }
+}
+
+// group starts of every plan, concatenated
+__global__ void k_b_starts(const long long* __restrict__ moff, const unsigned* __restrict__ bucket,
+                           const unsigned* __restrict__ ngroups, const long long* __restrict__ segoff, int np,
+                           long long* __restrict__ starts) {
+    const int p = blockIdx.x, g = threadIdx.x;
+    if (g < (int)ngroups[p]) starts[segoff[p] + g] = moff[p] + bucket[p * 256 + g];
+}
+
+// avg = sum / count per group (k_avg_seg's division)
+__global__ void k_b_avg(const double* __restrict__ s, const long long* __restrict__ starts, long long ng, long long total,
+                        double* __restrict__ avg) {
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x) {
+        long long m = ((g + 1 < ng) ? starts[g + 1] : total) - starts[g];
+        avg[g] = __ddiv_rn(s[g], (double)m);
+    }
+}
+
+static unsigned cap_grid(long long n) {
+    unsigned g = grid_for(n, 256);
+    return g > (unsigned)g_sms * 16 ? (unsigned)g_sms * 16 : g;
+}
+
+static V0 dev_col(const void* p, I typ, L n) {
+    V0 v;
+    memset(&v, 0, sizeof v);
+    v.len = n;
+    v.typ = typ;
+    v.g = (G)p;
+    return v;
+}
+
+static V0 int_scalar(I x) {
+    V0 v;
+    memset(&v, 0, sizeof v);
+    v.len = 1;
+    v.typ = H_I;
+    v.i32 = x;
+    v.g = (G)&v.b;
+    return v;
+}
+
+// One plan through the builtins, call by call, exactly as the interpreter
+// runs it.  Plans the batched kernels do not cover take this path, so every
+// plan of a batch gets the builtins' own result.
+static I plan_through_builtins(const hgpuJoinGroupPlan& q, hgpuJoinGroupResult* r) {
+    const L mark = getHeapOffset();
+    I rc = 0;
+    V0 pk = dev_col(q.dim_pk, H_I, q.ndim), date = dev_col(q.dim_date, H_I, q.ndim);
+    V0 fk = dev_col(q.fk, H_I, q.nfact), flag = dev_col(q.flag, H_C, q.nfact), status = dev_col(q.status, H_C, q.nfact);
+    V0 qty = dev_col(q.qty, H_E, q.nfact), price = dev_col(q.price, H_E, q.nfact), disc = dev_col(q.disc, H_E, q.nfact);
+    V0 lo = int_scalar(q.lo), hi = int_scalar(q.hi), one;
+    memset(&one, 0, sizeof one);
+    one.len = 1; one.typ = H_L; one.i64 = 1; one.g = (G)&one.b;
+    V0 eq;
+    memset(&eq, 0, sizeof eq);
+    eq.len = 1; eq.typ = H_Q; eq.q = getSymbol((S) "eq"); eq.g = (G)&eq.b;
+    V0 d1, d2, d3, pk2, j, fi, gf, gs, gq, gp, gd, lst, g, keys, vals, of, os, sq, ap, sd, cnt;
+    V0* ln;
+#define STEP(call) do { if ((rc = (call)) != 0) goto done; } while (0)
+    STEP(pfnGeq(&d1, &date, &lo));
+    STEP(pfnLt(&d2, &date, &hi));
+    STEP(pfnAnd(&d3, &d1, &d2));
+    STEP(pfnCompress(&pk2, &d3, &pk));
+    STEP(pfnJoinIndex(&j, &pk2, &fk, &eq));
+    STEP(pfnIndex(&fi, &j, &one));
+    STEP(pfnIndex(&gf, &flag, &fi));
+    STEP(pfnIndex(&gs, &status, &fi));
+    STEP(pfnIndex(&gq, &qty, &fi));
+    STEP(pfnIndex(&gp, &price, &fi));
+    STEP(pfnIndex(&gd, &disc, &fi));
+    STEP(init_list(&lst, H_G, 2));
+    ln = host_nodes(&lst);
+    ln[0] = gf; ln[1] = gs;
+    if (gf.len == 1) ln[0].g = (G)&ln[0].b;
+    if (gs.len == 1) ln[1].g = (G)&ln[1].b;
+    STEP(pfnGroup(&g, &lst));
+    STEP(pfnKeys(&keys, &g));
+    STEP(pfnValues(&vals, &g));
+    if (keys.len > HGPU_PLAN_MAX_GROUPS) { rc = set_error(E_NOT_IMPL, "more than 256 groups"); goto done; }
+    STEP(pfnIndex(&of, &gf, &keys));
+    STEP(pfnIndex(&os, &gs, &keys));
+    STEP(hgpuGroupSum(&sq, &gq, &vals));
+    STEP(hgpuGroupAvg(&ap, &gp, &vals));
+    STEP(hgpuGroupSum(&sd, &gd, &vals));
+    STEP(hgpuGroupLen(&cnt, &gq, &vals));
+    {
+        const L n = keys.len;
+        r->ngroups = n;
+        V0* src[6] = {&of, &os, &sq, &ap, &sd, &cnt};
+        void* dst[6] = {r->flag, r->st, r->sum_qty, r->avg_price, r->sum_disc, r->count};
+        const size_t es[6] = {1, 1, 8, 8, 8, 8};
+        for (int k = 0; k < 6 && n > 0; k++) {
+            if (n == 1 || !is_device_ptr(src[k]->g)) memcpy(dst[k], src[k]->g, es[k] * n);
+            else if (cudaMemcpyAsync(dst[k], src[k]->g, es[k] * n, cudaMemcpyDeviceToHost, g_stream) != cudaSuccess) {
+                rc = set_error(E_DEVICE, "copying a plan result");
+                goto done;
+            }
+        }
+        if (cudaStreamSynchronize(g_stream) != cudaSuccess) rc = set_error(E_DEVICE, "copying a plan result");
+    }
+#undef STEP
+done:
+    setHeapOffset(mark);
+    return rc;
+}
+
+}  // namespace hg
+
+using namespace hg;
+
+extern "C" I hgpuBatchJoinGroup(const hgpuJoinGroupPlan* plans, L nplans, hgpuJoinGroupResult* out) {
+    HG_CHECK(ensure_init());
+    ScratchScope ss;
+    const int np = (int)nplans;
+    if (np <= 0) return 0;
+    std::vector<DPlan> hp(np);
+    std::vector<long long> dtiles(np + 1), ftiles(np + 1);
+    dtiles[0] = ftiles[0] = 0;
+    long long fact_total = 0;
+    for (int p = 0; p < np; p++) {
+        const hgpuJoinGroupPlan& q = plans[p];
+        const void* ptrs[] = {q.dim_pk, q.dim_date, q.fk, q.flag, q.status, q.qty, q.price, q.disc};
+        for (const void* v : ptrs)
+            if (!is_device_ptr(v)) return set_error(E_DOMAIN, "batched plan %d: columns must be device or pinned memory", p);
+        DPlan& d = hp[p];
+        memset(&d, 0, sizeof d);
+        d.pk = q.dim_pk; d.date = q.dim_date; d.nd = q.ndim;
+        d.fk = q.fk; d.flag = (const int8_t*)q.flag; d.status = (const int8_t*)q.status;
+        d.qty = q.qty; d.price = q.price; d.disc = q.disc; d.nf = q.nfact;
+        d.lo = q.lo; d.hi = q.hi;
+        d.fact_off = fact_total;
+        fact_total += q.nfact;
+        dtiles[p + 1] = dtiles[p] + (q.ndim + BT - 1) / BT;
+        ftiles[p + 1] = ftiles[p] + (q.nfact + BT - 1) / BT;
+        out[p].status = 0;
+        out[p].ngroups = 0;
+    }
+    // device copies of the plan table and tile maps
+    DPlan* dP = (DPlan*)salloc(np * sizeof(DPlan));
+    long long* dT = (long long*)salloc((np + 1) * 8);
+    long long* fT = (long long*)salloc((np + 1) * 8);
+    long long* mm = (long long*)salloc(np * 16);
+    unsigned* dup = (unsigned*)salloc(np * 4 + 16);
+    if (!dP || !dT || !fT || !mm || !dup) return E_DEVICE_OOM;
+    std::vector<long long> mminit(2 * np);
+    for (int p = 0; p < np; p++) { mminit[2 * p] = LLONG_MAX; mminit[2 * p + 1] = LLONG_MIN; }
+    HG_CU(cudaMemcpyAsync(dT, dtiles.data(), (np + 1) * 8, cudaMemcpyHostToDevice, g_stream));
+    HG_CU(cudaMemcpyAsync(fT, ftiles.data(), (np + 1) * 8, cudaMemcpyHostToDevice, g_stream));
+    HG_CU(cudaMemcpyAsync(mm, mminit.data(), np * 16, cudaMemcpyHostToDevice, g_stream));
+    HG_CU(cudaMemcpyAsync(dP, hp.data(), np * sizeof(DPlan), cudaMemcpyHostToDevice, g_stream));
+    HG_CU(cudaMemsetAsync(dup, 0, np * 4, g_stream));
+    if (dtiles[np] > 0) HG_LAUNCH("b_minmax", (unsigned)dtiles[np], 256, 0, k_b_minmax, dP, dT, np, mm);
+    std::vector<long long> hmm(2 * np);
+    std::vector<char> plain(np, 0);
+    HG_CU(cudaMemcpyAsync(hmm.data(), mm, np * 16, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));
+    // presence bitmaps and code tables
+    long long bm_words = 0;
+    for (int p = 0; p < np; p++) {
+        long long lo = hmm[2 * p], hi = hmm[2 * p + 1];
+        if (hp[p].nd == 0) { lo = 0; hi = -1; }
+        unsigned long long range = hi >= lo ? (unsigned long long)(hi - lo) + 1 : 0;
+        if (range > 64ull * (unsigned long long)(hp[p].nd > 1024 ? hp[p].nd : 1024) || range >= (1ull << 32)) {
+            plain[p] = 1;  // too wide for a presence bitmap: no row is built or matched here
+            lo = 0; hi = -1; range = 0;
+            hp[p].nd = 0;
+        }
+        hp[p].kmin = lo;
+        hp[p].kmax = hi;
+        bm_words += (long long)((range + 31) / 32) + 1;
+    }
+    unsigned* bm = (unsigned*)salloc((size_t)bm_words * 4);
+    unsigned* cb = (unsigned*)salloc((size_t)np * 2048 * 4);
+    unsigned short* dn = (unsigned short*)salloc((size_t)np * 65536 * 2);
+    if (!bm || !cb || !dn) return E_DEVICE_OOM;
+    HG_CU(cudaMemsetAsync(bm, 0, (size_t)bm_words * 4, g_stream));
+    HG_CU(cudaMemsetAsync(cb, 0, (size_t)np * 2048 * 4, g_stream));
+    {
+        long long w = 0;
+        for (int p = 0; p < np; p++) {
+            hp[p].bitmap = bm + w;
+            unsigned long long range = hp[p].kmax >= hp[p].kmin ? (unsigned long long)(hp[p].kmax - hp[p].kmin) + 1 : 0;
+            w += (long long)((range + 31) / 32) + 1;
+            hp[p].codebits = cb + (size_t)p * 2048;
+            hp[p].dense = dn + (size_t)p * 65536;
+        }
+    }
+    HG_CU(cudaMemcpyAsync(dP, hp.data(), np * sizeof(DPlan), cudaMemcpyHostToDevice, g_stream));
+    unsigned long long* nsel = (unsigned long long*)salloc(np * 8 + 16);
+    if (!nsel) return E_DEVICE_OOM;
+    HG_CU(cudaMemsetAsync(nsel, 0, np * 8, g_stream));
+    if (dtiles[np] > 0) HG_LAUNCH("b_build", (unsigned)dtiles[np], 256, 0, k_b_build, dP, dT, np, dup, nsel);
+    // probe
+    unsigned* fi = (unsigned*)salloc((size_t)(fact_total > 0 ? fact_total : 1) * 4);
+    unsigned long long* mcount = (unsigned long long*)salloc(np * 8 + 16);
+    long long* moff = (long long*)salloc((np + 1) * 8);
+    char* st = (char*)salloc((size_t)ftiles[np] * 8 + 64);
+    if (!fi || !mcount || !moff || !st) return E_DEVICE_OOM;
+    HG_CU(cudaMemsetAsync(mcount, 0, np * 8, g_stream));
+    HG_CU(cudaMemsetAsync(st, 0, (size_t)ftiles[np] * 8 + 64, g_stream));
+    if (ftiles[np] > 0)
+        HG_LAUNCH("b_probe", (unsigned)ftiles[np], 256, 0, k_b_probe, dP, fT, np, fi, (unsigned long long*)st,
+                  (unsigned*)(st + (size_t)ftiles[np] * 8), mcount, g_derr);
+    HG_LAUNCH("b_offsets", 1, 32, 0, k_b_offsets, mcount, np, moff);
+    // gather (over the fact tile map: a plan has at most as many matches as rows)
+    std::vector<unsigned long long> hm(np);
+    HG_CU(cudaMemcpyAsync(hm.data(), mcount, np * 8, cudaMemcpyDeviceToHost, g_stream));
+    std::vector<unsigned> hdup(np);
+    std::vector<unsigned long long> hsel(np);
+    HG_CU(cudaMemcpyAsync(hdup.data(), dup, np * 4, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaMemcpyAsync(hsel.data(), nsel, np * 8, cudaMemcpyDeviceToHost, g_stream));
+    HG_CHECK(check_device_errors());
+    // A repeated dimension key emits several rows per fact row, and a
+    // compressed key column longer than the fact table makes @join_index
+    // build on the fact side and emit rows in key-row order: both plans run
+    // through the builtins instead.
+    for (int p = 0; p < np; p++)
+        if (hdup[p] || hsel[p] > (unsigned long long)hp[p].nf) plain[p] = 1;
+    long long mtot = 0;
+    std::vector<long long> mtiles(np + 1), hmoff(np + 1);
+    mtiles[0] = 0;
+    for (int p = 0; p < np; p++) {
+        hmoff[p] = mtot;
+        mtot += (long long)hm[p];
+        mtiles[p + 1] = mtiles[p] + ((long long)hm[p] + BT - 1) / BT;
+    }
+    hmoff[np] = mtot;
+    long long* mT = (long long*)salloc((np + 1) * 8);
+    unsigned* code = (unsigned*)salloc((size_t)(mtot > 0 ? mtot : 1) * 4);
+    double* vq = (double*)salloc((size_t)(mtot > 0 ? mtot : 1) * 8);
+    double* vp = (double*)salloc((size_t)(mtot > 0 ? mtot : 1) * 8);
+    double* vd = (double*)salloc((size_t)(mtot > 0 ? mtot : 1) * 8);
+    long long* rows = (long long*)salloc((size_t)(mtot > 0 ? mtot : 1) * 8);
+    unsigned* ngroups = (unsigned*)salloc(np * 4 + 16);
+    unsigned* codes = (unsigned*)salloc((size_t)np * 256 * 4);
+    unsigned* hist = (unsigned*)salloc((size_t)np * 256 * 4);
+    unsigned* bucket = (unsigned*)salloc((size_t)np * 256 * 4);
+    char* st2 = (char*)salloc((size_t)mtiles[np] * 256 * 8 + 64);
+    if (!mT || !code || !vq || !vp || !vd || !rows || !ngroups || !codes || !hist || !bucket || !st2) return E_DEVICE_OOM;
+    HG_CU(cudaMemcpyAsync(mT, mtiles.data(), (np + 1) * 8, cudaMemcpyHostToDevice, g_stream));
+    HG_CU(cudaMemsetAsync(hist, 0, (size_t)np * 256 * 4, g_stream));
+    HG_CU(cudaMemsetAsync(st2, 0, (size_t)mtiles[np] * 256 * 8 + 64, g_stream));
+    if (mtiles[np] > 0) {
+        HG_LAUNCH("b_gather", (unsigned)mtiles[np], 256, 0, k_b_gather, dP, mT, np, fi, mcount, moff, code, vq, vp, vd);
+        HG_LAUNCH("b_dense", np, 256, 0, k_b_dense, dP, ngroups, codes);
+        HG_LAUNCH("b_hist", (unsigned)mtiles[np], 256, 0, k_b_hist, dP, mT, np, mcount, moff, code, hist);
+        HG_LAUNCH("b_bucket", np, 256, 0, k_b_bucket, hist, bucket);
+        HG_LAUNCH("b_sort", (unsigned)mtiles[np], 256, 0, k_b_sort, dP, mT, np, mcount, moff, code, bucket, rows,
+                  (unsigned long long*)st2, (unsigned*)(st2 + (size_t)mtiles[np] * 256 * 8), g_derr);
+    }
+    std::vector<unsigned> hg(np);
+    HG_CU(cudaMemcpyAsync(hg.data(), ngroups, np * 4, cudaMemcpyDeviceToHost, g_stream));
+    HG_CHECK(check_device_errors());
+    std::vector<long long> segoff(np + 1);
+    segoff[0] = 0;
+    for (int p = 0; p < np; p++) {
+        if (hm[p] == 0) hg[p] = 0;
+        if (hg[p] > 256) {  // the result holds 256 groups
+            plain[p] = 1;
+            hg[p] = 0;
+        }
+        segoff[p + 1] = segoff[p] + hg[p];
+    }
+    const long long nseg = segoff[np];
+    long long* dseg = (long long*)salloc((np + 1) * 8);
+    long long* starts = (long long*)salloc((size_t)(nseg > 0 ? nseg : 1) * 8);
+    double* sq = (double*)salloc((size_t)(nseg > 0 ? nseg : 1) * 8);
+    double* sp = (double*)salloc((size_t)(nseg > 0 ? nseg : 1) * 8);
+    double* sd = (double*)salloc((size_t)(nseg > 0 ? nseg : 1) * 8);
+    if (!dseg || !starts || !sq || !sp || !sd) return E_DEVICE_OOM;
+    unsigned* ng_dev = ngroups;
+    if (nseg > 0) {
+        HG_CU(cudaMemcpyAsync(dseg, segoff.data(), (np + 1) * 8, cudaMemcpyHostToDevice, g_stream));
+        HG_CU(cudaMemcpyAsync(ng_dev, hg.data(), np * 4, cudaMemcpyHostToDevice, g_stream));
+        HG_LAUNCH("b_starts", np, 256, 0, k_b_starts, moff, bucket, ng_dev, dseg, np, starts);
+        HG_CHECK(seg_sum_f64(vq, rows, mtot, starts, nseg, mtot, sq));
+        HG_CHECK(seg_sum_f64(vp, rows, mtot, starts, nseg, mtot, sp));
+        HG_CHECK(seg_sum_f64(vd, rows, mtot, starts, nseg, mtot, sd));
+        HG_LAUNCH("b_avg", cap_grid(nseg), 256, 0, k_b_avg, sp, starts, nseg, mtot, sp);
+    }
+    std::vector<long long> hst(nseg > 0 ? nseg : 1);
+    std::vector<double> hq(nseg > 0 ? nseg : 1), hpv(nseg > 0 ? nseg : 1), hd(nseg > 0 ? nseg : 1);
+    std::vector<unsigned> hcodes((size_t)np * 256);
+    if (nseg > 0) {
+        HG_CU(cudaMemcpyAsync(hst.data(), starts, nseg * 8, cudaMemcpyDeviceToHost, g_stream));
+        HG_CU(cudaMemcpyAsync(hq.data(), sq, nseg * 8, cudaMemcpyDeviceToHost, g_stream));
+        HG_CU(cudaMemcpyAsync(hpv.data(), sp, nseg * 8, cudaMemcpyDeviceToHost, g_stream));
+        HG_CU(cudaMemcpyAsync(hd.data(), sd, nseg * 8, cudaMemcpyDeviceToHost, g_stream));
+        HG_CU(cudaMemcpyAsync(hcodes.data(), codes, (size_t)np * 256 * 4, cudaMemcpyDeviceToHost, g_stream));
+    }
+    HG_CHECK(check_device_errors());
+    for (int p = 0; p < np; p++) {
+        hgpuJoinGroupResult& r = out[p];
+        if (plain[p]) continue;
+        r.ngroups = hg[p];
+        for (unsigned g = 0; g < hg[p]; g++) {
+            long long k = segoff[p] + g;
+            long long e = (g + 1 < hg[p]) ? hst[k + 1] : hmoff[p + 1];
+            long long cnt = e - hst[k];
+            unsigned c = hcodes[(size_t)p * 256 + g];
+            r.flag[g] = (C)(c >> 8);
+            r.st[g] = (C)(c & 255);
+            r.count[g] = cnt;
+            r.sum_qty[g] = hq[k];
+            r.sum_disc[g] = hd[k];
+            r.avg_price[g] = hpv[k];
+        }
+    }
+    for (int p = 0; p < np; p++)
+        if (plain[p]) out[p].status = plan_through_builtins(plans[p], &out[p]);
+    return 0;
+}

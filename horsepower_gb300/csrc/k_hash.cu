@@ -24,6 +24,8 @@
 // (build row, probe row) pairs with ballot/popc compaction.  Keys with
 // duplicate build rows use a count / scan / write path over a CSR of build
 // rows sorted per slot.
+#include <climits>
+
 #include "dev_common.cuh"
 
 namespace hg {
@@ -74,7 +76,31 @@ struct Table {
     unsigned* special;  // 64-bit keys: [0] min row, [1] count of the key equal to EMPTY
     unsigned* flags;    // [0] = a key was inserted twice
     unsigned long long cap;  // slots; the home slot is (hash32 * cap) >> 32
+    // presence filter read before any slot: a miss costs one small,
+    // cache-resident bitmap read instead of a walk along the probe sequence
+    unsigned* filter;
+    unsigned long long fmask;  // hash mode: filter bits - 1
+    // direct mode (integer keys whose range is at most a few times n):
+    // slots is a u32 row array indexed by key - kmin, filter bit = key - kmin
+    int direct;
+    long long kmin, kmax;
 };
+
+template <typename K>
+__device__ __forceinline__ long long key_signed(K k) {
+    if constexpr (sizeof(K) == 4) return (long long)(int)k;
+    else return (long long)k;
+}
+// filter bit of a key, or -1 when the key cannot be present (outside the direct range)
+template <typename K>
+__device__ __forceinline__ long long filter_bit(const Table<K>& t, K k) {
+    if (t.direct) {
+        long long v = key_signed<K>(k);
+        return (v < t.kmin || v > t.kmax) ? -1 : v - t.kmin;
+    }
+    unsigned long long h = hash_key<K>(k);
+    return (long long)(((h >> 17) ^ (h << 7)) & t.fmask);
+}
 
 template <typename K>
 __device__ __forceinline__ unsigned long long home_slot(K k, unsigned long long cap) {
@@ -88,6 +114,20 @@ __device__ __forceinline__ unsigned long long next_slot(unsigned long long h, un
 
 template <typename K>
 __device__ __forceinline__ void table_insert(Table<K> t, K k, unsigned r, unsigned* derr) {
+    {
+        long long fb = filter_bit<K>(t, k);
+        if (fb < 0) { flag_error(derr, DERR_CAPACITY); return; }
+        atomicOr(&t.filter[fb >> 5], 1u << (fb & 31));
+        if (t.direct) {
+            unsigned* row = (unsigned*)t.slots;
+            unsigned prev = atomicCAS(&row[fb], 0xffffffffu, r);
+            if (prev != 0xffffffffu) {
+                atomicMin(&row[fb], r);
+                atomicOr(t.flags, 1u);
+            }
+            return;
+        }
+    }
     unsigned long long h = home_slot<K>(k, t.cap);
     if constexpr (sizeof(K) == 4) {
         unsigned long long* sl = (unsigned long long*)t.slots;
@@ -136,44 +176,68 @@ __device__ __forceinline__ void table_insert(Table<K> t, K k, unsigned r, unsign
 template <typename K, int N>
 __device__ __forceinline__ void table_find_n(const Table<K>& t, const K* key, const bool* valid, long long* slot,
                                              unsigned* row) {
+    // 1. presence filter: N independent reads of a small bitmap
+    long long fb[N];
+    unsigned fw[N];
+    bool cand[N];
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+        fb[j] = valid[j] ? filter_bit<K>(t, key[j]) : -1;
+        fw[j] = fb[j] >= 0 ? __ldg(t.filter + (fb[j] >> 5)) : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+        cand[j] = fb[j] >= 0 && ((fw[j] >> (fb[j] & 31)) & 1u);
+        slot[j] = -1;
+        row[j] = 0xffffffffu;
+    }
+    if (t.direct) {  // 2a. one row read per candidate
+        const unsigned* rs = (const unsigned*)t.slots;
+        unsigned rr[N];
+#pragma unroll
+        for (int j = 0; j < N; j++) rr[j] = cand[j] ? __ldg(rs + fb[j]) : 0xffffffffu;
+#pragma unroll
+        for (int j = 0; j < N; j++)
+            if (cand[j] && rr[j] != 0xffffffffu) { slot[j] = fb[j]; row[j] = rr[j]; }
+        return;
+    }
+    // 2b. hash slots of the candidates, first reads issued together
     unsigned long long h[N];
     if constexpr (sizeof(K) == 4) {
         const unsigned long long* sl = (const unsigned long long*)t.slots;
-        unsigned long long s[N];
+        unsigned long long sv[N];
 #pragma unroll
-        for (int j = 0; j < N; j++) { h[j] = home_slot<K>(key[j], t.cap); s[j] = valid[j] ? __ldg(sl + h[j]) : ~0ull; }
+        for (int j = 0; j < N; j++) { h[j] = home_slot<K>(key[j], t.cap); sv[j] = cand[j] ? __ldg(sl + h[j]) : ~0ull; }
 #pragma unroll
         for (int j = 0; j < N; j++) {
-            slot[j] = -1; row[j] = 0xffffffffu;
-            if (!valid[j]) continue;
+            if (!cand[j]) continue;
             for (unsigned long long p = 0; p < t.cap; p++) {
-                if (s[j] == ~0ull) break;
-                if ((unsigned)(s[j] >> 32) == (unsigned)key[j]) { slot[j] = (long long)h[j]; row[j] = (unsigned)s[j]; break; }
+                if (sv[j] == ~0ull) break;
+                if ((unsigned)(sv[j] >> 32) == (unsigned)key[j]) { slot[j] = (long long)h[j]; row[j] = (unsigned)sv[j]; break; }
                 h[j] = next_slot(h[j], t.cap);
-                s[j] = __ldg(sl + h[j]);
+                sv[j] = __ldg(sl + h[j]);
             }
         }
     } else {
         const ulonglong2* sl = (const ulonglong2*)t.slots;
-        ulonglong2 s[N];
+        ulonglong2 sv[N];
 #pragma unroll
         for (int j = 0; j < N; j++) {
             h[j] = home_slot<K>(key[j], t.cap);
-            s[j] = (valid[j] && key[j] != ~0ull) ? __ldg(sl + h[j]) : make_ulonglong2(~0ull, ~0ull);
+            sv[j] = (cand[j] && key[j] != ~0ull) ? __ldg(sl + h[j]) : make_ulonglong2(~0ull, ~0ull);
         }
 #pragma unroll
         for (int j = 0; j < N; j++) {
-            slot[j] = -1; row[j] = 0xffffffffu;
-            if (!valid[j]) continue;
+            if (!cand[j]) continue;
             if (key[j] == ~0ull) {
                 if (t.special[1]) { slot[j] = -2; row[j] = t.special[0]; }
                 continue;
             }
             for (unsigned long long p = 0; p < t.cap; p++) {
-                if (s[j].x == ~0ull) break;
-                if (s[j].x == (unsigned long long)key[j]) { slot[j] = (long long)h[j]; row[j] = (unsigned)s[j].y; break; }
+                if (sv[j].x == ~0ull) break;
+                if (sv[j].x == (unsigned long long)key[j]) { slot[j] = (long long)h[j]; row[j] = (unsigned)sv[j].y; break; }
                 h[j] = next_slot(h[j], t.cap);
-                s[j] = __ldg(sl + h[j]);
+                sv[j] = __ldg(sl + h[j]);
             }
         }
     }
@@ -197,27 +261,84 @@ __global__ void k_build(Table<K> t, const void* __restrict__ x, int typ, long lo
     }
 }
 
+__global__ void k_key_minmax(const void* __restrict__ x, int typ, long long n, long long* mm) {
+    long long a = LLONG_MAX, b = LLONG_MIN;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        long long v;
+        switch (typ) {
+        case H_J: v = ((const int8_t*)x)[i]; break;
+        case H_H: v = ((const int16_t*)x)[i]; break;
+        case H_I: v = ((const int32_t*)x)[i]; break;
+        default: v = ((const long long*)x)[i]; break;
+        }
+        a = v < a ? v : a;
+        b = v > b ? v : b;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        long long q = __shfl_xor_sync(0xffffffffu, a, o); a = q < a ? q : a;
+        long long r = __shfl_xor_sync(0xffffffffu, b, o); b = r > b ? r : b;
+    }
+    if (lane_id() == 0) { atomicMin(mm, a); atomicMax(mm + 1, b); }
+}
+
 template <typename K>
-static I table_create(Table<K>* t, long long n, bool with_count) {
-    unsigned long long cap = (unsigned long long)((double)n / g_load_factor) + 16;
-    if (cap > 0xffffffffull) cap = 0xffffffffull;
+static I table_create(Table<K>* t, long long n, bool with_count, int direct, long long kmin, long long kmax) {
     const size_t ss = sizeof(K) == 4 ? 8 : 16;
-    t->cap = cap;
-    t->slots = salloc(cap * ss);
-    t->cnt = with_count ? (unsigned*)salloc(cap * 4) : nullptr;
+    t->direct = direct;
+    t->kmin = kmin;
+    t->kmax = kmax;
+    unsigned long long fbits;
+    if (direct) {
+        t->cap = (unsigned long long)(kmax - kmin + 1);
+        fbits = t->cap;
+        t->slots = salloc(t->cap * 4);
+    } else {
+        unsigned long long cap = (unsigned long long)((double)n / g_load_factor) + 16;
+        if (cap > 0xffffffffull) cap = 0xffffffffull;
+        t->cap = cap;
+        fbits = 4096;
+        while (fbits < 16ull * (unsigned long long)n) fbits <<= 1;
+        t->slots = salloc(cap * ss);
+    }
+    t->fmask = fbits - 1;
+    size_t fwords = (size_t)((fbits + 31) / 32);
+    t->filter = (unsigned*)salloc(fwords * 4);
+    t->cnt = with_count ? (unsigned*)salloc(t->cap * 4) : nullptr;
     t->special = (unsigned*)salloc(32);
-    if (!t->slots || (with_count && !t->cnt) || !t->special) return E_DEVICE_OOM;
+    if (!t->slots || !t->filter || (with_count && !t->cnt) || !t->special) return E_DEVICE_OOM;
     t->flags = t->special + 2;
-    HG_CU(cudaMemsetAsync(t->slots, 0xff, cap * ss, g_stream));
-    if (with_count) HG_CU(cudaMemsetAsync(t->cnt, 0, cap * 4, g_stream));
+    HG_CU(cudaMemsetAsync(t->slots, 0xff, t->cap * (direct ? 4 : ss), g_stream));
+    HG_CU(cudaMemsetAsync(t->filter, 0, fwords * 4, g_stream));
+    if (with_count) HG_CU(cudaMemsetAsync(t->cnt, 0, t->cap * 4, g_stream));
     HG_CU(cudaMemsetAsync(t->special, 0xff, 4, g_stream));
     HG_CU(cudaMemsetAsync(t->special + 1, 0, 12, g_stream));
     return 0;
 }
 
+// Builds the table of x's keys.  Integer keys whose range is at most 8n
+// (and below 2^31) use direct addressing; others hash.
 template <typename K>
 static I table_build(Table<K>* t, const void* x, int typ, long long n, bool with_count) {
-    HG_CHECK(table_create<K>(t, n, with_count));
+    int direct = 0;
+    long long kmin = 0, kmax = -1;
+    if (n > 0 && (typ == H_J || typ == H_H || typ == H_I || typ == H_L)) {
+        long long* mm = (long long*)salloc(16);
+        if (!mm) return E_DEVICE_OOM;
+        long long init[2] = {LLONG_MAX, LLONG_MIN};
+        HG_CU(cudaMemcpyAsync(mm, init, 16, cudaMemcpyHostToDevice, g_stream));
+        unsigned g = grid_for(n, 256);
+        if (g > (unsigned)g_sms * 8) g = g_sms * 8;
+        HG_LAUNCH("key_minmax", g, 256, 0, k_key_minmax, x, typ, n, mm);
+        long long h[2];
+        HG_CU(cudaMemcpyAsync(h, mm, 16, cudaMemcpyDeviceToHost, g_stream));
+        HG_CU(cudaStreamSynchronize(g_stream));
+        unsigned long long range = (unsigned long long)h[1] - (unsigned long long)h[0] + 1ull;
+        unsigned long long lim = 8ull * (unsigned long long)n;
+        if (lim < (1ull << 16)) lim = 1ull << 16;
+        if (range <= lim && range < (1ull << 31)) { direct = 1; kmin = h[0]; kmax = h[1]; }
+    }
+    HG_CHECK(table_create<K>(t, n, with_count, direct, kmin, kmax));
     if (n > 0) {
         unsigned grid = grid_for(n, 256);
         if (grid > (unsigned)g_sms * 16) grid = g_sms * 16;
@@ -349,6 +470,11 @@ __device__ __forceinline__ bool key_stream(const void* p, int typ, long long i, 
     }
 }
 
+// One pass per 4096-row tile: each lane looks up 16 probe rows, 8 at a time
+// with all their reads in flight together (streamed key, presence-filter
+// bit, then the build row of the candidates), keeps the build rows in
+// registers, takes the tile's output offset from a decoupled look-back and
+// writes the (build row, probe row) pairs with ballot/popc.
 template <typename K>
 __global__ void __launch_bounds__(JT_THREADS, 4) k_join_probe(Table<K> t, LinearBuild lin, int mode,
                                                               const void* __restrict__ y, int ytyp, long long n,

@@ -109,33 +109,10 @@ __global__ void __launch_bounds__(256) k_seg_chunk(const T* __restrict__ src, co
     const long long base = s + (c - (long long)chunk0[lo]) * TILE_SUM;
     bool bad = false;
     A acc = ident;
-    T v[16];
-    // all 16 loads of the lane are issued before the fixed-order accumulation
-    if constexpr (GATHER) {
-        long long r[16];
-#pragma unroll
-        for (int k = 0; k < 16; k++) {
-            long long j = base + k * 256 + threadIdx.x;
-            r[k] = j < e ? __ldg(rows + j) : 0;
-        }
-#pragma unroll
-        for (int k = 0; k < 16; k++) {
-            long long j = base + k * 256 + threadIdx.x;
-            bool ok = r[k] >= 0 && r[k] < nx;
-            if (j < e && !ok) bad = true;
-            v[k] = (j < e && ok) ? src[r[k]] : T(0);
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < 16; k++) {
-            long long j = base + k * 256 + threadIdx.x;
-            v[k] = j < e ? src[j] : T(0);
-        }
-    }
-#pragma unroll
+#pragma unroll 4
     for (int k = 0; k < 16; k++) {
         long long j = base + k * 256 + threadIdx.x;
-        if (j < e) acc = sop<A, OP>(acc, (A)v[k]);
+        if (j < e) acc = sop<A, OP>(acc, (A)seg_elem<T, GATHER>(src, rows, nx, j, bad));
     }
     acc = swarp<A, OP>(acc);
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
@@ -222,6 +199,13 @@ static I seg_reduce(const T* src, const long long* rows, long long nx, const lon
     HG_CHECK((seg_reduce<A, A, OP, false>(part, nullptr, 0, pstarts, nbig, (long long)nchunks, ident, res)));
     HG_LAUNCH("scatter_big", gcap(nbig), 256, 0, k_scatter_big<A>, res, big, nbig, out);
     return last_launch_error();
+}
+
+// f64 sums of segments gathered through row ids, for the batched plans: the
+// same kernels and order as hgpuGroupSum.
+I seg_sum_f64(const double* src, const long long* rows, long long nx, const long long* starts, long long ng,
+              long long total, double* out) {
+    return seg_reduce<double, double, OP_SUM, true>(src, rows, nx, starts, ng, total, 0.0, out);
 }
 
 // ---------------------------------------------------------- finishing steps

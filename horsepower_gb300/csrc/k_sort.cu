@@ -85,12 +85,18 @@ __global__ void k_bucket_base(const unsigned long long* __restrict__ hist, unsig
 }
 
 template <typename K, bool FIRST>
-__global__ void __launch_bounds__(RS_THREADS) k_onesweep(const K* __restrict__ kin, const unsigned* __restrict__ vin,
+__global__ void __launch_bounds__(RS_THREADS, 3) k_onesweep(const K* __restrict__ kin, const unsigned* __restrict__ vin,
                                                          K* __restrict__ kout, unsigned* __restrict__ vout, long long n,
                                                          int shift, int bits, const unsigned long long* __restrict__ bucket,
                                                          unsigned long long* status, unsigned* ticket, unsigned* derr) {
+    // dynamic shared memory: the tile's keys and row ids in digit order
+    extern __shared__ __align__(16) unsigned char os_smem[];
+    K* skey = reinterpret_cast<K*>(os_smem);
+    unsigned* sval = reinterpret_cast<unsigned*>(os_smem + RS_TILE * sizeof(K));
     __shared__ unsigned whist[8][256];
+    __shared__ unsigned dstart[256];
     __shared__ unsigned long long dbase[256];
+    __shared__ unsigned wscan[8];
     __shared__ long long tile_id;
     for (int i = threadIdx.x; i < 8 * 256; i += RS_THREADS) (&whist[0][0])[i] = 0;
     if (threadIdx.x == 0) tile_id = atomicAdd(ticket, 1u);
@@ -100,13 +106,18 @@ __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const K* __restrict__ k
     const long long wbase = t * RS_TILE + (long long)w * (32 * RS_ITEMS);
     const unsigned dmask = (1u << bits) - 1;
     K key[RS_ITEMS];
-    unsigned val[RS_ITEMS], dig[RS_ITEMS], rank[RS_ITEMS];
+    unsigned val[RS_ITEMS], rd[RS_ITEMS];  // rd = digit << 16 | rank within the warp's items
 #pragma unroll
     for (int k = 0; k < RS_ITEMS; k++) {
         long long i = wbase + k * 32 + lane;
         bool valid = i < n;
         key[k] = valid ? kin[i] : K(0);
         val[k] = FIRST ? (unsigned)i : (valid ? vin[i] : 0u);
+    }
+#pragma unroll
+    for (int k = 0; k < RS_ITEMS; k++) {
+        long long i = wbase + k * 32 + lane;
+        bool valid = i < n;
         unsigned d = valid ? ((unsigned)((unsigned long long)key[k] >> shift) & dmask) : 0xffffffffu;
         unsigned peers = __match_any_sync(0xffffffffu, d);
         int leader = __ffs(peers) - 1;
@@ -116,8 +127,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const K* __restrict__ k
             whist[w][d] = pre + __popc(peers);
         }
         pre = __shfl_sync(0xffffffffu, pre, leader);
-        rank[k] = pre + __popc(peers & lanemask_lt());
-        dig[k] = d;
+        rd[k] = ((d & 0xffffu) << 16) | (pre + __popc(peers & lanemask_lt()));
         __syncwarp();
     }
     __syncthreads();
@@ -125,6 +135,13 @@ __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const K* __restrict__ k
         const int d = threadIdx.x;  // one thread per digit
         unsigned c = 0;
         for (int ww = 0; ww < 8; ww++) { unsigned h = whist[ww][d]; whist[ww][d] = c; c += h; }
+        // tile-local start of digit d: exclusive scan of the 256 digit counts
+        unsigned inc = warp_incl_scan(c);
+        if (lane == 31) wscan[w] = inc;
+        __syncthreads();
+        unsigned before = 0;
+        for (unsigned ww = 0; ww < w; ww++) before += wscan[ww];
+        dstart[d] = before + inc - c;
         unsigned long long* st = status + (size_t)t * 256 + d;
         unsigned long long excl = 0;
         if (d <= (int)dmask) {
@@ -133,13 +150,13 @@ __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const K* __restrict__ k
                 st_release(st, LB_AGG | c);
                 long long j = t - 1, spins = 0;
                 while (j >= 0) {
-                    unsigned long long s = ld_acquire(status + (size_t)j * 256 + d);
-                    unsigned long long f = s >> 62;
+                    unsigned long long sv = ld_acquire(status + (size_t)j * 256 + d);
+                    unsigned long long f = sv >> 62;
                     if (f == 0) {
                         if (++spins > SPIN_LIMIT) { flag_error(derr, DERR_TIMEOUT); break; }
                         continue;
                     }
-                    excl += s & LB_MASK;
+                    excl += sv & LB_MASK;
                     if (f == 2) break;
                     j--;
                 }
@@ -149,15 +166,26 @@ __global__ void __launch_bounds__(RS_THREADS) k_onesweep(const K* __restrict__ k
         dbase[d] = bucket[d] + excl;
     }
     __syncthreads();
+    // place the tile in digit order in shared memory ...
 #pragma unroll
     for (int k = 0; k < RS_ITEMS; k++) {
         long long i = wbase + k * 32 + lane;
         if (i < n) {
-            unsigned d = dig[k];
-            unsigned long long pos = dbase[d] + whist[w][d] + rank[k];
-            kout[pos] = key[k];
-            vout[pos] = val[k];
+            unsigned d = rd[k] >> 16;
+            unsigned local = dstart[d] + whist[w][d] + (rd[k] & 0xffffu);
+            skey[local] = key[k];
+            sval[local] = val[k];
         }
+    }
+    __syncthreads();
+    // ... and write each digit's run contiguously (consecutive threads, consecutive addresses)
+    const long long tn = (n - t * RS_TILE) < RS_TILE ? (n - t * RS_TILE) : RS_TILE;
+    for (int i = threadIdx.x; i < tn; i += RS_THREADS) {
+        K kk = skey[i];
+        unsigned d = (unsigned)((unsigned long long)kk >> shift) & dmask;
+        unsigned long long pos = dbase[d] + (unsigned long long)(i - (int)dstart[d]);
+        kout[pos] = kk;
+        vout[pos] = sval[i];
     }
 }
 
@@ -246,11 +274,18 @@ I radix_sort(const K* keys, long long n, const K** kres, const unsigned** vres, 
         K* ko = kb[p & 1];
         unsigned* vo = vb[p & 1];
         unsigned* ticket = (unsigned*)(st + (size_t)ntiles * 256 * 8);
+        const size_t dsm = (size_t)RS_TILE * (sizeof(K) + 4);
+        static bool attr_set = false;
+        if (!attr_set) {
+            cudaFuncSetAttribute(k_onesweep<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
+            cudaFuncSetAttribute(k_onesweep<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
+            attr_set = true;
+        }
         if (p == 0 && !init_vals)
-            HG_LAUNCH("onesweep", (unsigned)ntiles, RS_THREADS, 0, (k_onesweep<K, true>), kin, vin, ko, vo, n,
+            HG_LAUNCH("onesweep", (unsigned)ntiles, RS_THREADS, dsm, (k_onesweep<K, true>), kin, vin, ko, vo, n,
                       lo + p * bits, bits, bucket + p * 256, (unsigned long long*)st, ticket, g_derr);
         else
-            HG_LAUNCH("onesweep", (unsigned)ntiles, RS_THREADS, 0, (k_onesweep<K, false>), kin, vin, ko, vo, n,
+            HG_LAUNCH("onesweep", (unsigned)ntiles, RS_THREADS, dsm, (k_onesweep<K, false>), kin, vin, ko, vo, n,
                       lo + p * bits, bits, bucket + p * 256, (unsigned long long*)st, ticket, g_derr);
         kin = ko;
         vin = vo;

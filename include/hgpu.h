@@ -205,6 +205,33 @@ I hgpuChainDestroy(hgpuChain c);
 /* Multi-column compress sharing one mask: pattern.cc:452-520 (V *z, V x, V *y) */
 I hgpuCompressMany(V *z, V x, V *y, L n);
 
+/* ---------------- batched plans ----------------
+ * Many independent filter-join-aggregate queries run stage by stage in shared
+ * launches (no counterpart in the reference, which runs one query at a time).
+ * Each plan is the join + group-by query of plans.join_group: filter the
+ * dimension on date in [lo, hi), join its pk to the fact fk, group the matches
+ * on (flag, status) and aggregate sum(qty), avg(price), sum(disc), count.
+ * Per-plan results are bit-identical to running the plan's builtins alone.
+ * Columns must be device or pinned host memory. */
+typedef struct {
+    const I *dim_pk, *dim_date; L ndim;
+    const I *fk; const C *flag, *status; const E *qty, *price, *disc; L nfact;
+    I lo, hi;
+} hgpuJoinGroupPlan;
+#define HGPU_PLAN_MAX_GROUPS 256
+typedef struct {
+    I status;                         /* 0, or E_NOT_IMPL for a plan outside the batched scope */
+    L ngroups;                        /* groups in ascending (flag<<8 | status) order */
+    C flag[HGPU_PLAN_MAX_GROUPS], st[HGPU_PLAN_MAX_GROUPS];
+    E sum_qty[HGPU_PLAN_MAX_GROUPS], avg_price[HGPU_PLAN_MAX_GROUPS], sum_disc[HGPU_PLAN_MAX_GROUPS];
+    L count[HGPU_PLAN_MAX_GROUPS];
+} hgpuJoinGroupResult;
+I hgpuBatchJoinGroup(const hgpuJoinGroupPlan *plans, L nplans, hgpuJoinGroupResult *out);
+/* Seeded synthetic join tables generated on the device (benchmarks): dim is
+ * filled with a 2-node list (pk = a permutation of 0..ndim-1, date), fact with
+ * a 6-node list (fk, flag, status, qty, price, disc). */
+I hgpuSynthJoinTables(unsigned long long seed, L nfact, L ndim, V dim, V fact);
+
 /* ---------------- runtime extensions ---------------- */
 #define HGPU_RESIDENT_DEVICE 0   /* outputs stay in HBM (default) */
 #define HGPU_RESIDENT_HOST   1   /* outputs are copied to pinned host memory on return */
