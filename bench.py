@@ -285,6 +285,9 @@ def run_batched(args):
 
     for _ in range(args.warmup):
         got = batched()
+    from horsepower_gb300 import autotune
+    tuned, table = autotune.tune(gpu, batched, reps=2)
+    got = batched()
     ref = one_at_a_time()
     exact = all(np.array_equal(g[k], np.asarray(w[k]).astype(g[k].dtype)) for g, w in zip(got, ref) for k in range(6))
     clocks = Clocks()
@@ -305,6 +308,16 @@ def run_batched(args):
         t_plain.append(Lb.hgpuTimerStop())
     ms_p = statistics.median(t_plain)
     n = len(plans)
+    # per-kernel device time of one batched call (CUDA events per launch; outside the timed region)
+    Lb.hgpuProfileRead.restype = C.c_int32
+    Lb.hgpuProfileRead.argtypes = [C.c_int32, C.POINTER(C.c_char_p), C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+    Lb.hgpuProfileReset()
+    Lb.hgpuProfile(1)
+    batched()
+    Lb.hgpuProfile(0)
+    names, tot, cnt = (C.c_char_p * 128)(), (C.c_double * 128)(), (C.c_longlong * 128)()
+    nk = Lb.hgpuProfileRead(128, names, tot, cnt)
+    kern = sorted(((names[i].decode(), tot[i]) for i in range(min(nk, 128))), key=lambda r: -r[1])
     return {
         "metric": "batched join + group-by plans: queries/s", "value": n / (ms_b / 1000), "unit": "queries/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_b, "higher_is_better": True,
@@ -315,6 +328,77 @@ def run_batched(args):
         "speedup_vs_plain": ms_p / ms_b, "bit_exact_vs_plain": bool(exact),
         "fact_rows_per_s": total_rows / (ms_b / 1000),
         "gpu_launches": int(launches), "clocks": clk,
+        "kernels_ms": {k: round(t, 4) for k, t in kern},
+        "autotune": {"chosen": tuned, "ms": {k: {str(v): round(t, 3) for v, t in d.items()} for k, d in table.items()}},
+    }
+
+
+def run_served(args):
+    """The served form: lineitem (6,001,215 rows), the join tables (59,986,052 x
+    15,000,000) and the order table (150,000,000 rows, Zipf(1.1) keys over
+    10,000,000 values) resident in HBM; Poisson request streams of the
+    60/30/10 filter-aggregate / join + group-by / top-1000 mix at several
+    rates, through the continuous-batching loop and through the plain
+    one-request-at-a-time builtin path.  Returns the JSON line."""
+    import horsepower_gb300
+    from horsepower_gb300 import batch as B
+    from horsepower_gb300 import serve as S
+    gpu = horsepower_gb300.load()
+    Lb = gpu.lib
+    line = S.line_table(gpu, 6_001_215, seed=0)
+    dim, fact = B.synth_tables(gpu, 1, args.fact, args.dim)
+    order = S.order_table(gpu, args.order_rows, seed=2)
+    srv = S.Server(gpu, line, dim, fact, order, budget=args.budget_gb << 30)
+    warm = S.request_stream(64, 0.0, seed=99)
+    for _ in range(args.warmup):
+        srv.run(warm)
+        srv.run(warm[:16], S.PLAIN)
+    rates = [int(r) for r in args.rates.split(",")]
+    table = []
+    clocks = Clocks()
+    clocks.start()
+    l0 = Lb.hgpuLaunchCount()
+    for rate in rates:
+        n = max(50, int(rate * args.serve_seconds))
+        reqs = S.request_stream(n, rate, seed=7 + rate)
+        row = {"rate": rate, "requests": n}
+        for name, mode in (("served", S.BATCHED), ("plain", S.PLAIN)):
+            _, st, _ = srv.run(reqs, mode)
+            row[name] = {"qps": round(st.qps, 1), "p50_ms": round(st.p50_ms, 3), "p99_ms": round(st.p99_ms, 3),
+                         "mean_ms": round(st.mean_ms, 3), "steps": st.steps, "max_step_requests": st.max_step_requests,
+                         "max_step_gb": round(st.max_step_bytes / 2 ** 30, 3), "rejected": st.rejected}
+        table.append(row)
+    launches = Lb.hgpuLaunchCount() - l0
+    clk = clocks.stop()
+    # per-kernel device time of one burst of 256 requests admitted together
+    # (CUDA events per launch; outside the timed streams)
+    Lb.hgpuProfileRead.restype = C.c_int32
+    Lb.hgpuProfileRead.argtypes = [C.c_int32, C.POINTER(C.c_char_p), C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+    burst = S.request_stream(256, 0.0, seed=5)
+    Lb.hgpuProfileReset()
+    Lb.hgpuProfile(1)
+    _, bst, _ = srv.run(burst)
+    Lb.hgpuProfile(0)
+    names, tot, cnt = (C.c_char_p * 128)(), (C.c_double * 128)(), (C.c_longlong * 128)()
+    nk = Lb.hgpuProfileRead(128, names, tot, cnt)
+    kern = sorted(((names[i].decode(), tot[i], cnt[i]) for i in range(min(nk, 128))), key=lambda r: -r[1])
+    srv.close()
+    top = table[-1]
+    return {
+        "metric": "served requests: queries/s and p99 latency (continuous batching vs one request per launch sequence)",
+        "value": top["served"]["qps"], "unit": "queries/s", "n_gpus": 1, "steps": len(rates), "warmup": args.warmup,
+        "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32+int64+f64", "data": "synthetic (seeded; join and order tables generated on the device)",
+        "config": {"workload": "Poisson request stream: 60% q6 filter-aggregate (random 365-day window), "
+                               "30% join + group-by (random 365-day dim window), 10% top-1000 order on a random "
+                               "key range; tables resident", "lineitem_rows": 6_001_215, "fact_rows": args.fact,
+                   "dim_rows": args.dim, "order_rows": args.order_rows, "budget_gb": args.budget_gb,
+                   "seconds_per_rate": args.serve_seconds},
+        "p99_ms": top["served"]["p99_ms"], "p50_ms": top["served"]["p50_ms"],
+        "plain": top["plain"], "speedup_qps_vs_plain": round(top["served"]["qps"] / max(top["plain"]["qps"], 1e-9), 2),
+        "rates": table, "gpu_launches": int(launches), "clocks": clk,
+        "burst_256": {"wall_ms": round(1e3 * bst.wall_s, 2), "steps": bst.steps,
+                      "kernels_ms": {k: [round(t, 3), int(c)] for k, t, c in kern[:24]}},
     }
 
 
@@ -346,13 +430,17 @@ def main():
     ap.add_argument("--dim", type=int, default=15_000_000)
     ap.add_argument("--cpu-scale", type=int, default=10)
     ap.add_argument("--cpu-reps", type=int, default=3)
-    ap.add_argument("--workload", default="join_group", choices=["join_group", "batched"])
+    ap.add_argument("--workload", default="join_group", choices=["join_group", "batched", "served"])
+    ap.add_argument("--rates", default="200,1000,5000")
+    ap.add_argument("--serve-seconds", type=float, default=1.5)
+    ap.add_argument("--order-rows", type=int, default=150_000_000)
+    ap.add_argument("--budget-gb", type=int, default=32)
     ap.add_argument("--plans", type=int, default=256)
     ap.add_argument("--max-fact", type=int, default=20_000_000)
     args = ap.parse_args()
     rank, ws, dist = dist_init(args.gpus)
-    if args.workload == "batched" and args.impl == "gb300":
-        line = run_batched(args)
+    if args.workload in ("batched", "served") and args.impl == "gb300":
+        line = run_batched(args) if args.workload == "batched" else run_served(args)
         if rank == 0:
             print(json.dumps(line))
         return

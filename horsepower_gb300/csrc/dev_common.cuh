@@ -106,6 +106,70 @@ __device__ __forceinline__ unsigned long long lookback_exclusive(unsigned long l
     return excl;
 }
 
+// lookback_exclusive restricted to the tiles [first, t) (a segmented scan
+// restarts at `first`)
+__device__ __forceinline__ unsigned long long lookback_seg(unsigned long long* status, long long t, long long first,
+                                                           unsigned long long agg, unsigned* derr) {
+    const unsigned lane = lane_id();
+    if (t == first) {
+        if (lane == 0) st_release(&status[t], LB_INC | agg);
+        return 0;
+    }
+    if (lane == 0) st_release(&status[t], LB_AGG | agg);
+    unsigned long long excl = 0;
+    long long base = t - 1, spins = 0;
+    for (;;) {
+        long long j = base - (long long)lane;
+        unsigned long long s = (j >= first) ? ld_acquire(&status[j]) : LB_INC;
+        unsigned flag = (unsigned)(s >> 62);
+        unsigned inc = __ballot_sync(0xffffffffu, flag == 2);
+        unsigned notready = __ballot_sync(0xffffffffu, flag == 0);
+        int stop = inc ? __ffs(inc) - 1 : 31;
+        unsigned upto = stop == 31 ? 0xffffffffu : ((1u << (stop + 1)) - 1u);
+        if (notready & upto) {
+            if (++spins > SPIN_LIMIT) {
+                if (lane == 0) flag_error(derr, DERR_TIMEOUT);
+                break;
+            }
+            continue;
+        }
+        unsigned long long v = ((int)lane <= stop && j >= first) ? (s & LB_MASK) : 0;
+        excl += warp_sum(v);
+        if (inc) break;
+        base -= 32;
+    }
+    if (lane == 0) st_release(&status[t], LB_INC | (excl + agg));
+    return excl;
+}
+
+// Look-back along one chain of status words (status[j * stride] for tiles j
+// in [first, t)), one thread per chain: the per-digit prefixes of the radix
+// passes.
+__device__ __forceinline__ unsigned long long chain_lookback(unsigned long long* status, size_t stride, long long t,
+                                                             long long first, unsigned long long c, unsigned* derr) {
+    unsigned long long* st = status + (size_t)t * stride;
+    if (t == first) {
+        st_release(st, LB_INC | c);
+        return 0;
+    }
+    st_release(st, LB_AGG | c);
+    unsigned long long excl = 0;
+    long long j = t - 1, spins = 0;
+    while (j >= first) {
+        unsigned long long sv = ld_acquire(status + (size_t)j * stride);
+        unsigned long long f = sv >> 62;
+        if (f == 0) {
+            if (++spins > SPIN_LIMIT) { flag_error(derr, DERR_TIMEOUT); break; }
+            continue;
+        }
+        excl += sv & LB_MASK;
+        if (f == 2) break;
+        j--;
+    }
+    st_release(st, LB_INC | (excl + c));
+    return excl;
+}
+
 // ---- fixed-order deterministic tile sum (used by @sum/@avg and every
 // segmented sum).  A chunk of up to TILE_SUM = 4096 elements is summed as:
 //   lane t (0..255) accumulates e[t], e[t+256], ..., e[t+3840] in order

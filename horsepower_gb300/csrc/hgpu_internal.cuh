@@ -55,6 +55,13 @@ I sync();
 // arenas
 void* dalloc(size_t bytes);                    // output arena; nullptr when exhausted
 bool dshrink(void* p, size_t new_bytes);       // shrink the LAST output allocation
+
+// autotuner knobs (hgpuSetTuning)
+extern int g_tile_rows;                         // rows per lane of the tiled probe kernels: 8, 16, 32
+void set_hash_load_factor(double f);
+double get_hash_load_factor();
+void set_radix_digit_bits(int b);
+int get_radix_digit_bits();
 long long out_mark();                          // output-arena cursor (for undoing a failed call)
 void out_rewind(long long m);
 void* salloc(size_t bytes);                    // scratch arena

@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <climits>
 #include <cstring>
+#include <map>
 #include <vector>
 
 #include "dev_common.cuh"
@@ -64,36 +65,14 @@ __device__ __forceinline__ int plan_of_tile(const long long* tile_first, int np,
     return lo;
 }
 
-// decoupled look-back restricted to the tiles [first, t) of one plan
-__device__ __forceinline__ unsigned long long lookback_seg(unsigned long long* status, long long t, long long first,
-                                                          unsigned long long agg, unsigned* derr) {
-    const unsigned lane = lane_id();
-    if (t == first) {
-        if (lane == 0) st_release(&status[t], LB_INC | agg);
-        return 0;
-    }
-    if (lane == 0) st_release(&status[t], LB_AGG | agg);
-    unsigned long long excl = 0;
-    long long base = t - 1, spins = 0;
-    for (;;) {
-        long long j = base - (long long)lane;
-        unsigned long long s = (j >= first) ? ld_acquire(&status[j]) : LB_INC;
-        unsigned flag = (unsigned)(s >> 62);
-        unsigned inc = __ballot_sync(0xffffffffu, flag == 2);
-        unsigned notready = __ballot_sync(0xffffffffu, flag == 0);
-        int stop = inc ? __ffs(inc) - 1 : 31;
-        unsigned upto = stop == 31 ? 0xffffffffu : ((1u << (stop + 1)) - 1u);
-        if (notready & upto) {
-            if (++spins > SPIN_LIMIT) { if (lane == 0) flag_error(derr, DERR_TIMEOUT); break; }
-            continue;
-        }
-        unsigned long long v = ((int)lane <= stop && j >= first) ? (s & LB_MASK) : 0;
-        excl += warp_sum(v);
-        if (inc) break;
-        base -= 32;
-    }
-    if (lane == 0) st_release(&status[t], LB_INC | (excl + agg));
-    return excl;
+// cp.async global -> shared, 4 bytes (holds no register while in flight)
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
 // ---------------------------------------------------------------- stage 0/1
@@ -112,7 +91,15 @@ __global__ void k_b_minmax(const DPlan* __restrict__ P, const long long* __restr
         long long q = __shfl_xor_sync(0xffffffffu, a, o); a = q < a ? q : a;
         long long r = __shfl_xor_sync(0xffffffffu, b, o); b = r > b ? r : b;
     }
-    if (lane_id() == 0) { atomicMin(&mm[2 * p], a); atomicMax(&mm[2 * p + 1], b); }
+    // one atomic pair per block: per-warp atomics on a plan's two words serialise
+    __shared__ long long wa[8], wb[8];
+    if (lane_id() == 0) { wa[threadIdx.x >> 5] = a; wb[threadIdx.x >> 5] = b; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) { a = wa[w] < a ? wa[w] : a; b = wb[w] > b ? wb[w] : b; }
+        atomicMin(&mm[2 * p], a);
+        atomicMax(&mm[2 * p + 1], b);
+    }
 }
 
 // dimension rows inside the date window set their key's presence bit; nsel
@@ -134,18 +121,31 @@ __global__ void k_b_build(const DPlan* __restrict__ P, const long long* __restri
             cnt++;
         }
     }
+    __shared__ unsigned wc[8];
     cnt = warp_sum(cnt);
-    if (lane_id() == 0 && cnt) atomicAdd(&nsel[p], (unsigned long long)cnt);
+    if (lane_id() == 0) wc[threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned c = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) c += wc[w];
+        if (c) atomicAdd(&nsel[p], (unsigned long long)c);
+    }
 }
 
 // ---------------------------------------------------------------- stage 2
-// probe: matched fact rows of each plan, compacted in row order
+// probe: matched fact rows of each plan, compacted in row order.  A tile is
+// 256 x R fact rows (R, 8 to 32, is the autotuner's tile knob); each warp
+// owns 32 x R consecutive rows and takes its output offset from its own
+// look-back over the plan's warp sub-tiles, with no block barrier.
+template <int R>
 __global__ void __launch_bounds__(256) k_b_probe(const DPlan* __restrict__ P, const long long* __restrict__ tile_first,
                                                  int np, unsigned* __restrict__ fi, unsigned long long* status,
                                                  unsigned* ticket, unsigned long long* __restrict__ mcount,
                                                  unsigned* derr) {
-    __shared__ unsigned warp_tot[8];
-    __shared__ unsigned long long tile_off;
+    constexpr long long SUB = 32LL * R;
+    extern __shared__ unsigned bp_smem[];
+    unsigned(*koff)[256] = reinterpret_cast<unsigned(*)[256]>(bp_smem);            // key - kmin, NONE when out of range
+    unsigned(*word)[256] = reinterpret_cast<unsigned(*)[256]>(bp_smem + R * 256);  // presence word of the key
     __shared__ long long tile_id;
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) tile_id = atomicAdd(ticket, 1u);
@@ -153,40 +153,179 @@ __global__ void __launch_bounds__(256) k_b_probe(const DPlan* __restrict__ P, co
     const long long t = tile_id;
     const int p = plan_of_tile(tile_first, np, t);
     const DPlan& q = P[p];
-    const long long first = tile_first[p];
-    const long long base = (t - first) * BT + (long long)warp * 512;
+    const long long sub = t * 8 + warp, first = tile_first[p] * 8;
+    const long long base = (sub - first) * SUB;  // plan-relative first row of the sub-tile
+    // keys, then their presence words, fetched by cp.async into the thread's
+    // own shared-memory column: all R loads of a group in flight together
+    constexpr unsigned NONE = 0xffffffffu;
+    const unsigned me = threadIdx.x;
+    const long long nf = q.nf;
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+        long long i = base + k * 32 + lane;
+        if (i < nf) cp_async4(&koff[k][me], q.fk + i);
+    }
+    cp_async_wait_all();
+    const unsigned long long range = (unsigned long long)(q.kmax - q.kmin);  // < 2^31 (host check)
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+        long long i = base + k * 32 + lane;
+        long long v = i < nf ? (long long)(int)koff[k][me] - q.kmin : -1;
+        unsigned o = (q.kmax >= q.kmin && (unsigned long long)v <= range) ? (unsigned)v : NONE;
+        koff[k][me] = o;
+        if (o != NONE) cp_async4(&word[k][me], q.bitmap + (o >> 5));
+    }
+    cp_async_wait_all();
     unsigned hits = 0;  // bit k: round k matched
     unsigned cnt = 0;
 #pragma unroll
-    for (int k = 0; k < 16; k++) {
+    for (int k = 0; k < R; k++) {
+        unsigned o = koff[k][me];
+        bool m = o != NONE && ((word[k][me] >> (o & 31)) & 1u);
+        hits |= (unsigned)m << k;
+        cnt += __popc(__ballot_sync(0xffffffffu, m));
+    }
+    unsigned long long off = lookback_seg(status, sub, first, cnt, derr);
+    if (lane == 0 && base < q.nf && base + SUB >= q.nf) mcount[p] = off + cnt;  // the plan's last sub-tile
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+        bool sel = (hits >> k) & 1u;
+        unsigned bal = __ballot_sync(0xffffffffu, sel);
+        if (sel) fi[q.fact_off + off + __popc(bal & lanemask_lt())] = (unsigned)(base + k * 32 + lane);
+        off += __popc(bal);
+    }
+}
+
+// ---------------------------------------------------------------- shared tables
+// Plans over the same dimension and fact columns (a served stream's join
+// requests) share one probe: the dimension's dates are stored by key once,
+// every fact row looks up the date of its dimension row once, and each plan
+// then only selects the rows whose date lies in its window.  With unique
+// keys the selected rows are exactly the rows the plan's own probe matches,
+// in the same (fact-row) order.
+constexpr unsigned short NO_DATE = 0xffffu;
+
+__global__ void k_sh_minmax(const int* __restrict__ a, const int* __restrict__ b, long long n, long long* mm) {
+    long long amin = LLONG_MAX, amax = LLONG_MIN, bmin = LLONG_MAX, bmax = LLONG_MIN;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        long long x = a[i], y = b[i];
+        amin = x < amin ? x : amin; amax = x > amax ? x : amax;
+        bmin = y < bmin ? y : bmin; bmax = y > bmax ? y : bmax;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        long long q;
+        q = __shfl_xor_sync(0xffffffffu, amin, o); amin = q < amin ? q : amin;
+        q = __shfl_xor_sync(0xffffffffu, amax, o); amax = q > amax ? q : amax;
+        q = __shfl_xor_sync(0xffffffffu, bmin, o); bmin = q < bmin ? q : bmin;
+        q = __shfl_xor_sync(0xffffffffu, bmax, o); bmax = q > bmax ? q : bmax;
+    }
+    if (lane_id() == 0) {
+        atomicMin(&mm[0], amin); atomicMax(&mm[1], amax);
+        atomicMin(&mm[2], bmin); atomicMax(&mm[3], bmax);
+    }
+}
+
+// date offset by key (NO_DATE where no dimension row has the key), a
+// repeated-key flag, and the histogram of the dimension's date offsets
+__global__ void k_sh_build(const int* __restrict__ pk, const int* __restrict__ date, long long nd, long long kmin,
+                           int dmin, int drange, unsigned short* __restrict__ dt, unsigned* __restrict__ dimhist,
+                           unsigned* dup) {
+    extern __shared__ unsigned sh_hist[];
+    const bool local = drange <= 8192;
+    if (local) for (int i = threadIdx.x; i < drange; i += blockDim.x) sh_hist[i] = 0;
+    __syncthreads();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nd; i += (long long)gridDim.x * blockDim.x) {
+        long long k = (long long)pk[i] - kmin;
+        unsigned short dv = (unsigned short)(date[i] - dmin);
+        unsigned short old = atomicCAS(dt + k, NO_DATE, dv);
+        if (old != NO_DATE) atomicOr(dup, 1u);
+        if (local) atomicAdd(&sh_hist[dv], 1u);
+        else atomicAdd(&dimhist[dv], 1u);
+    }
+    __syncthreads();
+    if (local)
+        for (int i = threadIdx.x; i < drange; i += blockDim.x)
+            if (sh_hist[i]) atomicAdd(&dimhist[i], sh_hist[i]);
+}
+
+// date offset of every fact row's dimension row, and their histogram
+__global__ void k_sh_probe(const int* __restrict__ fk, long long nf, long long kmin, unsigned long long kspan,
+                           const unsigned short* __restrict__ dt, int drange, unsigned short* __restrict__ dd,
+                           unsigned* __restrict__ facthist) {
+    extern __shared__ unsigned sh_hist[];
+    const bool local = drange <= 8192;
+    if (local) for (int i = threadIdx.x; i < drange; i += blockDim.x) sh_hist[i] = 0;
+    __syncthreads();
+    for (long long i0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) * 4; i0 < nf;
+         i0 += (long long)gridDim.x * blockDim.x * 4) {
+        unsigned short d[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            long long i = i0 + u;
+            d[u] = NO_DATE;
+            if (i < nf) {
+                unsigned long long v = (unsigned long long)((long long)__ldcs(fk + i) - kmin);
+                if (v < kspan) d[u] = __ldg(dt + v);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (i0 + u < nf) {
+                dd[i0 + u] = d[u];
+                if (d[u] != NO_DATE) {
+                    if (local) atomicAdd(&sh_hist[d[u]], 1u);
+                    else atomicAdd(&facthist[d[u]], 1u);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (local)
+        for (int i = threadIdx.x; i < drange; i += blockDim.x)
+            if (sh_hist[i]) atomicAdd(&facthist[i], sh_hist[i]);
+}
+
+struct CPlan {
+    const unsigned short* dd;
+    long long nf;
+    int dlo, dhi;        // selected date offsets [dlo, dhi)
+    long long fact_off;  // the plan's region of the matched-row buffer
+    int p;               // index in the batch
+};
+
+// each plan's rows with a date offset in its window, compacted in row order
+// (the layout and per-warp look-back of k_b_probe)
+template <int R>
+__global__ void __launch_bounds__(256) k_sh_select(const CPlan* __restrict__ P, const long long* __restrict__ tile_first,
+                                                   int np, unsigned* __restrict__ fi, unsigned long long* status,
+                                                   unsigned* ticket, unsigned long long* __restrict__ mcount,
+                                                   unsigned* derr) {
+    constexpr long long SUB = 32LL * R;
+    __shared__ long long tile_id;
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) tile_id = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const long long t = tile_id;
+    const int c = plan_of_tile(tile_first, np, t);
+    const CPlan& q = P[c];
+    const long long sub = t * 8 + warp, first = tile_first[c] * 8;
+    const long long base = (sub - first) * SUB;
+    unsigned hits = 0, cnt = 0;
+#pragma unroll
+    for (int k = 0; k < R; k++) {
         long long i = base + k * 32 + lane;
         bool m = false;
         if (i < q.nf) {
-            long long v = (long long)__ldcs(q.fk + i);
-            if (v >= q.kmin && v <= q.kmax) {
-                long long b = v - q.kmin;
-                m = (__ldg(q.bitmap + (b >> 5)) >> (b & 31)) & 1u;
-            }
+            int d = (int)__ldcs(q.dd + i);
+            m = d >= q.dlo && d < q.dhi;  // NO_DATE is above every window
         }
         hits |= (unsigned)m << k;
         cnt += __popc(__ballot_sync(0xffffffffu, m));
     }
-    if (lane == 0) warp_tot[warp] = cnt;
-    __syncthreads();
-    if (warp == 0) {
-        unsigned v = lane < 8 ? warp_tot[lane] : 0;
-        unsigned agg = warp_sum(v);
-        unsigned long long excl = lookback_seg(status, t, first, agg, derr);
-        if (lane == 0) {
-            tile_off = excl;
-            if ((t - first + 1) * BT >= q.nf) mcount[p] = excl + agg;  // the plan's last tile
-        }
-    }
-    __syncthreads();
-    unsigned long long off = tile_off;
-    for (unsigned w = 0; w < warp; w++) off += warp_tot[w];
+    unsigned long long off = lookback_seg(status, sub, first, cnt, derr);
+    if (lane == 0 && base < q.nf && base + SUB >= q.nf) mcount[q.p] = off + cnt;
 #pragma unroll
-    for (int k = 0; k < 16; k++) {
+    for (int k = 0; k < R; k++) {
         bool sel = (hits >> k) & 1u;
         unsigned bal = __ballot_sync(0xffffffffu, sel);
         if (sel) fi[q.fact_off + off + __popc(bal & lanemask_lt())] = (unsigned)(base + k * 32 + lane);
@@ -210,21 +349,59 @@ __global__ void k_b_gather(const DPlan* __restrict__ P, const long long* __restr
                            const unsigned* __restrict__ fi, const unsigned long long* __restrict__ mcount,
                            const long long* __restrict__ moff, unsigned* __restrict__ code, double* __restrict__ qty,
                            double* __restrict__ price, double* __restrict__ disc) {
+    // codes seen by this block, merged into the plan's presence bits once
+    // at the end (a few atomics per block instead of a few per warp)
+    __shared__ unsigned seen[2048];
+    for (int k = threadIdx.x; k < 2048; k += blockDim.x) seen[k] = 0;
+    __syncthreads();
     const long long t = blockIdx.x;
     const int p = plan_of_tile(tile_first, np, t);
     const DPlan& q = P[p];
     const long long r0 = (t - tile_first[p]) * BT;
     const long long m = (long long)mcount[p], o = moff[p];
-    for (long long i = r0 + threadIdx.x; i < r0 + BT && i < m; i += blockDim.x) {
-        unsigned r = fi[q.fact_off + i];
-        unsigned c = ((unsigned)(uint8_t)q.flag[r] << 8) | (unsigned)(uint8_t)q.status[r];
-        code[o + i] = c;
-        qty[o + i] = q.qty[r];
-        price[o + i] = q.price[r];
-        disc[o + i] = q.disc[r];
-        unsigned peers = __match_any_sync(__activemask(), c);
-        if ((int)lane_id() == __ffs(peers) - 1) atomicOr(&q.codebits[c >> 5], 1u << (c & 31));
+    const long long end = (r0 + BT < m) ? r0 + BT : m;
+    const unsigned* __restrict__ rows = fi + q.fact_off;
+    const int8_t* __restrict__ fl = q.flag;
+    const int8_t* __restrict__ stt = q.status;
+    const double* __restrict__ cq = q.qty;
+    const double* __restrict__ cp = q.price;
+    const double* __restrict__ cd = q.disc;
+    // 4 rows per thread per round, all 24 loads issued before any store
+    for (long long i0 = r0 + threadIdx.x; i0 < end; i0 += 4 * (long long)blockDim.x) {
+        unsigned r[4];
+        bool v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            v[u] = i0 + u * (long long)blockDim.x < end;
+            r[u] = v[u] ? rows[i0 + u * blockDim.x] : 0u;
+        }
+        unsigned c[4];
+        double a[4], b[4], d[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (v[u]) {
+                c[u] = ((unsigned)(uint8_t)fl[r[u]] << 8) | (unsigned)(uint8_t)stt[r[u]];
+                a[u] = cq[r[u]];
+                b[u] = cp[r[u]];
+                d[u] = cd[r[u]];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (v[u]) {
+                long long i = o + i0 + u * (long long)blockDim.x;
+                code[i] = c[u];
+                qty[i] = a[u];
+                price[i] = b[u];
+                disc[i] = d[u];
+                unsigned bit = 1u << (c[u] & 31);
+                if (!(seen[c[u] >> 5] & bit)) atomicOr(&seen[c[u] >> 5], bit);
+            }
+        }
     }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 2048; k += blockDim.x)
+        if (seen[k]) atomicOr(&q.codebits[k], seen[k]);
 }
 
 // code -> dense group id (ascending codes), one block per plan
@@ -323,25 +500,7 @@ __global__ void __launch_bounds__(256) k_b_sort(const DPlan* __restrict__ P, con
         const int d = threadIdx.x;
         unsigned c = 0;
         for (int ww = 0; ww < 8; ww++) { unsigned h = whist[ww][d]; whist[ww][d] = c; c += h; }
-        unsigned long long* st = status + (size_t)t * 256 + d;
-        unsigned long long excl = 0;
-        if (t == first) st_release(st, LB_INC | c);
-        else {
-            st_release(st, LB_AGG | c);
-            long long j = t - 1, spins = 0;
-            while (j >= first) {
-                unsigned long long s = ld_acquire(status + (size_t)j * 256 + d);
-                unsigned long long f = s >> 62;
-                if (f == 0) {
-                    if (++spins > SPIN_LIMIT) { flag_error(derr, DERR_TIMEOUT); break; }
-                    continue;
-                }
-                excl += s & LB_MASK;
-                if (f == 2) break;
-                j--;
-            }
-            st_release(st, LB_INC | (excl + c));
-        }
+        const unsigned long long excl = chain_lookback(status + d, 256, t, first, c, derr);
         dbase[d] = (unsigned long long)o + bucket[p * 256 + d] + excl;
     }
     __syncthreads();
@@ -399,7 +558,7 @@ static V0 int_scalar(I x) {
 // One plan through the builtins, call by call, exactly as the interpreter
 // runs it.  Plans the batched kernels do not cover take this path, so every
 // plan of a batch gets the builtins' own result.
-static I plan_through_builtins(const hgpuJoinGroupPlan& q, hgpuJoinGroupResult* r) {
+I plan_through_builtins(const hgpuJoinGroupPlan& q, hgpuJoinGroupResult* r) {
     const L mark = getHeapOffset();
     I rc = 0;
     V0 pk = dev_col(q.dim_pk, H_I, q.ndim), date = dev_col(q.dim_date, H_I, q.ndim);
@@ -461,6 +620,99 @@ done:
     return rc;
 }
 
+// Finds the plans that share all their tables with another plan of the
+// batch, runs one probe per distinct table set, and describes each such
+// plan's window selection (cplans).  Marks plans for the builtin path where
+// the shared result could differ from the plan's own builtins: a repeated
+// dimension key, or a compressed key column longer than the fact table.
+// Table sets whose key range is too wide for a direct date table, or whose
+// dates span more than 65,534 days, are left to the per-plan path.
+static I shared_probe(const hgpuJoinGroupPlan* plans, int np, std::vector<char>* shared, std::vector<char>* plain,
+                      std::vector<unsigned long long>* sel, std::vector<unsigned long long>* mexp,
+                      std::vector<CPlan>* cplans) {
+    std::map<std::vector<const void*>, std::vector<int>> sets;
+    for (int p = 0; p < np; p++) {
+        const hgpuJoinGroupPlan& q = plans[p];
+        std::vector<const void*> k = {q.dim_pk, q.dim_date, q.fk, q.flag, q.status, q.qty, q.price, q.disc,
+                                      (const void*)(intptr_t)q.ndim, (const void*)(intptr_t)q.nfact};
+        sets[k].push_back(p);
+    }
+    std::vector<std::vector<int>> groups;
+    for (auto& kv : sets)
+        if (kv.second.size() >= 2 && plans[kv.second[0]].ndim > 0 && plans[kv.second[0]].nfact > 0)
+            groups.push_back(kv.second);
+    if (groups.empty()) return 0;
+    const int ng = (int)groups.size();
+    long long* mm = (long long*)salloc((size_t)ng * 32);
+    if (!mm) return E_DEVICE_OOM;
+    std::vector<long long> init(4 * ng);
+    for (int g = 0; g < ng; g++) { init[4 * g] = init[4 * g + 2] = LLONG_MAX; init[4 * g + 1] = init[4 * g + 3] = LLONG_MIN; }
+    HG_CU(cudaMemcpyAsync(mm, init.data(), (size_t)ng * 32, cudaMemcpyHostToDevice, g_stream));
+    for (int g = 0; g < ng; g++) {
+        const hgpuJoinGroupPlan& q = plans[groups[g][0]];
+        unsigned gr = grid_for(q.ndim, 256);
+        if (gr > (unsigned)g_sms * 8) gr = g_sms * 8;
+        HG_LAUNCH("sh_minmax", gr, 256, 0, k_sh_minmax, q.dim_pk, q.dim_date, q.ndim, mm + 4 * g);
+    }
+    std::vector<long long> hmm(4 * ng);
+    HG_CU(cudaMemcpyAsync(hmm.data(), mm, (size_t)ng * 32, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));
+    struct Built { int g; long long kmin; unsigned long long kspan; int dmin, drange; unsigned* dimhist; unsigned* facthist;
+                   unsigned* dup; unsigned short* dd; };
+    std::vector<Built> built;
+    for (int g = 0; g < ng; g++) {
+        const hgpuJoinGroupPlan& q = plans[groups[g][0]];
+        long long kmin = hmm[4 * g], kmax = hmm[4 * g + 1], dmin = hmm[4 * g + 2], dmax = hmm[4 * g + 3];
+        unsigned long long kspan = (unsigned long long)(kmax - kmin) + 1, drange = (unsigned long long)(dmax - dmin) + 1;
+        if (kspan > 64ull * (unsigned long long)(q.ndim > 1024 ? q.ndim : 1024) || kspan >= (1ull << 31) ||
+            drange > 65535ull)
+            continue;
+        unsigned short* dt = (unsigned short*)salloc(kspan * 2);
+        unsigned* hists = (unsigned*)salloc(drange * 8 + 16);
+        unsigned short* dd = (unsigned short*)salloc((size_t)q.nfact * 2);
+        if (!dt || !hists || !dd) return E_DEVICE_OOM;
+        HG_CU(cudaMemsetAsync(dt, 0xff, kspan * 2, g_stream));
+        HG_CU(cudaMemsetAsync(hists, 0, drange * 8 + 16, g_stream));
+        Built b{g, kmin, kspan, (int)dmin, (int)drange, hists, hists + drange, hists + 2 * drange, dd};
+        const size_t smem = drange <= 8192 ? drange * 4 : 0;
+        unsigned gr = grid_for(q.ndim, 256);
+        if (gr > (unsigned)g_sms * 8) gr = g_sms * 8;
+        HG_LAUNCH("sh_build", gr, 256, smem, k_sh_build, q.dim_pk, q.dim_date, q.ndim, kmin, b.dmin, b.drange, dt,
+                  b.dimhist, b.dup);
+        gr = grid_for((q.nfact + 3) / 4, 256);
+        if (gr > (unsigned)g_sms * 8) gr = g_sms * 8;
+        HG_LAUNCH("sh_probe", gr, 256, smem, k_sh_probe, q.fk, q.nfact, kmin, kspan, (const unsigned short*)dt,
+                  b.drange, dd, b.facthist);
+        built.push_back(b);
+    }
+    if (built.empty()) return 0;
+    for (Built& b : built) {
+        std::vector<unsigned> h((size_t)b.drange * 2 + 1);
+        HG_CU(cudaMemcpyAsync(h.data(), b.dimhist, ((size_t)b.drange * 2 + 1) * 4, cudaMemcpyDeviceToHost, g_stream));
+        HG_CHECK(check_device_errors());
+        std::vector<unsigned long long> cd(b.drange + 1, 0), cf(b.drange + 1, 0);
+        for (int i = 0; i < b.drange; i++) {
+            cd[i + 1] = cd[i] + h[i];
+            cf[i + 1] = cf[i] + h[b.drange + i];
+        }
+        const bool dup = h[2 * (size_t)b.drange] != 0;
+        for (int p : groups[b.g]) {
+            const hgpuJoinGroupPlan& q = plans[p];
+            if (dup) { (*plain)[p] = 1; continue; }
+            long long lo = (long long)q.lo - b.dmin, hi = (long long)q.hi - b.dmin;
+            lo = lo < 0 ? 0 : (lo > b.drange ? b.drange : lo);
+            hi = hi < 0 ? 0 : (hi > b.drange ? b.drange : hi);
+            if (hi < lo) hi = lo;
+            (*sel)[p] = cd[hi] - cd[lo];
+            if ((*sel)[p] > (unsigned long long)q.nfact) { (*plain)[p] = 1; continue; }
+            (*mexp)[p] = cf[hi] - cf[lo];
+            (*shared)[p] = 1;
+            cplans->push_back(CPlan{b.dd, q.nfact, (int)lo, (int)hi, 0, p});
+        }
+    }
+    return 0;
+}
+
 }  // namespace hg
 
 using namespace hg;
@@ -471,6 +723,8 @@ extern "C" I hgpuBatchJoinGroup(const hgpuJoinGroupPlan* plans, L nplans, hgpuJo
     const int np = (int)nplans;
     if (np <= 0) return 0;
     std::vector<DPlan> hp(np);
+    const int R = g_tile_rows;
+    const long long ptile = 256LL * R;  // fact rows per probe tile
     std::vector<long long> dtiles(np + 1), ftiles(np + 1);
     dtiles[0] = ftiles[0] = 0;
     long long fact_total = 0;
@@ -485,12 +739,28 @@ extern "C" I hgpuBatchJoinGroup(const hgpuJoinGroupPlan* plans, L nplans, hgpuJo
         d.fk = q.fk; d.flag = (const int8_t*)q.flag; d.status = (const int8_t*)q.status;
         d.qty = q.qty; d.price = q.price; d.disc = q.disc; d.nf = q.nfact;
         d.lo = q.lo; d.hi = q.hi;
-        d.fact_off = fact_total;
-        fact_total += q.nfact;
-        dtiles[p + 1] = dtiles[p] + (q.ndim + BT - 1) / BT;
-        ftiles[p + 1] = ftiles[p] + (q.nfact + BT - 1) / BT;
         out[p].status = 0;
         out[p].ngroups = 0;
+    }
+    std::vector<char> plain(np, 0);
+    // plans over the same tables: one shared probe, then a window selection each
+    std::vector<CPlan> cplans;
+    std::vector<long long> ctiles(1, 0);
+    std::vector<char> shared(np, 0);
+    std::vector<unsigned long long> sh_sel(np, 0), sh_m(np, 0);
+    HG_CHECK(shared_probe(plans, np, &shared, &plain, &sh_sel, &sh_m, &cplans));
+    for (int p = 0; p < np; p++) {
+        const hgpuJoinGroupPlan& q = plans[p];
+        DPlan& d = hp[p];
+        if (shared[p] || plain[p]) { d.nd = 0; d.nf = 0; }  // no per-plan build or probe
+        d.fact_off = fact_total;
+        fact_total += shared[p] ? (long long)sh_m[p] : (plain[p] ? 0 : q.nfact);
+        dtiles[p + 1] = dtiles[p] + (d.nd + BT - 1) / BT;
+        ftiles[p + 1] = ftiles[p] + (d.nf + ptile - 1) / ptile;
+    }
+    for (CPlan& c : cplans) {
+        c.fact_off = hp[c.p].fact_off;
+        ctiles.push_back(ctiles.back() + (c.nf + ptile - 1) / ptile);
     }
     // device copies of the plan table and tile maps
     DPlan* dP = (DPlan*)salloc(np * sizeof(DPlan));
@@ -508,7 +778,6 @@ extern "C" I hgpuBatchJoinGroup(const hgpuJoinGroupPlan* plans, L nplans, hgpuJo
     HG_CU(cudaMemsetAsync(dup, 0, np * 4, g_stream));
     if (dtiles[np] > 0) HG_LAUNCH("b_minmax", (unsigned)dtiles[np], 256, 0, k_b_minmax, dP, dT, np, mm);
     std::vector<long long> hmm(2 * np);
-    std::vector<char> plain(np, 0);
     HG_CU(cudaMemcpyAsync(hmm.data(), mm, np * 16, cudaMemcpyDeviceToHost, g_stream));
     HG_CU(cudaStreamSynchronize(g_stream));
     // presence bitmaps and code tables
@@ -517,7 +786,8 @@ extern "C" I hgpuBatchJoinGroup(const hgpuJoinGroupPlan* plans, L nplans, hgpuJo
         long long lo = hmm[2 * p], hi = hmm[2 * p + 1];
         if (hp[p].nd == 0) { lo = 0; hi = -1; }
         unsigned long long range = hi >= lo ? (unsigned long long)(hi - lo) + 1 : 0;
-        if (range > 64ull * (unsigned long long)(hp[p].nd > 1024 ? hp[p].nd : 1024) || range >= (1ull << 32)) {
+        if (!shared[p] && !plain[p] &&
+            (range > 64ull * (unsigned long long)(hp[p].nd > 1024 ? hp[p].nd : 1024) || range >= (1ull << 31))) {
             plain[p] = 1;  // too wide for a presence bitmap: no row is built or matched here
             lo = 0; hi = -1; range = 0;
             hp[p].nd = 0;
@@ -551,13 +821,40 @@ extern "C" I hgpuBatchJoinGroup(const hgpuJoinGroupPlan* plans, L nplans, hgpuJo
     unsigned* fi = (unsigned*)salloc((size_t)(fact_total > 0 ? fact_total : 1) * 4);
     unsigned long long* mcount = (unsigned long long*)salloc(np * 8 + 16);
     long long* moff = (long long*)salloc((np + 1) * 8);
-    char* st = (char*)salloc((size_t)ftiles[np] * 8 + 64);
+    char* st = (char*)salloc((size_t)ftiles[np] * 64 + 64);  // a status word per warp sub-tile, then the ticket
     if (!fi || !mcount || !moff || !st) return E_DEVICE_OOM;
     HG_CU(cudaMemsetAsync(mcount, 0, np * 8, g_stream));
-    HG_CU(cudaMemsetAsync(st, 0, (size_t)ftiles[np] * 8 + 64, g_stream));
-    if (ftiles[np] > 0)
-        HG_LAUNCH("b_probe", (unsigned)ftiles[np], 256, 0, k_b_probe, dP, fT, np, fi, (unsigned long long*)st,
-                  (unsigned*)(st + (size_t)ftiles[np] * 8), mcount, g_derr);
+    HG_CU(cudaMemsetAsync(st, 0, (size_t)ftiles[np] * 64 + 64, g_stream));
+    if (ftiles[np] > 0) {
+        unsigned long long* sw = (unsigned long long*)st;
+        unsigned* tk = (unsigned*)(st + (size_t)ftiles[np] * 64);
+        const unsigned nt = (unsigned)ftiles[np];
+        const size_t sm = (size_t)2 * R * 256 * 4;
+        static bool attr = false;
+        if (!attr) {
+            HG_CU(cudaFuncSetAttribute(k_b_probe<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 32 * 256 * 4));
+            attr = true;
+        }
+        if (R == 8) HG_LAUNCH("b_probe", nt, 256, sm, k_b_probe<8>, dP, fT, np, fi, sw, tk, mcount, g_derr);
+        else if (R == 32) HG_LAUNCH("b_probe", nt, 256, sm, k_b_probe<32>, dP, fT, np, fi, sw, tk, mcount, g_derr);
+        else HG_LAUNCH("b_probe", nt, 256, sm, k_b_probe<16>, dP, fT, np, fi, sw, tk, mcount, g_derr);
+    }
+    if (!cplans.empty() && ctiles.back() > 0) {
+        const int nc = (int)cplans.size();
+        CPlan* dC = (CPlan*)salloc(nc * sizeof(CPlan));
+        long long* cT = (long long*)salloc((nc + 1) * 8);
+        char* cst = (char*)salloc((size_t)ctiles.back() * 64 + 64);
+        if (!dC || !cT || !cst) return E_DEVICE_OOM;
+        HG_CU(cudaMemcpyAsync(dC, cplans.data(), nc * sizeof(CPlan), cudaMemcpyHostToDevice, g_stream));
+        HG_CU(cudaMemcpyAsync(cT, ctiles.data(), (nc + 1) * 8, cudaMemcpyHostToDevice, g_stream));
+        HG_CU(cudaMemsetAsync(cst, 0, (size_t)ctiles.back() * 64 + 64, g_stream));
+        unsigned long long* sw = (unsigned long long*)cst;
+        unsigned* tk = (unsigned*)(cst + (size_t)ctiles.back() * 64);
+        const unsigned nt = (unsigned)ctiles.back();
+        if (R == 8) HG_LAUNCH("sh_select", nt, 256, 0, k_sh_select<8>, dC, cT, nc, fi, sw, tk, mcount, g_derr);
+        else if (R == 32) HG_LAUNCH("sh_select", nt, 256, 0, k_sh_select<32>, dC, cT, nc, fi, sw, tk, mcount, g_derr);
+        else HG_LAUNCH("sh_select", nt, 256, 0, k_sh_select<16>, dC, cT, nc, fi, sw, tk, mcount, g_derr);
+    }
     HG_LAUNCH("b_offsets", 1, 32, 0, k_b_offsets, mcount, np, moff);
     // gather (over the fact tile map: a plan has at most as many matches as rows)
     std::vector<unsigned long long> hm(np);
@@ -571,8 +868,10 @@ extern "C" I hgpuBatchJoinGroup(const hgpuJoinGroupPlan* plans, L nplans, hgpuJo
     // compressed key column longer than the fact table makes @join_index
     // build on the fact side and emit rows in key-row order: both plans run
     // through the builtins instead.
-    for (int p = 0; p < np; p++)
+    for (int p = 0; p < np; p++) {
+        if (shared[p]) continue;  // checked by shared_probe
         if (hdup[p] || hsel[p] > (unsigned long long)hp[p].nf) plain[p] = 1;
+    }
     long long mtot = 0;
     std::vector<long long> mtiles(np + 1), hmoff(np + 1);
     mtiles[0] = 0;

@@ -7,12 +7,14 @@
 // selected the output aliases the input (copyV, :1513-1515).  pfnWhere
 // (:728-762) does the same writing i64 row numbers.
 //
-// GB300 kernel: one pass.  A tile is 4096 rows handled by 8 warps; each lane
-// reads its 16 mask bytes with one 128-bit load and counts them with popc;
-// the tile's offset comes from a decoupled look-back over tile status words;
-// each warp then walks its 512 rows in rounds of 32, and selected lanes write
-// to consecutive positions found with ballot/popc.  Values are only read for
-// selected rows, so a sparse mask reads a fraction of the value column.
+// GB300 kernels: a tile is 4096 rows handled by 8 warps; each lane reads its
+// 16 mask bytes with one 128-bit load and counts them with popc.  A count
+// pass writes the tiles' counts, one block scans them, and a scatter pass
+// re-reads the mask (1 byte a row) and writes each tile's selected rows from
+// its offset: each warp walks its 512 rows in rounds of 32, and selected
+// lanes write to consecutive positions found with ballot/popc.  Values are
+// only read for selected rows, so a sparse mask reads a fraction of the
+// value column.
 #include "dev_common.cuh"
 
 namespace hg {
@@ -37,46 +39,89 @@ __device__ __forceinline__ void copy_elem(const void* src, void* dst, long long 
     }
 }
 
-__global__ void __launch_bounds__(CT_THREADS) k_compact(const uint8_t* __restrict__ mask, long long n, CompactCols cols,
-                                                        unsigned long long* status, unsigned* ticket,
-                                                        unsigned long long* total, unsigned* derr) {
+// A lane's 16 mask bytes (rows base+lofs .. +15), as 0/1 bytes
+__device__ __forceinline__ uint4 load_mask16(const uint8_t* __restrict__ mask, long long n, long long base, int lofs) {
+    if (base + lofs + 16 <= n) return __ldcs(reinterpret_cast<const uint4*>(mask + base + lofs));
+    uint8_t b[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) b[k] = (base + lofs + k < n) ? (mask[base + lofs + k] != 0) : 0;
+    return *reinterpret_cast<uint4*>(b);
+}
+
+// pass 1: selected rows per 4096-row tile
+__global__ void __launch_bounds__(CT_THREADS) k_compact_count(const uint8_t* __restrict__ mask, long long n,
+                                                              unsigned* __restrict__ counts) {
+    __shared__ unsigned warp_tot[8];
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    const long long base = (long long)blockIdx.x * CT_TILE;
+    const uint4 m4 = load_mask16(mask, n, base, (int)threadIdx.x * 16);
+    unsigned c = warp_sum(__popc(m4.x) + __popc(m4.y) + __popc(m4.z) + __popc(m4.w));
+    if (lane == 0) warp_tot[warp] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned t = 0;
+        for (int w = 0; w < 8; w++) t += warp_tot[w];
+        counts[blockIdx.x] = t;
+    }
+}
+
+// exclusive scan of the tile counts in one block (tiles are 4096 rows, so
+// even 2^31 rows make only 2^19 counts); out[ntiles] = total
+__global__ void __launch_bounds__(1024) k_scan_counts(const unsigned* __restrict__ in, long long n,
+                                                      unsigned long long* __restrict__ out) {
+    __shared__ unsigned long long wsum[32];
+    __shared__ unsigned long long carry;
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (long long c0 = 0; c0 < n; c0 += 1024 * 8) {
+        const long long b = c0 + (long long)threadIdx.x * 8;
+        unsigned v[8];
+        unsigned long long s = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            v[k] = b + k < n ? in[b + k] : 0u;
+            s += v[k];
+        }
+        unsigned long long incl = warp_incl_scan64(s);
+        if (lane == 31) wsum[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long x = wsum[lane];
+            unsigned long long xi = warp_incl_scan64(x);
+            wsum[lane] = xi - x;
+        }
+        __syncthreads();
+        unsigned long long off = carry + wsum[warp] + (incl - s);
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            if (b + k < n) out[b + k] = off;
+            off += v[k];
+        }
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = off;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[n] = carry;
+}
+
+// pass 2: each tile writes its selected rows from its known offset; each warp
+// walks its 512 rows in rounds of 32 and selected lanes write to consecutive
+// positions found with ballot/popc
+__global__ void __launch_bounds__(CT_THREADS) k_compact_scatter(const uint8_t* __restrict__ mask, long long n,
+                                                                CompactCols cols,
+                                                                const unsigned long long* __restrict__ offs) {
     __shared__ __align__(16) uint8_t smask[CT_TILE];
     __shared__ unsigned warp_tot[8];
-    __shared__ unsigned long long tile_off;
-    __shared__ long long tile_id;
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) tile_id = atomicAdd(ticket, 1u);
-    __syncthreads();
-    const long long t = tile_id;
-    const long long base = t * CT_TILE;
-    // ---- phase 1: count (blocked: lane owns 16 consecutive mask bytes)
-    const int lofs = (int)warp * 512 + (int)lane * 16;
-    uint4 m4 = make_uint4(0, 0, 0, 0);
-    if (base + lofs + 16 <= n) {
-        m4 = __ldcs(reinterpret_cast<const uint4*>(mask + base + lofs));
-    } else {
-        uint8_t b[16];
-#pragma unroll
-        for (int k = 0; k < 16; k++) b[k] = (base + lofs + k < n) ? (mask[base + lofs + k] != 0) : 0;
-        m4 = *reinterpret_cast<uint4*>(b);
-    }
+    const long long base = (long long)blockIdx.x * CT_TILE;
+    const int lofs = (int)threadIdx.x * 16;
+    const uint4 m4 = load_mask16(mask, n, base, lofs);
     *reinterpret_cast<uint4*>(smask + lofs) = m4;
-    unsigned cnt = __popc(m4.x) + __popc(m4.y) + __popc(m4.z) + __popc(m4.w);
-    unsigned wsum = warp_sum(cnt);
-    if (lane == 0) warp_tot[warp] = wsum;
+    unsigned c = warp_sum(__popc(m4.x) + __popc(m4.y) + __popc(m4.z) + __popc(m4.w));
+    if (lane == 0) warp_tot[warp] = c;
     __syncthreads();
-    if (warp == 0) {
-        unsigned v = lane < 8 ? warp_tot[lane] : 0;
-        unsigned agg = warp_sum(v);
-        unsigned long long excl = lookback_exclusive(status, t, agg, derr);
-        if (lane == 0) {
-            tile_off = excl;
-            if (base + CT_TILE >= n) *total = excl + agg;  // last tile
-        }
-    }
-    __syncthreads();
-    // ---- phase 2: scatter (warp-striped rounds of 32 rows)
-    unsigned long long off = tile_off;
+    unsigned long long off = offs[blockIdx.x];
     for (unsigned w = 0; w < warp; w++) off += warp_tot[w];
     const int wbase = (int)warp * 512;
 #pragma unroll 4
@@ -87,26 +132,29 @@ __global__ void __launch_bounds__(CT_THREADS) k_compact(const uint8_t* __restric
         if (sel) {
             const long long o = (long long)off + __popc(bal & lanemask_lt());
             const long long i = base + li;
-            for (int c = 0; c < cols.ncol; c++) copy_elem(cols.src[c], cols.dst[c], i, o, cols.es[c]);
+            for (int c2 = 0; c2 < cols.ncol; c2++) copy_elem(cols.src[c2], cols.dst[c2], i, o, cols.es[c2]);
         }
         off += __popc(bal);
     }
 }
 
-// Runs the single-pass compaction; *count receives the number of selected rows.
+// Compaction in two passes with no dependence between tiles: count per
+// tile, scan the counts, scatter.  (A single pass with a decoupled look-back
+// across tiles measured several times slower here: the tiles waited on the
+// look-back chain rather than on memory.)  *count receives the number of
+// selected rows.
 static I compact(const uint8_t* mask, long long n, CompactCols& cols, long long* count) {
     long long ntiles = (n + CT_TILE - 1) / CT_TILE;
     if (ntiles == 0) { *count = 0; return 0; }
-    char* s = (char*)salloc(ntiles * 8 + 64);
-    if (!s) return E_DEVICE_OOM;
-    unsigned long long* status = (unsigned long long*)s;
-    unsigned* ticket = (unsigned*)(s + ntiles * 8);
-    unsigned long long* total = (unsigned long long*)(s + ntiles * 8 + 8);
-    HG_CU(cudaMemsetAsync(s, 0, ntiles * 8 + 64, g_stream));
-    HG_LAUNCH("compact", (unsigned)ntiles, CT_THREADS, 0, k_compact, mask, n, cols, status, ticket, total, g_derr);
+    unsigned* counts = (unsigned*)salloc(ntiles * 4);
+    unsigned long long* offs = (unsigned long long*)salloc((ntiles + 1) * 8);
+    if (!counts || !offs) return E_DEVICE_OOM;
+    HG_LAUNCH("compact_count", (unsigned)ntiles, CT_THREADS, 0, k_compact_count, mask, n, counts);
+    HG_LAUNCH("compact_scan", 1, 1024, 0, k_scan_counts, counts, ntiles, offs);
+    HG_LAUNCH("compact", (unsigned)ntiles, CT_THREADS, 0, k_compact_scatter, mask, n, cols, offs);
     HG_CHECK(last_launch_error());
     unsigned long long h = 0;
-    HG_CU(cudaMemcpyAsync(&h, total, 8, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaMemcpyAsync(&h, offs + ntiles, 8, cudaMemcpyDeviceToHost, g_stream));
     HG_CHECK(check_device_errors());  // synchronises
     *count = (long long)h;
     return 0;

@@ -32,8 +32,9 @@ namespace hg {
 
 I scan_exclusive(const unsigned* in, long long n, unsigned long long* out, unsigned long long* total_h);
 
-static double g_load_factor = 0.5;  // autotuned 0.5 - 0.8
-void set_hash_load_factor(double f) { g_load_factor = f < 0.25 ? 0.25 : (f > 0.9 ? 0.9 : f); }
+static double g_load_factor = 0.5;  // hash-table load factor, 0.5 - 0.8 (autotuner knob)
+void set_hash_load_factor(double f) { g_load_factor = f < 0.5 ? 0.5 : (f > 0.8 ? 0.8 : f); }
+double get_hash_load_factor() { return g_load_factor; }
 
 __device__ __forceinline__ unsigned long long fmix64(unsigned long long k) {
     k ^= k >> 33; k *= 0xff51afd7ed558ccdULL; k ^= k >> 33; k *= 0xc4ceb9fe1a85ec53ULL; k ^= k >> 33;
@@ -470,28 +471,29 @@ __device__ __forceinline__ bool key_stream(const void* p, int typ, long long i, 
     }
 }
 
-// One pass per 4096-row tile: each lane looks up 16 probe rows, 8 at a time
+// One pass per tile of 256 x R probe rows.  Each warp owns 32 x R
+// consecutive rows (lane l: rows l, l+32, ...) and looks them up 8 at a time
 // with all their reads in flight together (streamed key, presence-filter
-// bit, then the build row of the candidates), keeps the build rows in
-// registers, takes the tile's output offset from a decoupled look-back and
-// writes the (build row, probe row) pairs with ballot/popc.
-template <typename K>
-__global__ void __launch_bounds__(JT_THREADS, 4) k_join_probe(Table<K> t, LinearBuild lin, int mode,
-                                                              const void* __restrict__ y, int ytyp, long long n,
-                                                              long long* __restrict__ zb, long long* __restrict__ zp,
-                                                              unsigned long long* status, unsigned* ticket,
-                                                              unsigned long long* total, unsigned* derr) {
-    __shared__ unsigned warp_tot[8];
-    __shared__ unsigned long long tile_off;
+// bit, then the build row of the candidates), keeping the build rows in
+// registers.  Each warp then takes its output offset from its own decoupled
+// look-back over the warp sub-tiles (no block barrier: while one warp waits
+// for its prefix the others keep loading) and writes the (build row, probe
+// row) pairs with ballot/popc.  R (8, 16 or 32) is the autotuner's tile knob.
+template <typename K, int R>
+__global__ void __launch_bounds__(JT_THREADS, (R > 16 ? 2 : 4)) k_join_probe(
+    Table<K> t, LinearBuild lin, int mode, const void* __restrict__ y, int ytyp, long long n,
+    long long* __restrict__ zb, long long* __restrict__ zp, unsigned long long* status, unsigned* ticket,
+    unsigned long long* total, unsigned* derr) {
+    constexpr long long SUB = 32LL * R;  // rows per warp sub-tile
     __shared__ long long tile_id;
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) tile_id = atomicAdd(ticket, 1u);
     __syncthreads();
-    const long long t0 = tile_id, base = t0 * JT_TILE + (long long)warp * 512;
-    unsigned hit[16];  // build row of each of the lane's 16 probe rows, 0xffffffff if none
+    const long long sub = tile_id * (JT_THREADS / 32) + warp, base = sub * SUB;
+    unsigned hit[R];  // build row of each of the lane's R probe rows, 0xffffffff if none
     unsigned cnt = 0;
 #pragma unroll
-    for (int h8 = 0; h8 < 16; h8 += 8) {
+    for (int h8 = 0; h8 < R; h8 += 8) {
         K key[8];
         bool valid[8];
 #pragma unroll
@@ -519,23 +521,12 @@ __global__ void __launch_bounds__(JT_THREADS, 4) k_join_probe(Table<K> t, Linear
         }
     }
 #pragma unroll
-    for (int k = 0; k < 16; k++) cnt += __popc(__ballot_sync(0xffffffffu, hit[k] != 0xffffffffu));
-    if (lane == 0) warp_tot[warp] = cnt;
-    __syncthreads();
-    if (warp == 0) {
-        unsigned v = lane < 8 ? warp_tot[lane] : 0;
-        unsigned agg = warp_sum(v);
-        unsigned long long excl = lookback_exclusive(status, t0, agg, derr);
-        if (lane == 0) {
-            tile_off = excl;
-            if ((t0 + 1) * JT_TILE >= n) *total = excl + agg;
-        }
-    }
-    __syncthreads();
-    unsigned long long off = tile_off;
-    for (unsigned w = 0; w < warp; w++) off += warp_tot[w];
+    for (int k = 0; k < R; k++) cnt += __popc(__ballot_sync(0xffffffffu, hit[k] != 0xffffffffu));
+    const unsigned long long excl = lookback_exclusive(status, sub, cnt, derr);
+    if (lane == 0 && base < n && base + SUB >= n) *total = excl + cnt;  // the sub-tile holding row n-1
+    unsigned long long off = excl;
 #pragma unroll
-    for (int k = 0; k < 16; k++) {
+    for (int k = 0; k < R; k++) {
         bool sel = hit[k] != 0xffffffffu;
         unsigned bal = __ballot_sync(0xffffffffu, sel);
         if (sel) {
@@ -624,35 +615,147 @@ static I join_outputs(V z, long long m, long long** zb, long long** zp) {
     return 0;
 }
 
-// Probe in one pass with compaction; build rows and probe rows land in
-// scratch, then move into exact-size outputs.
+// Asynchronous copies global -> shared (cp.async, 4 bytes): a load that holds
+// no register while in flight, so a thread can keep all of its lookups
+// outstanding at once.  Each thread reads back only the slots it filled.
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+// Probe of a direct-addressed table with i32 keys (the common shape: a
+// dimension's dense integer key).  Same sub-tile layout, look-back and output
+// as k_join_probe, but every load is a cp.async into the thread's own
+// shared-memory column: the R keys, then their R presence-filter words, then
+// the R build rows of the candidates, each group all in flight together and
+// holding no registers, so occupancy stays high.
+template <int R>
+__global__ void __launch_bounds__(JT_THREADS, (R > 16 ? 2 : 4)) k_join_probe_direct(
+    Table<unsigned> t, const int* __restrict__ y, long long n, long long* __restrict__ zb,
+    long long* __restrict__ zp, unsigned long long* status, unsigned* ticket, unsigned long long* total,
+    unsigned* derr) {
+    constexpr long long SUB = 32LL * R;
+    constexpr unsigned NONE = 0xffffffffu;
+    extern __shared__ unsigned jp_smem[];
+    unsigned(*off)[JT_THREADS] = reinterpret_cast<unsigned(*)[JT_THREADS]>(jp_smem);  // key - kmin, NONE when out of range or no candidate
+    unsigned(*buf)[JT_THREADS] = reinterpret_cast<unsigned(*)[JT_THREADS]>(jp_smem + R * JT_THREADS);  // filter word, then build row
+    __shared__ long long tile_id;
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5, me = threadIdx.x;
+    if (threadIdx.x == 0) tile_id = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const long long sub = tile_id * (JT_THREADS / 32) + warp, base = sub * SUB;
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+        long long i = base + k * 32 + lane;
+        if (i < n) cp_async4(&off[k][me], y + i);
+    }
+    cp_async_wait_all();
+    const unsigned long long range = (unsigned long long)(t.kmax - t.kmin);  // < 2^31 in direct mode
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+        long long i = base + k * 32 + lane;
+        long long v = i < n ? (long long)(int)off[k][me] - t.kmin : -1;
+        unsigned o = (unsigned long long)v <= range ? (unsigned)v : NONE;
+        off[k][me] = o;
+        if (o != NONE) cp_async4(&buf[k][me], t.filter + (o >> 5));
+    }
+    cp_async_wait_all();
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+        unsigned o = off[k][me];
+        if (o != NONE) {
+            if ((buf[k][me] >> (o & 31)) & 1u) cp_async4(&buf[k][me], (const unsigned*)t.slots + o);
+            else off[k][me] = NONE;
+        }
+    }
+    cp_async_wait_all();
+    unsigned hit = 0, cnt = 0;
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+        bool h = off[k][me] != NONE && buf[k][me] != NONE;
+        hit |= (unsigned)h << k;
+        cnt += __popc(__ballot_sync(0xffffffffu, h));
+    }
+    const unsigned long long excl = lookback_exclusive(status, sub, cnt, derr);
+    if (lane == 0 && base < n && base + SUB >= n) *total = excl + cnt;  // the sub-tile holding row n-1
+    unsigned long long pos = excl;
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+        bool sel = (hit >> k) & 1u;
+        unsigned bal = __ballot_sync(0xffffffffu, sel);
+        if (sel) {
+            long long o = (long long)pos + __popc(bal & lanemask_lt());
+            __stcs(zb + o, (long long)buf[k][me]);
+            __stcs(zp + o, base + k * 32 + lane);
+        }
+        pos += __popc(bal);
+    }
+}
+
+// s: one status word per warp sub-tile, then the tile ticket and the total
+template <typename K, int R>
+static I launch_probe(const Table<K>& t, const LinearBuild& lin, int mode, const void* py, I ytyp, long long ny,
+                      long long* zb, long long* zp, char* s, long long ntiles) {
+    const long long nsub = ntiles * (JT_THREADS / 32);
+    unsigned long long* total = (unsigned long long*)(s + nsub * 8 + 8);
+    if constexpr (sizeof(K) == 4) {
+        if (mode == 0 && t.direct && ytyp == H_I) {
+            const size_t sm = (size_t)2 * R * JT_THREADS * 4;
+            static bool attr = false;
+            if (!attr) {
+                HG_CU(cudaFuncSetAttribute(k_join_probe_direct<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+                attr = true;
+            }
+            HG_LAUNCH("join_probe", (unsigned)ntiles, JT_THREADS, sm, k_join_probe_direct<R>, t, (const int*)py, ny,
+                      zb, zp, (unsigned long long*)s, (unsigned*)(s + nsub * 8), total, g_derr);
+            return last_launch_error();
+        }
+    }
+    HG_LAUNCH("join_probe", (unsigned)ntiles, JT_THREADS, 0, (k_join_probe<K, R>), t, lin, mode, py, (int)ytyp, ny, zb,
+              zp, (unsigned long long*)s, (unsigned*)(s + nsub * 8), total, g_derr);
+    return last_launch_error();
+}
+
+// Probe in one pass with compaction, writing straight into the two output
+// vectors: both are allocated for ny rows, the second (the last allocation)
+// shrinks to the m matches afterwards, the first keeps its unused tail until
+// the arena is rewound.  No copy of the pairs is made.
 template <typename K>
 static I join_probe_unique(V z, const Table<K>& t, const LinearBuild& lin, int mode, const void* py, I ytyp,
                            long long ny, long long nbuild) {
-    long long ntiles = (ny + JT_TILE - 1) / JT_TILE;
-    long long* sb = (long long*)salloc((size_t)(ny > 0 ? ny : 1) * 8);
-    long long* sp = (long long*)salloc((size_t)(ny > 0 ? ny : 1) * 8);
-    char* s = (char*)salloc(ntiles * 8 + 64);
-    if (!sb || !sp || !s) return E_DEVICE_OOM;
+    const int R = g_tile_rows;
+    const long long tile = (long long)JT_THREADS * R;
+    long long ntiles = (ny + tile - 1) / tile;
+    HG_CHECK(init_list(z, H_G, 2));
+    V0* e = host_nodes(z);
+    const size_t cap = (size_t)(ny > 1 ? ny : 2) * 8;
+    long long* zb = (long long*)dalloc(cap);
+    long long* zp = (long long*)dalloc(cap);
+    const long long sbytes = ntiles * (JT_THREADS / 32) * 8 + 64;
+    char* s = (char*)salloc(sbytes);
+    if (!zb || !zp || !s) return E_DEVICE_OOM;
     unsigned long long m = 0;
     if (ntiles > 0) {
-        HG_CU(cudaMemsetAsync(s, 0, ntiles * 8 + 64, g_stream));
-        unsigned long long* total = (unsigned long long*)(s + ntiles * 8 + 8);
-        HG_LAUNCH("join_probe", (unsigned)ntiles, JT_THREADS, 0, k_join_probe<K>, t, lin, mode, py, (int)ytyp, ny,
-                  sb, sp, (unsigned long long*)s, (unsigned*)(s + ntiles * 8), total, g_derr);
-        HG_CHECK(last_launch_error());
-        HG_CU(cudaMemcpyAsync(&m, total, 8, cudaMemcpyDeviceToHost, g_stream));
+        HG_CU(cudaMemsetAsync(s, 0, sbytes, g_stream));
+        if (R == 8) HG_CHECK((launch_probe<K, 8>(t, lin, mode, py, ytyp, ny, zb, zp, s, ntiles)));
+        else if (R == 32) HG_CHECK((launch_probe<K, 32>(t, lin, mode, py, ytyp, ny, zb, zp, s, ntiles)));
+        else HG_CHECK((launch_probe<K, 16>(t, lin, mode, py, ytyp, ny, zb, zp, s, ntiles)));
+        HG_CU(cudaMemcpyAsync(&m, s + sbytes - 56, 8, cudaMemcpyDeviceToHost, g_stream));
         HG_CHECK(check_device_errors());
     }
-    long long *zb, *zp;
-    HG_CHECK(join_outputs(z, (long long)m, &zb, &zp));
-    V0* e = host_nodes(z);
-    if (m > 0) {
-        HG_CU(cudaMemcpyAsync(zb, sb, m * 8, cudaMemcpyDeviceToDevice, g_stream));
-        HG_CU(cudaMemcpyAsync(zp, sp, m * 8, cudaMemcpyDeviceToDevice, g_stream));
+    dshrink(zp, (size_t)(m > 1 ? m : 1) * 8);
+    long long* outs[2] = {zb, zp};
+    for (int i = 0; i < 2; i++) {
+        e[i].typ = H_L;
+        e[i].len = (L)m;
+        e[i].g = m > 1 ? (G)outs[i] : (G)&e[i].b;
+        e[i].i64 = 0;
+        HG_CHECK(finish_out(&e[i], outs[i]));
     }
-    HG_CHECK(finish_out(&e[0], zb));
-    HG_CHECK(finish_out(&e[1], zp));
     register_bound(e[0].g, e[0].len, nbuild);
     register_bound(e[1].g, e[1].len, ny);
     return 0;

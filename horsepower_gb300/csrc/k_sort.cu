@@ -36,8 +36,9 @@ I compact_rows(const uint8_t* mask, long long n, long long* out, long long* coun
 I scan_exclusive(const unsigned* in, long long n, unsigned long long* out, unsigned long long* total_h);
 
 constexpr int RS_THREADS = 256, RS_ITEMS = 16, RS_TILE = RS_THREADS * RS_ITEMS;
-static int g_digit_bits = 8;  // autotuned 4..8
+static int g_digit_bits = 8;  // LSD digit width, 4 - 8 bits (autotuner knob)
 void set_radix_digit_bits(int b) { g_digit_bits = b < 4 ? 4 : (b > 8 ? 8 : b); }
+int get_radix_digit_bits() { return g_digit_bits; }
 
 template <typename K>
 __global__ void k_key_bits(const K* __restrict__ k, long long n, unsigned long long* orv, unsigned long long* andv) {
@@ -142,27 +143,8 @@ __global__ void __launch_bounds__(RS_THREADS, 3) k_onesweep(const K* __restrict_
         unsigned before = 0;
         for (unsigned ww = 0; ww < w; ww++) before += wscan[ww];
         dstart[d] = before + inc - c;
-        unsigned long long* st = status + (size_t)t * 256 + d;
         unsigned long long excl = 0;
-        if (d <= (int)dmask) {
-            if (t == 0) st_release(st, LB_INC | c);
-            else {
-                st_release(st, LB_AGG | c);
-                long long j = t - 1, spins = 0;
-                while (j >= 0) {
-                    unsigned long long sv = ld_acquire(status + (size_t)j * 256 + d);
-                    unsigned long long f = sv >> 62;
-                    if (f == 0) {
-                        if (++spins > SPIN_LIMIT) { flag_error(derr, DERR_TIMEOUT); break; }
-                        continue;
-                    }
-                    excl += sv & LB_MASK;
-                    if (f == 2) break;
-                    j--;
-                }
-                st_release(st, LB_INC | (excl + c));
-            }
-        }
+        if (d <= (int)dmask) excl = chain_lookback(status + d, 256, t, 0, c, derr);
         dbase[d] = bucket[d] + excl;
     }
     __syncthreads();

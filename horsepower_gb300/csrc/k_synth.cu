@@ -11,6 +11,9 @@
 //   dim.date 8035 + U{0..2525}          fact.fk   U{0..ndim-1}
 //   fact.flag U{0,1,2}   fact.status U{0,1}   fact.qty U{1..50} (as f64)
 //   fact.price round(qty * U(900,105000) / 100, 2)   fact.disc U{0..10}/100
+#include <cmath>
+#include <vector>
+
 #include "dev_common.cuh"
 
 namespace hg {
@@ -68,6 +71,22 @@ __global__ void k_synth_fact(unsigned long long seed, long long nf, long long nd
     }
 }
 
+// Zipf keys by inverse CDF: key = 1 + (number of CDF entries <= u), u uniform
+// in [0, 1); sec uniform over [0, 2^20].
+__global__ void k_synth_order(unsigned long long seed, long long n, const double* __restrict__ cdf, long long nr,
+                              long long* __restrict__ key, int* __restrict__ sec) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double u = (double)(rnd(seed, 8, i) >> 11) * (1.0 / 9007199254740992.0);
+        long long lo = 0, hi = nr;  // first index with cdf > u
+        while (lo < hi) {
+            long long mid = (lo + hi) >> 1;
+            if (cdf[mid] <= u) lo = mid + 1; else hi = mid;
+        }
+        key[i] = lo + 1;
+        sec[i] = (int)(rnd(seed, 9, i) % ((1ull << 20) + 1));
+    }
+}
+
 }  // namespace hg
 
 using namespace hg;
@@ -108,5 +127,37 @@ extern "C" I hgpuSynthJoinTables(unsigned long long seed, L nfact, L ndim, V dim
     void* fp[6] = {fk, flag, status, qty, price, disc};
     for (int i = 0; i < 2; i++) HG_CHECK(finish_out(&d[i], dp[i]));
     for (int i = 0; i < 6; i++) HG_CHECK(finish_out(&f[i], fp[i]));
+    return 0;
+}
+
+// Fills order (a list of 2 nodes: key i64, sec i32) with device-resident
+// columns: key Zipf over 1..nranks with exponent s (cdf computed here, in
+// double precision), sec uniform over [0, 2^20].
+extern "C" I hgpuSynthOrderTable(unsigned long long seed, L n, L nranks, E s, V order) {
+    HG_CHECK(ensure_init());
+    if (n < 0 || nranks < 1 || nranks > (1LL << 30)) return E_DOMAIN;
+    ScratchScope ss;
+    HG_CHECK(init_list(order, H_G, 2));
+    V0* o = host_nodes(order);
+    void *key, *sec;
+    HG_CHECK(alloc_out(&o[0], H_L, n, &key));
+    HG_CHECK(alloc_out(&o[1], H_I, n, &sec));
+    std::vector<double> cdf((size_t)nranks);
+    double acc = 0.0;
+    for (L r = 0; r < nranks; r++) cdf[(size_t)r] = (acc += pow((double)(r + 1), -s));
+    for (L r = 0; r < nranks; r++) cdf[(size_t)r] /= acc;
+    double* dc = (double*)salloc((size_t)nranks * 8);
+    if (!dc) return E_DEVICE_OOM;
+    HG_CU(cudaMemcpyAsync(dc, cdf.data(), (size_t)nranks * 8, cudaMemcpyHostToDevice, g_stream));
+    if (n > 0) {
+        unsigned g = grid_for(n, 256);
+        if (g > (unsigned)g_sms * 32) g = g_sms * 32;
+        HG_LAUNCH("synth_order", g, 256, 0, k_synth_order, seed, n, (const double*)dc, nranks, (long long*)key,
+                  (int*)sec);
+    }
+    HG_CHECK(last_launch_error());
+    HG_CHECK(check_device_errors());
+    HG_CHECK(finish_out(&o[0], key));
+    HG_CHECK(finish_out(&o[1], sec));
     return 0;
 }

@@ -40,6 +40,8 @@ I cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
     return e == cudaErrorMemoryAllocation ? E_DEVICE_OOM : E_DEVICE;
 }
 
+int g_tile_rows = 16;  // autotuner knob: probe rows per thread of the tiled join probes
+
 // ------------------------------------------------------------------ arenas
 // A bump arena over a list of chunks.  A mark is (chunk index, cursor).
 struct Arena {
@@ -560,6 +562,24 @@ I hgpuProfileRead(I cap, const char** names, double* total_ms, L* launches) {
 }
 
 L hgpuLaunchCount(void) { return g_launches; }
+
+I hgpuSetTuning(I knob, E value) {
+    switch (knob) {
+    case HGPU_TUNE_HASH_LOAD: set_hash_load_factor(value); return 0;
+    case HGPU_TUNE_RADIX_BITS: set_radix_digit_bits((int)value); return 0;
+    case HGPU_TUNE_TILE_ROWS: g_tile_rows = value <= 8 ? 8 : (value <= 16 ? 16 : 32); return 0;
+    default: return E_DOMAIN;
+    }
+}
+
+E hgpuGetTuning(I knob) {
+    switch (knob) {
+    case HGPU_TUNE_HASH_LOAD: return get_hash_load_factor();
+    case HGPU_TUNE_RADIX_BITS: return (E)get_radix_digit_bits();
+    case HGPU_TUNE_TILE_ROWS: return (E)g_tile_rows;
+    default: return -1.0;
+    }
+}
 
 static cudaEvent_t g_t0 = nullptr, g_t1 = nullptr;
 I hgpuTimerStart(void) {

@@ -5,6 +5,9 @@
     python -m horsepower_gb300.profile_cases group     # @group on two 1-byte columns, 8.67M rows
     python -m horsepower_gb300.profile_cases order     # @order (i64 key, i32 sec), N rows
     python -m horsepower_gb300.profile_cases gather    # @index f64 by ascending row ids
+    python -m horsepower_gb300.profile_cases q6        # fused q6 chain, 6M rows
+    python -m horsepower_gb300.profile_cases shared    # 16 batched join plans over one pair of tables
+    ... --tune tile_rows=32 --tune hash_load=0.7       # autotuner knobs
 
 Inputs are seeded, uploaded once, and each case runs --reps times on
 device-resident data, printing the CUDA-event time per call.
@@ -43,11 +46,15 @@ def timed(L, fn, reps):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["join", "compress", "group", "order", "gather", "q6"])
+    ap.add_argument("case", choices=["join", "compress", "group", "order", "gather", "q6", "shared"])
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--rows", type=int, default=0)
+    ap.add_argument("--tune", action="append", default=[], help="knob=value (autotuner knobs)")
     a = ap.parse_args()
     L = load()
+    if a.tune:
+        from . import autotune
+        autotune.apply(L, {kv.split("=")[0]: float(kv.split("=")[1]) for kv in a.tune})
     rng = np.random.default_rng(5)
     if a.case == "join":
         F = a.rows or 59_986_052
@@ -81,6 +88,12 @@ def main():
         x = dev(L, rng.standard_normal(n), H_E)
         idx = dev(L, np.flatnonzero(rng.random(n) < 0.1445).astype(np.int64), H_L)
         t = timed(L, lambda: L.call("pfnIndex", x, idx), a.reps)
+    elif a.case == "shared":
+        from . import batch as B
+        n = a.rows or 59_986_052
+        dim, fact = B.synth_tables(L, 1, n, n // 4)
+        plans = [B.make_plan(dim, fact, D.DAYS0 + 100 * k, D.DAYS0 + 100 * k + 365) for k in range(16)]
+        t = timed(L, lambda: B.run_batch(L, plans), a.reps)
     else:
         from . import plans as P
         tb = D.filter_table(a.rows or 6_001_215)

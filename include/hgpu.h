@@ -220,7 +220,7 @@ typedef struct {
 } hgpuJoinGroupPlan;
 #define HGPU_PLAN_MAX_GROUPS 256
 typedef struct {
-    I status;                         /* 0, or E_NOT_IMPL for a plan outside the batched scope */
+    I status;                         /* 0, or the error code of the plan's builtins */
     L ngroups;                        /* groups in ascending (flag<<8 | status) order */
     C flag[HGPU_PLAN_MAX_GROUPS], st[HGPU_PLAN_MAX_GROUPS];
     E sum_qty[HGPU_PLAN_MAX_GROUPS], avg_price[HGPU_PLAN_MAX_GROUPS], sum_disc[HGPU_PLAN_MAX_GROUPS];
@@ -231,6 +231,60 @@ I hgpuBatchJoinGroup(const hgpuJoinGroupPlan *plans, L nplans, hgpuJoinGroupResu
  * filled with a 2-node list (pk = a permutation of 0..ndim-1, date), fact with
  * a 6-node list (fk, flag, status, qty, price, disc). */
 I hgpuSynthJoinTables(unsigned long long seed, L nfact, L ndim, V dim, V fact);
+/* Seeded synthetic order table on the device: a 2-node list (key i64 Zipf(s)
+ * over 1..nranks, sec i32 uniform over [0, 2^20]). */
+I hgpuSynthOrderTable(unsigned long long seed, L n, L nranks, E s, V order);
+
+/* ---------------- served form ----------------
+ * A request loop over tables resident in HBM (no counterpart in the
+ * reference).  Requests arrive over time; each step of the loop admits the
+ * waiting requests in arrival order while their HBM footprints fit the
+ * server's budget, runs them together (all filter-aggregates in one
+ * shared-scan launch, all join + group-bys through hgpuBatchJoinGroup, the
+ * top-k orders one after another), and stamps their completion.  Requests
+ * that arrive while a step runs join the next one.  A request's result does
+ * not depend on which other requests share its step. */
+typedef struct {
+    /* filter-aggregate table: q6-shaped lineitem columns */
+    const I *l_shipdate, *l_qty; const E *l_disc, *l_price; L nline;
+    /* join tables (as hgpuJoinGroupPlan) */
+    const I *dim_pk, *dim_date; L ndim;
+    const I *fk; const C *flag, *status; const E *qty, *price, *disc; L nfact;
+    /* order table: i64 key, i32 secondary */
+    const L *o_key; const I *o_sec; L norder;
+} hgpuServeTables;
+#define HGPU_REQ_FILTER_AGG 0   /* sum(price*disc) where shipdate in [lo,hi) and the q6 predicate */
+#define HGPU_REQ_JOIN_GROUP 1   /* the hgpuJoinGroupPlan query with dim.date in [lo,hi) */
+#define HGPU_REQ_TOPK_ORDER 2   /* first k rows of the stable ascending @order on (key, sec) among key in [klo,khi) */
+#define HGPU_TOPK 1000
+typedef struct {
+    I kind;
+    I lo, hi;                 /* date window */
+    L klo, khi;               /* key range */
+    double arrival_s;         /* seconds from the start of the stream; requests sorted by it */
+} hgpuRequest;
+typedef struct {
+    I status;                 /* 0, E_ADMISSION (footprint above the budget) or a builtin's error */
+    E value;                  /* filter-aggregate result */
+    hgpuJoinGroupResult *group;  /* join + group-by result: caller-owned, may be NULL */
+    L *rows;                  /* top-k row ids (caller-owned, HGPU_TOPK entries), may be NULL */
+    L nrows;
+    double admit_s, done_s;   /* seconds from the start of the stream */
+    L step;                   /* loop step that ran the request */
+    L footprint;              /* HBM bytes the request was admitted with */
+} hgpuResponse;
+typedef struct {
+    L steps, rejected, max_step_requests;
+    L max_step_bytes;         /* largest admitted footprint of one step */
+    double wall_s, qps, p50_ms, p99_ms, mean_ms, max_ms;
+} hgpuServeStats;
+typedef struct hgpu_server_s *hgpuServer;
+#define HGPU_SERVE_BATCHED 0  /* continuous batching (the served form) */
+#define HGPU_SERVE_PLAIN   1  /* one request at a time through its builtins, in arrival order */
+I hgpuServerCreate(hgpuServer *out, const hgpuServeTables *tables, L hbm_budget_bytes, L max_step_requests);
+L hgpuServerFootprint(hgpuServer s, const hgpuRequest *r);   /* admission estimate, bytes */
+I hgpuServerRun(hgpuServer s, const hgpuRequest *req, L n, hgpuResponse *out, I mode, hgpuServeStats *stats);
+I hgpuServerDestroy(hgpuServer s);
 
 /* ---------------- runtime extensions ---------------- */
 #define HGPU_RESIDENT_DEVICE 0   /* outputs stay in HBM (default) */
@@ -256,6 +310,16 @@ L    hgpuLaunchCount(void);           /* kernels launched by this library since 
 /* Event timer on the library stream */
 I    hgpuTimerStart(void);
 double hgpuTimerStop(void);
+/* Autotuner knobs.  None of them changes a result: every setting gives the
+ * same bits (stable sorts, order-preserving compaction, fixed-order sums).
+ * Values outside a knob's range are clamped; hgpuGetTuning returns the
+ * value in force. */
+#define HGPU_TUNE_HASH_LOAD  0   /* hash-table load factor, 0.5 - 0.8 (default 0.5) */
+#define HGPU_TUNE_RADIX_BITS 1   /* LSD radix digit width of @group/@order, 4 - 8 bits (default 8) */
+#define HGPU_TUNE_TILE_ROWS  2   /* probe rows per thread of the tiled join probes: 8, 16, 32
+                                    (tile = 256 x that; default 16) */
+I    hgpuSetTuning(I knob, E value);
+E    hgpuGetTuning(I knob);
 
 /* Allocation-free f64 sum (no counterpart in the reference).  For callers that
  * cannot allocate device memory where they need a sum: code running during a

@@ -138,3 +138,30 @@ def test_batch_vs_oracle(L):
     assert np.array_equal(got[5], want[5])
     for k in (2, 3, 4):
         assert np.allclose(got[k], want[k], rtol=1e-12, atol=0)
+
+
+def test_shared_tables(L):
+    """Plans over identical tables take the shared probe; its results equal
+    each plan's builtins, including the cases it must hand back to them (a
+    repeated key, a compressed key column longer than the fact table)."""
+    dim, fact = B.synth_tables(L, 61, 300_000, 75_000)
+    wins = [(D.WIN_LO, D.WIN_HI), (D.DAYS0, D.DAYS0 + 30), (9000, 9000), (0, 1 << 30), (D.WIN_LO, D.WIN_HI)]
+    got = B.run_batch(L, [B.make_plan(dim, fact, lo, hi) for lo, hi in wins])
+    for (lo, hi), g in zip(wins, got):
+        identical(g, plain(L, dim, fact, lo, hi))
+    identical(got[0], got[4])
+    rng = np.random.default_rng(62)
+    n, nd = 50_000, 20_000
+    f2 = dict(fk=rng.integers(0, nd, n).astype(np.int32), flag=rng.integers(0, 3, n).astype(np.int8),
+              status=rng.integers(0, 2, n).astype(np.int8), qty=rng.integers(1, 51, n).astype(np.float64),
+              price=np.round(rng.uniform(900, 105000, n)) / 100, disc=rng.integers(0, 11, n) / 100)
+    d2 = dict(pk=rng.integers(0, nd // 2, nd).astype(np.int32), date=(8035 + rng.integers(0, 2526, nd)).astype(np.int32))
+    dd, ff = B.device_tables(L, d2, f2)               # repeated keys
+    ds, fs = B.synth_tables(L, 63, 4_000, 40_000)     # dimension longer than the fact table
+    plans = [B.make_plan(dd, ff), B.make_plan(dd, ff, D.DAYS0, D.DAYS0 + 900),
+             B.make_plan(ds, fs, 0, 1 << 30), B.make_plan(ds, fs, D.WIN_LO, D.WIN_LO + 60)]
+    got = B.run_batch(L, plans)
+    identical(got[0], plain(L, dd, ff))
+    identical(got[1], plain(L, dd, ff, D.DAYS0, D.DAYS0 + 900))
+    identical(got[2], plain(L, ds, fs, 0, 1 << 30))
+    identical(got[3], plain(L, ds, fs, D.WIN_LO, D.WIN_LO + 60))

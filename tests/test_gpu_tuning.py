@@ -1,0 +1,98 @@
+"""Autotuner knobs (hgpuSetTuning) change speed, never results.
+
+Every setting of each knob must give bit-identical outputs: @join_index in
+direct-addressed and hashed mode across tile sizes and load factors, @group
+and @order across radix digit widths, and batched plans across tile sizes.
+"""
+import numpy as np
+import pytest
+
+from horsepower_gb300 import autotune as T
+from horsepower_gb300 import batch as B
+from horsepower_gb300.abi import H_B, H_I, H_L
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def L():
+    import horsepower_gb300
+    L = horsepower_gb300.load()
+    yield L
+    T.apply(L, {"tile_rows": 16, "hash_load": 0.5, "radix_bits": 8})
+
+
+def outputs(L, fn):
+    z = fn()
+    return L.to_py(z)
+
+
+def same(a, b):
+    if isinstance(a, np.ndarray):
+        return a.dtype == b.dtype and np.array_equal(a, b)
+    if isinstance(a, tuple):
+        return all(same(p, q) for p, q in zip(a[1:], b[1:]))
+    return len(a) == len(b) and all(same(p, q) for p, q in zip(a, b))
+
+
+@pytest.mark.parametrize("wide", [False, True])
+def test_join_knobs(L, wide):
+    rng = np.random.default_rng(21)
+    nd, nf = 300_000, 2_000_001
+    pk = rng.permutation(nd).astype(np.int64) * (5000 if wide else 1)
+    build = pk[rng.random(nd) < 0.3]
+    probe = rng.choice(pk, nf) + rng.integers(0, 2, nf) * (7 if wide else nd)
+    x, y = L.vec(build.astype(np.int32), H_I), L.vec(probe.astype(np.int32), H_I)
+    f = L.sym("eq")
+    T.apply(L, {"tile_rows": 16, "hash_load": 0.5})
+    ref = outputs(L, lambda: L.call("pfnJoinIndex", x, y, f))
+    assert ref[0].size > 0
+    for tr in (8, 16, 32):
+        for hl in (0.5, 0.65, 0.8):
+            T.apply(L, {"tile_rows": tr, "hash_load": hl})
+            assert same(outputs(L, lambda: L.call("pfnJoinIndex", x, y, f)), ref), (tr, hl)
+    T.apply(L, {"tile_rows": 16, "hash_load": 0.5})
+
+
+def test_radix_bits(L):
+    rng = np.random.default_rng(22)
+    n = 1_500_000
+    key = np.minimum(rng.zipf(1.1, n), 1_000_000).astype(np.int64)
+    sec = rng.integers(0, 2 ** 20 + 1, n).astype(np.int32)
+    k, s = L.vec(key, H_L), L.vec(sec, H_I)
+    d = L.vec(np.array([1, 1], bool), H_B)
+    T.apply(L, {"radix_bits": 8})
+    ref_o = outputs(L, lambda: L.call("pfnOrderBy", L.list([k, s]), d))
+    ref_g = outputs(L, lambda: L.call("pfnGroup", k))
+    for b in (4, 5, 6, 7):
+        T.apply(L, {"radix_bits": b})
+        assert T.current(L)["radix_bits"] == b
+        assert same(outputs(L, lambda: L.call("pfnOrderBy", L.list([k, s]), d)), ref_o), b
+        assert same(outputs(L, lambda: L.call("pfnGroup", k)), ref_g), b
+    T.apply(L, {"radix_bits": 8})
+
+
+def test_batched_tile_rows(L):
+    tabs = [B.synth_tables(L, 500 + i, n, max(1, n // 4)) for i, n in enumerate([5000, 70_000, 400_000, 1_300_000])]
+    plans = [B.make_plan(d, f) for d, f in tabs]
+    T.apply(L, {"tile_rows": 16})
+    ref = B.run_batch(L, plans)
+    for tr in (8, 32):
+        T.apply(L, {"tile_rows": tr})
+        got = B.run_batch(L, plans)
+        for g, r in zip(got, ref):
+            for a, b in zip(g, r):
+                assert np.array_equal(a, b)
+    T.apply(L, {"tile_rows": 16})
+
+
+def test_tune_and_clamp(L):
+    T.apply(L, {"hash_load": 0.95, "radix_bits": 2, "tile_rows": 100})
+    c = T.current(L)
+    assert c == {"tile_rows": 32, "hash_load": 0.8, "radix_bits": 4}
+    tabs = [B.synth_tables(L, 900 + i, n, n // 4) for i, n in enumerate([20_000, 200_000])]
+    plans = [B.make_plan(d, f) for d, f in tabs]
+    best, table = T.tune(L, lambda: B.run_batch(L, plans), knobs=("tile_rows",), reps=2,
+                         check=lambda out: [tuple(a.tobytes() for a in r) for r in out])
+    assert best["tile_rows"] in (8, 16, 32) and set(table["tile_rows"]) == {8, 16, 32}
+    assert T.current(L)["tile_rows"] == best["tile_rows"]
