@@ -31,6 +31,7 @@
 namespace hg {
 
 I scan_exclusive(const unsigned* in, long long n, unsigned long long* out, unsigned long long* total_h);
+I scan_counts(const unsigned* counts, long long n, unsigned long long* offs);
 I seg_sum_f64(const double* src, const long long* rows, long long nx, const long long* starts, long long ng,
               long long total, double* out);
 
@@ -133,32 +134,25 @@ __global__ void k_b_build(const DPlan* __restrict__ P, const long long* __restri
 }
 
 // ---------------------------------------------------------------- stage 2
-// probe: matched fact rows of each plan, compacted in row order.  A tile is
-// 256 x R fact rows (R, 8 to 32, is the autotuner's tile knob); each warp
-// owns 32 x R consecutive rows and takes its output offset from its own
-// look-back over the plan's warp sub-tiles, with no block barrier.
+// probe, pass 1: one bit per fact row of each plan (its key is in the
+// plan's presence bitmap) and the tile's count.  A tile is 256 x R rows (R,
+// 8 to 32, is the autotuner's tile knob): warp w owns words [w R, w R + R) of
+// the tile's 8 R bit words, lane l row 32 k + l of word k.  The keys and then
+// their presence words come by cp.async into the thread's own shared-memory
+// column, all R of a group in flight together.
 template <int R>
 __global__ void __launch_bounds__(256) k_b_probe(const DPlan* __restrict__ P, const long long* __restrict__ tile_first,
-                                                 int np, unsigned* __restrict__ fi, unsigned long long* status,
-                                                 unsigned* ticket, unsigned long long* __restrict__ mcount,
-                                                 unsigned* derr) {
-    constexpr long long SUB = 32LL * R;
+                                                 int np, unsigned* __restrict__ bits, unsigned* __restrict__ counts) {
     extern __shared__ unsigned bp_smem[];
     unsigned(*koff)[256] = reinterpret_cast<unsigned(*)[256]>(bp_smem);            // key - kmin, NONE when out of range
     unsigned(*word)[256] = reinterpret_cast<unsigned(*)[256]>(bp_smem + R * 256);  // presence word of the key
-    __shared__ long long tile_id;
-    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) tile_id = atomicAdd(ticket, 1u);
-    __syncthreads();
-    const long long t = tile_id;
+    __shared__ unsigned wc[8];
+    constexpr unsigned NONE = 0xffffffffu;
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5, me = threadIdx.x;
+    const long long t = blockIdx.x;
     const int p = plan_of_tile(tile_first, np, t);
     const DPlan& q = P[p];
-    const long long sub = t * 8 + warp, first = tile_first[p] * 8;
-    const long long base = (sub - first) * SUB;  // plan-relative first row of the sub-tile
-    // keys, then their presence words, fetched by cp.async into the thread's
-    // own shared-memory column: all R loads of a group in flight together
-    constexpr unsigned NONE = 0xffffffffu;
-    const unsigned me = threadIdx.x;
+    const long long base = (t - tile_first[p]) * (256LL * R) + (long long)warp * (32 * R);  // plan-relative row
     const long long nf = q.nf;
 #pragma unroll
     for (int k = 0; k < R; k++) {
@@ -176,24 +170,67 @@ __global__ void __launch_bounds__(256) k_b_probe(const DPlan* __restrict__ P, co
         if (o != NONE) cp_async4(&word[k][me], q.bitmap + (o >> 5));
     }
     cp_async_wait_all();
-    unsigned hits = 0;  // bit k: round k matched
     unsigned cnt = 0;
+    unsigned* wout = bits + t * (8LL * R) + (long long)warp * R;
 #pragma unroll
     for (int k = 0; k < R; k++) {
         unsigned o = koff[k][me];
         bool m = o != NONE && ((word[k][me] >> (o & 31)) & 1u);
-        hits |= (unsigned)m << k;
-        cnt += __popc(__ballot_sync(0xffffffffu, m));
+        unsigned bal = __ballot_sync(0xffffffffu, m);
+        if (lane == 0) wout[k] = bal;
+        cnt += __popc(bal);
     }
-    unsigned long long off = lookback_seg(status, sub, first, cnt, derr);
-    if (lane == 0 && base < q.nf && base + SUB >= q.nf) mcount[p] = off + cnt;  // the plan's last sub-tile
+    if (lane == 0) wc[warp] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned c = 0;
+        for (int w = 0; w < 8; w++) c += wc[w];
+        counts[t] = c;
+    }
+}
+
+// where each tile map's plan writes its rows: its region of the matched-row
+// buffer and its slot in mcount
+struct EmitPlan {
+    long long fact_off;
+    int p;
+};
+
+// pass 2 (probe and shared selection): each tile writes the plan-relative
+// row numbers of its set bits from its offset within the plan (the scan of
+// the tile counts, less the scan at the plan's first tile); warp w walks its
+// R words, and a word is already the ballot of its 32 rows.  The plan's last
+// tile stores the plan's match count.
+template <int R>
+__global__ void __launch_bounds__(256) k_b_emit(const EmitPlan* __restrict__ E, const long long* __restrict__ tile_first,
+                                                int np, const unsigned* __restrict__ bits,
+                                                const unsigned long long* __restrict__ offs, unsigned* __restrict__ fi,
+                                                unsigned long long* __restrict__ mcount) {
+    __shared__ unsigned wc[8];
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    const long long t = blockIdx.x;
+    const int c = plan_of_tile(tile_first, np, t);
+    const long long first = tile_first[c];
+    const unsigned* w = bits + t * (8LL * R) + (long long)warp * R;
+    unsigned wd[R];
+    unsigned cnt = 0;
 #pragma unroll
     for (int k = 0; k < R; k++) {
-        bool sel = (hits >> k) & 1u;
-        unsigned bal = __ballot_sync(0xffffffffu, sel);
-        if (sel) fi[q.fact_off + off + __popc(bal & lanemask_lt())] = (unsigned)(base + k * 32 + lane);
-        off += __popc(bal);
+        wd[k] = w[k];
+        cnt += __popc(wd[k]);
     }
+    if (lane == 0) wc[warp] = cnt;
+    __syncthreads();
+    unsigned long long off = offs[t] - offs[first];
+    for (unsigned v = 0; v < warp; v++) off += wc[v];
+    const long long base = (t - first) * (256LL * R) + (long long)warp * (32 * R);
+    unsigned* out = fi + E[c].fact_off;
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+        if ((wd[k] >> lane) & 1u) out[off + __popc(wd[k] & lanemask_lt())] = (unsigned)(base + k * 32 + lane);
+        off += __popc(wd[k]);
+    }
+    if (threadIdx.x == 0 && t + 1 == tile_first[c + 1]) mcount[E[c].p] = offs[t + 1] - offs[first];
 }
 
 // ---------------------------------------------------------------- shared tables
@@ -293,43 +330,39 @@ struct CPlan {
     int p;               // index in the batch
 };
 
-// each plan's rows with a date offset in its window, compacted in row order
-// (the layout and per-warp look-back of k_b_probe)
+// shared selection, pass 1: one bit per fact row of each plan (its date
+// offset lies in the plan's window) and the tile's count; the k_b_probe
+// layout
 template <int R>
 __global__ void __launch_bounds__(256) k_sh_select(const CPlan* __restrict__ P, const long long* __restrict__ tile_first,
-                                                   int np, unsigned* __restrict__ fi, unsigned long long* status,
-                                                   unsigned* ticket, unsigned long long* __restrict__ mcount,
-                                                   unsigned* derr) {
-    constexpr long long SUB = 32LL * R;
-    __shared__ long long tile_id;
+                                                   int np, unsigned* __restrict__ bits, unsigned* __restrict__ counts) {
+    __shared__ unsigned wc[8];
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) tile_id = atomicAdd(ticket, 1u);
-    __syncthreads();
-    const long long t = tile_id;
+    const long long t = blockIdx.x;
     const int c = plan_of_tile(tile_first, np, t);
     const CPlan& q = P[c];
-    const long long sub = t * 8 + warp, first = tile_first[c] * 8;
-    const long long base = (sub - first) * SUB;
-    unsigned hits = 0, cnt = 0;
+    const long long base = (t - tile_first[c]) * (256LL * R) + (long long)warp * (32 * R);
+    unsigned short d[R];
 #pragma unroll
     for (int k = 0; k < R; k++) {
         long long i = base + k * 32 + lane;
-        bool m = false;
-        if (i < q.nf) {
-            int d = (int)__ldcs(q.dd + i);
-            m = d >= q.dlo && d < q.dhi;  // NO_DATE is above every window
-        }
-        hits |= (unsigned)m << k;
-        cnt += __popc(__ballot_sync(0xffffffffu, m));
+        d[k] = i < q.nf ? __ldcs(q.dd + i) : NO_DATE;
     }
-    unsigned long long off = lookback_seg(status, sub, first, cnt, derr);
-    if (lane == 0 && base < q.nf && base + SUB >= q.nf) mcount[q.p] = off + cnt;
+    unsigned cnt = 0;
+    unsigned* wout = bits + t * (8LL * R) + (long long)warp * R;
 #pragma unroll
     for (int k = 0; k < R; k++) {
-        bool sel = (hits >> k) & 1u;
-        unsigned bal = __ballot_sync(0xffffffffu, sel);
-        if (sel) fi[q.fact_off + off + __popc(bal & lanemask_lt())] = (unsigned)(base + k * 32 + lane);
-        off += __popc(bal);
+        bool m = (int)d[k] >= q.dlo && (int)d[k] < q.dhi;  // NO_DATE is above every window
+        unsigned bal = __ballot_sync(0xffffffffu, m);
+        if (lane == 0) wout[k] = bal;
+        cnt += __popc(bal);
+    }
+    if (lane == 0) wc[warp] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned s = 0;
+        for (int w = 0; w < 8; w++) s += wc[w];
+        counts[t] = s;
     }
 }
 
@@ -817,43 +850,66 @@ extern "C" I hgpuBatchJoinGroup(const hgpuJoinGroupPlan* plans, L nplans, hgpuJo
     if (!nsel) return E_DEVICE_OOM;
     HG_CU(cudaMemsetAsync(nsel, 0, np * 8, g_stream));
     if (dtiles[np] > 0) HG_LAUNCH("b_build", (unsigned)dtiles[np], 256, 0, k_b_build, dP, dT, np, dup, nsel);
-    // probe
+    // probe: match bits and tile counts (per-plan probes, then the shared
+    // selections, as one tile map), a scan of the counts, and the emit pass
     unsigned* fi = (unsigned*)salloc((size_t)(fact_total > 0 ? fact_total : 1) * 4);
     unsigned long long* mcount = (unsigned long long*)salloc(np * 8 + 16);
     long long* moff = (long long*)salloc((np + 1) * 8);
-    char* st = (char*)salloc((size_t)ftiles[np] * 64 + 64);  // a status word per warp sub-tile, then the ticket
-    if (!fi || !mcount || !moff || !st) return E_DEVICE_OOM;
+    const long long nt_probe = ftiles[np], nt_all = nt_probe + ctiles.back();
+    unsigned* mbits = (unsigned*)salloc((size_t)(nt_all > 0 ? nt_all : 1) * 8 * R * 4);
+    unsigned* tcount = (unsigned*)salloc((size_t)(nt_all > 0 ? nt_all : 1) * 4);
+    unsigned long long* toffs = (unsigned long long*)salloc((size_t)(nt_all + 1) * 8);
+    if (!fi || !mcount || !moff || !mbits || !tcount || !toffs) return E_DEVICE_OOM;
     HG_CU(cudaMemsetAsync(mcount, 0, np * 8, g_stream));
-    HG_CU(cudaMemsetAsync(st, 0, (size_t)ftiles[np] * 64 + 64, g_stream));
-    if (ftiles[np] > 0) {
-        unsigned long long* sw = (unsigned long long*)st;
-        unsigned* tk = (unsigned*)(st + (size_t)ftiles[np] * 64);
-        const unsigned nt = (unsigned)ftiles[np];
+    // the combined tile map: every plan with probe tiles, then every shared selection
+    std::vector<EmitPlan> emit;
+    std::vector<long long> etiles(1, 0);
+    for (int p = 0; p < np; p++) {
+        emit.push_back(EmitPlan{hp[p].fact_off, p});
+        etiles.push_back(ftiles[p + 1]);
+    }
+    for (const CPlan& c : cplans) {
+        emit.push_back(EmitPlan{c.fact_off, c.p});
+        etiles.push_back(etiles.back() + ((c.nf + ptile - 1) / ptile));
+    }
+    if (nt_probe > 0) {
+        const unsigned nt = (unsigned)nt_probe;
         const size_t sm = (size_t)2 * R * 256 * 4;
         static bool attr = false;
         if (!attr) {
             HG_CU(cudaFuncSetAttribute(k_b_probe<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 32 * 256 * 4));
             attr = true;
         }
-        if (R == 8) HG_LAUNCH("b_probe", nt, 256, sm, k_b_probe<8>, dP, fT, np, fi, sw, tk, mcount, g_derr);
-        else if (R == 32) HG_LAUNCH("b_probe", nt, 256, sm, k_b_probe<32>, dP, fT, np, fi, sw, tk, mcount, g_derr);
-        else HG_LAUNCH("b_probe", nt, 256, sm, k_b_probe<16>, dP, fT, np, fi, sw, tk, mcount, g_derr);
+        if (R == 8) HG_LAUNCH("b_probe", nt, 256, sm, k_b_probe<8>, dP, fT, np, mbits, tcount);
+        else if (R == 32) HG_LAUNCH("b_probe", nt, 256, sm, k_b_probe<32>, dP, fT, np, mbits, tcount);
+        else HG_LAUNCH("b_probe", nt, 256, sm, k_b_probe<16>, dP, fT, np, mbits, tcount);
     }
-    if (!cplans.empty() && ctiles.back() > 0) {
+    if (ctiles.back() > 0) {
         const int nc = (int)cplans.size();
         CPlan* dC = (CPlan*)salloc(nc * sizeof(CPlan));
         long long* cT = (long long*)salloc((nc + 1) * 8);
-        char* cst = (char*)salloc((size_t)ctiles.back() * 64 + 64);
-        if (!dC || !cT || !cst) return E_DEVICE_OOM;
+        if (!dC || !cT) return E_DEVICE_OOM;
         HG_CU(cudaMemcpyAsync(dC, cplans.data(), nc * sizeof(CPlan), cudaMemcpyHostToDevice, g_stream));
         HG_CU(cudaMemcpyAsync(cT, ctiles.data(), (nc + 1) * 8, cudaMemcpyHostToDevice, g_stream));
-        HG_CU(cudaMemsetAsync(cst, 0, (size_t)ctiles.back() * 64 + 64, g_stream));
-        unsigned long long* sw = (unsigned long long*)cst;
-        unsigned* tk = (unsigned*)(cst + (size_t)ctiles.back() * 64);
         const unsigned nt = (unsigned)ctiles.back();
-        if (R == 8) HG_LAUNCH("sh_select", nt, 256, 0, k_sh_select<8>, dC, cT, nc, fi, sw, tk, mcount, g_derr);
-        else if (R == 32) HG_LAUNCH("sh_select", nt, 256, 0, k_sh_select<32>, dC, cT, nc, fi, sw, tk, mcount, g_derr);
-        else HG_LAUNCH("sh_select", nt, 256, 0, k_sh_select<16>, dC, cT, nc, fi, sw, tk, mcount, g_derr);
+        unsigned* cb2 = mbits + (size_t)nt_probe * 8 * R;
+        unsigned* cc2 = tcount + nt_probe;
+        if (R == 8) HG_LAUNCH("sh_select", nt, 256, 0, k_sh_select<8>, dC, cT, nc, cb2, cc2);
+        else if (R == 32) HG_LAUNCH("sh_select", nt, 256, 0, k_sh_select<32>, dC, cT, nc, cb2, cc2);
+        else HG_LAUNCH("sh_select", nt, 256, 0, k_sh_select<16>, dC, cT, nc, cb2, cc2);
+    }
+    if (nt_all > 0) {
+        const int ne = (int)emit.size();
+        EmitPlan* dE = (EmitPlan*)salloc(ne * sizeof(EmitPlan));
+        long long* eT = (long long*)salloc((ne + 1) * 8);
+        if (!dE || !eT) return E_DEVICE_OOM;
+        HG_CU(cudaMemcpyAsync(dE, emit.data(), ne * sizeof(EmitPlan), cudaMemcpyHostToDevice, g_stream));
+        HG_CU(cudaMemcpyAsync(eT, etiles.data(), (ne + 1) * 8, cudaMemcpyHostToDevice, g_stream));
+        HG_CHECK(scan_counts(tcount, nt_all, toffs));
+        const unsigned nt = (unsigned)nt_all;
+        if (R == 8) HG_LAUNCH("b_emit", nt, 256, 0, k_b_emit<8>, dE, eT, ne, mbits, toffs, fi, mcount);
+        else if (R == 32) HG_LAUNCH("b_emit", nt, 256, 0, k_b_emit<32>, dE, eT, ne, mbits, toffs, fi, mcount);
+        else HG_LAUNCH("b_emit", nt, 256, 0, k_b_emit<16>, dE, eT, ne, mbits, toffs, fi, mcount);
     }
     HG_LAUNCH("b_offsets", 1, 32, 0, k_b_offsets, mcount, np, moff);
     // gather (over the fact tile map: a plan has at most as many matches as rows)

@@ -105,6 +105,12 @@ __global__ void __launch_bounds__(1024) k_scan_counts(const unsigned* __restrict
     if (threadIdx.x == 0) out[n] = carry;
 }
 
+// offs[0..n) = exclusive prefix of counts[0..n), offs[n] = total (device)
+I scan_counts(const unsigned* counts, long long n, unsigned long long* offs) {
+    HG_LAUNCH("counts_scan", 1, 1024, 0, k_scan_counts, counts, n, offs);
+    return last_launch_error();
+}
+
 // pass 2: each tile writes its selected rows from its known offset; each warp
 // walks its 512 rows in rounds of 32 and selected lanes write to consecutive
 // positions found with ballot/popc

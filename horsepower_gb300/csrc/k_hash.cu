@@ -628,26 +628,24 @@ __device__ __forceinline__ void cp_async_wait_all() {
 }
 
 // Probe of a direct-addressed table with i32 keys (the common shape: a
-// dimension's dense integer key).  Same sub-tile layout, look-back and output
-// as k_join_probe, but every load is a cp.async into the thread's own
-// shared-memory column: the R keys, then their R presence-filter words, then
-// the R build rows of the candidates, each group all in flight together and
-// holding no registers, so occupancy stays high.
+// dimension's dense integer key), in two passes with no dependence between
+// tiles.  Pass 1: one bit per probe row -- the row's key is in the table,
+// read from the presence filter -- and each tile's count.  The keys and then
+// their filter words come by cp.async into the thread's own shared-memory
+// column, all R of a group in flight together.  A tile is 256 x R rows: warp
+// w owns words [w R, w R + R) of the tile's 8 R bit words, lane l row 32 k + l
+// of word k.
 template <int R>
-__global__ void __launch_bounds__(JT_THREADS, (R > 16 ? 2 : 4)) k_join_probe_direct(
-    Table<unsigned> t, const int* __restrict__ y, long long n, long long* __restrict__ zb,
-    long long* __restrict__ zp, unsigned long long* status, unsigned* ticket, unsigned long long* total,
-    unsigned* derr) {
-    constexpr long long SUB = 32LL * R;
-    constexpr unsigned NONE = 0xffffffffu;
+__global__ void __launch_bounds__(JT_THREADS, (R > 16 ? 2 : 4)) k_jp_match(Table<unsigned> t, const int* __restrict__ y,
+                                                                          long long n, unsigned* __restrict__ bits,
+                                                                          unsigned* __restrict__ counts) {
     extern __shared__ unsigned jp_smem[];
-    unsigned(*off)[JT_THREADS] = reinterpret_cast<unsigned(*)[JT_THREADS]>(jp_smem);  // key - kmin, NONE when out of range or no candidate
-    unsigned(*buf)[JT_THREADS] = reinterpret_cast<unsigned(*)[JT_THREADS]>(jp_smem + R * JT_THREADS);  // filter word, then build row
-    __shared__ long long tile_id;
+    unsigned(*off)[JT_THREADS] = reinterpret_cast<unsigned(*)[JT_THREADS]>(jp_smem);                   // key - kmin
+    unsigned(*buf)[JT_THREADS] = reinterpret_cast<unsigned(*)[JT_THREADS]>(jp_smem + R * JT_THREADS);  // filter word
+    __shared__ unsigned wc[JT_THREADS / 32];
+    constexpr unsigned NONE = 0xffffffffu;
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5, me = threadIdx.x;
-    if (threadIdx.x == 0) tile_id = atomicAdd(ticket, 1u);
-    __syncthreads();
-    const long long sub = tile_id * (JT_THREADS / 32) + warp, base = sub * SUB;
+    const long long base = (long long)blockIdx.x * (JT_THREADS * R) + (long long)warp * (32 * R);
 #pragma unroll
     for (int k = 0; k < R; k++) {
         long long i = base + k * 32 + lane;
@@ -664,36 +662,90 @@ __global__ void __launch_bounds__(JT_THREADS, (R > 16 ? 2 : 4)) k_join_probe_dir
         if (o != NONE) cp_async4(&buf[k][me], t.filter + (o >> 5));
     }
     cp_async_wait_all();
+    unsigned cnt = 0;
+    unsigned* wout = bits + (long long)blockIdx.x * (8 * R) + (long long)warp * R;
 #pragma unroll
     for (int k = 0; k < R; k++) {
         unsigned o = off[k][me];
-        if (o != NONE) {
-            if ((buf[k][me] >> (o & 31)) & 1u) cp_async4(&buf[k][me], (const unsigned*)t.slots + o);
-            else off[k][me] = NONE;
-        }
+        bool h = o != NONE && ((buf[k][me] >> (o & 31)) & 1u);
+        unsigned bal = __ballot_sync(0xffffffffu, h);
+        if (lane == 0) wout[k] = bal;
+        cnt += __popc(bal);
     }
-    cp_async_wait_all();
-    unsigned hit = 0, cnt = 0;
+    if (lane == 0) wc[warp] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned c = 0;
+        for (int w = 0; w < JT_THREADS / 32; w++) c += wc[w];
+        counts[blockIdx.x] = c;
+    }
+}
+
+// Pass 2: each tile writes the (build row, probe row) pairs of its set bits
+// from its offset (the scan of the tile counts); the build row of a matching
+// row is read from the table's row array.
+template <int R>
+__global__ void __launch_bounds__(JT_THREADS) k_jp_emit(Table<unsigned> t, const int* __restrict__ y, long long n,
+                                                        const unsigned* __restrict__ bits,
+                                                        const unsigned long long* __restrict__ offs,
+                                                        long long* __restrict__ zb, long long* __restrict__ zp) {
+    __shared__ unsigned wc[JT_THREADS / 32];
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    const unsigned* w = bits + (long long)blockIdx.x * (8 * R) + (long long)warp * R;
+    unsigned wd[R];
+    unsigned cnt = 0;
 #pragma unroll
     for (int k = 0; k < R; k++) {
-        bool h = off[k][me] != NONE && buf[k][me] != NONE;
-        hit |= (unsigned)h << k;
-        cnt += __popc(__ballot_sync(0xffffffffu, h));
+        wd[k] = w[k];
+        cnt += __popc(wd[k]);
     }
-    const unsigned long long excl = lookback_exclusive(status, sub, cnt, derr);
-    if (lane == 0 && base < n && base + SUB >= n) *total = excl + cnt;  // the sub-tile holding row n-1
-    unsigned long long pos = excl;
+    if (lane == 0) wc[warp] = cnt;
+    __syncthreads();
+    unsigned long long pos = offs[blockIdx.x];
+    for (unsigned v = 0; v < warp; v++) pos += wc[v];
+    const long long base = (long long)blockIdx.x * (JT_THREADS * R) + (long long)warp * (32 * R);
+    const unsigned* rows = (const unsigned*)t.slots;
+    // the build rows of the set bits, all loads issued before the stores
+    unsigned r[R];
 #pragma unroll
     for (int k = 0; k < R; k++) {
-        bool sel = (hit >> k) & 1u;
-        unsigned bal = __ballot_sync(0xffffffffu, sel);
-        if (sel) {
-            long long o = (long long)pos + __popc(bal & lanemask_lt());
-            __stcs(zb + o, (long long)buf[k][me]);
+        r[k] = 0;
+        if ((wd[k] >> lane) & 1u) r[k] = __ldg(rows + ((long long)__ldg(y + base + k * 32 + lane) - t.kmin));
+    }
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+        if ((wd[k] >> lane) & 1u) {
+            long long o = (long long)pos + __popc(wd[k] & lanemask_lt());
+            __stcs(zb + o, (long long)r[k]);
             __stcs(zp + o, base + k * 32 + lane);
         }
-        pos += __popc(bal);
+        pos += __popc(wd[k]);
     }
+}
+
+I scan_counts(const unsigned* counts, long long n, unsigned long long* offs);
+
+// the two passes and the scan between them; *m receives the match count
+template <int R>
+static I probe_direct(const Table<unsigned>& t, const int* y, long long ny, long long ntiles, long long* zb,
+                      long long* zp, unsigned long long* m) {
+    unsigned* bits = (unsigned*)salloc((size_t)ntiles * 8 * R * 4);
+    unsigned* counts = (unsigned*)salloc((size_t)ntiles * 4);
+    unsigned long long* offs = (unsigned long long*)salloc((size_t)(ntiles + 1) * 8);
+    if (!bits || !counts || !offs) return E_DEVICE_OOM;
+    const size_t sm = (size_t)2 * R * JT_THREADS * 4;
+    static bool attr = false;
+    if (!attr) {
+        HG_CU(cudaFuncSetAttribute(k_jp_match<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        attr = true;
+    }
+    HG_LAUNCH("join_probe", (unsigned)ntiles, JT_THREADS, sm, k_jp_match<R>, t, y, ny, bits, counts);
+    HG_CHECK(scan_counts(counts, ntiles, offs));
+    HG_LAUNCH("join_emit", (unsigned)ntiles, JT_THREADS, 0, k_jp_emit<R>, t, y, ny, (const unsigned*)bits,
+              (const unsigned long long*)offs, zb, zp);
+    HG_CHECK(last_launch_error());
+    HG_CU(cudaMemcpyAsync(m, offs + ntiles, 8, cudaMemcpyDeviceToHost, g_stream));
+    return 0;
 }
 
 // s: one status word per warp sub-tile, then the tile ticket and the total
@@ -702,19 +754,6 @@ static I launch_probe(const Table<K>& t, const LinearBuild& lin, int mode, const
                       long long* zb, long long* zp, char* s, long long ntiles) {
     const long long nsub = ntiles * (JT_THREADS / 32);
     unsigned long long* total = (unsigned long long*)(s + nsub * 8 + 8);
-    if constexpr (sizeof(K) == 4) {
-        if (mode == 0 && t.direct && ytyp == H_I) {
-            const size_t sm = (size_t)2 * R * JT_THREADS * 4;
-            static bool attr = false;
-            if (!attr) {
-                HG_CU(cudaFuncSetAttribute(k_join_probe_direct<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-                attr = true;
-            }
-            HG_LAUNCH("join_probe", (unsigned)ntiles, JT_THREADS, sm, k_join_probe_direct<R>, t, (const int*)py, ny,
-                      zb, zp, (unsigned long long*)s, (unsigned*)(s + nsub * 8), total, g_derr);
-            return last_launch_error();
-        }
-    }
     HG_LAUNCH("join_probe", (unsigned)ntiles, JT_THREADS, 0, (k_join_probe<K, R>), t, lin, mode, py, (int)ytyp, ny, zb,
               zp, (unsigned long long*)s, (unsigned*)(s + nsub * 8), total, g_derr);
     return last_launch_error();
@@ -739,7 +778,17 @@ static I join_probe_unique(V z, const Table<K>& t, const LinearBuild& lin, int m
     char* s = (char*)salloc(sbytes);
     if (!zb || !zp || !s) return E_DEVICE_OOM;
     unsigned long long m = 0;
-    if (ntiles > 0) {
+    bool direct = false;
+    if constexpr (sizeof(K) == 4) direct = mode == 0 && t.direct && ytyp == H_I;
+    if (ntiles > 0 && direct) {
+        if constexpr (sizeof(K) == 4) {
+            const int* y = (const int*)py;
+            if (R == 8) HG_CHECK(probe_direct<8>(t, y, ny, ntiles, zb, zp, &m));
+            else if (R == 32) HG_CHECK(probe_direct<32>(t, y, ny, ntiles, zb, zp, &m));
+            else HG_CHECK(probe_direct<16>(t, y, ny, ntiles, zb, zp, &m));
+        }
+        HG_CHECK(check_device_errors());
+    } else if (ntiles > 0) {
         HG_CU(cudaMemsetAsync(s, 0, sbytes, g_stream));
         if (R == 8) HG_CHECK((launch_probe<K, 8>(t, lin, mode, py, ytyp, ny, zb, zp, s, ntiles)));
         else if (R == 32) HG_CHECK((launch_probe<K, 32>(t, lin, mode, py, ytyp, ny, zb, zp, s, ntiles)));

@@ -40,7 +40,7 @@ I cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
     return e == cudaErrorMemoryAllocation ? E_DEVICE_OOM : E_DEVICE;
 }
 
-int g_tile_rows = 16;  // autotuner knob: probe rows per thread of the tiled join probes
+int g_tile_rows = 8;  // autotuner knob: probe rows per thread of the tiled join probes
 
 // ------------------------------------------------------------------ arenas
 // A bump arena over a list of chunks.  A mark is (chunk index, cursor).

@@ -317,7 +317,7 @@ double hgpuTimerStop(void);
 #define HGPU_TUNE_HASH_LOAD  0   /* hash-table load factor, 0.5 - 0.8 (default 0.5) */
 #define HGPU_TUNE_RADIX_BITS 1   /* LSD radix digit width of @group/@order, 4 - 8 bits (default 8) */
 #define HGPU_TUNE_TILE_ROWS  2   /* probe rows per thread of the tiled join probes: 8, 16, 32
-                                    (tile = 256 x that; default 16) */
+                                    (tile = 256 x that; default 8) */
 I    hgpuSetTuning(I knob, E value);
 E    hgpuGetTuning(I knob);
 

@@ -19,7 +19,7 @@ def L():
     import horsepower_gb300
     L = horsepower_gb300.load()
     yield L
-    T.apply(L, {"tile_rows": 16, "hash_load": 0.5, "radix_bits": 8})
+    T.apply(L, {"tile_rows": 8, "hash_load": 0.5, "radix_bits": 8})
 
 
 def outputs(L, fn):
@@ -44,14 +44,14 @@ def test_join_knobs(L, wide):
     probe = rng.choice(pk, nf) + rng.integers(0, 2, nf) * (7 if wide else nd)
     x, y = L.vec(build.astype(np.int32), H_I), L.vec(probe.astype(np.int32), H_I)
     f = L.sym("eq")
-    T.apply(L, {"tile_rows": 16, "hash_load": 0.5})
+    T.apply(L, {"tile_rows": 8, "hash_load": 0.5})
     ref = outputs(L, lambda: L.call("pfnJoinIndex", x, y, f))
     assert ref[0].size > 0
     for tr in (8, 16, 32):
         for hl in (0.5, 0.65, 0.8):
             T.apply(L, {"tile_rows": tr, "hash_load": hl})
             assert same(outputs(L, lambda: L.call("pfnJoinIndex", x, y, f)), ref), (tr, hl)
-    T.apply(L, {"tile_rows": 16, "hash_load": 0.5})
+    T.apply(L, {"tile_rows": 8, "hash_load": 0.5})
 
 
 def test_radix_bits(L):
@@ -75,15 +75,15 @@ def test_radix_bits(L):
 def test_batched_tile_rows(L):
     tabs = [B.synth_tables(L, 500 + i, n, max(1, n // 4)) for i, n in enumerate([5000, 70_000, 400_000, 1_300_000])]
     plans = [B.make_plan(d, f) for d, f in tabs]
-    T.apply(L, {"tile_rows": 16})
+    T.apply(L, {"tile_rows": 8})
     ref = B.run_batch(L, plans)
-    for tr in (8, 32):
+    for tr in (16, 32):
         T.apply(L, {"tile_rows": tr})
         got = B.run_batch(L, plans)
         for g, r in zip(got, ref):
             for a, b in zip(g, r):
                 assert np.array_equal(a, b)
-    T.apply(L, {"tile_rows": 16})
+    T.apply(L, {"tile_rows": 8})
 
 
 def test_tune_and_clamp(L):
