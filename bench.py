@@ -402,6 +402,123 @@ def run_served(args):
     }
 
 
+def run_builtins(args):
+    """Each accelerated builtin alone on device-resident inputs of the
+    configurations' shapes: call time (CUDA events on the library stream,
+    host work and result-size reads included), the device time of its
+    kernels, rows/s, and algorithmic GB/s (inputs read once, outputs written
+    once) against the measured HBM copy bandwidth.  Returns the JSON line."""
+    import horsepower_gb300
+    from horsepower_gb300 import batch as B
+    from horsepower_gb300 import serve as S
+    from horsepower_gb300.abi import H_B, H_C, H_E, H_I, H_L
+    gpu = horsepower_gb300.load()
+    Lb = gpu.lib
+    Lb.hgpuTimerStop.restype = C.c_double
+    Lb.getHeapOffset.restype = C.c_longlong
+    Lb.setHeapOffset.argtypes = [C.c_longlong]
+    Lb.hgpuProfileRead.restype = C.c_int32
+    Lb.hgpuProfileRead.argtypes = [C.c_int32, C.POINTER(C.c_char_p), C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+    hbm, src = peaks()
+    rng = np.random.default_rng(17)
+    dev = lambda a, t: B.to_device(gpu, a, t)
+    rows = {}
+
+    def measure(name, fn, nrows, nbytes, reps=args.steps):
+        for _ in range(max(1, args.warmup)):
+            m = Lb.getHeapOffset(); fn(); Lb.setHeapOffset(m)
+        ts = []
+        for _ in range(reps):
+            m = Lb.getHeapOffset()
+            Lb.hgpuSync()
+            Lb.hgpuTimerStart()
+            fn()
+            ts.append(Lb.hgpuTimerStop())
+            Lb.setHeapOffset(m)
+        Lb.hgpuProfileReset()
+        Lb.hgpuProfile(1)
+        m = Lb.getHeapOffset(); fn(); Lb.setHeapOffset(m)
+        Lb.hgpuProfile(0)
+        names, tot, cnt = (C.c_char_p * 64)(), (C.c_double * 64)(), (C.c_longlong * 64)()
+        nk = Lb.hgpuProfileRead(64, names, tot, cnt)
+        kern_ms = sum(tot[i] for i in range(min(nk, 64)))
+        call_ms = statistics.median(ts)
+        rows[name] = {"rows": nrows, "call_ms": round(call_ms, 4), "kernel_ms": round(kern_ms, 4),
+                      "rows_per_s": nrows / (call_ms / 1e3), "gbs_call": round(nbytes / (call_ms / 1e3) / 1e9, 1),
+                      "gbs_kernels": round(nbytes / (kern_ms / 1e3) / 1e9, 1) if kern_ms > 0 else None,
+                      "frac_kernels": round(nbytes / (kern_ms / 1e3) / 1e9 / hbm, 3) if kern_ms > 0 else None,
+                      "algorithmic_bytes": int(nbytes),
+                      "kernels": {names[i].decode(): [round(tot[i], 4), int(cnt[i])] for i in range(min(nk, 64))}}
+
+    # ---- filter-aggregate table (6,001,215 rows) and a 60M-row stream
+    t0 = D.filter_table(6_001_215, seed=0)
+    ship, qty = dev(t0["shipdate"], H_I), dev(t0["qty"], H_I)
+    disc, price = dev(t0["disc"], H_E), dev(t0["price"], H_E)
+    m6 = gpu.call("pfnAnd", gpu.call("pfnGeq", ship, gpu.scalar(D.WIN_LO, H_I)), gpu.call("pfnLt", ship, gpu.scalar(D.WIN_HI, H_I)))
+    n6 = 6_001_215
+    sel6 = int(((t0["shipdate"] >= D.WIN_LO) & (t0["shipdate"] < D.WIN_HI)).sum())
+    measure("compress_f64_6M", lambda: gpu.call("pfnCompress", m6, price), n6, n6 + 16 * sel6)
+    ch = P.Chain(gpu, P.Q6_CHAIN.format(lo=D.WIN_LO, hi=D.WIN_HI))
+    measure("q6_fused_chain_6M", lambda: ch.run([ship, qty, disc, price]), n6, 24 * n6)
+    measure("q6_builtins_6M", lambda: P.filter_aggregate(gpu, dict(shipdate=ship, qty=qty, disc=disc, price=price)),
+            n6, 24 * n6)
+    N = 60_000_000
+    a = dev(rng.standard_normal(N), H_E)
+    b = dev(rng.standard_normal(N), H_E)
+    mk = dev(rng.random(N) < 0.5, H_B)
+    mk2 = dev(rng.random(N) < 0.5, H_B)
+    measure("compare_f64_60M", lambda: gpu.call("pfnGt", a, gpu.scalar(0.25, H_E)), N, 9 * N)
+    measure("arith_mul_f64_60M", lambda: gpu.call("pfnMul", a, b), N, 24 * N)
+    measure("logic_and_60M", lambda: gpu.call("pfnAnd", mk, mk2), N, 3 * N)
+    measure("compress_f64_60M_half", lambda: gpu.call("pfnCompress", mk, a), N, N + 16 * (N // 2))
+    measure("where_60M_half", lambda: gpu.call("pfnWhere", mk), N, N + 8 * (N // 2))
+    measure("sum_f64_60M", lambda: gpu.call("pfnSum", a), N, 8 * N)
+    measure("max_f64_60M", lambda: gpu.call("pfnMax", a), N, 8 * N)
+    idx = dev(np.flatnonzero(rng.random(N) < 0.145).astype(np.int64), H_L)
+    M = int(idx.len)
+    measure("index_f64_asc_8.7M_of_60M", lambda: gpu.call("pfnIndex", a, idx), M, 24 * M)
+    ridx = dev(rng.integers(0, N, M).astype(np.int64), H_L)
+    measure("index_f64_random_8.7M_of_60M", lambda: gpu.call("pfnIndex", a, ridx), M, 24 * M)
+    # ---- join (the join + group-by configuration)
+    dim, fact = B.synth_tables(gpu, 1, args.fact, args.dim)
+    keep = gpu.call("pfnCompress", gpu.call("pfnAnd", gpu.call("pfnGeq", dim["date"], gpu.scalar(D.WIN_LO, H_I)),
+                                            gpu.call("pfnLt", dim["date"], gpu.scalar(D.WIN_HI, H_I))), dim["pk"])
+    eqs = gpu.sym("eq")
+    j = gpu.call("pfnJoinIndex", keep, fact["fk"], eqs)
+    Mj = int(V0.from_address(j.g).len)
+    measure("join_index_60M_x_2.2M", lambda: gpu.call("pfnJoinIndex", keep, fact["fk"], eqs), args.fact,
+            4 * args.fact + 4 * int(keep.len) + 16 * Mj)
+    measure("member_60M_in_2.2M", lambda: gpu.call("pfnMember", fact["fk"], keep), args.fact,
+            4 * args.fact + 4 * int(keep.len) + args.fact)
+    measure("index_of_60M_in_2.2M", lambda: gpu.call("pfnIndexOf", keep, fact["fk"]), args.fact,
+            4 * args.fact + 4 * int(keep.len) + 8 * args.fact)
+    g2 = gpu.call("pfnGroup", gpu.list([fact["flag"], fact["status"]]))
+    measure("group_trie_2x1B_60M", lambda: gpu.call("pfnGroup", gpu.list([fact["flag"], fact["status"]])), args.fact,
+            2 * args.fact + 8 * args.fact)
+    # ---- high-cardinality group-by and stable order (150M rows)
+    o = S.order_table(gpu, args.order_rows, seed=2)
+    pay = dev(rng.uniform(0.0, 1e5, args.order_rows), H_E)
+    n2 = args.order_rows
+    measure("group_i64_zipf_150M", lambda: gpu.call("pfnGroup", o["key"]), n2, 16 * n2, reps=max(2, args.steps // 2))
+    g = gpu.call("pfnGroup", o["key"])
+    vals = gpu.call("pfnValues", g)
+    ng = int(gpu.call("pfnKeys", g).len)
+    measure("group_sum_f64_150M", lambda: gpu.call("hgpuGroupSum", pay, vals), n2, 16 * n2 + 8 * ng)
+    measure("group_len_150M", lambda: gpu.call("hgpuGroupLen", pay, vals), n2, 16 * ng)  # group starts in, lengths out
+    dirs = gpu.vec(np.array([1, 1], bool), H_B)
+    measure("order_i64_i32_150M", lambda: gpu.call("pfnOrderBy", gpu.list([o["key"], o["sec"]]), dirs), n2, 20 * n2,
+            reps=max(2, args.steps // 2))
+    top = max(rows.items(), key=lambda kv: kv[1]["kernel_ms"])
+    return {
+        "metric": "GB/s & rows/s per builtin", "value": top[1]["gbs_kernels"], "unit": "GB/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "per builtin", "data": "synthetic (seeded)",
+        "config": {"workload": "each builtin alone on the configurations' shapes; inputs resident in HBM, "
+                               "larger than L2 (except the 6M-row table)", "peak_gbs": hbm, "peak_source": src},
+        "builtins": rows,
+    }
+
+
 def cpu_sample(args):
     """The oracle port on a bounded sample of the workload (fact and dim scaled by 1/10)."""
     ora = Builtins(os.path.join(ROOT, "oracle", "_build", "liboracle.so"), "oracle")
@@ -430,7 +547,7 @@ def main():
     ap.add_argument("--dim", type=int, default=15_000_000)
     ap.add_argument("--cpu-scale", type=int, default=10)
     ap.add_argument("--cpu-reps", type=int, default=3)
-    ap.add_argument("--workload", default="join_group", choices=["join_group", "batched", "served"])
+    ap.add_argument("--workload", default="join_group", choices=["join_group", "batched", "served", "builtins"])
     ap.add_argument("--rates", default="200,1000,5000")
     ap.add_argument("--serve-seconds", type=float, default=1.5)
     ap.add_argument("--order-rows", type=int, default=150_000_000)
@@ -439,8 +556,8 @@ def main():
     ap.add_argument("--max-fact", type=int, default=20_000_000)
     args = ap.parse_args()
     rank, ws, dist = dist_init(args.gpus)
-    if args.workload in ("batched", "served") and args.impl == "gb300":
-        line = run_batched(args) if args.workload == "batched" else run_served(args)
+    if args.workload in ("batched", "served", "builtins") and args.impl == "gb300":
+        line = {"batched": run_batched, "served": run_served, "builtins": run_builtins}[args.workload](args)
         if rank == 0:
             print(json.dumps(line))
         return

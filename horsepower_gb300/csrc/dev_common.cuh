@@ -170,6 +170,31 @@ __device__ __forceinline__ unsigned long long chain_lookback(unsigned long long*
     return excl;
 }
 
+// ---- compareFloat (h_primitive.cc:1061) against a fixed double s without
+// FP64 arithmetic.  With s fixed, compareFloat(v, s) is a non-decreasing step
+// function of v (-1, then 0, then 1) and compareFloat(s, v) a non-increasing
+// one, so both reduce to two thresholds on an integer image of v that keeps
+// the IEEE order: c = ord(v) < ta ? ca : (ord(v) < tb ? cb : cc).  The host
+// finds the thresholds by bisection, evaluating compareFloat itself in
+// double arithmetic; NaN compares as 1 either way round.
+struct F64Cmp {
+    long long ta, tb;
+    int ca, cb, cc;
+};
+__host__ __device__ __forceinline__ long long f64_ord(unsigned long long b) {
+    return (b >> 63) ? -(long long)(b & 0x7fffffffffffffffull) : (long long)b;  // -0.0 and +0.0 both map to 0
+}
+__host__ __device__ __forceinline__ bool f64_nan_bits(unsigned long long b) {
+    return (b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+}
+__device__ __forceinline__ int f64_cmp_fixed(double v, const F64Cmp& t) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    if (f64_nan_bits(b)) return 1;
+    const long long o = f64_ord(b);
+    return o < t.ta ? t.ca : (o < t.tb ? t.cb : t.cc);
+}
+F64Cmp f64_cmp_thresholds(double s, bool scalar_first);  // host (k_elementwise.cu)
+
 // ---- fixed-order deterministic tile sum (used by @sum/@avg and every
 // segmented sum).  A chunk of up to TILE_SUM = 4096 elements is summed as:
 //   lane t (0..255) accumulates e[t], e[t+256], ..., e[t+3840] in order

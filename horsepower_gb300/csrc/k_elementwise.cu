@@ -15,6 +15,9 @@
 // chunk is aligned and complete.  Operands of different types are first
 // converted to the common type (the reference's promoteValue), then the
 // same-type kernel runs.
+#include <climits>
+#include <cstring>
+
 #include "dev_common.cuh"
 
 namespace hg {
@@ -265,6 +268,65 @@ static I vector_as(V x, I xt, const T** out) {
     return 0;
 }
 
+static int compare_float_host(double a, double b) {
+    return a < b ? ((b - a) < H_EPSILON ? 0 : -1) : ((a - b) < H_EPSILON ? 0 : 1);
+}
+static double from_ord(long long o) {
+    unsigned long long b = o >= 0 ? (unsigned long long)o : (0x8000000000000000ull | (unsigned long long)(-o));
+    double d;
+    memcpy(&d, &b, 8);
+    return d;
+}
+
+F64Cmp f64_cmp_thresholds(double s, bool scalar_first) {
+    F64Cmp t;
+    if (s != s) {  // a NaN operand compares as 1 everywhere
+        t.ta = t.tb = LLONG_MAX;
+        t.ca = t.cb = t.cc = 1;
+        return t;
+    }
+    const long long lo = f64_ord(0xfff0000000000000ull), hi = f64_ord(0x7ff0000000000000ull) + 1;  // -inf .. +inf + 1
+    auto c = [&](long long o) { return scalar_first ? compare_float_host(s, from_ord(o)) : compare_float_host(from_ord(o), s); };
+    // smallest o in [lo, hi] with pred(o); o = hi stands for "no such value"
+    auto first = [&](auto pred) {
+        long long a = lo, b = hi;
+        while (a < b) {
+            long long m = a + (long long)(((unsigned long long)b - (unsigned long long)a) / 2);  // b - a can exceed 2^63
+            if (pred(m)) b = m; else a = m + 1;
+        }
+        return a;
+    };
+    if (!scalar_first) {  // compareFloat(v, s): -1, 0, 1 as v grows
+        t.ta = first([&](long long o) { return c(o) >= 0; });
+        t.tb = first([&](long long o) { return c(o) >= 1; });
+        t.ca = -1; t.cb = 0; t.cc = 1;
+    } else {  // compareFloat(s, v): 1, 0, -1 as v grows
+        t.ta = first([&](long long o) { return c(o) <= 0; });
+        t.tb = first([&](long long o) { return c(o) <= -1; });
+        t.ca = 1; t.cb = 0; t.cc = -1;
+    }
+    return t;
+}
+
+// a double vector against a fixed double, by the integer thresholds
+__global__ void __launch_bounds__(256) k_compare_f64_fixed(const double* __restrict__ x, bool* __restrict__ z,
+                                                           long long n, int op, F64Cmp t) {
+    long long nchunks = (n + 15) / 16;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < nchunks;
+         c += (long long)gridDim.x * blockDim.x) {
+        long long i0 = c * 16;
+        double a[16];
+        load16(x, i0, n, a);
+        bool r[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            int cv = f64_cmp_fixed(a[k], t);
+            r[k] = op == 0 ? cv < 0 : op == 1 ? cv <= 0 : op == 2 ? cv > 0 : op == 3 ? cv >= 0 : op == 4 ? cv == 0 : cv != 0;
+        }
+        store16(z, i0, n, r);
+    }
+}
+
 template <typename T>
 static I run_compare(V z, V x, V y, I typX, int op) {
     bool ox = x->len == 1, oy = y->len == 1;
@@ -276,6 +338,15 @@ static I run_compare(V z, V x, V y, I typX, int op) {
     if (mode == MODE_VS) HG_CHECK(scalar_as<T>(y, &sy)); else HG_CHECK(vector_as<T>(y, typX, &py));
     void* dz;
     HG_CHECK(alloc_out(z, H_B, n, &dz));
+    if constexpr (std::is_same<T, double>::value) {
+        if (mode != MODE_VV && n > 0) {  // one side fixed: integer thresholds instead of FP64 subtractions
+            const F64Cmp t = f64_cmp_thresholds(mode == MODE_SV ? sx : sy, mode == MODE_SV);
+            HG_LAUNCH("compare", ew_grid(n), 256, 0, k_compare_f64_fixed, mode == MODE_SV ? py : px, (bool*)dz,
+                      (long long)n, op, t);
+            HG_CHECK(last_launch_error());
+            return finish_out(z, dz);
+        }
+    }
     if (n > 0) HG_LAUNCH("compare", ew_grid(n), 256, 0, k_compare<T>, px, py, (bool*)dz, (long long)n, op, mode, sx, sy);
     HG_CHECK(last_launch_error());
     return finish_out(z, dz);

@@ -178,6 +178,16 @@ struct Gen {
             std::string ca = std::string("((") + ctype(t) + ")" + a[0] + ")", cb = std::string("((") + ctype(t) + ")" + a[1] + ")";
             if (cmp.count(o)) {
                 n->typ = H_B;
+                const bool la = n->kids[0]->op == "lit", lb = n->kids[1]->op == "lit";
+                if (t == H_E && la != lb) {
+                    // f64 against a literal: compareFloat by integer thresholds (no FP64 subtraction)
+                    const std::string& lt = (la ? n->kids[0] : n->kids[1])->lit;
+                    const double sv = strtod(lt.substr(0, lt.find(':')).c_str(), nullptr);
+                    const F64Cmp th = f64_cmp_thresholds(sv, la);
+                    return "hg_cmpf_fixed(" + (la ? cb : ca) + ", " + std::to_string(th.ta) + "LL, " +
+                           std::to_string(th.tb) + "LL, " + std::to_string(th.ca) + ", " + std::to_string(th.cb) +
+                           ", " + std::to_string(th.cc) + ", " + std::to_string(cmp.at(o)) + ")";
+                }
                 return "hg_cmp<" + std::string(ctype(t)) + ">(" + std::to_string(cmp.at(o)) + ", " + ca + ", " + cb + ")";
             }
             if (ari.at(o) == 3) uses_div = true;
@@ -196,6 +206,16 @@ static const char* kPrelude = R"(
 template <typename T> struct hg_is_f { static const bool v = false; };
 template <> struct hg_is_f<float> { static const bool v = true; };
 template <> struct hg_is_f<double> { static const bool v = true; };
+__device__ __forceinline__ bool hg_cmpf_fixed(double v, long long ta, long long tb, int ca, int cb, int cc, int op) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    int c;
+    if ((b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) c = 1;
+    else {
+        const long long o = (b >> 63) ? -(long long)(b & 0x7fffffffffffffffull) : (long long)b;
+        c = o < ta ? ca : (o < tb ? cb : cc);
+    }
+    return op == 0 ? c < 0 : op == 1 ? c <= 0 : op == 2 ? c > 0 : op == 3 ? c >= 0 : op == 4 ? c == 0 : c != 0;
+}
 template <typename T> __device__ __forceinline__ bool hg_cmp(int op, T a, T b) {
     if (hg_is_f<T>::v) {
         int c = a < b ? ((double)(b - a) < 1e-13 ? 0 : -1) : ((double)(a - b) < 1e-13 ? 0 : 1);

@@ -313,16 +313,19 @@ __global__ void k_node_lens(const V0* __restrict__ nodes, long long ng, unsigned
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x)
         lens[g] = (unsigned)nodes[g].len;
 }
-// copies each element's payload (es bytes per item) to data + off[g]; an
-// inline element's payload sits in the node itself
-__global__ void k_node_copy(const V0* __restrict__ nodes, long long ng, const unsigned long long* __restrict__ off,
-                            int es, char* __restrict__ data) {
+// copies each element's payload to data + off[g] * es, one warp per element
+// and one item per lane; `nodes` is a device copy of the host node array at
+// host_base, so an inline element (its g points into its own host node)
+// reads its item from the copy
+template <typename T>
+__global__ void k_node_copy(const V0* __restrict__ nodes, long long ng, unsigned long long host_base,
+                            const unsigned long long* __restrict__ off, T* __restrict__ data) {
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
     for (long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ng; g += warps) {
-        const V0& v = nodes[g];
-        const char* src = (v.len <= 1) ? (const char*)&v.b : (const char*)v.g;
-        long long nb = v.len * es;
-        for (long long b = lane_id(); b < nb; b += 32) data[off[g] * es + b] = src[b];
+        const V0 v = nodes[g];
+        const unsigned long long own = host_base + (unsigned long long)g * sizeof(V0) + offsetof(V0, b);
+        const T* src = ((unsigned long long)v.g == own) ? reinterpret_cast<const T*>(&nodes[g].b) : (const T*)v.g;
+        for (long long b = lane_id(); b < v.len; b += 32) data[off[g] + b] = src[b];
     }
 }
 __global__ void k_offsets_i64(const unsigned long long* __restrict__ a, long long n, long long* __restrict__ b) {
@@ -331,9 +334,8 @@ __global__ void k_offsets_i64(const unsigned long long* __restrict__ a, long lon
 }
 
 // Segments of a list whose elements all have type `typ`.  Lists built by this
-// library are found in the registry; any other list is read through its
-// nodes (copied to pinned memory first when the caller's node array is
-// pageable).  Payloads must be device-readable.
+// library are found in the registry; any other list is read through a device
+// copy of its nodes.  Payloads must be device-readable.
 static I list_segments(V y, I typ, const long long** starts, long long* total, const void** data,
                        ListInfo** info = nullptr) {
     long long ng = y->len;
@@ -350,15 +352,19 @@ static I list_segments(V y, I typ, const long long** starts, long long* total, c
     int es = esize(typ);
     for (long long g = 0; g < ng; g++) {
         if (nodes[g].typ != typ) return set_error(E_TYPE, "list element %lld has type %d, expected %d", g, nodes[g].typ, typ);
-        if (nodes[g].len > 1 && !is_device_ptr(nodes[g].g))
+        const bool inl = nodes[g].g == (G)&nodes[g].b;
+        if (nodes[g].len > 0 && !inl && !is_device_ptr(nodes[g].g))
             return set_error(E_NOT_IMPL, "list element %lld lives in pageable host memory; stage it with hgpuToDevice", g);
+        if (inl && nodes[g].len > 1) return set_error(E_DOMAIN, "list element %lld: inline node with %lld items", g, nodes[g].len);
     }
-    if (!is_device_ptr(nodes)) {
-        V0* pin = (V0*)halloc((size_t)(ng > 0 ? ng : 1) * sizeof(V0));
-        if (!pin) return E_DEVICE_OOM;
-        memcpy(pin, nodes, (size_t)ng * sizeof(V0));
-        nodes = pin;
-    }
+    // the kernels read a device copy of the node array (one bulk copy, not
+    // one host access per node)
+    const unsigned long long host_base = (unsigned long long)(uintptr_t)nodes;
+    V0* dn = (V0*)salloc((size_t)(ng > 0 ? ng : 1) * sizeof(V0));
+    if (!dn) return E_DEVICE_OOM;
+    if (ng > 0) HG_CU(cudaMemcpyAsync(dn, nodes, (size_t)ng * sizeof(V0), cudaMemcpyDefault, g_stream));
+    if (!is_device_ptr(nodes)) HG_CU(cudaStreamSynchronize(g_stream));  // pageable source: finish before returning
+    nodes = dn;
     unsigned* lens = (unsigned*)salloc((size_t)(ng > 0 ? ng : 1) * 4);
     unsigned long long* off = (unsigned long long*)salloc((size_t)(ng > 0 ? ng : 1) * 8);
     long long* st = (long long*)salloc((size_t)(ng > 0 ? ng : 1) * 8);
@@ -371,7 +377,14 @@ static I list_segments(V y, I typ, const long long** starts, long long* total, c
     char* d = (char*)salloc((size_t)(tot > 0 ? tot : 1) * es);
     if (!d) return E_DEVICE_OOM;
     if (ng > 0) {
-        HG_LAUNCH("node_copy", gcap(ng * 32), 256, 0, k_node_copy, nodes, ng, off, es, d);
+        const unsigned gr = gcap(ng * 32);
+        switch (es) {
+        case 1: HG_LAUNCH("node_copy", gr, 256, 0, k_node_copy<uint8_t>, nodes, ng, host_base, off, (uint8_t*)d); break;
+        case 2: HG_LAUNCH("node_copy", gr, 256, 0, k_node_copy<uint16_t>, nodes, ng, host_base, off, (uint16_t*)d); break;
+        case 4: HG_LAUNCH("node_copy", gr, 256, 0, k_node_copy<uint32_t>, nodes, ng, host_base, off, (uint32_t*)d); break;
+        default: HG_LAUNCH("node_copy", gr, 256, 0, k_node_copy<unsigned long long>, nodes, ng, host_base, off,
+                           (unsigned long long*)d); break;
+        }
         HG_LAUNCH("offsets", gcap(ng), 256, 0, k_offsets_i64, off, ng, st);
     }
     *starts = st;
@@ -380,21 +393,24 @@ static I list_segments(V y, I typ, const long long** starts, long long* total, c
     return last_launch_error();
 }
 
-// writes ng one-element nodes holding vals[g] (es bytes) into a pinned node array
-__global__ void k_scalar_nodes(const char* __restrict__ vals, long long ng, int es, I typ, V0* __restrict__ nodes) {
+// writes ng one-element nodes holding vals[g] (es bytes) into a device
+// staging copy of the host node array at host_base (node g inline: its g
+// points at its own host node)
+__global__ void k_scalar_nodes(const char* __restrict__ vals, long long ng, int es, I typ, V0* __restrict__ out,
+                               unsigned long long host_base) {
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x) {
         V0 v;
         v.len = 1;
         v.typ = typ;
         v.i64 = 0;
         for (int b = 0; b < es; b++) ((char*)&v.b)[b] = vals[g * es + b];
-        v.g = (G)&nodes[g].b;
-        nodes[g] = v;
+        v.g = (G)(host_base + (unsigned long long)g * sizeof(V0) + offsetof(V0, b));
+        out[g] = v;
     }
 }
 // segment nodes over a contiguous payload (inline when one element)
 __global__ void k_segment_nodes(const char* __restrict__ data, const long long* __restrict__ starts, long long ng,
-                                long long total, int es, I typ, V0* __restrict__ nodes) {
+                                long long total, int es, I typ, V0* __restrict__ out, unsigned long long host_base) {
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x) {
         long long s = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total;
         V0 v;
@@ -403,11 +419,11 @@ __global__ void k_segment_nodes(const char* __restrict__ data, const long long* 
         v.i64 = 0;
         if (e - s == 1) {
             for (int b = 0; b < es; b++) ((char*)&v.b)[b] = data[s * es + b];
-            v.g = (G)&nodes[g].b;
+            v.g = (G)(host_base + (unsigned long long)g * sizeof(V0) + offsetof(V0, b));
         } else {
             v.g = (G)(data + s * es);
         }
-        nodes[g] = v;
+        out[g] = v;
     }
 }
 
@@ -472,7 +488,11 @@ I pfnEachRight(V z, V x, V y, I (*foo)(V, V, V)) {
             HG_CHECK(check_device_errors());
             HG_CU(cudaMemcpyAsync(keep, starts, (size_t)ng * 8, cudaMemcpyDeviceToDevice, g_stream));
             HG_CHECK(init_list(z, H_G, ng));
-            HG_LAUNCH("segment_nodes", gcap(ng), 256, 0, k_segment_nodes, data, keep, ng, total, es, x->typ, host_nodes(z));
+            V0* stage = (V0*)salloc((size_t)ng * sizeof(V0));
+            if (!stage) return E_DEVICE_OOM;
+            HG_LAUNCH("segment_nodes", gcap(ng), 256, 0, k_segment_nodes, data, keep, ng, total, es, x->typ, stage,
+                      (unsigned long long)(uintptr_t)host_nodes(z));
+            HG_CU(cudaMemcpyAsync(host_nodes(z), stage, (size_t)ng * sizeof(V0), cudaMemcpyDeviceToHost, g_stream));
             HG_CHECK(last_launch_error());
             HG_CHECK(sync());
             register_list({host_nodes(z), ng, LIST_SEGMENTS, x->typ, keep, total, data, 0, 0, 0, 0, nullptr, nullptr, nullptr});
@@ -514,7 +534,11 @@ I pfnEach(V z, V x, I (*foo)(V, V)) {
             if (!keep) return E_DEVICE_OOM;
             HG_CU(cudaMemcpyAsync(keep, res, (size_t)ng * es, cudaMemcpyDeviceToDevice, g_stream));
             HG_CHECK(init_list(z, H_G, ng));
-            HG_LAUNCH("scalar_nodes", gcap(ng), 256, 0, k_scalar_nodes, keep, ng, es, typ, host_nodes(z));
+            V0* stage = (V0*)salloc((size_t)ng * sizeof(V0));
+            if (!stage) return E_DEVICE_OOM;
+            HG_LAUNCH("scalar_nodes", gcap(ng), 256, 0, k_scalar_nodes, keep, ng, es, typ, stage,
+                      (unsigned long long)(uintptr_t)host_nodes(z));
+            HG_CU(cudaMemcpyAsync(host_nodes(z), stage, (size_t)ng * sizeof(V0), cudaMemcpyDeviceToHost, g_stream));
             HG_CHECK(last_launch_error());
             HG_CHECK(sync());
             register_list({host_nodes(z), ng, LIST_SCALARS, typ, nullptr, ng, keep, 0, 0, 0, 0, nullptr, nullptr, nullptr});

@@ -34,11 +34,6 @@ I plan_through_builtins(const hgpuJoinGroupPlan& q, hgpuJoinGroupResult* r);
 
 constexpr int SQ_MAXW = 256;  // request windows per shared-scan launch
 
-// compareFloat (h_primitive.cc:1061): equal within an absolute 1e-13
-__device__ __forceinline__ int cmpf(double a, double b) {
-    return a < b ? ((b - a) < H_EPSILON ? 0 : -1) : ((a - b) < H_EPSILON ? 0 : 1);
-}
-
 // One block per 4096-row tile of the lineitem table.  Each thread evaluates
 // the request-independent part of q6 (qty < 24, 0.05 <= disc <= 0.07, the
 // value price*disc) for its 16 rows once, then for every request window sums
@@ -48,7 +43,7 @@ __device__ __forceinline__ int cmpf(double a, double b) {
 __global__ void __launch_bounds__(256) k_s_q6(const int* __restrict__ ship, const int* __restrict__ qty,
                                               const double* __restrict__ disc, const double* __restrict__ price,
                                               long long n, const int* __restrict__ lohi, int nw,
-                                              double* __restrict__ part, long long ntiles) {
+                                              double* __restrict__ part, long long ntiles, F64Cmp d_lo, F64Cmp d_hi) {
     __shared__ int s_lo[SQ_MAXW], s_hi[SQ_MAXW];
     __shared__ double ws[SQ_MAXW][8];
     for (int w = threadIdx.x; w < nw; w += 256) {
@@ -66,7 +61,7 @@ __global__ void __launch_bounds__(256) k_s_q6(const int* __restrict__ ship, cons
         v[k] = 0.0;
         if (i < n) {
             double dc = disc[i];
-            bool c = qty[i] < 24 && cmpf(dc, 0.05) >= 0 && cmpf(dc, 0.07) <= 0;
+            bool c = qty[i] < 24 && f64_cmp_fixed(dc, d_lo) >= 0 && f64_cmp_fixed(dc, d_hi) <= 0;
             d[k] = ship[i];
             v[k] = __dmul_rn(price[i], dc);
             live |= (unsigned)c << k;
@@ -461,10 +456,11 @@ static I filter_aggs(const hgpu_server_s* s, const hgpuRequest* req, const std::
     double* part = (double*)salloc((size_t)nw * ntiles * 8);
     if (!dl || !part) return E_DEVICE_OOM;
     HG_CU(cudaMemcpyAsync(dl, lohi.data(), 8 * nw, cudaMemcpyHostToDevice, g_stream));
+    const F64Cmp d_lo = f64_cmp_thresholds(0.05, false), d_hi = f64_cmp_thresholds(0.07, false);
     for (long long c0 = 0; c0 < nw; c0 += SQ_MAXW) {
         int cw = (int)std::min<long long>(SQ_MAXW, nw - c0);
         HG_LAUNCH("serve_q6", (unsigned)ntiles, 256, 0, k_s_q6, t.l_shipdate, t.l_qty, t.l_disc, t.l_price, t.nline,
-                  dl + 2 * c0, cw, part + c0 * ntiles, ntiles);
+                  dl + 2 * c0, cw, part + c0 * ntiles, ntiles, d_lo, d_hi);
     }
     double* cur = part;
     long long m = ntiles;

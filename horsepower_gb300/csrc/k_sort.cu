@@ -85,6 +85,11 @@ __global__ void k_bucket_base(const unsigned long long* __restrict__ hist, unsig
     base[p * 256 + d] = s[d];
 }
 
+// One LSD pass per launch: each tile ranks its keys by digit (warp
+// match_any, per-warp histograms), takes each digit's global offset from a
+// decoupled look-back over the per-digit counts of the preceding tiles,
+// stages the tile in shared memory in digit order and writes each digit's
+// run contiguously.
 template <typename K, bool FIRST>
 __global__ void __launch_bounds__(RS_THREADS, 3) k_onesweep(const K* __restrict__ kin, const unsigned* __restrict__ vin,
                                                          K* __restrict__ kout, unsigned* __restrict__ vout, long long n,
@@ -361,12 +366,6 @@ __global__ void k_minmax_i64(const void* p, int typ, long long n, long long* mn,
     }
     if (lane_id() == 0) { atomicMin(mn, a); atomicMax(mx, b); }
 }
-__global__ void k_any_high(const long long* __restrict__ x, long long n, unsigned* flag) {
-    bool any = false;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        any |= (x[i] >> 32) > 0;
-    if (__any_sync(0xffffffffu, any) && lane_id() == 0) atomicOr(flag, 1u);
-}
 
 // ------------------------------------------------------------- permutations
 __global__ void k_widen(const unsigned* __restrict__ v, long long n, long long* __restrict__ out, int reverse) {
@@ -401,9 +400,11 @@ __global__ void k_bound_cols(ColSet c, const unsigned* __restrict__ perm, long l
     }
 }
 
-// keys[g] = perm[start[g]]; node g = group g's rows (inline when one row)
+// keys[g] = perm[start[g]]; node g = group g's rows (inline when one row),
+// written to a device staging copy of the host node array at host_base
 __global__ void k_group_nodes(const long long* __restrict__ starts, long long ng, long long n,
-                              const long long* __restrict__ perm, long long* __restrict__ keys, V0* __restrict__ nodes) {
+                              const long long* __restrict__ perm, long long* __restrict__ keys, V0* __restrict__ nodes,
+                              unsigned long long host_base) {
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x) {
         long long s = starts[g], e = (g + 1 < ng) ? starts[g + 1] : n;
         long long first = perm[s];
@@ -413,7 +414,7 @@ __global__ void k_group_nodes(const long long* __restrict__ starts, long long ng
         v.typ = H_L;
         if (e - s == 1) {
             v.i64 = first;
-            v.g = (G)&nodes[g].b;
+            v.g = (G)(host_base + (unsigned long long)g * sizeof(V0) + offsetof(V0, b));
         } else {
             v.i64 = 0;
             v.g = (G)(perm + s);
@@ -551,15 +552,13 @@ static I sort_int_column(V x, const void* p, long long n, SortResult* r) {
         r->key_injective = true;
         return sort_by_spec(s, n, 32, r);
     }
-    unsigned* flag = (unsigned*)salloc(16);
-    if (!flag) return E_DEVICE_OOM;
-    HG_CU(cudaMemsetAsync(flag, 0, 4, g_stream));
-    if (n > 0) HG_LAUNCH("any_high", gcap(n), 256, 0, k_any_high, (const long long*)p, n, flag);
-    unsigned f = 0;
-    HG_CU(cudaMemcpyAsync(&f, flag, 4, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    // some value has (x >> 32) > 0 exactly when the maximum is >= 2^32; the
+    // low 32 bits are injective when every value lies in one 2^32-wide range
+    long long mn = 0, mx = 0;
+    if (n > 0) HG_CHECK(col_minmax(p, H_L, n, &mn, &mx));
+    const bool f = n > 0 && mx >= (1LL << 32);
     s.xf[0] = f ? XF_RAW64 : XF_LOW32;
-    r->key_injective = f != 0;
+    r->key_injective = f || n == 0 || ((unsigned long long)mx - (unsigned long long)mn) < (1ull << 32);
     return sort_by_spec(s, n, f ? 64 : 32, r);
 }
 
@@ -705,9 +704,13 @@ static I group_dict(V z, const SortResult& r, long long n, const ColSet* cols) {
     void* dkeys;
     HG_CHECK(alloc_out(&kv[0], H_L, G, &dkeys));
     HG_CHECK(init_list(&kv[1], H_G, G));
-    if (G > 0)
-        HG_LAUNCH("group_nodes", gcap(G), 256, 0, k_group_nodes, starts, G, n, perm, (long long*)dkeys,
-                  host_nodes(&kv[1]));
+    if (G > 0) {
+        V0* stage = (V0*)salloc((size_t)G * sizeof(V0));
+        if (!stage) return E_DEVICE_OOM;
+        HG_LAUNCH("group_nodes", gcap(G), 256, 0, k_group_nodes, starts, G, n, perm, (long long*)dkeys, stage,
+                  (unsigned long long)(uintptr_t)host_nodes(&kv[1]));
+        HG_CU(cudaMemcpyAsync(host_nodes(&kv[1]), stage, (size_t)G * sizeof(V0), cudaMemcpyDeviceToHost, g_stream));
+    }
     HG_CHECK(last_launch_error());
     HG_CHECK(finish_out(&kv[0], dkeys));
     register_bound(kv[0].g, kv[0].len, n);

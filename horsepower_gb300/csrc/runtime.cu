@@ -121,6 +121,16 @@ struct Arena {
             if ((const char*)p >= c.base && (const char*)p < c.base + c.cap) return true;
         return false;
     }
+    // false when p is an allocation of this arena at or after the cursor
+    // (released by a rewind); memory the arena does not own counts as live
+    bool live(const void* p) const {
+        for (size_t k = 0; k < chunks.size(); k++) {
+            const Chunk& c = chunks[k];
+            if ((const char*)p >= c.base && (const char*)p < c.base + c.cap)
+                return k < cur_chunk || (k == cur_chunk && (size_t)((const char*)p - c.base) < c.cur);
+        }
+        return true;
+    }
 };
 
 static size_t env_mb(const char* name, size_t dflt_mb) {
@@ -431,8 +441,20 @@ L setHeapOffset(L cur) {
     cudaStreamSynchronize(g_stream);
     g_out->rewind(g_marks[(size_t)cur].first);
     g_host->rewind(g_marks[(size_t)cur].second);
-    g_lists.clear();  // their node arrays and payloads are released
-    g_bounds.clear();
+    // forget the lists and index ranges whose memory was released; a list
+    // that survives drops a segment plan allocated after the mark
+    auto live = [](const void* p) { return !p || (g_out->live(p) && g_host->live(p)); };
+    std::vector<ListInfo> keep;
+    for (ListInfo& li : g_lists) {
+        if (!live(li.nodes) || !live(li.starts) || !live(li.data)) continue;
+        if (li.planned && (!live(li.big) || !live(li.chunk0) || !live(li.pstarts))) li.planned = 0;
+        keep.push_back(li);
+    }
+    g_lists.swap(keep);
+    std::vector<Bound> kb;
+    for (const Bound& b : g_bounds)
+        if (live(b.data)) kb.push_back(b);
+    g_bounds.swap(kb);
     g_marks.resize((size_t)cur + 1);
     return cur;
 }

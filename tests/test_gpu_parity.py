@@ -238,3 +238,21 @@ def test_join_group_pipeline(libs):
         assert np.array_equal(a[k], b[k])
     for k in (2, 3, 4):
         assert np.allclose(a[k], b[k], rtol=RTOL, atol=0)
+
+
+@pytest.mark.parametrize("s", [0.05, 0.07, 0.0, -0.0, 1e-13, -1e-13, 5e-14, 24.0, 1e300, -1e300, 5e-324,
+                               float("inf"), float("-inf"), float("nan"), 123456.789])
+def test_compare_f64_scalar_edges(libs, s):
+    """f64 compares against a scalar (either side) at compareFloat's 1e-13
+    boundaries, signed zeros, infinities, NaN and denormals: bit-exact."""
+    rng = np.random.default_rng(int(abs(s) * 1000) % 9973 if np.isfinite(s) else 7)
+    base = 0.0 if not np.isfinite(s) else s
+    v = [0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, -5e-324, s, np.nextafter(s, np.inf), np.nextafter(s, -np.inf)]
+    v += [base + k * 2.5e-15 for k in range(-60, 61)] + [base + k * 1e-14 for k in range(-30, 31)]
+    v += list(rng.standard_normal(2000) * 10.0 ** rng.integers(-20, 20, 2000))
+    v = np.array(v * 3, dtype=np.float64)
+    for fn in ("pfnLt", "pfnLeq", "pfnGt", "pfnGeq", "pfnEq", "pfnNeq"):
+        a, b = both(libs, fn, lambda L: (L.vec(v, H_E), L.scalar(s, H_E)))
+        assert same(a, b), (fn, "vs")
+        a, b = both(libs, fn, lambda L: (L.scalar(s, H_E), L.vec(v, H_E)))
+        assert same(a, b), (fn, "sv")
