@@ -41,7 +41,8 @@ __device__ __forceinline__ void copy_elem(const void* src, void* dst, long long 
 
 // A lane's 16 mask bytes (rows base+lofs .. +15), as 0/1 bytes
 __device__ __forceinline__ uint4 load_mask16(const uint8_t* __restrict__ mask, long long n, long long base, int lofs) {
-    if (base + lofs + 16 <= n) return __ldcs(reinterpret_cast<const uint4*>(mask + base + lofs));
+    if (base + lofs + 16 <= n && ((reinterpret_cast<uintptr_t>(mask + base + lofs) & 15) == 0))
+        return __ldcs(reinterpret_cast<const uint4*>(mask + base + lofs));
     uint8_t b[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) b[k] = (base + lofs + k < n) ? (mask[base + lofs + k] != 0) : 0;

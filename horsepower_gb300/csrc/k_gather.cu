@@ -17,19 +17,38 @@ __device__ __forceinline__ long long load_idx(const void* y, long long i) {
 
 template <typename ET, typename IT>
 __global__ void __launch_bounds__(256) k_gather(const ET* __restrict__ x, long long nx, const void* __restrict__ y,
-                                                ET* __restrict__ z, long long n, unsigned* derr) {
+                                                ET* __restrict__ z, long long n, unsigned* derr, int vec) {
     bool bad = false;
     long long stride = (long long)gridDim.x * blockDim.x * 4;
     for (long long i0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 4; i0 < n; i0 += stride) {
         long long ix[4];
+        if constexpr (sizeof(IT) == 8) {
+            if (vec && i0 + 4 <= n) {  // the thread's 4 indices: two 16-byte loads (i0 is a multiple of 4)
+                const longlong2* q = reinterpret_cast<const longlong2*>((const long long*)y + i0);
+                longlong2 a = __ldcs(q), b = __ldcs(q + 1);
+                ix[0] = a.x; ix[1] = a.y; ix[2] = b.x; ix[3] = b.y;
+            } else {
 #pragma unroll
-        for (int k = 0; k < 4; k++) ix[k] = (i0 + k < n) ? load_idx<IT>(y, i0 + k) : 0;
+                for (int k = 0; k < 4; k++) ix[k] = (i0 + k < n) ? load_idx<IT>(y, i0 + k) : 0;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++) ix[k] = (i0 + k < n) ? load_idx<IT>(y, i0 + k) : 0;
+        }
         ET v[4];
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             bool ok = ix[k] >= 0 && ix[k] < nx;
             if (!ok && i0 + k < n) bad = true;
             v[k] = (ok && i0 + k < n) ? __ldg(x + ix[k]) : ET(0);
+        }
+        if constexpr (sizeof(ET) == 8) {
+            if (vec && i0 + 4 <= n) {
+                ulonglong2* q = reinterpret_cast<ulonglong2*>(z + i0);
+                q[0] = make_ulonglong2((unsigned long long)v[0], (unsigned long long)v[1]);
+                q[1] = make_ulonglong2((unsigned long long)v[2], (unsigned long long)v[3]);
+                continue;
+            }
         }
 #pragma unroll
         for (int k = 0; k < 4; k++)
@@ -43,12 +62,14 @@ static void launch_gather(const void* x, long long nx, const void* y, I ytyp, vo
     unsigned grid = grid_for((n + 3) / 4, 256);
     unsigned cap = (unsigned)g_sms * 16;
     if (grid > cap) grid = cap;
+    // 16-byte index loads and value stores need both vectors 16-byte aligned
+    const int vec = (((uintptr_t)y | (uintptr_t)z) & 15) == 0;
     switch (ytyp) {
-    case H_B: HG_LAUNCH("gather", grid, 256, 0, (k_gather<ET, bool>), (const ET*)x, nx, y, (ET*)z, n, g_derr); break;
-    case H_J: HG_LAUNCH("gather", grid, 256, 0, (k_gather<ET, int8_t>), (const ET*)x, nx, y, (ET*)z, n, g_derr); break;
-    case H_H: HG_LAUNCH("gather", grid, 256, 0, (k_gather<ET, int16_t>), (const ET*)x, nx, y, (ET*)z, n, g_derr); break;
-    case H_I: HG_LAUNCH("gather", grid, 256, 0, (k_gather<ET, int32_t>), (const ET*)x, nx, y, (ET*)z, n, g_derr); break;
-    default: HG_LAUNCH("gather", grid, 256, 0, (k_gather<ET, long long>), (const ET*)x, nx, y, (ET*)z, n, g_derr); break;
+    case H_B: HG_LAUNCH("gather", grid, 256, 0, (k_gather<ET, bool>), (const ET*)x, nx, y, (ET*)z, n, g_derr, vec); break;
+    case H_J: HG_LAUNCH("gather", grid, 256, 0, (k_gather<ET, int8_t>), (const ET*)x, nx, y, (ET*)z, n, g_derr, vec); break;
+    case H_H: HG_LAUNCH("gather", grid, 256, 0, (k_gather<ET, int16_t>), (const ET*)x, nx, y, (ET*)z, n, g_derr, vec); break;
+    case H_I: HG_LAUNCH("gather", grid, 256, 0, (k_gather<ET, int32_t>), (const ET*)x, nx, y, (ET*)z, n, g_derr, vec); break;
+    default: HG_LAUNCH("gather", grid, 256, 0, (k_gather<ET, long long>), (const ET*)x, nx, y, (ET*)z, n, g_derr, vec); break;
     }
 }
 

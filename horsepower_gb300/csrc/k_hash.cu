@@ -630,44 +630,33 @@ __device__ __forceinline__ void cp_async_wait_all() {
 // Probe of a direct-addressed table with i32 keys (the common shape: a
 // dimension's dense integer key), in two passes with no dependence between
 // tiles.  Pass 1: one bit per probe row -- the row's key is in the table,
-// read from the presence filter -- and each tile's count.  The keys and then
-// their filter words come by cp.async into the thread's own shared-memory
-// column, all R of a group in flight together.  A tile is 256 x R rows: warp
-// w owns words [w R, w R + R) of the tile's 8 R bit words, lane l row 32 k + l
-// of word k.
+// read from the presence filter -- and each tile's count.  A tile is 256 x R
+// rows: warp w owns words [w R, w R + R) of the tile's 8 R bit words, lane l
+// row 32 k + l of word k.
 template <int R>
-__global__ void __launch_bounds__(JT_THREADS, (R > 16 ? 2 : 4)) k_jp_match(Table<unsigned> t, const int* __restrict__ y,
-                                                                          long long n, unsigned* __restrict__ bits,
-                                                                          unsigned* __restrict__ counts) {
-    extern __shared__ unsigned jp_smem[];
-    unsigned(*off)[JT_THREADS] = reinterpret_cast<unsigned(*)[JT_THREADS]>(jp_smem);                   // key - kmin
-    unsigned(*buf)[JT_THREADS] = reinterpret_cast<unsigned(*)[JT_THREADS]>(jp_smem + R * JT_THREADS);  // filter word
+__global__ void __launch_bounds__(JT_THREADS) k_jp_match(Table<unsigned> t, const int* __restrict__ y, long long n,
+                                                         unsigned* __restrict__ bits, unsigned* __restrict__ counts) {
     __shared__ unsigned wc[JT_THREADS / 32];
-    constexpr unsigned NONE = 0xffffffffu;
-    const unsigned lane = lane_id(), warp = threadIdx.x >> 5, me = threadIdx.x;
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
     const long long base = (long long)blockIdx.x * (JT_THREADS * R) + (long long)warp * (32 * R);
-#pragma unroll
-    for (int k = 0; k < R; k++) {
-        long long i = base + k * 32 + lane;
-        if (i < n) cp_async4(&off[k][me], y + i);
-    }
-    cp_async_wait_all();
     const unsigned long long range = (unsigned long long)(t.kmax - t.kmin);  // < 2^31 in direct mode
+    // keys (coalesced across the warp), then all R filter words, every load
+    // issued before the first is used
+    unsigned off[R];
 #pragma unroll
     for (int k = 0; k < R; k++) {
         long long i = base + k * 32 + lane;
-        long long v = i < n ? (long long)(int)off[k][me] - t.kmin : -1;
-        unsigned o = (unsigned long long)v <= range ? (unsigned)v : NONE;
-        off[k][me] = o;
-        if (o != NONE) cp_async4(&buf[k][me], t.filter + (o >> 5));
+        long long v = i < n ? (long long)__ldcs(y + i) - t.kmin : -1;
+        off[k] = (unsigned long long)v <= range ? (unsigned)v : 0xffffffffu;
     }
-    cp_async_wait_all();
+    unsigned word[R];
+#pragma unroll
+    for (int k = 0; k < R; k++) word[k] = off[k] != 0xffffffffu ? __ldg(t.filter + (off[k] >> 5)) : 0u;
     unsigned cnt = 0;
     unsigned* wout = bits + (long long)blockIdx.x * (8 * R) + (long long)warp * R;
 #pragma unroll
     for (int k = 0; k < R; k++) {
-        unsigned o = off[k][me];
-        bool h = o != NONE && ((buf[k][me] >> (o & 31)) & 1u);
+        bool h = off[k] != 0xffffffffu && ((word[k] >> (off[k] & 31)) & 1u);
         unsigned bal = __ballot_sync(0xffffffffu, h);
         if (lane == 0) wout[k] = bal;
         cnt += __popc(bal);
@@ -733,13 +722,7 @@ static I probe_direct(const Table<unsigned>& t, const int* y, long long ny, long
     unsigned* counts = (unsigned*)salloc((size_t)ntiles * 4);
     unsigned long long* offs = (unsigned long long*)salloc((size_t)(ntiles + 1) * 8);
     if (!bits || !counts || !offs) return E_DEVICE_OOM;
-    const size_t sm = (size_t)2 * R * JT_THREADS * 4;
-    static bool attr = false;
-    if (!attr) {
-        HG_CU(cudaFuncSetAttribute(k_jp_match<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        attr = true;
-    }
-    HG_LAUNCH("join_probe", (unsigned)ntiles, JT_THREADS, sm, k_jp_match<R>, t, y, ny, bits, counts);
+    HG_LAUNCH("join_probe", (unsigned)ntiles, JT_THREADS, 0, k_jp_match<R>, t, y, ny, bits, counts);
     HG_CHECK(scan_counts(counts, ntiles, offs));
     HG_LAUNCH("join_emit", (unsigned)ntiles, JT_THREADS, 0, k_jp_emit<R>, t, y, ny, (const unsigned*)bits,
               (const unsigned long long*)offs, zb, zp);

@@ -256,3 +256,35 @@ def test_compare_f64_scalar_edges(libs, s):
         assert same(a, b), (fn, "vs")
         a, b = both(libs, fn, lambda L: (L.scalar(s, H_E), L.vec(v, H_E)))
         assert same(a, b), (fn, "sv")
+
+
+def test_unaligned_device_views(libs):
+    """Device vectors that start at an odd element offset (views into another
+    vector) take the unvectorised paths and give the same results."""
+    from horsepower_gb300.abi import V0
+    gpu, ora = libs
+    rng = np.random.default_rng(44)
+    n = 1_000_003
+    m = rng.random(n + 1) < 0.3
+    v = rng.standard_normal(n + 1)
+    idx = np.sort(rng.integers(0, n, n // 3 + 1)).astype(np.int64)
+
+    def dev_view(L, arr, typ, skip):
+        h = L.vec(arr, typ)
+        d = V0()
+        assert L.lib.hgpuToDevice(C.byref(d), C.byref(h)) == 0
+        L._keep.append(d)
+        w = V0()
+        w.typ, w.len, w.g = typ, arr.size - skip, d.g + skip * arr.itemsize
+        L._keep.append(w)
+        return w
+
+    got = gpu.to_py(gpu.call("pfnCompress", dev_view(gpu, m, H_B, 1), dev_view(gpu, v, H_E, 1)))
+    assert np.array_equal(got, v[1:][m[1:]])
+    got = gpu.to_py(gpu.call("pfnIndex", dev_view(gpu, v, H_E, 1), dev_view(gpu, idx, H_L, 1)))
+    assert np.array_equal(got, v[1:][idx[1:]])
+    got = gpu.to_py(gpu.call("pfnGeq", dev_view(gpu, v, H_E, 1), gpu.scalar(0.25, H_E)))
+    want = ora.to_py(ora.call("pfnGeq", ora.vec(v[1:], H_E), ora.scalar(0.25, H_E)))
+    assert np.array_equal(got, want)
+    gpu.free_inputs()
+    ora.free_inputs()
