@@ -132,7 +132,7 @@ def algorithmic_bytes(F, Dn, Dp, M, G):
         "onesweep": 2 * 2 * M,                                # group key bytes (2 x 1 byte) in
         "widen": 8 * M,
         "seg_chunk": 3 * (8 + 8) * M,                         # rows + values of three aggregates
-        "seg_small": 3 * (8 + 8) * M,
+        "seg_warps": 3 * (8 + 8) * M,
     }
 
 

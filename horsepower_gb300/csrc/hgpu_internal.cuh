@@ -144,6 +144,9 @@ struct ListInfo {
     const long long* big;
     const unsigned long long* chunk0;
     const long long* pstarts;
+    // cached segment ids by size class and the class counts (output arena)
+    const unsigned* cls_ids;
+    const unsigned* cls_cnt;
 };
 void register_list(const ListInfo& g);
 ListInfo* find_list(const V0* nodes, long long ng);

@@ -58,33 +58,120 @@ __device__ __forceinline__ T seg_elem(const T* __restrict__ src, const long long
     }
 }
 
-// one warp per segment of at most 4096 elements (longer segments are skipped)
+// Segments by size class, so that each is reduced by the narrowest unit that
+// reproduces the tile tree exactly: sizes 0-1, 2, 3-4, 5-8, 9-16, 17-32
+// (classes 0-5), 33-4096 (6) and longer (7).
+constexpr int SEG_CLASSES = 8;
+__device__ __forceinline__ int seg_class(long long m) {
+    if (m <= 1) return 0;
+    if (m > TILE_SUM) return 7;
+    if (m > 32) return 6;
+    return 32 - __clz((int)(m - 1));  // ceil(log2 m): 2 -> 1, 3-4 -> 2, ..., 17-32 -> 5
+}
+// pass 1: segments per class (cnt[c])
+__global__ void k_seg_class_count(const long long* __restrict__ starts, long long ng, long long total,
+                                  unsigned* __restrict__ cnt) {
+    __shared__ unsigned sc[SEG_CLASSES];
+    if (threadIdx.x < SEG_CLASSES) sc[threadIdx.x] = 0;
+    __syncthreads();
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g < ng) atomicAdd(&sc[seg_class(((g + 1 < ng) ? starts[g + 1] : total) - starts[g])], 1u);
+    __syncthreads();
+    if (threadIdx.x < SEG_CLASSES && sc[threadIdx.x]) atomicAdd(&cnt[threadIdx.x], sc[threadIdx.x]);
+}
+// pass 2: the segment ids of class c at ids[off_c ...] (off_c = segments of
+// lower classes; order inside a class is immaterial); cur[c] counts the
+// places taken
+__global__ void k_seg_class_ids(const long long* __restrict__ starts, long long ng, long long total,
+                                const unsigned* __restrict__ cnt, unsigned* __restrict__ cur,
+                                unsigned* __restrict__ ids) {
+    __shared__ unsigned sc[SEG_CLASSES], sbase[SEG_CLASSES];
+    if (threadIdx.x < SEG_CLASSES) sc[threadIdx.x] = 0;
+    __syncthreads();
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    int c = 0;
+    unsigned local = 0;
+    if (g < ng) {
+        c = seg_class(((g + 1 < ng) ? starts[g + 1] : total) - starts[g]);
+        local = atomicAdd(&sc[c], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < SEG_CLASSES) {
+        unsigned off = 0;
+        for (int k = 0; k < (int)threadIdx.x; k++) off += cnt[k];
+        sbase[threadIdx.x] = sc[threadIdx.x] ? off + atomicAdd(&cur[threadIdx.x], sc[threadIdx.x]) : 0;
+    }
+    __syncthreads();
+    if (g < ng) ids[sbase[c] + local] = (unsigned)g;
+}
+
+// Segments of classes 0-6 in one launch, one warp-sized unit of work per
+// warp.  Class c <= 5 (at most P = 2^c elements): the segment's elements sit
+// in lanes 0..m-1 of warp 0 of the 256-lane tile and every other lane and
+// warp holds the identity, so the tile tree reduces to the xor butterfly
+// over the first P lanes; a warp reduces 32 / P such segments in sub-warps
+// of P lanes.  Class 6 (33 to 4096 elements): one warp walks the tile's 8
+// virtual warps.
 template <typename T, typename A, int OP, bool GATHER>
-__global__ void k_seg_small(const T* __restrict__ src, const long long* __restrict__ rows, long long nx,
-                            const long long* __restrict__ starts, long long ng, long long total, A ident,
-                            A* __restrict__ out, unsigned* derr) {
+__global__ void __launch_bounds__(256) k_seg_warps(const T* __restrict__ src, const long long* __restrict__ rows,
+                                                   long long nx, const long long* __restrict__ starts, long long ng,
+                                                   long long total, const unsigned* __restrict__ ids,
+                                                   const unsigned* __restrict__ cnt, A ident, A* __restrict__ out,
+                                                   unsigned* derr) {
+    __shared__ long long wfirst[8];  // first warp of each class; wfirst[7] = warps in all
+    __shared__ unsigned cfirst[7];   // first id of each class
+    if (threadIdx.x == 0) {
+        long long w = 0;
+        unsigned o = 0;
+        for (int c = 0; c < 7; c++) {
+            wfirst[c] = w;
+            cfirst[c] = o;
+            const long long per = c < 6 ? (32 >> c) : 1;  // segments per warp
+            w += ((long long)cnt[c] + per - 1) / per;
+            o += cnt[c];
+        }
+        wfirst[7] = w;
+    }
+    __syncthreads();
+    const unsigned lane = lane_id();
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
     bool bad = false;
-    for (long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ng; g += warps) {
-        const long long s = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total, m = e - s;
-        if (m > TILE_SUM) continue;
-        const unsigned lane = lane_id();
-        A ws[8];
-#pragma unroll
-        for (int v = 0; v < 8; v++) ws[v] = ident;
-        for (int v = 0; v < 8 && v * 32 < m; v++) {  // virtual warp v of the 256-lane tile
+    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < wfirst[7]; w += warps) {
+        int c = 0;
+        while (c < 6 && w >= wfirst[c + 1]) c++;
+        if (c < 6) {
+            const int P = 1 << c;
+            const unsigned q = lane >> c, j = lane & (P - 1);
+            const long long k = (w - wfirst[c]) * (32 >> c) + q;
             A acc = ident;
-            for (int k = 0; k < 16; k++) {
-                long long j = (long long)k * 256 + v * 32 + lane;
-                if (j >= m) break;
-                acc = sop<A, OP>(acc, (A)seg_elem<T, GATHER>(src, rows, nx, s + j, bad));
+            long long g = -1;
+            if (k < (long long)cnt[c]) {
+                g = ids[cfirst[c] + k];
+                const long long s = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total;
+                if ((long long)j < e - s) acc = sop<A, OP>(ident, (A)seg_elem<T, GATHER>(src, rows, nx, s + j, bad));
             }
-            ws[v] = swarp<A, OP>(acc);
-        }
-        if (lane == 0) {
-            A w01 = sop<A, OP>(ws[0], ws[1]), w23 = sop<A, OP>(ws[2], ws[3]);
-            A w45 = sop<A, OP>(ws[4], ws[5]), w67 = sop<A, OP>(ws[6], ws[7]);
-            out[g] = sop<A, OP>(sop<A, OP>(w01, w23), sop<A, OP>(w45, w67));
+            for (int o = P >> 1; o > 0; o >>= 1) acc = sop<A, OP>(acc, __shfl_xor_sync(0xffffffffu, acc, o));
+            if (j == 0 && g >= 0) out[g] = acc;
+        } else {
+            const long long g = ids[cfirst[6] + (w - wfirst[6])];
+            const long long s = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total, m = e - s;
+            A ws[8];
+#pragma unroll
+            for (int v = 0; v < 8; v++) ws[v] = ident;
+            for (int v = 0; v < 8 && v * 32 < m; v++) {  // virtual warp v of the 256-lane tile
+                A acc = ident;
+                for (int k = 0; k < 16; k++) {
+                    long long j = (long long)k * 256 + v * 32 + lane;
+                    if (j >= m) break;
+                    acc = sop<A, OP>(acc, (A)seg_elem<T, GATHER>(src, rows, nx, s + j, bad));
+                }
+                ws[v] = swarp<A, OP>(acc);
+            }
+            if (lane == 0) {
+                A w01 = sop<A, OP>(ws[0], ws[1]), w23 = sop<A, OP>(ws[2], ws[3]);
+                A w45 = sop<A, OP>(ws[4], ws[5]), w67 = sop<A, OP>(ws[6], ws[7]);
+                out[g] = sop<A, OP>(sop<A, OP>(w01, w23), sop<A, OP>(w45, w67));
+            }
         }
     }
     if (bad) flag_error(derr, DERR_INDEX);
@@ -163,8 +250,26 @@ template <typename T, typename A, int OP, bool GATHER>
 static I seg_reduce(const T* src, const long long* rows, long long nx, const long long* starts, long long ng,
                     long long total, A ident, A* out, ListInfo* li = nullptr) {
     if (ng == 0) return 0;
-    HG_LAUNCH("seg_small", gcap(ng * 32), 256, 0, (k_seg_small<T, A, OP, GATHER>), src, rows, nx, starts, ng, total,
-              ident, out, g_derr);
+    // segment ids by size class (kept with the list when there is one)
+    const unsigned *ids, *ccnt;
+    if (li && li->cls_ids) {
+        ids = li->cls_ids;
+        ccnt = li->cls_cnt;
+    } else {
+        unsigned* cc = (unsigned*)(li ? dalloc(2 * SEG_CLASSES * 4) : salloc(2 * SEG_CLASSES * 4));
+        unsigned* id = (unsigned*)(li ? dalloc((size_t)ng * 4) : salloc((size_t)ng * 4));
+        if (!cc || !id) return E_DEVICE_OOM;
+        HG_CU(cudaMemsetAsync(cc, 0, 2 * SEG_CLASSES * 4, g_stream));
+        const unsigned gb = (unsigned)((ng + 255) / 256);
+        HG_LAUNCH("seg_class", gb, 256, 0, k_seg_class_count, starts, ng, total, cc);
+        HG_LAUNCH("seg_class_ids", gb, 256, 0, k_seg_class_ids, starts, ng, total, (const unsigned*)cc,
+                  cc + SEG_CLASSES, id);
+        ids = id;
+        ccnt = cc;
+        if (li) { li->cls_ids = id; li->cls_cnt = cc; }
+    }
+    HG_LAUNCH("seg_warps", gcap(ng * 4), 256, 0, (k_seg_warps<T, A, OP, GATHER>), src, rows, nx, starts, ng, total, ids,
+              ccnt, ident, out, g_derr);
     long long nbig = 0;
     unsigned long long nchunks = 0;
     const long long *big, *pstarts;

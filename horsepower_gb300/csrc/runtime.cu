@@ -448,6 +448,7 @@ L setHeapOffset(L cur) {
     for (ListInfo& li : g_lists) {
         if (!live(li.nodes) || !live(li.starts) || !live(li.data)) continue;
         if (li.planned && (!live(li.big) || !live(li.chunk0) || !live(li.pstarts))) li.planned = 0;
+        if (li.cls_ids && (!live(li.cls_ids) || !live(li.cls_cnt))) li.cls_ids = li.cls_cnt = nullptr;
         keep.push_back(li);
     }
     g_lists.swap(keep);
