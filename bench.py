@@ -609,7 +609,9 @@ def main():
                 "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"]},
         "roofline": {"bound": "hbm", "kernel": top[0], "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None, "peak_source": src,
-                     "traffic": traffic, "algorithmic_bytes_per_step": tb},
+                     "traffic": traffic, "algorithmic_bytes_per_step": tb,
+                     "traffic_gbs": (traffic / (top[1] / args.steps / 1000) / 1e9) if traffic else None,
+                     "traffic_frac": (traffic / (top[1] / args.steps / 1000) / 1e9 / hbm) if traffic else None},
         "cpu_baseline": cpu,
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],

@@ -91,7 +91,7 @@ __global__ void k_bucket_base(const unsigned long long* __restrict__ hist, unsig
 // stages the tile in shared memory in digit order and writes each digit's
 // run contiguously.
 template <typename K, bool FIRST>
-__global__ void __launch_bounds__(RS_THREADS, 3) k_onesweep(const K* __restrict__ kin, const unsigned* __restrict__ vin,
+__global__ void __launch_bounds__(RS_THREADS, (sizeof(K) == 4 ? 4 : 3)) k_onesweep(const K* __restrict__ kin, const unsigned* __restrict__ vin,
                                                          K* __restrict__ kout, unsigned* __restrict__ vout, long long n,
                                                          int shift, int bits, const unsigned long long* __restrict__ bucket,
                                                          unsigned long long* status, unsigned* ticket, unsigned* derr) {

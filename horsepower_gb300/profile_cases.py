@@ -4,6 +4,7 @@
     python -m horsepower_gb300.profile_cases compress  # @compress f64, 6M rows, 1.8% selected
     python -m horsepower_gb300.profile_cases group     # @group on two 1-byte columns, 8.67M rows
     python -m horsepower_gb300.profile_cases order     # @order (i64 key, i32 sec), N rows
+    python -m horsepower_gb300.profile_cases groupkey  # @group on i64 Zipf keys, 150M rows
     python -m horsepower_gb300.profile_cases gather    # @index f64 by ascending row ids
     python -m horsepower_gb300.profile_cases q6        # fused q6 chain, 6M rows
     python -m horsepower_gb300.profile_cases shared    # 16 batched join plans over one pair of tables
@@ -46,7 +47,7 @@ def timed(L, fn, reps):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["join", "compress", "group", "order", "gather", "q6", "shared"])
+    ap.add_argument("case", choices=["join", "compress", "group", "groupkey", "order", "gather", "q6", "shared"])
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--rows", type=int, default=0)
     ap.add_argument("--tune", action="append", default=[], help="knob=value (autotuner knobs)")
@@ -76,6 +77,10 @@ def main():
         s = dev(L, rng.integers(0, 2, n).astype(np.int8), H_C)
         lst = L.list([f, s])
         t = timed(L, lambda: L.call("pfnGroup", lst), a.reps)
+    elif a.case == "groupkey":
+        from . import serve as S
+        o = S.order_table(L, a.rows or 150_000_000, seed=2)
+        t = timed(L, lambda: L.call("pfnGroup", o["key"]), a.reps)
     elif a.case == "order":
         n = a.rows or 20_000_000
         key = dev(L, np.minimum(rng.zipf(1.1, n), 10_000_000).astype(np.int64), H_L)
