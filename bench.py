@@ -363,10 +363,18 @@ def run_served(args):
         reqs = S.request_stream(n, rate, seed=7 + rate)
         row = {"rate": rate, "requests": n}
         for name, mode in (("served", S.BATCHED), ("plain", S.PLAIN)):
-            _, st, _ = srv.run(reqs, mode)
+            _, st, meta = srv.run(reqs, mode)
             row[name] = {"qps": round(st.qps, 1), "p50_ms": round(st.p50_ms, 3), "p99_ms": round(st.p99_ms, 3),
                          "mean_ms": round(st.mean_ms, 3), "steps": st.steps, "max_step_requests": st.max_step_requests,
                          "max_step_gb": round(st.max_step_bytes / 2 ** 30, 3), "rejected": st.rejected}
+            # the longest steps: their duration and request mix
+            steps = {}
+            for r, m in zip(reqs, meta):
+                e = steps.setdefault(m["step"], [m["admit_s"], m["done_s"], [0, 0, 0]])
+                e[2][r.kind] += 1
+            longest = sorted(steps.values(), key=lambda e: e[0] - e[1])[:3]
+            row[name]["longest_steps"] = [{"ms": round(1e3 * (e[1] - e[0]), 2), "filter_agg/join/topk": e[2]}
+                                          for e in longest]
         table.append(row)
     launches = Lb.hgpuLaunchCount() - l0
     clk = clocks.stop()

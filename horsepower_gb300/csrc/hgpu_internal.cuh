@@ -65,6 +65,7 @@ int get_radix_digit_bits();
 long long out_mark();                          // output-arena cursor (for undoing a failed call)
 void out_rewind(long long m);
 void* salloc(size_t bytes);                    // scratch arena
+I scratch_reserve(size_t bytes);               // pre-allocates a scratch chunk of that size
 void* halloc(size_t bytes);                    // pinned host arena
 struct ScratchScope {                          // rewinds the scratch arena on exit
     long long mark;

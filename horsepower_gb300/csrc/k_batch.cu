@@ -322,6 +322,200 @@ __global__ void k_sh_probe(const int* __restrict__ fk, long long nf, long long k
             if (sh_hist[i]) atomicAdd(&facthist[i], sh_hist[i]);
 }
 
+// ---------------------------------------------------------------- shared tables, grouped
+// When every row's (flag, status) code falls in at most SG_MAXG distinct
+// values, the plans over one table set skip the per-plan gather and sort:
+// one pass counts, per tile, the rows of each (plan, group), a scan turns the
+// counts into positions, and a second pass reads each fact tile once and
+// writes every plan's matching values straight into that plan's group-ordered
+// arrays (rows of a group in fact-row order, as the builtins' @group lists
+// them), which the fixed-order segmented sums then reduce in place.
+constexpr int SG_MAXG = 8, SG_MAXP = 32, SG_R = 8;
+constexpr long long SG_TILE = 256LL * SG_R;
+
+// presence bits of the codes (flag << 8 | status) over the fact table
+__global__ void k_sg_codes(const int8_t* __restrict__ flag, const int8_t* __restrict__ status, long long n,
+                           unsigned* __restrict__ bits) {
+    __shared__ unsigned sb[2048];
+    for (int i = threadIdx.x; i < 2048; i += blockDim.x) sb[i] = 0;
+    __syncthreads();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        unsigned c = ((unsigned)(uint8_t)flag[i] << 8) | (unsigned)(uint8_t)status[i];
+        unsigned bit = 1u << (c & 31);
+        if (!(sb[c >> 5] & bit)) atomicOr(&sb[c >> 5], bit);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 2048; i += blockDim.x)
+        if (sb[i]) atomicOr(&bits[i], sb[i]);
+}
+
+// The tile preamble shared by both passes: each lane's SG_R date offsets,
+// and in lane c (c < G) the ballot of "row has group c" for each round k
+// (mygb[k]), so that a (plan, group c) count is a popc in lane c.
+__device__ __forceinline__ void sg_tile(const unsigned short* __restrict__ dd, const int8_t* __restrict__ flag,
+                                        const int8_t* __restrict__ status, const unsigned char* __restrict__ dense,
+                                        long long nf, long long base, int G, unsigned short (&d)[SG_R],
+                                        unsigned (&mygb)[SG_R], unsigned char (&g)[SG_R]) {
+    const unsigned lane = lane_id();
+#pragma unroll
+    for (int k = 0; k < SG_R; k++) {
+        long long i = base + k * 32 + lane;
+        d[k] = 0xffffu;
+        g[k] = 0xff;
+        if (i < nf) {
+            d[k] = __ldcs(dd + i);
+            g[k] = __ldg(dense + (((unsigned)(uint8_t)flag[i] << 8) | (unsigned)(uint8_t)status[i]));
+        }
+        mygb[k] = 0;
+    }
+#pragma unroll
+    for (int k = 0; k < SG_R; k++)
+        for (int c = 0; c < G; c++) {
+            const unsigned b = __ballot_sync(0xffffffffu, g[k] == c);
+            if ((int)lane == c) mygb[k] = b;
+        }
+}
+
+// this warp's rows of every (plan, group): wc[w][pl * G + c]
+__device__ __forceinline__ void sg_warp_counts(const unsigned short (&d)[SG_R], const unsigned (&mygb)[SG_R],
+                                               const int* __restrict__ wins, int npl, int G, unsigned* wcw) {
+    const unsigned lane = lane_id();
+    for (int pl = 0; pl < npl; pl++) {
+        const int lo = wins[2 * pl], hi = wins[2 * pl + 1];
+        unsigned n = 0;
+#pragma unroll
+        for (int k = 0; k < SG_R; k++) n += __popc(__ballot_sync(0xffffffffu, (int)d[k] >= lo && (int)d[k] < hi) & mygb[k]);
+        if ((int)lane < G) wcw[pl * G + lane] = n;
+    }
+}
+
+// pass 1: counts[(pl * G + g) * ntiles + t] = rows of plan pl and group g in tile t
+__global__ void __launch_bounds__(256) k_sg_count(const unsigned short* __restrict__ dd, const int8_t* __restrict__ flag,
+                                                  const int8_t* __restrict__ status,
+                                                  const unsigned char* __restrict__ dense, long long nf,
+                                                  const int* __restrict__ wins, int npl, int G,
+                                                  unsigned* __restrict__ counts, long long ntiles) {
+    __shared__ unsigned wc[8][SG_MAXP * SG_MAXG];
+    const unsigned w = threadIdx.x >> 5;
+    const long long t = blockIdx.x, base = t * SG_TILE + (long long)w * (32 * SG_R);
+    unsigned short d[SG_R];
+    unsigned mygb[SG_R];
+    unsigned char g[SG_R];
+    sg_tile(dd, flag, status, dense, nf, base, G, d, mygb, g);
+    sg_warp_counts(d, mygb, wins, npl, G, wc[w]);
+    __syncthreads();
+    for (int j = threadIdx.x; j < npl * G; j += blockDim.x) {
+        unsigned n = 0;
+        for (int v = 0; v < 8; v++) n += wc[v][j];
+        counts[(long long)j * ntiles + t] = n;
+    }
+}
+
+// one block per (plan, group): exclusive scan of its tile counts into offs,
+// total into totals[j]
+__global__ void __launch_bounds__(1024) k_sg_scan(const unsigned* __restrict__ counts, long long ntiles,
+                                                  unsigned long long* __restrict__ offs,
+                                                  unsigned long long* __restrict__ totals) {
+    __shared__ unsigned long long wsum[32];
+    __shared__ unsigned long long carry;
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    const long long j = blockIdx.x;
+    const unsigned* in = counts + j * ntiles;
+    unsigned long long* out = offs + j * ntiles;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (long long c0 = 0; c0 < ntiles; c0 += 1024 * 8) {
+        const long long b = c0 + (long long)threadIdx.x * 8;
+        unsigned v[8];
+        unsigned long long sum = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            v[k] = b + k < ntiles ? in[b + k] : 0u;
+            sum += v[k];
+        }
+        unsigned long long incl = warp_incl_scan64(sum);
+        if (lane == 31) wsum[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long x = wsum[lane];
+            wsum[lane] = warp_incl_scan64(x) - x;
+        }
+        __syncthreads();
+        unsigned long long off = carry + wsum[warp] + (incl - sum);
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            if (b + k < ntiles) out[b + k] = off;
+            off += v[k];
+        }
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = off;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) totals[j] = carry;
+}
+
+// pass 2: every plan's matching rows of the tile, values written to
+// base[j] + offs[j * ntiles + t] + (rows of the same (plan, group) earlier in
+// the tile).  Lane c keeps the next position of group c; a matching row takes
+// its group's position (shuffled from lane g) plus the matching rows of its
+// group in lower lanes of the round.
+__global__ void __launch_bounds__(256) k_sg_scatter(const unsigned short* __restrict__ dd, const int8_t* __restrict__ flag,
+                                                    const int8_t* __restrict__ status,
+                                                    const unsigned char* __restrict__ dense, const double* __restrict__ qty,
+                                                    const double* __restrict__ price, const double* __restrict__ disc,
+                                                    long long nf, const int* __restrict__ wins, int npl, int G,
+                                                    const unsigned long long* __restrict__ offs,
+                                                    const unsigned long long* __restrict__ base, long long ntiles,
+                                                    double* __restrict__ vq, double* __restrict__ vp,
+                                                    double* __restrict__ vd) {
+    __shared__ unsigned wc[8][SG_MAXP * SG_MAXG];
+    const unsigned lane = lane_id(), w = threadIdx.x >> 5;
+    const long long t = blockIdx.x, rbase = t * SG_TILE + (long long)w * (32 * SG_R);
+    unsigned short d[SG_R];
+    unsigned mygb[SG_R];
+    unsigned char g[SG_R];
+    sg_tile(dd, flag, status, dense, nf, rbase, G, d, mygb, g);
+    double q[SG_R], pr[SG_R], ds[SG_R];
+#pragma unroll
+    for (int k = 0; k < SG_R; k++) {
+        long long i = rbase + k * 32 + lane;
+        const bool ok = i < nf;
+        q[k] = ok ? __ldcs(qty + i) : 0.0;
+        pr[k] = ok ? __ldcs(price + i) : 0.0;
+        ds[k] = ok ? __ldcs(disc + i) : 0.0;
+    }
+    sg_warp_counts(d, mygb, wins, npl, G, wc[w]);
+    __syncthreads();
+    for (int j = threadIdx.x; j < npl * G; j += blockDim.x) {
+        unsigned acc = 0;
+        for (int v = 0; v < 8; v++) { unsigned n = wc[v][j]; wc[v][j] = acc; acc += n; }
+    }
+    __syncthreads();
+    for (int pl = 0; pl < npl; pl++) {
+        const int lo = wins[2 * pl], hi = wins[2 * pl + 1];
+        unsigned long long pos = 0;  // lane c < G: next position of group c
+        if ((int)lane < G) {
+            const int j = pl * G + (int)lane;
+            pos = base[j] + offs[(long long)j * ntiles + t] + wc[w][j];
+        }
+#pragma unroll
+        for (int k = 0; k < SG_R; k++) {
+            const bool m = (int)d[k] >= lo && (int)d[k] < hi;
+            const unsigned mb = __ballot_sync(0xffffffffu, m);
+            const int src = g[k] & 7;  // a non-matching lane's group is immaterial
+            const unsigned same = __shfl_sync(0xffffffffu, mygb[k], src);
+            const unsigned long long at = __shfl_sync(0xffffffffu, pos, src);
+            if (m) {
+                const unsigned long long o = at + __popc(mb & same & lanemask_lt());
+                vq[o] = q[k];
+                vp[o] = pr[k];
+                vd[o] = ds[k];
+            }
+            pos += __popc(mb & mygb[k]);
+        }
+    }
+}
+
 struct CPlan {
     const unsigned short* dd;
     long long nf;
@@ -653,6 +847,112 @@ done:
     return rc;
 }
 
+I seg_sum_f64_direct(const double* src, const long long* starts, long long ng, long long total, double* out);
+
+// The grouped path for the plans `ps` over one table set (date offsets dd
+// already computed).  Returns 1 when it ran (results in out[p], done[p] set),
+// 0 when the table set has more than SG_MAXG codes.
+static I shared_grouped(const hgpuJoinGroupPlan* plans, const std::vector<int>& ps, const std::vector<int>& plo,
+                        const std::vector<int>& phi, const unsigned short* dd, hgpuJoinGroupResult* out,
+                        std::vector<char>* done, int* ran) {
+    *ran = 0;
+    const hgpuJoinGroupPlan& q0 = plans[ps[0]];
+    const long long nf = q0.nfact;
+    unsigned* bits = (unsigned*)salloc(2048 * 4);
+    unsigned char* dense = (unsigned char*)salloc(65536);
+    if (!bits || !dense) return E_DEVICE_OOM;
+    HG_CU(cudaMemsetAsync(bits, 0, 2048 * 4, g_stream));
+    unsigned gr = grid_for(nf, 256);
+    if (gr > (unsigned)g_sms * 4) gr = g_sms * 4;
+    HG_LAUNCH("sg_codes", gr, 256, 0, k_sg_codes, (const int8_t*)q0.flag, (const int8_t*)q0.status, nf, bits);
+    std::vector<unsigned> hb(2048);
+    HG_CU(cudaMemcpyAsync(hb.data(), bits, 2048 * 4, cudaMemcpyDeviceToHost, g_stream));
+    HG_CHECK(check_device_errors());
+    std::vector<unsigned char> hd(65536, 0xff);
+    std::vector<unsigned> code_of;
+    for (unsigned c = 0; c < 65536; c++)
+        if ((hb[c >> 5] >> (c & 31)) & 1u) {
+            if (code_of.size() >= (size_t)SG_MAXG) return 0;  // too many codes: the general path
+            hd[c] = (unsigned char)code_of.size();
+            code_of.push_back(c);
+        }
+    const int G = (int)code_of.size();
+    if (G == 0) return 0;
+    HG_CU(cudaMemcpyAsync(dense, hd.data(), 65536, cudaMemcpyHostToDevice, g_stream));
+    const long long ntiles = (nf + SG_TILE - 1) / SG_TILE;
+    for (size_t c0 = 0; c0 < ps.size(); c0 += SG_MAXP) {
+        ScratchScope inner;
+        const int npl = (int)std::min<size_t>(SG_MAXP, ps.size() - c0);
+        const int nj = npl * G;
+        std::vector<int> hw(2 * npl);
+        for (int k = 0; k < npl; k++) { hw[2 * k] = plo[c0 + k]; hw[2 * k + 1] = phi[c0 + k]; }
+        int* wins = (int*)salloc(8 * npl);
+        unsigned* counts = (unsigned*)salloc((size_t)nj * ntiles * 4);
+        unsigned long long* offs = (unsigned long long*)salloc((size_t)nj * ntiles * 8);
+        unsigned long long* totals = (unsigned long long*)salloc((size_t)nj * 8);
+        unsigned long long* base = (unsigned long long*)salloc((size_t)nj * 8);
+        if (!wins || !counts || !offs || !totals || !base) return E_DEVICE_OOM;
+        HG_CU(cudaMemcpyAsync(wins, hw.data(), 8 * npl, cudaMemcpyHostToDevice, g_stream));
+        HG_LAUNCH("sg_count", (unsigned)ntiles, 256, 0, k_sg_count, dd, (const int8_t*)q0.flag,
+                  (const int8_t*)q0.status, (const unsigned char*)dense, nf, (const int*)wins, npl, G, counts, ntiles);
+        HG_LAUNCH("sg_scan", (unsigned)nj, 1024, 0, k_sg_scan, (const unsigned*)counts, ntiles, offs, totals);
+        std::vector<unsigned long long> ht(nj), hbase(nj);
+        HG_CU(cudaMemcpyAsync(ht.data(), totals, (size_t)nj * 8, cudaMemcpyDeviceToHost, g_stream));
+        HG_CHECK(check_device_errors());
+        // each plan's groups in ascending code order, plans one after another
+        unsigned long long tot = 0;
+        std::vector<long long> seg_start;
+        std::vector<int> seg_j;
+        for (int j = 0; j < nj; j++) {
+            hbase[j] = tot;
+            if (ht[j]) { seg_start.push_back((long long)tot); seg_j.push_back(j); }
+            tot += ht[j];
+        }
+        const long long nseg = (long long)seg_start.size();
+        double* vq = (double*)salloc((size_t)(tot ? tot : 1) * 8);
+        double* vp = (double*)salloc((size_t)(tot ? tot : 1) * 8);
+        double* vd = (double*)salloc((size_t)(tot ? tot : 1) * 8);
+        long long* st = (long long*)salloc((size_t)(nseg ? nseg : 1) * 8);
+        double* res = (double*)salloc((size_t)(nseg ? nseg : 1) * 3 * 8);
+        if (!vq || !vp || !vd || !st || !res) return E_DEVICE_OOM;
+        HG_CU(cudaMemcpyAsync(base, hbase.data(), (size_t)nj * 8, cudaMemcpyHostToDevice, g_stream));
+        if (tot > 0) {
+            HG_LAUNCH("sg_scatter", (unsigned)ntiles, 256, 0, k_sg_scatter, dd, (const int8_t*)q0.flag,
+                      (const int8_t*)q0.status, (const unsigned char*)dense, q0.qty, q0.price, q0.disc, nf,
+                      (const int*)wins, npl, G, (const unsigned long long*)offs, (const unsigned long long*)base,
+                      ntiles, vq, vp, vd);
+            HG_CU(cudaMemcpyAsync(st, seg_start.data(), (size_t)nseg * 8, cudaMemcpyHostToDevice, g_stream));
+            HG_CHECK(seg_sum_f64_direct(vq, st, nseg, (long long)tot, res));
+            HG_CHECK(seg_sum_f64_direct(vp, st, nseg, (long long)tot, res + nseg));
+            HG_CHECK(seg_sum_f64_direct(vd, st, nseg, (long long)tot, res + 2 * nseg));
+            HG_LAUNCH("b_avg", (unsigned)((nseg + 255) / 256), 256, 0, k_b_avg, (const double*)(res + nseg),
+                      (const long long*)st, nseg, (long long)tot, res + nseg);
+        }
+        std::vector<double> hr((size_t)(nseg ? nseg : 1) * 3);
+        if (nseg > 0) HG_CU(cudaMemcpyAsync(hr.data(), res, (size_t)nseg * 3 * 8, cudaMemcpyDeviceToHost, g_stream));
+        HG_CHECK(check_device_errors());
+        for (int k = 0; k < npl; k++) {
+            hgpuJoinGroupResult& r = out[ps[c0 + k]];
+            r.status = 0;
+            r.ngroups = 0;
+        }
+        for (long long e = 0; e < nseg; e++) {
+            const int j = seg_j[e], k = j / G, c = j % G;
+            hgpuJoinGroupResult& r = out[ps[c0 + k]];
+            const long long g = r.ngroups++;
+            r.flag[g] = (C)(code_of[c] >> 8);
+            r.st[g] = (C)(code_of[c] & 255);
+            r.count[g] = (L)ht[j];
+            r.sum_qty[g] = hr[e];
+            r.avg_price[g] = hr[nseg + e];
+            r.sum_disc[g] = hr[2 * nseg + e];
+        }
+        for (int k = 0; k < npl; k++) (*done)[ps[c0 + k]] = 1;
+    }
+    *ran = 1;
+    return 0;
+}
+
 // Finds the plans that share all their tables with another plan of the
 // batch, runs one probe per distinct table set, and describes each such
 // plan's window selection (cplans).  Marks plans for the builtin path where
@@ -662,7 +962,7 @@ done:
 // dates span more than 65,534 days, are left to the per-plan path.
 static I shared_probe(const hgpuJoinGroupPlan* plans, int np, std::vector<char>* shared, std::vector<char>* plain,
                       std::vector<unsigned long long>* sel, std::vector<unsigned long long>* mexp,
-                      std::vector<CPlan>* cplans) {
+                      std::vector<CPlan>* cplans, hgpuJoinGroupResult* out, std::vector<char>* done) {
     std::map<std::vector<const void*>, std::vector<int>> sets;
     for (int p = 0; p < np; p++) {
         const hgpuJoinGroupPlan& q = plans[p];
@@ -729,6 +1029,7 @@ static I shared_probe(const hgpuJoinGroupPlan* plans, int np, std::vector<char>*
             cf[i + 1] = cf[i] + h[b.drange + i];
         }
         const bool dup = h[2 * (size_t)b.drange] != 0;
+        std::vector<int> ps, plo, phi;
         for (int p : groups[b.g]) {
             const hgpuJoinGroupPlan& q = plans[p];
             if (dup) { (*plain)[p] = 1; continue; }
@@ -739,8 +1040,17 @@ static I shared_probe(const hgpuJoinGroupPlan* plans, int np, std::vector<char>*
             (*sel)[p] = cd[hi] - cd[lo];
             if ((*sel)[p] > (unsigned long long)q.nfact) { (*plain)[p] = 1; continue; }
             (*mexp)[p] = cf[hi] - cf[lo];
-            (*shared)[p] = 1;
-            cplans->push_back(CPlan{b.dd, q.nfact, (int)lo, (int)hi, 0, p});
+            ps.push_back(p);
+            plo.push_back((int)lo);
+            phi.push_back((int)hi);
+        }
+        if (ps.empty()) continue;
+        int ran = 0;
+        HG_CHECK(shared_grouped(plans, ps, plo, phi, b.dd, out, done, &ran));
+        if (ran) continue;
+        for (size_t k = 0; k < ps.size(); k++) {
+            (*shared)[ps[k]] = 1;
+            cplans->push_back(CPlan{b.dd, plans[ps[k]].nfact, plo[k], phi[k], 0, ps[k]});
         }
     }
     return 0;
@@ -781,13 +1091,14 @@ extern "C" I hgpuBatchJoinGroup(const hgpuJoinGroupPlan* plans, L nplans, hgpuJo
     std::vector<long long> ctiles(1, 0);
     std::vector<char> shared(np, 0);
     std::vector<unsigned long long> sh_sel(np, 0), sh_m(np, 0);
-    HG_CHECK(shared_probe(plans, np, &shared, &plain, &sh_sel, &sh_m, &cplans));
+    std::vector<char> done(np, 0);  // results already written by the grouped shared path
+    HG_CHECK(shared_probe(plans, np, &shared, &plain, &sh_sel, &sh_m, &cplans, out, &done));
     for (int p = 0; p < np; p++) {
         const hgpuJoinGroupPlan& q = plans[p];
         DPlan& d = hp[p];
-        if (shared[p] || plain[p]) { d.nd = 0; d.nf = 0; }  // no per-plan build or probe
+        if (shared[p] || plain[p] || done[p]) { d.nd = 0; d.nf = 0; }  // no per-plan build or probe
         d.fact_off = fact_total;
-        fact_total += shared[p] ? (long long)sh_m[p] : (plain[p] ? 0 : q.nfact);
+        fact_total += shared[p] ? (long long)sh_m[p] : ((plain[p] || done[p]) ? 0 : q.nfact);
         dtiles[p + 1] = dtiles[p] + (d.nd + BT - 1) / BT;
         ftiles[p + 1] = ftiles[p] + (d.nf + ptile - 1) / ptile;
     }
@@ -819,7 +1130,7 @@ extern "C" I hgpuBatchJoinGroup(const hgpuJoinGroupPlan* plans, L nplans, hgpuJo
         long long lo = hmm[2 * p], hi = hmm[2 * p + 1];
         if (hp[p].nd == 0) { lo = 0; hi = -1; }
         unsigned long long range = hi >= lo ? (unsigned long long)(hi - lo) + 1 : 0;
-        if (!shared[p] && !plain[p] &&
+        if (!shared[p] && !plain[p] && !done[p] &&
             (range > 64ull * (unsigned long long)(hp[p].nd > 1024 ? hp[p].nd : 1024) || range >= (1ull << 31))) {
             plain[p] = 1;  // too wide for a presence bitmap: no row is built or matched here
             lo = 0; hi = -1; range = 0;
@@ -925,7 +1236,7 @@ extern "C" I hgpuBatchJoinGroup(const hgpuJoinGroupPlan* plans, L nplans, hgpuJo
     // build on the fact side and emit rows in key-row order: both plans run
     // through the builtins instead.
     for (int p = 0; p < np; p++) {
-        if (shared[p]) continue;  // checked by shared_probe
+        if (shared[p] || done[p]) continue;  // checked by shared_probe
         if (hdup[p] || hsel[p] > (unsigned long long)hp[p].nf) plain[p] = 1;
     }
     long long mtot = 0;
@@ -1003,7 +1314,7 @@ extern "C" I hgpuBatchJoinGroup(const hgpuJoinGroupPlan* plans, L nplans, hgpuJo
     HG_CHECK(check_device_errors());
     for (int p = 0; p < np; p++) {
         hgpuJoinGroupResult& r = out[p];
-        if (plain[p]) continue;
+        if (plain[p] || done[p]) continue;
         r.ngroups = hg[p];
         for (unsigned g = 0; g < hg[p]; g++) {
             long long k = segoff[p] + g;

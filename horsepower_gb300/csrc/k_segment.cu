@@ -313,6 +313,11 @@ I seg_sum_f64(const double* src, const long long* rows, long long nx, const long
     return seg_reduce<double, double, OP_SUM, true>(src, rows, nx, starts, ng, total, 0.0, out);
 }
 
+// f64 sums of contiguous segments (no row indirection), same order
+I seg_sum_f64_direct(const double* src, const long long* starts, long long ng, long long total, double* out) {
+    return seg_reduce<double, double, OP_SUM, false>(src, nullptr, 0, starts, ng, total, 0.0, out);
+}
+
 // ---------------------------------------------------------- finishing steps
 template <typename A>
 __global__ void k_avg_seg(const A* __restrict__ s, const long long* __restrict__ starts, long long ng, long long total,

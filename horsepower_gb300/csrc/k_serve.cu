@@ -595,8 +595,10 @@ I hgpuServerCreate(hgpuServer* out, const hgpuServeTables* tables, L hbm_budget_
     s->t = *tables;
     s->budget = hbm_budget_bytes > 0 ? hbm_budget_bytes : (L)32 << 30;
     s->max_step = max_step_requests;
-    I rc = 0;
-    if (s->t.ndim > 0 && s->t.dim_date) rc = build_cum(s->t.dim_date, 0, s->t.ndim, 1 << 20, &s->dim_dates);
+    // the budget is the scratch the admitted requests of a step may hold:
+    // reserve it now, so that no step waits on a device allocation
+    I rc = scratch_reserve((size_t)s->budget);
+    if (!rc && s->t.ndim > 0 && s->t.dim_date) rc = build_cum(s->t.dim_date, 0, s->t.ndim, 1 << 20, &s->dim_dates);
     if (!rc && s->t.norder > 0 && s->t.o_key) rc = build_cum(s->t.o_key, 1, s->t.norder, 1 << 26, &s->keys);
     if (rc) {
         delete s;

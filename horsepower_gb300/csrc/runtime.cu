@@ -116,6 +116,21 @@ struct Arena {
         last_bytes = need;
         return true;
     }
+    // makes sure a chunk of at least `bytes` exists after the current one, so
+    // that a later request of that size finds memory without a cudaMalloc
+    bool reserve(size_t bytes) {
+        for (size_t k = cur_chunk; k < chunks.size(); k++)
+            if (chunks[k].cap >= bytes) return true;
+        char* base = nullptr;
+        cudaError_t e = host ? cudaHostAlloc((void**)&base, bytes, cudaHostAllocPortable | cudaHostAllocMapped)
+                             : cudaMalloc((void**)&base, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        chunks.push_back({base, bytes, 0});
+        return true;
+    }
     bool contains(const void* p) const {
         for (auto& c : chunks)
             if ((const char*)p >= c.base && (const char*)p < c.base + c.cap) return true;
@@ -178,6 +193,9 @@ bool dshrink(void* p, size_t new_bytes) { return g_out->shrink(p, new_bytes); }
 long long out_mark() { return g_out->mark(); }
 void out_rewind(long long m) { g_out->rewind(m); }
 void* salloc(size_t bytes) { return g_scratch->alloc(bytes); }
+I scratch_reserve(size_t bytes) {
+    return g_scratch->reserve(bytes) ? 0 : set_error(E_DEVICE_OOM, "scratch arena: cannot reserve %zu bytes", bytes);
+}
 void* halloc(size_t bytes) { return g_host->alloc(bytes); }
 ScratchScope::ScratchScope() : mark(g_scratch ? g_scratch->mark() : 0) {}
 ScratchScope::~ScratchScope() {
