@@ -136,6 +136,11 @@ class Builtins:
         self._keep.append(v)
         return v
 
+    def syms(self, names):
+        """A symbol vector (H_Q) of several names, e.g. the ops of a multi-column join."""
+        ids = np.array([self.lib.getSymbol(n.encode()) for n in names], dtype=np.int64)
+        return self.vec(ids, H_Q)
+
     def list(self, items, typ=H_G):
         arr = (V0 * max(len(items), 1))()
         for i, it in enumerate(items):

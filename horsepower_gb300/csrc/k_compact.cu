@@ -167,6 +167,16 @@ static I compact(const uint8_t* mask, long long n, CompactCols& cols, long long*
     return 0;
 }
 
+// i64 columns compacted by one mask (the multi-column join's pair filter);
+// dst[c] must hold n rows, *count receives the rows kept
+I compact_i64_cols(const uint8_t* mask, long long n, const long long* const* src, long long** dst, int ncol,
+                   long long* count) {
+    CompactCols cols{};
+    cols.ncol = ncol;
+    for (int c = 0; c < ncol; c++) { cols.src[c] = src[c]; cols.dst[c] = dst[c]; cols.es[c] = 8; }
+    return compact(mask, n, cols, count);
+}
+
 static bool compress_type_ok(I t) {
     // types pfnCompress handles (h_primitive.cc:1497-1510)
     return t == H_B || t == H_J || t == H_H || t == H_I || t == H_L || t == H_F || t == H_E || t == H_Q ||

@@ -25,6 +25,8 @@
 // duplicate build rows use a count / scan / write path over a CSR of build
 // rows sorted per slot.
 #include <climits>
+#include <cstring>
+#include <vector>
 
 #include "dev_common.cuh"
 
@@ -1025,6 +1027,148 @@ I pfnMember(V z, V y, V x) {
     return E_DOMAIN;
 }
 
+}  // extern "C"
+
+namespace hg {
+
+I compact_i64_cols(const uint8_t* mask, long long n, const long long* const* src, long long** dst, int ncol,
+                   long long* count);
+
+// element i of a real column, converted to T as promoteValue converts it
+template <typename T>
+__device__ __forceinline__ T elem_as(const void* p, int typ, long long i) {
+    switch (typ) {
+    case H_B: return (T)((const bool*)p)[i];
+    case H_J: case H_C: return (T)((const int8_t*)p)[i];
+    case H_H: return (T)((const int16_t*)p)[i];
+    case H_I: case H_M: case H_D: case H_U: case H_W: case H_T: return (T)((const int32_t*)p)[i];
+    case H_F: return (T)((const float*)p)[i];
+    case H_E: return (T)((const double*)p)[i];
+    default: return (T)((const long long*)p)[i];
+    }
+}
+
+// keep[k] = COMP(op, x[a[k]], y[b[k]]) in type T: the exact compares of
+// compareOneColumn (h_system.cc:818-838, COMP h_primitive.cc:1063-1066)
+template <typename T>
+__global__ void k_pair_keep(const void* __restrict__ x, int xt, const void* __restrict__ y, int yt,
+                            const long long* __restrict__ a, const long long* __restrict__ b, long long m, int op,
+                            uint8_t* __restrict__ keep) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m; k += (long long)gridDim.x * blockDim.x) {
+        const T u = elem_as<T>(x, xt, a[k]), v = elem_as<T>(y, yt, b[k]);
+        bool r;
+        switch (op) {
+        case 0: r = u < v; break;
+        case 1: r = u <= v; break;
+        case 2: r = u > v; break;
+        case 3: r = u >= v; break;
+        case 4: r = u == v; break;
+        case 5: r = u != v; break;
+        default: r = false; break;
+        }
+        keep[k] = r;
+    }
+}
+
+static int op_of_symbol(L q) {
+    const char* n = getSymbolStr(q);
+    if (!n) return -1;
+    return !strcmp(n, "lt") ? 0 : !strcmp(n, "leq") ? 1 : !strcmp(n, "gt") ? 2 : !strcmp(n, "geq") ? 3
+         : !strcmp(n, "eq") ? 4 : !strcmp(n, "neq") ? 5 : -1;
+}
+
+// pfnJoinIndexMultiple (h_primitive.cc:2094-2110): join on the first @eq
+// column (else the first @neq, else column 0) without the shorter-side swap
+// (joinOneColumn, h_system.cc:856-880), then keep the pairs whose other
+// columns compare true, column by column in order (joinOtherColumns,
+// :846-853).  The first column's join must be an equi-join on i32/i64 keys
+// (the reference's hash path; its nested-loop and non-equi joins are
+// quadratic and are not reproduced).
+static I join_multi(V z, V x, V y, V f) {
+    if (x->typ != H_G || y->typ != H_G) return E_DOMAIN;
+    const long long nc = f->len;
+    if (x->len != nc || y->len != nc) return E_LENGTH;
+    std::vector<L> sym((size_t)nc);
+    if (is_device_ptr(f->g) && !is_inline(f))
+        HG_CU(cudaMemcpy(sym.data(), f->g, (size_t)nc * 8, cudaMemcpyDeviceToHost));
+    else
+        memcpy(sym.data(), f->g, (size_t)nc * 8);
+    std::vector<int> ops((size_t)nc);
+    long long fx = -1;
+    for (long long i = 0; i < nc && fx < 0; i++) if ((ops[i] = op_of_symbol(sym[i])) == 4) fx = i;
+    for (long long i = 0; i < nc; i++) ops[i] = op_of_symbol(sym[i]);
+    for (long long i = 0; i < nc && fx < 0; i++) if (ops[i] == 5) fx = i;
+    if (fx < 0) fx = 0;
+    for (long long i = 0; i < nc; i++) if (ops[i] < 0) return E_DOMAIN;
+    if (ops[fx] != 4) return set_error(E_NOT_IMPL, "multi-column join without an @eq column is outside the path");
+    V0* xc = host_nodes(x);
+    V0* yc = host_nodes(y);
+    const long long nx = xc[0].len, ny = yc[0].len;
+    for (long long i = 0; i < nc; i++) {
+        if (xc[i].len != nx || yc[i].len != ny) return E_LENGTH;
+        if (!is_real(xc[i].typ) || !is_real(yc[i].typ)) return E_TYPE;
+    }
+    const I typ = xc[fx].typ > yc[fx].typ ? xc[fx].typ : yc[fx].typ;
+    if (typ != H_I && typ != H_L) return set_error(E_NOT_IMPL, "hash join keys must be i32 or i64");
+    const void *px, *py;
+    HG_CHECK(promote_to(&xc[fx], typ, &px));
+    HG_CHECK(promote_to(&yc[fx], typ, &py));
+    const long long mark = out_mark();
+    V0 j;
+    if (typ == H_I) HG_CHECK(join_hash<unsigned>(&j, px, typ, nx, py, ny));
+    else HG_CHECK(join_hash<unsigned long long>(&j, px, typ, nx, py, ny));
+    V0* jn = host_nodes(&j);
+    long long m = jn[0].len;
+    // the pairs as device vectors (a length-1 result is inline in its node)
+    long long* cur[2];
+    for (int c = 0; c < 2; c++) {
+        cur[c] = (long long*)salloc((size_t)(m > 0 ? m : 1) * 8);
+        if (!cur[c]) return E_DEVICE_OOM;
+        if (m > 0) HG_CU(cudaMemcpyAsync(cur[c], jn[c].g, (size_t)m * 8, cudaMemcpyDefault, g_stream));
+    }
+    uint8_t* keep = (uint8_t*)salloc((size_t)(m > 0 ? m : 1));
+    long long* nxt[2] = {(long long*)salloc((size_t)(m > 0 ? m : 1) * 8), (long long*)salloc((size_t)(m > 0 ? m : 1) * 8)};
+    if (!keep || !nxt[0] || !nxt[1]) return E_DEVICE_OOM;
+    for (long long i = 0; i < nc && m > 0; i++) {
+        if (i == fx) continue;
+        const void *ax, *ay;
+        HG_CHECK(in_ptr(&xc[i], &ax));
+        HG_CHECK(in_ptr(&yc[i], &ay));
+        const I tm = xc[i].typ > yc[i].typ ? xc[i].typ : yc[i].typ;
+        const unsigned g = grid_cap(m);
+        switch (tm) {
+        case H_F: HG_LAUNCH("pair_keep", g, 256, 0, k_pair_keep<float>, ax, (int)xc[i].typ, ay, (int)yc[i].typ, cur[0], cur[1], m, ops[i], keep); break;
+        case H_E: HG_LAUNCH("pair_keep", g, 256, 0, k_pair_keep<double>, ax, (int)xc[i].typ, ay, (int)yc[i].typ, cur[0], cur[1], m, ops[i], keep); break;
+        case H_L: HG_LAUNCH("pair_keep", g, 256, 0, k_pair_keep<long long>, ax, (int)xc[i].typ, ay, (int)yc[i].typ, cur[0], cur[1], m, ops[i], keep); break;
+        case H_I: HG_LAUNCH("pair_keep", g, 256, 0, k_pair_keep<int>, ax, (int)xc[i].typ, ay, (int)yc[i].typ, cur[0], cur[1], m, ops[i], keep); break;
+        case H_H: HG_LAUNCH("pair_keep", g, 256, 0, k_pair_keep<short>, ax, (int)xc[i].typ, ay, (int)yc[i].typ, cur[0], cur[1], m, ops[i], keep); break;
+        case H_J: HG_LAUNCH("pair_keep", g, 256, 0, k_pair_keep<signed char>, ax, (int)xc[i].typ, ay, (int)yc[i].typ, cur[0], cur[1], m, ops[i], keep); break;
+        default: HG_LAUNCH("pair_keep", g, 256, 0, k_pair_keep<bool>, ax, (int)xc[i].typ, ay, (int)yc[i].typ, cur[0], cur[1], m, ops[i], keep); break;
+        }
+        long long kept = 0;
+        HG_CHECK(compact_i64_cols(keep, m, (const long long* const*)cur, nxt, 2, &kept));
+        std::swap(cur[0], nxt[0]);
+        std::swap(cur[1], nxt[1]);
+        m = kept;
+    }
+    out_rewind(mark);  // the single-column join's outputs
+    HG_CHECK(init_list(z, H_G, 2));
+    V0* e = host_nodes(z);
+    for (int c = 0; c < 2; c++) {
+        void* d;
+        HG_CHECK(alloc_out(&e[c], H_L, m, &d));
+        if (m > 0) HG_CU(cudaMemcpyAsync(d, cur[c], (size_t)m * 8, cudaMemcpyDeviceToDevice, g_stream));
+        HG_CHECK(finish_out(&e[c], d));
+    }
+    register_bound(e[0].g, e[0].len, nx);
+    register_bound(e[1].g, e[1].len, ny);
+    return 0;
+}
+
+}  // namespace hg
+
+extern "C" {
+
 I pfnJoinIndex(V z, V x, V y, V f) {
     HG_CHECK(ensure_init());
     ScratchScope ss;
@@ -1036,7 +1180,7 @@ I pfnJoinIndex(V z, V x, V y, V f) {
         }
         return join_single(z, x, y, f);
     }
-    if (f->len > 1) return set_error(E_NOT_IMPL, "multi-column join is outside the current path");
+    if (f->len > 1) return join_multi(z, x, y, f);
     return E_DOMAIN;
 }
 

@@ -191,7 +191,11 @@ I sync() {
 void* dalloc(size_t bytes) { return g_out->alloc(bytes); }
 bool dshrink(void* p, size_t new_bytes) { return g_out->shrink(p, new_bytes); }
 long long out_mark() { return g_out->mark(); }
-void out_rewind(long long m) { g_out->rewind(m); }
+static void prune_registries();
+void out_rewind(long long m) {
+    g_out->rewind(m);
+    prune_registries();
+}
 void* salloc(size_t bytes) { return g_scratch->alloc(bytes); }
 I scratch_reserve(size_t bytes) {
     return g_scratch->reserve(bytes) ? 0 : set_error(E_DEVICE_OOM, "scratch arena: cannot reserve %zu bytes", bytes);
@@ -409,6 +413,24 @@ I last_launch_error() {
     return 0;
 }
 
+// forget the lists and index ranges whose memory was released by a rewind;
+// a list that survives drops a segment plan allocated after the mark
+static void prune_registries() {
+    auto live = [](const void* p) { return !p || (g_out->live(p) && g_host->live(p)); };
+    std::vector<ListInfo> keep;
+    for (ListInfo& li : g_lists) {
+        if (!live(li.nodes) || !live(li.starts) || !live(li.data)) continue;
+        if (li.planned && (!live(li.big) || !live(li.chunk0) || !live(li.pstarts))) li.planned = 0;
+        if (li.cls_ids && (!live(li.cls_ids) || !live(li.cls_cnt))) li.cls_ids = li.cls_cnt = nullptr;
+        keep.push_back(li);
+    }
+    g_lists.swap(keep);
+    std::vector<Bound> kb;
+    for (const Bound& b : g_bounds)
+        if (live(b.data)) kb.push_back(b);
+    g_bounds.swap(kb);
+}
+
 }  // namespace hg
 
 using namespace hg;
@@ -459,21 +481,7 @@ L setHeapOffset(L cur) {
     cudaStreamSynchronize(g_stream);
     g_out->rewind(g_marks[(size_t)cur].first);
     g_host->rewind(g_marks[(size_t)cur].second);
-    // forget the lists and index ranges whose memory was released; a list
-    // that survives drops a segment plan allocated after the mark
-    auto live = [](const void* p) { return !p || (g_out->live(p) && g_host->live(p)); };
-    std::vector<ListInfo> keep;
-    for (ListInfo& li : g_lists) {
-        if (!live(li.nodes) || !live(li.starts) || !live(li.data)) continue;
-        if (li.planned && (!live(li.big) || !live(li.chunk0) || !live(li.pstarts))) li.planned = 0;
-        if (li.cls_ids && (!live(li.cls_ids) || !live(li.cls_cnt))) li.cls_ids = li.cls_cnt = nullptr;
-        keep.push_back(li);
-    }
-    g_lists.swap(keep);
-    std::vector<Bound> kb;
-    for (const Bound& b : g_bounds)
-        if (live(b.data)) kb.push_back(b);
-    g_bounds.swap(kb);
+    prune_registries();
     g_marks.resize((size_t)cur + 1);
     return cur;
 }

@@ -163,7 +163,7 @@ I pfnLen(V z, V x);             /* h_primitive.cc:656-662 */
 I pfnIndex  (V z, V x, V y);    /* h_primitive.cc:43-94 */
 I pfnIndexOf(V z, V x, V y);    /* h_primitive.cc:1523-1579 */
 I pfnMember (V z, V y, V x);    /* h_primitive.cc:2287-2336 (note argument order) */
-I pfnJoinIndex(V z, V x, V y, V f); /* h_primitive.cc:2122-2155 */
+I pfnJoinIndex(V z, V x, V y, V f); /* h_primitive.cc:2122-2155; several columns: pfnJoinIndexMultiple :2094-2110 */
 /* Grouping and ordering */
 I pfnGroup    (V z, V x);       /* h_primitive.cc:993-999 */
 I pfnGroupTrie(V z, V x);       /* h_primitive.cc:2656-2681 */

@@ -763,6 +763,94 @@ static I join_single(V z, V x, V y, V f) {
     }
 }
 
+static I op_of_sym(L q) {
+    S n = getSymbolStr(q);
+    if (!n) R -1;
+    R !strcmp(n, "lt") ? 0 : !strcmp(n, "leq") ? 1 : !strcmp(n, "gt") ? 2 : !strcmp(n, "geq") ? 3
+    : !strcmp(n, "eq") ? 4 : !strcmp(n, "neq") ? 5 : -1;
+}
+/* element i of a real column as a double / an i64 (promoteValue's C casts);
+ * COMP on the promoted type (h_primitive.cc:1063-1066) */
+static E elem_e(V x, L i) {
+    switch (vp(x)) {
+    case H_B: R (E)sB(x)[i]; case H_J: case H_C: R (E)((signed char *)vg(x))[i]; case H_H: R (E)sH(x)[i];
+    case H_I: R (E)sI(x)[i]; case H_F: R (E)sF(x)[i]; case H_E: R sE(x)[i]; default: R (E)sL(x)[i];
+    }
+}
+static L elem_l(V x, L i) {
+    switch (vp(x)) {
+    case H_B: R sB(x)[i]; case H_J: case H_C: R ((signed char *)vg(x))[i]; case H_H: R sH(x)[i];
+    case H_I: R sI(x)[i]; default: R sL(x)[i];
+    }
+}
+static B comp_pair(V x, V y, L a, L b, I op) {
+    I t = MAX(vp(x), vp(y));
+    if (t == H_F) {
+        F u = vp(x) == H_F ? sF(x)[a] : (F)elem_l(x, a), v = vp(y) == H_F ? sF(y)[b] : (F)elem_l(y, b);
+        R op == 0 ? u < v : op == 1 ? u <= v : op == 2 ? u > v : op == 3 ? u >= v : op == 4 ? u == v : u != v;
+    }
+    if (t == H_E) {
+        E u = elem_e(x, a), v = elem_e(y, b);
+        R op == 0 ? u < v : op == 1 ? u <= v : op == 2 ? u > v : op == 3 ? u >= v : op == 4 ? u == v : u != v;
+    }
+    L u = elem_l(x, a), v = elem_l(y, b);
+    switch (t) {  /* narrower integer types wrap as the promoted C type would */
+    case H_B: u = (B)u; v = (B)v; break;
+    case H_J: u = (signed char)u; v = (signed char)v; break;
+    case H_H: u = (short)u; v = (short)v; break;
+    case H_I: u = (int)u; v = (int)v; break;
+    default: break;
+    }
+    R op == 0 ? u < v : op == 1 ? u <= v : op == 2 ? u > v : op == 3 ? u >= v : op == 4 ? u == v : u != v;
+}
+/* pfnJoinIndexMultiple: h_primitive.cc:2094-2110 — join on the first @eq
+ * column (getFirstEqual :2088-2092; else @neq, else column 0) with no
+ * shorter-side swap and no linear path (joinOneColumn, h_system.cc:856-880),
+ * then keep the pairs whose other columns compare true, column by column
+ * (joinOtherColumns :846-853, compareOneColumn :818-838).  Equi-joins on
+ * i32/i64 keys only (the reference's hash path; i64 is an extension). */
+static I join_multi(V z, V x, V y, V f) {
+    if (vp(x) != H_G || vp(y) != H_G) R E_DOMAIN;
+    L nc = vn(f);
+    if (vn(x) != nc || vn(y) != nc) R E_LENGTH;
+    L fx = -1;
+    for (L i = 0; i < nc && fx < 0; i++) if (op_of_sym(sL(f)[i]) == 4) fx = i;
+    for (L i = 0; i < nc && fx < 0; i++) if (op_of_sym(sL(f)[i]) == 5) fx = i;
+    if (fx < 0) fx = 0;
+    for (L i = 0; i < nc; i++) if (op_of_sym(sL(f)[i]) < 0) R E_DOMAIN;
+    if (op_of_sym(sL(f)[fx]) != 4) R E_NOT_IMPL;
+    V x0 = vV(x, fx), y0 = vV(y, fx);
+    L nx = vn(x0), ny = vn(y0);
+    for (L i = 0; i < nc; i++) {
+        if (vn(vV(x, i)) != nx || vn(vV(y, i)) != ny) R E_LENGTH;
+        if (!hgo_is_real(vp(vV(x, i))) || !hgo_is_real(vp(vV(y, i)))) R E_TYPE;
+    }
+    I typMax = MAX(vp(x0), vp(y0));
+    if (typMax != H_I && typMax != H_L) R E_NOT_IMPL;
+    V0 tx, ty, j0, j1;
+    CHECKE(hgo_promote(&tx, x0, typMax));
+    CHECKE(hgo_promote(&ty, y0, typMax));
+    CHECKE(join_hash(&j0, &j1, &tx, &ty));
+    L m = vn(&j0);
+    L *a = malloc(sizeof(L) * (m > 0 ? m : 1)), *b = malloc(sizeof(L) * (m > 0 ? m : 1));
+    memcpy(a, sL(&j0), sizeof(L) * m);
+    memcpy(b, sL(&j1), sizeof(L) * m);
+    for (L i = 0; i < nc; i++) {
+        if (i == fx) continue;
+        I op = op_of_sym(sL(f)[i]);
+        L k = 0;
+        for (L q = 0; q < m; q++) if (comp_pair(vV(x, i), vV(y, i), a[q], b[q], op)) { a[k] = a[q]; b[k] = b[q]; k++; }
+        m = k;
+    }
+    initV(z, H_G, 2);
+    initV(vV(z, 0), H_L, m);
+    initV(vV(z, 1), H_L, m);
+    memcpy(sL(vV(z, 0)), a, sizeof(L) * m);
+    memcpy(sL(vV(z, 1)), b, sizeof(L) * m);
+    free(a); free(b);
+    R 0;
+}
+
 /* pfnJoinIndex: h_primitive.cc:2122-2155 — the shorter side is built; when x
  * is strictly longer the call is mirrored and the two outputs swapped. */
 I pfnJoinIndex(V z, V x, V y, V f) {
@@ -770,7 +858,7 @@ I pfnJoinIndex(V z, V x, V y, V f) {
         if (vn(x) > vn(y)) { CHECKE(join_single(z, y, x, f)); hgo_swap2(z); R 0; }
         R join_single(z, x, y, f);
     }
-    if (vn(f) > 1) R E_NOT_IMPL;  /* multi-column join: outside the current path */
+    if (vn(f) > 1) R join_multi(z, x, y, f);
     R E_DOMAIN;
 }
 

@@ -7,7 +7,7 @@ builtin library (compiled from its sources) and stores inputs and outputs in
 (CPU suite) and through libhgpu (GPU suite) and compare.
 
 Argument encoding (so a fixture can be rebuilt without this module):
-  ("vec", array, typ) | ("scalar", value, typ) | ("sym", name) | ("list", [args]) | ("bools", array)
+  ("vec", array, typ) | ("scalar", value, typ) | ("sym", name) | ("syms", [names]) | ("list", [args]) | ("bools", array)
 Case flags:
   tol        relative tolerance for float outputs (0 = bit-exact)
   canonical  compare a @group / @order result up to the order of tied rows
@@ -218,4 +218,20 @@ def build_cases():
                       tol=1e-12, canonical=False, error=0))
     cases.append(dict(name="group_sum_chain_i32", fn="@chain_group_agg", args=[V(gk, H_I), V(rng.integers(-1000, 1000, 5000).astype(np.int32), H_I)],
                       tol=0.0, canonical=False, error=0))
+    # ---- multi-column join_index (h_primitive.cc:2094-2110; joinOtherColumns h_system.cc:846-853)
+    nb, npr = 3000, 9000
+    bk = rng.integers(0, 2000, nb).astype(np.int32)                 # repeated keys: several pairs per probe row
+    pk2 = rng.integers(0, 2000, npr).astype(np.int32)
+    ba, pa = rng.integers(0, 50, nb).astype(np.int32), rng.integers(0, 50, npr).astype(np.int32)
+    bd, pd = np.round(rng.standard_normal(nb), 1), np.round(rng.standard_normal(npr), 1)
+    bl, pl = rng.integers(0, 30, nb).astype(np.int64), rng.integers(0, 30, npr).astype(np.int64)
+    for ops, tag in [(["eq", "lt"], "eq_lt"), (["geq", "eq"], "geq_eq"), (["eq", "neq"], "eq_neq"), (["eq", "leq"], "eq_leq"),
+                     (["eq", "gt"], "eq_gt"), (["eq", "eq"], "eq_eq")]:
+        add(f"join_multi_{tag}", "pfnJoinIndex", Ls(V(bk, H_I), V(ba, H_I)), Ls(V(pk2, H_I), V(pa, H_I)), ("syms", ops))
+    add("join_multi_f64", "pfnJoinIndex", Ls(V(bk, H_I), V(bd, H_E)), Ls(V(pk2, H_I), V(pd, H_E)), ("syms", ["eq", "lt"]))
+    add("join_multi_mixed", "pfnJoinIndex", Ls(V(bk, H_I), V(bl, H_L), V(bd, H_E)),
+        Ls(V(pk2, H_I), V(pa, H_I), V(pd.astype(np.float32), H_F)), ("syms", ["eq", "geq", "neq"]))
+    add("join_multi_small_build", "pfnJoinIndex", Ls(V([4, 7, 4], H_I), V([1, 2, 3], H_I)),
+        Ls(V(rng.integers(0, 9, 200).astype(np.int32), H_I), V(rng.integers(0, 4, 200).astype(np.int32), H_I)), ("syms", ["eq", "lt"]))
+    add("join_multi_len_mismatch", "pfnJoinIndex", Ls(V(bk, H_I), V(ba, H_I)), Ls(V(pk2, H_I)), ("syms", ["eq", "lt"]), error=5)
     return cases

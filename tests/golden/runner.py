@@ -14,6 +14,8 @@ def build_arg(lib, spec):
         return lib.scalar(spec[1], spec[2])
     if kind == "sym":
         return lib.sym(spec[1])
+    if kind == "syms":
+        return lib.syms(spec[1])
     if kind == "list":
         return lib.list([build_arg(lib, s) for s in spec[1]])
     raise ValueError(kind)
@@ -87,6 +89,8 @@ def store(case, rc, obj, out):
             return ["scalar", float(spec[1]) if isinstance(spec[1], float) else int(spec[1]), int(spec[2])]
         if spec[0] == "sym":
             return ["sym", spec[1]]
+        if spec[0] == "syms":
+            return ["syms", list(spec[1])]
         if spec[0] == "list":
             return ["list", [enc(s) for s in spec[1]]]
         raise ValueError(spec)
@@ -116,6 +120,8 @@ def load(path):
                 return ("scalar", spec[1], spec[2])
             if spec[0] == "sym":
                 return ("sym", spec[1])
+            if spec[0] == "syms":
+                return ("syms", spec[1])
             return ("list", [dec(s) for s in spec[1]])
 
         case = dict(name=name, fn=meta["fn"], tol=meta["tol"], canonical=meta["canonical"],

@@ -313,3 +313,25 @@ def test_group_sum_tree_order(libs):
         want = ora.lib.hgoTreeSumF64(x.ctypes.data, x.size)
         assert sums[gi].tobytes() == np.float64(want).tobytes(), (len(rows), sums[gi], want)
     gpu.free_inputs()
+
+
+@pytest.mark.parametrize("ops", [["eq", "lt"], ["geq", "eq", "neq"], ["eq", "eq"]])
+def test_join_multi_large(libs, ops):
+    """Multi-column @join_index at 1M x 3M rows with repeated keys: GPU vs oracle."""
+    rng = np.random.default_rng(46)
+    nb, npr = 1_000_000, 3_000_000
+    cols_b = [rng.integers(0, 400_000, nb).astype(np.int32), rng.integers(0, 60, nb).astype(np.int64),
+              np.round(rng.standard_normal(nb), 2)]
+    cols_p = [rng.integers(0, 400_000, npr).astype(np.int32), rng.integers(0, 60, npr).astype(np.int32),
+              np.round(rng.standard_normal(npr), 2)]
+    types_b, types_p = [H_I, H_L, H_E], [H_I, H_I, H_E]
+    k = len(ops)
+    if ops[0] != "eq":  # put the key column where the first @eq is
+        cols_b = [cols_b[1], cols_b[0], cols_b[2]]
+        cols_p = [cols_p[1], cols_p[0], cols_p[2]]
+        types_b = [types_b[1], types_b[0], types_b[2]]
+        types_p = [types_p[1], types_p[0], types_p[2]]
+    a, b = both(libs, "pfnJoinIndex", lambda L: (L.list([L.vec(c, t) for c, t in zip(cols_b[:k], types_b[:k])]),
+                                                 L.list([L.vec(c, t) for c, t in zip(cols_p[:k], types_p[:k])]),
+                                                 L.syms(ops)))
+    assert same(a, b) and a[0].size > 0
