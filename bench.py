@@ -500,6 +500,20 @@ def run_builtins(args):
             4 * args.fact + 4 * int(keep.len) + args.fact)
     measure("index_of_60M_in_2.2M", lambda: gpu.call("pfnIndexOf", keep, fact["fk"]), args.fact,
             4 * args.fact + 4 * int(keep.len) + 8 * args.fact)
+    # ---- enum / foreign-key path: the fact's foreign key over the 15M-row key column
+    #      (a permutation: hashed), the same keys sorted and sparse (binary search),
+    #      and the semi-join mask carried through the enum's index
+    nd = int(dim["pk"].len)
+    measure("enum_fk_60M_over_15M_hash", lambda: gpu.call("pfnEnum", dim["pk"], fact["fk"]), args.fact,
+            4 * args.fact + 4 * nd + 8 * args.fact)
+    en = gpu.call("pfnEnum", dim["pk"], fact["fk"])
+    ev = gpu.call("pfnValues", en)
+    dmask = gpu.call("pfnLt", dim["date"], gpu.scalar(D.WIN_HI, H_I))
+    measure("enum_semijoin_mask_60M", lambda: gpu.call("pfnIndex", dmask, ev), args.fact, 8 * args.fact + args.fact)
+    spk = dev(np.arange(nd, dtype=np.int64) * 4 + 1, H_L)
+    sfk = gpu.call("pfnIndex", spk, fact["fk"])
+    measure("enum_fk_60M_over_15M_sorted_i64", lambda: gpu.call("pfnEnum", spk, sfk), args.fact,
+            8 * args.fact + 8 * nd + 8 * args.fact)
     g2 = gpu.call("pfnGroup", gpu.list([fact["flag"], fact["status"]]))
     measure("group_trie_2x1B_60M", lambda: gpu.call("pfnGroup", gpu.list([fact["flag"], fact["status"]])), args.fact,
             2 * args.fact + 8 * args.fact)

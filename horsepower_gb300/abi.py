@@ -28,7 +28,7 @@ TYPE_OF = {np.dtype(np.bool_): H_B, np.dtype(np.int8): H_J, np.dtype(np.int16): 
            np.dtype(np.int32): H_I, np.dtype(np.int64): H_L, np.dtype(np.float32): H_F,
            np.dtype(np.float64): H_E}
 ERR = {1: "E_DOMAIN", 2: "E_GENERAL", 3: "E_INDEX", 4: "E_DIV_ZERO", 5: "E_LENGTH", 6: "E_TYPE",
-       9: "E_MATCH", 11: "E_RAZE_LIST", 12: "E_UNKNOWN", 99: "E_NOT_IMPL", 100: "E_DEVICE",
+       9: "E_MATCH", 10: "E_ENUM_INDEX", 11: "E_RAZE_LIST", 12: "E_UNKNOWN", 99: "E_NOT_IMPL", 100: "E_DEVICE",
        101: "E_DEVICE_OOM", 102: "E_DEVICE_TIMEOUT", 103: "E_NO_DEVICE", 104: "E_ADMISSION",
        105: "E_CANCELLED"}
 

@@ -141,8 +141,15 @@ I pfnList(V z, L n, V x[]) {
     return 0;
 }
 
-// pfnKeys / pfnValues on dicts and tables (h_primitive.cc:191-217, h_system.cc:508-515)
+// pfnKeys / pfnValues on dicts, tables and enums (h_primitive.cc:191-217, h_system.cc:501-515)
 I pfnKeys(V z, V x) {
+    if (x->typ == H_Y) {  // the enum's key node (copyV)
+        if (!x->y || !x->y->ek) return E_DOMAIN;
+        V ek = (V)x->y->ek;
+        *z = *ek;
+        if (is_inline(ek)) z->g = (G)&z->b;
+        return 0;
+    }
     if (x->typ != H_N && x->typ != H_A) return E_DOMAIN;
     V0* e = host_nodes(x);
     *z = e[0];
@@ -150,6 +157,22 @@ I pfnKeys(V z, V x) {
     return 0;
 }
 I pfnValues(V z, V x) {
+    if (x->typ == H_Y) {  // copyEnumIndex (h_system.cc:501-506): the i64 index itself
+        z->typ = H_L;
+        z->len = x->len;
+        if (x->len > 1) { z->g = x->g; return 0; }
+        z->g = (G)&z->b;
+        z->i64 = 0;
+        if (x->len == 1) {
+            HG_CHECK(ensure_init());
+            V0 t = *x;
+            t.typ = H_L;
+            uint64_t bits;
+            HG_CHECK(read_elem0(&t, &bits));
+            z->i64 = (L)bits;
+        }
+        return 0;
+    }
     if (x->typ != H_N && x->typ != H_A) return E_DOMAIN;
     V0* e = host_nodes(x) + 1;
     *z = *e;

@@ -120,14 +120,10 @@ __device__ __forceinline__ void table_insert(Table<K> t, K k, unsigned r, unsign
     {
         long long fb = filter_bit<K>(t, k);
         if (fb < 0) { flag_error(derr, DERR_CAPACITY); return; }
-        atomicOr(&t.filter[fb >> 5], 1u << (fb & 31));
-        if (t.direct) {
+        if (t.filter) atomicOr(&t.filter[fb >> 5], 1u << (fb & 31));
+        if (t.direct) {  // the minimum row wins; a second insert flags a repeated key
             unsigned* row = (unsigned*)t.slots;
-            unsigned prev = atomicCAS(&row[fb], 0xffffffffu, r);
-            if (prev != 0xffffffffu) {
-                atomicMin(&row[fb], r);
-                atomicOr(t.flags, 1u);
-            }
+            if (atomicMin(&row[fb], r) != 0xffffffffu) atomicOr(t.flags, 1u);
             return;
         }
     }
@@ -286,7 +282,8 @@ __global__ void k_key_minmax(const void* __restrict__ x, int typ, long long n, l
 }
 
 template <typename K>
-static I table_create(Table<K>* t, long long n, bool with_count, int direct, long long kmin, long long kmax) {
+static I table_create(Table<K>* t, long long n, bool with_count, int direct, long long kmin, long long kmax,
+                      bool filter = true) {
     const size_t ss = sizeof(K) == 4 ? 8 : 16;
     t->direct = direct;
     t->kmin = kmin;
@@ -304,15 +301,16 @@ static I table_create(Table<K>* t, long long n, bool with_count, int direct, lon
         while (fbits < 16ull * (unsigned long long)n) fbits <<= 1;
         t->slots = salloc(cap * ss);
     }
+    if (!direct) filter = true;  // hash probes always read the filter first
     t->fmask = fbits - 1;
     size_t fwords = (size_t)((fbits + 31) / 32);
-    t->filter = (unsigned*)salloc(fwords * 4);
+    t->filter = filter ? (unsigned*)salloc(fwords * 4) : nullptr;
     t->cnt = with_count ? (unsigned*)salloc(t->cap * 4) : nullptr;
     t->special = (unsigned*)salloc(32);
-    if (!t->slots || !t->filter || (with_count && !t->cnt) || !t->special) return E_DEVICE_OOM;
+    if (!t->slots || (filter && !t->filter) || (with_count && !t->cnt) || !t->special) return E_DEVICE_OOM;
     t->flags = t->special + 2;
     HG_CU(cudaMemsetAsync(t->slots, 0xff, t->cap * (direct ? 4 : ss), g_stream));
-    HG_CU(cudaMemsetAsync(t->filter, 0, fwords * 4, g_stream));
+    if (filter) HG_CU(cudaMemsetAsync(t->filter, 0, fwords * 4, g_stream));
     if (with_count) HG_CU(cudaMemsetAsync(t->cnt, 0, t->cap * 4, g_stream));
     HG_CU(cudaMemsetAsync(t->special, 0xff, 4, g_stream));
     HG_CU(cudaMemsetAsync(t->special + 1, 0, 12, g_stream));
@@ -322,7 +320,9 @@ static I table_create(Table<K>* t, long long n, bool with_count, int direct, lon
 // Builds the table of x's keys.  Integer keys whose range is at most 8n
 // (and below 2^31) use direct addressing; others hash.
 template <typename K>
-static I table_build(Table<K>* t, const void* x, int typ, long long n, bool with_count) {
+// `dense_unfiltered`: a direct table whose keys fill at least half of their
+// range gets no presence filter (index_of then reads the row word alone).
+static I table_build(Table<K>* t, const void* x, int typ, long long n, bool with_count, bool dense_unfiltered = false) {
     int direct = 0;
     long long kmin = 0, kmax = -1;
     if (n > 0 && (typ == H_J || typ == H_H || typ == H_I || typ == H_L)) {
@@ -341,7 +341,8 @@ static I table_build(Table<K>* t, const void* x, int typ, long long n, bool with
         if (lim < (1ull << 16)) lim = 1ull << 16;
         if (range <= lim && range < (1ull << 31)) { direct = 1; kmin = h[0]; kmax = h[1]; }
     }
-    HG_CHECK(table_create<K>(t, n, with_count, direct, kmin, kmax));
+    const bool filter = !(dense_unfiltered && direct && 2 * n >= kmax - kmin + 1);
+    HG_CHECK(table_create<K>(t, n, with_count, direct, kmin, kmax, filter));
     if (n > 0) {
         unsigned grid = grid_for(n, 256);
         if (grid > (unsigned)g_sms * 16) grid = g_sms * 16;
@@ -354,9 +355,17 @@ static I table_build(Table<K>* t, const void* x, int typ, long long n, bool with
 static bool key64(I typ) { return typ == H_L || typ == H_E; }
 
 // ------------------------------------------------------------------ index_of
+// Optional miss flag: set when some probe found no equal key (its index is
+// len(x)).  pfnEnum turns that into E_ENUM_INDEX (h_primitive.cc:2204).
+// Every lane of a warp reaches the call (the grid-stride loops exit
+// uniformly), so one ballot per warp suffices.
+__device__ __forceinline__ void note_miss(unsigned* miss, bool missed) {
+    if (miss && __any_sync(0xffffffffu, missed) && lane_id() == 0) atomicOr(miss, 1u);
+}
 template <typename K>
 __global__ void k_index_of(Table<K> t, const void* __restrict__ y, int typ, long long n, long long lenX,
-                           long long* __restrict__ z) {
+                           long long* __restrict__ z, unsigned* miss) {
+    bool missed = false;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         K k;
         long long r = lenX;
@@ -365,26 +374,174 @@ __global__ void k_index_of(Table<K> t, const void* __restrict__ y, int typ, long
             if (table_find<K>(t, k, &row) != -1) r = row;
         }
         z[i] = r;
+        missed |= r >= lenX;
     }
+    note_miss(miss, missed);
 }
 
-// has_up / has_down over adjacent pairs (isOrdered, h_system.cc:678-698)
+// has_up / has_down over adjacent pairs (isOrdered, h_system.cc:678-698),
+// plus bit 4 when some adjacent pair is equal (a strictly increasing x has
+// flags == 1)
 template <typename T>
 __global__ void k_order_flags(const T* __restrict__ x, long long n, unsigned* flags) {
-    bool up = false, down = false;
+    bool up = false, down = false, eq = false;
     for (long long i = 1 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         T a = x[i - 1], b = x[i];
         up |= b > a;
         down |= b < a;
+        eq |= b == a;
     }
     if (__any_sync(0xffffffffu, up) && lane_id() == 0) atomicOr(flags, 1u);
     if (__any_sync(0xffffffffu, down) && lane_id() == 0) atomicOr(flags, 2u);
+    if (__any_sync(0xffffffffu, eq) && lane_id() == 0) atomicOr(flags, 4u);
 }
 
-// binarySearch_I/L (h_system.cc:715-729) and searchOrdered (:731-745)
+// Strictly increasing x: a key has one index, so any exact search returns
+// what the reference's binary search returns.  Instead of ~log2(n)
+// dependent loads per probe, a bucket table over the key range narrows each
+// search to a few keys: bucket b = (key - x0) >> s holds x[bst[b] .. bst[b+1]),
+// with about four keys per bucket, so a probe reads two adjacent table words
+// and usually one line of x.
+__device__ __forceinline__ unsigned long long bucket_of(long long v, long long x0, int s) {
+    return ((unsigned long long)v - (unsigned long long)x0) >> s;
+}
+// bst[b] = first index of bucket b, for every non-empty bucket (rest stay ~0u)
+template <typename T>
+__global__ void k_bucket_firsts(const T* __restrict__ x, long long n, long long x0, int s, unsigned* __restrict__ bst,
+                                unsigned long long nb) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        unsigned long long b = bucket_of((long long)x[i], x0, s);
+        if (i == 0 || bucket_of((long long)x[i - 1], x0, s) != b) bst[b] = (unsigned)i;
+        if (i == n - 1) bst[nb] = (unsigned)n;
+    }
+}
+// empty bucket b: the first index whose key is >= the bucket's first value
+template <typename T>
+__global__ void k_bucket_fill(const T* __restrict__ x, long long n, long long x0, int s, unsigned* __restrict__ bst,
+                              unsigned long long nb) {
+    for (unsigned long long b = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; b < nb;
+         b += (unsigned long long)gridDim.x * blockDim.x) {
+        if (bst[b] != ~0u) continue;
+        const long long start = (long long)((unsigned long long)x0 + (b << s));
+        long long lo = 0, hi = n;
+        while (lo < hi) {
+            long long mid = (lo + hi) >> 1;
+            if ((long long)x[mid] < start) lo = mid + 1; else hi = mid;
+        }
+        bst[b] = (unsigned)lo;
+    }
+}
+template <typename T>
+__global__ void k_search_bucketed(const T* __restrict__ x, long long lenX, long long x0, long long xl, int s,
+                                  const unsigned* __restrict__ bst, const void* __restrict__ y, int ytyp, long long n,
+                                  long long* __restrict__ z, unsigned* miss) {
+    bool missed = false;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        long long v;
+        switch (ytyp) {
+        case H_B: v = ((const bool*)y)[i]; break;
+        case H_J: v = ((const int8_t*)y)[i]; break;
+        case H_H: v = ((const int16_t*)y)[i]; break;
+        case H_I: v = ((const int32_t*)y)[i]; break;
+        default: v = ((const long long*)y)[i]; break;
+        }
+        long long r = lenX;
+        if (v >= x0 && v <= xl) {
+            const unsigned long long b = bucket_of(v, x0, s);
+            unsigned lo = __ldg(bst + b), hi = __ldg(bst + b + 1);
+            while (lo < hi) {
+                unsigned mid = (lo + hi) >> 1;
+                if ((long long)x[mid] < v) lo = mid + 1; else hi = mid;
+            }
+            if (lo < (unsigned long long)lenX && (long long)x[lo] == v) r = lo;
+        }
+        z[i] = r;
+        missed |= r >= lenX;
+    }
+    note_miss(miss, missed);
+}
+
+__device__ __forceinline__ long long probe_val(const void* __restrict__ y, int ytyp, long long i) {
+    switch (ytyp) {
+    case H_B: return ((const bool*)y)[i];
+    case H_J: return ((const int8_t*)y)[i];
+    case H_H: return ((const int16_t*)y)[i];
+    case H_I: return ((const int32_t*)y)[i];
+    default: return ((const long long*)y)[i];
+    }
+}
+
+// Strictly increasing keys over a range of at most 8 per key: a rank table.
+// Word w covers keys x0 + 64w .. x0 + 64w + 63 and holds {bit set of the
+// keys present, index of the first of them}, so the index of key v is
+// first + popcount(bits below v's bit): one 16-byte read per probe from a
+// table of at most 2 bytes per key (L2 resident for tens of millions of keys).
+template <typename T>
+__global__ void k_rank_bits(const T* __restrict__ x, long long x0, const unsigned* __restrict__ bst, unsigned long long nw,
+                            ulonglong2* __restrict__ ent) {
+    for (unsigned long long w = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; w < nw;
+         w += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned lo = bst[w], hi = bst[w + 1];
+        unsigned long long bits = 0;
+        for (unsigned i = lo; i < hi; i++) bits |= 1ull << (((unsigned long long)(long long)x[i] - (unsigned long long)x0) & 63u);
+        ent[w] = make_ulonglong2(bits, (unsigned long long)lo);
+    }
+}
+__global__ void k_search_rank(long long x0, long long xl, const ulonglong2* __restrict__ ent, const void* __restrict__ y,
+                              int ytyp, long long n, long long lenX, long long* __restrict__ z, unsigned* miss) {
+    bool missed = false;
+#pragma unroll 1
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long v = probe_val(y, ytyp, i);
+        long long r = lenX;
+        if (v >= x0 && v <= xl) {
+            const unsigned long long d = (unsigned long long)v - (unsigned long long)x0;
+            const ulonglong2 e = __ldg(ent + (d >> 6));
+            const unsigned bit = (unsigned)(d & 63u);
+            if ((e.x >> bit) & 1ull) r = (long long)e.y + __popcll(e.x & ((1ull << bit) - 1ull));
+        }
+        z[i] = r;
+        missed |= r >= lenX;
+    }
+    note_miss(miss, missed);
+}
+
+// index_of on a direct-addressed table.  Dense keys (FILTER false): the row
+// word alone says present or absent (~0u), one read per probe.  Sparse keys,
+// where most probes miss: the presence filter first, a row only for hits.
+template <typename K, bool FILTER>
+__global__ void k_index_of_direct(const unsigned* __restrict__ rows, const unsigned* __restrict__ filter, long long kmin,
+                                  long long kmax, const void* __restrict__ y, int typ, long long n, long long lenX,
+                                  long long* __restrict__ z, unsigned* miss) {
+    bool missed = false;
+#pragma unroll 1
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        K k;
+        long long r = lenX;
+        if (key_at<K>(y, typ, i, &k)) {
+            const long long v = key_signed<K>(k);
+            if (v >= kmin && v <= kmax) {
+                const long long off = v - kmin;
+                bool cand = true;
+                if constexpr (FILTER) cand = (__ldg(filter + (off >> 5)) >> (off & 31)) & 1u;
+                if (cand) {
+                    const unsigned rr = __ldg(rows + off);
+                    if (rr != 0xffffffffu) r = rr;
+                }
+            }
+        }
+        z[i] = r;
+        missed |= r >= lenX;
+    }
+    note_miss(miss, missed);
+}
+
+// binarySearch_I/L (h_system.cc:715-729) and searchOrdered (:731-745); y is
+// read as words of `ytyp` (x's type, as the reference reads it)
 template <typename T>
 __global__ void k_search_ordered(const T* __restrict__ x, long long lenX, const void* __restrict__ y, int ytyp,
-                                 long long n, long long* __restrict__ z) {
+                                 long long n, long long* __restrict__ z, unsigned* miss) {
+    bool missed = false;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         long long v;
         switch (ytyp) {
@@ -406,7 +563,9 @@ __global__ void k_search_ordered(const T* __restrict__ x, long long lenX, const 
             }
         }
         z[i] = r;
+        missed |= r >= lenX;
     }
+    note_miss(miss, missed);
 }
 
 __global__ void k_first_false(const bool* __restrict__ x, long long n, unsigned long long* first) {
@@ -414,10 +573,15 @@ __global__ void k_first_false(const bool* __restrict__ x, long long n, unsigned 
         if (!x[i]) atomicMin(first, (unsigned long long)i);
 }
 __global__ void k_index_of_bool(const bool* __restrict__ y, long long n, const unsigned long long* first,
-                                long long lenX, long long* __restrict__ z) {
+                                long long lenX, long long* __restrict__ z, unsigned* miss) {
     long long f = (*first == ~0ull) ? lenX : (long long)*first;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        z[i] = y[i] ? 0 : f;
+    bool missed = false;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        long long r = y[i] ? 0 : f;
+        z[i] = r;
+        missed |= r >= lenX;
+    }
+    note_miss(miss, missed);
 }
 
 static unsigned grid_cap(long long n) {
@@ -901,20 +1065,66 @@ static I join_single(V z, V x, V y, V f) {
     return join_probe_unique<unsigned long long>(z, none, lin, 1, py, typ, ny, nx);
 }
 
-}  // namespace hg
+// Strictly increasing i32/i64 x of n >= 2 keys: bucket table in scratch, then the probe.
+template <typename T>
+static I search_bucketed_t(const T* x, long long lenX, const void* py, I ytyp, long long n, long long* z, unsigned* miss) {
+    T ends[2];
+    HG_CU(cudaMemcpyAsync(&ends[0], x, sizeof(T), cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaMemcpyAsync(&ends[1], x + lenX - 1, sizeof(T), cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));
+    const long long x0 = (long long)ends[0], xl = (long long)ends[1];
+    const unsigned long long range = (unsigned long long)xl - (unsigned long long)x0;
+    const bool rank = range < 8ull * (unsigned long long)lenX;  // rank table of <= 2 bytes per key
+    int s = 6;
+    if (!rank) {
+        const unsigned long long target = (unsigned long long)(lenX / 4);
+        s = 0;
+        while ((range >> s) + 1 > target) s++;
+    }
+    const unsigned long long nb = (range >> s) + 1;
+    unsigned* bst = (unsigned*)salloc((size_t)(nb + 1) * 4);
+    if (!bst) return E_DEVICE_OOM;
+    HG_CU(cudaMemsetAsync(bst, 0xff, (size_t)(nb + 1) * 4, g_stream));
+    HG_LAUNCH("bucket_firsts", grid_cap(lenX), 256, 0, k_bucket_firsts<T>, x, lenX, x0, s, bst, nb);
+    HG_LAUNCH("bucket_fill", grid_cap((long long)nb), 256, 0, k_bucket_fill<T>, x, lenX, x0, s, bst, nb);
+    if (rank) {
+        ulonglong2* ent = (ulonglong2*)salloc((size_t)nb * sizeof(ulonglong2));
+        if (!ent) return E_DEVICE_OOM;
+        HG_LAUNCH("rank_bits", grid_cap((long long)nb), 256, 0, k_rank_bits<T>, x, x0, bst, nb, ent);
+        HG_LAUNCH("search_rank", grid_cap(n), 256, 0, k_search_rank, x0, xl, ent, py, (int)ytyp, n, lenX, z, miss);
+    } else {
+        HG_LAUNCH("search_bucketed", grid_cap(n), 256, 0, k_search_bucketed<T>, x, lenX, x0, xl, s, bst, py, (int)ytyp, n, z, miss);
+    }
+    return last_launch_error();
+}
+static I search_bucketed(const void* px, I xtyp, long long lenX, const void* py, I ytyp, long long n, long long* z,
+                         unsigned* miss) {
+    if (xtyp == H_I) return search_bucketed_t<int32_t>((const int32_t*)px, lenX, py, ytyp, n, z, miss);
+    return search_bucketed_t<long long>((const long long*)px, lenX, py, ytyp, n, z, miss);
+}
 
-using namespace hg;
-
-extern "C" {
-
-I pfnIndexOf(V z, V x, V y) {
-    HG_CHECK(ensure_init());
-    ScratchScope ss;
+// pfnIndexOf (h_primitive.cc:1523-1579).  Real x and y: a monotone int x is
+// binary searched (searchOrdered, h_system.cc:731-745), anything else is
+// hashed on the promoted type (lib_index_of_*, h_libs.cc:299-373).  Dates,
+// times and symbols of one type hash as the integers of their width
+// (h_libs.h:25-31 maps lib_index_of_M/D/U/W/T to _I and Q/Z to _L), with no
+// ordered search.  `miss` (optional, device) is set when some y has no equal x.
+static I index_of(V z, V x, V y, unsigned* miss) {
+    V0 xa, ya;
+    bool hash_only = false;
+    if (x->typ == y->typ && (is_dtime(x->typ) || x->typ == H_Q)) {
+        xa = *x; ya = *y;
+        xa.typ = ya.typ = esize(x->typ) == 4 ? H_I : H_L;
+        if (is_inline(x)) xa.g = (G)&xa.b;
+        if (is_inline(y)) ya.g = (G)&ya.b;
+        x = &xa; y = &ya;
+        hash_only = true;
+    }
     if (!(is_real(x->typ) && is_real(y->typ)))
         return x->typ == y->typ ? set_error(E_NOT_IMPL, "index_of on this type is outside the path") : E_TYPE;
     long long lenX = x->len, n = y->len;
     void* dz;
-    if ((x->typ == H_I || x->typ == H_L)) {
+    if (!hash_only && (x->typ == H_I || x->typ == H_L)) {
         const void* px;
         HG_CHECK(in_ptr(x, &px));
         unsigned* flags = (unsigned*)salloc(16);
@@ -927,13 +1137,21 @@ I pfnIndexOf(V z, V x, V y) {
         unsigned fl = 0;
         HG_CU(cudaMemcpyAsync(&fl, flags, 4, cudaMemcpyDeviceToHost, g_stream));
         HG_CU(cudaStreamSynchronize(g_stream));
-        if (fl != 3) {  // monotone or constant: searchOrdered
+        if ((fl & 3) != 3) {  // monotone or constant: searchOrdered
+            // The reference reads y through x's element type (vI(y,i) / vL(y,i),
+            // h_system.cc:735-742): a y at least as wide is read as its first
+            // len(y) words of x's width; a narrower y would be read past its end.
+            if (esize(y->typ) < esize(x->typ))
+                return set_error(E_TYPE, "index_of: ordered %d-byte keys probed with %d-byte values", esize(x->typ), esize(y->typ));
+            const I ywords = x->typ;
             const void* py;
             HG_CHECK(in_ptr(y, &py));
             HG_CHECK(alloc_out(z, H_L, n, &dz));
-            if (n > 0) {
-                if (x->typ == H_I) HG_LAUNCH("search_ordered", grid_cap(n), 256, 0, k_search_ordered<int32_t>, (const int32_t*)px, lenX, py, (int)y->typ, n, (long long*)dz);
-                else HG_LAUNCH("search_ordered", grid_cap(n), 256, 0, k_search_ordered<long long>, (const long long*)px, lenX, py, (int)y->typ, n, (long long*)dz);
+            if (n > 0 && fl == 1 && lenX >= 64) {
+                HG_CHECK(search_bucketed(px, x->typ, lenX, py, ywords, n, (long long*)dz, miss));
+            } else if (n > 0) {
+                if (x->typ == H_I) HG_LAUNCH("search_ordered", grid_cap(n), 256, 0, k_search_ordered<int32_t>, (const int32_t*)px, lenX, py, (int)ywords, n, (long long*)dz, miss);
+                else HG_LAUNCH("search_ordered", grid_cap(n), 256, 0, k_search_ordered<long long>, (const long long*)px, lenX, py, (int)ywords, n, (long long*)dz, miss);
             }
             HG_CHECK(last_launch_error());
             return finish_out(z, dz);
@@ -949,22 +1167,104 @@ I pfnIndexOf(V z, V x, V y) {
         if (!first) return E_DEVICE_OOM;
         HG_CU(cudaMemsetAsync(first, 0xff, 8, g_stream));
         if (lenX > 0) HG_LAUNCH("first_false", grid_cap(lenX), 256, 0, k_first_false, (const bool*)px, lenX, first);
-        if (n > 0) HG_LAUNCH("index_of_bool", grid_cap(n), 256, 0, k_index_of_bool, (const bool*)py, n, first, lenX, (long long*)dz);
+        if (n > 0) HG_LAUNCH("index_of_bool", grid_cap(n), 256, 0, k_index_of_bool, (const bool*)py, n, first, lenX, (long long*)dz, miss);
         HG_CHECK(last_launch_error());
         return finish_out(z, dz);
     }
     if (key64(typ)) {
         Table<unsigned long long> t;
-        HG_CHECK(table_build<unsigned long long>(&t, px, typ, lenX, false));
-        if (n > 0) HG_LAUNCH("index_of", grid_cap(n), 256, 0, k_index_of<unsigned long long>, t, py, (int)typ, n, lenX, (long long*)dz);
+        HG_CHECK(table_build<unsigned long long>(&t, px, typ, lenX, false, true));
+        if (n > 0 && t.direct && t.filter)
+            HG_LAUNCH("index_of_direct", grid_cap(n), 256, 0, (k_index_of_direct<unsigned long long, true>),
+                      (const unsigned*)t.slots, t.filter, t.kmin, t.kmax, py, (int)typ, n, lenX, (long long*)dz, miss);
+        else if (n > 0 && t.direct)
+            HG_LAUNCH("index_of_direct", grid_cap(n), 256, 0, (k_index_of_direct<unsigned long long, false>),
+                      (const unsigned*)t.slots, t.filter, t.kmin, t.kmax, py, (int)typ, n, lenX, (long long*)dz, miss);
+        else if (n > 0) HG_LAUNCH("index_of", grid_cap(n), 256, 0, k_index_of<unsigned long long>, t, py, (int)typ, n, lenX, (long long*)dz, miss);
     } else {
         Table<unsigned> t;
-        HG_CHECK(table_build<unsigned>(&t, px, typ, lenX, false));
-        if (n > 0) HG_LAUNCH("index_of", grid_cap(n), 256, 0, k_index_of<unsigned>, t, py, (int)typ, n, lenX, (long long*)dz);
+        HG_CHECK(table_build<unsigned>(&t, px, typ, lenX, false, true));
+        if (n > 0 && t.direct && t.filter)
+            HG_LAUNCH("index_of_direct", grid_cap(n), 256, 0, (k_index_of_direct<unsigned, true>),
+                      (const unsigned*)t.slots, t.filter, t.kmin, t.kmax, py, (int)typ, n, lenX, (long long*)dz, miss);
+        else if (n > 0 && t.direct)
+            HG_LAUNCH("index_of_direct", grid_cap(n), 256, 0, (k_index_of_direct<unsigned, false>),
+                      (const unsigned*)t.slots, t.filter, t.kmin, t.kmax, py, (int)typ, n, lenX, (long long*)dz, miss);
+        else if (n > 0) HG_LAUNCH("index_of", grid_cap(n), 256, 0, k_index_of<unsigned>, t, py, (int)typ, n, lenX, (long long*)dz, miss);
     }
     HG_CHECK(last_launch_error());
     HG_CHECK(check_device_errors());
     return finish_out(z, dz);
+}
+
+}  // namespace hg
+
+using namespace hg;
+
+extern "C" {
+
+I pfnIndexOf(V z, V x, V y) {
+    HG_CHECK(ensure_init());
+    ScratchScope ss;
+    return index_of(z, x, y, nullptr);
+}
+
+// pfnEnum (h_primitive.cc:2198-2222): the enum of the foreign-key column y
+// over the key column x.  The index is index_of(x, y) with the miss flag
+// folded into the probe kernels, so the range check of :2204
+// (E_ENUM_INDEX when some y has no equal key) costs no second pass.  The
+// node is H_Y with len(y) and the i64 index (device, never inline) in g; its
+// header {source -1, ek x, ev y} points at the caller's x and y, which must
+// outlive it, as in the reference.  The index is registered as lying in
+// [0, len(x)), so @index(column of x, @values(enum)) skips its bounds check.
+// Two equal-length lists (multi-column keys, :2210-2219) are not built: the
+// reference's own schemas add only single-column foreign keys (global.cc,
+// addFKey2 is commented out).
+I pfnEnum(V z, V x, V y) {
+    HG_CHECK(ensure_init());
+    ScratchScope ss;
+    if (x->typ == H_G && y->typ == H_G)
+        return x->len == y->len ? set_error(E_NOT_IMPL, "enum over multi-column keys is outside the path") : E_DOMAIN;
+    if (!is_basic(x->typ)) return E_DOMAIN;
+    long long mark = out_mark();
+    unsigned* miss = (unsigned*)salloc(16);
+    if (!miss) return E_DEVICE_OOM;
+    HG_CU(cudaMemsetAsync(miss, 0, 4, g_stream));
+    V0 ind;
+    I e = index_of(&ind, x, y, miss);
+    if (e) { out_rewind(mark); return e; }
+    unsigned h = 0;
+    HG_CU(cudaMemcpyAsync(&h, miss, 4, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));
+    if (h) { out_rewind(mark); return E_ENUM_INDEX; }
+    Y hdr = (Y)halloc(sizeof(Y0));
+    if (!hdr) { out_rewind(mark); return E_DEVICE_OOM; }
+    hdr->source = -1;
+    hdr->ek = (G)x;
+    hdr->ev = (G)y;
+    G payload = ind.g;
+    if (is_inline(&ind)) {
+        void* d = dalloc(16);
+        if (!d) { out_rewind(mark); return E_DEVICE_OOM; }
+        HG_CU(cudaMemcpyAsync(d, &ind.b, 8, cudaMemcpyHostToDevice, g_stream));
+        HG_CU(cudaStreamSynchronize(g_stream));
+        payload = (G)d;
+    }
+    z->typ = H_Y;
+    z->len = y->len;
+    z->g = payload;
+    z->y = hdr;
+    register_bound(payload, z->len, x->len);
+    return apply_residency(z);
+}
+
+// pfnFetch (h_primitive.cc:219-225): copyV of the enum's value node.
+I pfnFetch(V z, V x) {
+    if (x->typ != H_Y || !x->y || !x->y->ev) return E_DOMAIN;
+    V ev = (V)x->y->ev;
+    *z = *ev;
+    if (is_inline(ev)) z->g = (G)&z->b;
+    return 0;
 }
 
 I pfnMember(V z, V y, V x) {

@@ -306,6 +306,18 @@ static I to_host_rec(V z, V x, bool in_place) {
         }
         return 0;
     }
+    if (x->typ == H_Y) {  // enum: the i64 index moves, the header stays shared
+        V0 hdr = *x;
+        if (z != x) *z = hdr;
+        if (g_host->contains(hdr.g)) return 0;
+        size_t nb = (size_t)(hdr.len > 0 ? hdr.len : 1) * 8;
+        void* h = g_host->alloc(nb);
+        if (!h) return E_DEVICE_OOM;
+        if (hdr.len > 0) HG_CU(cudaMemcpyAsync(h, hdr.g, (size_t)hdr.len * 8, cudaMemcpyDefault, g_stream));
+        HG_CU(cudaStreamSynchronize(g_stream));
+        z->g = (G)h;
+        return 0;
+    }
     if (!is_basic(x->typ)) return set_error(E_NOT_IMPL, "hgpuToHost: type %d", x->typ);
     V0 hdr = *x;
     if (z != x) *z = hdr;
@@ -464,7 +476,11 @@ V initV(V x, I typ, L len) {
     x->typ = typ;
     x->len = len;
     if (is_basic(typ)) x->g = (len > 1) ? (G)halloc((size_t)getTypeSize(typ, len)) : (G)&x->b;
-    else x->g = (G)halloc((size_t)(len > 0 ? len : 1) * sizeof(V0));
+    else if (typ == H_Y) {  // i64 index out of line plus a header (h_memory.cc:184-194)
+        x->g = (G)halloc((size_t)(len > 0 ? len : 1) * 8);
+        x->y = (Y)halloc(sizeof(Y0));
+        if (x->y) memset(x->y, 0, sizeof(Y0));
+    } else x->g = (G)halloc((size_t)(len > 0 ? len : 1) * sizeof(V0));
     return x;
 }
 
@@ -526,6 +542,15 @@ static I to_device_rec(V z, V x) {
         for (L i = 0; i < hdr.len; i++) HG_CHECK(to_device_rec((V0*)z->g + i, (V0*)hdr.g + i));
         return 0;
     }
+    if (x->typ == H_Y) {  // enum payloads are never inline (initV, h_memory.cc:184-194)
+        V0 hdr = *x;
+        *z = hdr;
+        void* d = dalloc((size_t)(hdr.len > 1 ? hdr.len : 2) * 8);
+        if (!d) return E_DEVICE_OOM;
+        if (hdr.len > 0) HG_CU(cudaMemcpyAsync(d, hdr.g, (size_t)hdr.len * 8, cudaMemcpyDefault, g_stream));
+        z->g = (G)d;
+        return 0;
+    }
     if (!is_basic(x->typ)) return set_error(E_NOT_IMPL, "hgpuToDevice: type %d", x->typ);
     V0 hdr = *x;
     *z = hdr;
@@ -551,7 +576,7 @@ I hgpuToDevice(V z, V x) {
 
 I hgpuIsDevice(V x) {
     if (ensure_init()) return 0;
-    if (!is_basic(x->typ) || is_inline(x)) return 0;
+    if (!(is_basic(x->typ) || x->typ == H_Y) || is_inline(x) || x->len < 1) return 0;
     if (g_host->contains(x->g)) return 0;
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, x->g) != cudaSuccess) { cudaGetLastError(); return 0; }

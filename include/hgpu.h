@@ -49,7 +49,14 @@ typedef long long L, Q, Z;
 typedef float     F;
 typedef double    E;
 typedef struct { F real, imag; } X;
-struct hgpu_enum_s;   /* reference Y0 (common.h:23); enums are outside the path */
+/* Enum header: the reference's Y0 (common.h:19).  `source` names the enum's
+ * table column (-1 for one made by pfnEnum), `ek` is the key node (the
+ * primary-key column, a V stored as G) and `ev` the value node (the
+ * foreign-key column).  An H_Y node holds the header in its union member `y`
+ * and its i64 index into ek in `g`, always out of line (initV,
+ * h_memory.cc:184-194). */
+struct hgpu_enum_s { Q source; G ek, ev; };
+typedef struct hgpu_enum_s Y0, *Y;
 struct hgpu_table_s;  /* reference A0 (common.h:25); tables are outside the path */
 
 /* Value node: field order and union members of src/horseir/v3/backend/common.h:31-55.
@@ -163,6 +170,12 @@ I pfnLen(V z, V x);             /* h_primitive.cc:656-662 */
 I pfnIndex  (V z, V x, V y);    /* h_primitive.cc:43-94 */
 I pfnIndexOf(V z, V x, V y);    /* h_primitive.cc:1523-1579 */
 I pfnMember (V z, V y, V x);    /* h_primitive.cc:2287-2336 (note argument order) */
+/* Enum / foreign-key path: pfnEnum builds the enum of y (foreign-key column)
+ * over x (primary-key column) as index_of(x, y), E_ENUM_INDEX when some y has
+ * no key; pfnFetch returns y back.  pfnAddFKey (h_primitive.cc:2425-2466) is
+ * pfnEnum over two table columns plus table metadata. */
+I pfnEnum   (V z, V x, V y);    /* h_primitive.cc:2198-2222 */
+I pfnFetch  (V z, V x);         /* h_primitive.cc:219-225 */
 I pfnJoinIndex(V z, V x, V y, V f); /* h_primitive.cc:2122-2155; several columns: pfnJoinIndexMultiple :2094-2110 */
 /* Grouping and ordering */
 I pfnGroup    (V z, V x);       /* h_primitive.cc:993-999 */
@@ -171,8 +184,8 @@ I pfnGroupBasic(V z, V x);      /* h_primitive.cc:1002-1057 */
 I pfnOrderBy  (V z, V x, V y);  /* h_primitive.cc:1769-1816 */
 /* List plumbing used by the segmented-reduction chain (each_right @index -> each @sum -> raze) */
 I pfnList (V z, L n, V x[]);    /* h_primitive.cc:32-36 */
-I pfnKeys (V z, V x);           /* h_primitive.cc:191-203 */
-I pfnValues(V z, V x);          /* h_primitive.cc:205-217 */
+I pfnKeys (V z, V x);           /* h_primitive.cc:191-203 (dict, table, enum key) */
+I pfnValues(V z, V x);          /* h_primitive.cc:205-217 (dict, table, enum index) */
 I pfnEach     (V z, V x, I (*foo)(V, V));        /* h_primitive.cc:1818-1832 */
 I pfnEachRight(V z, V x, V y, I (*foo)(V, V, V)); /* h_primitive.cc:1882-1904 */
 I pfnRaze (V z, V x);           /* h_primitive.cc:935-955 */

@@ -77,6 +77,7 @@ V initV(V x, I typ, L len) {
     else {
         x->g = hgo_alloc(getTypeSize(typ, len));
         if (typ == H_G || typ == H_N) memset(x->g, 0, (size_t)getTypeSize(typ, len));
+        if (typ == H_Y) { x->y = (Y)hgo_alloc(sizeof(Y0)); memset(x->y, 0, sizeof(Y0)); }
     }
     R x;
 }
@@ -209,7 +210,7 @@ I pfnCompress(V z, V x, V y) {
     count_per_thread(sB(x), lenX, par);
     for (L i = 0; i < nc; i++) lenZ += par[i];
     for (L i = 1; i < nc; i++) off[i] = par[i - 1] + off[i - 1];
-    switch (typZ) {  /* types handled at h_primitive.cc:1497-1510 */
+    switch (typZ) {  /* types handled at h_primitive.cc:1497-1510; an enum exits at :1492-1494 */
     case H_B: case H_J: case H_C: case H_H: case H_I: case H_L: case H_F: case H_E: case H_Q: case H_S: case H_D: break;
     default: free(par); free(off); R E_NOT_IMPL;
     }
@@ -552,8 +553,7 @@ static B key_bits(V x, L i, uint64_t *k) {
 
 /* binarySearch_I/L and searchOrdered: h_system.cc:715-745 — returns the index
  * the recursion lands on, or len(x).  An empty x (which the reference reads
- * at x[0]) yields len(x)=0.  A probe vector of another type is read through
- * its conversion to x's type (the reference reads it at x's width). */
+ * at x[0]) yields len(x)=0. */
 static L bsearch_L(const L *x, L low, L high, L val) {
     for (;;) {
         L mid = (low + high) >> 1;
@@ -576,24 +576,21 @@ I pfnIndexOf(V z, V x, V y) {
     if (hgo_is_real(vp(x)) && hgo_is_real(vp(y))) {
         L lenX = vn(x), lenZ = vn(y);
         if (hgo_is_ordered(x)) {
-            V0 ty;
-            CHECKE(hgo_promote(&ty, y, vp(x) == H_I && vp(y) <= H_I ? H_I : H_L));
+            /* searchOrdered (h_system.cc:731-745) reads y through x's element
+             * type, vI(y,i) / vL(y,i), whatever y's type: a y at least as wide
+             * as x is read as its first len(y) words of x's width; a narrower y
+             * would be read past its end (undefined): E_TYPE here. */
+            if (getTypeSize(vp(y), 1) < getTypeSize(vp(x), 1)) R E_TYPE;
             initV(z, H_L, lenZ);
             if (lenX == 0) { for (L i = 0; i < lenZ; i++) sL(z)[i] = 0; R 0; }
             if (vp(x) == H_I) {
-                if (vp(&ty) == H_I) {
+                const I *yw = (const I *)vg(y);
 #pragma omp parallel for
-                    for (L i = 0; i < lenZ; i++) { L k = bsearch_I(sI(x), 0, lenX, sI(&ty)[i]); sL(z)[i] = k < 0 ? lenX : k; }
-                } else {  /* i64 probes against i32 x: compare in i64 */
-                    for (L i = 0; i < lenZ; i++) {
-                        L v = sL(&ty)[i], k = -1, low = 0, high = lenX;
-                        for (;;) { L mid = (low + high) >> 1; if ((L)sI(x)[mid] == v) { k = mid; break; } if (low == mid) break; if ((L)sI(x)[mid] > v) high = mid; else low = mid; }
-                        sL(z)[i] = k < 0 ? lenX : k;
-                    }
-                }
+                for (L i = 0; i < lenZ; i++) { L k = bsearch_I(sI(x), 0, lenX, yw[i]); sL(z)[i] = k < 0 ? lenX : k; }
             } else {
+                const L *yw = (const L *)vg(y);
 #pragma omp parallel for
-                for (L i = 0; i < lenZ; i++) { L k = bsearch_L(sL(x), 0, lenX, sL(&ty)[i]); sL(z)[i] = k < 0 ? lenX : k; }
+                for (L i = 0; i < lenZ; i++) { L k = bsearch_L(sL(x), 0, lenX, yw[i]); sL(z)[i] = k < 0 ? lenX : k; }
             }
             R 0;
         }
@@ -621,9 +618,49 @@ I pfnIndexOf(V z, V x, V y) {
         ht_free(&t);
         R 0;
     }
-    if (vp(x) == vp(y)) R E_NOT_IMPL;  /* dates, symbols, strings, lists: outside the path */
+    if (vp(x) == vp(y) && (is_dtime(vp(x)) || vp(x) == H_Q)) {
+        /* INDEXOF(M/D/Z/U/W/T/Q) = lib_index_of_I/L (h_libs.h:25-31): hashed,
+         * never binary searched */
+        V0 tx = *x, ty = *y;
+        tx.typ = ty.typ = getTypeSize(vp(x), 1) == 4 ? H_I : H_L;
+        if (vg(x) == (G)&x->b) tx.g = (G)&tx.b;
+        if (vg(y) == (G)&y->b) ty.g = (G)&ty.b;
+        L lenX = vn(x), lenZ = vn(y);
+        initV(z, H_L, lenZ);
+        HT t;
+        ht_init(&t, lenX);
+        for (L i = 0; i < lenX; i++) { uint64_t k; if (key_bits(&tx, i, &k)) ht_insert(&t, k, i); }
+        for (L i = 0; i < lenZ; i++) {
+            uint64_t k; L r = -1;
+            if (key_bits(&ty, i, &k)) r = ht_find(&t, k);
+            sL(z)[i] = r < 0 ? lenX : r;
+        }
+        ht_free(&t);
+        R 0;
+    }
+    if (vp(x) == vp(y)) R E_NOT_IMPL;  /* strings, lists: outside the path */
     R E_TYPE;
 }
+
+/* pfnEnum: h_primitive.cc:2198-2222 (basic x).  The enum's index is
+ * index_of(x, y); an index >= len(x) is E_ENUM_INDEX (:2204).  Header
+ * {source -1, ek x, ev y} (initEnum, h_primitive.h:12-16).  Two lists of
+ * equal length (multi-column keys) are outside the path: E_NOT_IMPL. */
+I pfnEnum(V z, V x, V y) {
+    if (vp(x) == H_G && vp(y) == H_G) R vn(x) == vn(y) ? E_NOT_IMPL : E_DOMAIN;
+    if (!hgo_is_basic(vp(x))) R E_DOMAIN;
+    V0 ind;
+    CHECKE(pfnIndexOf(&ind, x, y));
+    L lenZ = vn(&ind);
+    for (L i = 0; i < lenZ; i++) if (sL(&ind)[i] >= vn(x)) R E_ENUM_INDEX;
+    initV(z, H_Y, lenZ);
+    z->y->source = -1; z->y->ek = (G)x; z->y->ev = (G)y;
+    memcpy(vg(z), sL(&ind), (size_t)lenZ * 8);
+    R 0;
+}
+
+/* pfnFetch: h_primitive.cc:219-225 */
+I pfnFetch(V z, V x) { if (vp(x) == H_Y) R hgo_copyV(z, (V)x->y->ev); R E_DOMAIN; }
 
 /* pfnMember(z, y, x): h_primitive.cc:2287-2336, lib_member_*: h_libs.cc:897-1018.
  * z[i] = y[i] in x.  Sets of <= 2 elements use direct compares (== on the
@@ -870,8 +907,17 @@ I pfnList(V z, L n, V x[]) {
     R 0;
 }
 /* pfnKeys / pfnValues on a dict: h_primitive.cc:191-217, getDictValue h_system.cc:508-515 */
-I pfnKeys(V z, V x) { if (vp(x) == H_N || vp(x) == H_A) R hgo_copyV(z, vV(x, 0)); R E_DOMAIN; }
-I pfnValues(V z, V x) { if (vp(x) == H_N || vp(x) == H_A) R hgo_copyV(z, vV(x, 1)); R E_DOMAIN; }
+I pfnKeys(V z, V x) {
+    if (vp(x) == H_Y) R hgo_copyV(z, (V)x->y->ek);
+    if (vp(x) == H_N || vp(x) == H_A) R hgo_copyV(z, vV(x, 0));
+    R E_DOMAIN;
+}
+/* enum: copyEnumIndex (h_system.cc:501-506), the index as an i64 vector */
+I pfnValues(V z, V x) {
+    if (vp(x) == H_Y) { z->typ = H_L; z->len = vn(x); z->g = vg(x); R 0; }
+    if (vp(x) == H_N || vp(x) == H_A) R hgo_copyV(z, vV(x, 1));
+    R E_DOMAIN;
+}
 
 /* pfnEach: h_primitive.cc:1818-1832 (plain lists) */
 I pfnEach(V z, V x, I (*foo)(V, V)) {

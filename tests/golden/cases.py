@@ -234,4 +234,45 @@ def build_cases():
     add("join_multi_small_build", "pfnJoinIndex", Ls(V([4, 7, 4], H_I), V([1, 2, 3], H_I)),
         Ls(V(rng.integers(0, 9, 200).astype(np.int32), H_I), V(rng.integers(0, 4, 200).astype(np.int32), H_I)), ("syms", ["eq", "lt"]))
     add("join_multi_len_mismatch", "pfnJoinIndex", Ls(V(bk, H_I), V(ba, H_I)), Ls(V(pk2, H_I)), ("syms", ["eq", "lt"]), error=5)
+
+    # ---- index_of on dates and symbols: hashed as ints, first occurrence (h_libs.h:25-31)
+    dd = np.sort(rng.integers(9000, 9400, 3000)).astype(np.int32)      # sorted with repeats
+    add("index_of_date", "pfnIndexOf", V(dd, H_D), V(rng.integers(8990, 9410, 4000).astype(np.int32), H_D))
+    names = [f"s{i}" for i in range(40)]
+    add("index_of_sym", "pfnIndexOf", ("syms", [names[i] for i in rng.integers(0, 30, 200)]),
+        ("syms", [names[i] for i in rng.integers(0, 40, 300)]))
+    add("index_of_date_vs_int", "pfnIndexOf", V(dd, H_D), V([9100], H_I), error=6)
+    # strictly increasing keys (bucketed search on the GPU): skewed gaps, negatives, extremes
+    sk = np.concatenate([np.arange(-3000, 2000, 3), [10 ** 12, 10 ** 12 + 5, 2 ** 62]]).astype(np.int64)
+    probe = np.concatenate([rng.integers(-3100, 2100, 3000), [10 ** 12, 10 ** 12 + 1, 2 ** 62, -2 ** 63, 2 ** 63 - 1]])
+    add("index_of_strict_skewed", "pfnIndexOf", V(sk, H_L), V(probe.astype(np.int64), H_L))
+    si = np.unique(rng.integers(-2 ** 31, 2 ** 31 - 1, 5000)).astype(np.int32)
+    add("index_of_strict_i32", "pfnIndexOf", V(si, H_I),
+        V(np.concatenate([si[rng.integers(0, si.size, 2000)], rng.integers(-2 ** 31, 2 ** 31 - 1, 500)]).astype(np.int64), H_L))
+
+    # ---- enum / foreign-key path (pfnEnum h_primitive.cc:2198-2222, pfnFetch/Keys/Values :191-225):
+    #      chain outputs are values, fetch, keys, len, @index(key-side mask, values),
+    #      the indices kept by a mask over the foreign keys and the key column gathered
+    #      through them (the pattern of the reference's hand-written q5 plan)
+    pk = rng.permutation(20000).astype(np.int32)                      # unsorted primary key: hash
+    fk = pk[rng.integers(0, 20000, 50000)]
+    cases.append(dict(name="enum_hash_i32", fn="@chain_enum", tol=0.0, canonical=False, error=0,
+                      args=[V(pk, H_I), V(fk, H_I), V(rng.random(50000) < 0.3, H_B), V(rng.random(20000) < 0.5, H_B)]))
+    pks = np.arange(1, 30001, dtype=np.int64) * 4                    # sorted primary key: binary search
+    fks = pks[rng.integers(0, 30000, 60000)]
+    cases.append(dict(name="enum_sorted_i64", fn="@chain_enum", tol=0.0, canonical=False, error=0,
+                      args=[V(pks, H_L), V(fks, H_L), V(rng.random(60000) < 0.05, H_B), V(rng.random(30000) < 0.2, H_B)]))
+    cases.append(dict(name="enum_promote", fn="@chain_enum", tol=0.0, canonical=False, error=0,
+                      args=[V(pk.astype(np.int64), H_L), V(fk[:5000], H_I), V(rng.random(5000) < 0.5, H_B), V(rng.random(20000) < 0.5, H_B)]))
+    dk = rng.permutation(np.arange(8000, 9000)).astype(np.int32)
+    cases.append(dict(name="enum_date", fn="@chain_enum", tol=0.0, canonical=False, error=0,
+                      args=[V(dk, H_D), V(dk[rng.integers(0, 1000, 3000)], H_D), V(rng.random(3000) < 0.5, H_B), V(rng.random(1000) < 0.5, H_B)]))
+    cases.append(dict(name="enum_one", fn="@chain_enum", tol=0.0, canonical=False, error=0,
+                      args=[V([5, 9, 2], H_I), V([2], H_I), V([True], H_B), V([True, False, True], H_B)]))
+    cases.append(dict(name="enum_keep_one", fn="@chain_enum", tol=0.0, canonical=False, error=0,
+                      args=[V([5, 9, 2], H_I), V([2, 5, 9, 9], H_I), V([False, False, True, False], H_B), V([True, False, True], H_B)]))
+    add("enum_missing_key", "pfnEnum", V(pk, H_I), V(np.append(fk[:1000], 20001).astype(np.int32), H_I), error=10)
+    add("enum_empty_key", "pfnEnum", V(np.zeros(0, np.int32), H_I), V([3], H_I), error=10)
+    add("enum_type", "pfnEnum", V(pk, H_I), V(np.zeros(3, np.int32), H_D), error=6)
+    add("enum_list_len", "pfnEnum", Ls(V(pk[:10], H_I), V(pk[:10], H_I)), Ls(V(fk[:10], H_I)), error=1)
     return cases

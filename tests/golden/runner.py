@@ -44,6 +44,17 @@ def run_case(lib, case, fused=False):
                     e = lib.call("pfnEach", t, lib.fn_ptr(agg))
                     outs.append(lib.to_py(lib.call("pfnRaze", e)))
             return 0, outs
+        if fn == "@chain_enum":
+            # x: key column, y: foreign-key column, m: mask over y, pm: mask over x.
+            # The foreign-key step of a plan: values, a semi-join mask through
+            # the index, the kept indices and the gathered key column.
+            e = lib.call("pfnEnum", args[0], args[1])
+            idx = lib.call("pfnValues", e)
+            kept = lib.call("pfnCompress", args[2], idx)
+            outs = [lib.to_py(idx), lib.to_py(lib.call("pfnFetch", e)), lib.to_py(lib.call("pfnKeys", e)),
+                    lib.to_py(lib.call("pfnLen", e)), lib.to_py(lib.call("pfnIndex", args[3], idx)),
+                    lib.to_py(kept), lib.to_py(lib.call("pfnIndex", args[0], kept))]
+            return 0, outs
         z = lib.call(fn, *args)
         return 0, lib.to_py(z)
     except BuiltinError as e:
