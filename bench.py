@@ -465,7 +465,8 @@ def run_builtins(args):
     m6 = gpu.call("pfnAnd", gpu.call("pfnGeq", ship, gpu.scalar(D.WIN_LO, H_I)), gpu.call("pfnLt", ship, gpu.scalar(D.WIN_HI, H_I)))
     n6 = 6_001_215
     sel6 = int(((t0["shipdate"] >= D.WIN_LO) & (t0["shipdate"] < D.WIN_HI)).sum())
-    measure("compress_f64_6M", lambda: gpu.call("pfnCompress", m6, price), n6, n6 + 16 * sel6)
+    # compress: the mask and the values read once, the kept values written once (9 B/row + 8 B/kept)
+    measure("compress_f64_6M", lambda: gpu.call("pfnCompress", m6, price), n6, 9 * n6 + 8 * sel6)
     ch = P.Chain(gpu, P.Q6_CHAIN.format(lo=D.WIN_LO, hi=D.WIN_HI))
     measure("q6_fused_chain_6M", lambda: ch.run([ship, qty, disc, price]), n6, 24 * n6)
     measure("q6_builtins_6M", lambda: P.filter_aggregate(gpu, dict(shipdate=ship, qty=qty, disc=disc, price=price)),
@@ -478,7 +479,7 @@ def run_builtins(args):
     measure("compare_f64_60M", lambda: gpu.call("pfnGt", a, gpu.scalar(0.25, H_E)), N, 9 * N)
     measure("arith_mul_f64_60M", lambda: gpu.call("pfnMul", a, b), N, 24 * N)
     measure("logic_and_60M", lambda: gpu.call("pfnAnd", mk, mk2), N, 3 * N)
-    measure("compress_f64_60M_half", lambda: gpu.call("pfnCompress", mk, a), N, N + 16 * (N // 2))
+    measure("compress_f64_60M_half", lambda: gpu.call("pfnCompress", mk, a), N, 9 * N + 8 * (N // 2))
     measure("where_60M_half", lambda: gpu.call("pfnWhere", mk), N, N + 8 * (N // 2))
     measure("sum_f64_60M", lambda: gpu.call("pfnSum", a), N, 8 * N)
     measure("max_f64_60M", lambda: gpu.call("pfnMax", a), N, 8 * N)
@@ -521,10 +522,12 @@ def run_builtins(args):
     o = S.order_table(gpu, args.order_rows, seed=2)
     pay = dev(rng.uniform(0.0, 1e5, args.order_rows), H_E)
     n2 = args.order_rows
-    measure("group_i64_zipf_150M", lambda: gpu.call("pfnGroup", o["key"]), n2, 16 * n2, reps=max(2, args.steps // 2))
     g = gpu.call("pfnGroup", o["key"])
     vals = gpu.call("pfnValues", g)
     ng = int(gpu.call("pfnKeys", g).len)
+    # group: keys in (8N), row lists (8N) + group keys and starts (16G) out
+    measure("group_i64_zipf_150M", lambda: gpu.call("pfnGroup", o["key"]), n2, 16 * n2 + 16 * ng,
+            reps=max(2, args.steps // 2))
     measure("group_sum_f64_150M", lambda: gpu.call("hgpuGroupSum", pay, vals), n2, 16 * n2 + 8 * ng)
     measure("group_len_150M", lambda: gpu.call("hgpuGroupLen", pay, vals), n2, 16 * ng)  # group starts in, lengths out
     dirs = gpu.vec(np.array([1, 1], bool), H_B)

@@ -18,6 +18,7 @@ import numpy as np
 
 H_B, H_J, H_H, H_I, H_L, H_F, H_E, H_X, H_C, H_Q, H_S = 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10
 H_M, H_D, H_Z, H_U, H_W, H_T, H_G, H_N, H_Y = 11, 12, 13, 14, 15, 16, 17, 18, 19
+H_A = 90
 
 DTYPE = {
     H_B: np.bool_, H_J: np.int8, H_H: np.int16, H_I: np.int32, H_L: np.int64,
@@ -98,6 +99,8 @@ class Builtins:
             L.hgpuIsDevice.restype = C.c_int32
             L.hgpuIsDevice.argtypes = [PV]
             L.hgpuLastError.restype = C.c_char_p
+        L.getSymbolStr.restype = C.c_char_p
+        L.getSymbolStr.argtypes = [C.c_longlong]
         L.initBackend()
         self._keep = []
 
@@ -192,6 +195,26 @@ class Builtins:
                 raise BuiltinError("hgpuToHost", rc, (self.lib.hgpuLastError() or b"").decode())
             return _read_host(h)
         return _read_host(v)
+
+
+def table_columns(lib, t):
+    """An H_A table node -> (column names, columns).  Numeric columns come back
+    as numpy arrays, symbols as lists of str, strings as lists of bytes."""
+    assert t.typ == H_A, t.typ
+    keys = V0.from_address(t.g)
+    vals = V0.from_address(t.g + 32)
+    names = [lib.lib.getSymbolStr(int(i)).decode() for i in np.atleast_1d(lib.to_py(keys))]
+    cols = []
+    for j in range(vals.len):
+        c = V0.from_address(vals.g + 32 * j)
+        if c.typ == H_Q:
+            cols.append([lib.lib.getSymbolStr(int(i)).decode() for i in lib.to_py(c)])
+        elif c.typ == H_S:
+            ptrs = [c.i64] if c.len == 1 else list((C.c_uint64 * c.len).from_address(c.g)) if c.len else []
+            cols.append([C.string_at(p) for p in ptrs])
+        else:
+            cols.append(lib.to_py(c))
+    return names, cols
 
 
 def _read_host(v):

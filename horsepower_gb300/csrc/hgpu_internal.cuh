@@ -73,6 +73,8 @@ struct ScratchScope {                          // rewinds the scratch arena on e
     ~ScratchScope();
 };
 bool is_device_ptr(const void* p);             // payload readable by kernels without staging
+bool host_readable(const void* p);             // payload readable by host code without a copy
+int residency();                               // HGPU_RESIDENT_DEVICE or HGPU_RESIDENT_HOST
 
 // ------------------------------------------------------------- value model
 inline bool is_int(I t) { return t == H_B || t == H_J || t == H_H || t == H_I || t == H_L; }

@@ -1,0 +1,1236 @@
+// Table ingest: the reference's binary table format (serializeV /
+// readSerializeV, h_io.cc:626-772) and its CSV reader (readCSV, loadCSV,
+// getField, loadItem; h_io.cc:50-188), with column payloads landing in HBM.
+//
+// Binary: payloads stream from the file through two pinned staging buffers;
+// the fread of one chunk overlaps the host-to-device copy of the previous.
+//
+// CSV: the whole file is copied to HBM once, then
+//   1. line ends: per-tile newline counts, a scan, an ordered scatter;
+//   2. one warp per line stages the line in shared memory, trims it as
+//      getField does, finds the separators with ballots and hands field j to
+//      lane j, which converts it with loadItem's function for its column's
+//      type (strtol semantics for atoi/atol, sscanf %d-%d-%d, first char);
+//   3. floats: decimal significand and exponent in one pass; Clinger's exact
+//      fast path (significand <= 2^53 and |exponent| <= 22: one correctly
+//      rounded IEEE operation on exact operands) covers decimals such as
+//      TPC-H's; every other input goes to a slow pass that decides the
+//      rounding exactly with big-integer arithmetic, so values equal glibc's
+//      correctly rounded strtod / strtof bit for bit;
+//   4. symbols: FNV-1a hashes, a first-occurrence table, the distinct texts
+//      interned on the host in first-occurrence order, ids mapped back on the
+//      GPU and every row's text checked against its representative's;
+//   5. strings: lengths scanned to offsets, texts and their pointers written
+//      straight into pinned host memory by the GPU.
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dev_common.cuh"
+#include "hgpu_internal.cuh"
+
+extern "C" {
+C LINE_SEP = '|';        // h_io.cc:9
+B LINE_HEADER = false;   // h_io.cc:11
+L LINE_MAX_CHAR = 1024;  // h_io.cc:8 (fgets buffer size)
+}
+
+namespace hg {
+
+I compact_rows(const uint8_t* mask, long long n, long long* out, long long* count);
+I scan_exclusive(const unsigned* in, long long n, unsigned long long* out, unsigned long long* total_h);
+I scan_counts(const unsigned* counts, long long n, unsigned long long* offs);
+
+namespace {
+
+// ------------------------------------------------------------------ staging
+constexpr size_t STAGE_BYTES = 32u << 20;
+struct Staging {
+    void* buf[2] = {nullptr, nullptr};
+    cudaEvent_t ev[2];
+    bool ready = false;
+};
+Staging g_stage;
+
+I stage_init() {
+    if (g_stage.ready) return 0;
+    for (int k = 0; k < 2; k++) {
+        HG_CU(cudaHostAlloc(&g_stage.buf[k], STAGE_BYTES, cudaHostAllocDefault));
+        HG_CU(cudaEventCreateWithFlags(&g_stage.ev[k], cudaEventDisableTiming));
+    }
+    g_stage.ready = true;
+    return 0;
+}
+
+I io_fail(const char* what) { return set_error(E_GENERAL, "%s", what); }
+
+// fp -> dst (device), `bytes` bytes, double-buffered
+I stream_in(FILE* fp, void* dst, size_t bytes) {
+    HG_CHECK(stage_init());
+    size_t done = 0;
+    int k = 0;
+    while (done < bytes) {
+        const size_t c = bytes - done < STAGE_BYTES ? bytes - done : STAGE_BYTES;
+        HG_CU(cudaEventSynchronize(g_stage.ev[k]));  // the copy out of this buffer has finished
+        if (fread(g_stage.buf[k], 1, c, fp) != c) {
+            cudaStreamSynchronize(g_stream);
+            return io_fail("fread: unexpected end of file");
+        }
+        HG_CU(cudaMemcpyAsync((char*)dst + done, g_stage.buf[k], c, cudaMemcpyHostToDevice, g_stream));
+        HG_CU(cudaEventRecord(g_stage.ev[k], g_stream));
+        done += c;
+        k ^= 1;
+    }
+    HG_CU(cudaStreamSynchronize(g_stream));
+    return 0;
+}
+
+// src (device) -> fp, double-buffered
+I stream_out(FILE* fp, const void* src, size_t bytes) {
+    HG_CHECK(stage_init());
+    const size_t nchunks = (bytes + STAGE_BYTES - 1) / STAGE_BYTES;
+    auto issue = [&](size_t j) -> I {
+        const size_t off = j * STAGE_BYTES, c = bytes - off < STAGE_BYTES ? bytes - off : STAGE_BYTES;
+        HG_CU(cudaMemcpyAsync(g_stage.buf[j & 1], (const char*)src + off, c, cudaMemcpyDeviceToHost, g_stream));
+        HG_CU(cudaEventRecord(g_stage.ev[j & 1], g_stream));
+        return 0;
+    };
+    if (nchunks) HG_CHECK(issue(0));
+    for (size_t j = 0; j < nchunks; j++) {
+        if (j + 1 < nchunks) HG_CHECK(issue(j + 1));
+        HG_CU(cudaEventSynchronize(g_stage.ev[j & 1]));
+        const size_t off = j * STAGE_BYTES, c = bytes - off < STAGE_BYTES ? bytes - off : STAGE_BYTES;
+        if (fwrite(g_stage.buf[j & 1], 1, c, fp) != c) {
+            cudaStreamSynchronize(g_stream);
+            return io_fail("fwrite failed");
+        }
+    }
+    return 0;
+}
+
+#define RD(p, n)                                                                              \
+    do {                                                                                      \
+        if ((n) > 0 && fread((p), 1, (size_t)(n), fp) != (size_t)(n)) return io_fail("fread: unexpected end of file"); \
+    } while (0)
+#define WR(p, n)                                                                              \
+    do {                                                                                      \
+        if ((n) > 0 && fwrite((p), 1, (size_t)(n), fp) != (size_t)(n)) return io_fail("fwrite failed"); \
+    } while (0)
+
+bool raw_payload(I t) { return is_real(t) || t == H_C || is_dtime(t) || t == H_X; }
+
+// An i64 payload (symbol ids) from host memory into a node of type typ.
+I put_words(V x, I typ, const std::vector<L>& w) {
+    x->typ = typ;
+    x->len = (L)w.size();
+    if (w.size() <= 1) {
+        x->g = (G)&x->b;
+        x->i64 = w.empty() ? 0 : w[0];
+        return 0;
+    }
+    void* d = dalloc(w.size() * 8);
+    if (!d) return E_DEVICE_OOM;
+    HG_CU(cudaMemcpyAsync(d, w.data(), w.size() * 8, cudaMemcpyHostToDevice, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));
+    x->g = (G)d;
+    return 0;
+}
+
+// ------------------------------------------------------- binary: read side
+I read_node(V x, FILE* fp) {
+    V0 hdr;
+    RD(&hdr, sizeof(V0));
+    const I typ = hdr.typ;
+    const L len = hdr.len;
+    if (len < 0) return set_error(E_GENERAL, "serialized node: negative length %lld", len);
+    if (raw_payload(typ)) {
+        const size_t nb = (size_t)getTypeSize(typ, len);
+        x->typ = typ;
+        x->len = len;
+        if (len <= 1) {  // inline, as initV leaves it (h_memory.cc:184-187)
+            x->i64 = hdr.i64;
+            x->g = (G)&x->b;
+            RD(&x->b, nb);
+            return 0;
+        }
+        void* d = dalloc(nb);
+        if (!d) return E_DEVICE_OOM;
+        x->g = (G)d;
+        return stream_in(fp, d, nb);
+    }
+    switch (typ) {
+    case H_Q: {  // readSerializeQ (h_io.cc:716-722): lengths, then NUL-terminated texts
+        std::vector<L> sz((size_t)len), ids((size_t)len);
+        RD(sz.data(), 8 * len);
+        std::string buf;
+        for (L i = 0; i < len; i++) {
+            if (sz[i] < 0) return set_error(E_GENERAL, "serialized symbol: negative length");
+            buf.assign((size_t)sz[i] + 1, '\0');
+            RD(&buf[0], sz[i] + 1);
+            ids[i] = getSymbol((S)buf.c_str());
+        }
+        return put_words(x, H_Q, ids);
+    }
+    case H_S: {  // readSerializeS (h_io.cc:724-729)
+        std::vector<L> sz((size_t)len);
+        RD(sz.data(), 8 * len);
+        S* ptrs = len <= 1 ? (S*)&x->b : (S*)halloc((size_t)len * sizeof(S));
+        if (!ptrs) return E_DEVICE_OOM;
+        for (L i = 0; i < len; i++) {
+            if (sz[i] < 0) return set_error(E_GENERAL, "serialized string: negative length");
+            S t = (S)halloc((size_t)sz[i] + 1);
+            if (!t) return E_DEVICE_OOM;
+            RD(t, sz[i] + 1);
+            ptrs[i] = t;
+        }
+        x->typ = H_S;
+        x->len = len;
+        x->g = (G)ptrs;
+        if (len == 0) x->g = (G)&x->b;
+        return 0;
+    }
+    case H_G: {  // readSerializeG (h_io.cc:731-733)
+        HG_CHECK(init_list(x, H_G, len));
+        V0* e = (V0*)x->g;
+        memset(e, 0, (size_t)(len > 0 ? len : 1) * sizeof(V0));
+        for (L i = 0; i < len; i++) HG_CHECK(read_node(e + i, fp));
+        return 0;
+    }
+    case H_A: {  // readSerializeA (h_io.cc:735-745): A0, keys, values
+        if (len != 2) return set_error(E_GENERAL, "serialized table: %lld nodes, not 2", len);
+        HG_CHECK(init_list(x, H_A, 2));
+        V0* e = (V0*)x->g;
+        memset(e, 0, 2 * sizeof(V0));
+        A a = (A)halloc(sizeof(A0));
+        if (!a) return E_DEVICE_OOM;
+        RD(a, sizeof(A0));
+        a->fkey = nullptr;  // a pointer of the writing process
+        x->a = a;
+        HG_CHECK(read_node(e + 0, fp));
+        HG_CHECK(read_node(e + 1, fp));
+        return 0;
+    }
+    default:
+        return set_error(E_NOT_IMPL, "serialized node of type %d", typ);  // EP in the reference
+    }
+}
+
+// ------------------------------------------------------ binary: write side
+I host_words(V x, std::vector<L>* w) {  // an 8-byte payload as host words
+    w->resize((size_t)x->len);
+    if (x->len == 0) return 0;
+    if (host_readable(x->g)) {
+        memcpy(w->data(), x->g, (size_t)x->len * 8);
+        return 0;
+    }
+    HG_CU(cudaMemcpyAsync(w->data(), x->g, (size_t)x->len * 8, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));
+    return 0;
+}
+
+I write_node(V x, FILE* fp) {
+    WR(x, sizeof(V0));
+    const I typ = x->typ;
+    const L len = x->len;
+    if (raw_payload(typ)) {  // serializeBasic (h_io.cc:640-643)
+        const size_t nb = (size_t)esize(typ) * (size_t)len;
+        if (nb > 0) {
+            if (host_readable(x->g)) WR(x->g, nb);
+            else HG_CHECK(stream_out(fp, x->g, nb));
+        }
+        if (typ == H_C) {
+            const char nul = 0;
+            WR(&nul, 1);
+        }
+        return 0;
+    }
+    switch (typ) {
+    case H_Q: {  // serializeQ (h_io.cc:645-648)
+        std::vector<L> ids;
+        HG_CHECK(host_words(x, &ids));
+        for (L id : ids) {
+            const L n = (L)strlen(getSymbolStr(id));
+            WR(&n, 8);
+        }
+        for (L id : ids) {
+            S s = getSymbolStr(id);
+            WR(s, strlen(s) + 1);
+        }
+        return 0;
+    }
+    case H_S: {  // serializeS (h_io.cc:650-654)
+        std::vector<L> w;
+        HG_CHECK(host_words(x, &w));
+        for (L p : w) {
+            const L n = (L)strlen((S)p);
+            WR(&n, 8);
+        }
+        for (L p : w) WR((S)p, strlen((S)p) + 1);
+        return 0;
+    }
+    case H_G: {  // serializeG (h_io.cc:656-658)
+        V0* e = host_nodes(x);
+        for (L i = 0; i < len; i++) HG_CHECK(write_node(e + i, fp));
+        return 0;
+    }
+    case H_A: {  // serializeA (h_io.cc:660-668)
+        A0 a{};
+        if (x->a) a = *x->a;
+        a.fkey = nullptr;
+        WR(&a, sizeof(A0));
+        V0* e = host_nodes(x);
+        HG_CHECK(write_node(e + 0, fp));
+        HG_CHECK(write_node(e + 1, fp));
+        return 0;
+    }
+    default:
+        return set_error(E_NOT_IMPL, "serializing a node of type %d", typ);  // EP in the reference
+    }
+}
+
+// ====================================================================== CSV
+constexpr int NL_TILE = 1 << 16;   // bytes per newline-count tile
+constexpr int NL_THREADS = 256;    // 256 bytes per thread per tile
+constexpr int CSV_WARPS = 8;       // lines per block (one warp each)
+constexpr int CSV_MAXLINE = 4096;  // largest LINE_MAX_CHAR accepted (shared memory per warp)
+constexpr int CSV_MAXCOLS = 256;
+
+enum : unsigned {
+    CSV_FIELDS = 1u,     // a line with another number of fields than columns
+    CSV_LONG = 2u,       // a line longer than LINE_MAX_CHAR - 1 (fgets would split it)
+    CSV_NUL = 4u,        // a NUL byte inside a line
+    CSV_DATE = 8u,       // a date field sscanf cannot read completely
+    CSV_HEXNAN = 16u,    // hexadecimal float or nan(...) payload: not accepted
+    CSV_SLOWFULL = 32u,  // more slow-path floats than the slow list holds
+};
+
+// newlines in the PER bytes of one thread (16-byte loads when the segment is whole)
+constexpr int NL_PER = NL_TILE / NL_THREADS;
+__device__ __forceinline__ unsigned nl_in_word(unsigned w) { return __popc(__vcmpeq4(w, 0x0a0a0a0au)) >> 3; }
+__device__ unsigned nl_count_seg(const char* __restrict__ buf, long long n, long long t0) {
+    unsigned c = 0;
+    if (t0 + NL_PER <= n) {
+        const uint4* p = (const uint4*)(buf + t0);
+#pragma unroll 4
+        for (int k = 0; k < NL_PER / 16; k++) {
+            const uint4 v = p[k];
+            c += nl_in_word(v.x) + nl_in_word(v.y) + nl_in_word(v.z) + nl_in_word(v.w);
+        }
+    } else {
+        for (long long i = t0; i < n && i < t0 + NL_PER; i++) c += buf[i] == '\n';
+    }
+    return c;
+}
+__global__ void k_nl_count(const char* __restrict__ buf, long long n, unsigned* __restrict__ counts) {
+    const long long t0 = (long long)blockIdx.x * NL_TILE + (long long)threadIdx.x * NL_PER;
+    unsigned c = nl_count_seg(buf, n, t0);
+    c = __reduce_add_sync(0xffffffffu, c);
+    __shared__ unsigned ws[NL_THREADS / 32];
+    if (lane_id() == 0) ws[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned t = 0;
+        for (int w = 0; w < NL_THREADS / 32; w++) t += ws[w];
+        counts[blockIdx.x] = t;
+    }
+}
+
+// positions of the newlines of each tile, in order (offs: exclusive tile prefix)
+__global__ void k_nl_scatter(const char* __restrict__ buf, long long n, const unsigned long long* __restrict__ offs,
+                             long long* __restrict__ pos) {
+    const long long t0 = (long long)blockIdx.x * NL_TILE + (long long)threadIdx.x * NL_PER;
+    const unsigned c = nl_count_seg(buf, n, t0);
+    // exclusive prefix of c over the block (thread order = byte order)
+    const unsigned incl = warp_incl_scan(c);
+    __shared__ unsigned ws[NL_THREADS / 32];
+    if (lane_id() == 31) ws[threadIdx.x >> 5] = incl;
+    __syncthreads();
+    unsigned before = 0;
+    for (unsigned w = 0; w < (threadIdx.x >> 5); w++) before += ws[w];
+    unsigned long long o = offs[blockIdx.x] + before + (incl - c);
+    if (c == 0) return;
+    for (long long i = t0; i < n && i < t0 + NL_PER; i++)
+        if (buf[i] == '\n') pos[o++] = i;
+}
+
+struct CsvCol {
+    int typ;
+    void* out;                 // column payload (device), or the span array for symbols and strings
+};
+struct CsvArgs {
+    const char* buf;
+    long long size;            // file bytes
+    const long long* nl;       // newline positions
+    long long nnl;
+    long long first_line;      // 1 when the first line is a header
+    long long rows;
+    int ncols;
+    char sep;
+    int maxline;               // LINE_MAX_CHAR
+    int lstride;               // shared-memory bytes per line (maxline rounded up to 16)
+    const CsvCol* cols;
+    unsigned* err;             // [0] codes, [1] first bad row (atomicMin)
+    unsigned long long* slow;  // (span, row << 16 | col) pairs of floats for the slow pass
+    unsigned* nslow;
+    unsigned slow_cap;
+};
+
+__device__ __forceinline__ unsigned row32(long long r) { return r < 0xffffffffll ? (unsigned)r : 0xfffffffeu; }
+__device__ __forceinline__ bool c_space(unsigned char c) { return c == ' ' || (c >= '\t' && c <= '\r'); }
+__device__ __forceinline__ bool c_digit(unsigned char c) { return c >= '0' && c <= '9'; }
+__device__ __forceinline__ bool c_skip(unsigned char c) { return c == ' ' || c == '\r' || c == '\n'; }
+
+// strtol(s, NULL, 10): whitespace, sign, decimal digits; clamps to the long range
+__device__ long long dev_strtol(const char* p, int n, int* end = nullptr) {
+    int i = 0;
+    while (i < n && c_space(p[i])) i++;
+    bool neg = false;
+    if (i < n && (p[i] == '+' || p[i] == '-')) { neg = p[i] == '-'; i++; }
+    const unsigned long long lim = neg ? 9223372036854775808ull : 9223372036854775807ull;
+    unsigned long long acc = 0;
+    bool ovf = false, any = false;
+    for (; i < n && c_digit(p[i]); i++) {
+        const unsigned d = p[i] - '0';
+        any = true;
+        if (!ovf) {
+            if (acc > (lim - d) / 10) ovf = true;
+            else acc = acc * 10 + d;
+        }
+    }
+    if (end) *end = any ? i : -1;
+    if (ovf) return neg ? LLONG_MIN : LLONG_MAX;
+    return neg ? (long long)(0ull - acc) : (long long)acc;
+}
+
+// one %d of sscanf: whitespace, sign, at least one digit; stored as int
+__device__ bool scan_int(const char* p, int n, int* pos, int* v) {
+    int end;
+    long long x = dev_strtol(p + *pos, n - *pos, &end);
+    if (end < 0) return false;
+    *pos += end;
+    *v = (int)(unsigned)(unsigned long long)x;
+    return true;
+}
+
+// strtod front end: sign, up to 19 significant digits in w, decimal exponent
+struct Dec {
+    unsigned long long w;
+    long long e10;
+    bool neg, trunc;
+    int kind;  // 0 number, 1 inf, 2 nan, 3 no conversion, 4 unsupported (hex, nan payload)
+};
+__device__ __forceinline__ unsigned char lower(unsigned char c) { return (c >= 'A' && c <= 'Z') ? c + 32 : c; }
+__device__ bool match_word(const char* p, int n, int i, const char* w) {
+    for (int k = 0; w[k]; k++)
+        if (i + k >= n || lower(p[i + k]) != (unsigned char)w[k]) return false;
+    return true;
+}
+__device__ Dec parse_dec(const char* p, int n) {
+    Dec d{0ull, 0, false, false, 3};
+    int i = 0;
+    while (i < n && c_space(p[i])) i++;
+    if (i < n && (p[i] == '+' || p[i] == '-')) { d.neg = p[i] == '-'; i++; }
+    if (match_word(p, n, i, "inf")) { d.kind = 1; return d; }
+    if (match_word(p, n, i, "nan")) { d.kind = (i + 3 < n && p[i + 3] == '(') ? 4 : 2; return d; }
+    if (i + 1 < n && p[i] == '0' && (p[i + 1] == 'x' || p[i + 1] == 'X')) {
+        const int j = i + 2;
+        const bool hex = j < n && (c_digit(p[j]) || (lower(p[j]) >= 'a' && lower(p[j]) <= 'f') ||
+                                   (p[j] == '.' && j + 1 < n && (c_digit(p[j + 1]) || (lower(p[j + 1]) >= 'a' && lower(p[j + 1]) <= 'f'))));
+        if (hex) { d.kind = 4; return d; }
+    }
+    int nd = 0;
+    long long eadj = 0;
+    bool any = false;
+    for (; i < n && c_digit(p[i]); i++) {
+        any = true;
+        const unsigned v = p[i] - '0';
+        if (d.w == 0 && v == 0) continue;
+        if (nd < 19) { d.w = d.w * 10 + v; nd++; }
+        else { eadj++; if (v) d.trunc = true; }
+    }
+    if (i < n && p[i] == '.') {
+        i++;
+        for (; i < n && c_digit(p[i]); i++) {
+            any = true;
+            const unsigned v = p[i] - '0';
+            if (d.w == 0 && v == 0) { eadj--; continue; }
+            if (nd < 19) { d.w = d.w * 10 + v; nd++; eadj--; }
+            else if (v) d.trunc = true;
+        }
+    }
+    if (!any) return d;  // no conversion: 0.0
+    d.kind = 0;
+    if (i < n && (p[i] == 'e' || p[i] == 'E')) {
+        int j = i + 1;
+        bool eneg = false;
+        if (j < n && (p[j] == '+' || p[j] == '-')) { eneg = p[j] == '-'; j++; }
+        if (j < n && c_digit(p[j])) {
+            long long ex = 0;
+            for (; j < n && c_digit(p[j]); j++) ex = ex < 100000000 ? ex * 10 + (p[j] - '0') : ex;
+            eadj += eneg ? -ex : ex;
+        }
+    }
+    d.e10 = eadj;
+    return d;
+}
+
+__device__ __forceinline__ double pow10_exact(int k) {  // 10^k for 0 <= k <= 22, exact in binary64
+    double r = 1.0;
+    for (int j = 0; j < k; j++) r *= 10.0;
+    return r;
+}
+__device__ __forceinline__ float pow10f_exact(int k) {  // 10^k for 0 <= k <= 10, exact in binary32
+    float r = 1.0f;
+    for (int j = 0; j < k; j++) r *= 10.0f;
+    return r;
+}
+
+// Clinger's fast path for doubles: true and *out when exact
+__device__ bool fast_f64(const Dec& d, double* out) {
+    if (d.kind == 1) { *out = d.neg ? -__longlong_as_double(0x7ff0000000000000ll) : __longlong_as_double(0x7ff0000000000000ll); return true; }
+    if (d.kind == 2) { *out = __longlong_as_double(d.neg ? (long long)0xfff8000000000000ull : 0x7ff8000000000000ll); return true; }
+    if (d.kind == 3) { *out = 0.0; return true; }
+    if (d.w == 0) { *out = d.neg ? -0.0 : 0.0; return true; }
+    if (d.trunc || d.w > (1ull << 53) || d.e10 < -22 || d.e10 > 22) return false;
+    const double w = (double)d.w;
+    double r = d.e10 >= 0 ? __dmul_rn(w, pow10_exact((int)d.e10)) : __ddiv_rn(w, pow10_exact((int)-d.e10));
+    *out = d.neg ? -r : r;
+    return true;
+}
+__device__ bool fast_f32(const Dec& d, float* out) {
+    if (d.kind == 1) { *out = __int_as_float(d.neg ? (int)0xff800000u : 0x7f800000); return true; }
+    if (d.kind == 2) { *out = __int_as_float(d.neg ? (int)0xffc00000u : 0x7fc00000); return true; }
+    if (d.kind == 3) { *out = 0.0f; return true; }
+    if (d.w == 0) { *out = d.neg ? -0.0f : 0.0f; return true; }
+    if (d.trunc) return false;
+    if (d.w <= (1ull << 24) && d.e10 >= -10 && d.e10 <= 10) {
+        const float w = (float)d.w;
+        float r = d.e10 >= 0 ? __fmul_rn(w, pow10f_exact((int)d.e10)) : __fdiv_rn(w, pow10f_exact((int)-d.e10));
+        *out = d.neg ? -r : r;
+        return true;
+    }
+    // exact double, then one rounding to float unless the double is a float midpoint
+    double x;
+    if (!fast_f64(d, &x)) return false;
+    const float f = __double2float_rn(x);
+    if (isinf(f) && !isinf(x)) return false;  // next to the overflow threshold: decide exactly
+    if ((double)f != x) {
+        const float g = nextafterf(f, (double)f < x ? INFINITY : -INFINITY);
+        if (isfinite(g) && __dadd_rn((double)f, (double)g) * 0.5 == x) return false;
+    }
+    *out = f;
+    return true;
+}
+
+// One warp per line.
+__global__ void __launch_bounds__(CSV_WARPS * 32) k_csv_parse(CsvArgs a) {
+    extern __shared__ char csv_smem[];
+    const int warp = threadIdx.x >> 5, lane = lane_id();
+    char* line = csv_smem + (size_t)warp * (a.lstride + CSV_MAXCOLS * 4);
+    int* seps = (int*)(line + a.lstride);
+    for (long long r = (long long)blockIdx.x * CSV_WARPS + warp; r < a.rows; r += (long long)gridDim.x * CSV_WARPS) {
+        const long long li = r + a.first_line;
+        const long long s = li == 0 ? 0 : a.nl[li - 1] + 1;
+        const bool has_nl = li < a.nnl;
+        const long long e = has_nl ? a.nl[li] : a.size;
+        const long long len = e - s;
+        if (len + (has_nl ? 1 : 0) > a.maxline - 1) {
+            if (lane == 0) { atomicOr(a.err, CSV_LONG); atomicMin(a.err + 1, row32(r)); }
+            continue;
+        }
+        bool nul = false;
+        for (int k = lane; k < len; k += 32) {
+            const char c = a.buf[s + k];
+            line[k] = c;
+            nul |= c == 0;
+        }
+        __syncwarp();
+        if (__any_sync(0xffffffffu, nul)) {
+            if (lane == 0) { atomicOr(a.err, CSV_NUL); atomicMin(a.err + 1, row32(r)); }
+            continue;
+        }
+        // trim(line): leading ' ', trailing ' ', '\r', '\n' (h_io.cc:190-204)
+        int ls = 0, le = (int)len;
+        if (lane == 0) {
+            while (ls < le && line[ls] == ' ') ls++;
+            while (le > ls && c_skip((unsigned char)line[le - 1])) le--;
+        }
+        ls = __shfl_sync(0xffffffffu, ls, 0);
+        le = __shfl_sync(0xffffffffu, le, 0);
+        // separators, in order (getField, h_io.cc:126-143)
+        int nsep = 0;
+        for (int b = ls; b < le; b += 32) {
+            const int k = b + lane;
+            const bool is = k < le && line[k] == a.sep;
+            const unsigned m = __ballot_sync(0xffffffffu, is);
+            const int idx = nsep + __popc(m & ((1u << lane) - 1u));
+            if (is && idx < a.ncols) seps[idx] = k;
+            nsep += __popc(m);
+        }
+        __syncwarp();
+        const int loaded = a.sep == ' ' ? nsep + 1 : nsep;
+        if (loaded != a.ncols) {
+            if (lane == 0) { atomicOr(a.err, CSV_FIELDS); atomicMin(a.err + 1, row32(r)); }
+            continue;
+        }
+        for (int j = lane; j < a.ncols; j += 32) {
+            int fb = j == 0 ? ls : seps[j - 1] + 1;
+            int fe = j < nsep ? seps[j] : le;
+            // trimSelf(tmp): leading ' ', trailing ' ', '\r', '\n'
+            while (fb < fe && line[fb] == ' ') fb++;
+            while (fe > fb && c_skip((unsigned char)line[fe - 1])) fe--;
+            const char* f = line + fb;
+            const int n = fe - fb;
+            const CsvCol c = a.cols[j];
+            switch (c.typ) {
+            case H_B: ((bool*)c.out)[r] = (int)(unsigned)(unsigned long long)dev_strtol(f, n) != 0; break;
+            case H_J: ((int8_t*)c.out)[r] = (int8_t)(int)(unsigned)(unsigned long long)dev_strtol(f, n); break;
+            case H_H: ((int16_t*)c.out)[r] = (int16_t)(int)(unsigned)(unsigned long long)dev_strtol(f, n); break;
+            case H_I: ((int32_t*)c.out)[r] = (int32_t)(unsigned)(unsigned long long)dev_strtol(f, n); break;
+            case H_L: ((long long*)c.out)[r] = dev_strtol(f, n); break;
+            case H_C: ((char*)c.out)[r] = n > 0 ? f[0] : 0; break;
+            case H_D: {  // sscanf(s, "%d-%d-%d") -> a*10000 + b*100 + c
+                int pos = 0, y, m, dd;
+                bool ok = scan_int(f, n, &pos, &y) && pos < n && f[pos] == '-' && (pos++, scan_int(f, n, &pos, &m)) &&
+                          pos < n && f[pos] == '-' && (pos++, scan_int(f, n, &pos, &dd));
+                if (!ok) { atomicOr(a.err, CSV_DATE); atomicMin(a.err + 1, row32(r)); break; }
+                ((int32_t*)c.out)[r] = (int32_t)((unsigned)y * 10000u + (unsigned)m * 100u + (unsigned)dd);
+                break;
+            }
+            case H_E:
+            case H_F: {
+                const Dec d = parse_dec(f, n);
+                if (d.kind == 4) { atomicOr(a.err, CSV_HEXNAN); atomicMin(a.err + 1, row32(r)); break; }
+                bool done;
+                if (c.typ == H_E) { double v; done = fast_f64(d, &v); if (done) ((double*)c.out)[r] = v; }
+                else { float v; done = fast_f32(d, &v); if (done) ((float*)c.out)[r] = v; }
+                if (!done) {
+                    const unsigned k = atomicAdd(a.nslow, 1u);
+                    if (k < a.slow_cap) {
+                        a.slow[2 * k] = ((unsigned long long)(s + fb) << 16) | (unsigned long long)n;
+                        a.slow[2 * k + 1] = ((unsigned long long)r << 16) | (unsigned long long)j;
+                    } else {
+                        atomicOr(a.err, CSV_SLOWFULL);
+                    }
+                }
+                break;
+            }
+            default:  // H_Q, H_S: the field's span for the symbol and string passes
+                ((unsigned long long*)c.out)[r] = ((unsigned long long)(s + fb) << 16) | (unsigned long long)n;
+                break;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------- exact decimal conversion
+// Big unsigned integers of up to BIG_LIMBS 32-bit limbs, little endian.  A
+// decimal of up to 800 significant digits (more only add a sticky bit: a
+// binary64 midpoint has at most 767 significant digits, so digits beyond the
+// 800th cannot move the value across one) scaled by 2^s or 10^k fits 4096 bits.
+constexpr int BIG_LIMBS = 128;
+constexpr int MAX_SIG = 800;
+struct Big {
+    unsigned v[BIG_LIMBS];
+    int n;  // limbs in use (v[n-1] != 0 unless n == 0)
+};
+__device__ void big_set(Big& b, unsigned long long x) {
+    b.n = 0;
+    while (x) { b.v[b.n++] = (unsigned)x; x >>= 32; }
+}
+__device__ void big_mul_small(Big& b, unsigned m) {
+    unsigned long long carry = 0;
+    for (int i = 0; i < b.n; i++) {
+        const unsigned long long t = (unsigned long long)b.v[i] * m + carry;
+        b.v[i] = (unsigned)t;
+        carry = t >> 32;
+    }
+    if (carry && b.n < BIG_LIMBS) b.v[b.n++] = (unsigned)carry;
+}
+__device__ void big_add_small(Big& b, unsigned a) {
+    unsigned long long carry = a;
+    for (int i = 0; i < b.n && carry; i++) {
+        const unsigned long long t = (unsigned long long)b.v[i] + carry;
+        b.v[i] = (unsigned)t;
+        carry = t >> 32;
+    }
+    if (carry && b.n < BIG_LIMBS) b.v[b.n++] = (unsigned)carry;
+}
+__device__ void big_mul_pow10(Big& b, int k) {
+    while (k >= 9) { big_mul_small(b, 1000000000u); k -= 9; }
+    unsigned m = 1;
+    while (k-- > 0) m *= 10;
+    if (m != 1) big_mul_small(b, m);
+}
+__device__ int big_bitlen(const Big& b) { return b.n == 0 ? 0 : 32 * (b.n - 1) + (32 - __clz(b.v[b.n - 1])); }
+__device__ void big_shl(Big& b, int s) {
+    if (b.n == 0 || s == 0) return;
+    const int w = s >> 5, r = s & 31;
+    int nn = b.n + w + 1;
+    if (nn > BIG_LIMBS) nn = BIG_LIMBS;
+    for (int i = nn - 1; i >= 0; i--) {
+        const int j = i - w;
+        unsigned hi = (j >= 0 && j < b.n) ? b.v[j] : 0u;
+        unsigned lo = (j - 1 >= 0 && j - 1 < b.n) ? b.v[j - 1] : 0u;
+        b.v[i] = r ? (hi << r) | (lo >> (32 - r)) : hi;
+    }
+    b.n = nn;
+    while (b.n > 0 && b.v[b.n - 1] == 0) b.n--;
+}
+__device__ void big_shr1(Big& b) {
+    for (int i = 0; i < b.n; i++) b.v[i] = (b.v[i] >> 1) | (i + 1 < b.n ? b.v[i + 1] << 31 : 0u);
+    while (b.n > 0 && b.v[b.n - 1] == 0) b.n--;
+}
+__device__ int big_cmp(const Big& a, const Big& b) {
+    if (a.n != b.n) return a.n < b.n ? -1 : 1;
+    for (int i = a.n - 1; i >= 0; i--)
+        if (a.v[i] != b.v[i]) return a.v[i] < b.v[i] ? -1 : 1;
+    return 0;
+}
+__device__ void big_sub(Big& a, const Big& b) {  // a -= b, a >= b
+    long long borrow = 0;
+    for (int i = 0; i < a.n; i++) {
+        long long t = (long long)a.v[i] - (i < b.n ? (long long)b.v[i] : 0) - borrow;
+        borrow = t < 0;
+        a.v[i] = (unsigned)(t + (borrow << 32));
+    }
+    while (a.n > 0 && a.v[a.n - 1] == 0) a.n--;
+}
+__device__ bool big_low_bits_nonzero(const Big& b, int k) {  // any of bits [0, k)
+    for (int i = 0; i < b.n && 32 * i < k; i++) {
+        const int take = k - 32 * i;
+        const unsigned m = take >= 32 ? 0xffffffffu : ((1u << take) - 1u);
+        if (b.v[i] & m) return true;
+    }
+    return false;
+}
+__device__ unsigned long long big_bits(const Big& b, int lo, int cnt) {  // bits [lo, lo + cnt), cnt <= 64
+    unsigned long long r = 0;
+    for (int k = 0; k < cnt; k++) {
+        const int bit = lo + k, i = bit >> 5;
+        if (i < b.n && ((b.v[i] >> (bit & 31)) & 1u)) r |= 1ull << k;
+    }
+    return r;
+}
+
+// value = m * 2^u, m < 2^(p+1) already rounded to p bits (or fewer when subnormal)
+__device__ unsigned long long encode(unsigned long long m, int u, int p, int bias, bool* inf) {
+    *inf = false;
+    if (m == 0) return 0;
+    const int top = 63 - __clzll(m), lead = top + u;  // exponent of the leading bit
+    if (lead > bias) { *inf = true; return 0; }
+    if (lead < 1 - bias) return m;  // subnormal: u is the subnormal unit, m < 2^(p-1)
+    if (top < p - 1) m <<= (p - 1 - top);  // leading bit to the implicit position
+    const unsigned long long frac = m & ((1ull << (p - 1)) - 1ull);
+    return ((unsigned long long)(lead + bias) << (p - 1)) | frac;
+}
+
+// Correctly rounded binary64 (p = 53) or binary32 (p = 24) value of the
+// decimal text, returned as its bit pattern (round to nearest, ties to even).
+__device__ unsigned long long exact_decimal(const char* p_, int n, int p, Big& D, Big& A, Big& T) {
+    const int bias = p == 53 ? 1023 : 127, emin = 1 - bias;
+    const unsigned long long sign_bit = p == 53 ? (1ull << 63) : (1ull << 31);
+    const unsigned long long inf_bits = p == 53 ? 0x7ff0000000000000ull : 0x7f800000ull;
+    int i = 0;
+    while (i < n && c_space(p_[i])) i++;
+    bool neg = false;
+    if (i < n && (p_[i] == '+' || p_[i] == '-')) { neg = p_[i] == '-'; i++; }
+    const unsigned long long sgn = neg ? sign_bit : 0ull;
+    // digits into D (in 9-digit chunks), exponent, sticky
+    big_set(D, 0);
+    int nd = 0;
+    long long e10 = 0;
+    bool trunc = false;
+    unsigned chunk = 0;
+    int cl = 0;
+    auto push = [&](unsigned v) {
+        chunk = chunk * 10 + v;
+        if (++cl == 9) { big_mul_small(D, 1000000000u); big_add_small(D, chunk); chunk = 0; cl = 0; }
+    };
+    for (; i < n && c_digit(p_[i]); i++) {
+        const unsigned v = p_[i] - '0';
+        if (nd == 0 && v == 0) continue;
+        if (nd < MAX_SIG) { push(v); nd++; }
+        else { e10++; if (v) trunc = true; }
+    }
+    if (i < n && p_[i] == '.') {
+        i++;
+        for (; i < n && c_digit(p_[i]); i++) {
+            const unsigned v = p_[i] - '0';
+            if (nd == 0 && v == 0) { e10--; continue; }
+            if (nd < MAX_SIG) { push(v); nd++; e10--; }
+            else if (v) trunc = true;
+        }
+    }
+    if (cl) {
+        unsigned m = 1;
+        for (int k = 0; k < cl; k++) m *= 10;
+        big_mul_small(D, m);
+        big_add_small(D, chunk);
+    }
+    if (i < n && (p_[i] == 'e' || p_[i] == 'E')) {
+        int j = i + 1;
+        bool eneg = false;
+        if (j < n && (p_[j] == '+' || p_[j] == '-')) { eneg = p_[j] == '-'; j++; }
+        if (j < n && c_digit(p_[j])) {
+            long long ex = 0;
+            for (; j < n && c_digit(p_[j]); j++) ex = ex < 100000000 ? ex * 10 + (p_[j] - '0') : ex;
+            e10 += eneg ? -ex : ex;
+        }
+    }
+    if (nd == 0) return sgn;  // zero
+    const long long dexp = nd + e10;  // value in [10^(dexp-1), 10^dexp)
+    if (dexp > (p == 53 ? 310 : 40)) return sgn | inf_bits;
+    if (dexp < (p == 53 ? -324 : -46)) return sgn;
+    bool inf;
+    unsigned long long bits;
+    if (e10 >= 0) {
+        big_mul_pow10(D, (int)e10);
+        const int L = big_bitlen(D);
+        if (L <= p) {  // exact integer (no truncated digits possible here)
+            bits = encode(big_bits(D, 0, L), 0, p, bias, &inf);
+        } else {
+            const int sh = L - p - 1;
+            const unsigned long long q = big_bits(D, sh, p + 1);
+            const bool sticky = trunc || big_low_bits_nonzero(D, sh);
+            unsigned long long m = q >> 1;
+            if ((q & 1ull) && (sticky || (m & 1ull))) m++;
+            int u = sh + 1;
+            if (m == (1ull << p)) { m >>= 1; u++; }
+            bits = encode(m, u, p, bias, &inf);
+        }
+        return inf ? (sgn | inf_bits) : (sgn | bits);
+    }
+    // value = D / 10^k: q = floor(D * 2^s / 10^k) with p + 1 bits (fewer when subnormal)
+    const int k = (int)-e10;
+    const int smax = p - emin;  // result unit 2^(1 - s) never below the subnormal unit
+    big_set(T, 1);
+    big_mul_pow10(T, k);  // T = 10^k
+    const int bq = big_bitlen(T);
+    int s = p + bq - big_bitlen(D);
+    if (s > smax) s = smax;
+    unsigned long long q = 0;
+    for (int attempt = 0; attempt < 3; attempt++) {
+        // A = D * 2^max(s,0); T' = 10^k * 2^max(-s,0) * 2^(p+2)
+        A = D;
+        if (s > 0) big_shl(A, s);
+        big_set(T, 1);
+        big_mul_pow10(T, k);
+        if (s < 0) big_shl(T, -s);
+        big_shl(T, p + 2);
+        q = 0;
+        for (int b = p + 2; b >= 0; b--) {
+            if (big_cmp(A, T) >= 0) { big_sub(A, T); q |= 1ull << b; }
+            big_shr1(T);
+        }
+        if (s < smax && q < (1ull << p)) { s++; continue; }
+        if (q >= (1ull << (p + 1))) { s--; continue; }
+        break;
+    }
+    const bool sticky = trunc || A.n != 0;
+    unsigned long long m = q >> 1;
+    if ((q & 1ull) && (sticky || (m & 1ull))) m++;
+    int u = 1 - s;
+    if (m == (1ull << p)) { m >>= 1; u++; }
+    bits = encode(m, u, p, bias, &inf);
+    return inf ? (sgn | inf_bits) : (sgn | bits);
+}
+
+__global__ void k_csv_slow(const char* __restrict__ buf, const unsigned long long* __restrict__ slow, unsigned nslow,
+                           const CsvCol* __restrict__ cols, Big* __restrict__ work) {
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < nslow; t += gridDim.x * blockDim.x) {
+        const unsigned long long span = slow[2 * t], meta = slow[2 * t + 1];
+        const char* f = buf + (span >> 16);
+        const int n = (int)(span & 0xffffull);
+        const long long r = (long long)(meta >> 16);
+        const int j = (int)(meta & 0xffffull);
+        const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
+        Big* w = work + 3ull * g;
+        if (cols[j].typ == H_E) ((unsigned long long*)cols[j].out)[r] = exact_decimal(f, n, 53, w[0], w[1], w[2]);
+        else ((unsigned*)cols[j].out)[r] = (unsigned)exact_decimal(f, n, 24, w[0], w[1], w[2]);
+    }
+}
+
+// ---------------------------------------------------------- symbols, strings
+__device__ __forceinline__ unsigned long long span_hash(const char* buf, unsigned long long span) {
+    // FNV-1a, 64-bit
+    const char* f = buf + (span >> 16);
+    const int n = (int)(span & 0xffffull);
+    unsigned long long h = 0xcbf29ce484222325ull;
+    for (int k = 0; k < n; k++) h = (h ^ (unsigned char)f[k]) * 0x100000001b3ull;
+    return h == ~0ull ? h - 1 : h;
+}
+// first-occurrence table: key = text hash, value = smallest row
+__global__ void k_sym_insert(const char* __restrict__ buf, const unsigned long long* __restrict__ spans, long long rows,
+                             unsigned long long* __restrict__ keys, unsigned long long* __restrict__ first,
+                             unsigned long long mask, unsigned* derr) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < rows; r += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long h = span_hash(buf, spans[r]);
+        unsigned long long sl = (h * 0x9e3779b97f4a7c15ull) >> 20 & mask;
+        for (unsigned long long p = 0; p <= mask; p++) {
+            const unsigned long long cur = atomicCAS(keys + sl, ~0ull, h);
+            if (cur == ~0ull || cur == h) { atomicMin(first + sl, (unsigned long long)r); break; }
+            sl = (sl + 1) & mask;
+            if (p == mask) atomicOr(derr, DERR_CAPACITY);
+        }
+    }
+}
+__global__ void k_sym_rep(const char* __restrict__ buf, const unsigned long long* __restrict__ spans, long long rows,
+                          const unsigned long long* __restrict__ keys, const unsigned long long* __restrict__ first,
+                          unsigned long long mask, long long* __restrict__ rep, uint8_t* __restrict__ is_first) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < rows; r += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long h = span_hash(buf, spans[r]);
+        unsigned long long sl = (h * 0x9e3779b97f4a7c15ull) >> 20 & mask;
+        long long f = r;
+        for (unsigned long long p = 0; p <= mask; p++) {
+            if (keys[sl] == h) { f = (long long)first[sl]; break; }
+            sl = (sl + 1) & mask;
+        }
+        rep[r] = f;
+        is_first[r] = f == r;
+    }
+}
+// distinct texts, NUL-terminated, packed at offs[k] (pinned host blob)
+__global__ void k_sym_pack(const char* __restrict__ buf, const unsigned long long* __restrict__ spans,
+                           const long long* __restrict__ drows, long long nd, const unsigned long long* __restrict__ offs,
+                           char* __restrict__ blob, unsigned* __restrict__ dpos) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nd; k += (long long)gridDim.x * blockDim.x) {
+        const long long r = drows[k];
+        const unsigned long long sp = spans[r];
+        const char* f = buf + (sp >> 16);
+        const int n = (int)(sp & 0xffffull);
+        char* o = blob + offs[k];
+        for (int i = 0; i < n; i++) o[i] = f[i];
+        o[n] = 0;
+        dpos[r] = (unsigned)k;
+    }
+}
+__global__ void k_sym_lengths(const unsigned long long* __restrict__ spans, const long long* __restrict__ drows, long long nd,
+                              unsigned* __restrict__ lens) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nd; k += (long long)gridDim.x * blockDim.x)
+        lens[k] = (unsigned)(spans[drows[k]] & 0xffffull) + 1u;
+}
+// ids per row, and the row's text checked against its representative's
+__global__ void k_sym_ids(const char* __restrict__ buf, const unsigned long long* __restrict__ spans, long long rows,
+                          const long long* __restrict__ rep, const unsigned* __restrict__ dpos,
+                          const long long* __restrict__ ids, long long* __restrict__ out, unsigned* __restrict__ bad) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < rows; r += (long long)gridDim.x * blockDim.x) {
+        const long long f = rep[r];
+        out[r] = ids[dpos[f]];
+        if (f != r) {
+            const unsigned long long a = spans[r], b = spans[f];
+            bool same = (a & 0xffffull) == (b & 0xffffull);
+            const char *pa = buf + (a >> 16), *pb = buf + (b >> 16);
+            for (int i = 0; same && i < (int)(a & 0xffffull); i++) same = pa[i] == pb[i];
+            if (!same) atomicOr(bad, 1u);
+        }
+    }
+}
+__global__ void k_str_lengths(const unsigned long long* __restrict__ spans, long long rows, unsigned* __restrict__ lens) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < rows; r += (long long)gridDim.x * blockDim.x)
+        lens[r] = (unsigned)(spans[r] & 0xffffull) + 1u;
+}
+// texts and their pointers written into pinned host memory
+__global__ void k_str_pack(const char* __restrict__ buf, const unsigned long long* __restrict__ spans, long long rows,
+                           const unsigned long long* __restrict__ offs, char* blob, char** ptrs) {
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < rows; r += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long sp = spans[r];
+        const char* f = buf + (sp >> 16);
+        const int n = (int)(sp & 0xffffull);
+        char* o = blob + offs[r];
+        for (int i = 0; i < n; i++) o[i] = f[i];
+        o[n] = 0;
+        ptrs[r] = o;
+    }
+}
+
+unsigned grid_of(long long n) {
+    unsigned g = grid_for(n, 256);
+    return g > (unsigned)g_sms * 16 ? (unsigned)g_sms * 16 : g;
+}
+
+I csv_symbols(const char* dbuf, const unsigned long long* spans, long long rows, long long* out) {
+    unsigned long long cap = 1024;
+    while (cap < 2ull * (unsigned long long)rows) cap <<= 1;
+    unsigned long long* keys = (unsigned long long*)salloc(cap * 8);
+    unsigned long long* first = (unsigned long long*)salloc(cap * 8);
+    long long* rep = (long long*)salloc((size_t)rows * 8);
+    uint8_t* isf = (uint8_t*)salloc((size_t)rows);
+    long long* drows = (long long*)salloc((size_t)rows * 8);
+    unsigned* dpos = (unsigned*)salloc((size_t)rows * 4);
+    unsigned* bad = (unsigned*)salloc(16);
+    if (!keys || !first || !rep || !isf || !drows || !dpos || !bad) return E_DEVICE_OOM;
+    HG_CU(cudaMemsetAsync(keys, 0xff, cap * 8, g_stream));
+    HG_CU(cudaMemsetAsync(first, 0xff, cap * 8, g_stream));
+    HG_CU(cudaMemsetAsync(bad, 0, 4, g_stream));
+    HG_LAUNCH("sym_insert", grid_of(rows), 256, 0, k_sym_insert, dbuf, spans, rows, keys, first, cap - 1, g_derr);
+    HG_LAUNCH("sym_rep", grid_of(rows), 256, 0, k_sym_rep, dbuf, spans, rows, keys, first, cap - 1, rep, isf);
+    HG_CHECK(last_launch_error());
+    long long nd = 0;
+    HG_CHECK(compact_rows(isf, rows, drows, &nd));
+    unsigned* lens = (unsigned*)salloc((size_t)(nd > 0 ? nd : 1) * 4);
+    unsigned long long* offs = (unsigned long long*)salloc((size_t)(nd + 1) * 8);
+    if (!lens || !offs) return E_DEVICE_OOM;
+    unsigned long long total = 0;
+    if (nd > 0) {
+        HG_LAUNCH("sym_lengths", grid_of(nd), 256, 0, k_sym_lengths, spans, drows, nd, lens);
+        HG_CHECK(scan_exclusive(lens, nd, offs, &total));
+    }
+    char* blob = (char*)halloc(total > 0 ? total : 1);
+    if (!blob) return E_DEVICE_OOM;
+    if (nd > 0) HG_LAUNCH("sym_pack", grid_of(nd), 256, 0, k_sym_pack, dbuf, spans, drows, nd, offs, blob, dpos);
+    std::vector<unsigned long long> hoffs((size_t)nd);
+    if (nd > 0) HG_CU(cudaMemcpyAsync(hoffs.data(), offs, (size_t)nd * 8, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CHECK(last_launch_error());
+    // interning in first-occurrence order, as loadItem's getSymbol calls meet the texts
+    std::vector<L> ids((size_t)nd);
+    for (long long k = 0; k < nd; k++) ids[k] = getSymbol(blob + hoffs[k]);
+    long long* dids = (long long*)salloc((size_t)(nd > 0 ? nd : 1) * 8);
+    if (!dids) return E_DEVICE_OOM;
+    if (nd > 0) HG_CU(cudaMemcpyAsync(dids, ids.data(), (size_t)nd * 8, cudaMemcpyHostToDevice, g_stream));
+    HG_LAUNCH("sym_ids", grid_of(rows), 256, 0, k_sym_ids, dbuf, spans, rows, rep, dpos, dids, out, bad);
+    unsigned hb = 0;
+    HG_CU(cudaMemcpyAsync(&hb, bad, 4, cudaMemcpyDeviceToHost, g_stream));
+    HG_CHECK(check_device_errors());
+    if (hb) return set_error(E_GENERAL, "readCSV: two symbol texts share a 64-bit hash");
+    return 0;
+}
+
+I csv_strings(const char* dbuf, const unsigned long long* spans, long long rows, S** ptrs_out) {
+    unsigned* lens = (unsigned*)salloc((size_t)rows * 4);
+    unsigned long long* offs = (unsigned long long*)salloc((size_t)(rows + 1) * 8);
+    if (!lens || !offs) return E_DEVICE_OOM;
+    HG_LAUNCH("str_lengths", grid_of(rows), 256, 0, k_str_lengths, spans, rows, lens);
+    unsigned long long total = 0;
+    HG_CHECK(scan_exclusive(lens, rows, offs, &total));
+    char* blob = (char*)halloc(total > 0 ? total : 1);
+    S* ptrs = (S*)halloc((size_t)rows * sizeof(S));
+    if (!blob || !ptrs) return E_DEVICE_OOM;
+    HG_LAUNCH("str_pack", grid_of(rows), 256, 0, k_str_pack, dbuf, spans, rows, offs, blob, ptrs);
+    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CHECK(last_launch_error());
+    *ptrs_out = ptrs;
+    return 0;
+}
+
+I read_csv(V z, S fileName, L numCols, L* types, Q* symList) {
+    if (numCols <= 0 || numCols > CSV_MAXCOLS) return set_error(E_NOT_IMPL, "readCSV: %lld columns", numCols);
+    if (LINE_MAX_CHAR < 2 || LINE_MAX_CHAR > CSV_MAXLINE)
+        return set_error(E_NOT_IMPL, "readCSV: LINE_MAX_CHAR %lld outside [2, %d]", LINE_MAX_CHAR, CSV_MAXLINE);
+    for (L j = 0; j < numCols; j++) {
+        const I t = (I)types[j];
+        if (!(t == H_B || t == H_J || t == H_H || t == H_I || t == H_L || t == H_F || t == H_E || t == H_C || t == H_Q ||
+              t == H_S || t == H_D))
+            return set_error(E_NOT_IMPL, "readCSV: column %lld of type %d (loadItem has no conversion)", j, t);
+    }
+    FILE* fp = fopen(fileName, "rb");
+    if (!fp) return set_error(E_GENERAL, "readCSV: cannot open %s", fileName);
+    fseek(fp, 0, SEEK_END);
+    const long long size = ftell(fp);
+    fseek(fp, 0, SEEK_SET);
+    if (size < 0) { fclose(fp); return io_fail("readCSV: cannot size the file"); }
+    char* dbuf = (char*)salloc((size_t)size + 64);
+    if (!dbuf) { fclose(fp); return E_DEVICE_OOM; }
+    I e = stream_in(fp, dbuf, (size_t)size);
+    fclose(fp);
+    if (e) return e;
+    // newline positions
+    const long long ntiles = (size + NL_TILE - 1) / NL_TILE;
+    unsigned* counts = (unsigned*)salloc((size_t)(ntiles > 0 ? ntiles : 1) * 4);
+    unsigned long long* toffs = (unsigned long long*)salloc((size_t)(ntiles + 1) * 8);
+    if (!counts || !toffs) return E_DEVICE_OOM;
+    long long nnl = 0;
+    long long* nl = nullptr;
+    if (ntiles > 0) {
+        HG_LAUNCH("csv_nl_count", (unsigned)ntiles, NL_THREADS, 0, k_nl_count, dbuf, size, counts);
+        HG_CHECK(scan_counts(counts, ntiles, toffs));
+        unsigned long long h = 0;
+        HG_CU(cudaMemcpyAsync(&h, toffs + ntiles, 8, cudaMemcpyDeviceToHost, g_stream));
+        HG_CU(cudaStreamSynchronize(g_stream));
+        nnl = (long long)h;
+        nl = (long long*)salloc((size_t)(nnl > 0 ? nnl : 1) * 8);
+        if (!nl) return E_DEVICE_OOM;
+        HG_LAUNCH("csv_nl_scatter", (unsigned)ntiles, NL_THREADS, 0, k_nl_scatter, dbuf, size, toffs, nl);
+        HG_CHECK(last_launch_error());
+    }
+    char last = '\n';
+    if (size > 0) HG_CU(cudaMemcpy(&last, dbuf + size - 1, 1, cudaMemcpyDeviceToHost));
+    const long long lines = nnl + (size > 0 && last != '\n' ? 1 : 0);
+    const long long first_line = (LINE_HEADER && lines > 0) ? 1 : 0;
+    const long long rows = lines - first_line;
+    // columns
+    std::vector<CsvCol> hc((size_t)numCols);
+    std::vector<void*> spans((size_t)numCols, nullptr);
+    for (L j = 0; j < numCols; j++) {
+        const I t = (I)types[j];
+        const size_t es = (t == H_Q || t == H_S) ? 8 : (size_t)esize(t);
+        void* d = (t == H_Q || t == H_S) ? salloc((size_t)(rows > 0 ? rows : 1) * 8)
+                                         : dalloc((size_t)(rows > 1 ? rows : 2) * es + (t == H_C ? 1 : 0));
+        if (!d) return E_DEVICE_OOM;
+        hc[j].typ = t;
+        hc[j].out = d;
+        if (t == H_Q || t == H_S) spans[j] = d;
+    }
+    CsvCol* dcols = (CsvCol*)salloc(sizeof(CsvCol) * (size_t)numCols);
+    unsigned* err = (unsigned*)salloc(16);
+    const unsigned slow_cap = 1u << 22;
+    unsigned long long* slow = (unsigned long long*)salloc((size_t)slow_cap * 16);
+    unsigned* nslow = (unsigned*)salloc(16);
+    if (!dcols || !err || !slow || !nslow) return E_DEVICE_OOM;
+    HG_CU(cudaMemcpyAsync(dcols, hc.data(), sizeof(CsvCol) * (size_t)numCols, cudaMemcpyHostToDevice, g_stream));
+    const unsigned init_err[2] = {0u, 0xffffffffu};
+    HG_CU(cudaMemcpyAsync(err, init_err, 8, cudaMemcpyHostToDevice, g_stream));
+    HG_CU(cudaMemsetAsync(nslow, 0, 4, g_stream));
+    if (rows > 0) {
+        const int lstride = (int)((LINE_MAX_CHAR + 15) & ~15LL);
+        CsvArgs a{dbuf, size, nl, nnl, first_line, rows, (int)numCols, (char)LINE_SEP, (int)LINE_MAX_CHAR, lstride, dcols,
+                  err, slow, nslow, slow_cap};
+        const size_t smem = (size_t)CSV_WARPS * ((size_t)lstride + CSV_MAXCOLS * 4);
+        HG_CU(cudaFuncSetAttribute(k_csv_parse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        long long blocks = (rows + CSV_WARPS - 1) / CSV_WARPS;
+        if (blocks > (long long)g_sms * 32) blocks = (long long)g_sms * 32;
+        HG_LAUNCH("csv_parse", (unsigned)blocks, CSV_WARPS * 32, smem, k_csv_parse, a);
+        HG_CHECK(last_launch_error());
+    }
+    unsigned herr[2], hslow = 0;
+    HG_CU(cudaMemcpyAsync(herr, err, 8, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaMemcpyAsync(&hslow, nslow, 4, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));
+    if (herr[0]) {
+        const long long line = (long long)herr[1] + first_line + 1;
+        const char* why = (herr[0] & CSV_FIELDS)   ? "a line whose field count differs from the column count"
+                          : (herr[0] & CSV_LONG)   ? "a line longer than LINE_MAX_CHAR - 1 characters"
+                          : (herr[0] & CSV_NUL)    ? "a NUL byte"
+                          : (herr[0] & CSV_DATE)   ? "a date that %d-%d-%d cannot read"
+                          : (herr[0] & CSV_HEXNAN) ? "a hexadecimal float or a nan(...) payload"
+                                                   : "too many long decimals";
+        return set_error(herr[0] & (CSV_HEXNAN | CSV_SLOWFULL) ? E_NOT_IMPL : E_GENERAL, "readCSV: %s (line %lld)", why, line);
+    }
+    if (hslow > 0) {
+        const unsigned want = hslow < 65536u ? hslow : 65536u, blocks = (want + 127) / 128;
+        Big* work = (Big*)salloc((size_t)blocks * 128 * 3 * sizeof(Big));  // three per launched thread
+        if (!work) return E_DEVICE_OOM;
+        HG_LAUNCH("csv_slow", blocks, 128, 0, k_csv_slow, dbuf, slow, hslow, dcols, work);
+        HG_CHECK(last_launch_error());
+    }
+    // symbols and strings
+    std::vector<V0> colv((size_t)numCols);
+    for (L j = 0; j < numCols; j++) {
+        const I t = (I)types[j];
+        V0& c = colv[j];
+        memset(&c, 0, sizeof(V0));
+        c.typ = t;
+        c.len = rows;
+        if (t == H_Q) {
+            long long* ids = (long long*)dalloc((size_t)(rows > 1 ? rows : 2) * 8);
+            if (!ids) return E_DEVICE_OOM;
+            if (rows > 0) HG_CHECK(csv_symbols(dbuf, (const unsigned long long*)spans[j], rows, ids));
+            c.g = (G)ids;
+        } else if (t == H_S) {
+            S* ptrs = nullptr;
+            if (rows > 0) HG_CHECK(csv_strings(dbuf, (const unsigned long long*)spans[j], rows, &ptrs));
+            c.g = (G)ptrs;
+        } else {
+            c.g = (G)hc[j].out;
+        }
+        if (rows <= 1) {  // length-0/1 vectors are inline (initV)
+            uint64_t bits = 0;
+            if (rows == 1) {
+                if (t == H_S) bits = (uint64_t)(uintptr_t)((S*)c.g)[0];
+                else HG_CU(cudaMemcpy(&bits, c.g, (size_t)esize(t), cudaMemcpyDeviceToHost));
+            }
+            c.i64 = (L)bits;
+            c.g = (G)&c.b;
+        }
+    }
+    HG_CHECK(check_device_errors());
+    // the table: A0 {rows, cols}, keys = symList, values = the columns (allocTable, h_memory.cc:168-172)
+    HG_CHECK(init_list(z, H_A, 2));
+    V0* e2 = (V0*)z->g;
+    memset(e2, 0, 2 * sizeof(V0));
+    A hdr = (A)halloc(sizeof(A0));
+    if (!hdr) return E_DEVICE_OOM;
+    hdr->row = rows;
+    hdr->col = numCols;
+    hdr->fkey = nullptr;
+    z->a = hdr;
+    V0& keys = e2[0];
+    keys.typ = H_Q;
+    keys.len = numCols;
+    if (numCols == 1) { keys.g = (G)&keys.b; keys.i64 = symList[0]; }
+    else {
+        L* kp = (L*)halloc((size_t)numCols * 8);
+        if (!kp) return E_DEVICE_OOM;
+        memcpy(kp, symList, (size_t)numCols * 8);
+        keys.g = (G)kp;
+    }
+    HG_CHECK(init_list(&e2[1], H_G, numCols));
+    V0* cols = (V0*)e2[1].g;
+    for (L j = 0; j < numCols; j++) {
+        cols[j] = colv[j];
+        if (colv[j].len <= 1) cols[j].g = (G)&cols[j].b;
+    }
+    return apply_residency(z);
+}
+
+}  // namespace
+}  // namespace hg
+
+using namespace hg;
+
+extern "C" {
+
+I hgpuReadSerialized(V x, FILE* fp) {
+    HG_CHECK(ensure_init());
+    if (!x || !fp) return E_DOMAIN;
+    const long long mark = out_mark();
+    I e = read_node(x, fp);
+    if (!e) e = apply_residency(x);
+    if (e) out_rewind(mark);
+    return e;
+}
+
+I hgpuWriteSerialized(V x, FILE* fp) {
+    HG_CHECK(ensure_init());
+    if (!x || !fp) return E_DOMAIN;
+    return write_node(x, fp);
+}
+
+I hgpuReadCSV(V z, S fileName, L numCols, L* types, Q* symList) {
+    HG_CHECK(ensure_init());
+    if (!z || !fileName || !types || !symList) return E_DOMAIN;
+    ScratchScope ss;
+    const long long mark = out_mark();
+    I e = read_csv(z, fileName, numCols, types, symList);
+    if (e) out_rewind(mark);
+    return e;
+}
+
+void serializeV(V x, FILE* fp) {
+    if (hgpuWriteSerialized(x, fp)) {
+        fprintf(stderr, "[ERROR] serializeV: %s\n", hgpuLastError());
+        exit(1);
+    }
+}
+
+void readSerializeV(V x, FILE* fp) {
+    if (hgpuReadSerialized(x, fp)) {
+        fprintf(stderr, "[ERROR] readSerializeV: %s\n", hgpuLastError());
+        exit(1);
+    }
+}
+
+V readCSV(S fileName, L numCols, L* types, Q* symList) {
+    V z = allocNode();
+    if (!z || hgpuReadCSV(z, fileName, numCols, types, symList)) {
+        fprintf(stderr, "[ERROR] readCSV: %s\n", hgpuLastError());
+        exit(99);
+    }
+    return z;
+}
+
+}  // extern "C"

@@ -217,6 +217,19 @@ bool is_device_ptr(const void* p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged || a.type == cudaMemoryTypeHost;
 }
 
+// memory the host can read directly (pinned arena, other pinned or pageable memory)
+bool host_readable(const void* p) {
+    if (!p || g_host->contains(p)) return true;
+    if (g_out->contains(p) || g_scratch->contains(p)) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return true;
+    }
+    return a.type != cudaMemoryTypeDevice;
+}
+int residency() { return g_residency; }
+
 int esize(I t) {
     switch (t) {
     case H_B: case H_J: case H_C: return 1;
@@ -295,11 +308,12 @@ I init_list(V z, I typ, L n) {
 V0* host_nodes(V x) { return (V0*)x->g; }
 
 static I to_host_rec(V z, V x, bool in_place) {
-    if (x->typ == H_G || x->typ == H_N) {
+    if (x->typ == H_G || x->typ == H_N || x->typ == H_A) {
         V0* src = (V0*)x->g;
         if (!in_place) {
             V0 hdr = *x;
             HG_CHECK(init_list(z, hdr.typ, hdr.len));
+            if (hdr.typ == H_A) z->a = hdr.a;  // the table header is host memory already
             for (L i = 0; i < hdr.len; i++) HG_CHECK(to_host_rec((V0*)z->g + i, src + i, false));
         } else {
             for (L i = 0; i < x->len; i++) HG_CHECK(to_host_rec(src + i, src + i, true));
@@ -536,9 +550,10 @@ I hgpuToHost(V z, V x) {
 }
 
 static I to_device_rec(V z, V x) {
-    if (x->typ == H_G || x->typ == H_N) {
+    if (x->typ == H_G || x->typ == H_N || x->typ == H_A) {
         V0 hdr = *x;
         HG_CHECK(init_list(z, hdr.typ, hdr.len));
+        if (hdr.typ == H_A) z->a = hdr.a;
         for (L i = 0; i < hdr.len; i++) HG_CHECK(to_device_rec((V0*)z->g + i, (V0*)hdr.g + i));
         return 0;
     }

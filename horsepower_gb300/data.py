@@ -67,3 +67,122 @@ def group_table(n=150_000_000, nranks=10_000_000, seed=2, chunk=10_000_000):
     payload = rng.uniform(0.0, 1e5, n)
     sec = rng.integers(0, 2 ** 20 + 1, n).astype(np.int32)
     return dict(key=key, payload=payload, sec=sec)
+
+
+# ----------------------------------------------------------------- CSV text
+# The reference loads lineitem from '|'-separated text with a trailing '|'
+# (backend/load_db.cc:111-129: i32 x4, f64 x4, char x2, date x3, sym x2, str).
+LINEITEM_TYPES = [3, 3, 3, 3, 6, 6, 6, 6, 8, 8, 12, 12, 12, 9, 9, 10]
+LINEITEM_NAMES = ["l_orderkey", "l_partkey", "l_suppkey", "l_linenumber", "l_quantity", "l_extendedprice",
+                  "l_discount", "l_tax", "l_returnflag", "l_linestatus", "l_shipdate", "l_commitdate",
+                  "l_receiptdate", "l_shipinstruct", "l_shipmode", "l_comment"]
+_INSTRUCT = ["DELIVER IN PERSON", "COLLECT COD", "NONE", "TAKE BACK RETURN"]
+_MODES = ["REG AIR", "AIR", "RAIL", "SHIP", "TRUCK", "MAIL", "FOB"]
+
+
+def _digits(m, col, width, values):
+    """Right-aligned decimal digits of non-negative ints, left padding spaces."""
+    v = values.astype(np.int64).copy()
+    for k in range(width - 1, -1, -1):
+        d = (v % 10).astype(np.uint8) + 48
+        m[:, col + k] = np.where((v > 0) | (k == width - 1), d, 32)
+        v //= 10
+
+
+def _text(m, col, width, choices, idx):
+    """Left-aligned texts from `choices`, right padding spaces."""
+    tab = np.full((len(choices), width), 32, np.uint8)
+    for i, c in enumerate(choices):
+        tab[i, :len(c)] = np.frombuffer(c.encode(), np.uint8)
+    m[:, col:col + width] = tab[idx]
+
+
+def lineitem_csv(rows, seed=7):
+    """(text bytes, expected columns) of a lineitem-shaped table in the
+    reference's .tbl layout, fields space-padded to fixed widths (the reader
+    trims them).  Expected values are what strtod / atoi / the date rule give
+    for each field: prices are cents / 100.0, which is the correctly rounded
+    double of the two-decimal text."""
+    rng = np.random.default_rng(seed)
+    orderkey = (np.arange(rows, dtype=np.int64) // 4) * 4 + 1
+    partkey = rng.integers(1, 200_001, rows)
+    suppkey = rng.integers(1, 10_001, rows)
+    linenum = rng.integers(1, 8, rows)
+    qty = rng.integers(1, 51, rows)
+    cents = qty * rng.integers(90_000, 210_001, rows)  # retail price $900-$2100 per unit
+    disc = rng.integers(0, 11, rows)
+    tax = rng.integers(0, 9, rows)
+    flag = rng.integers(0, 3, rows)
+    status = rng.integers(0, 2, rows)
+    dates = [(rng.integers(1992, 1999, rows), rng.integers(1, 13, rows), rng.integers(1, 29, rows)) for _ in range(3)]
+    ins = rng.integers(0, len(_INSTRUCT), rows)
+    mode = rng.integers(0, len(_MODES), rows)
+    clen = rng.integers(10, 44, rows)
+    widths = [9, 7, 6, 1, 5, 9, 4, 4, 1, 1, 10, 10, 10, 17, 7, 43]
+    W = sum(widths) + len(widths) + 1
+    m = np.empty((rows, W), np.uint8)
+    col = 0
+
+    def sep():
+        nonlocal col
+        m[:, col] = ord("|")
+        col += 1
+
+    for vals, w in [(orderkey, 9), (partkey, 7), (suppkey, 6), (linenum, 1)]:
+        _digits(m, col, w, vals)
+        col += w
+        sep()
+    for units, hundredths, w in [(qty, np.zeros(rows, np.int64), 5), (cents // 100, cents % 100, 9),
+                                 (np.zeros(rows, np.int64), disc, 4), (np.zeros(rows, np.int64), tax, 4)]:
+        _digits(m, col, w - 3, units)
+        m[:, col + w - 3] = ord(".")
+        m[:, col + w - 2] = (hundredths // 10).astype(np.uint8) + 48
+        m[:, col + w - 1] = (hundredths % 10).astype(np.uint8) + 48
+        col += w
+        sep()
+    m[:, col] = np.frombuffer(b"ANR", np.uint8)[flag]
+    col += 1
+    sep()
+    m[:, col] = np.frombuffer(b"OF", np.uint8)[status]
+    col += 1
+    sep()
+    for y, mo, d in dates:
+        for k, (v, w) in enumerate([(y, 4), (mo, 2), (d, 2)]):
+            for j in range(w - 1, -1, -1):
+                m[:, col + j] = (v % 10).astype(np.uint8) + 48
+                v = v // 10
+            col += w
+            if k < 2:
+                m[:, col] = ord("-")
+                col += 1
+        sep()
+    _text(m, col, 17, _INSTRUCT, ins)
+    col += 17
+    sep()
+    _text(m, col, 7, _MODES, mode)
+    col += 7
+    sep()
+    letters = rng.integers(97, 123, (rows, 43)).astype(np.uint8)
+    letters[rng.random((rows, 43)) < 0.15] = 32
+    letters[:, 0] = rng.integers(97, 123, rows)
+    pos = np.arange(43)[None, :]
+    letters[pos == (clen - 1)[:, None]] = 120  # a letter ends each comment
+    letters[pos >= clen[:, None]] = 32
+    m[:, col:col + 43] = letters
+    col += 43
+    sep()
+    m[:, col] = ord("\n")
+    text = m.tobytes()
+    comments = [bytes(r[:n]) for r, n in zip(letters, clen)] if rows <= 2_000_000 else None
+    exp = {
+        "l_orderkey": orderkey.astype(np.int32), "l_partkey": partkey.astype(np.int32),
+        "l_suppkey": suppkey.astype(np.int32), "l_linenumber": linenum.astype(np.int32),
+        "l_quantity": qty.astype(np.float64), "l_extendedprice": cents / 100.0,
+        "l_discount": disc / 100.0, "l_tax": tax / 100.0,
+        "l_returnflag": np.frombuffer(b"ANR", np.uint8)[flag].astype(np.int8),
+        "l_linestatus": np.frombuffer(b"OF", np.uint8)[status].astype(np.int8),
+        "l_shipinstruct": ins, "l_shipmode": mode, "l_comment": comments,
+    }
+    for name, (y, mo, d) in zip(["l_shipdate", "l_commitdate", "l_receiptdate"], dates):
+        exp[name] = (y * 10000 + mo * 100 + d).astype(np.int32)
+    return text, exp

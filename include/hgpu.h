@@ -31,6 +31,7 @@
 
 #include <stdint.h>
 #include <stddef.h>
+#include <stdio.h>
 #ifndef __cplusplus
 #include <stdbool.h>
 #endif
@@ -57,7 +58,11 @@ typedef struct { F real, imag; } X;
  * h_memory.cc:184-194). */
 struct hgpu_enum_s { Q source; G ek, ev; };
 typedef struct hgpu_enum_s Y0, *Y;
-struct hgpu_table_s;  /* reference A0 (common.h:25); tables are outside the path */
+/* Table header: the reference's A0 (common.h:21): row and column counts and
+ * its foreign-key list (always NULL here).  An H_A node holds it in `a` and
+ * its two nodes {keys (symbols), values (list of columns)} in `g`. */
+struct hgpu_table_s { L row, col; void *fkey; };
+typedef struct hgpu_table_s A0, *A;
 
 /* Value node: field order and union members of src/horseir/v3/backend/common.h:31-55.
  * sizeof(V0) == 32 on LP64. */
@@ -346,6 +351,37 @@ E    hgpuGetTuning(I knob);
  * on the GPU race, so issue them on one stream.  The first call on a device
  * looks up the array's address; make it before any stream capture. */
 I    hgpuSumF64Static(const double *x, L n, double *result, void *stream);
+
+/* ---------------- ingest: binary tables and CSV (h_io.cc) ----------------
+ * The reference's table loaders with column payloads landing in HBM (or in
+ * pinned host memory under HGPU_RESIDENT_HOST).
+ *
+ * Binary format (serializeV / readSerializeV, h_io.cc:626-772): each node is
+ * its 32-byte V0 followed by its payload; basic vectors as raw elements (char
+ * vectors with a trailing NUL), symbols and strings as len(x) i64 lengths
+ * then NUL-terminated texts, lists and tables as their nodes in order (a
+ * table writes its 24-byte A0 first).  Files written by either library read
+ * back in the other.  Payloads stream through pinned staging buffers, the
+ * file read of one chunk overlapping the host-to-device copy of the last.
+ *
+ * CSV (readCSV / loadCSV / getField / loadItem, h_io.cc:50-188): the file is
+ * copied to HBM once; lines, fields and every column are parsed on the GPU
+ * with the reference's conversions (atoi, atol, strtof, strtod bit-exact,
+ * including the slow decimal cases; %d-%d-%d dates as yyyymmdd; first
+ * character; symbols interned in first-occurrence order; strings copied to
+ * pinned host memory).  LINE_SEP / LINE_HEADER / LINE_MAX_CHAR are the
+ * reference's format globals (h_io.cc:8-11). */
+I    hgpuWriteSerialized(V x, FILE *fp);   /* serializeV, h_io.cc:672-697 */
+I    hgpuReadSerialized(V x, FILE *fp);    /* readSerializeV, h_io.cc:748-772 */
+I    hgpuReadCSV(V z, S fileName, L numCols, L *types, Q *symList);  /* readCSV, h_io.cc:50-71 */
+/* The reference's own entry points: like its EP, they print the error and
+ * exit the process when the load fails. */
+void serializeV(V x, FILE *fp);
+void readSerializeV(V x, FILE *fp);
+V    readCSV(S fileName, L numCols, L *types, Q *symList);
+extern C LINE_SEP;                         /* field separator, '|' (h_io.cc:9) */
+extern B LINE_HEADER;                      /* true: the first line is skipped (h_io.cc:11) */
+extern L LINE_MAX_CHAR;                    /* fgets buffer: lines of up to LINE_MAX_CHAR-1 characters (h_io.cc:8) */
 
 #ifdef __cplusplus
 }

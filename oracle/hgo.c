@@ -83,13 +83,35 @@ V initV(V x, I typ, L len) {
 }
 
 /* ---------------------------------------------------------------- symbols */
-/* Interning table standing in for h_symbol.cc:146-241 (ids are table slots). */
-static char *hgo_syms[4096];
-static L hgo_nsyms = 0;
+/* Interning table standing in for h_symbol.cc:146-241: ids are assigned in
+ * order of first appearance; an open-addressed hash of the texts finds them. */
+static char **hgo_syms = NULL;
+static L hgo_nsyms = 0, hgo_symcap = 0;
+static L *hgo_symtab = NULL, hgo_symtab_n = 0;  /* slots hold id + 1, 0 = empty */
+static uint64_t sym_hash(const char *s) { uint64_t h = 1469598103934665603ULL; while (*s) h = (h ^ (unsigned char)*s++) * 1099511628211ULL; R h; }
+static void sym_rehash(L n) {
+    free(hgo_symtab);
+    hgo_symtab_n = n;
+    hgo_symtab = (L *)calloc((size_t)n, sizeof(L));
+    for (L i = 0; i < hgo_nsyms; i++) {
+        L k = (L)(sym_hash(hgo_syms[i]) & (uint64_t)(n - 1));
+        while (hgo_symtab[k]) k = (k + 1) & (n - 1);
+        hgo_symtab[k] = i + 1;
+    }
+}
 L getSymbol(S name) {
-    for (L i = 0; i < hgo_nsyms; i++) if (!strcmp(hgo_syms[i], name)) R i;
-    if (hgo_nsyms >= 4096) R -1;
+    if (2 * (hgo_nsyms + 1) > hgo_symtab_n) sym_rehash(hgo_symtab_n ? 2 * hgo_symtab_n : 1024);
+    L k = (L)(sym_hash(name) & (uint64_t)(hgo_symtab_n - 1));
+    while (hgo_symtab[k]) {
+        if (!strcmp(hgo_syms[hgo_symtab[k] - 1], name)) R hgo_symtab[k] - 1;
+        k = (k + 1) & (hgo_symtab_n - 1);
+    }
+    if (hgo_nsyms == hgo_symcap) {
+        hgo_symcap = hgo_symcap ? 2 * hgo_symcap : 1024;
+        hgo_syms = (char **)realloc(hgo_syms, (size_t)hgo_symcap * sizeof(char *));
+    }
     hgo_syms[hgo_nsyms] = strdup(name);
+    hgo_symtab[k] = hgo_nsyms + 1;
     R hgo_nsyms++;
 }
 S getSymbolStr(L x) { R (x >= 0 && x < hgo_nsyms) ? hgo_syms[x] : (S) ""; }

@@ -57,6 +57,11 @@ B    hgo_is_ordered(V x);  /* isOrdered: h_system.cc:678-698 */
 I    hgo_copyV(V z, V x);  /* copyV: h_system.cc:70-73 */
 void hgo_swap2(V z);       /* swap2: h_system.cc:47-56 */
 
+/* hgo_io.c: readCSV / serializeV / readSerializeV restated (h_io.cc) */
+I    hgoReadCSV(V z, S fileName, L numCols, L *types, Q *symList);
+I    hgoWriteSerialized(V x, FILE *fp);
+I    hgoReadSerialized(V x, FILE *fp);
+
 /* hgo_sort.c */
 L    hgo_cmp_item(V t, L a, L b, B *isUp);   /* lib_quicksort_cmp_item: h_libs.cc:455-488 */
 L    hgo_cmp_list(V val, L a, L b, B *isUp); /* lib_quicksort_cmp:      h_libs.cc:448-453 */
