@@ -544,6 +544,128 @@ def run_builtins(args):
     }
 
 
+def run_ingest(args):
+    """readCSV of a 6,001,215-row lineitem-shaped .tbl (the reference's
+    load_db.cc lineitem schema) from the page cache into HBM, and the same
+    table through readSerializeV.  Text GB/s and rows/s end to end (file
+    read, host-to-device copy, parse, symbols, strings), the kernels' split,
+    and the oracle's readCSV (the reference's serial fgets/strtod loop) on a
+    bounded sample of the same file."""
+    import tempfile
+    import horsepower_gb300
+    from horsepower_gb300.abi import table_columns  # noqa: F401
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    from ingest_run import Ingest
+    gpu = horsepower_gb300.load()
+    Lb = gpu.lib
+    Lb.hgpuTimerStop.restype = C.c_double
+    Lb.getHeapOffset.restype = C.c_longlong
+    Lb.setHeapOffset.argtypes = [C.c_longlong]
+    Lb.hgpuProfileRead.restype = C.c_int32
+    Lb.hgpuProfileRead.argtypes = [C.c_int32, C.POINTER(C.c_char_p), C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+    hbm, src = peaks()
+    rows = args.ingest_rows
+    text, _ = D.lineitem_csv(rows, seed=9)
+    tmp = tempfile.mkdtemp(prefix="hgpu_ingest_")
+    path = os.path.join(tmp, "lineitem.tbl")
+    with open(path, "wb") as f:
+        f.write(text)
+    nbytes = len(text)
+    del text
+    ing = Ingest(gpu)
+    clocks = Clocks()
+
+    def one():
+        m = Lb.getHeapOffset()
+        Lb.hgpuSync()
+        t0 = time.perf_counter()
+        rc, t = ing.csv(path, D.LINEITEM_TYPES, D.LINEITEM_NAMES)
+        Lb.hgpuSync()
+        dt = time.perf_counter() - t0
+        if rc:
+            raise RuntimeError(Lb.hgpuLastError())
+        return dt, m, t
+
+    for _ in range(max(1, args.warmup)):
+        _, m, _ = one()
+        Lb.setHeapOffset(m)
+    clocks.start()
+    ts = []
+    for _ in range(args.steps):
+        dt, m, _ = one()
+        ts.append(dt)
+        Lb.setHeapOffset(m)
+    clk = clocks.stop()
+    Lb.hgpuProfileReset()
+    Lb.hgpuProfile(1)
+    _, m, t = one()
+    Lb.hgpuProfile(0)
+    names, tot, cnt = (C.c_char_p * 64)(), (C.c_double * 64)(), (C.c_longlong * 64)()
+    nk = Lb.hgpuProfileRead(64, names, tot, cnt)
+    kern = sorted(((names[i].decode(), tot[i], int(cnt[i])) for i in range(min(nk, 64))), key=lambda k: -k[1])
+    # the binary format of the same table
+    binp = os.path.join(tmp, "lineitem.bin")
+    assert ing.save(binp, t) == 0
+    bsize = os.path.getsize(binp)
+    Lb.setHeapOffset(m)
+    bts = []
+    for k in range(max(1, args.warmup) + args.steps):
+        m2 = Lb.getHeapOffset()
+        t0 = time.perf_counter()
+        rc, _ = ing.load(binp)
+        Lb.hgpuSync()
+        if k >= max(1, args.warmup):
+            bts.append(time.perf_counter() - t0)
+        Lb.setHeapOffset(m2)
+        assert rc == 0
+    sec = statistics.median(ts)
+    parse_ms = dict((k, v) for k, v, _ in kern).get("csv_parse")
+    col_bytes = rows * (4 * 4 + 8 * 4 + 2 + 4 * 3 + 8 * 2 + 8)  # values written (strings as pointers)
+    # CPU: the oracle's readCSV on the first rows of the same file
+    sample_rows = max(1, rows // args.cpu_scale)
+    spath = os.path.join(tmp, "sample.tbl")
+    with open(path, "rb") as f, open(spath, "wb") as g:
+        for _ in range(sample_rows):
+            g.write(f.readline())
+    ora = Builtins(os.path.join(ROOT, "oracle", "_build", "liboracle.so"), "oracle")
+    oing = Ingest(ora)
+    ctimes = []
+    for _ in range(args.cpu_reps):
+        mo = ora.lib.getHeapOffset()
+        t0 = time.perf_counter()
+        rc, _ = oing.csv(spath, D.LINEITEM_TYPES, D.LINEITEM_NAMES)
+        ctimes.append(time.perf_counter() - t0)
+        ora.lib.setHeapOffset(mo)
+        assert rc == 0
+    cpu_rows_s = sample_rows / statistics.median(ctimes)
+    for q in (path, binp, spath):
+        os.remove(q)
+    os.rmdir(tmp)
+    achieved = (nbytes + col_bytes) / (parse_ms / 1e3) / 1e9 if parse_ms else None
+    return {
+        "metric": "readCSV text GB/s and rows/s (lineitem .tbl -> table in HBM)", "value": nbytes / sec / 1e9,
+        "unit": "GB/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8 text -> i32/f64/char/date/sym/str",
+        "data": "synthetic (seeded lineitem-shaped text, space-padded fields)",
+        "config": {"workload": f"readCSV lineitem {rows:,} rows, 16 columns (load_db.cc:111-129 types), "
+                               "file in the page cache", "bytes": nbytes},
+        "rows_per_s": rows / sec,
+        "e2e": {"value": nbytes / sec / 1e9, "unit": "GB/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": rows * 40, "rows_per_s": rows / sec},
+        "kernels_ms": {k: [round(v, 3), c] for k, v, c in kern[:16]},
+        "roofline": {"bound": "hbm", "kernel": "csv_parse", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm if achieved else None, "peak_source": src,
+                     "algorithmic_bytes": nbytes + col_bytes, "traffic": None},
+        "binary_load": {"bytes": bsize, "ms": statistics.median(bts) * 1e3,
+                        "gbs": bsize / statistics.median(bts) / 1e9},
+        "cpu_baseline": {"value": cpu_rows_s, "unit": "rows/s", "cores": 1, "kind": "port",
+                         "sample": f"first {sample_rows:,} rows of the same file, oracle readCSV (serial, as "
+                                   f"the reference's fgets loop), median of {len(ctimes)}",
+                         "gbs": cpu_rows_s * nbytes / rows / 1e9},
+        "gpu_launches": int(sum(c for _, _, c in kern)), "clocks": clk,
+    }
+
+
 def cpu_sample(args):
     """The oracle port on a bounded sample of the workload (fact and dim scaled by 1/10)."""
     ora = Builtins(os.path.join(ROOT, "oracle", "_build", "liboracle.so"), "oracle")
@@ -572,7 +694,9 @@ def main():
     ap.add_argument("--dim", type=int, default=15_000_000)
     ap.add_argument("--cpu-scale", type=int, default=10)
     ap.add_argument("--cpu-reps", type=int, default=3)
-    ap.add_argument("--workload", default="join_group", choices=["join_group", "batched", "served", "builtins"])
+    ap.add_argument("--workload", default="join_group",
+                    choices=["join_group", "batched", "served", "builtins", "ingest"])
+    ap.add_argument("--ingest-rows", type=int, default=6_001_215)
     ap.add_argument("--rates", default="200,1000,5000")
     ap.add_argument("--serve-seconds", type=float, default=1.5)
     ap.add_argument("--order-rows", type=int, default=150_000_000)
@@ -581,8 +705,9 @@ def main():
     ap.add_argument("--max-fact", type=int, default=20_000_000)
     args = ap.parse_args()
     rank, ws, dist = dist_init(args.gpus)
-    if args.workload in ("batched", "served", "builtins") and args.impl == "gb300":
-        line = {"batched": run_batched, "served": run_served, "builtins": run_builtins}[args.workload](args)
+    if args.workload in ("batched", "served", "builtins", "ingest") and args.impl == "gb300":
+        line = {"batched": run_batched, "served": run_served, "builtins": run_builtins,
+                "ingest": run_ingest}[args.workload](args)
         if rank == 0:
             print(json.dumps(line))
         return

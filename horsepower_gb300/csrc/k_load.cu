@@ -7,10 +7,10 @@
 //
 // CSV: the whole file is copied to HBM once, then
 //   1. line ends: per-tile newline counts, a scan, an ordered scatter;
-//   2. one warp per line stages the line in shared memory, trims it as
-//      getField does, finds the separators with ballots and hands field j to
-//      lane j, which converts it with loadItem's function for its column's
-//      type (strtol semantics for atoi/atol, sscanf %d-%d-%d, first char);
+//   2. one warp per 32 lines: the warp trims each line as getField does and
+//      finds its separators with ballots, then converts column by column,
+//      lane i taking line i, with loadItem's function for the column's type
+//      (strtol semantics for atoi/atol, sscanf %d-%d-%d, first char);
 //   3. floats: decimal significand and exponent in one pass; Clinger's exact
 //      fast path (significand <= 2^53 and |exponent| <= 22: one correctly
 //      rounded IEEE operation on exact operands) covers decimals such as
@@ -22,10 +22,14 @@
 //      GPU and every row's text checked against its representative's;
 //   5. strings: lengths scanned to offsets, texts and their pointers written
 //      straight into pinned host memory by the GPU.
+#include <unistd.h>
+
+#include <atomic>
 #include <climits>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "dev_common.cuh"
@@ -87,6 +91,75 @@ I stream_in(FILE* fp, void* dst, size_t bytes) {
     return 0;
 }
 
+// Large reads from a regular file: worker threads pread disjoint chunks into
+// their own pinned buffers and copy them to HBM on their own streams, so file
+// reads (memory copies out of the page cache) run on several cores at once.
+constexpr size_t PAR_CHUNK = 8u << 20;
+constexpr int PAR_THREADS = 8;
+struct ParWorker {
+    void* buf[2] = {nullptr, nullptr};
+    cudaEvent_t ev[2];
+    cudaStream_t st;
+    bool ready = false;
+};
+ParWorker g_par[PAR_THREADS];
+
+I par_init(int t) {
+    ParWorker& w = g_par[t];
+    if (w.ready) return 0;
+    for (int k = 0; k < 2; k++) {
+        HG_CU(cudaHostAlloc(&w.buf[k], PAR_CHUNK, cudaHostAllocDefault));
+        HG_CU(cudaEventCreateWithFlags(&w.ev[k], cudaEventDisableTiming));
+    }
+    HG_CU(cudaStreamCreateWithFlags(&w.st, cudaStreamNonBlocking));
+    w.ready = true;
+    return 0;
+}
+
+I stream_in_par(FILE* fp, void* dst, size_t bytes) {
+    const off_t pos = ftello(fp);
+    if (pos < 0 || bytes < 4 * PAR_CHUNK) return stream_in(fp, dst, bytes);
+    int dev = 0;
+    HG_CU(cudaGetDevice(&dev));
+    unsigned hw = std::thread::hardware_concurrency();
+    int nt = (int)(hw / 2 > 1 ? hw / 2 : 1);
+    if (nt > PAR_THREADS) nt = PAR_THREADS;
+    for (int t = 0; t < nt; t++) HG_CHECK(par_init(t));
+    const int fd = fileno(fp);
+    std::atomic<size_t> next(0);
+    std::atomic<int> bad(0);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; t++) {
+        th.emplace_back([&, t]() {
+            cudaSetDevice(dev);
+            ParWorker& w = g_par[t];
+            int k = 0;
+            for (;;) {
+                const size_t c0 = next.fetch_add(PAR_CHUNK);
+                if (c0 >= bytes || bad.load()) break;
+                const size_t c = bytes - c0 < PAR_CHUNK ? bytes - c0 : PAR_CHUNK;
+                if (cudaEventSynchronize(w.ev[k]) != cudaSuccess) { bad = 2; break; }
+                size_t got = 0;
+                while (got < c) {
+                    const ssize_t r = pread(fd, (char*)w.buf[k] + got, c - got, pos + (off_t)(c0 + got));
+                    if (r <= 0) break;
+                    got += (size_t)r;
+                }
+                if (got != c) { bad = 1; break; }
+                if (cudaMemcpyAsync((char*)dst + c0, w.buf[k], c, cudaMemcpyHostToDevice, w.st) != cudaSuccess ||
+                    cudaEventRecord(w.ev[k], w.st) != cudaSuccess) { bad = 2; break; }
+                k ^= 1;
+            }
+            if (cudaStreamSynchronize(w.st) != cudaSuccess) bad = 2;
+        });
+    }
+    for (auto& x : th) x.join();
+    if (bad.load() == 1) return io_fail("pread: unexpected end of file");
+    if (bad.load() == 2) return set_error(E_DEVICE, "copying file chunks to the device");
+    if (fseeko(fp, pos + (off_t)bytes, SEEK_SET) != 0) return io_fail("fseek failed");
+    return 0;
+}
+
 // src (device) -> fp, double-buffered
 I stream_out(FILE* fp, const void* src, size_t bytes) {
     HG_CHECK(stage_init());
@@ -139,6 +212,27 @@ I put_words(V x, I typ, const std::vector<L>& w) {
 }
 
 // ------------------------------------------------------- binary: read side
+I csv_symbols(const char* dbuf, const unsigned long long* spans, long long rows, long long* out);
+
+// len(x) i64 lengths, then the NUL-terminated texts in one read; *offs gets
+// each text's offset in *blob (host memory).
+I read_texts(FILE* fp, L len, std::vector<char>* blob, std::vector<unsigned long long>* offs) {
+    std::vector<L> sz((size_t)len);
+    RD(sz.data(), 8 * len);
+    size_t total = 0;
+    offs->resize((size_t)len);
+    for (L i = 0; i < len; i++) {
+        if (sz[i] < 0) return set_error(E_GENERAL, "serialized text: negative length");
+        (*offs)[i] = total;
+        total += (size_t)sz[i] + 1;
+    }
+    blob->resize(total > 0 ? total : 1);
+    RD(blob->data(), total);
+    for (L i = 0; i < len; i++)
+        if ((*blob)[(*offs)[i] + (size_t)sz[i]] != 0) return set_error(E_GENERAL, "serialized text without its NUL");
+    return 0;
+}
+
 I read_node(V x, FILE* fp) {
     V0 hdr;
     RD(&hdr, sizeof(V0));
@@ -158,32 +252,53 @@ I read_node(V x, FILE* fp) {
         void* d = dalloc(nb);
         if (!d) return E_DEVICE_OOM;
         x->g = (G)d;
-        return stream_in(fp, d, nb);
+        return stream_in_par(fp, d, nb);
     }
     switch (typ) {
     case H_Q: {  // readSerializeQ (h_io.cc:716-722): lengths, then NUL-terminated texts
-        std::vector<L> sz((size_t)len), ids((size_t)len);
-        RD(sz.data(), 8 * len);
-        std::string buf;
-        for (L i = 0; i < len; i++) {
-            if (sz[i] < 0) return set_error(E_GENERAL, "serialized symbol: negative length");
-            buf.assign((size_t)sz[i] + 1, '\0');
-            RD(&buf[0], sz[i] + 1);
-            ids[i] = getSymbol((S)buf.c_str());
+        std::vector<char> blob;
+        std::vector<unsigned long long> offs;
+        HG_CHECK(read_texts(fp, len, &blob, &offs));
+        bool short_texts = true;
+        for (L i = 0; i < len && short_texts; i++)
+            short_texts = strlen(blob.data() + offs[i]) < 0xffff;
+        if (len <= 1 || !short_texts) {  // interned one by one, in order
+            std::vector<L> ids((size_t)len);
+            for (L i = 0; i < len; i++) ids[i] = getSymbol(blob.data() + offs[i]);
+            return put_words(x, H_Q, ids);
         }
-        return put_words(x, H_Q, ids);
+        // on the GPU: distinct texts interned in first-occurrence order, as the loop would
+        std::vector<unsigned long long> spans((size_t)len);
+        for (L i = 0; i < len; i++) spans[i] = (offs[i] << 16) | (unsigned long long)strlen(blob.data() + offs[i]);
+        char* dblob = (char*)salloc(blob.size());
+        unsigned long long* dspans = (unsigned long long*)salloc((size_t)len * 8);
+        long long* ids = (long long*)dalloc((size_t)len * 8);
+        if (!dblob || !dspans || !ids) return E_DEVICE_OOM;
+        HG_CU(cudaMemcpyAsync(dblob, blob.data(), blob.size(), cudaMemcpyHostToDevice, g_stream));
+        HG_CU(cudaMemcpyAsync(dspans, spans.data(), (size_t)len * 8, cudaMemcpyHostToDevice, g_stream));
+        HG_CHECK(csv_symbols(dblob, dspans, len, ids));
+        x->typ = H_Q;
+        x->len = len;
+        x->g = (G)ids;
+        return 0;
     }
-    case H_S: {  // readSerializeS (h_io.cc:724-729)
+    case H_S: {  // readSerializeS (h_io.cc:724-729): the texts land in one pinned block
         std::vector<L> sz((size_t)len);
         RD(sz.data(), 8 * len);
-        S* ptrs = len <= 1 ? (S*)&x->b : (S*)halloc((size_t)len * sizeof(S));
-        if (!ptrs) return E_DEVICE_OOM;
+        size_t total = 0;
         for (L i = 0; i < len; i++) {
             if (sz[i] < 0) return set_error(E_GENERAL, "serialized string: negative length");
-            S t = (S)halloc((size_t)sz[i] + 1);
-            if (!t) return E_DEVICE_OOM;
-            RD(t, sz[i] + 1);
-            ptrs[i] = t;
+            total += (size_t)sz[i] + 1;
+        }
+        char* blob = (char*)halloc(total > 0 ? total : 1);
+        S* ptrs = len <= 1 ? (S*)&x->b : (S*)halloc((size_t)len * sizeof(S));
+        if (!blob || !ptrs) return E_DEVICE_OOM;
+        RD(blob, total);
+        size_t o = 0;
+        for (L i = 0; i < len; i++) {
+            if (blob[o + (size_t)sz[i]] != 0) return set_error(E_GENERAL, "serialized string without its NUL");
+            ptrs[i] = blob + o;
+            o += (size_t)sz[i] + 1;
         }
         x->typ = H_S;
         x->len = len;
@@ -293,8 +408,7 @@ I write_node(V x, FILE* fp) {
 // ====================================================================== CSV
 constexpr int NL_TILE = 1 << 16;   // bytes per newline-count tile
 constexpr int NL_THREADS = 256;    // 256 bytes per thread per tile
-constexpr int CSV_WARPS = 8;       // lines per block (one warp each)
-constexpr int CSV_MAXLINE = 4096;  // largest LINE_MAX_CHAR accepted (shared memory per warp)
+constexpr int CSV_MAXLINE = 65535;  // largest LINE_MAX_CHAR accepted (16-bit field offsets)
 constexpr int CSV_MAXCOLS = 256;
 
 enum : unsigned {
@@ -351,8 +465,25 @@ __global__ void k_nl_scatter(const char* __restrict__ buf, long long n, const un
     for (unsigned w = 0; w < (threadIdx.x >> 5); w++) before += ws[w];
     unsigned long long o = offs[blockIdx.x] + before + (incl - c);
     if (c == 0) return;
-    for (long long i = t0; i < n && i < t0 + NL_PER; i++)
-        if (buf[i] == '\n') pos[o++] = i;
+    if (t0 + NL_PER <= n) {
+        const uint4* p = (const uint4*)(buf + t0);
+        for (int k = 0; k < NL_PER / 16; k++) {
+            const uint4 v = p[k];
+            const unsigned w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                unsigned m = __vcmpeq4(w[q], 0x0a0a0a0au);  // 0xff in each newline byte
+                while (m) {
+                    const int b = __ffs(m) - 1;
+                    pos[o++] = t0 + 16 * k + 4 * q + (b >> 3);
+                    m &= ~(0xffu << (b & ~7));
+                }
+            }
+        }
+    } else {
+        for (long long i = t0; i < n && i < t0 + NL_PER; i++)
+            if (buf[i] == '\n') pos[o++] = i;
+    }
 }
 
 struct CsvCol {
@@ -369,7 +500,6 @@ struct CsvArgs {
     int ncols;
     char sep;
     int maxline;               // LINE_MAX_CHAR
-    int lstride;               // shared-memory bytes per line (maxline rounded up to 16)
     const CsvCol* cols;
     unsigned* err;             // [0] codes, [1] first bad row (atomicMin)
     unsigned long long* slow;  // (span, row << 16 | col) pairs of floats for the slow pass
@@ -524,102 +654,156 @@ __device__ bool fast_f32(const Dec& d, float* out) {
     return true;
 }
 
-// One warp per line.
-__global__ void __launch_bounds__(CSV_WARPS * 32) k_csv_parse(CsvArgs a) {
-    extern __shared__ char csv_smem[];
-    const int warp = threadIdx.x >> 5, lane = lane_id();
-    char* line = csv_smem + (size_t)warp * (a.lstride + CSV_MAXCOLS * 4);
-    int* seps = (int*)(line + a.lstride);
-    for (long long r = (long long)blockIdx.x * CSV_WARPS + warp; r < a.rows; r += (long long)gridDim.x * CSV_WARPS) {
-        const long long li = r + a.first_line;
-        const long long s = li == 0 ? 0 : a.nl[li - 1] + 1;
-        const bool has_nl = li < a.nnl;
-        const long long e = has_nl ? a.nl[li] : a.size;
-        const long long len = e - s;
-        if (len + (has_nl ? 1 : 0) > a.maxline - 1) {
-            if (lane == 0) { atomicOr(a.err, CSV_LONG); atomicMin(a.err + 1, row32(r)); }
-            continue;
-        }
-        bool nul = false;
-        for (int k = lane; k < len; k += 32) {
-            const char c = a.buf[s + k];
-            line[k] = c;
-            nul |= c == 0;
-        }
-        __syncwarp();
-        if (__any_sync(0xffffffffu, nul)) {
-            if (lane == 0) { atomicOr(a.err, CSV_NUL); atomicMin(a.err + 1, row32(r)); }
-            continue;
-        }
-        // trim(line): leading ' ', trailing ' ', '\r', '\n' (h_io.cc:190-204)
-        int ls = 0, le = (int)len;
-        if (lane == 0) {
-            while (ls < le && line[ls] == ' ') ls++;
-            while (le > ls && c_skip((unsigned char)line[le - 1])) le--;
-        }
-        ls = __shfl_sync(0xffffffffu, ls, 0);
-        le = __shfl_sync(0xffffffffu, le, 0);
-        // separators, in order (getField, h_io.cc:126-143)
-        int nsep = 0;
-        for (int b = ls; b < le; b += 32) {
-            const int k = b + lane;
-            const bool is = k < le && line[k] == a.sep;
-            const unsigned m = __ballot_sync(0xffffffffu, is);
-            const int idx = nsep + __popc(m & ((1u << lane) - 1u));
-            if (is && idx < a.ncols) seps[idx] = k;
-            nsep += __popc(m);
-        }
-        __syncwarp();
-        const int loaded = a.sep == ' ' ? nsep + 1 : nsep;
-        if (loaded != a.ncols) {
-            if (lane == 0) { atomicOr(a.err, CSV_FIELDS); atomicMin(a.err + 1, row32(r)); }
-            continue;
-        }
-        for (int j = lane; j < a.ncols; j += 32) {
-            int fb = j == 0 ? ls : seps[j - 1] + 1;
-            int fe = j < nsep ? seps[j] : le;
-            // trimSelf(tmp): leading ' ', trailing ' ', '\r', '\n'
-            while (fb < fe && line[fb] == ' ') fb++;
-            while (fe > fb && c_skip((unsigned char)line[fe - 1])) fe--;
-            const char* f = line + fb;
-            const int n = fe - fb;
-            const CsvCol c = a.cols[j];
-            switch (c.typ) {
-            case H_B: ((bool*)c.out)[r] = (int)(unsigned)(unsigned long long)dev_strtol(f, n) != 0; break;
-            case H_J: ((int8_t*)c.out)[r] = (int8_t)(int)(unsigned)(unsigned long long)dev_strtol(f, n); break;
-            case H_H: ((int16_t*)c.out)[r] = (int16_t)(int)(unsigned)(unsigned long long)dev_strtol(f, n); break;
-            case H_I: ((int32_t*)c.out)[r] = (int32_t)(unsigned)(unsigned long long)dev_strtol(f, n); break;
-            case H_L: ((long long*)c.out)[r] = dev_strtol(f, n); break;
-            case H_C: ((char*)c.out)[r] = n > 0 ? f[0] : 0; break;
-            case H_D: {  // sscanf(s, "%d-%d-%d") -> a*10000 + b*100 + c
-                int pos = 0, y, m, dd;
-                bool ok = scan_int(f, n, &pos, &y) && pos < n && f[pos] == '-' && (pos++, scan_int(f, n, &pos, &m)) &&
-                          pos < n && f[pos] == '-' && (pos++, scan_int(f, n, &pos, &dd));
-                if (!ok) { atomicOr(a.err, CSV_DATE); atomicMin(a.err + 1, row32(r)); break; }
-                ((int32_t*)c.out)[r] = (int32_t)((unsigned)y * 10000u + (unsigned)m * 100u + (unsigned)dd);
-                break;
+// Field conversion by column type (loadItem, h_io.cc:164-181).
+__device__ __forceinline__ void csv_convert(const CsvArgs& a, const CsvCol& c, int j, long long r, const char* f, int n,
+                                            unsigned long long off) {
+    switch (c.typ) {
+    case H_B: ((bool*)c.out)[r] = (int)(unsigned)(unsigned long long)dev_strtol(f, n) != 0; break;
+    case H_J: ((int8_t*)c.out)[r] = (int8_t)(int)(unsigned)(unsigned long long)dev_strtol(f, n); break;
+    case H_H: ((int16_t*)c.out)[r] = (int16_t)(int)(unsigned)(unsigned long long)dev_strtol(f, n); break;
+    case H_I: ((int32_t*)c.out)[r] = (int32_t)(unsigned)(unsigned long long)dev_strtol(f, n); break;
+    case H_L: ((long long*)c.out)[r] = dev_strtol(f, n); break;
+    case H_C: ((char*)c.out)[r] = n > 0 ? f[0] : 0; break;
+    case H_D: {  // sscanf(s, "%d-%d-%d") -> a*10000 + b*100 + c
+        int pos = 0, y, m, dd;
+        bool ok = scan_int(f, n, &pos, &y) && pos < n && f[pos] == '-' && (pos++, scan_int(f, n, &pos, &m)) &&
+                  pos < n && f[pos] == '-' && (pos++, scan_int(f, n, &pos, &dd));
+        if (!ok) { atomicOr(a.err, CSV_DATE); atomicMin(a.err + 1, row32(r)); break; }
+        ((int32_t*)c.out)[r] = (int32_t)((unsigned)y * 10000u + (unsigned)m * 100u + (unsigned)dd);
+        break;
+    }
+    case H_E:
+    case H_F: {
+        const Dec d = parse_dec(f, n);
+        if (d.kind == 4) { atomicOr(a.err, CSV_HEXNAN); atomicMin(a.err + 1, row32(r)); break; }
+        bool done;
+        if (c.typ == H_E) { double v; done = fast_f64(d, &v); if (done) ((double*)c.out)[r] = v; }
+        else { float v; done = fast_f32(d, &v); if (done) ((float*)c.out)[r] = v; }
+        if (!done) {
+            const unsigned k = atomicAdd(a.nslow, 1u);
+            if (k < a.slow_cap) {
+                a.slow[2 * k] = (off << 16) | (unsigned long long)n;
+                a.slow[2 * k + 1] = ((unsigned long long)r << 16) | (unsigned long long)j;
+            } else {
+                atomicOr(a.err, CSV_SLOWFULL);
             }
-            case H_E:
-            case H_F: {
-                const Dec d = parse_dec(f, n);
-                if (d.kind == 4) { atomicOr(a.err, CSV_HEXNAN); atomicMin(a.err + 1, row32(r)); break; }
-                bool done;
-                if (c.typ == H_E) { double v; done = fast_f64(d, &v); if (done) ((double*)c.out)[r] = v; }
-                else { float v; done = fast_f32(d, &v); if (done) ((float*)c.out)[r] = v; }
-                if (!done) {
-                    const unsigned k = atomicAdd(a.nslow, 1u);
-                    if (k < a.slow_cap) {
-                        a.slow[2 * k] = ((unsigned long long)(s + fb) << 16) | (unsigned long long)n;
-                        a.slow[2 * k + 1] = ((unsigned long long)r << 16) | (unsigned long long)j;
-                    } else {
-                        atomicOr(a.err, CSV_SLOWFULL);
+        }
+        break;
+    }
+    default:  // H_Q, H_S: the field's span for the symbol and string passes
+        ((unsigned long long*)c.out)[r] = (off << 16) | (unsigned long long)n;
+        break;
+    }
+}
+
+// One warp per batch of 32 consecutive lines.  Phase A: lane i scans line i
+// in aligned 16-byte words, finding separators (and NULs) four bytes at a
+// time with byte-wise compares, and records each field's (start, length) in
+// shared memory.  Phase B converts column by column, lane i taking line i,
+// so every lane runs the same conversion and a column's stores are
+// contiguous.  A separator that getField's trimming could remove (' ',
+// '\r', '\n') needs the line's trimmed bounds first, so such lines are
+// scanned twice.
+__device__ __forceinline__ unsigned byte_mask(long long o, long long lo, long long hi) {
+    // 0xff in each byte k of the word at offset o with lo <= o + k < hi
+    const long long a = lo - o > 0 ? lo - o : 0, b = hi - o < 4 ? hi - o : 4;
+    if (b <= a) return 0u;
+    const unsigned long long top = (1ull << (8 * b)) - 1ull, low = (1ull << (8 * a)) - 1ull;
+    return (unsigned)(top & ~low);
+}
+
+__global__ void k_csv_parse(CsvArgs a) {
+    extern __shared__ unsigned csv_fields[];
+    const int warp = threadIdx.x >> 5, lane = lane_id();
+    const int nc = a.ncols;
+    unsigned* fld = csv_fields + (size_t)warp * 32 * nc;  // [32][nc]: start << 16 | length (within the line)
+    const int warps = (int)((blockDim.x >> 5) * gridDim.x);
+    const unsigned sep4 = 0x01010101u * (unsigned char)a.sep;
+    const bool sep_trimmed = a.sep == ' ' || a.sep == '\r' || a.sep == '\n';
+    for (long long base = ((long long)blockIdx.x * (blockDim.x >> 5) + warp) * 32; base < a.rows; base += (long long)warps * 32) {
+        const long long myrow = base + lane;
+        long long ms = 0, me = 0;
+        bool ok = myrow < a.rows;
+        if (ok) {
+            const long long li = myrow + a.first_line;
+            ms = li == 0 ? 0 : a.nl[li - 1] + 1;
+            const bool has_nl = li < a.nnl;
+            me = has_nl ? a.nl[li] : a.size;
+            if (me - ms + (has_nl ? 1 : 0) > a.maxline - 1) {
+                atomicOr(a.err, CSV_LONG);
+                atomicMin(a.err + 1, row32(myrow));
+                ok = false;
+            }
+        }
+        // ---- phase A
+        if (ok) {
+            long long ls = ms, le = me;  // getField's trimmed bounds, needed only when the separator is trimmable
+            if (sep_trimmed) {
+                long long first = me, last = ms - 1;
+                for (long long q = ms & ~15LL; q < me; q += 16) {
+                    const uint4 v = *(const uint4*)(a.buf + q);
+                    const unsigned w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int t = 0; t < 4; t++) {
+                        const long long o = q + 4 * t;
+                        const unsigned valid = byte_mask(o, ms, me);
+                        const unsigned notsp = ~__vcmpeq4(w[t], 0x20202020u) & valid;
+                        const unsigned notskip = ~(__vcmpeq4(w[t], 0x20202020u) | __vcmpeq4(w[t], 0x0d0d0d0du) |
+                                                   __vcmpeq4(w[t], 0x0a0a0a0au)) & valid;
+                        if (notsp && first == me) first = o + ((__ffs(notsp) - 1) >> 3);
+                        if (notskip) last = o + ((31 - __clz(notskip)) >> 3);
                     }
                 }
-                break;
+                ls = first;
+                le = last + 1;
+                if (ls >= le) { ls = ms; le = ms; }
             }
-            default:  // H_Q, H_S: the field's span for the symbol and string passes
-                ((unsigned long long*)c.out)[r] = ((unsigned long long)(s + fb) << 16) | (unsigned long long)n;
-                break;
+            int nf = 0;
+            long long start = ls;
+            bool nul = false;
+            for (long long q = ms & ~15LL; q < me; q += 16) {
+                const uint4 v = *(const uint4*)(a.buf + q);
+                const unsigned w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int t = 0; t < 4; t++) {
+                    const long long o = q + 4 * t;
+                    nul |= (__vcmpeq4(w[t], 0u) & byte_mask(o, ms, me)) != 0u;
+                    unsigned m = __vcmpeq4(w[t], sep4) & byte_mask(o, ls, le);
+                    while (m) {
+                        const int bb = __ffs(m) - 1;
+                        const long long pos = o + (bb >> 3);
+                        if (nf < nc) fld[lane * nc + nf] = ((unsigned)(start - ms) << 16) | (unsigned)(pos - start);
+                        nf++;
+                        start = pos + 1;
+                        m &= ~(0xffu << (bb & ~7));
+                    }
+                }
+            }
+            if (a.sep == ' ') {  // getField also loads the remainder after the last ' '
+                if (nf < nc) fld[lane * nc + nf] = ((unsigned)(start - ms) << 16) | (unsigned)(le > start ? le - start : 0);
+                nf++;
+            }
+            if (nul) {
+                atomicOr(a.err, CSV_NUL);
+                atomicMin(a.err + 1, row32(myrow));
+                ok = false;
+            } else if (nf != nc) {
+                atomicOr(a.err, CSV_FIELDS);
+                atomicMin(a.err + 1, row32(myrow));
+                ok = false;
+            }
+        }
+        __syncwarp();
+        // ---- phase B
+        for (int j = 0; j < nc; j++) {
+            const CsvCol c = a.cols[j];
+            if (ok) {
+                const unsigned f = fld[lane * nc + j];
+                int fb = (int)(f >> 16), fe = fb + (int)(f & 0xffffu);
+                const char* p = a.buf + ms;
+                while (fb < fe && p[fb] == ' ') fb++;  // trimSelf
+                while (fe > fb && c_skip((unsigned char)p[fe - 1])) fe--;
+                csv_convert(a, c, j, myrow, p + fb, fe - fb, (unsigned long long)(ms + fb));
             }
         }
         __syncwarp();
@@ -871,8 +1055,13 @@ __global__ void k_sym_insert(const char* __restrict__ buf, const unsigned long l
         const unsigned long long h = span_hash(buf, spans[r]);
         unsigned long long sl = (h * 0x9e3779b97f4a7c15ull) >> 20 & mask;
         for (unsigned long long p = 0; p <= mask; p++) {
-            const unsigned long long cur = atomicCAS(keys + sl, ~0ull, h);
-            if (cur == ~0ull || cur == h) { atomicMin(first + sl, (unsigned long long)r); break; }
+            unsigned long long cur = *(volatile unsigned long long*)(keys + sl);
+            if (cur == ~0ull) cur = atomicCAS(keys + sl, ~0ull, h);
+            if (cur == ~0ull || cur == h) {
+                // most rows of a repeated text find a smaller row there already
+                if (*(volatile unsigned long long*)(first + sl) > (unsigned long long)r) atomicMin(first + sl, (unsigned long long)r);
+                break;
+            }
             sl = (sl + 1) & mask;
             if (p == mask) atomicOr(derr, DERR_CAPACITY);
         }
@@ -933,17 +1122,25 @@ __global__ void k_str_lengths(const unsigned long long* __restrict__ spans, long
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < rows; r += (long long)gridDim.x * blockDim.x)
         lens[r] = (unsigned)(spans[r] & 0xffffull) + 1u;
 }
-// texts and their pointers written into pinned host memory
+// texts packed NUL-terminated into a device blob (one warp per 32 rows, a
+// lane per byte of each text), and each row's pointer into the host copy
 __global__ void k_str_pack(const char* __restrict__ buf, const unsigned long long* __restrict__ spans, long long rows,
-                           const unsigned long long* __restrict__ offs, char* blob, char** ptrs) {
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < rows; r += (long long)gridDim.x * blockDim.x) {
-        const unsigned long long sp = spans[r];
-        const char* f = buf + (sp >> 16);
-        const int n = (int)(sp & 0xffffull);
-        char* o = blob + offs[r];
-        for (int i = 0; i < n; i++) o[i] = f[i];
-        o[n] = 0;
-        ptrs[r] = o;
+                           const unsigned long long* __restrict__ offs, char* __restrict__ dblob,
+                           unsigned long long host_base, unsigned long long* __restrict__ ptrs) {
+    const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int lane = lane_id();
+    for (long long base = w0 * 32; base < rows; base += nw * 32) {
+        const long long mine = base + lane;
+        if (mine < rows) ptrs[mine] = host_base + offs[mine];
+        const long long last = base + 32 < rows ? base + 32 : rows;
+        for (long long r = base; r < last; r++) {
+            const unsigned long long sp = spans[r];
+            const char* f = buf + (sp >> 16);
+            const int n = (int)(sp & 0xffffull);
+            char* o = dblob + offs[r];
+            for (int i = lane; i <= n; i += 32) o[i] = i < n ? f[i] : 0;
+        }
     }
 }
 
@@ -1009,8 +1206,13 @@ I csv_strings(const char* dbuf, const unsigned long long* spans, long long rows,
     HG_CHECK(scan_exclusive(lens, rows, offs, &total));
     char* blob = (char*)halloc(total > 0 ? total : 1);
     S* ptrs = (S*)halloc((size_t)rows * sizeof(S));
-    if (!blob || !ptrs) return E_DEVICE_OOM;
-    HG_LAUNCH("str_pack", grid_of(rows), 256, 0, k_str_pack, dbuf, spans, rows, offs, blob, ptrs);
+    char* dblob = (char*)salloc(total > 0 ? total : 1);
+    unsigned long long* dptrs = (unsigned long long*)salloc((size_t)rows * 8);
+    if (!blob || !ptrs || !dblob || !dptrs) return E_DEVICE_OOM;
+    HG_LAUNCH("str_pack", grid_of(rows * 32), 256, 0, k_str_pack, dbuf, spans, rows, offs, dblob,
+              (unsigned long long)(uintptr_t)blob, dptrs);
+    HG_CU(cudaMemcpyAsync(blob, dblob, total, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaMemcpyAsync(ptrs, dptrs, (size_t)rows * 8, cudaMemcpyDeviceToHost, g_stream));
     HG_CU(cudaStreamSynchronize(g_stream));
     HG_CHECK(last_launch_error());
     *ptrs_out = ptrs;
@@ -1035,7 +1237,7 @@ I read_csv(V z, S fileName, L numCols, L* types, Q* symList) {
     if (size < 0) { fclose(fp); return io_fail("readCSV: cannot size the file"); }
     char* dbuf = (char*)salloc((size_t)size + 64);
     if (!dbuf) { fclose(fp); return E_DEVICE_OOM; }
-    I e = stream_in(fp, dbuf, (size_t)size);
+    I e = stream_in_par(fp, dbuf, (size_t)size);
     fclose(fp);
     if (e) return e;
     // newline positions
@@ -1086,14 +1288,16 @@ I read_csv(V z, S fileName, L numCols, L* types, Q* symList) {
     HG_CU(cudaMemcpyAsync(err, init_err, 8, cudaMemcpyHostToDevice, g_stream));
     HG_CU(cudaMemsetAsync(nslow, 0, 4, g_stream));
     if (rows > 0) {
-        const int lstride = (int)((LINE_MAX_CHAR + 15) & ~15LL);
-        CsvArgs a{dbuf, size, nl, nnl, first_line, rows, (int)numCols, (char)LINE_SEP, (int)LINE_MAX_CHAR, lstride, dcols,
+        CsvArgs a{dbuf, size, nl, nnl, first_line, rows, (int)numCols, (char)LINE_SEP, (int)LINE_MAX_CHAR, dcols,
                   err, slow, nslow, slow_cap};
-        const size_t smem = (size_t)CSV_WARPS * ((size_t)lstride + CSV_MAXCOLS * 4);
+        const size_t per_warp = (size_t)(32 * numCols) * 4;
+        int wpb = (int)(98304 / per_warp);
+        wpb = wpb > 8 ? 8 : wpb < 1 ? 1 : wpb;
+        const size_t smem = per_warp * (size_t)wpb;
         HG_CU(cudaFuncSetAttribute(k_csv_parse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        long long blocks = (rows + CSV_WARPS - 1) / CSV_WARPS;
-        if (blocks > (long long)g_sms * 32) blocks = (long long)g_sms * 32;
-        HG_LAUNCH("csv_parse", (unsigned)blocks, CSV_WARPS * 32, smem, k_csv_parse, a);
+        long long blocks = (rows + 32LL * wpb - 1) / (32LL * wpb);
+        if (blocks > (long long)g_sms * 16) blocks = (long long)g_sms * 16;
+        HG_LAUNCH("csv_parse", (unsigned)blocks, wpb * 32, smem, k_csv_parse, a);
         HG_CHECK(last_launch_error());
     }
     unsigned herr[2], hslow = 0;
@@ -1187,6 +1391,7 @@ extern "C" {
 I hgpuReadSerialized(V x, FILE* fp) {
     HG_CHECK(ensure_init());
     if (!x || !fp) return E_DOMAIN;
+    ScratchScope ss;
     const long long mark = out_mark();
     I e = read_node(x, fp);
     if (!e) e = apply_residency(x);

@@ -8,6 +8,7 @@
     python -m horsepower_gb300.profile_cases gather    # @index f64 by ascending row ids
     python -m horsepower_gb300.profile_cases q6        # fused q6 chain, 6M rows
     python -m horsepower_gb300.profile_cases shared    # 16 batched join plans over one pair of tables
+    python -m horsepower_gb300.profile_cases csv       # readCSV of a lineitem-shaped .tbl, N rows
     ... --tune tile_rows=32 --tune hash_load=0.7       # autotuner knobs
 
 Inputs are seeded, uploaded once, and each case runs --reps times on
@@ -47,7 +48,7 @@ def timed(L, fn, reps):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["join", "compress", "group", "groupkey", "order", "gather", "q6", "shared"])
+    ap.add_argument("case", choices=["join", "compress", "group", "groupkey", "order", "gather", "q6", "shared", "csv"])
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--rows", type=int, default=0)
     ap.add_argument("--tune", action="append", default=[], help="knob=value (autotuner knobs)")
@@ -99,6 +100,22 @@ def main():
         dim, fact = B.synth_tables(L, 1, n, n // 4)
         plans = [B.make_plan(dim, fact, D.DAYS0 + 100 * k, D.DAYS0 + 100 * k + 365) for k in range(16)]
         t = timed(L, lambda: B.run_batch(L, plans), a.reps)
+    elif a.case == "csv":
+        import os
+        import tempfile
+        text, _ = D.lineitem_csv(a.rows or 1_000_000, seed=9)
+        fd, path = tempfile.mkstemp(suffix=".tbl")
+        os.write(fd, text)
+        os.close(fd)
+        ty = (C.c_longlong * 16)(*D.LINEITEM_TYPES)
+        sy = (C.c_longlong * 16)(*[L.lib.getSymbol(n.encode()) for n in D.LINEITEM_NAMES])
+        L.lib.hgpuReadCSV.argtypes = [C.c_void_p, C.c_char_p, C.c_longlong, C.c_void_p, C.c_void_p]
+
+        def run():
+            z = V0()
+            assert L.lib.hgpuReadCSV(C.addressof(z), path.encode(), 16, ty, sy) == 0
+        t = timed(L, run, a.reps)
+        os.remove(path)
     else:
         from . import plans as P
         tb = D.filter_table(a.rows or 6_001_215)
