@@ -95,7 +95,7 @@ I stream_in(FILE* fp, void* dst, size_t bytes) {
 // their own pinned buffers and copy them to HBM on their own streams, so file
 // reads (memory copies out of the page cache) run on several cores at once.
 constexpr size_t PAR_CHUNK = 8u << 20;
-constexpr int PAR_THREADS = 8;
+constexpr int PAR_THREADS = 16;
 struct ParWorker {
     void* buf[2] = {nullptr, nullptr};
     cudaEvent_t ev[2];
@@ -122,7 +122,7 @@ I stream_in_par(FILE* fp, void* dst, size_t bytes) {
     int dev = 0;
     HG_CU(cudaGetDevice(&dev));
     unsigned hw = std::thread::hardware_concurrency();
-    int nt = (int)(hw / 2 > 1 ? hw / 2 : 1);
+    int nt = (int)(hw > 1 ? hw : 1);
     if (nt > PAR_THREADS) nt = PAR_THREADS;
     for (int t = 0; t < nt; t++) HG_CHECK(par_init(t));
     const int fd = fileno(fp);
@@ -156,6 +156,42 @@ I stream_in_par(FILE* fp, void* dst, size_t bytes) {
     for (auto& x : th) x.join();
     if (bad.load() == 1) return io_fail("pread: unexpected end of file");
     if (bad.load() == 2) return set_error(E_DEVICE, "copying file chunks to the device");
+    if (fseeko(fp, pos + (off_t)bytes, SEEK_SET) != 0) return io_fail("fseek failed");
+    return 0;
+}
+
+// fp -> host memory: the same disjoint-chunk preads, straight into dst
+I read_par_host(FILE* fp, void* dst, size_t bytes) {
+    const off_t pos = ftello(fp);
+    if (pos < 0 || bytes < 4 * PAR_CHUNK) {
+        if (bytes && fread(dst, 1, bytes, fp) != bytes) return io_fail("fread: unexpected end of file");
+        return 0;
+    }
+    unsigned hw = std::thread::hardware_concurrency();
+    int nt = (int)(hw > 1 ? hw : 1);
+    if (nt > PAR_THREADS) nt = PAR_THREADS;
+    const int fd = fileno(fp);
+    std::atomic<size_t> next(0);
+    std::atomic<int> bad(0);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; t++) {
+        th.emplace_back([&]() {
+            for (;;) {
+                const size_t c0 = next.fetch_add(PAR_CHUNK);
+                if (c0 >= bytes || bad.load()) break;
+                const size_t c = bytes - c0 < PAR_CHUNK ? bytes - c0 : PAR_CHUNK;
+                size_t got = 0;
+                while (got < c) {
+                    const ssize_t r = pread(fd, (char*)dst + c0 + got, c - got, pos + (off_t)(c0 + got));
+                    if (r <= 0) break;
+                    got += (size_t)r;
+                }
+                if (got != c) { bad = 1; break; }
+            }
+        });
+    }
+    for (auto& x : th) x.join();
+    if (bad.load()) return io_fail("pread: unexpected end of file");
     if (fseeko(fp, pos + (off_t)bytes, SEEK_SET) != 0) return io_fail("fseek failed");
     return 0;
 }
@@ -213,24 +249,24 @@ I put_words(V x, I typ, const std::vector<L>& w) {
 
 // ------------------------------------------------------- binary: read side
 I csv_symbols(const char* dbuf, const unsigned long long* spans, long long rows, long long* out);
+unsigned grid_of(long long n);
 
-// len(x) i64 lengths, then the NUL-terminated texts in one read; *offs gets
-// each text's offset in *blob (host memory).
-I read_texts(FILE* fp, L len, std::vector<char>* blob, std::vector<unsigned long long>* offs) {
-    std::vector<L> sz((size_t)len);
-    RD(sz.data(), 8 * len);
-    size_t total = 0;
-    offs->resize((size_t)len);
-    for (L i = 0; i < len; i++) {
-        if (sz[i] < 0) return set_error(E_GENERAL, "serialized text: negative length");
-        (*offs)[i] = total;
-        total += (size_t)sz[i] + 1;
+__global__ void k_text_lengths(const long long* __restrict__ sz, long long n, unsigned* __restrict__ lens) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        lens[i] = (unsigned)sz[i] + 1u;
+}
+// span of text i = (offset << 16) | strlen; the text must end at its stored length
+__global__ void k_text_spans(const char* __restrict__ blob, const long long* __restrict__ sz,
+                             const unsigned long long* __restrict__ offs, long long n,
+                             unsigned long long* __restrict__ spans, unsigned* bad) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long o = offs[i];
+        const int k = (int)sz[i];
+        if (blob[o + k] != 0) atomicOr(bad, 1u);
+        int l = 0;
+        while (l < k && blob[o + l] != 0) l++;
+        spans[i] = (o << 16) | (unsigned long long)l;
     }
-    blob->resize(total > 0 ? total : 1);
-    RD(blob->data(), total);
-    for (L i = 0; i < len; i++)
-        if ((*blob)[(*offs)[i] + (size_t)sz[i]] != 0) return set_error(E_GENERAL, "serialized text without its NUL");
-    return 0;
 }
 
 I read_node(V x, FILE* fp) {
@@ -256,26 +292,46 @@ I read_node(V x, FILE* fp) {
     }
     switch (typ) {
     case H_Q: {  // readSerializeQ (h_io.cc:716-722): lengths, then NUL-terminated texts
-        std::vector<char> blob;
-        std::vector<unsigned long long> offs;
-        HG_CHECK(read_texts(fp, len, &blob, &offs));
+        std::vector<L> sz((size_t)len);
+        RD(sz.data(), 8 * len);
+        size_t total = 0;
         bool short_texts = true;
-        for (L i = 0; i < len && short_texts; i++)
-            short_texts = strlen(blob.data() + offs[i]) < 0xffff;
+        for (L i = 0; i < len; i++) {
+            if (sz[i] < 0) return set_error(E_GENERAL, "serialized symbol: negative length");
+            total += (size_t)sz[i] + 1;
+            short_texts = short_texts && sz[i] < 0xffff;
+        }
         if (len <= 1 || !short_texts) {  // interned one by one, in order
+            std::vector<char> blob(total > 0 ? total : 1);
+            RD(blob.data(), total);
             std::vector<L> ids((size_t)len);
-            for (L i = 0; i < len; i++) ids[i] = getSymbol(blob.data() + offs[i]);
+            size_t o = 0;
+            for (L i = 0; i < len; i++) {
+                if (blob[o + (size_t)sz[i]] != 0) return set_error(E_GENERAL, "serialized text without its NUL");
+                ids[i] = getSymbol(blob.data() + o);
+                o += (size_t)sz[i] + 1;
+            }
             return put_words(x, H_Q, ids);
         }
-        // on the GPU: distinct texts interned in first-occurrence order, as the loop would
-        std::vector<unsigned long long> spans((size_t)len);
-        for (L i = 0; i < len; i++) spans[i] = (offs[i] << 16) | (unsigned long long)strlen(blob.data() + offs[i]);
-        char* dblob = (char*)salloc(blob.size());
+        // on the GPU: texts straight into HBM, distinct ones interned in first-occurrence order
+        char* dblob = (char*)salloc(total);
+        long long* dsz = (long long*)salloc((size_t)len * 8);
+        unsigned* lens = (unsigned*)salloc((size_t)len * 4);
+        unsigned long long* offs = (unsigned long long*)salloc((size_t)(len + 1) * 8);
         unsigned long long* dspans = (unsigned long long*)salloc((size_t)len * 8);
+        unsigned* bad = (unsigned*)salloc(16);
         long long* ids = (long long*)dalloc((size_t)len * 8);
-        if (!dblob || !dspans || !ids) return E_DEVICE_OOM;
-        HG_CU(cudaMemcpyAsync(dblob, blob.data(), blob.size(), cudaMemcpyHostToDevice, g_stream));
-        HG_CU(cudaMemcpyAsync(dspans, spans.data(), (size_t)len * 8, cudaMemcpyHostToDevice, g_stream));
+        if (!dblob || !dsz || !lens || !offs || !dspans || !bad || !ids) return E_DEVICE_OOM;
+        HG_CHECK(stream_in_par(fp, dblob, total));
+        HG_CU(cudaMemcpyAsync(dsz, sz.data(), (size_t)len * 8, cudaMemcpyHostToDevice, g_stream));
+        HG_CU(cudaMemsetAsync(bad, 0, 4, g_stream));
+        HG_LAUNCH("text_lengths", grid_of(len), 256, 0, k_text_lengths, dsz, len, lens);
+        HG_CHECK(scan_exclusive(lens, len, offs, nullptr));
+        HG_LAUNCH("text_spans", grid_of(len), 256, 0, k_text_spans, dblob, dsz, offs, len, dspans, bad);
+        unsigned hb = 0;
+        HG_CU(cudaMemcpyAsync(&hb, bad, 4, cudaMemcpyDeviceToHost, g_stream));
+        HG_CU(cudaStreamSynchronize(g_stream));
+        if (hb) return set_error(E_GENERAL, "serialized text without its NUL");
         HG_CHECK(csv_symbols(dblob, dspans, len, ids));
         x->typ = H_Q;
         x->len = len;
@@ -293,7 +349,7 @@ I read_node(V x, FILE* fp) {
         char* blob = (char*)halloc(total > 0 ? total : 1);
         S* ptrs = len <= 1 ? (S*)&x->b : (S*)halloc((size_t)len * sizeof(S));
         if (!blob || !ptrs) return E_DEVICE_OOM;
-        RD(blob, total);
+        HG_CHECK(read_par_host(fp, blob, total));
         size_t o = 0;
         for (L i = 0; i < len; i++) {
             if (blob[o + (size_t)sz[i]] != 0) return set_error(E_GENERAL, "serialized string without its NUL");
