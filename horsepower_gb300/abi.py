@@ -144,6 +144,34 @@ class Builtins:
         ids = np.array([self.lib.getSymbol(n.encode()) for n in names], dtype=np.int64)
         return self.vec(ids, H_Q)
 
+    def strs(self, texts):
+        """A string vector (H_S): host pointers to NUL-terminated copies of `texts` (bytes)."""
+        bufs = [C.create_string_buffer(t) for t in texts]
+        ptrs = (C.c_void_p * max(len(texts), 1))(*[C.addressof(b) for b in bufs])
+        v = V0()
+        v.typ, v.len = H_S, len(texts)
+        if len(texts) <= 1:
+            if texts:
+                v.i64 = C.addressof(bufs[0])
+            v.g = C.addressof(v) + V0.u.offset
+        else:
+            v.g = C.addressof(ptrs)
+        self._keep.append((v, bufs, ptrs))
+        return v
+
+    def chars(self, text):
+        """A char vector (H_C) over `text` (bytes), NUL after the last character."""
+        arr = np.frombuffer(text + b"\0", np.int8)
+        v = V0()
+        v.typ, v.len = H_C, len(text)
+        if len(text) <= 1:
+            C.memmove(C.addressof(v) + V0.u.offset, arr.ctypes.data, arr.nbytes)
+            v.g = C.addressof(v) + V0.u.offset
+        else:
+            v.g = arr.ctypes.data
+        self._keep.append((v, arr))
+        return v
+
     def list(self, items, typ=H_G):
         arr = (V0 * max(len(items), 1))()
         for i, it in enumerate(items):

@@ -161,6 +161,17 @@ ListInfo* find_list(const V0* nodes, long long ng);
 void register_bound(const void* data, long long len, long long bound);
 bool known_in_range(const void* data, long long len, long long limit);
 
+// String columns whose texts also live in HBM as one blob, each text's span
+// = (offset << 16) | length (the CSV reader registers the columns it makes).
+void register_strings(const void* ptrs, long long n, const char* blob, const unsigned long long* spans);
+bool find_strings(const void* ptrs, long long n, const char** blob, const unsigned long long** spans);
+// The host symbol table: ids are 0 .. symbol_count() - 1 in order of interning.
+L symbol_count();
+const char* symbol_text(L id);
+
+// pfnCompare on two symbol operands (k_string.cu)
+I compare_symbols(V z, V x, V y, I op);
+
 // reduction mode (1 = fixed-order deterministic tile tree)
 extern int g_reduce_mode;
 

@@ -416,7 +416,8 @@ I pfnCompare(V z, V x, V y, I op) {
         case H_C: return run_compare<int8_t>(z, x, y, H_C, op);  // signed char, as the reference's x86 build
         case H_M: case H_D: case H_U: case H_T: return run_compare<int32_t>(z, x, y, x->typ, op);
         case H_Z: return run_compare<long long>(z, x, y, H_Z, op);
-        default: return set_error(E_NOT_IMPL, "compare on symbols/strings is outside the accelerated path");
+        case H_Q: return compare_symbols(z, x, y, op);
+        default: return set_error(E_NOT_IMPL, "compare of type %d (no case in the reference)", x->typ);
         }
     }
     return E_TYPE;

@@ -1182,13 +1182,17 @@ __global__ void k_str_lengths(const unsigned long long* __restrict__ spans, long
 // lane per byte of each text), and each row's pointer into the host copy
 __global__ void k_str_pack(const char* __restrict__ buf, const unsigned long long* __restrict__ spans, long long rows,
                            const unsigned long long* __restrict__ offs, char* __restrict__ dblob,
-                           unsigned long long host_base, unsigned long long* __restrict__ ptrs) {
+                           unsigned long long host_base, unsigned long long* __restrict__ ptrs,
+                           unsigned long long* __restrict__ bspans) {
     const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
     const int lane = lane_id();
     for (long long base = w0 * 32; base < rows; base += nw * 32) {
         const long long mine = base + lane;
-        if (mine < rows) ptrs[mine] = host_base + offs[mine];
+        if (mine < rows) {
+            ptrs[mine] = host_base + offs[mine];
+            bspans[mine] = (offs[mine] << 16) | (spans[mine] & 0xffffull);  // the text within the device blob
+        }
         const long long last = base + 32 < rows ? base + 32 : rows;
         for (long long r = base; r < last; r++) {
             const unsigned long long sp = spans[r];
@@ -1262,15 +1266,18 @@ I csv_strings(const char* dbuf, const unsigned long long* spans, long long rows,
     HG_CHECK(scan_exclusive(lens, rows, offs, &total));
     char* blob = (char*)halloc(total > 0 ? total : 1);
     S* ptrs = (S*)halloc((size_t)rows * sizeof(S));
-    char* dblob = (char*)salloc(total > 0 ? total : 1);
+    // the device copy stays (output arena) so @like can read the column in HBM
+    char* dblob = (char*)dalloc(total > 0 ? total : 1);
+    unsigned long long* bspans = (unsigned long long*)dalloc((size_t)rows * 8);
     unsigned long long* dptrs = (unsigned long long*)salloc((size_t)rows * 8);
-    if (!blob || !ptrs || !dblob || !dptrs) return E_DEVICE_OOM;
+    if (!blob || !ptrs || !dblob || !bspans || !dptrs) return E_DEVICE_OOM;
     HG_LAUNCH("str_pack", grid_of(rows * 32), 256, 0, k_str_pack, dbuf, spans, rows, offs, dblob,
-              (unsigned long long)(uintptr_t)blob, dptrs);
+              (unsigned long long)(uintptr_t)blob, dptrs, bspans);
     HG_CU(cudaMemcpyAsync(blob, dblob, total, cudaMemcpyDeviceToHost, g_stream));
     HG_CU(cudaMemcpyAsync(ptrs, dptrs, (size_t)rows * 8, cudaMemcpyDeviceToHost, g_stream));
     HG_CU(cudaStreamSynchronize(g_stream));
     HG_CHECK(last_launch_error());
+    if (rows > 1) register_strings(ptrs, rows, dblob, bspans);
     *ptrs_out = ptrs;
     return 0;
 }

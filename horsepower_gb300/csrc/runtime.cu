@@ -11,6 +11,10 @@
 
 #include "hgpu_internal.cuh"
 
+// the symbol table (getSymbol / getSymbolStr): texts by id, ids by text
+static std::unordered_map<std::string, L>* g_sym_ids;
+static std::vector<std::string>* g_sym_names;
+
 namespace hg {
 
 cudaStream_t g_stream = nullptr;
@@ -441,8 +445,36 @@ I last_launch_error() {
 
 // forget the lists and index ranges whose memory was released by a rewind;
 // a list that survives drops a segment plan allocated after the mark
+// String columns whose texts also sit in HBM (written by the CSV reader):
+// the host pointer array -> the device blob and each text's span.
+struct StrCols { const void* ptrs; long long n; const char* blob; const unsigned long long* spans; };
+static std::vector<StrCols> g_strcols;
+void register_strings(const void* ptrs, long long n, const char* blob, const unsigned long long* spans) {
+    if (g_strcols.size() > 64) g_strcols.erase(g_strcols.begin());
+    g_strcols.push_back({ptrs, n, blob, spans});
+}
+bool find_strings(const void* ptrs, long long n, const char** blob, const unsigned long long** spans) {
+    for (size_t i = g_strcols.size(); i-- > 0;)
+        if (g_strcols[i].ptrs == ptrs && g_strcols[i].n == n) {
+            *blob = g_strcols[i].blob;
+            *spans = g_strcols[i].spans;
+            return true;
+        }
+    return false;
+}
+
+// The symbol table as seen by host code: count and texts by id.
+L symbol_count() { return g_sym_names ? (L)g_sym_names->size() : 0; }
+const char* symbol_text(L id) { return (*g_sym_names)[(size_t)id].c_str(); }
+
 static void prune_registries() {
     auto live = [](const void* p) { return !p || (g_out->live(p) && g_host->live(p)); };
+    {
+        std::vector<StrCols> keep;
+        for (StrCols& c : g_strcols)
+            if (live(c.ptrs) && live(c.blob) && live(c.spans)) keep.push_back(c);
+        g_strcols.swap(keep);
+    }
     std::vector<ListInfo> keep;
     for (ListInfo& li : g_lists) {
         if (!live(li.nodes) || !live(li.starts) || !live(li.data)) continue;
@@ -521,8 +553,6 @@ L getTypeSize(I typ, L len) {
     return (L)esize(typ) * len + (typ == H_C ? 1 : 0);
 }
 
-static std::unordered_map<std::string, L>* g_sym_ids;
-static std::vector<std::string>* g_sym_names;
 L getSymbol(S name) {
     if (!g_sym_ids) { g_sym_ids = new std::unordered_map<std::string, L>(); g_sym_names = new std::vector<std::string>(); }
     auto it = g_sym_ids->find(name);

@@ -175,6 +175,12 @@ I pfnLen(V z, V x);             /* h_primitive.cc:656-662 */
 I pfnIndex  (V z, V x, V y);    /* h_primitive.cc:43-94 */
 I pfnIndexOf(V z, V x, V y);    /* h_primitive.cc:1523-1579 */
 I pfnMember (V z, V y, V x);    /* h_primitive.cc:2287-2336 (note argument order) */
+/* @like (h_primitive.cc:1670-1758): x chars / symbols / strings against one
+ * SQL pattern y ('%' any run, '_' any byte; neither matches '\n', as the
+ * reference's translated PCRE2 pattern); z bool, one per row (one for chars).
+ * Patterns holding other regex metacharacters, and one pattern per row:
+ * E_NOT_IMPL. */
+I pfnLike   (V z, V x, V y);
 /* Enum / foreign-key path: pfnEnum builds the enum of y (foreign-key column)
  * over x (primary-key column) as index_of(x, y), E_ENUM_INDEX when some y has
  * no key; pfnFetch returns y back.  pfnAddFKey (h_primitive.cc:2425-2466) is

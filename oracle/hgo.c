@@ -294,6 +294,12 @@ I pfnWhere(V z, V x) {
     else { _Pragma("omp parallel for simd") for (L i = 0; i < n; i++) { L ix = i, iy = i; (void)ix; (void)iy; EXPR; } }
 
 /* pfnCompare: h_primitive.cc:1073-1170 */
+/* compareSymbol (h_symbol.cc:241-243) under COMPFN's operator (h_primitive.cc:1068-1071) */
+static B sym_op(I op, L u, L v) {
+    int c = u == v ? 0 : strcmp(getSymbolStr(u), getSymbolStr(v));
+    R op == 0 ? c < 0 : op == 1 ? c <= 0 : op == 2 ? c > 0 : op == 3 ? c >= 0 : op == 4 ? c == 0 : c != 0;
+}
+
 I pfnCompare(V z, V x, V y, I op) {
     if (!(is_comparable(vp(x)) && is_comparable(vp(y)))) R E_DOMAIN;
     B ox = vn(x) == 1, oy = vn(y) == 1;
@@ -325,7 +331,8 @@ I pfnCompare(V z, V x, V y, I op) {
                     BCAST_LOOP(lenZ, r[i] = COMP(op, a[ix], b[iy])) } break;
         case H_M: case H_D: case H_U: case H_T: { I *a = sI(x), *b = sI(y); BCAST_LOOP(lenZ, r[i] = COMP(op, a[ix], b[iy])) } break;
         case H_Z: { L *a = sL(x), *b = sL(y); BCAST_LOOP(lenZ, r[i] = COMP(op, a[ix], b[iy])) } break;
-        default: R E_NOT_IMPL;  /* symbols/strings (compareSymbol/strcmp) are outside the path */
+        case H_Q: { L *a = sL(x), *b = sL(y); BCAST_LOOP(lenZ, r[i] = sym_op(op, a[ix], b[iy])) } break;
+        default: R E_NOT_IMPL;  /* H_W has no case in the reference (EP) */
         }
         R 0;
     }

@@ -2,9 +2,11 @@
  *
  * Oracle test infrastructure: used only to compile the reference builtin
  * library into oracle/_ref/ for golden vectors.  The reference's @like
- * builtin (the only PCRE2 user) is outside the accelerated path, so the
- * functions below are declared here and defined in pcre2_stub.c as stubs that
- * abort if ever called.  Names and signatures follow the public PCRE2 10.x API.
+ * builtin is the only PCRE2 user.  Where the system has libpcre2-8 the
+ * Makefile defines REF_PCRE2_SYSTEM and links it (the names below map to its
+ * _8 exports), so @like runs as in the reference; elsewhere ref_shim.c
+ * defines the functions as stubs that abort if ever called.  Names and
+ * signatures follow the public PCRE2 10.x API.
  */
 #ifndef HGPU_REF_PCRE2_STUB_H
 #define HGPU_REF_PCRE2_STUB_H
@@ -12,6 +14,23 @@
 #include <stdint.h>
 #ifdef __cplusplus
 extern "C" {
+#endif
+#ifdef REF_PCRE2_SYSTEM
+/* the system's libpcre2-8 exports the 8-bit API with a _8 suffix */
+#define pcre2_compile pcre2_compile_8
+#define pcre2_code_free pcre2_code_free_8
+#define pcre2_config pcre2_config_8
+#define pcre2_pattern_info pcre2_pattern_info_8
+#define pcre2_jit_compile pcre2_jit_compile_8
+#define pcre2_jit_match pcre2_jit_match_8
+#define pcre2_match pcre2_match_8
+#define pcre2_match_data_create_from_pattern pcre2_match_data_create_from_pattern_8
+#define pcre2_match_data_free pcre2_match_data_free_8
+#define pcre2_match_context_create pcre2_match_context_create_8
+#define pcre2_match_context_free pcre2_match_context_free_8
+#define pcre2_jit_stack_create pcre2_jit_stack_create_8
+#define pcre2_jit_stack_assign pcre2_jit_stack_assign_8
+#define pcre2_jit_stack_free pcre2_jit_stack_free_8
 #endif
 typedef const unsigned char *PCRE2_SPTR;
 typedef size_t PCRE2_SIZE;

@@ -17,6 +17,7 @@ int findDefByName(void *chain, char *name) { (void)chain; (void)name; return 0; 
 void *getNodeParams(void *n) { (void)n; return 0; }
 void *getNodeFunc(void *n) { (void)n; return 0; }
 
+#ifndef REF_PCRE2_SYSTEM
 static void no_pcre(const char *f) {
     fprintf(stderr, "oracle/_ref: %s reached (PCRE2 is stubbed; @like is outside the path)\n", f);
     abort();
@@ -36,3 +37,4 @@ void pcre2_match_data_free(void *a) { (void)a; no_pcre("pcre2_match_data_free");
 void pcre2_match_context_free(void *a) { (void)a; no_pcre("pcre2_match_context_free"); }
 void pcre2_jit_stack_assign(void *a, void *b, void *c) { (void)a; (void)b; (void)c; no_pcre("pcre2_jit_stack_assign"); }
 void pcre2_jit_stack_free(void *a) { (void)a; no_pcre("pcre2_jit_stack_free"); }
+#endif

@@ -274,5 +274,44 @@ def build_cases():
     add("enum_missing_key", "pfnEnum", V(pk, H_I), V(np.append(fk[:1000], 20001).astype(np.int32), H_I), error=10)
     add("enum_empty_key", "pfnEnum", V(np.zeros(0, np.int32), H_I), V([3], H_I), error=10)
     add("enum_type", "pfnEnum", V(pk, H_I), V(np.zeros(3, np.int32), H_D), error=6)
+
+    # ---- symbol compares (compareSymbol h_symbol.cc:241-243 under COMPFN h_primitive.cc:1068-1071)
+    words = ["MAIL", "AIR", "REG AIR", "SHIP", "TRUCK", "RAIL", "FOB", "", "AIRMAIL", "air", "A", "MAIL "]
+    sa = [words[i] for i in rng.integers(0, len(words), 400)]
+    sb = [words[i] for i in rng.integers(0, len(words), 400)]
+    for op in ["pfnLt", "pfnLeq", "pfnGt", "pfnGeq", "pfnEq", "pfnNeq"]:
+        add(f"sym_{op[3:].lower()}_vv", op, ("syms", sa), ("syms", sb))
+        add(f"sym_{op[3:].lower()}_vs", op, ("syms", sa), ("sym", "RAIL"))
+        add(f"sym_{op[3:].lower()}_sv", op, ("sym", "AIR"), ("syms", sb))
+
+    # ---- @like (pfnLike h_primitive.cc:1670-1758; genLikeString h_system.cc:319-334; PCRE2 anchored)
+    letters = np.frombuffer(b"abcdefghijklmnopqrstuvwxyz      .", np.uint8)
+    comments = []
+    for k in range(600):
+        n = int(rng.integers(0, 40))
+        t = bytes(letters[rng.integers(0, len(letters), n)])
+        if k % 7 == 0:
+            t = t[:n // 2] + b"special" + t[n // 2:] + b"requests"
+        if k % 11 == 0:
+            t = b"PROMO " + t
+        comments.append(t)
+    comments += [b"", b"\n", b"abc", b"abc\n", b"ab\nc", b"a.c", b"abc.", b"a\\b", b"50%", b"special requests",
+                 b"xspecialyrequestsz\n", b"\xe9t\xe9", b"a_c", b"aXc"]
+    pats = ["%special%requests%", "PROMO%", "%requests", "_b%", "a.c", "a_c", "%", "", "abc", "%.%", "a\\b",
+            "50%", "%s%s%s%", "__", "%\n%", "\xe9%"]
+    for i, pat in enumerate(pats):
+        if not pat:  # the reference's empty pattern reaches PCRE2 as NULL (crash); tested elsewhere
+            continue
+        pb = pat.encode("latin-1")
+        add(f"like_str_{i}", "pfnLike", ("strs", comments), ("strs", [pb]))
+    syms = ["MAIL", "AIR", "REG AIR", "SHIP", "TRUCK", "RAIL", "FOB", "AIRMAIL", "PROMO BRASS", "LARGE BRASS", "STANDARD"]
+    col = [syms[i] for i in rng.integers(0, len(syms), 500)]
+    for i, pat in enumerate(["%AIR%", "%BRASS", "PROMO%", "_A%", "%", "SHIP", "M__L"]):
+        add(f"like_sym_{i}", "pfnLike", ("syms", col), ("sym", pat))
+        add(f"like_sym_str_{i}", "pfnLike", ("syms", col), ("strs", [pat.encode()]))
+    add("like_chars", "pfnLike", ("chars", b"forest green"), ("strs", [b"%green"]))
+    add("like_chars_pat", "pfnLike", ("strs", [b"a", b"b", b"", b"ab"]), ("chars", b"_"))
+    add("like_domain", "pfnLike", V([1, 2], H_I), ("strs", [b"%"]), error=1)
+    add("like_length", "pfnLike", ("strs", [b"a", b"b", b"c"]), ("strs", [b"a", b"b"]), error=5)
     add("enum_list_len", "pfnEnum", Ls(V(pk[:10], H_I), V(pk[:10], H_I)), Ls(V(fk[:10], H_I)), error=1)
     return cases

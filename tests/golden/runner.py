@@ -18,6 +18,10 @@ def build_arg(lib, spec):
         return lib.syms(spec[1])
     if kind == "list":
         return lib.list([build_arg(lib, s) for s in spec[1]])
+    if kind == "strs":
+        return lib.strs(list(spec[1]))
+    if kind == "chars":
+        return lib.chars(spec[1])
     raise ValueError(kind)
 
 
@@ -104,6 +108,13 @@ def store(case, rc, obj, out):
             return ["syms", list(spec[1])]
         if spec[0] == "list":
             return ["list", [enc(s) for s in spec[1]]]
+        if spec[0] in ("strs", "chars"):
+            k = f"{name}/in{len(ins)}"
+            ins.append(k)
+            texts = list(spec[1]) if spec[0] == "strs" else [spec[1]]
+            out[k] = np.frombuffer(b"".join(texts), np.uint8) if texts and any(texts) else np.zeros(0, np.uint8)
+            out[k + "_len"] = np.array([len(t) for t in texts], np.int64)
+            return [spec[0], k]
         raise ValueError(spec)
 
     meta["args"] = [enc(a) for a in case["args"]]
@@ -133,6 +144,13 @@ def load(path):
                 return ("sym", spec[1])
             if spec[0] == "syms":
                 return ("syms", spec[1])
+            if spec[0] in ("strs", "chars"):
+                raw, lens = z[spec[1]].tobytes(), z[spec[1] + "_len"]
+                texts, o = [], 0
+                for n in lens:
+                    texts.append(raw[o:o + int(n)])
+                    o += int(n)
+                return ("strs", texts) if spec[0] == "strs" else ("chars", texts[0])
             return ("list", [dec(s) for s in spec[1]])
 
         case = dict(name=name, fn=meta["fn"], tol=meta["tol"], canonical=meta["canonical"],
