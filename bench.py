@@ -603,6 +603,30 @@ def run_ingest(args):
     names, tot, cnt = (C.c_char_p * 64)(), (C.c_double * 64)(), (C.c_longlong * 64)()
     nk = Lb.hgpuProfileRead(64, names, tot, cnt)
     kern = sorted(((names[i].decode(), tot[i], int(cnt[i])) for i in range(min(nk, 64))), key=lambda k: -k[1])
+    # string and symbol builtins on the loaded table (comments matched in HBM)
+    vals = V0.from_address(t.g + 32)
+    col = lambda j: V0.from_address(vals.g + 32 * j)  # noqa: E731
+    pat = gpu.strs([b"%special%requests%"])
+    smode = gpu.sym("MAIL")
+
+    def timed_call(fn, reps=args.steps):
+        for _ in range(max(1, args.warmup)):
+            mm = Lb.getHeapOffset(); fn(); Lb.setHeapOffset(mm)
+        out = []
+        for _ in range(reps):
+            mm = Lb.getHeapOffset()
+            Lb.hgpuSync()
+            Lb.hgpuTimerStart()
+            fn()
+            out.append(Lb.hgpuTimerStop())
+            Lb.setHeapOffset(mm)
+        return statistics.median(out)
+    strings = {
+        "like_comment_ms": timed_call(lambda: gpu.call("pfnLike", col(15), pat)),
+        "like_shipmode_ms": timed_call(lambda: gpu.call("pfnLike", col(14), gpu.sym("%AIR%"))),
+        "lt_shipmode_ms": timed_call(lambda: gpu.call("pfnLt", col(14), smode)),
+    }
+    strings["like_comment_gbs"] = (nbytes * 43 / 161) / (strings["like_comment_ms"] / 1e3) / 1e9
     # the binary format of the same table
     binp = os.path.join(tmp, "lineitem.bin")
     assert ing.save(binp, t) == 0
@@ -638,6 +662,12 @@ def run_ingest(args):
         ora.lib.setHeapOffset(mo)
         assert rc == 0
     cpu_rows_s = sample_rows / statistics.median(ctimes)
+    rc, ot = oing.csv(spath, D.LINEITEM_TYPES, D.LINEITEM_NAMES)
+    ovals = V0.from_address(ot.g + 32)
+    ocol = lambda j: V0.from_address(ovals.g + 32 * j)  # noqa: E731
+    t0 = time.perf_counter()
+    ora.call("pfnLike", ocol(15), ora.strs([b"%special%requests%"]))
+    cpu_like_rows_s = sample_rows / (time.perf_counter() - t0)
     for q in (path, binp, spath):
         os.remove(q)
     os.rmdir(tmp)
@@ -656,6 +686,8 @@ def run_ingest(args):
         "roofline": {"bound": "hbm", "kernel": "csv_parse", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm if achieved else None, "peak_source": src,
                      "algorithmic_bytes": nbytes + col_bytes, "traffic": None},
+        "strings": dict(strings, rows=rows, cpu_like_rows_s=cpu_like_rows_s,
+                        cpu_like_note=f"oracle pfnLike (OpenMP, {os.cpu_count()} threads) on the {sample_rows:,}-row sample"),
         "binary_load": {"bytes": bsize, "ms": statistics.median(bts) * 1e3,
                         "gbs": bsize / statistics.median(bts) / 1e9},
         "cpu_baseline": {"value": cpu_rows_s, "unit": "rows/s", "cores": 1, "kind": "port",
