@@ -58,6 +58,35 @@ __device__ __forceinline__ T seg_elem(const T* __restrict__ src, const long long
     }
 }
 
+// The 16 elements k * 256 + (first - k * 256 ...) of one lane of a 256-lane
+// tile: positions first + k * 256, k = 0..15, those below `end` loaded (row
+// numbers first, then the values, so all 16 gathers are in flight together).
+template <typename T, bool GATHER>
+__device__ __forceinline__ void seg_load16(const T* __restrict__ src, const long long* __restrict__ rows, long long nx,
+                                           long long first, long long end, T v[16], bool& bad) {
+    if constexpr (GATHER) {
+        long long r[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            const long long j = first + (long long)k * 256;
+            r[k] = j < end ? rows[j] : 0;
+        }
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            const bool in = first + (long long)k * 256 < end;
+            const bool ok = r[k] >= 0 && r[k] < nx;
+            bad |= in && !ok;
+            v[k] = (in && ok) ? src[r[k]] : T(0);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            const long long j = first + (long long)k * 256;
+            v[k] = j < end ? src[j] : T(0);
+        }
+    }
+}
+
 // Segments by size class, so that each is reduced by the narrowest unit that
 // reproduces the tile tree exactly: sizes 0-1, 2, 3-4, 5-8, 9-16, 17-32
 // (classes 0-5), 33-4096 (6) and longer (7).
@@ -105,73 +134,92 @@ __global__ void k_seg_class_ids(const long long* __restrict__ starts, long long 
     if (g < ng) ids[sbase[c] + local] = (unsigned)g;
 }
 
-// Segments of classes 0-6 in one launch, one warp-sized unit of work per
-// warp.  Class c <= 5 (at most P = 2^c elements): the segment's elements sit
-// in lanes 0..m-1 of warp 0 of the 256-lane tile and every other lane and
-// warp holds the identity, so the tile tree reduces to the xor butterfly
-// over the first P lanes; a warp reduces 32 / P such segments in sub-warps
-// of P lanes.  Class 6 (33 to 4096 elements): one warp walks the tile's 8
-// virtual warps.
+// Segments of classes 0-5 in one launch.  Class c (at most P = 2^c
+// elements): the segment's elements sit in lanes 0..m-1 of warp 0 of the
+// 256-lane tile and every other lane and warp holds the identity, so the
+// tile tree reduces to the xor butterfly over the first P lanes; a warp
+// reduces 32 / P such segments in sub-warps of P lanes.
 template <typename T, typename A, int OP, bool GATHER>
 __global__ void __launch_bounds__(256) k_seg_warps(const T* __restrict__ src, const long long* __restrict__ rows,
                                                    long long nx, const long long* __restrict__ starts, long long ng,
                                                    long long total, const unsigned* __restrict__ ids,
                                                    const unsigned* __restrict__ cnt, A ident, A* __restrict__ out,
                                                    unsigned* derr) {
-    __shared__ long long wfirst[8];  // first warp of each class; wfirst[7] = warps in all
-    __shared__ unsigned cfirst[7];   // first id of each class
+    __shared__ long long wfirst[7];  // first warp of each class 0-5; wfirst[6] = warps in all
+    __shared__ unsigned cfirst[6];   // first id of each class
     if (threadIdx.x == 0) {
         long long w = 0;
         unsigned o = 0;
-        for (int c = 0; c < 7; c++) {
+        for (int c = 0; c < 6; c++) {
             wfirst[c] = w;
             cfirst[c] = o;
-            const long long per = c < 6 ? (32 >> c) : 1;  // segments per warp
+            const long long per = 32 >> c;  // segments per warp
             w += ((long long)cnt[c] + per - 1) / per;
             o += cnt[c];
         }
-        wfirst[7] = w;
+        wfirst[6] = w;
     }
     __syncthreads();
     const unsigned lane = lane_id();
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
     bool bad = false;
-    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < wfirst[7]; w += warps) {
+    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < wfirst[6]; w += warps) {
         int c = 0;
-        while (c < 6 && w >= wfirst[c + 1]) c++;
-        if (c < 6) {
-            const int P = 1 << c;
-            const unsigned q = lane >> c, j = lane & (P - 1);
-            const long long k = (w - wfirst[c]) * (32 >> c) + q;
-            A acc = ident;
-            long long g = -1;
-            if (k < (long long)cnt[c]) {
-                g = ids[cfirst[c] + k];
-                const long long s = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total;
-                if ((long long)j < e - s) acc = sop<A, OP>(ident, (A)seg_elem<T, GATHER>(src, rows, nx, s + j, bad));
-            }
-            for (int o = P >> 1; o > 0; o >>= 1) acc = sop<A, OP>(acc, __shfl_xor_sync(0xffffffffu, acc, o));
-            if (j == 0 && g >= 0) out[g] = acc;
-        } else {
-            const long long g = ids[cfirst[6] + (w - wfirst[6])];
-            const long long s = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total, m = e - s;
-            A ws[8];
+        while (c < 5 && w >= wfirst[c + 1]) c++;
+        const int P = 1 << c;
+        const unsigned q = lane >> c, j = lane & (P - 1);
+        const long long k = (w - wfirst[c]) * (32 >> c) + q;
+        A acc = ident;
+        long long g = -1;
+        if (k < (long long)cnt[c]) {
+            g = ids[cfirst[c] + k];
+            const long long s = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total;
+            if ((long long)j < e - s) acc = sop<A, OP>(ident, (A)seg_elem<T, GATHER>(src, rows, nx, s + j, bad));
+        }
+        for (int o = P >> 1; o > 0; o >>= 1) acc = sop<A, OP>(acc, __shfl_xor_sync(0xffffffffu, acc, o));
+        if (j == 0 && g >= 0) out[g] = acc;
+    }
+    if (bad) flag_error(derr, DERR_INDEX);
+}
+
+// Class 6 (33 to 4096 elements): one warp per segment walks the tile's 8
+// virtual warps, each lane's 16 elements loaded before they are added in order.
+template <typename T, typename A, int OP, bool GATHER>
+__global__ void __launch_bounds__(256) k_seg_mid(const T* __restrict__ src, const long long* __restrict__ rows,
+                                                 long long nx, const long long* __restrict__ starts, long long ng,
+                                                 long long total, const unsigned* __restrict__ ids,
+                                                 const unsigned* __restrict__ cnt, A ident, A* __restrict__ out,
+                                                 unsigned* derr) {
+    __shared__ unsigned first;
+    if (threadIdx.x == 0) {
+        unsigned o = 0;
+        for (int c = 0; c < 6; c++) o += cnt[c];
+        first = o;
+    }
+    __syncthreads();
+    const long long n6 = cnt[6];
+    const unsigned lane = lane_id();
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    bool bad = false;
+    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n6; w += warps) {
+        const long long g = ids[first + w];
+        const long long s = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total, m = e - s;
+        A ws[8];
 #pragma unroll
-            for (int v = 0; v < 8; v++) ws[v] = ident;
-            for (int v = 0; v < 8 && v * 32 < m; v++) {  // virtual warp v of the 256-lane tile
-                A acc = ident;
-                for (int k = 0; k < 16; k++) {
-                    long long j = (long long)k * 256 + v * 32 + lane;
-                    if (j >= m) break;
-                    acc = sop<A, OP>(acc, (A)seg_elem<T, GATHER>(src, rows, nx, s + j, bad));
-                }
-                ws[v] = swarp<A, OP>(acc);
-            }
-            if (lane == 0) {
-                A w01 = sop<A, OP>(ws[0], ws[1]), w23 = sop<A, OP>(ws[2], ws[3]);
-                A w45 = sop<A, OP>(ws[4], ws[5]), w67 = sop<A, OP>(ws[6], ws[7]);
-                out[g] = sop<A, OP>(sop<A, OP>(w01, w23), sop<A, OP>(w45, w67));
-            }
+        for (int v = 0; v < 8; v++) ws[v] = ident;
+        for (int v = 0; v < 8 && v * 32 < m; v++) {  // virtual warp v of the 256-lane tile
+            T x[16];
+            seg_load16<T, GATHER>(src, rows, nx, s + v * 32 + lane, e, x, bad);
+            A acc = ident;
+#pragma unroll
+            for (int k = 0; k < 16; k++)
+                if ((long long)k * 256 + v * 32 + lane < m) acc = sop<A, OP>(acc, (A)x[k]);
+            ws[v] = swarp<A, OP>(acc);
+        }
+        if (lane == 0) {
+            A w01 = sop<A, OP>(ws[0], ws[1]), w23 = sop<A, OP>(ws[2], ws[3]);
+            A w45 = sop<A, OP>(ws[4], ws[5]), w67 = sop<A, OP>(ws[6], ws[7]);
+            out[g] = sop<A, OP>(sop<A, OP>(w01, w23), sop<A, OP>(w45, w67));
         }
     }
     if (bad) flag_error(derr, DERR_INDEX);
@@ -195,12 +243,12 @@ __global__ void __launch_bounds__(256) k_seg_chunk(const T* __restrict__ src, co
     const long long s = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total;
     const long long base = s + (c - (long long)chunk0[lo]) * TILE_SUM;
     bool bad = false;
+    T v[16];
+    seg_load16<T, GATHER>(src, rows, nx, base + threadIdx.x, e, v, bad);
     A acc = ident;
-#pragma unroll 4
-    for (int k = 0; k < 16; k++) {
-        long long j = base + k * 256 + threadIdx.x;
-        if (j < e) acc = sop<A, OP>(acc, (A)seg_elem<T, GATHER>(src, rows, nx, j, bad));
-    }
+#pragma unroll
+    for (int k = 0; k < 16; k++)
+        if (base + k * 256 + threadIdx.x < e) acc = sop<A, OP>(acc, (A)v[k]);
     acc = swarp<A, OP>(acc);
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
     __syncthreads();
@@ -270,6 +318,8 @@ static I seg_reduce(const T* src, const long long* rows, long long nx, const lon
     }
     HG_LAUNCH("seg_warps", gcap(ng * 4), 256, 0, (k_seg_warps<T, A, OP, GATHER>), src, rows, nx, starts, ng, total, ids,
               ccnt, ident, out, g_derr);
+    HG_LAUNCH("seg_mid", gcap(ng), 256, 0, (k_seg_mid<T, A, OP, GATHER>), src, rows, nx, starts, ng, total, ids, ccnt,
+              ident, out, g_derr);
     long long nbig = 0;
     unsigned long long nchunks = 0;
     const long long *big, *pstarts;
