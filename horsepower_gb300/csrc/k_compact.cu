@@ -145,6 +145,52 @@ __global__ void __launch_bounds__(CT_THREADS) k_compact_scatter(const uint8_t* _
     }
 }
 
+// Single-column scatter with the element size fixed at compile time (ES = 0:
+// the row number as i64, for @where; the only instance launched).  The
+// tile's kept values are staged in shared memory in output order, then
+// written out by consecutive threads to consecutive addresses, so every
+// output line is written whole.
+template <int ES>
+__global__ void __launch_bounds__(CT_THREADS) k_compact_scatter1(const uint8_t* __restrict__ mask, long long n,
+                                                                 const void* __restrict__ src, void* __restrict__ dst,
+                                                                 const unsigned long long* __restrict__ offs) {
+    using E = typename std::conditional<ES == 1, uint8_t,
+              typename std::conditional<ES == 2, uint16_t,
+              typename std::conditional<ES == 4, uint32_t, unsigned long long>::type>::type>::type;
+    __shared__ __align__(16) uint8_t smask[CT_TILE];
+    __shared__ __align__(16) E sbuf[CT_TILE];
+    __shared__ unsigned warp_tot[8];
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    const long long base = (long long)blockIdx.x * CT_TILE;
+    const int lofs = (int)threadIdx.x * 16;
+    const uint4 m4 = load_mask16(mask, n, base, lofs);
+    *reinterpret_cast<uint4*>(smask + lofs) = m4;
+    unsigned c = warp_sum(__popc(m4.x) + __popc(m4.y) + __popc(m4.z) + __popc(m4.w));
+    if (lane == 0) warp_tot[warp] = c;
+    __syncthreads();
+    unsigned loc = 0, total = 0;
+    for (unsigned w = 0; w < 8; w++) {
+        if (w < warp) loc += warp_tot[w];
+        total += warp_tot[w];
+    }
+    const int wbase = (int)warp * 512;
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        const int li = wbase + k * 32 + (int)lane;
+        const bool sel = smask[li] != 0;
+        const unsigned bal = __ballot_sync(0xffffffffu, sel);
+        if (sel) {
+            const unsigned o = loc + __popc(bal & lanemask_lt());
+            if constexpr (ES == 0) sbuf[o] = (unsigned long long)(base + li);
+            else sbuf[o] = reinterpret_cast<const E*>(src)[base + li];
+        }
+        loc += __popc(bal);
+    }
+    __syncthreads();
+    E* out = reinterpret_cast<E*>(dst) + offs[blockIdx.x];
+    for (unsigned k = threadIdx.x; k < total; k += CT_THREADS) out[k] = sbuf[k];
+}
+
 // Compaction in two passes with no dependence between tiles: count per
 // tile, scan the counts, scatter.  (A single pass with a decoupled look-back
 // across tiles measured several times slower here: the tiles waited on the
@@ -158,7 +204,11 @@ static I compact(const uint8_t* mask, long long n, CompactCols& cols, long long*
     if (!counts || !offs) return E_DEVICE_OOM;
     HG_LAUNCH("compact_count", (unsigned)ntiles, CT_THREADS, 0, k_compact_count, mask, n, counts);
     HG_LAUNCH("compact_scan", 1, 1024, 0, k_scan_counts, counts, ntiles, offs);
-    HG_LAUNCH("compact", (unsigned)ntiles, CT_THREADS, 0, k_compact_scatter, mask, n, cols, offs);
+    if (cols.ncol == 1 && cols.es[0] == 0) {  // @where: staged row numbers (measured 0.094 -> 0.074 ms at 60M)
+        HG_LAUNCH("compact", (unsigned)ntiles, CT_THREADS, 0, k_compact_scatter1<0>, mask, n, cols.src[0], cols.dst[0], offs);
+    } else {  // value columns: direct stores measured faster than staging for 8-byte values
+        HG_LAUNCH("compact", (unsigned)ntiles, CT_THREADS, 0, k_compact_scatter, mask, n, cols, offs);
+    }
     HG_CHECK(last_launch_error());
     unsigned long long h = 0;
     HG_CU(cudaMemcpyAsync(&h, offs + ntiles, 8, cudaMemcpyDeviceToHost, g_stream));
