@@ -66,6 +66,8 @@ long long out_mark();                          // output-arena cursor (for undoi
 void out_rewind(long long m);
 void* salloc(size_t bytes);                    // scratch arena
 I scratch_reserve(size_t bytes);               // pre-allocates a scratch chunk of that size
+I out_reserve(size_t bytes);                   // ... an output-arena chunk
+I host_reserve(size_t bytes);                  // ... a pinned host-arena chunk
 void* halloc(size_t bytes);                    // pinned host arena
 struct ScratchScope {                          // rewinds the scratch arena on exit
     long long mark;

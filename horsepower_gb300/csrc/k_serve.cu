@@ -596,8 +596,13 @@ I hgpuServerCreate(hgpuServer* out, const hgpuServeTables* tables, L hbm_budget_
     s->budget = hbm_budget_bytes > 0 ? hbm_budget_bytes : (L)32 << 30;
     s->max_step = max_step_requests;
     // the budget is the scratch the admitted requests of a step may hold:
-    // reserve it now, so that no step waits on a device allocation
+    // reserve it now, so that no step waits on a device allocation.  The
+    // output arena (step results) and the pinned host arena (list nodes,
+    // copied-out rows) get chunks up front too: pinning a fresh host chunk
+    // mid-run took tens of milliseconds and set a step's latency.
     I rc = scratch_reserve((size_t)s->budget);
+    if (!rc) rc = out_reserve((size_t)s->budget / 4);
+    if (!rc) rc = host_reserve((size_t)1 << 30);
     if (!rc && s->t.ndim > 0 && s->t.dim_date) rc = build_cum(s->t.dim_date, 0, s->t.ndim, 1 << 20, &s->dim_dates);
     if (!rc && s->t.norder > 0 && s->t.o_key) rc = build_cum(s->t.o_key, 1, s->t.norder, 1 << 26, &s->keys);
     if (rc) {

@@ -205,6 +205,12 @@ I scratch_reserve(size_t bytes) {
     return g_scratch->reserve(bytes) ? 0 : set_error(E_DEVICE_OOM, "scratch arena: cannot reserve %zu bytes", bytes);
 }
 void* halloc(size_t bytes) { return g_host->alloc(bytes); }
+I out_reserve(size_t bytes) {
+    return g_out->reserve(bytes) ? 0 : set_error(E_DEVICE_OOM, "output arena: cannot reserve %zu bytes", bytes);
+}
+I host_reserve(size_t bytes) {
+    return g_host->reserve(bytes) ? 0 : set_error(E_DEVICE_OOM, "host arena: cannot reserve %zu bytes", bytes);
+}
 ScratchScope::ScratchScope() : mark(g_scratch ? g_scratch->mark() : 0) {}
 ScratchScope::~ScratchScope() {
     if (g_scratch) g_scratch->rewind(mark);
