@@ -221,12 +221,18 @@ def run_gb300(args, rank, ws, dist):
         pinned[key] = pv
     h2d = sum(v.len * ESIZE[v.typ] for v in pinned.values())
 
+    # uploads in the order the query first reads the columns; each runs on the
+    # copy stream and a builtin waits only for the columns it reads
+    first_use = [("dim", "date"), ("dim", "pk"), ("fact", "fk"), ("fact", "flag"), ("fact", "status"),
+                 ("fact", "qty"), ("fact", "price"), ("fact", "disc")]
+    upload_order = [k for k in first_use if k in pinned] + [k for k in pinned if k not in first_use]
+
     def e2e_step():
         mark = Lb.getHeapOffset()
         dv = {}
-        for key, pv in pinned.items():
+        for key in upload_order:
             z = V0()
-            Lb.hgpuToDevice(C.byref(z), C.byref(pv))
+            Lb.hgpuToDeviceAsync(C.byref(z), C.byref(pinned[key]))
             dv[key] = z
         out = P.join_group(gpu, {k: dv[("dim", k)] for k in dim}, {k: dv[("fact", k)] for k in fact})
         vals = [gpu.to_py(o) for o in out]

@@ -75,6 +75,7 @@ struct ScratchScope {                          // rewinds the scratch arena on e
     ~ScratchScope();
 };
 bool is_device_ptr(const void* p);             // payload readable by kernels without staging
+void wait_pending(const void* p);              // library stream waits for an upload into p, if one is in flight
 bool host_readable(const void* p);             // payload readable by host code without a copy
 int residency();                               // HGPU_RESIDENT_DEVICE or HGPU_RESIDENT_HOST
 

@@ -18,6 +18,7 @@ static std::vector<std::string>* g_sym_names;
 namespace hg {
 
 cudaStream_t g_stream = nullptr;
+static cudaStream_t g_copy_stream = nullptr;  // asynchronous uploads (hgpuToDeviceAsync)
 int g_sms = 0;
 unsigned* g_derr = nullptr;
 int g_reduce_mode = 1;
@@ -176,6 +177,7 @@ I ensure_init() {
     HG_CU(cudaSetDevice(0));
     HG_CU(cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, 0));
     HG_CU(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+    HG_CU(cudaStreamCreateWithFlags(&g_copy_stream, cudaStreamNonBlocking));
     HG_CU(cudaMalloc((void**)&g_derr, 256));
     HG_CU(cudaMemset(g_derr, 0, 256));
     if (!g_out) g_out = new Arena(env_mb("HGPU_DEVICE_CHUNK_MB", 4096), false);
@@ -196,7 +198,9 @@ void* dalloc(size_t bytes) { return g_out->alloc(bytes); }
 bool dshrink(void* p, size_t new_bytes) { return g_out->shrink(p, new_bytes); }
 long long out_mark() { return g_out->mark(); }
 static void prune_registries();
+void wait_all_pending();
 void out_rewind(long long m) {
+    wait_all_pending();
     g_out->rewind(m);
     prune_registries();
 }
@@ -250,9 +254,49 @@ int esize(I t) {
     }
 }
 
+// ------------------------------------------------------- asynchronous uploads
+// hgpuToDeviceAsync copies on a second stream; the library stream waits on a
+// copy's event only when a builtin first reads its destination (in_ptr,
+// read_elem0, a copy out), or at hgpuWait / hgpuSync / setHeapOffset, so
+// kernels on other inputs run while the copy is in flight.
+struct Pending { const char* p; size_t bytes; cudaEvent_t ev; };
+static std::vector<Pending> g_pending;
+static std::vector<cudaEvent_t> g_upload_events;
+static cudaEvent_t pool_event() {
+    if (!g_upload_events.empty()) {
+        cudaEvent_t e = g_upload_events.back();
+        g_upload_events.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    return e;
+}
+void wait_pending(const void* p) {
+    if (g_pending.empty() || !p) return;
+    for (size_t i = 0; i < g_pending.size();) {
+        const Pending& q = g_pending[i];
+        if ((const char*)p >= q.p && (const char*)p < q.p + q.bytes) {
+            cudaStreamWaitEvent(g_stream, q.ev, 0);
+            g_upload_events.push_back(q.ev);
+            g_pending.erase(g_pending.begin() + (long)i);
+        } else {
+            i++;
+        }
+    }
+}
+void wait_all_pending() {
+    for (const Pending& q : g_pending) {
+        cudaStreamWaitEvent(g_stream, q.ev, 0);
+        g_upload_events.push_back(q.ev);
+    }
+    g_pending.clear();
+}
+
 I in_ptr(V x, const void** p) {
     size_t nb = (size_t)x->len * esize(x->typ);
     if (x->len == 0) { *p = nullptr; return 0; }
+    if (!is_inline(x)) wait_pending(x->g);
     if (!is_inline(x) && is_device_ptr(x->g)) { *p = x->g; return 0; }
     void* d = salloc(nb);
     if (!d) return E_DEVICE_OOM;
@@ -264,6 +308,7 @@ I in_ptr(V x, const void** p) {
 I read_elem0(V x, uint64_t* bits) {
     *bits = 0;
     if (x->len < 1) return E_LENGTH;
+    if (!is_inline(x)) wait_pending(x->g);
     int es = esize(x->typ);
     if (is_inline(x) || !is_device_ptr(x->g) || g_host->contains(x->g)) {
         memcpy(bits, x->g, es);
@@ -343,6 +388,7 @@ static I to_host_rec(V z, V x, bool in_place) {
         return 0;
     }
     if (!is_basic(x->typ)) return set_error(E_NOT_IMPL, "hgpuToHost: type %d", x->typ);
+    if (!is_inline(x)) wait_pending(x->g);
     V0 hdr = *x;
     if (z != x) *z = hdr;
     if (is_inline(x)) {
@@ -545,7 +591,8 @@ L getHeapOffset(void) {
 L setHeapOffset(L cur) {
     if (ensure_init()) return cur;
     if (cur < 0 || (size_t)cur >= g_marks.size()) return cur;
-    // work already queued may still read the region being released
+    // work already queued (and uploads in flight) may still use the region being released
+    wait_all_pending();
     cudaStreamSynchronize(g_stream);
     g_out->rewind(g_marks[(size_t)cur].first);
     g_host->rewind(g_marks[(size_t)cur].second);
@@ -625,6 +672,32 @@ I hgpuToDevice(V z, V x) {
     return to_device_rec(z, x);
 }
 
+I hgpuToDeviceAsync(V z, V x) {
+    HG_CHECK(ensure_init());
+    if (!is_basic(x->typ) || x->len <= 1) return to_device_rec(z, x);
+    const size_t nb = (size_t)x->len * esize(x->typ);
+    void* d = dalloc(nb);
+    if (!d) return E_DEVICE_OOM;
+    cudaEvent_t before = pool_event(), done = pool_event();
+    if (!before || !done) return set_error(E_DEVICE, "hgpuToDeviceAsync: no event");
+    // the destination may be arena memory that queued library work still uses
+    HG_CU(cudaEventRecord(before, g_stream));
+    HG_CU(cudaStreamWaitEvent(g_copy_stream, before, 0));
+    HG_CU(cudaMemcpyAsync(d, x->g, nb, cudaMemcpyDefault, g_copy_stream));
+    HG_CU(cudaEventRecord(done, g_copy_stream));
+    g_upload_events.push_back(before);
+    g_pending.push_back({(const char*)d, nb, done});
+    *z = *x;
+    z->g = (G)d;
+    return 0;
+}
+
+I hgpuWait(V z) {
+    HG_CHECK(ensure_init());
+    if (z && !is_inline(z)) wait_pending(z->g);
+    return 0;
+}
+
 I hgpuIsDevice(V x) {
     if (ensure_init()) return 0;
     if (!(is_basic(x->typ) || x->typ == H_Y) || is_inline(x) || x->len < 1) return 0;
@@ -636,6 +709,7 @@ I hgpuIsDevice(V x) {
 
 I hgpuSync(void) {
     HG_CHECK(ensure_init());
+    wait_all_pending();
     HG_CU(cudaStreamSynchronize(g_stream));
     return check_device_errors();
 }

@@ -57,12 +57,14 @@ def join_group(L, dim, fact, lo=D.WIN_LO, hi=D.WIN_HI):
     fi = L.call("pfnIndex", j, L.scalar(1, H_L))
     flag = L.call("pfnIndex", fact["flag"], fi)
     status = L.call("pfnIndex", fact["status"], fi)
-    qty = L.call("pfnIndex", fact["qty"], fi)
-    price = L.call("pfnIndex", fact["price"], fi)
-    disc = L.call("pfnIndex", fact["disc"], fi)
     g = L.call("pfnGroup", L.list([flag, status]))
     keys = L.call("pfnKeys", g)
     vals = L.call("pfnValues", g)
+    # the measure columns are gathered last: uploads of them still in flight
+    # (hgpuToDeviceAsync) overlap everything above
+    qty = L.call("pfnIndex", fact["qty"], fi)
+    price = L.call("pfnIndex", fact["price"], fi)
+    disc = L.call("pfnIndex", fact["disc"], fi)
     out_flag = L.call("pfnIndex", flag, keys)
     out_status = L.call("pfnIndex", status, keys)
     sum_qty = group_agg(L, "pfnSum", qty, vals)

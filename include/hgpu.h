@@ -320,6 +320,14 @@ I    hgpuGetResidency(void);
 I    hgpuToHost(V z, V x);
 I    hgpuToDevice(V z, V x);
 I    hgpuIsDevice(V x);               /* 1 when x's payload lives in HBM */
+/* Asynchronous upload of a vector: the copy runs on a second stream, and the
+ * library stream waits for it only when a builtin first reads z (or at
+ * hgpuWait(z), hgpuSync, setHeapOffset), so kernels on inputs already in HBM
+ * overlap the copy.  x's host memory must stay unchanged until then.  The
+ * batched and served entry points take device pointers: call hgpuWait on
+ * their inputs first. */
+I    hgpuToDeviceAsync(V z, V x);
+I    hgpuWait(V z);
 I    hgpuSync(void);                  /* wait for the library stream; returns sticky device errors */
 void*hgpuStream(void);                /* the cudaStream_t every kernel is launched on */
 const char *hgpuLastError(void);      /* text of the last error (thread-local) */

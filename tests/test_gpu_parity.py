@@ -240,6 +240,36 @@ def test_join_group_pipeline(libs):
         assert np.allclose(a[k], b[k], rtol=RTOL, atol=0)
 
 
+def test_join_group_async_uploads(libs):
+    """The same query on columns uploaded with hgpuToDeviceAsync (copies on a
+    second stream, builtins waiting per column) equals the synchronous
+    upload, bit for bit, across heap rewinds that release the uploads."""
+    import ctypes as C
+    from horsepower_gb300 import data as D, plans as P
+    from horsepower_gb300.abi import V0
+    gpu, _ = libs
+    dim, fact = D.join_tables(6_000_000, 1_500_000, seed=6)
+    hd, hf = P.host_nodes(gpu, dim, P.DIM_TYPES), P.host_nodes(gpu, fact, P.FACT_TYPES)
+    Lb = gpu.lib
+    Lb.getHeapOffset.restype = C.c_longlong
+    results = []
+    for fn in (Lb.hgpuToDevice, Lb.hgpuToDeviceAsync, Lb.hgpuToDeviceAsync):
+        mark = Lb.getHeapOffset()
+        up = {}
+        for part, nodes in (("dim", hd), ("fact", hf)):
+            for k, v in nodes.items():
+                z = V0()
+                assert fn(C.byref(z), C.byref(v)) == 0
+                up[(part, k)] = z
+        r = P.join_group(gpu, {k: up[("dim", k)] for k in hd}, {k: up[("fact", k)] for k in hf})
+        results.append([gpu.to_py(v) for v in r])
+        Lb.setHeapOffset(C.c_longlong(mark))
+    for other in results[1:]:
+        for a, b in zip(results[0], other):
+            assert a.dtype == b.dtype and np.array_equal(a, b)
+    gpu.free_inputs()
+
+
 @pytest.mark.parametrize("s", [0.05, 0.07, 0.0, -0.0, 1e-13, -1e-13, 5e-14, 24.0, 1e300, -1e300, 5e-324,
                                float("inf"), float("-inf"), float("nan"), 123456.789])
 def test_compare_f64_scalar_edges(libs, s):
