@@ -675,6 +675,8 @@ static I order_columns_exact(int nc, V* cols, const void** ptrs, const B* asc, l
 }
 
 // Builds the @group dict from a sorted permutation.
+static I group_finish(V z, long long* starts, long long G, long long* perm, long long n);
+
 static I group_dict(V z, const SortResult& r, long long n, const ColSet* cols) {
     uint8_t* flags = (uint8_t*)salloc((size_t)(n > 0 ? n : 1));
     long long* starts = (long long*)salloc((size_t)(n > 0 ? n : 1) * 8);
@@ -692,8 +694,6 @@ static I group_dict(V z, const SortResult& r, long long n, const ColSet* cols) {
         if (G > 0) HG_CU(cudaMemcpyAsync(keep, starts, (size_t)G * 8, cudaMemcpyDeviceToDevice, g_stream));
         starts = keep;
     }
-    HG_CHECK(init_list(z, H_N, 2));
-    V0* kv = host_nodes(z);
     // permutation as i64 (the rows of every group, concatenated)
     long long* perm = nullptr;
     if (n > 0) {
@@ -701,6 +701,14 @@ static I group_dict(V z, const SortResult& r, long long n, const ColSet* cols) {
         if (!perm) return E_DEVICE_OOM;
         HG_LAUNCH("widen", gcap(n), 256, 0, k_widen, r.perm, n, perm, 0);
     }
+    return group_finish(z, starts, G, perm, n);
+}
+
+// The dict of a grouping from its G group starts and its permutation (both
+// i64, output arena): keys = each group's first row, values = the row lists.
+static I group_finish(V z, long long* starts, long long G, long long* perm, long long n) {
+    HG_CHECK(init_list(z, H_N, 2));
+    V0* kv = host_nodes(z);
     void* dkeys;
     HG_CHECK(alloc_out(&kv[0], H_L, G, &dkeys));
     HG_CHECK(init_list(&kv[1], H_G, G));
@@ -753,6 +761,131 @@ static I sort_char(const void* p, long long n, SortResult* r) {
     return sort_by_spec(s, n, 8, r);
 }
 
+// ---- two char columns with few distinct (c0, c1) pairs: a counting sort.
+// Codes are c0 << 8 | c1 (unsigned bytes), the key order the radix path
+// sorts by; a code's bucket is its rank among the codes present.  Per
+// 4096-row tile: bucket counts (pass 1), one scan over (bucket, tile), then
+// each row's stable position (pass 2), written straight as an i64 row list.
+constexpr int TS_TILE = 4096, TS_MAXG = 256;
+__global__ void k_trie_present(const uint8_t* __restrict__ c0, const uint8_t* __restrict__ c1, long long n,
+                               unsigned* __restrict__ bitmap) {
+    __shared__ unsigned sb[2048];
+    for (int i = threadIdx.x; i < 2048; i += blockDim.x) sb[i] = 0;
+    __syncthreads();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const unsigned code = ((unsigned)c0[i] << 8) | c1[i];
+        atomicOr(&sb[code >> 5], 1u << (code & 31));
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 2048; i += blockDim.x)
+        if (sb[i]) atomicOr(&bitmap[i], sb[i]);
+}
+struct TrieRank { unsigned bits[2048]; unsigned short wpre[2048]; };
+__device__ __forceinline__ unsigned trie_bucket(const TrieRank& t, unsigned code) {
+    const unsigned w = code >> 5;
+    return t.wpre[w] + __popc(t.bits[w] & ((1u << (code & 31)) - 1u));
+}
+__device__ void load_rank(TrieRank& s, const TrieRank* g) {
+    for (int i = threadIdx.x; i < 2048; i += blockDim.x) { s.bits[i] = g->bits[i]; s.wpre[i] = g->wpre[i]; }
+}
+// pass 1: counts[b * T + tile]
+__global__ void __launch_bounds__(256) k_trie_count(const uint8_t* __restrict__ c0, const uint8_t* __restrict__ c1,
+                                                    long long n, const TrieRank* __restrict__ rk, int G, long long T,
+                                                    unsigned* __restrict__ counts) {
+    __shared__ TrieRank r;
+    __shared__ unsigned cnt[TS_MAXG];
+    load_rank(r, rk);
+    for (int i = threadIdx.x; i < G; i += blockDim.x) cnt[i] = 0;
+    __syncthreads();
+    const long long base = (long long)blockIdx.x * TS_TILE;
+    for (int k = threadIdx.x; k < TS_TILE; k += blockDim.x) {
+        const long long i = base + k;
+        const bool in = i < n;
+        const unsigned b = in ? trie_bucket(r, ((unsigned)c0[i] << 8) | c1[i]) : 0xffffffffu;
+        const unsigned peers = __match_any_sync(0xffffffffu, b);
+        if (in && (int)lane_id() == __ffs(peers) - 1) atomicAdd(&cnt[b], __popc(peers));
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < G; b += blockDim.x) counts[(long long)b * T + blockIdx.x] = cnt[b];
+}
+// pass 2: perm[offs[b * T + tile] + rank of the row among the tile's rows of bucket b] = row
+__global__ void __launch_bounds__(256) k_trie_scatter(const uint8_t* __restrict__ c0, const uint8_t* __restrict__ c1,
+                                                      long long n, const TrieRank* __restrict__ rk, int G, long long T,
+                                                      const unsigned long long* __restrict__ offs,
+                                                      long long* __restrict__ perm) {
+    __shared__ TrieRank r;
+    __shared__ unsigned wcnt[8][TS_MAXG];  // per warp: rows of each bucket, then the warp's base
+    load_rank(r, rk);
+    const unsigned lane = lane_id(), w = threadIdx.x >> 5;
+    for (int b = lane; b < G; b += 32) wcnt[w][b] = 0;
+    __syncthreads();
+    const long long base = (long long)blockIdx.x * TS_TILE + (long long)w * (TS_TILE / 8);
+    unsigned bk[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) {  // warp w owns rows base .. base + 511, in order
+        const long long i = base + k * 32 + lane;
+        const bool in = i < n;
+        bk[k] = in ? trie_bucket(r, ((unsigned)c0[i] << 8) | c1[i]) : 0xffffffffu;
+        const unsigned peers = __match_any_sync(0xffffffffu, bk[k]);
+        if (in && (int)lane == __ffs(peers) - 1) wcnt[w][bk[k]] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < G; b += blockDim.x) {  // warps' exclusive bases per bucket
+        unsigned c = 0;
+        for (int ww = 0; ww < 8; ww++) { const unsigned h = wcnt[ww][b]; wcnt[ww][b] = c; c += h; }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        const long long i = base + k * 32 + lane;
+        const bool in = i < n;
+        const unsigned peers = __match_any_sync(0xffffffffu, bk[k]);
+        const int leader = __ffs(peers) - 1;
+        unsigned pre = 0;
+        if (in && (int)lane == leader) { pre = wcnt[w][bk[k]]; wcnt[w][bk[k]] = pre + __popc(peers); }
+        pre = __shfl_sync(0xffffffffu, pre, leader);
+        if (in) perm[offs[(long long)bk[k] * T + blockIdx.x] + pre + __popc(peers & lanemask_lt())] = i;
+        __syncwarp();
+    }
+}
+__global__ void k_trie_starts(const unsigned long long* __restrict__ offs, int G, long long T, long long* __restrict__ starts) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < G) starts[b] = (long long)offs[(long long)b * T];
+}
+
+// *done = 1 with the dict in z; 0 when too many pairs are present for the counting path
+static I trie_small(V z, const void* p0, const void* p1, long long n, int* done) {
+    *done = 0;
+    unsigned* bitmap = (unsigned*)salloc(2048 * 4);
+    if (!bitmap) return E_DEVICE_OOM;
+    HG_CU(cudaMemsetAsync(bitmap, 0, 2048 * 4, g_stream));
+    unsigned grid = grid_for(n, 256);
+    if (grid > (unsigned)g_sms * 4) grid = g_sms * 4;
+    HG_LAUNCH("trie_present", grid, 256, 0, k_trie_present, (const uint8_t*)p0, (const uint8_t*)p1, n, bitmap);
+    TrieRank hr;
+    HG_CU(cudaMemcpyAsync(hr.bits, bitmap, 2048 * 4, cudaMemcpyDeviceToHost, g_stream));
+    HG_CU(cudaStreamSynchronize(g_stream));
+    unsigned G = 0;
+    for (int i = 0; i < 2048; i++) { hr.wpre[i] = (unsigned short)G; G += (unsigned)__builtin_popcount(hr.bits[i]); }
+    if (G == 0 || G > (unsigned)TS_MAXG) return 0;
+    TrieRank* drk = (TrieRank*)salloc(sizeof(TrieRank));
+    const long long T = (n + TS_TILE - 1) / TS_TILE;
+    unsigned* counts = (unsigned*)salloc((size_t)G * (size_t)T * 4);
+    unsigned long long* offs = (unsigned long long*)salloc(((size_t)G * (size_t)T + 1) * 8);
+    long long* perm = (long long*)dalloc((size_t)n * 8);
+    long long* starts = (long long*)dalloc((size_t)G * 8);
+    if (!drk || !counts || !offs || !perm || !starts) return E_DEVICE_OOM;
+    HG_CU(cudaMemcpyAsync(drk, &hr, sizeof(TrieRank), cudaMemcpyHostToDevice, g_stream));
+    HG_LAUNCH("trie_count", (unsigned)T, 256, 0, k_trie_count, (const uint8_t*)p0, (const uint8_t*)p1, n, drk, (int)G, T, counts);
+    HG_CHECK(scan_exclusive(counts, (long long)G * T, offs, nullptr));
+    HG_LAUNCH("trie_scatter", (unsigned)T, 256, 0, k_trie_scatter, (const uint8_t*)p0, (const uint8_t*)p1, n, drk, (int)G, T, offs, perm);
+    HG_LAUNCH("trie_starts", 1, 256, 0, k_trie_starts, offs, (int)G, T, starts);
+    HG_CHECK(last_launch_error());
+    *done = 1;
+    return group_finish(z, starts, (long long)G, perm, n);
+}
+
 }  // namespace hg
 
 using namespace hg;
@@ -767,6 +900,11 @@ I pfnGroupTrie(V z, V x) {
     const void *p0, *p1;
     HG_CHECK(in_ptr(&c[0], &p0));
     HG_CHECK(in_ptr(&c[1], &p1));
+    if (n >= TS_TILE) {
+        int done = 0;
+        HG_CHECK(trie_small(z, p0, p1, n, &done));
+        if (done) return 0;
+    }
     KeySpec s{};
     s.ncol = 2;
     s.col[0] = p0; s.typ[0] = H_C; s.xf[0] = XF_UBYTE; s.shift[0] = 8;
