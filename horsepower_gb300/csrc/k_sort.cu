@@ -541,7 +541,7 @@ static I col_minmax(const void* p, I typ, long long n, long long* mn, long long*
 }
 
 // Single-column keys following the reference's radix rules (i32 / i64).
-static I sort_int_column(V x, const void* p, long long n, SortResult* r) {
+static I sort_int_column(V x, const void* p, long long n, SortResult* r, const long long* known_mm = nullptr) {
     KeySpec s{};
     s.ncol = 1;
     s.col[0] = p;
@@ -555,7 +555,8 @@ static I sort_int_column(V x, const void* p, long long n, SortResult* r) {
     // some value has (x >> 32) > 0 exactly when the maximum is >= 2^32; the
     // low 32 bits are injective when every value lies in one 2^32-wide range
     long long mn = 0, mx = 0;
-    if (n > 0) HG_CHECK(col_minmax(p, H_L, n, &mn, &mx));
+    if (known_mm) { mn = known_mm[0]; mx = known_mm[1]; }
+    else if (n > 0) HG_CHECK(col_minmax(p, H_L, n, &mn, &mx));
     const bool f = n > 0 && mx >= (1LL << 32);
     s.xf[0] = f ? XF_RAW64 : XF_LOW32;
     r->key_injective = f || n == 0 || ((unsigned long long)mx - (unsigned long long)mn) < (1ull << 32);
@@ -761,19 +762,32 @@ static I sort_char(const void* p, long long n, SortResult* r) {
     return sort_by_spec(s, n, 8, r);
 }
 
-// ---- two char columns with few distinct (c0, c1) pairs: a counting sort.
-// Codes are c0 << 8 | c1 (unsigned bytes), the key order the radix path
-// sorts by; a code's bucket is its rank among the codes present.  Per
-// 4096-row tile: bucket counts (pass 1), one scan over (bucket, tile), then
-// each row's stable position (pass 2), written straight as an i64 row list.
+// ---- groupings with few distinct keys of a 16-bit code: a counting sort.
+// The code of a row keeps the key order the radix path sorts by: c0 << 8 |
+// c1 for two char columns (unsigned bytes), v - min for a non-negative
+// integer column spanning fewer than 65536 values.  A code's bucket is its
+// rank among the codes present.  Per 4096-row tile: bucket counts (pass 1),
+// one scan over (bucket, tile), then each row's stable position (pass 2),
+// written straight as an i64 row list.
 constexpr int TS_TILE = 4096, TS_MAXG = 256;
-__global__ void k_trie_present(const uint8_t* __restrict__ c0, const uint8_t* __restrict__ c1, long long n,
-                               unsigned* __restrict__ bitmap) {
+struct CodeChars {
+    const uint8_t* c0;
+    const uint8_t* c1;
+    __device__ __forceinline__ unsigned operator()(long long i) const { return ((unsigned)c0[i] << 8) | c1[i]; }
+};
+template <typename T>
+struct CodeInt {
+    const T* p;
+    long long mn;
+    __device__ __forceinline__ unsigned operator()(long long i) const { return (unsigned)((long long)p[i] - mn); }
+};
+template <typename Code>
+__global__ void k_trie_present(Code code_of, long long n, unsigned* __restrict__ bitmap) {
     __shared__ unsigned sb[2048];
     for (int i = threadIdx.x; i < 2048; i += blockDim.x) sb[i] = 0;
     __syncthreads();
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const unsigned code = ((unsigned)c0[i] << 8) | c1[i];
+        const unsigned code = code_of(i);
         atomicOr(&sb[code >> 5], 1u << (code & 31));
     }
     __syncthreads();
@@ -789,9 +803,9 @@ __device__ void load_rank(TrieRank& s, const TrieRank* g) {
     for (int i = threadIdx.x; i < 2048; i += blockDim.x) { s.bits[i] = g->bits[i]; s.wpre[i] = g->wpre[i]; }
 }
 // pass 1: counts[b * T + tile]
-__global__ void __launch_bounds__(256) k_trie_count(const uint8_t* __restrict__ c0, const uint8_t* __restrict__ c1,
-                                                    long long n, const TrieRank* __restrict__ rk, int G, long long T,
-                                                    unsigned* __restrict__ counts) {
+template <typename Code>
+__global__ void __launch_bounds__(256) k_trie_count(Code code_of, long long n, const TrieRank* __restrict__ rk, int G,
+                                                    long long T, unsigned* __restrict__ counts) {
     __shared__ TrieRank r;
     __shared__ unsigned cnt[TS_MAXG];
     load_rank(r, rk);
@@ -801,7 +815,7 @@ __global__ void __launch_bounds__(256) k_trie_count(const uint8_t* __restrict__ 
     for (int k = threadIdx.x; k < TS_TILE; k += blockDim.x) {
         const long long i = base + k;
         const bool in = i < n;
-        const unsigned b = in ? trie_bucket(r, ((unsigned)c0[i] << 8) | c1[i]) : 0xffffffffu;
+        const unsigned b = in ? trie_bucket(r, code_of(i)) : 0xffffffffu;
         const unsigned peers = __match_any_sync(0xffffffffu, b);
         if (in && (int)lane_id() == __ffs(peers) - 1) atomicAdd(&cnt[b], __popc(peers));
     }
@@ -809,9 +823,9 @@ __global__ void __launch_bounds__(256) k_trie_count(const uint8_t* __restrict__ 
     for (int b = threadIdx.x; b < G; b += blockDim.x) counts[(long long)b * T + blockIdx.x] = cnt[b];
 }
 // pass 2: perm[offs[b * T + tile] + rank of the row among the tile's rows of bucket b] = row
-__global__ void __launch_bounds__(256) k_trie_scatter(const uint8_t* __restrict__ c0, const uint8_t* __restrict__ c1,
-                                                      long long n, const TrieRank* __restrict__ rk, int G, long long T,
-                                                      const unsigned long long* __restrict__ offs,
+template <typename Code>
+__global__ void __launch_bounds__(256) k_trie_scatter(Code code_of, long long n, const TrieRank* __restrict__ rk, int G,
+                                                      long long T, const unsigned long long* __restrict__ offs,
                                                       long long* __restrict__ perm) {
     __shared__ TrieRank r;
     __shared__ unsigned wcnt[8][TS_MAXG];  // per warp: rows of each bucket, then the warp's base
@@ -825,7 +839,7 @@ __global__ void __launch_bounds__(256) k_trie_scatter(const uint8_t* __restrict_
     for (int k = 0; k < 16; k++) {  // warp w owns rows base .. base + 511, in order
         const long long i = base + k * 32 + lane;
         const bool in = i < n;
-        bk[k] = in ? trie_bucket(r, ((unsigned)c0[i] << 8) | c1[i]) : 0xffffffffu;
+        bk[k] = in ? trie_bucket(r, code_of(i)) : 0xffffffffu;
         const unsigned peers = __match_any_sync(0xffffffffu, bk[k]);
         if (in && (int)lane == __ffs(peers) - 1) wcnt[w][bk[k]] += __popc(peers);
         __syncwarp();
@@ -854,15 +868,16 @@ __global__ void k_trie_starts(const unsigned long long* __restrict__ offs, int G
     if (b < G) starts[b] = (long long)offs[(long long)b * T];
 }
 
-// *done = 1 with the dict in z; 0 when too many pairs are present for the counting path
-static I trie_small(V z, const void* p0, const void* p1, long long n, int* done) {
+// *done = 1 with the dict in z; 0 when too many codes are present for the counting path
+template <typename Code>
+static I small_group(V z, Code code_of, long long n, int* done) {
     *done = 0;
     unsigned* bitmap = (unsigned*)salloc(2048 * 4);
     if (!bitmap) return E_DEVICE_OOM;
     HG_CU(cudaMemsetAsync(bitmap, 0, 2048 * 4, g_stream));
     unsigned grid = grid_for(n, 256);
     if (grid > (unsigned)g_sms * 4) grid = g_sms * 4;
-    HG_LAUNCH("trie_present", grid, 256, 0, k_trie_present, (const uint8_t*)p0, (const uint8_t*)p1, n, bitmap);
+    HG_LAUNCH("trie_present", grid, 256, 0, k_trie_present<Code>, code_of, n, bitmap);
     TrieRank hr;
     HG_CU(cudaMemcpyAsync(hr.bits, bitmap, 2048 * 4, cudaMemcpyDeviceToHost, g_stream));
     HG_CU(cudaStreamSynchronize(g_stream));
@@ -877,9 +892,9 @@ static I trie_small(V z, const void* p0, const void* p1, long long n, int* done)
     long long* starts = (long long*)dalloc((size_t)G * 8);
     if (!drk || !counts || !offs || !perm || !starts) return E_DEVICE_OOM;
     HG_CU(cudaMemcpyAsync(drk, &hr, sizeof(TrieRank), cudaMemcpyHostToDevice, g_stream));
-    HG_LAUNCH("trie_count", (unsigned)T, 256, 0, k_trie_count, (const uint8_t*)p0, (const uint8_t*)p1, n, drk, (int)G, T, counts);
+    HG_LAUNCH("trie_count", (unsigned)T, 256, 0, k_trie_count<Code>, code_of, n, drk, (int)G, T, counts);
     HG_CHECK(scan_exclusive(counts, (long long)G * T, offs, nullptr));
-    HG_LAUNCH("trie_scatter", (unsigned)T, 256, 0, k_trie_scatter, (const uint8_t*)p0, (const uint8_t*)p1, n, drk, (int)G, T, offs, perm);
+    HG_LAUNCH("trie_scatter", (unsigned)T, 256, 0, k_trie_scatter<Code>, code_of, n, drk, (int)G, T, offs, perm);
     HG_LAUNCH("trie_starts", 1, 256, 0, k_trie_starts, offs, (int)G, T, starts);
     HG_CHECK(last_launch_error());
     *done = 1;
@@ -902,7 +917,7 @@ I pfnGroupTrie(V z, V x) {
     HG_CHECK(in_ptr(&c[1], &p1));
     if (n >= TS_TILE) {
         int done = 0;
-        HG_CHECK(trie_small(z, p0, p1, n, &done));
+        HG_CHECK(small_group(z, CodeChars{(const uint8_t*)p0, (const uint8_t*)p1}, n, &done));
         if (done) return 0;
     }
     KeySpec s{};
@@ -922,7 +937,19 @@ I pfnGroupBasic(V z, V x) {
     if (x->typ == H_I || x->typ == H_L) {
         const void* p;
         HG_CHECK(in_ptr(x, &p));
-        HG_CHECK(sort_int_column(x, p, x->len, &r));
+        long long mm[2] = {0, 0};
+        bool have_mm = false;
+        if (x->len >= TS_TILE) {  // few non-negative values in a narrow range: the counting path
+            HG_CHECK(col_minmax(p, x->typ, x->len, &mm[0], &mm[1]));
+            have_mm = true;
+            if (mm[0] >= 0 && mm[1] - mm[0] < 65536) {
+                int done = 0;
+                if (x->typ == H_I) HG_CHECK(small_group(z, CodeInt<int32_t>{(const int32_t*)p, mm[0]}, x->len, &done));
+                else HG_CHECK(small_group(z, CodeInt<long long>{(const long long*)p, mm[0]}, x->len, &done));
+                if (done) return 0;
+            }
+        }
+        HG_CHECK(sort_int_column(x, p, x->len, &r, have_mm && x->typ == H_L ? mm : nullptr));
         if (r.key_injective) return group_dict(z, r, x->len, nullptr);
         ColSet cs{};
         cs.ncol = 1; cs.col[0] = p; cs.typ[0] = x->typ;

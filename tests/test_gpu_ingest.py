@@ -142,3 +142,40 @@ def test_csv_host_residency(libs):
         IC.assert_same_table(table_columns(gpu, t), IC.load_table(EXPECT, case["id"]), "host residency")
     finally:
         gpu.lib.hgpuSetResidency(0)
+
+
+def test_random_fields_match_oracle(libs, tmp_path):
+    """Seeded random field texts (signs, spaces, tabs, junk suffixes, long
+    digit runs, exponents, dates with signs and spaces) through every
+    conversion, GPU against the oracle's strtol / strtod / strtof / sscanf."""
+    rng = np.random.default_rng(31)
+    n = 200_000
+
+    def num_text(k):
+        sign = ["", "+", "-", " -", "\t"][k % 5]
+        digits = "".join(rng.choice(list("0123456789"), int(rng.integers(1, 25))))
+        frac = "" if k % 3 else "." + "".join(rng.choice(list("0123456789"), int(rng.integers(0, 12))))
+        exp = "" if k % 4 else f"e{int(rng.integers(-330, 330))}"
+        tail = ["", "", "x", " 7", "e", "."][k % 6]
+        return f"{sign}{digits}{frac}{exp}{tail}"
+
+    def date_text(k):
+        y, m, d = int(rng.integers(-3000, 3000)), int(rng.integers(-20, 40)), int(rng.integers(-5, 40))
+        plus = lambda v: f"+{v}" if v >= 0 else f"{v}"  # noqa: E731  ("+-5" is not a %d)
+        return [f"{y}-{m}-{d}", f" {y}- {m}- {d}", f"{plus(y)}-{plus(m)}-{d}junk", f"{y}-{m:02d}-{d:02d}"][k % 4]
+
+    lines = []
+    for k in range(n):
+        t = num_text(k)
+        lines.append(f"{t}|{t}|{t}|{t}|{t}|{t}|{t}|{date_text(k)}|{t[:1] or 'q'}|\n")
+    p = tmp_path / "random.tbl"
+    p.write_text("".join(lines))
+    from horsepower_gb300.abi import H_B, H_C, H_D, H_F, H_H, H_I, H_J, H_L
+    types = [H_E, H_F, H_L, H_I, H_J, H_H, H_B, H_D, H_C]
+    outs = []
+    for lib, ing in libs:
+        rc, t = ing.csv(str(p), types, [f"c{j}" for j in range(len(types))])
+        assert rc == 0
+        outs.append(table_columns(lib, t)[1])
+    for j, (a, b) in enumerate(zip(*outs)):
+        assert IC.same_column(a, b), f"column {j}"

@@ -365,3 +365,14 @@ def test_join_multi_large(libs, ops):
                                                  L.list([L.vec(c, t) for c, t in zip(cols_p[:k], types_p[:k])]),
                                                  L.syms(ops)))
     assert same(a, b) and a[0].size > 0
+
+
+@pytest.mark.parametrize("typ,lo,hi", [(H_I, 0, 50), (H_L, 1000, 1200), (H_I, 0, 300), (H_I, -5, 40), (H_L, 0, 70000)])
+def test_group_narrow_ints(libs, typ, lo, hi):
+    """@group on one integer column: narrow non-negative ranges with at most
+    256 values take the counting path, others the radix path; both equal the
+    oracle's group dict (keys, and every group's rows in order)."""
+    rng = np.random.default_rng(hi)
+    x = rng.integers(lo, hi, 300_000).astype(np.int32 if typ == H_I else np.int64)
+    a, b = both(libs, "pfnGroup", lambda L: (L.vec(x, typ),))
+    assert same(a, b)
