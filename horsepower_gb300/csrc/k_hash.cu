@@ -1109,9 +1109,9 @@ static I search_bucketed(const void* px, I xtyp, long long lenX, const void* py,
 // times and symbols of one type hash as the integers of their width
 // (h_libs.h:25-31 maps lib_index_of_M/D/U/W/T to _I and Q/Z to _L), with no
 // ordered search.  `miss` (optional, device) is set when some y has no equal x.
-static I index_of(V z, V x, V y, unsigned* miss) {
+static I index_of(V z, V x, V y, unsigned* miss, bool force_hash = false) {
     V0 xa, ya;
-    bool hash_only = false;
+    bool hash_only = force_hash;
     if (x->typ == y->typ && (is_dtime(x->typ) || x->typ == H_Q)) {
         xa = *x; ya = *y;
         xa.typ = ya.typ = esize(x->typ) == 4 ? H_I : H_L;
@@ -1197,6 +1197,105 @@ static I index_of(V z, V x, V y, unsigned* miss) {
     return finish_out(z, dz);
 }
 
+// ---- @index_of on two lists of columns (lib_index_of_G, h_libs.cc:370-373;
+// compareTuple h_system.cc:567-589): the first row of x whose every column
+// equals the y row's, or len(x).  Integer columns (i8/i16/i32/i64) of the
+// same type on both sides are packed into one 64-bit code per row (each
+// column's offset from x's minimum, at the width of x's range), so equal
+// tuples are equal codes; a y value outside x's range cannot match and gets
+// a code no x row has.  The codes go through the hash path (first occurrence).
+struct PackSpec {
+    const void* col[8];
+    int typ[8];
+    long long mn[8], mx[8];
+    int shift[8];
+    int nc;
+};
+__global__ void k_pack_rows(PackSpec s, long long n, unsigned long long* __restrict__ out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        unsigned long long key = 0;
+        bool ok = true;
+        for (int c = 0; c < s.nc; c++) {
+            long long v;
+            switch (s.typ[c]) {
+            case H_J: v = ((const int8_t*)s.col[c])[i]; break;
+            case H_H: v = ((const int16_t*)s.col[c])[i]; break;
+            case H_I: v = ((const int32_t*)s.col[c])[i]; break;
+            default: v = ((const long long*)s.col[c])[i]; break;
+            }
+            ok = ok && v >= s.mn[c] && v <= s.mx[c];
+            key |= ((unsigned long long)v - (unsigned long long)s.mn[c]) << s.shift[c];
+        }
+        out[i] = ok ? key : ~0ull;
+    }
+}
+__global__ void k_fill_i64(long long* __restrict__ z, long long n, long long v) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) z[i] = v;
+}
+
+static I index_of_list(V z, V x, V y, unsigned* miss) {
+    if (x->len != y->len) return E_DOMAIN;  // isListIndexOf, h_system.cc:591-603
+    const int nc = (int)x->len;
+    V0 *xc = host_nodes(x), *yc = host_nodes(y);
+    const long long lenX = nc > 0 ? xc[0].len : 0, lenY = nc > 0 ? yc[0].len : 0;
+    for (int c = 0; c < nc; c++)
+        if (xc[c].len != lenX || yc[c].len != lenY) return E_LENGTH;
+    if (nc > 8) return set_error(E_NOT_IMPL, "index_of on more than 8 columns");
+    bool same_types = true;
+    for (int c = 0; c < nc; c++) {
+        const I tx = xc[c].typ, ty = yc[c].typ;
+        if (!(tx == H_J || tx == H_H || tx == H_I || tx == H_L) || !(ty == H_J || ty == H_H || ty == H_I || ty == H_L))
+            return set_error(E_NOT_IMPL, "index_of on lists holding columns of type %d/%d", tx, ty);
+        same_types = same_types && tx == ty;
+    }
+    void* dz;
+    HG_CHECK(alloc_out(z, H_L, lenY, &dz));
+    if (lenY == 0) return finish_out(z, dz);
+    if (!same_types || lenX == 0) {  // compareTupleItem: columns of different types never compare equal
+        HG_LAUNCH("fill", grid_cap(lenY), 256, 0, k_fill_i64, (long long*)dz, lenY, lenX);
+        if (miss) HG_CU(cudaMemsetAsync(miss, 0xff, 4, g_stream));
+        HG_CHECK(last_launch_error());
+        return finish_out(z, dz);
+    }
+    PackSpec xs{}, ys{};
+    xs.nc = ys.nc = nc;
+    long long* mm = (long long*)salloc(16);
+    if (!mm) return E_DEVICE_OOM;
+    int shift = 0;
+    for (int c = nc - 1; c >= 0; c--) {
+        const void *px, *py;
+        HG_CHECK(in_ptr(&xc[c], &px));
+        HG_CHECK(in_ptr(&yc[c], &py));
+        long long init[2] = {LLONG_MAX, LLONG_MIN}, h[2];
+        HG_CU(cudaMemcpyAsync(mm, init, 16, cudaMemcpyHostToDevice, g_stream));
+        HG_LAUNCH("key_minmax", grid_cap(lenX), 256, 0, k_key_minmax, px, (int)xc[c].typ, lenX, mm);
+        HG_CU(cudaMemcpyAsync(h, mm, 16, cudaMemcpyDeviceToHost, g_stream));
+        HG_CU(cudaStreamSynchronize(g_stream));
+        const unsigned long long span = (unsigned long long)h[1] - (unsigned long long)h[0];
+        const int bits = span == 0 ? 0 : 64 - __builtin_clzll(span);
+        xs.col[c] = px; ys.col[c] = py;
+        xs.typ[c] = ys.typ[c] = xc[c].typ;
+        xs.mn[c] = ys.mn[c] = h[0];
+        xs.mx[c] = ys.mx[c] = h[1];
+        xs.shift[c] = ys.shift[c] = shift;
+        shift += bits;
+        if (shift > 63) return set_error(E_NOT_IMPL, "index_of on lists whose columns span more than 63 bits together");
+    }
+    unsigned long long* kx = (unsigned long long*)salloc((size_t)(lenX > 1 ? lenX : 2) * 8);
+    unsigned long long* ky = (unsigned long long*)salloc((size_t)(lenY > 1 ? lenY : 2) * 8);
+    if (!kx || !ky) return E_DEVICE_OOM;
+    HG_LAUNCH("pack_rows", grid_cap(lenX), 256, 0, k_pack_rows, xs, lenX, kx);
+    HG_LAUNCH("pack_rows", grid_cap(lenY), 256, 0, k_pack_rows, ys, lenY, ky);
+    HG_CHECK(last_launch_error());
+    V0 vx{}, vy{};
+    vx.typ = vy.typ = H_L;
+    vx.len = lenX; vx.g = (G)kx;
+    vy.len = lenY; vy.g = (G)ky;
+    if (lenX == 1) { HG_CU(cudaMemcpy(&vx.b, kx, 8, cudaMemcpyDeviceToHost)); vx.g = (G)&vx.b; }
+    if (lenY == 1) { HG_CU(cudaMemcpy(&vy.b, ky, 8, cudaMemcpyDeviceToHost)); vy.g = (G)&vy.b; }
+    return index_of(z, &vx, &vy, miss, true);
+}
+
 }  // namespace hg
 
 using namespace hg;
@@ -1206,6 +1305,7 @@ extern "C" {
 I pfnIndexOf(V z, V x, V y) {
     HG_CHECK(ensure_init());
     ScratchScope ss;
+    if (x->typ == H_G && y->typ == H_G) return index_of_list(z, x, y, nullptr);
     return index_of(z, x, y, nullptr);
 }
 
@@ -1217,21 +1317,20 @@ I pfnIndexOf(V z, V x, V y) {
 // header {source -1, ek x, ev y} points at the caller's x and y, which must
 // outlive it, as in the reference.  The index is registered as lying in
 // [0, len(x)), so @index(column of x, @values(enum)) skips its bounds check.
-// Two equal-length lists (multi-column keys, :2210-2219) are not built: the
-// reference's own schemas add only single-column foreign keys (global.cc,
-// addFKey2 is commented out).
+// Two lists of the same number of columns (multi-column keys, :2210-2219)
+// take the multi-column index_of.
 I pfnEnum(V z, V x, V y) {
     HG_CHECK(ensure_init());
     ScratchScope ss;
-    if (x->typ == H_G && y->typ == H_G)
-        return x->len == y->len ? set_error(E_NOT_IMPL, "enum over multi-column keys is outside the path") : E_DOMAIN;
-    if (!is_basic(x->typ)) return E_DOMAIN;
+    const bool lists = x->typ == H_G && y->typ == H_G;
+    if (lists && x->len != y->len) return E_DOMAIN;
+    if (!lists && !is_basic(x->typ)) return E_DOMAIN;
     long long mark = out_mark();
     unsigned* miss = (unsigned*)salloc(16);
     if (!miss) return E_DEVICE_OOM;
     HG_CU(cudaMemsetAsync(miss, 0, 4, g_stream));
     V0 ind;
-    I e = index_of(&ind, x, y, miss);
+    I e = lists ? index_of_list(&ind, x, y, miss) : index_of(&ind, x, y, miss);
     if (e) { out_rewind(mark); return e; }
     unsigned h = 0;
     HG_CU(cudaMemcpyAsync(&h, miss, 4, cudaMemcpyDeviceToHost, g_stream));
@@ -1251,10 +1350,10 @@ I pfnEnum(V z, V x, V y) {
         payload = (G)d;
     }
     z->typ = H_Y;
-    z->len = y->len;
+    z->len = ind.len;
     z->g = payload;
     z->y = hdr;
-    register_bound(payload, z->len, x->len);
+    register_bound(payload, z->len, lists ? (x->len > 0 ? host_nodes(x)[0].len : 0) : x->len);
     return apply_residency(z);
 }
 

@@ -600,8 +600,53 @@ static L bsearch_I(const I *x, L low, L high, I val) {
     }
 }
 
+static L elem_l(V x, L i);
+
+/* pfnIndexOf on two lists (lib_index_of_G, h_libs.cc:370-373; isListIndexOf
+ * h_system.cc:591-603): for each y row, the first x row whose columns all
+ * equal it (compareTuple, h_system.cc:567-589: columns of different types
+ * never compare equal), else len(x).  Integer columns only here (float,
+ * string and complex columns: E_NOT_IMPL; the reference exits on the others). */
+static I index_of_list(V z, V x, V y) {
+    if (vn(x) != vn(y)) R E_DOMAIN;
+    L nc = vn(x), lenX = nc ? vn(vV(x, 0)) : 0, lenY = nc ? vn(vV(y, 0)) : 0;
+    for (L c = 0; c < nc; c++) if (vn(vV(x, c)) != lenX || vn(vV(y, c)) != lenY) R E_LENGTH;
+    if (nc > 8) R E_NOT_IMPL;
+    B same = 1;
+    for (L c = 0; c < nc; c++) {
+        I tx = vp(vV(x, c)), ty = vp(vV(y, c));
+        if (!(tx == H_J || tx == H_H || tx == H_I || tx == H_L) || !(ty == H_J || ty == H_H || ty == H_I || ty == H_L)) R E_NOT_IMPL;
+        same = same && tx == ty;
+    }
+    initV(z, H_L, lenY);
+    if (!same || lenX == 0) { for (L i = 0; i < lenY; i++) sL(z)[i] = lenX; R 0; }
+    L cap = 16; while (cap < 2 * lenX) cap <<= 1;
+    L *slot = (L *)malloc(sizeof(L) * (size_t)cap);
+    for (L k = 0; k < cap; k++) slot[k] = -1;
+#define ROW_HASH(V_, r_) ({ uint64_t h_ = 1469598103934665603ULL; for (L c_ = 0; c_ < nc; c_++) h_ = mix64(h_ ^ (uint64_t)elem_l(vV(V_, c_), r_)); h_; })
+#define ROW_EQ(A_, a_, B_, b_) ({ B e_ = 1; for (L c_ = 0; c_ < nc && e_; c_++) e_ = elem_l(vV(A_, c_), a_) == elem_l(vV(B_, c_), b_); e_; })
+    for (L r = 0; r < lenX; r++) {  /* first occurrence of each tuple */
+        L k = (L)(ROW_HASH(x, r) & (uint64_t)(cap - 1));
+        while (slot[k] >= 0 && !ROW_EQ(x, slot[k], x, r)) k = (k + 1) & (cap - 1);
+        if (slot[k] < 0) slot[k] = r;
+    }
+    for (L i = 0; i < lenY; i++) {
+        L k = (L)(ROW_HASH(y, i) & (uint64_t)(cap - 1)), found = lenX;
+        while (slot[k] >= 0) {
+            if (ROW_EQ(x, slot[k], y, i)) { found = slot[k]; break; }
+            k = (k + 1) & (cap - 1);
+        }
+        sL(z)[i] = found;
+    }
+#undef ROW_HASH
+#undef ROW_EQ
+    free(slot);
+    R 0;
+}
+
 /* pfnIndexOf: h_primitive.cc:1523-1579, lib_index_of_*: h_libs.cc:299-373 */
 I pfnIndexOf(V z, V x, V y) {
+    if (vp(x) == H_G && vp(y) == H_G) R index_of_list(z, x, y);
     if (hgo_is_real(vp(x)) && hgo_is_real(vp(y))) {
         L lenX = vn(x), lenZ = vn(y);
         if (hgo_is_ordered(x)) {
@@ -671,17 +716,18 @@ I pfnIndexOf(V z, V x, V y) {
     R E_TYPE;
 }
 
-/* pfnEnum: h_primitive.cc:2198-2222 (basic x).  The enum's index is
- * index_of(x, y); an index >= len(x) is E_ENUM_INDEX (:2204).  Header
- * {source -1, ek x, ev y} (initEnum, h_primitive.h:12-16).  Two lists of
- * equal length (multi-column keys) are outside the path: E_NOT_IMPL. */
+/* pfnEnum: h_primitive.cc:2198-2222.  The enum's index is index_of(x, y);
+ * an index >= the key rows is E_ENUM_INDEX (:2204, :2216).  Header
+ * {source -1, ek x, ev y} (initEnum, h_primitive.h:12-16).  x and y may be
+ * two lists of the same number of columns (multi-column keys). */
 I pfnEnum(V z, V x, V y) {
-    if (vp(x) == H_G && vp(y) == H_G) R vn(x) == vn(y) ? E_NOT_IMPL : E_DOMAIN;
-    if (!hgo_is_basic(vp(x))) R E_DOMAIN;
+    B lists = vp(x) == H_G && vp(y) == H_G;
+    if (lists && vn(x) != vn(y)) R E_DOMAIN;
+    if (!lists && !hgo_is_basic(vp(x))) R E_DOMAIN;
     V0 ind;
     CHECKE(pfnIndexOf(&ind, x, y));
-    L lenZ = vn(&ind);
-    for (L i = 0; i < lenZ; i++) if (sL(&ind)[i] >= vn(x)) R E_ENUM_INDEX;
+    L lenZ = vn(&ind), lenX = lists ? (vn(x) ? vn(vV(x, 0)) : 0) : vn(x);
+    for (L i = 0; i < lenZ; i++) if (sL(&ind)[i] >= lenX) R E_ENUM_INDEX;
     initV(z, H_Y, lenZ);
     z->y->source = -1; z->y->ek = (G)x; z->y->ev = (G)y;
     memcpy(vg(z), sL(&ind), (size_t)lenZ * 8);

@@ -275,6 +275,27 @@ def build_cases():
     add("enum_empty_key", "pfnEnum", V(np.zeros(0, np.int32), H_I), V([3], H_I), error=10)
     add("enum_type", "pfnEnum", V(pk, H_I), V(np.zeros(3, np.int32), H_D), error=6)
 
+    # ---- @index_of / @enum on lists of columns (lib_index_of_G h_libs.cc:370-373, compareTuple h_system.cc:567-589)
+    ka = rng.integers(0, 40, 3000).astype(np.int32)
+    kb = rng.integers(-5, 25, 3000).astype(np.int64)
+    qa = rng.integers(0, 45, 4000).astype(np.int32)
+    qb = rng.integers(-8, 28, 4000).astype(np.int64)
+    add("index_of_list_il", "pfnIndexOf", Ls(V(ka, H_I), V(kb, H_L)), Ls(V(qa, H_I), V(qb, H_L)))
+    add("index_of_list_3", "pfnIndexOf", Ls(V(ka.astype(np.int16), H_H), V(kb.astype(np.int8), H_J), V(ka, H_I)),
+        Ls(V(qa.astype(np.int16), H_H), V(qb.astype(np.int8), H_J), V(qa, H_I)))
+    add("index_of_list_types", "pfnIndexOf", Ls(V(ka, H_I), V(kb, H_L)), Ls(V(qa.astype(np.int64), H_L), V(qb, H_L)))
+    add("index_of_list_one", "pfnIndexOf", Ls(V(ka, H_I)), Ls(V(qa, H_I)))
+    add("index_of_list_ncols", "pfnIndexOf", Ls(V(ka, H_I), V(kb, H_L)), Ls(V(qa, H_I)), error=1)
+    add("index_of_list_ragged", "pfnIndexOf", Ls(V(ka, H_I), V(kb[:10], H_L)), Ls(V(qa, H_I), V(qb, H_L)), error=5)
+    pairs = np.unique(np.stack([ka, kb], 1), axis=0)
+    pick = pairs[rng.integers(0, len(pairs), 5000)]
+    cases.append(dict(name="enum_list", fn="@chain_enum", tol=0.0, canonical=False, error=0,
+                      args=[Ls(V(pairs[:, 0].astype(np.int32), H_I), V(pairs[:, 1], H_L)),
+                            Ls(V(pick[:, 0].astype(np.int32), H_I), V(pick[:, 1], H_L)),
+                            V(rng.random(5000) < 0.5, H_B), V(rng.random(len(pairs)) < 0.5, H_B)]))
+    add("enum_list_missing", "pfnEnum", Ls(V(pairs[:, 0].astype(np.int32), H_I), V(pairs[:, 1], H_L)),
+        Ls(V([999], H_I), V([0], H_L)), error=10)
+
     # ---- symbol compares (compareSymbol h_symbol.cc:241-243 under COMPFN h_primitive.cc:1068-1071)
     words = ["MAIL", "AIR", "REG AIR", "SHIP", "TRUCK", "RAIL", "FOB", "", "AIRMAIL", "air", "A", "MAIL "]
     sa = [words[i] for i in rng.integers(0, len(words), 400)]

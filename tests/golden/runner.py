@@ -55,9 +55,11 @@ def run_case(lib, case, fused=False):
             e = lib.call("pfnEnum", args[0], args[1])
             idx = lib.call("pfnValues", e)
             kept = lib.call("pfnCompress", args[2], idx)
+            from horsepower_gb300.abi import V0
+            keycol = V0.from_address(args[0].g) if args[0].typ == H_G else args[0]  # first key column
             outs = [lib.to_py(idx), lib.to_py(lib.call("pfnFetch", e)), lib.to_py(lib.call("pfnKeys", e)),
                     lib.to_py(lib.call("pfnLen", e)), lib.to_py(lib.call("pfnIndex", args[3], idx)),
-                    lib.to_py(kept), lib.to_py(lib.call("pfnIndex", args[0], kept))]
+                    lib.to_py(kept), lib.to_py(lib.call("pfnIndex", keycol, kept))]
             return 0, outs
         z = lib.call(fn, *args)
         return 0, lib.to_py(z)
