@@ -1478,25 +1478,40 @@ I hgpuReadCSV(V z, S fileName, L numCols, L* types, Q* symList) {
     return e;
 }
 
+// The reference's void / V-returning loaders stop the process on a bad file
+// (EP, exit codes 1 and 99); they still do for those cases.  A device
+// failure (E_DEVICE and above) does not end the process: the error is
+// printed, kept for hgpuLastError, and the node is left empty (readCSV
+// returns NULL).  hgpuReadCSV / hgpuReadSerialized / hgpuWriteSerialized
+// return every status instead.
+static void loader_failed(const char* what, I rc, int code) {
+    fprintf(stderr, "[ERROR] %s: %s\n", what, hgpuLastError());
+    if (rc < E_DEVICE) exit(code);
+}
+
 void serializeV(V x, FILE* fp) {
-    if (hgpuWriteSerialized(x, fp)) {
-        fprintf(stderr, "[ERROR] serializeV: %s\n", hgpuLastError());
-        exit(1);
-    }
+    const I rc = hgpuWriteSerialized(x, fp);
+    if (rc) loader_failed("serializeV", rc, 1);
 }
 
 void readSerializeV(V x, FILE* fp) {
-    if (hgpuReadSerialized(x, fp)) {
-        fprintf(stderr, "[ERROR] readSerializeV: %s\n", hgpuLastError());
-        exit(1);
+    const I rc = hgpuReadSerialized(x, fp);
+    if (rc) {
+        loader_failed("readSerializeV", rc, 1);
+        memset(x, 0, sizeof(V0));
     }
 }
 
 V readCSV(S fileName, L numCols, L* types, Q* symList) {
     V z = allocNode();
-    if (!z || hgpuReadCSV(z, fileName, numCols, types, symList)) {
-        fprintf(stderr, "[ERROR] readCSV: %s\n", hgpuLastError());
-        exit(99);
+    if (!z) {
+        loader_failed("readCSV", E_DEVICE_OOM, 99);
+        return nullptr;
+    }
+    const I rc = hgpuReadCSV(z, fileName, numCols, types, symList);
+    if (rc) {
+        loader_failed("readCSV", rc, 99);
+        return nullptr;
     }
     return z;
 }

@@ -173,7 +173,7 @@ I pfnMax(V z, V x);
 I pfnLen(V z, V x);             /* h_primitive.cc:656-662 */
 /* Gather / search */
 I pfnIndex  (V z, V x, V y);    /* h_primitive.cc:43-94 */
-I pfnIndexOf(V z, V x, V y);    /* h_primitive.cc:1523-1579 */
+I pfnIndexOf(V z, V x, V y);    /* h_primitive.cc:1523-1579 (vectors, or two lists of integer columns) */
 I pfnMember (V z, V y, V x);    /* h_primitive.cc:2287-2336 (note argument order) */
 /* @like (h_primitive.cc:1670-1758): x chars / symbols / strings against one
  * SQL pattern y ('%' any run, '_' any byte; neither matches '\n', as the
@@ -389,7 +389,9 @@ I    hgpuWriteSerialized(V x, FILE *fp);   /* serializeV, h_io.cc:672-697 */
 I    hgpuReadSerialized(V x, FILE *fp);    /* readSerializeV, h_io.cc:748-772 */
 I    hgpuReadCSV(V z, S fileName, L numCols, L *types, Q *symList);  /* readCSV, h_io.cc:50-71 */
 /* The reference's own entry points: like its EP, they print the error and
- * exit the process when the load fails. */
+ * exit the process when the file cannot be read or parsed; a device failure
+ * (E_DEVICE and above) is printed and kept for hgpuLastError without ending
+ * the process (readCSV then returns NULL). */
 void serializeV(V x, FILE *fp);
 void readSerializeV(V x, FILE *fp);
 V    readCSV(S fileName, L numCols, L *types, Q *symList);
