@@ -7,13 +7,15 @@
 //   pfnReduce :802-839 serial MIN/MAX fold from x[0]; empty input gives
 //                     LLONG_MAX/LLONG_MIN (as i64), FLT_MAX/FLT_MIN, DBL_MAX/DBL_MIN
 //
-// GB300: every reduction runs the fixed-order tile tree of dev_common.cuh
-// (tiles of 4096, 256 lanes x 16 strided elements, xor butterfly, pairwise
-// warp combine), recursively over the tile partials until one value is
-// left.  Float sums are therefore bit-identical from run to run and equal to
-// the oracle's restatement of the same order; they differ from the
-// reference's thread-count-dependent order by rounding only (tested at 1e-12
-// relative for f64).
+// GB300: reductions work on 4096-element tiles, then on the tile partials,
+// until one value is left.  f64 sums add in 128-bit fixed point on the
+// integer pipe (GB300's FP64 rate would bound a DADD sum below HBM speed);
+// f32 and integer sums and integer min/max run the fixed-order tile tree of
+// dev_common.cuh; f64/f32 min/max reproduce the reference's serial fold,
+// NaN and signed zeros included, on integer keys.  Float sums are
+// bit-identical from run to run and equal to the oracle's restatements; they
+// differ from the reference's thread-count-dependent order by rounding only
+// (tested at 1e-12 relative for f64).
 #include <cfloat>
 #include <climits>
 
@@ -71,6 +73,344 @@ __global__ void __launch_bounds__(256) k_tile_reduce(const T* __restrict__ x, lo
     }
 }
 
+// ---- f64 @sum / @avg on the integer pipe.
+// GB300 runs FP64 arithmetic at a small fraction of its integer rate, so a
+// sum that adds with DADD is bound by the FP64 units, not by HBM.  Each tile
+// of 4096 elements is instead summed exactly in a 128-bit fixed-point
+// accumulator and rounded once:
+//   E    the largest biased exponent among the tile's finite elements (>= 1),
+//   F    min(62, E - 1); one unit is 2^(E - 1075 - F),
+//   an element m * 2^(e - 1075) (m the 53-bit significand; a subnormal has
+//        e = 1 and no implicit bit) is m * 2^(e - E + F) units, truncated
+//        toward zero when e - E + F < 0 (only elements more than 2^62 times
+//        below the tile's largest binade lose bits),
+//   the total (|total| < 4096 * 2^115 < 2^127) is rounded to nearest-even.
+// A NaN in the tile, or +inf with -inf, gives the quiet NaN 0x7ff8...; an
+// infinity otherwise gives itself.  Longer vectors sum their tile partials
+// the same way until one value is left.  Within a tile the result does not
+// depend on the order of the elements; the oracle restates it bit for bit.
+struct Fx128 {
+    unsigned long long lo, hi;
+};
+
+__device__ __forceinline__ void fx_add(Fx128& a, unsigned long long lo, unsigned long long hi) {
+    asm("add.cc.u64 %0, %0, %2;\n\taddc.u64 %1, %1, %3;" : "+l"(a.lo), "+l"(a.hi) : "l"(lo), "l"(hi));
+}
+
+// The element with bits b in units of 2^(E - 1075 - F), signed, added to a.
+__device__ __forceinline__ void fx_accumulate(Fx128& a, unsigned long long b, int E, int F) {
+    const int e = (int)((b >> 52) & 0x7ff);
+    const unsigned long long m = (b & 0xfffffffffffffull) | ((unsigned long long)(e != 0) << 52);
+    const int k = F - E + (e > 1 ? e : 1);
+    unsigned long long lo, hi;
+    if (k >= 0) {
+        lo = m << k;
+        hi = k ? m >> (64 - k) : 0ull;
+    } else {
+        lo = k > -64 ? m >> (-k) : 0ull;
+        hi = 0;
+    }
+    const unsigned long long s = (unsigned long long)((long long)b >> 63);  // all ones when negative
+    fx_add(a, lo ^ s, hi ^ s);
+    fx_add(a, s & 1ull, 0ull);
+}
+
+// Round a (signed, |a| < 2^127) times 2^sexp to the nearest double (ties to
+// even).  sexp >= -1074, so a result below 2^-1022 is exact.
+__device__ __forceinline__ unsigned long long fx_round(Fx128 a, int sexp) {
+    const unsigned long long sign = a.hi >> 63;
+    unsigned long long lo = a.lo, hi = a.hi;
+    if (sign) {
+        lo = ~lo + 1ull;
+        hi = ~hi + (lo == 0 ? 1ull : 0ull);
+    }
+    if (!hi && !lo) return 0ull;
+    const int p = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);
+    int biased = p + sexp + 1023;
+    if (biased <= 0) return (sign << 63) | (lo << (sexp + 1074));  // subnormal: p <= 51, exact
+    const int sh = p - 52;
+    unsigned long long M;
+    bool up;
+    if (sh <= 0) {
+        M = lo << (-sh);
+        up = false;
+    } else if (sh < 64) {
+        M = (lo >> sh) | (hi << (64 - sh));
+        const unsigned long long rem = lo & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        up = rem > half || (rem == half && (M & 1ull));
+    } else {
+        const int r = sh - 64;
+        M = hi >> r;
+        if (r == 0) {
+            up = lo > (1ull << 63) || (lo == (1ull << 63) && (M & 1ull));
+        } else {
+            const unsigned long long remhi = hi & ((1ull << r) - 1ull), halfhi = 1ull << (r - 1);
+            up = remhi > halfhi || (remhi == halfhi && (lo != 0 || (M & 1ull)));
+        }
+    }
+    if (up && ++M == (1ull << 53)) {
+        M >>= 1;
+        biased++;
+    }
+    if (biased >= 2047) return (sign << 63) | 0x7ff0000000000000ull;
+    return (sign << 63) | ((unsigned long long)biased << 52) | (M & 0xfffffffffffffull);
+}
+
+// Block = 256 threads, one 4096-element tile per block.
+__global__ void __launch_bounds__(256) k_tile_sum_fx(const unsigned long long* __restrict__ x, long long n,
+                                                     double* __restrict__ out) {
+    __shared__ unsigned s_e[8], s_f[8];
+    __shared__ Fx128 s_acc[8];
+    const long long base = (long long)blockIdx.x * TILE_SUM;
+    unsigned long long v[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        const long long i = base + k * 256 + threadIdx.x;
+        v[k] = i < n ? x[i] : 0ull;
+    }
+    unsigned emax = 1, flags = 0;
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        const unsigned e = (unsigned)(v[k] >> 52) & 0x7ffu;
+        if (e == 0x7ffu) flags |= (v[k] & 0xfffffffffffffull) ? 1u : ((v[k] >> 63) ? 4u : 2u);
+        else emax = max(emax, e);
+    }
+    const unsigned w = threadIdx.x >> 5;
+    emax = __reduce_max_sync(0xffffffffu, emax);
+    flags = __reduce_or_sync(0xffffffffu, flags);
+    if (lane_id() == 0) {
+        s_e[w] = emax;
+        s_f[w] = flags;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        emax = max(emax, s_e[j]);
+        flags |= s_f[j];
+    }
+    if (flags) {  // NaN / infinity: uniform over the block
+        if (threadIdx.x == 0) {
+            const unsigned long long r = ((flags & 1u) || (flags & 6u) == 6u) ? 0x7ff8000000000000ull
+                                         : (flags & 2u)                       ? 0x7ff0000000000000ull
+                                                                              : 0xfff0000000000000ull;
+            out[blockIdx.x] = __longlong_as_double((long long)r);
+        }
+        return;
+    }
+    const int E = (int)emax, F = min(62, E - 1);
+    Fx128 acc = {0ull, 0ull};
+#pragma unroll
+    for (int k = 0; k < 16; k++) fx_accumulate(acc, v[k], E, F);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long l2 = __shfl_xor_sync(0xffffffffu, acc.lo, o);
+        const unsigned long long h2 = __shfl_xor_sync(0xffffffffu, acc.hi, o);
+        fx_add(acc, l2, h2);
+    }
+    if (lane_id() == 0) s_acc[w] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Fx128 t = s_acc[0];
+#pragma unroll
+        for (int j = 1; j < 8; j++) fx_add(t, s_acc[j].lo, s_acc[j].hi);
+        out[blockIdx.x] = __longlong_as_double((long long)fx_round(t, E - 1075 - F));
+    }
+}
+
+// f64 sum of n >= 1 elements at x into *result by fixed-point tiles, level
+// after level.  With `fixed` null the levels come from the scratch arena and
+// launches go through HG_LAUNCH on the library stream; otherwise `fixed`
+// holds two level buffers (fixed[0] >= ceil(n/4096) doubles, fixed[1] >=
+// ceil(n/4096^2)) and the kernels go on stream s untracked.
+static void fx_launch(unsigned grid, const void* in, long long n, double* out, cudaStream_t s, bool tracked) {
+    if (tracked) HG_LAUNCH("tile_sum_fx", grid, 256, 0, k_tile_sum_fx, (const unsigned long long*)in, n, out);
+    else k_tile_sum_fx<<<grid, 256, 0, s>>>((const unsigned long long*)in, n, out);
+}
+
+static I fx_sum_f64(const double* x, long long n, double* result, cudaStream_t s, double* const* fixed) {
+    const bool tracked = fixed == nullptr;
+    long long tiles = (n + TILE_SUM - 1) / TILE_SUM;
+    double* part = tracked ? (double*)salloc((size_t)tiles * sizeof(double)) : fixed[0];
+    if (!part) return E_DEVICE_OOM;
+    fx_launch((unsigned)tiles, x, n, tiles == 1 ? result : part, s, tracked);
+    HG_CHECK(last_launch_error());
+    long long m = tiles;
+    double* cur = part;
+    while (m > 1) {
+        long long t2 = (m + TILE_SUM - 1) / TILE_SUM;
+        double* nxt = tracked ? (double*)salloc((size_t)t2 * sizeof(double)) : (cur == fixed[0] ? fixed[1] : fixed[0]);
+        if (!nxt) return E_DEVICE_OOM;
+        fx_launch((unsigned)t2, cur, m, t2 == 1 ? result : nxt, s, tracked);
+        HG_CHECK(last_launch_error());
+        cur = nxt;
+        m = t2;
+    }
+    return 0;
+}
+
+// ---- f64 / f32 @min / @max: the reference's serial fold
+//   t = x[0]; for each v: t = (t > v) ? t : v      (min: t < v)
+// without FP64 compares.  A NaN never wins a compare, so the fold restarts
+// after the last NaN: the result is x[n-1] when that is NaN, else the
+// maximum of the elements after the last NaN, equal values (+0.0 and -0.0)
+// going to the later one.  Each tile (and each block of tile summaries)
+// finds its last NaN position J first, then the largest (key, position)
+// among its elements after J, the key being an integer image of the value
+// that keeps the IEEE order with -0.0 == +0.0.  A summary is (J, key,
+// position); combining summaries in any grouping keeps this meaning, and the
+// last step reads the answer's bits from x.
+template <typename T>
+__device__ __forceinline__ long long fkey(T v) {
+    if constexpr (sizeof(T) == 8) return f64_ord((unsigned long long)__double_as_longlong(v));
+    else {
+        const unsigned b = __float_as_uint(v);
+        return (b >> 31) ? -(long long)(b & 0x7fffffffu) : (long long)b;
+    }
+}
+template <typename T>
+__device__ __forceinline__ bool fnan(T v) {
+    if constexpr (sizeof(T) == 8) return f64_nan_bits((unsigned long long)__double_as_longlong(v));
+    else return (__float_as_uint(v) & 0x7fffffffu) > 0x7f800000u;
+}
+
+// Is (k2, p2) the better candidate than (k1, p1)?  p < 0 marks "none".
+template <int OP>
+__device__ __forceinline__ bool mm_better(long long k2, long long p2, long long k1, long long p1) {
+    if (p2 < 0) return false;
+    if (p1 < 0) return true;
+    if (k2 != k1) return OP == RED_MAX ? k2 > k1 : k2 < k1;
+    return p2 > p1;
+}
+
+template <int OP>
+__device__ __forceinline__ void mm_block_finish(long long J, long long bk, long long bp, long long* onan, long long* okey,
+                                                long long* opos) {
+    __shared__ long long s_k[8], s_p[8];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const long long k2 = __shfl_xor_sync(0xffffffffu, bk, o), p2 = __shfl_xor_sync(0xffffffffu, bp, o);
+        if (mm_better<OP>(k2, p2, bk, bp)) {
+            bk = k2;
+            bp = p2;
+        }
+    }
+    if (lane_id() == 0) {
+        s_k[threadIdx.x >> 5] = bk;
+        s_p[threadIdx.x >> 5] = bp;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        bk = s_k[0];
+        bp = s_p[0];
+        for (int j = 1; j < 8; j++)
+            if (mm_better<OP>(s_k[j], s_p[j], bk, bp)) {
+                bk = s_k[j];
+                bp = s_p[j];
+            }
+        onan[blockIdx.x] = J;
+        okey[blockIdx.x] = bk;
+        opos[blockIdx.x] = bp;
+    }
+}
+
+__device__ __forceinline__ long long block_max_i64(long long v) {
+    __shared__ long long s_m[8];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, (long long)__shfl_xor_sync(0xffffffffu, v, o));
+    if (lane_id() == 0) s_m[threadIdx.x >> 5] = v;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 8; j++) v = max(v, s_m[j]);
+    return v;
+}
+
+// Tile summaries of x: one 4096-element tile per 256-thread block.
+template <typename T, int OP>
+__global__ void __launch_bounds__(256) k_tile_minmax_f(const T* __restrict__ x, long long n, long long* __restrict__ onan,
+                                                       long long* __restrict__ okey, long long* __restrict__ opos) {
+    const long long base = (long long)blockIdx.x * TILE_SUM;
+    const int lim = (int)min((long long)TILE_SUM, n - base);
+    T v[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        const int off = k * 256 + (int)threadIdx.x;
+        v[k] = off < lim ? x[base + off] : T(0);
+    }
+    int lastnan = -1;
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        const int off = k * 256 + (int)threadIdx.x;
+        if (off < lim && fnan(v[k])) lastnan = off;
+    }
+    lastnan = __reduce_max_sync(0xffffffffu, lastnan);
+    const long long J = block_max_i64(lastnan);
+    long long bk = 0, bp = -1;
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        const int off = k * 256 + (int)threadIdx.x;
+        if (off < lim && off > J) {
+            const long long key = fkey(v[k]);
+            if (bp < 0 || (OP == RED_MAX ? key >= bk : key <= bk)) {
+                bk = key;
+                bp = off;
+            }
+        }
+    }
+    mm_block_finish<OP>(J >= 0 ? base + J : -1, bk, bp >= 0 ? base + bp : -1, onan, okey, opos);
+}
+
+// Summaries of m consecutive summaries, 4096 per block.
+template <int OP>
+__global__ void __launch_bounds__(256) k_minmax_combine(const long long* __restrict__ inan, const long long* __restrict__ ikey,
+                                                        const long long* __restrict__ ipos, long long m,
+                                                        long long* __restrict__ onan, long long* __restrict__ okey,
+                                                        long long* __restrict__ opos) {
+    const long long base = (long long)blockIdx.x * TILE_SUM;
+    long long J = -1;
+    for (int k = 0; k < 16; k++) {
+        const long long i = base + k * 256 + threadIdx.x;
+        if (i < m) J = max(J, inan[i]);
+    }
+    J = block_max_i64(J);
+    long long bk = 0, bp = -1;
+    for (int k = 0; k < 16; k++) {
+        const long long i = base + k * 256 + threadIdx.x;
+        if (i < m && ipos[i] > J && mm_better<OP>(ikey[i], ipos[i], bk, bp)) {
+            bk = ikey[i];
+            bp = ipos[i];
+        }
+    }
+    mm_block_finish<OP>(J, bk, bp, onan, okey, opos);
+}
+
+template <typename T>
+__global__ void k_minmax_pick(const T* __restrict__ x, const long long* nan, const long long* pos, T* out) {
+    *out = x[*pos >= 0 ? *pos : *nan];
+}
+
+template <typename T, int OP>
+static I run_minmax_float(V x, void* dres) {
+    const void* p;
+    HG_CHECK(in_ptr(x, &p));
+    const long long n = x->len;
+    long long m = (n + TILE_SUM - 1) / TILE_SUM;
+    long long* a = (long long*)salloc((size_t)m * 3 * sizeof(long long));
+    if (!a) return E_DEVICE_OOM;
+    HG_LAUNCH("tile_minmax", (unsigned)m, 256, 0, (k_tile_minmax_f<T, OP>), (const T*)p, n, a, a + m, a + 2 * m);
+    HG_CHECK(last_launch_error());
+    while (m > 1) {
+        const long long m2 = (m + TILE_SUM - 1) / TILE_SUM;
+        long long* b = (long long*)salloc((size_t)m2 * 3 * sizeof(long long));
+        if (!b) return E_DEVICE_OOM;
+        HG_LAUNCH("tile_minmax", (unsigned)m2, 256, 0, k_minmax_combine<OP>, a, a + m, a + 2 * m, m, b, b + m2, b + 2 * m2);
+        HG_CHECK(last_launch_error());
+        a = b;
+        m = m2;
+    }
+    HG_LAUNCH("minmax_pick", 1, 1, 0, k_minmax_pick<T>, (const T*)p, a, a + 2, (T*)dres);
+    return last_launch_error();
+}
+
 // Reduces n elements of x to one value at *result (device); levels of tile
 // partials live in scratch.
 template <typename T, typename A, int OP>
@@ -124,7 +464,15 @@ static I sum_into(V x, I* typZ, void** dres) {
     case H_I: return run_sum<int32_t, long long>(x, (long long*)*dres);
     case H_L: return run_sum<long long, long long>(x, (long long*)*dres);
     case H_F: return run_sum<float, float>(x, (float*)*dres);
-    default: return run_sum<double, double>(x, (double*)*dres);
+    default: {
+        const void* p;
+        HG_CHECK(in_ptr(x, &p));
+        if (x->len == 0) {
+            HG_CU(cudaMemsetAsync(*dres, 0, sizeof(double), g_stream));
+            return 0;
+        }
+        return fx_sum_f64((const double*)p, x->len, (double*)*dres, g_stream, nullptr);
+    }
     }
 }
 
@@ -218,8 +566,8 @@ I pfnReduce(V z, V x, I op) {
     case H_H: HG_CHECK(mn ? run_minmax<int16_t, RED_MIN>(x, d, INT16_MAX) : run_minmax<int16_t, RED_MAX>(x, d, INT16_MIN)); break;
     case H_I: HG_CHECK(mn ? run_minmax<int32_t, RED_MIN>(x, d, INT32_MAX) : run_minmax<int32_t, RED_MAX>(x, d, INT32_MIN)); break;
     case H_L: HG_CHECK(mn ? run_minmax<long long, RED_MIN>(x, d, LLONG_MAX) : run_minmax<long long, RED_MAX>(x, d, LLONG_MIN)); break;
-    case H_F: HG_CHECK(mn ? run_minmax<float, RED_MIN>(x, d, __builtin_huge_valf()) : run_minmax<float, RED_MAX>(x, d, -__builtin_huge_valf())); break;
-    default: HG_CHECK(mn ? run_minmax<double, RED_MIN>(x, d, __builtin_huge_val()) : run_minmax<double, RED_MAX>(x, d, -__builtin_huge_val())); break;
+    case H_F: HG_CHECK(mn ? run_minmax_float<float, RED_MIN>(x, d) : run_minmax_float<float, RED_MAX>(x, d)); break;
+    default: HG_CHECK(mn ? run_minmax_float<double, RED_MIN>(x, d) : run_minmax_float<double, RED_MAX>(x, d)); break;
     }
     z->typ = x->typ;
     z->len = 1;
@@ -287,18 +635,9 @@ extern "C" I hgpuSumF64Static(const double* x, L n, double* result, void* stream
         return 0;
     }
     double* level0 = (double*)g_static_sum_ptr[dev];                  // up to 65,536 tile partials
-    double* level1 = level0 + HGPU_STATIC_SUM_MAX_TILES;              // up to 16 partials of those
-    long long tiles = (n + TILE_SUM - 1) / TILE_SUM;
-    k_tile_reduce<double, double, RED_SUM><<<(unsigned)tiles, 256, 0, s>>>(x, n, tiles == 1 ? result : level0, 0.0);
-    long long m = tiles;
-    double* cur = level0;
-    while (m > 1) {
-        long long t2 = (m + TILE_SUM - 1) / TILE_SUM;
-        double* nxt = (cur == level0) ? level1 : level0;
-        k_tile_reduce<double, double, RED_SUM><<<(unsigned)t2, 256, 0, s>>>(cur, m, t2 == 1 ? result : nxt, 0.0);
-        cur = nxt;
-        m = t2;
-    }
+    double* const levels[2] = {level0, level0 + HGPU_STATIC_SUM_MAX_TILES};  // then up to 16 partials of those
+    I rc = fx_sum_f64(x, n, result, s, levels);
+    if (rc) return rc;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "hgpuSumF64Static launch", __FILE__, __LINE__);
     return 0;

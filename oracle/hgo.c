@@ -1100,8 +1100,8 @@ I hgpuCompressMany(V *z, V x, V *y, L n) {
 }
 
 /* ------------------------------------------------ fixed-order tile tree sum */
-/* Restatement of libhgpu's deterministic summation order, for bit-exact
- * checks of its f64/f32 sums (the reference's own order depends on the
+/* Restatement of libhgpu's deterministic summation order for segmented
+ * (per-group) sums, for bit-exact checks (the reference's own order depends on the
  * OpenMP thread count, so against it sums agree within a tolerance only):
  * chunks of 4096 elements; lane t (0..255) adds e[t], e[t+256], ... from
  * +0.0; each 32-lane group folds by a xor butterfly (offsets 16,8,4,2,1);
@@ -1126,6 +1126,75 @@ static E tile_tree_f64(const E *x, L n) {
     }
     return ((ws[0] + ws[1]) + (ws[2] + ws[3])) + ((ws[4] + ws[5]) + (ws[6] + ws[7]));
 }
+/* libhgpu's f64 @sum/@avg: each 4096-element tile summed exactly in fixed
+ * point and rounded once, tile partials summed the same way until one value
+ * is left.  Restated from the definition: E = the largest biased exponent of
+ * the tile's finite elements (at least 1), F = min(62, E - 1), unit
+ * 2^(E - 1075 - F); each element's magnitude m * 2^(e - 1075) (subnormals at
+ * e = 1) is floor(m * 2^(e - E + F)) units with its sign; the signed total is
+ * rounded to nearest, ties to even.  NaN, or +inf with -inf, gives the quiet
+ * NaN 0x7ff8...; one kind of infinity gives itself. */
+static E u64_as_f64(unsigned long long b) { E d; memcpy(&d, &b, 8); return d; }
+static unsigned long long f64_bits(E d) { unsigned long long b; memcpy(&b, &d, 8); return b; }
+
+static E fixed_round(__int128 total, int unit_exp) {
+    int neg = total < 0;
+    unsigned __int128 mag = neg ? (unsigned __int128)(-total) : (unsigned __int128)total;
+    if (mag == 0) return 0.0;
+    int p = 127;
+    while (!((mag >> p) & 1)) p--;
+    /* value = mag * 2^unit_exp; normal iff p + unit_exp >= -1022 */
+    unsigned long long bits;
+    if (p + unit_exp < -1022) {
+        bits = (unsigned long long)(mag << (unit_exp + 1074)); /* exact: a multiple of 2^-1074 */
+    } else {
+        int drop = p - 52, ex = p + unit_exp;
+        unsigned __int128 sig = drop > 0 ? mag >> drop : mag << -drop;
+        if (drop > 0) {
+            unsigned __int128 rem = mag - (sig << drop), half = (unsigned __int128)1 << (drop - 1);
+            if (rem > half || (rem == half && (sig & 1))) sig++;
+            if (sig >> 53) { sig >>= 1; ex++; }
+        }
+        if (ex > 1023) bits = 0x7ff0000000000000ull;
+        else bits = ((unsigned long long)(ex + 1023) << 52) | ((unsigned long long)sig & 0xfffffffffffffull);
+    }
+    return u64_as_f64(bits | ((unsigned long long)neg << 63));
+}
+
+static E tile_fixed_f64(const E *x, L n) {
+    int E_ = 1, nan = 0, pinf = 0, ninf = 0;
+    for (L i = 0; i < n; i++) {
+        unsigned long long b = f64_bits(x[i]);
+        int e = (int)((b >> 52) & 0x7ff);
+        if (e == 0x7ff) { if (b & 0xfffffffffffffull) nan = 1; else if (b >> 63) ninf = 1; else pinf = 1; }
+        else if (e > E_) E_ = e;
+    }
+    if (nan || (pinf && ninf)) return u64_as_f64(0x7ff8000000000000ull);
+    if (pinf) return u64_as_f64(0x7ff0000000000000ull);
+    if (ninf) return u64_as_f64(0xfff0000000000000ull);
+    int F = E_ - 1 < 62 ? E_ - 1 : 62;
+    __int128 total = 0;
+    for (L i = 0; i < n; i++) {
+        unsigned long long b = f64_bits(x[i]);
+        int e = (int)((b >> 52) & 0x7ff);
+        unsigned __int128 m = (b & 0xfffffffffffffull) | (e ? 1ull << 52 : 0);
+        int k = F - E_ + (e > 1 ? e : 1);
+        unsigned __int128 units = k >= 0 ? m << k : (k > -128 ? m >> -k : 0);
+        total += (b >> 63) ? -(__int128)units : (__int128)units;
+    }
+    return fixed_round(total, E_ - 1075 - F);
+}
+
+E hgoFixedSumF64(const E *x, L n) {
+    if (n <= 4096) return n ? tile_fixed_f64(x, n) : 0.0;
+    L m = (n + 4095) / 4096;
+    E *p = malloc(sizeof(E) * m);
+    for (L c = 0; c < m; c++) p[c] = tile_fixed_f64(x + c * 4096, (n - c * 4096) < 4096 ? (n - c * 4096) : 4096);
+    E r = hgoFixedSumF64(p, m);
+    free(p);
+    return r;
+}
+
 E hgoTreeSumF64(const E *x, L n) {
     if (n <= 4096) return tile_tree_f64(x, n);
     L m = (n + 4095) / 4096;

@@ -123,6 +123,29 @@ def build_cases():
         add(f"sum_empty_{typ}", "pfnSum", V(np.zeros(0, dt), typ))
     add("sum_one", "pfnSum", V([3.25], H_E))
     add("len", "pfnLen", V(xe, H_E))
+    # min/max fold restarting after NaNs, signed zeros, infinities; sums over
+    # specials and wide exponent ranges (own generator: the cases above keep
+    # their inputs)
+    r2 = np.random.default_rng(5150)
+    for typ, dt in [(H_E, np.float64), (H_F, np.float32)]:
+        pool = np.array([0.0, -0.0, 1.5, -1.5, np.inf, -np.inf, 3.0, -7.25], dt)
+        mixed = pool[r2.integers(0, pool.size, 9000)]
+        mixed[[17, 4100, 5000, 8190]] = np.nan
+        last = mixed.copy()
+        last[-1] = np.nan
+        for nm, arr in [("nan_mid", mixed), ("nan_last", last), ("zeros", np.array([0.0, -0.0, 0.0, -0.0], dt)),
+                        ("zeros_rev", np.array([-0.0, 0.0, -0.0], dt)), ("nan_first", np.array([np.nan, 2.0, -3.0], dt)),
+                        ("one_nan", np.array([np.nan], dt))]:
+            add(f"min_{nm}_{typ}", "pfnMin", V(arr, typ))
+            add(f"max_{nm}_{typ}", "pfnMax", V(arr, typ))
+    wide = r2.standard_normal(9000) * np.ldexp(1.0, r2.integers(-80, 80, 9000))
+    add("sum_wide_exponents", "pfnSum", V(wide, H_E), tol=1e-12)
+    add("avg_wide_exponents", "pfnAvg", V(wide, H_E), tol=1e-12)
+    add("sum_subnormals", "pfnSum", V(np.array([5e-324, 1e-310, -2e-320, 3e-315]), H_E), tol=1e-12)
+    add("sum_inf", "pfnSum", V(np.array([1.0, np.inf, 2.0]), H_E))
+    add("sum_inf_minus_inf", "pfnSum", V(np.array([np.inf, 1.0, -np.inf]), H_E))
+    add("sum_nan", "pfnSum", V(np.array([1.0, np.nan, 2.0]), H_E))
+    add("sum_neg_zeros", "pfnSum", V(np.array([-0.0, -0.0]), H_E))
 
     # ---- gather (h_primitive.cc:43-94)
     src = {H_E: rng.standard_normal(7000), H_I: rng.integers(-99, 99, 7000).astype(np.int32),

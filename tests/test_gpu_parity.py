@@ -25,8 +25,9 @@ def libs():
     import horsepower_gb300
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
     ora = Builtins(os.path.join(ROOT, "oracle", "_build", "liboracle.so"), "oracle")
-    ora.lib.hgoTreeSumF64.restype = C.c_double
-    ora.lib.hgoTreeSumF64.argtypes = [C.c_void_p, C.c_longlong]
+    for fn in (ora.lib.hgoTreeSumF64, ora.lib.hgoFixedSumF64):
+        fn.restype = C.c_double
+        fn.argtypes = [C.c_void_p, C.c_longlong]
     return horsepower_gb300.load(), ora
 
 
@@ -83,13 +84,74 @@ def test_sum_deterministic_and_within_tolerance(libs):
     x = rng.uniform(0, 1e5, 20_000_000)
     r1 = gpu.to_py(gpu.call("pfnSum", gpu.vec(x, H_E)))[0]
     r2 = gpu.to_py(gpu.call("pfnSum", gpu.vec(x, H_E)))[0]
-    assert r1 == r2, "fixed-order sum is not reproducible"
-    fixed = ora.lib.hgoTreeSumF64(x.ctypes.data, x.size)
-    assert r1 == fixed, f"GPU sum {r1!r} != oracle restatement of the fixed order {fixed!r}"
+    assert r1 == r2, "fixed-point tile sum is not reproducible"
+    fixed = ora.lib.hgoFixedSumF64(x.ctypes.data, x.size)
+    assert r1 == fixed, f"GPU sum {r1!r} != oracle restatement of the fixed-point tiles {fixed!r}"
     ref = ora.to_py(ora.call("pfnSum", ora.vec(x, H_E)))[0]
     assert abs(r1 - ref) <= RTOL * abs(ref)
     gpu.free_inputs()
     ora.free_inputs()
+
+
+@pytest.mark.parametrize("kind", ["wide", "cancel", "subnormal", "huge", "tiny_tail", "specials"])
+def test_sum_fixed_point_bit_exact(libs, kind):
+    """f64 @sum/@avg: 128-bit fixed-point tiles, bit-exact against the oracle's
+    restatement over 1 to 3 levels of tiles, and within 1e-12 of the reference
+    order where the exact sum is not cancelled away."""
+    gpu, ora = libs
+    rng = np.random.default_rng(16)
+    n = 17_000_001
+    if kind == "wide":
+        x = rng.standard_normal(n) * np.ldexp(1.0, rng.integers(-200, 200, n))
+    elif kind == "cancel":
+        x = rng.standard_normal(n)
+        x = np.concatenate([x, -x[::-1]])
+    elif kind == "subnormal":
+        x = rng.standard_normal(n) * 1e-310
+    elif kind == "huge":  # partial sums past DBL_MAX: the exact tiles overflow only at the end
+        x = np.full(n, 1.7976931348623157e308 / 3)
+    elif kind == "tiny_tail":  # elements 2^100 below the largest binade of their tile
+        x = np.where(rng.random(n) < 0.001, 1e30, rng.standard_normal(n))
+    else:
+        x = rng.standard_normal(n)
+        x[[5, 9_000_000]] = [np.inf, np.inf]
+    for fn in ("pfnSum", "pfnAvg"):
+        got = gpu.to_py(gpu.call(fn, gpu.vec(x, H_E)))[0]
+        want = ora.lib.hgoFixedSumF64(x.ctypes.data, x.size)
+        if fn == "pfnAvg":
+            want = want / x.size
+        assert np.float64(got).tobytes() == np.float64(want).tobytes(), (fn, got, want)
+        if kind in ("wide", "subnormal", "tiny_tail"):
+            ref = ora.to_py(ora.call(fn, ora.vec(x, H_E)))[0]
+            assert abs(got - ref) <= RTOL * abs(ref), (fn, got, ref)
+    gpu.free_inputs()
+    ora.free_inputs()
+
+
+@pytest.mark.parametrize("typ", [H_E, 5])
+def test_minmax_float_serial_fold_bits(libs, typ):
+    """f64/f32 @min/@max follow the reference's serial fold bit for bit: the
+    fold restarts after the last NaN, ends on a trailing NaN, and of equal
+    values (-0.0 and +0.0) keeps the later one; sizes span several tile
+    levels."""
+    gpu, ora = libs
+    rng = np.random.default_rng(17)
+    dt = np.float64 if typ == H_E else np.float32
+    n = 20_000_003
+    pool = np.array([0.0, -0.0, 1.0, -1.0, 2.5, -2.5, np.inf, -np.inf], dt)
+    base = pool[rng.integers(0, pool.size, n)]
+    normal = rng.standard_normal(n).astype(dt)
+    cases = [base, normal]
+    for arr in (base, normal):
+        for pos in ([17], [n // 2, n - 5000], [n - 1], [0, 4096 * 4096 + 3]):
+            a = arr.copy()
+            a[pos] = np.nan
+            cases.append(a)
+    cases.append(np.where(rng.random(n) < 0.5, dt(0.0), dt(-0.0)).astype(dt))
+    for a in cases:
+        for fn in ("pfnMin", "pfnMax"):
+            g, o = both(libs, fn, lambda L: (L.vec(a, typ),))
+            assert g.tobytes() == o.tobytes(), (fn, g, o)
 
 
 @pytest.mark.parametrize("fn", ["pfnMin", "pfnMax", "pfnSum", "pfnAvg"])
