@@ -110,6 +110,12 @@ class Builtins:
         self._keep.append(v)
         return v
 
+    def node_array(self, nodes):
+        """A `V *` array over nodes (kept alive by this object)."""
+        arr = (PV * max(len(nodes), 1))(*[C.pointer(v) for v in nodes])
+        self._keep.append(arr)
+        return arr
+
     def vec(self, arr, typ=None):
         """A host vector node over a numpy array (kept alive by this object)."""
         arr = np.ascontiguousarray(arr)

@@ -6,6 +6,8 @@
 // a device read out of bounds is never issued.  For a non-i64 index vector
 // the reference reads the narrow buffer at 8-byte stride (:60); here the
 // promoted value is used.
+#include <vector>
+
 #include "dev_common.cuh"
 
 namespace hg {
@@ -84,11 +86,149 @@ I gather_into(const void* x, long long nx, int es, const void* y, I ytyp, void* 
     return last_launch_error();
 }
 
+// ---- several columns gathered by one index (pattern.cc:558-672, the
+// "common index" pattern: every use of an index vector is an @index with it
+// as the second argument).  Each thread reads its four indices once and
+// issues the loads of every column, so the index vector is read once and
+// the columns' loads overlap.
+constexpr int GM_MAXCOL = 8;
+struct GatherCols {
+    const void* src[GM_MAXCOL];
+    void* dst[GM_MAXCOL];
+    long long nx[GM_MAXCOL];
+    int es[GM_MAXCOL];
+    int ncol;
+};
+
+template <int ES>
+struct UintOf;
+template <> struct UintOf<1> { using T = uint8_t; };
+template <> struct UintOf<2> { using T = uint16_t; };
+template <> struct UintOf<4> { using T = uint32_t; };
+template <> struct UintOf<8> { using T = unsigned long long; };
+
+template <int ES>
+__device__ __forceinline__ void gm_column(const void* src, long long nx, void* dst, const long long (&ix)[4],
+                                          long long i0, long long n, bool full, bool& bad) {
+    using ET = typename UintOf<ES>::T;
+    ET v[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const bool in = i0 + k < n, ok = ix[k] >= 0 && ix[k] < nx;
+        if (in && !ok) bad = true;
+        v[k] = (in && ok) ? __ldg((const ET*)src + ix[k]) : ET(0);
+    }
+    ET* z = (ET*)dst + i0;
+    if (full) {  // i0 is a multiple of 4 and dst is 16-byte aligned
+        if constexpr (ES == 1) {
+            *(uint32_t*)z = (uint32_t)v[0] | ((uint32_t)v[1] << 8) | ((uint32_t)v[2] << 16) | ((uint32_t)v[3] << 24);
+        } else if constexpr (ES == 2) {
+            *(uint2*)z = make_uint2((uint32_t)v[0] | ((uint32_t)v[1] << 16), (uint32_t)v[2] | ((uint32_t)v[3] << 16));
+        } else if constexpr (ES == 4) {
+            *(uint4*)z = make_uint4(v[0], v[1], v[2], v[3]);
+        } else {
+            ((ulonglong2*)z)[0] = make_ulonglong2(v[0], v[1]);
+            ((ulonglong2*)z)[1] = make_ulonglong2(v[2], v[3]);
+        }
+        return;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        if (i0 + k < n) z[k] = v[k];
+}
+
+template <typename IT>
+__global__ void __launch_bounds__(256) k_gather_many(GatherCols c, const void* __restrict__ y, long long n, unsigned* derr,
+                                                     int vec) {
+    bool bad = false;
+    const long long stride = (long long)gridDim.x * blockDim.x * 4;
+    for (long long i0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 4; i0 < n; i0 += stride) {
+        const bool full = vec && i0 + 4 <= n;
+        long long ix[4];
+        if (full && sizeof(IT) == 8) {
+            const longlong2* q = reinterpret_cast<const longlong2*>((const long long*)y + i0);
+            const longlong2 a = __ldcs(q), b = __ldcs(q + 1);
+            ix[0] = a.x; ix[1] = a.y; ix[2] = b.x; ix[3] = b.y;
+        } else if (full && sizeof(IT) == 4) {
+            const int4 a = __ldcs(reinterpret_cast<const int4*>((const int32_t*)y + i0));
+            ix[0] = a.x; ix[1] = a.y; ix[2] = a.z; ix[3] = a.w;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++) ix[k] = (i0 + k < n) ? (long long)((const IT*)y)[i0 + k] : 0;
+        }
+        for (int j = 0; j < c.ncol; j++) {
+            switch (c.es[j]) {
+            case 1: gm_column<1>(c.src[j], c.nx[j], c.dst[j], ix, i0, n, full, bad); break;
+            case 2: gm_column<2>(c.src[j], c.nx[j], c.dst[j], ix, i0, n, full, bad); break;
+            case 4: gm_column<4>(c.src[j], c.nx[j], c.dst[j], ix, i0, n, full, bad); break;
+            default: gm_column<8>(c.src[j], c.nx[j], c.dst[j], ix, i0, n, full, bad); break;
+            }
+        }
+    }
+    if (bad) flag_error(derr, DERR_INDEX);
+}
+
+static I gather_many(const GatherCols& c, const void* y, I ytyp, long long n) {
+    if (n <= 0) return 0;
+    unsigned grid = grid_for((n + 3) / 4, 256);
+    const unsigned cap = (unsigned)g_sms * 16;
+    if (grid > cap) grid = cap;
+    uintptr_t al = (uintptr_t)y;
+    for (int j = 0; j < c.ncol; j++) al |= (uintptr_t)c.dst[j];
+    const int vec = (al & 15) == 0;
+    switch (ytyp) {
+    case H_B: HG_LAUNCH("gather_many", grid, 256, 0, k_gather_many<bool>, c, y, n, g_derr, 0); break;
+    case H_J: HG_LAUNCH("gather_many", grid, 256, 0, k_gather_many<int8_t>, c, y, n, g_derr, 0); break;
+    case H_H: HG_LAUNCH("gather_many", grid, 256, 0, k_gather_many<int16_t>, c, y, n, g_derr, 0); break;
+    case H_I: HG_LAUNCH("gather_many", grid, 256, 0, k_gather_many<int32_t>, c, y, n, g_derr, vec); break;
+    default: HG_LAUNCH("gather_many", grid, 256, 0, k_gather_many<long long>, c, y, n, g_derr, vec); break;
+    }
+    return last_launch_error();
+}
+
 }  // namespace hg
 
 using namespace hg;
 
 extern "C" {
+
+// z[k] = x[k][y] for k < n, as n pfnIndex calls on basic-typed columns, in
+// one pass over y.  Any index outside any column gives E_INDEX and no output.
+I hgpuIndexMany(V* z, V* x, V y, L n) {
+    HG_CHECK(ensure_init());
+    ScratchScope ss;
+    if (!is_int(y->typ)) return E_DOMAIN;
+    if (n < 1) return 0;
+    for (L k = 0; k < n; k++)
+        if (!is_basic(x[k]->typ)) return E_NOT_IMPL;
+    const void* py;
+    HG_CHECK(in_ptr(y, &py));
+    const long long m = y->len, mark = out_mark();
+    std::vector<void*> dz((size_t)n);
+    bool in_range = y->typ == H_L;
+    for (L k0 = 0; k0 < n; k0 += GM_MAXCOL) {
+        GatherCols c{};
+        c.ncol = (int)((n - k0) < GM_MAXCOL ? (n - k0) : GM_MAXCOL);
+        for (int j = 0; j < c.ncol; j++) {
+            V xk = x[k0 + j];
+            HG_CHECK(in_ptr(xk, &c.src[j]));
+            c.nx[j] = xk->len;
+            c.es[j] = esize(xk->typ);
+            I rc = alloc_out(z[k0 + j], xk->typ, m, &dz[(size_t)(k0 + j)]);
+            if (rc) { out_rewind(mark); return rc; }
+            c.dst[j] = dz[(size_t)(k0 + j)];
+            in_range = in_range && known_in_range(y->g, m, xk->len);
+        }
+        I rc = gather_many(c, py, y->typ, m);
+        if (rc) { out_rewind(mark); return rc; }
+    }
+    if (!in_range) {
+        I e = check_device_errors();
+        if (e) { out_rewind(mark); return e; }
+    }
+    for (L k = 0; k < n; k++) HG_CHECK(finish_out(z[k], dz[(size_t)k]));
+    return 0;
+}
 
 I pfnIndex(V z, V x, V y) {
     HG_CHECK(ensure_init());

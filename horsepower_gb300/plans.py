@@ -45,6 +45,25 @@ def group_agg(L, agg, x, vals):
     return L.call("pfnRaze", e)
 
 
+def index_many(L, cols, idx):
+    """@index of several columns by one index vector: the reference's common
+    index pattern (pattern.cc:558-672) through hgpuIndexMany where the library
+    has it, else one pfnIndex per column."""
+    import ctypes as C
+    from .abi import BuiltinError
+    fn = getattr(L.lib, "hgpuIndexMany", None)
+    if fn is None or len(cols) < 2:
+        return [L.call("pfnIndex", c, idx) for c in cols]
+    fn.restype = C.c_int32
+    fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong]
+    zs = [L.node() for _ in cols]
+    rc = fn(L.node_array(zs), L.node_array(cols), C.byref(idx), len(cols))
+    if rc:
+        detail = L.lib.hgpuLastError().decode() if L.has_device else ""
+        raise BuiltinError("hgpuIndexMany", rc, detail)
+    return zs
+
+
 def join_group(L, dim, fact, lo=D.WIN_LO, hi=D.WIN_HI):
     """Filter the dimension on its date, join it to the fact table, group the
     matches on (flag, status) and aggregate sum(qty), avg(price), sum(disc),
@@ -55,16 +74,14 @@ def join_group(L, dim, fact, lo=D.WIN_LO, hi=D.WIN_HI):
     pk2 = L.call("pfnCompress", d3, dim["pk"])
     j = L.call("pfnJoinIndex", pk2, fact["fk"], L.sym("eq"))
     fi = L.call("pfnIndex", j, L.scalar(1, H_L))
-    flag = L.call("pfnIndex", fact["flag"], fi)
-    status = L.call("pfnIndex", fact["status"], fi)
+    # every use of fi is an @index by it (the common index pattern); the
+    # measure columns are gathered in a second call, after the group, so
+    # uploads of them still in flight (hgpuToDeviceAsync) overlap the rest
+    flag, status = index_many(L, [fact["flag"], fact["status"]], fi)
     g = L.call("pfnGroup", L.list([flag, status]))
     keys = L.call("pfnKeys", g)
     vals = L.call("pfnValues", g)
-    # the measure columns are gathered last: uploads of them still in flight
-    # (hgpuToDeviceAsync) overlap everything above
-    qty = L.call("pfnIndex", fact["qty"], fi)
-    price = L.call("pfnIndex", fact["price"], fi)
-    disc = L.call("pfnIndex", fact["disc"], fi)
+    qty, price, disc = index_many(L, [fact["qty"], fact["price"], fact["disc"]], fi)
     out_flag = L.call("pfnIndex", flag, keys)
     out_status = L.call("pfnIndex", status, keys)
     sum_qty = group_agg(L, "pfnSum", qty, vals)

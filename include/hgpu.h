@@ -228,6 +228,11 @@ I hgpuChainRunMany(hgpuChain c, V *z, V *x);      /* compress sinks: one output 
 I hgpuChainDestroy(hgpuChain c);
 /* Multi-column compress sharing one mask: pattern.cc:452-520 (V *z, V x, V *y) */
 I hgpuCompressMany(V *z, V x, V *y, L n);
+/* Several columns gathered by one index, the "common index" pattern:
+ * pattern.cc:558-672 (genPatternIndex, `static I qN_patternindex_K(V *z, V *x,
+ * V y)`).  z[k] = x[k][y] as n pfnIndex calls on basic-typed columns; any
+ * index outside any column gives E_INDEX and no output. */
+I hgpuIndexMany(V *z, V *x, V y, L n);
 
 /* ---------------- batched plans ----------------
  * Many independent filter-join-aggregate queries run stage by stage in shared

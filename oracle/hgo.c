@@ -1099,6 +1099,13 @@ I hgpuCompressMany(V *z, V x, V *y, L n) {
     R 0;
 }
 
+/* Several columns gathered by one index (pattern.cc:558-672, the generated
+ * qN_patternindex_K): exactly n separate pfnIndex calls. */
+I hgpuIndexMany(V *z, V *x, V y, L n) {
+    for (L k = 0; k < n; k++) CHECKE(pfnIndex(z[k], x[k], y));
+    R 0;
+}
+
 /* ------------------------------------------------ fixed-order tile tree sum */
 /* Restatement of libhgpu's deterministic summation order for segmented
  * (per-group) sums, for bit-exact checks (the reference's own order depends on the

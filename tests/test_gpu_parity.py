@@ -438,3 +438,56 @@ def test_group_narrow_ints(libs, typ, lo, hi):
     x = rng.integers(lo, hi, 300_000).astype(np.int32 if typ == H_I else np.int64)
     a, b = both(libs, "pfnGroup", lambda L: (L.vec(x, typ),))
     assert same(a, b)
+
+
+def index_many(L, cols, idx):
+    fn = L.lib.hgpuIndexMany
+    fn.restype = C.c_int32
+    fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong]
+    zs = [L.node() for _ in cols]
+    rc = fn(L.node_array(zs), L.node_array(cols), C.byref(idx), len(cols))
+    return rc, zs
+
+
+@pytest.mark.parametrize("ityp", [H_L, H_I, 1])
+@pytest.mark.parametrize("n", [0, 1, 7, 1_000_003])
+def test_index_many_matches_separate_index(libs, ityp, n):
+    """hgpuIndexMany (the common index pattern, pattern.cc:558-672) equals one
+    pfnIndex per column: ten columns of every element width (two launches of
+    up to eight columns), index widths i64/i32/i8, ragged lengths."""
+    rng = np.random.default_rng(18)
+    nx = 120 if ityp == 1 else 3_000_017
+    cols = [(H_B, rng.random(nx) < 0.5), (1, rng.integers(-128, 127, nx).astype(np.int8)),
+            (2, rng.integers(-30000, 30000, nx).astype(np.int16)), (H_I, rng.integers(-9, 9, nx).astype(np.int32)),
+            (H_L, rng.integers(-2 ** 60, 2 ** 60, nx)), (H_E, rng.standard_normal(nx)),
+            (H_C, rng.integers(65, 90, nx).astype(np.int8)), (12, rng.integers(19900101, 19991231, nx).astype(np.int32)),
+            (5, rng.standard_normal(nx).astype(np.float32)), (H_L, np.arange(nx, dtype=np.int64))]
+    idx = rng.integers(0, nx, n)
+    outs = []
+    for L in libs:
+        xs = [L.vec(a, t) for t, a in cols]
+        y = L.vec(idx, ityp)
+        rc, zs = index_many(L, xs, y)
+        assert rc == 0
+        outs.append([L.to_py(z) for z in zs])
+        sep = [L.to_py(L.call("pfnIndex", x, y)) for x in xs]
+        assert all(same(a, b) for a, b in zip(outs[-1], sep))
+        L.free_inputs()
+    assert all(same(a, b) for a, b in zip(*outs))
+
+
+def test_index_many_errors(libs):
+    gpu = libs[0]
+    rng = np.random.default_rng(19)
+    a, b = rng.standard_normal(1000), rng.integers(0, 5, 500).astype(np.int32)
+    for bad in (1000, 500, -1):  # outside both, outside the shorter column only, negative
+        idx = rng.integers(0, 500, 100_000)
+        idx[77_777] = bad
+        rc, _ = index_many(gpu, [gpu.vec(a, H_E), gpu.vec(b, H_I)], gpu.vec(idx, H_L))
+        assert rc == 3, rc  # E_INDEX
+    rc, _ = index_many(gpu, [gpu.vec(a, H_E), gpu.vec(b, H_I)], gpu.vec(rng.random(10), H_E))
+    assert rc == 1  # E_DOMAIN: a float index
+    # the library is still usable after the errors
+    rc, zs = index_many(gpu, [gpu.vec(a, H_E), gpu.vec(b, H_I)], gpu.vec(np.array([3, 499], np.int64), H_L))
+    assert rc == 0 and gpu.to_py(zs[0]).tolist() == [a[3], a[499]] and gpu.to_py(zs[1]).tolist() == [b[3], b[499]]
+    gpu.free_inputs()
