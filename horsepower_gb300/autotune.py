@@ -5,6 +5,8 @@ Knobs and their search ranges:
   tile_rows   probe rows per thread of the tiled join probes (tile = 256 x it)
   hash_load   open-addressing hash-table load factor
   radix_bits  LSD radix digit width of @group / @order
+  l2_fetch    largest L2 fetch from DRAM in bytes (sparse sorted gathers prefer
+              32, random probes and scattered writes 64)
 
 No knob changes a result (stable sorts, order-preserving compaction,
 fixed-order sums), so tuning is a pure search over time: coordinate descent
@@ -19,10 +21,11 @@ import json
 import os
 import statistics
 
-TILE_ROWS, HASH_LOAD, RADIX_BITS = 2, 0, 1
+TILE_ROWS, HASH_LOAD, RADIX_BITS, L2_FETCH = 2, 0, 1, 3
 KNOBS = {"tile_rows": (TILE_ROWS, [8, 16, 32]),
          "hash_load": (HASH_LOAD, [0.5, 0.6, 0.7, 0.8]),
-         "radix_bits": (RADIX_BITS, [4, 5, 6, 7, 8])}
+         "radix_bits": (RADIX_BITS, [4, 5, 6, 7, 8]),
+         "l2_fetch": (L2_FETCH, [32, 64, 128])}
 
 
 def _bind(L):
@@ -57,7 +60,7 @@ def _time(L, fn, reps):
     return statistics.median(ts), out
 
 
-def tune(L, workload, knobs=("tile_rows", "hash_load", "radix_bits"), reps=3, tol=0.02, check=None, log=None):
+def tune(L, workload, knobs=("tile_rows", "hash_load", "radix_bits", "l2_fetch"), reps=3, tol=0.02, check=None, log=None):
     """Coordinate descent over `knobs` for `workload`; applies and returns
     (best setting, {knob: {value: ms}})."""
     _bind(L)

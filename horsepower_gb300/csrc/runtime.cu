@@ -46,6 +46,12 @@ I cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
 }
 
 int g_tile_rows = 8;  // autotuner knob: probe rows per thread of the tiled join probes
+// Autotuner knob: cudaLimitMaxL2FetchGranularity (bytes).  32 B speeds a
+// gather of 8-byte values by sorted row ids at 14% density by ~20% (fewer
+// bytes over-fetched) but slows scattered writes and random probes by
+// 12-18%; streaming kernels read whole lines either way.  The default keeps
+// the device's 64 B.
+static int g_l2_fetch = 64;
 
 // ------------------------------------------------------------------ arenas
 // A bump arena over a list of chunks.  A mark is (chunk index, cursor).
@@ -180,6 +186,7 @@ I ensure_init() {
     HG_CU(cudaStreamCreateWithFlags(&g_copy_stream, cudaStreamNonBlocking));
     HG_CU(cudaMalloc((void**)&g_derr, 256));
     HG_CU(cudaMemset(g_derr, 0, 256));
+    HG_CU(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t)g_l2_fetch));
     if (!g_out) g_out = new Arena(env_mb("HGPU_DEVICE_CHUNK_MB", 4096), false);
     if (!g_scratch) g_scratch = new Arena(env_mb("HGPU_SCRATCH_CHUNK_MB", 4096), false);
     if (!g_host) g_host = new Arena(env_mb("HGPU_HOST_CHUNK_MB", 256), true);
@@ -767,6 +774,13 @@ I hgpuSetTuning(I knob, E value) {
     case HGPU_TUNE_HASH_LOAD: set_hash_load_factor(value); return 0;
     case HGPU_TUNE_RADIX_BITS: set_radix_digit_bits((int)value); return 0;
     case HGPU_TUNE_TILE_ROWS: g_tile_rows = value <= 8 ? 8 : (value <= 16 ? 16 : 32); return 0;
+    case HGPU_TUNE_L2_FETCH:
+        g_l2_fetch = value <= 32 ? 32 : (value <= 64 ? 64 : 128);
+        if (g_inited) {
+            HG_CU(cudaStreamSynchronize(g_stream));
+            HG_CU(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t)g_l2_fetch));
+        }
+        return 0;
     default: return E_DOMAIN;
     }
 }
@@ -776,6 +790,7 @@ E hgpuGetTuning(I knob) {
     case HGPU_TUNE_HASH_LOAD: return get_hash_load_factor();
     case HGPU_TUNE_RADIX_BITS: return (E)get_radix_digit_bits();
     case HGPU_TUNE_TILE_ROWS: return (E)g_tile_rows;
+    case HGPU_TUNE_L2_FETCH: return (E)g_l2_fetch;
     default: return -1.0;
     }
 }

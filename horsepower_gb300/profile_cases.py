@@ -6,6 +6,7 @@
     python -m horsepower_gb300.profile_cases order     # @order (i64 key, i32 sec), N rows
     python -m horsepower_gb300.profile_cases groupkey  # @group on i64 Zipf keys, 150M rows
     python -m horsepower_gb300.profile_cases gather    # @index f64 by ascending row ids
+    python -m horsepower_gb300.profile_cases sum       # @sum then @max of f64, N rows
     python -m horsepower_gb300.profile_cases q6        # fused q6 chain, 6M rows
     python -m horsepower_gb300.profile_cases shared    # 16 batched join plans over one pair of tables
     python -m horsepower_gb300.profile_cases csv       # readCSV of a lineitem-shaped .tbl, N rows
@@ -48,7 +49,7 @@ def timed(L, fn, reps):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["join", "compress", "group", "groupkey", "order", "gather", "q6", "shared", "csv"])
+    ap.add_argument("case", choices=["join", "compress", "group", "groupkey", "order", "gather", "sum", "q6", "shared", "csv"])
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--rows", type=int, default=0)
     ap.add_argument("--tune", action="append", default=[], help="knob=value (autotuner knobs)")
@@ -94,6 +95,10 @@ def main():
         x = dev(L, rng.standard_normal(n), H_E)
         idx = dev(L, np.flatnonzero(rng.random(n) < 0.1445).astype(np.int64), H_L)
         t = timed(L, lambda: L.call("pfnIndex", x, idx), a.reps)
+    elif a.case == "sum":
+        n = a.rows or 60_000_000
+        x = dev(L, rng.uniform(0, 1e5, n), H_E)
+        t = timed(L, lambda: (L.call("pfnSum", x), L.call("pfnMax", x)), a.reps)
     elif a.case == "shared":
         from . import batch as B
         n = a.rows or 59_986_052

@@ -355,6 +355,8 @@ double hgpuTimerStop(void);
 #define HGPU_TUNE_RADIX_BITS 1   /* LSD radix digit width of @group/@order, 4 - 8 bits (default 8) */
 #define HGPU_TUNE_TILE_ROWS  2   /* probe rows per thread of the tiled join probes: 8, 16, 32
                                     (tile = 256 x that; default 8) */
+#define HGPU_TUNE_L2_FETCH   3   /* largest L2 fetch from DRAM, bytes: 32, 64 or 128 (default 64;
+                                    32 suits sparse sorted gathers, 64 random probes and scatters) */
 I    hgpuSetTuning(I knob, E value);
 E    hgpuGetTuning(I knob);
 

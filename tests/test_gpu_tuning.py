@@ -87,9 +87,11 @@ def test_batched_tile_rows(L):
 
 
 def test_tune_and_clamp(L):
-    T.apply(L, {"hash_load": 0.95, "radix_bits": 2, "tile_rows": 100})
+    T.apply(L, {"hash_load": 0.95, "radix_bits": 2, "tile_rows": 100, "l2_fetch": 1000})
     c = T.current(L)
-    assert c == {"tile_rows": 32, "hash_load": 0.8, "radix_bits": 4}
+    assert c == {"tile_rows": 32, "hash_load": 0.8, "radix_bits": 4, "l2_fetch": 128}
+    T.apply(L, {"l2_fetch": 10})
+    assert T.current(L)["l2_fetch"] == 32
     tabs = [B.synth_tables(L, 900 + i, n, n // 4) for i, n in enumerate([20_000, 200_000])]
     plans = [B.make_plan(d, f) for d, f in tabs]
     best, table = T.tune(L, lambda: B.run_batch(L, plans), knobs=("tile_rows",), reps=2,
