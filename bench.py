@@ -129,7 +129,8 @@ def algorithmic_bytes(F, Dn, Dp, M, G):
         "logic": 3 * Dn,                                      # and of the two masks
         "compact": (1 + 4) * Dn + 4 * Dp,                     # compress pk by the mask
         "hash_build": 4 * Dp,                                 # build keys
-        "join_probe": 4 * F + 16 * M,                         # probe keys in, index pairs out
+        "join_probe": 4 * F + 8 * M,                          # probe keys in, staged u32 pairs out
+        "join_emit": 8 * M + 16 * M,                          # staged pairs in, i64 index pairs out
         "gather_many": 2 * 8 * M + 2 * 2 * M + 3 * 16 * M,   # row ids (two calls) + values in, values out
         "gather": 2 * 8 * G * 2,                              # the group keys' flag and status
         "onesweep": 2 * 2 * M,                                # group key bytes (2 x 1 byte) in
