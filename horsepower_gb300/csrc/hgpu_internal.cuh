@@ -153,6 +153,9 @@ struct ListInfo {
     // cached segment ids by size class and the class counts (output arena)
     const unsigned* cls_ids;
     const unsigned* cls_cnt;
+    // host copy of the 8 class counts (cls_known), so empty classes launch nothing
+    int cls_known;
+    unsigned cls_host[8];
 };
 void register_list(const ListInfo& g);
 ListInfo* find_list(const V0* nodes, long long ng);

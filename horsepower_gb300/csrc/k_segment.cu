@@ -225,6 +225,35 @@ __global__ void __launch_bounds__(256) k_seg_mid(const T* __restrict__ src, cons
     if (bad) flag_error(derr, DERR_INDEX);
 }
 
+// The chunk partials of the long segments, one CTA per segment of at most
+// 4096 partials (the caller checks): thread t holds partials t, t + 256, ...
+// exactly as the tile tree places them (the order k_seg_mid's virtual warps
+// follow, whatever size class would have scheduled the segment); the result
+// goes straight to the segment's slot of out.
+template <typename A, int OP>
+__global__ void __launch_bounds__(256) k_seg_partials(const A* __restrict__ part, const long long* __restrict__ pstarts,
+                                                      const long long* __restrict__ big, long long nbig,
+                                                      long long nchunks, A ident, A* __restrict__ out) {
+    __shared__ A ws[8];
+    const long long g = blockIdx.x;
+    const long long s = pstarts[g], e = (g + 1 < nbig) ? pstarts[g + 1] : nchunks;
+    bool bad = false;
+    A v[16];
+    seg_load16<A, false>(part, nullptr, 0, s + threadIdx.x, e, v, bad);
+    A acc = ident;
+#pragma unroll
+    for (int k = 0; k < 16; k++)
+        if (s + k * 256 + threadIdx.x < e) acc = sop<A, OP>(acc, v[k]);
+    acc = swarp<A, OP>(acc);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        A w01 = sop<A, OP>(ws[0], ws[1]), w23 = sop<A, OP>(ws[2], ws[3]);
+        A w45 = sop<A, OP>(ws[4], ws[5]), w67 = sop<A, OP>(ws[6], ws[7]);
+        out[big[g]] = sop<A, OP>(sop<A, OP>(w01, w23), sop<A, OP>(w45, w67));
+    }
+}
+
 // one CTA per 4096-element chunk of the long segments
 template <typename T, typename A, int OP, bool GATHER>
 __global__ void __launch_bounds__(256) k_seg_chunk(const T* __restrict__ src, const long long* __restrict__ rows,
@@ -314,12 +343,30 @@ static I seg_reduce(const T* src, const long long* rows, long long nx, const lon
                   cc + SEG_CLASSES, id);
         ids = id;
         ccnt = cc;
-        if (li) { li->cls_ids = id; li->cls_cnt = cc; }
+        if (li) {
+            li->cls_ids = id;
+            li->cls_cnt = cc;
+            // a list's segments are reduced several times (one aggregate per
+            // column): read the class counts once, so empty classes are skipped
+            HG_CU(cudaMemcpyAsync(li->cls_host, cc, sizeof(li->cls_host), cudaMemcpyDeviceToHost, g_stream));
+            HG_CU(cudaStreamSynchronize(g_stream));
+            li->cls_known = 1;
+        }
     }
-    HG_LAUNCH("seg_warps", gcap(ng * 4), 256, 0, (k_seg_warps<T, A, OP, GATHER>), src, rows, nx, starts, ng, total, ids,
-              ccnt, ident, out, g_derr);
-    HG_LAUNCH("seg_mid", gcap(ng), 256, 0, (k_seg_mid<T, A, OP, GATHER>), src, rows, nx, starts, ng, total, ids, ccnt,
-              ident, out, g_derr);
+    const bool known = li && li->cls_known;
+    bool small = true, mid = true;
+    if (known) {
+        small = false;
+        for (int c = 0; c < 6; c++) small = small || li->cls_host[c] != 0;
+        mid = li->cls_host[6] != 0;
+    }
+    if (small)
+        HG_LAUNCH("seg_warps", gcap(ng * 4), 256, 0, (k_seg_warps<T, A, OP, GATHER>), src, rows, nx, starts, ng, total,
+                  ids, ccnt, ident, out, g_derr);
+    if (mid)
+        HG_LAUNCH("seg_mid", gcap(ng), 256, 0, (k_seg_mid<T, A, OP, GATHER>), src, rows, nx, starts, ng, total, ids,
+                  ccnt, ident, out, g_derr);
+    if (known && li->cls_host[7] == 0) return last_launch_error();
     long long nbig = 0;
     unsigned long long nchunks = 0;
     const long long *big, *pstarts;
@@ -350,7 +397,14 @@ static I seg_reduce(const T* src, const long long* rows, long long nx, const lon
     if (!part || !res) return E_DEVICE_OOM;
     HG_LAUNCH("seg_chunk", (unsigned)nchunks, 256, 0, (k_seg_chunk<T, A, OP, GATHER>), src, rows, nx, starts, ng,
               total, big, c0, nbig, ident, part, g_derr);
-    // partials of each long segment are reduced by the same procedure
+    // partials of each long segment are reduced by the same procedure: at
+    // most 4096 of them per segment (certain when there are at most 4096 in
+    // all) in one launch straight into out, else as segments of their own
+    if (nchunks <= (unsigned long long)TILE_SUM) {
+        HG_LAUNCH("seg_partials", (unsigned)nbig, 256, 0, (k_seg_partials<A, OP>), part, pstarts, big, nbig,
+                  (long long)nchunks, ident, out);
+        return last_launch_error();
+    }
     HG_CHECK((seg_reduce<A, A, OP, false>(part, nullptr, 0, pstarts, nbig, (long long)nchunks, ident, res)));
     HG_LAUNCH("scatter_big", gcap(nbig), 256, 0, k_scatter_big<A>, res, big, nbig, out);
     return last_launch_error();
