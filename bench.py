@@ -58,7 +58,60 @@ def peaks():
         return 6800.0, "fallback"
 
 
-class Clocks:
+class NvmlClocks:
+    """SM clock and clock-event reasons read through NVML (read-only queries)
+    every few milliseconds from a thread, so a timed region of a few tens of
+    milliseconds still gets samples.  Reason bits (nvml.h): 0x4 sw_power_cap,
+    0x8 hw_slowdown, 0x20 sw_thermal_slowdown, 0x40 hw_thermal_slowdown."""
+    BITS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, period_s=0.003):
+        import threading
+        self.nv = C.CDLL("libnvidia-ml.so.1")
+        if self.nv.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = C.c_void_p()
+        if self.nv.nvmlDeviceGetHandleByIndex_v2(int(os.environ.get("LOCAL_RANK", "0")), C.byref(self.h)) != 0:
+            raise OSError("no NVML handle")
+        self.reasons_fn = getattr(self.nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.period, self.samples, self.stop_ev, self.th = period_s, [], threading.Event(), None
+        self._threading = threading
+
+    def _sample(self):
+        mhz, rs = C.c_uint(), C.c_ulonglong()
+        if self.nv.nvmlDeviceGetClockInfo(self.h, 1, C.byref(mhz)) == 0 and self.reasons_fn(self.h, C.byref(rs)) == 0:
+            self.samples.append((mhz.value, rs.value))
+
+    def start(self):
+        def run():
+            while not self.stop_ev.is_set():
+                self._sample()
+                time.sleep(self.period)
+        self._sample()
+        self.th = self._threading.Thread(target=run, daemon=True)
+        self.th.start()
+
+    def stop(self):
+        self.stop_ev.set()
+        self.th.join()
+        self._sample()
+        mx = C.c_uint()
+        self.nv.nvmlDeviceGetMaxClockInfo(self.h, 1, C.byref(mx))
+        reasons = sorted({nm for _, r in self.samples for b, nm in self.BITS.items() if r & b})
+        sm = [m for m, _ in self.samples]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": float(mx.value), "reasons": reasons,
+                "samples": len(sm), "source": "nvml"}
+
+
+def Clocks():
+    try:
+        return NvmlClocks()
+    except Exception:
+        return SmiClocks()
+
+
+class SmiClocks:
     """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
 
     def __init__(self):
@@ -99,7 +152,7 @@ class Clocks:
                 if v.lower().startswith("active"):
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi"}
 
 
 def dist_init(n_gpus):

@@ -859,20 +859,44 @@ __global__ void __launch_bounds__(JT_THREADS) k_jp_stage(Table<unsigned> t, cons
     }
 }
 
+// Pass 2: one warp per four staged warps.  Lanes 0-3 read the four counts
+// and offsets; the first 32 pairs of all four regions are loaded before any
+// is stored (a region rarely holds more), so four loads are in flight per lane.
+constexpr int JU_GROUP = 4;
 __global__ void __launch_bounds__(256) k_jp_unstage(const uint2* __restrict__ stage, const unsigned* __restrict__ wcounts,
                                                     const unsigned* __restrict__ wpre,
                                                     const unsigned long long* __restrict__ toffs, long long nwarps, int per,
                                                     long long* __restrict__ zb, long long* __restrict__ zp) {
-    const long long w = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (w >= nwarps) return;
-    const unsigned c = wcounts[w];
-    const unsigned long long o = toffs[w / (JT_THREADS / 32)] + wpre[w];
-    const uint2* src = stage + w * per;
-    const long long base = w * per;
-    for (unsigned i = lane_id(); i < c; i += 32) {
-        const uint2 p = __ldcs(src + i);
-        __stcs(zb + o + i, (long long)p.x);
-        __stcs(zp + o + i, base + (long long)p.y);
+    const unsigned lane = lane_id();
+    const long long w0 = ((long long)blockIdx.x * 8 + (threadIdx.x >> 5)) * JU_GROUP;
+    if (w0 >= nwarps) return;
+    unsigned myc = 0;
+    unsigned long long myo = 0;
+    if (lane < JU_GROUP && w0 + lane < nwarps) {
+        myc = wcounts[w0 + lane];
+        myo = toffs[(w0 + lane) / (JT_THREADS / 32)] + wpre[w0 + lane];
+    }
+    unsigned c[JU_GROUP];
+    unsigned long long o[JU_GROUP];
+    uint2 p[JU_GROUP];
+#pragma unroll
+    for (int q = 0; q < JU_GROUP; q++) {
+        c[q] = __shfl_sync(0xffffffffu, myc, q);
+        o[q] = __shfl_sync(0xffffffffu, myo, q);
+        p[q] = lane < c[q] ? __ldcs(stage + (w0 + q) * per + lane) : make_uint2(0u, 0u);
+    }
+#pragma unroll
+    for (int q = 0; q < JU_GROUP; q++) {
+        const long long base = (w0 + q) * per;
+        if (lane < c[q]) {
+            __stcs(zb + o[q] + lane, (long long)p[q].x);
+            __stcs(zp + o[q] + lane, base + (long long)p[q].y);
+        }
+        for (unsigned i = lane + 32; i < c[q]; i += 32) {
+            const uint2 t = __ldcs(stage + base + i);
+            __stcs(zb + o[q] + i, (long long)t.x);
+            __stcs(zp + o[q] + i, base + (long long)t.y);
+        }
     }
 }
 
@@ -888,7 +912,7 @@ static I probe_direct_staged(const Table<unsigned>& t, const int* y, long long n
     if (!stage || !wcounts || !wpre || !tcounts || !toffs) return E_DEVICE_OOM;
     HG_LAUNCH("join_probe", (unsigned)ntiles, JT_THREADS, 0, k_jp_stage<R>, t, y, ny, stage, wcounts, wpre, tcounts);
     HG_CHECK(scan_counts(tcounts, ntiles, toffs));
-    HG_LAUNCH("join_emit", (unsigned)((nwarps + 7) / 8), 256, 0, k_jp_unstage, (const uint2*)stage,
+    HG_LAUNCH("join_emit", (unsigned)((nwarps + 8 * JU_GROUP - 1) / (8 * JU_GROUP)), 256, 0, k_jp_unstage, (const uint2*)stage,
               (const unsigned*)wcounts, (const unsigned*)wpre, (const unsigned long long*)toffs, nwarps, 32 * R, zb, zp);
     HG_CHECK(last_launch_error());
     HG_CU(cudaMemcpyAsync(m, toffs + ntiles, 8, cudaMemcpyDeviceToHost, g_stream));
