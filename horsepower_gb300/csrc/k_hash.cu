@@ -278,7 +278,16 @@ __global__ void k_key_minmax(const void* __restrict__ x, int typ, long long n, l
         long long q = __shfl_xor_sync(0xffffffffu, a, o); a = q < a ? q : a;
         long long r = __shfl_xor_sync(0xffffffffu, b, o); b = r > b ? r : b;
     }
-    if (lane_id() == 0) { atomicMin(mm, a); atomicMax(mm + 1, b); }
+    // one pair of atomics per block, not per warp (they serialise on two words)
+    __shared__ long long sa[32], sb[32];
+    const unsigned nw = (blockDim.x + 31) >> 5;
+    if (lane_id() == 0) { sa[threadIdx.x >> 5] = a; sb[threadIdx.x >> 5] = b; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (unsigned w = 1; w < nw; w++) { a = sa[w] < a ? sa[w] : a; b = sb[w] > b ? sb[w] : b; }
+        atomicMin(mm, a);
+        atomicMax(mm + 1, b);
+    }
 }
 
 template <typename K>

@@ -829,11 +829,12 @@ __global__ void __launch_bounds__(256) k_trie_scatter(Code code_of, long long n,
                                                       long long* __restrict__ perm) {
     __shared__ TrieRank r;
     __shared__ unsigned wcnt[8][TS_MAXG];  // per warp: rows of each bucket, then the warp's base
-    load_rank(r, rk);
+    load_rank(r, rk);  // once per block: each block walks several tiles
     const unsigned lane = lane_id(), w = threadIdx.x >> 5;
+    for (long long t = blockIdx.x; t < T; t += gridDim.x) {
     for (int b = lane; b < G; b += 32) wcnt[w][b] = 0;
     __syncthreads();
-    const long long base = (long long)blockIdx.x * TS_TILE + (long long)w * (TS_TILE / 8);
+    const long long base = t * TS_TILE + (long long)w * (TS_TILE / 8);
     unsigned bk[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) {  // warp w owns rows base .. base + 511, in order
@@ -859,8 +860,10 @@ __global__ void __launch_bounds__(256) k_trie_scatter(Code code_of, long long n,
         unsigned pre = 0;
         if (in && (int)lane == leader) { pre = wcnt[w][bk[k]]; wcnt[w][bk[k]] = pre + __popc(peers); }
         pre = __shfl_sync(0xffffffffu, pre, leader);
-        if (in) perm[offs[(long long)bk[k] * T + blockIdx.x] + pre + __popc(peers & lanemask_lt())] = i;
+        if (in) perm[offs[(long long)bk[k] * T + t] + pre + __popc(peers & lanemask_lt())] = i;
         __syncwarp();
+    }
+    __syncthreads();
     }
 }
 __global__ void k_trie_starts(const unsigned long long* __restrict__ offs, int G, long long T, long long* __restrict__ starts) {
@@ -892,9 +895,10 @@ static I small_group(V z, Code code_of, long long n, int* done) {
     long long* starts = (long long*)dalloc((size_t)G * 8);
     if (!drk || !counts || !offs || !perm || !starts) return E_DEVICE_OOM;
     HG_CU(cudaMemcpyAsync(drk, &hr, sizeof(TrieRank), cudaMemcpyHostToDevice, g_stream));
+    const unsigned tg = (unsigned)(T < (long long)g_sms * 4 ? T : (long long)g_sms * 4);
     HG_LAUNCH("trie_count", (unsigned)T, 256, 0, k_trie_count<Code>, code_of, n, drk, (int)G, T, counts);
     HG_CHECK(scan_exclusive(counts, (long long)G * T, offs, nullptr));
-    HG_LAUNCH("trie_scatter", (unsigned)T, 256, 0, k_trie_scatter<Code>, code_of, n, drk, (int)G, T, offs, perm);
+    HG_LAUNCH("trie_scatter", tg, 256, 0, k_trie_scatter<Code>, code_of, n, drk, (int)G, T, offs, perm);
     HG_LAUNCH("trie_starts", 1, 256, 0, k_trie_starts, offs, (int)G, T, starts);
     HG_CHECK(last_launch_error());
     *done = 1;
