@@ -223,9 +223,20 @@ def run_gb300(args, rank, ws, dist):
     ddim = {k: dev[("dim", k)] for k in dim}
     dfact = {k: dev[("fact", k)] for k in fact}
 
+    # the query as compiled C (queries/join_group.c), the form HorseIR runs a
+    # query in; the Python statement sequence (plans.join_group) must give the
+    # same bits
+    query = P.join_group_compiled if P.compiled_queries(gpu) else P.join_group
+    if query is not P.join_group:
+        mark = Lb.getHeapOffset()
+        a = [gpu.to_py(r) for r in P.join_group(gpu, ddim, dfact)]
+        b = [gpu.to_py(r) for r in query(gpu, ddim, dfact)]
+        Lb.setHeapOffset(mark)
+        assert all(x.tobytes() == y.tobytes() for x, y in zip(a, b)), "compiled query differs from the statement sequence"
+
     def step(d_, f_):
         mark = Lb.getHeapOffset()
-        out = P.join_group(gpu, d_, f_)
+        out = query(gpu, d_, f_)
         Lb.hgpuSync()
         Lb.setHeapOffset(mark)
         return out
@@ -234,7 +245,7 @@ def run_gb300(args, rank, ws, dist):
         step(ddim, dfact)
     # shapes of one step, for the algorithmic bytes
     mark = Lb.getHeapOffset()
-    res = P.join_group(gpu, ddim, dfact)
+    res = query(gpu, ddim, dfact)
     res_np = [gpu.to_py(r) for r in res]
     Lb.setHeapOffset(mark)
     M = int(res_np[5].sum())
@@ -300,7 +311,7 @@ def run_gb300(args, rank, ws, dist):
             z = V0()
             Lb.hgpuToDeviceAsync(C.byref(z), C.byref(pinned[key]))
             dv[key] = z
-        out = P.join_group(gpu, {k: dv[("dim", k)] for k in dim}, {k: dv[("fact", k)] for k in fact})
+        out = query(gpu, {k: dv[("dim", k)] for k in dim}, {k: dv[("fact", k)] for k in fact})
         vals = [gpu.to_py(o) for o in out]
         Lb.setHeapOffset(mark)
         return vals
@@ -317,6 +328,7 @@ def run_gb300(args, rank, ws, dist):
     d2h = sum(v.nbytes for v in vals)
 
     out = dict(rows_per_step=F, step_ms=step_ms, wall_s=wall, launches=launches, kernels=kernels,
+               driver="compiled C query (queries/join_group.c)" if query is not P.join_group else "python statements",
                profiled_step_ms=ms_profiled / args.steps,
                clocks=clk, e2e_rows_s=ws * F * args.steps / e2e_s, e2e_ms=1000 * e2e_s / args.steps,
                h2d=h2d, d2h=d2h, shapes=dict(F=F, D=Dn, Dp=Dp, M=M, G=G), result=[v.tolist() for v in res_np])
@@ -347,11 +359,13 @@ def run_batched(args):
         Lb.setHeapOffset(mark)
         return r
 
+    plain_query = P.join_group_compiled if P.compiled_queries(gpu) else P.join_group
+
     def one_at_a_time():
         out = []
         for d, f in tabs:
             mark = Lb.getHeapOffset()
-            r = P.join_group(gpu, d, f)
+            r = plain_query(gpu, d, f)
             out.append([gpu.to_py(v) for v in r])
             Lb.setHeapOffset(mark)
         return out
@@ -859,6 +873,7 @@ def main():
         "vs_baseline": None, "dtype": "int32+f64", "data": "synthetic (seeded, reference-shaped)",
         "config": {"workload": WORKLOAD, "fact_rows": sh["F"], "dim_rows": sh["D"], "dim_selected": sh["Dp"],
                    "matches": sh["M"], "groups": sh["G"], "l2": "inputs larger than L2 (1.9 GB per step)",
+                   "driver": r["driver"],
                    "parallelism": f"replicas x{ws}"},
         "e2e": {"value": r["e2e_rows_s"], "unit": "rows/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"]},

@@ -72,7 +72,32 @@ def build(verbose=False):
         os.replace(LIB + ".tmp", LIB)
     if verbose:
         print(f"libhgpu.so: {len(srcs)} translation units ({'rebuilt' if rebuilt else 'up to date'})")
+    build_queries(verbose)
     return LIB
+
+
+QSRC = os.path.join(PKG, "queries")
+QLIB = os.path.join(PKG, "libhgpu_queries.so")
+
+
+def build_queries(verbose=False):
+    """Compiled benchmark queries (callers of libhgpu, like the reference's
+    generated query code) -> libhgpu_queries.so, linked against libhgpu.so."""
+    srcs = sorted(glob.glob(os.path.join(QSRC, "*.c")))
+    h = hashlib.sha1(b"".join(open(p, "rb").read() for p in srcs) + _headers_digest().encode()).hexdigest()
+    stamp = os.path.join(OUT, "queries.sha")
+    if os.path.exists(QLIB) and os.path.exists(stamp) and open(stamp).read() == h:
+        return QLIB
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-I" + os.path.join(ROOT, "include"), "-o", QLIB + ".tmp"] + srcs + \
+          ["-L" + PKG, "-lhgpu", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"query build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(QLIB + ".tmp", QLIB)
+    open(stamp, "w").write(h)
+    if verbose:
+        print(f"libhgpu_queries.so: {len(srcs)} queries")
+    return QLIB
 
 
 if __name__ == "__main__":

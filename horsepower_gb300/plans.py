@@ -91,6 +91,39 @@ def join_group(L, dim, fact, lo=D.WIN_LO, hi=D.WIN_HI):
     return out_flag, out_status, sum_qty, avg_price, sum_disc, count
 
 
+_QUERIES = {}
+
+
+def compiled_queries(L):
+    """libhgpu_queries.so (the queries compiled to C, built by build.py), bound
+    to the already loaded libhgpu, or None when it is absent."""
+    import ctypes as C
+    import os
+    if id(L) in _QUERIES:
+        return _QUERIES[id(L)]
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libhgpu_queries.so")
+    q = None
+    if getattr(L, "has_device", False) and os.path.exists(path):
+        q = C.CDLL(path)
+        q.hgpuQueryJoinGroup.restype = C.c_int32
+        q.hgpuQueryJoinGroup.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]
+    _QUERIES[id(L)] = q
+    return q
+
+
+def join_group_compiled(L, dim, fact, lo=D.WIN_LO, hi=D.WIN_HI):
+    """join_group as the compiled C query (queries/join_group.c): the same
+    builtin calls, issued from C instead of Python."""
+    from .abi import BuiltinError
+    q = compiled_queries(L)
+    ins = [dim["date"], dim["pk"], fact["fk"], fact["flag"], fact["status"], fact["qty"], fact["price"], fact["disc"]]
+    outs = [L.node() for _ in range(6)]
+    rc = q.hgpuQueryJoinGroup(L.node_array(ins), lo, hi, L.node_array(outs))
+    if rc:
+        raise BuiltinError("hgpuQueryJoinGroup", rc, L.lib.hgpuLastError().decode())
+    return tuple(outs)
+
+
 def group_order(L, t):
     """@group(key) with per-group sum(payload) and count, and the stable
     ascending @order of (key, sec).  Returns (keys, sums, counts, order)."""

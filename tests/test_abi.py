@@ -36,6 +36,18 @@ def test_exports_every_declared_symbol(lib):
     assert len(declared()) > 50
 
 
+def test_compiled_queries_link_against_the_library(lib):
+    """libhgpu_queries.so (queries/*.c) is built beside libhgpu.so, exports
+    the compiled query and resolves the builtins it calls from libhgpu."""
+    path = os.path.join(ROOT, "horsepower_gb300", "libhgpu_queries.so")
+    assert os.path.exists(path)
+    out = subprocess.run(["nm", "-D", path], capture_output=True, text=True, check=True).stdout
+    assert any(ln.split()[-1] == "hgpuQueryJoinGroup" and " T " in ln for ln in out.splitlines())
+    undefined = {ln.split()[-1] for ln in out.splitlines() if " U " in ln}
+    assert {"pfnJoinIndex", "hgpuIndexMany", "hgpuGroupSum"} <= undefined
+    assert C.CDLL(path).hgpuQueryJoinGroup
+
+
 def test_sm103a_only(lib):
     # the build compiles for sm_103a only (one -gencode)
     from horsepower_gb300 import build as b
