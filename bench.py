@@ -155,9 +155,21 @@ class SmiClocks:
                 "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi"}
 
 
+def pin_local_gpu():
+    """One rank per GPU: before the library makes its CUDA context (it uses
+    device 0), narrow CUDA_VISIBLE_DEVICES to this rank's LOCAL_RANK-th GPU.
+    NVML (the clock samples) still addresses the GPU by LOCAL_RANK."""
+    if int(os.environ.get("WORLD_SIZE", "1")) <= 1 or "LOCAL_RANK" not in os.environ:
+        return
+    lr = int(os.environ["LOCAL_RANK"])
+    vis = [v for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+    os.environ["CUDA_VISIBLE_DEVICES"] = vis[lr] if lr < len(vis) else str(lr)
+
+
 def dist_init(n_gpus):
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    pin_local_gpu()
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
