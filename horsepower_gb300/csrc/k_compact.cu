@@ -75,15 +75,23 @@ __global__ void __launch_bounds__(1024) k_scan_counts(const unsigned* __restrict
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
-    for (long long c0 = 0; c0 < n; c0 += 1024 * 8) {
-        const long long b = c0 + (long long)threadIdx.x * 8;
-        unsigned v[8];
+    constexpr int PER = 16;  // 16384 counts per round
+    for (long long c0 = 0; c0 < n; c0 += 1024 * PER) {
+        const long long b = c0 + (long long)threadIdx.x * PER;
+        unsigned v[PER];
         unsigned long long s = 0;
+        if (b + PER <= n && (reinterpret_cast<uintptr_t>(in + b) & 15) == 0) {
 #pragma unroll
-        for (int k = 0; k < 8; k++) {
-            v[k] = b + k < n ? in[b + k] : 0u;
-            s += v[k];
+            for (int q = 0; q < PER / 4; q++) {
+                const uint4 t = __ldg(reinterpret_cast<const uint4*>(in + b) + q);
+                v[4 * q] = t.x; v[4 * q + 1] = t.y; v[4 * q + 2] = t.z; v[4 * q + 3] = t.w;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < PER; k++) v[k] = b + k < n ? in[b + k] : 0u;
         }
+#pragma unroll
+        for (int k = 0; k < PER; k++) s += v[k];
         unsigned long long incl = warp_incl_scan64(s);
         if (lane == 31) wsum[warp] = incl;
         __syncthreads();
@@ -95,7 +103,7 @@ __global__ void __launch_bounds__(1024) k_scan_counts(const unsigned* __restrict
         __syncthreads();
         unsigned long long off = carry + wsum[warp] + (incl - s);
 #pragma unroll
-        for (int k = 0; k < 8; k++) {
+        for (int k = 0; k < PER; k++) {
             if (b + k < n) out[b + k] = off;
             off += v[k];
         }
