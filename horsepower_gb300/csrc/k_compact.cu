@@ -29,16 +29,6 @@ struct CompactCols {
     int ncol;
 };
 
-__device__ __forceinline__ void copy_elem(const void* src, void* dst, long long i, long long o, int es) {
-    switch (es) {
-    case 1: ((uint8_t*)dst)[o] = ((const uint8_t*)src)[i]; break;
-    case 2: ((uint16_t*)dst)[o] = ((const uint16_t*)src)[i]; break;
-    case 4: ((uint32_t*)dst)[o] = ((const uint32_t*)src)[i]; break;
-    case 8: ((uint64_t*)dst)[o] = ((const uint64_t*)src)[i]; break;
-    default: ((long long*)dst)[o] = i; break;
-    }
-}
-
 // A lane's 16 mask bytes (rows base+lofs .. +15), as 0/1 bytes
 __device__ __forceinline__ uint4 load_mask16(const uint8_t* __restrict__ mask, long long n, long long base, int lofs) {
     if (base + lofs + 16 <= n && ((reinterpret_cast<uintptr_t>(mask + base + lofs) & 15) == 0))
@@ -123,6 +113,30 @@ I scan_counts(const unsigned* counts, long long n, unsigned long long* offs) {
 // pass 2: each tile writes its selected rows from its known offset; each warp
 // walks its 512 rows in rounds of 32 and selected lanes write to consecutive
 // positions found with ballot/popc
+// One column of a warp's 512 rows: the values of the lane's selected rows in
+// all 16 rounds are loaded before the first store (the stores could alias
+// the source as far as the compiler knows, so loads and stores interleaved
+// round by round would wait one memory latency per round).
+template <typename E>
+__device__ __forceinline__ void scatter_col(const void* __restrict__ src, void* __restrict__ dst, unsigned selbits,
+                                            long long rowbase, unsigned long long off) {
+    const unsigned lane = lane_id();
+    E v[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        const long long i = rowbase + k * 32 + lane;
+        if constexpr (sizeof(E) == 8 && std::is_signed<E>::value) v[k] = (E)i;  // @where: the row number
+        else v[k] = ((selbits >> k) & 1u) ? reinterpret_cast<const E*>(src)[i] : E(0);
+    }
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        const bool sel = (selbits >> k) & 1u;
+        const unsigned bal = __ballot_sync(0xffffffffu, sel);
+        if (sel) reinterpret_cast<E*>(dst)[off + __popc(bal & lanemask_lt())] = v[k];
+        off += __popc(bal);
+    }
+}
+
 __global__ void __launch_bounds__(CT_THREADS) k_compact_scatter(const uint8_t* __restrict__ mask, long long n,
                                                                 CompactCols cols,
                                                                 const unsigned long long* __restrict__ offs) {
@@ -139,17 +153,18 @@ __global__ void __launch_bounds__(CT_THREADS) k_compact_scatter(const uint8_t* _
     unsigned long long off = offs[blockIdx.x];
     for (unsigned w = 0; w < warp; w++) off += warp_tot[w];
     const int wbase = (int)warp * 512;
-#pragma unroll 4
-    for (int k = 0; k < 16; k++) {
-        const int li = wbase + k * 32 + (int)lane;
-        const bool sel = smask[li] != 0;
-        const unsigned bal = __ballot_sync(0xffffffffu, sel);
-        if (sel) {
-            const long long o = (long long)off + __popc(bal & lanemask_lt());
-            const long long i = base + li;
-            for (int c2 = 0; c2 < cols.ncol; c2++) copy_elem(cols.src[c2], cols.dst[c2], i, o, cols.es[c2]);
+    unsigned selbits = 0;  // bit k: row wbase + 32 k + lane is selected
+#pragma unroll
+    for (int k = 0; k < 16; k++) selbits |= (smask[wbase + k * 32 + (int)lane] != 0 ? 1u : 0u) << k;
+    const long long rowbase = base + wbase;
+    for (int c2 = 0; c2 < cols.ncol; c2++) {
+        switch (cols.es[c2]) {
+        case 1: scatter_col<uint8_t>(cols.src[c2], cols.dst[c2], selbits, rowbase, off); break;
+        case 2: scatter_col<uint16_t>(cols.src[c2], cols.dst[c2], selbits, rowbase, off); break;
+        case 4: scatter_col<uint32_t>(cols.src[c2], cols.dst[c2], selbits, rowbase, off); break;
+        case 8: scatter_col<unsigned long long>(cols.src[c2], cols.dst[c2], selbits, rowbase, off); break;
+        default: scatter_col<long long>(cols.src[c2], cols.dst[c2], selbits, rowbase, off); break;
         }
-        off += __popc(bal);
     }
 }
 
