@@ -993,7 +993,10 @@ static I join_probe_unique(V z, const Table<K>& t, const LinearBuild& lin, int m
 template <typename K>
 static I join_hash(V z, const void* px, I typ, long long nx, const void* py, long long ny) {
     Table<K> t;
-    HG_CHECK(table_build<K>(&t, px, typ, nx, true));
+    // the per-slot row counts serve only repeated build keys: they are
+    // allocated and zeroed once a repeat has been seen (a direct table of a
+    // 15M-key range would otherwise clear 60 MB per join for nothing)
+    HG_CHECK(table_build<K>(&t, px, typ, nx, false));
     unsigned long long nslots = t.cap + 1;  // + the side slot of 64-bit keys
     unsigned dup = 0;
     HG_CU(cudaMemcpyAsync(&dup, t.flags, 4, cudaMemcpyDeviceToHost, g_stream));
@@ -1002,6 +1005,9 @@ static I join_hash(V z, const void* px, I typ, long long nx, const void* py, lon
         LinearBuild lin{};
         return join_probe_unique<K>(z, t, lin, 0, py, typ, ny, nx);
     }
+    t.cnt = (unsigned*)salloc(t.cap * 4);
+    if (!t.cnt) return E_DEVICE_OOM;
+    HG_CU(cudaMemsetAsync(t.cnt, 0, t.cap * 4, g_stream));
     if (nx > 0) HG_LAUNCH("slot_counts", grid_cap(nx), 256, 0, k_slot_counts<K>, t, px, (int)typ, nx);
     // duplicate build keys: CSR of build rows per slot (special slot last)
     unsigned* cnt_all = (unsigned*)salloc(nslots * 4);
