@@ -596,7 +596,7 @@ I pfnLen(V z, V x) {
 // allowed there), callers with a fixed, pre-reserved memory budget, and
 // latency-critical paths that cannot afford the device-wide synchronisation
 // an allocation may cause.  hgpuSumF64Static serves them: it computes the same
-// fixed-order tile-tree sum as pfnSum on f64 data, but keeps the tile
+// fixed-point tile sum as pfnSum on f64 data, but keeps the tile
 // partials in the file-scope array below instead of the scratch arena, and
 // touches no arena, no cudaMalloc/cudaFree and no allocating library call.
 //

@@ -364,7 +364,7 @@ E    hgpuGetTuning(I knob);
  * cannot allocate device memory where they need a sum: code running during a
  * CUDA stream capture, under a fixed pre-reserved memory budget, or on a path
  * that cannot take the synchronisation an allocation may cause.  Same
- * fixed-order tile-tree result as pfnSum on f64 data.  x and result are
+ * fixed-point tile sum as pfnSum on f64 data (the same bits).  x and result are
  * device pointers the caller owns; the tile partials live in a static device
  * array (~512 KiB, held by every GPU that loads the library), so the call
  * makes no cudaMalloc/cudaFree and uses no arena.  n is limited to

@@ -5,7 +5,7 @@ they need a sum (inside a stream capture, under a fixed memory budget, or on
 a path that cannot take an allocation's synchronisation); it keeps its tile
 partials in a static device array.  The test calls it through the C ABI,
 twice in a row on the same static array, and compares both results with the
-arena-based pfnSum within the suite's f64 tolerance.  This file is collected
+arena-based pfnSum bit for bit (both sum the same fixed-point tiles).  This file is collected
 last so a failure here never hides the other tests.
 """
 import ctypes as C
@@ -39,7 +39,7 @@ def test_static_sum_matches_pfnsum_twice():
             assert rc == 0, L.lib.hgpuLastError()
             assert L.lib.hgpuSync() == 0
             got = L.to_py(dout)[0]
-            assert abs(got - expect) <= RTOL * abs(expect), (got, expect)
+            assert got == expect, (got, expect)  # the same fixed-point tiles as pfnSum: the same bits
         L.free_inputs()
 
 
