@@ -5,8 +5,8 @@ they need a sum (inside a stream capture, under a fixed memory budget, or on
 a path that cannot take an allocation's synchronisation); it keeps its tile
 partials in a static device array.  The test calls it through the C ABI,
 twice in a row on the same static array, and compares both results with the
-arena-based pfnSum bit for bit (both sum the same fixed-point tiles).  This file is collected
-last so a failure here never hides the other tests.
+arena-based pfnSum bit for bit (both sum the same fixed-point tiles).  This
+file is collected last so a failure here never hides the other tests.
 """
 import ctypes as C
 
@@ -16,7 +16,6 @@ import pytest
 from horsepower_gb300.abi import H_E, V0
 
 pytestmark = pytest.mark.gpu
-RTOL = 1e-12
 
 
 def test_static_sum_matches_pfnsum_twice():
