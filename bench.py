@@ -17,12 +17,19 @@ interpreter's sequence of builtin calls through libhgpu's C ABI.
           from a second pass of the same K steps with an event pair around
           every launch; the step time is taken without them.
   cpu_baseline  the CPU oracle port (a restatement of the reference's
-          builtins, OpenMP like the reference) on a bounded sample
+          builtins, OpenMP like the reference) on the same full-size tables;
+          the GPU's six result vectors must equal the oracle's (keys and
+          counts bit-exact, f64 aggregates within 1e-12) or the run fails
+  parity_vs_oracle  that comparison
 
-`--impl reference` runs the same query through the CPU oracle port on all
-host cores instead (the reference library itself cannot be built where its
-sources are absent).  Multi-GPU: every rank runs its own replica (weak
-scaling, no collective on the data path).
+`--impl reference` runs the same query on the same full-size tables through
+the CPU oracle port on all host cores instead, W warm-up and K timed steps
+(the reference library itself cannot be built where its sources are absent).
+Multi-GPU: every rank runs its own replica (weak scaling, no collective on
+the data path).
+
+Other workloads (`--workload`): builtins (each builtin alone), batched,
+served, ingest, and case (one builtin for a kernel profile).
 """
 import argparse
 import ctypes as C
@@ -206,7 +213,7 @@ def algorithmic_bytes(F, Dn, Dp, M, G):
     }
 
 
-def run_gb300(args, rank, ws, dist):
+def run_gb300(args, rank, ws, dist, dim, fact):
     import horsepower_gb300
     gpu = horsepower_gb300.load()
     Lb = gpu.lib
@@ -220,7 +227,6 @@ def run_gb300(args, rank, ws, dist):
     Lb.setHeapOffset.argtypes = [C.c_longlong]
 
     F, Dn = args.fact, args.dim
-    dim, fact = D.join_tables(F, Dn, seed=1 + rank)
     # device-resident copies of the tables
     host = {}
     dev = {}
@@ -798,22 +804,206 @@ def run_ingest(args):
     }
 
 
-def cpu_sample(args):
-    """The oracle port on a bounded sample of the workload (fact and dim scaled by 1/10)."""
+CASES = ["join", "compress", "group", "groupkey", "order", "gather", "sum", "q6", "shared", "csv",
+         "elementwise", "member", "index_of", "groupsum", "like", "quicksort"]
+
+
+def run_case(args):
+    """Single-builtin workloads for kernel profiling (ncu) and micro-benchmarks:
+    `python bench.py --workload case --case NAME [--rows N] [--reps R]
+    [--tune knob=value]`.  Inputs are seeded and uploaded once; the case runs
+    --reps times on device-resident data and prints the CUDA-event time per
+    call (not a bench line).
+
+      join         @join_index, 2.17M build keys x 60M probe keys
+      compress     @compress f64, 6M rows, 1.8% selected
+      group        @group on two 1-byte columns, 8.67M rows
+      groupkey     @group on i64 Zipf keys, 150M rows
+      order        @order (i64 key, i32 sec), 20M rows
+      gather       @index f64 by 14.5% ascending row ids of 60M
+      sum          @sum then @max of f64, 60M rows
+      q6           the fused q6 chain, 6M rows
+      shared       16 batched join plans over one pair of tables
+      csv          readCSV of a lineitem-shaped .tbl, 1M rows
+      elementwise  @gt f64 vs scalar, @mul f64, @and, 60M rows
+      member       @member of 60M probe keys in 2.17M keys
+      index_of     @index_of of 60M probe keys in 2.17M keys
+      groupsum     hgpuGroupSum of 3 f64 columns over the 6 (flag, status)
+                   groups of 8.67M rows (the join + group-by aggregates)
+      like         @like '%special%requests%' over loaded lineitem comments
+      quicksort    @order of one f64 column with ties (the reference's
+                   quicksort path), 2M rows
+    """
+    import horsepower_gb300
+    from horsepower_gb300.abi import H_B, H_C, H_E, H_I, H_L
+    L = horsepower_gb300.load()
+    Lb = L.lib
+    Lb.hgpuTimerStop.restype = C.c_double
+    Lb.getHeapOffset.restype = C.c_longlong
+    Lb.setHeapOffset.argtypes = [C.c_longlong]
+    if args.tune:
+        from horsepower_gb300 import autotune
+        autotune.apply(L, {kv.split("=")[0]: float(kv.split("=")[1]) for kv in args.tune})
+    rng = np.random.default_rng(5)
+    keep_alive = []
+
+    def dev(arr, typ):
+        h = L.vec(arr, typ)
+        d = V0()
+        assert Lb.hgpuToDevice(C.byref(d), C.byref(h)) == 0
+        keep_alive.append(d)
+        return d
+
+    def timed(fn):
+        out = []
+        for _ in range(args.reps):
+            mark = Lb.getHeapOffset()
+            Lb.hgpuSync()
+            Lb.hgpuTimerStart()
+            fn()
+            out.append(Lb.hgpuTimerStop())
+            Lb.setHeapOffset(mark)
+        return out
+
+    c = args.case
+    if c in ("join", "member", "index_of"):
+        F = args.rows or 59_986_052
+        D_ = 15_000_000
+        pk = rng.permutation(D_).astype(np.int32)
+        keep = (rng.integers(0, D.NDAYS, D_) < 365)
+        x = dev(pk[keep], H_I)
+        y = dev(rng.integers(0, D_, F).astype(np.int32), H_I)
+        f = L.sym("eq")
+        fn = {"join": lambda: L.call("pfnJoinIndex", x, y, f), "member": lambda: L.call("pfnMember", y, x),
+              "index_of": lambda: L.call("pfnIndexOf", x, y)}[c]
+        t = timed(fn)
+    elif c == "compress":
+        n = args.rows or 6_001_215
+        m = dev(rng.random(n) < 0.018, H_B)
+        v = dev(rng.standard_normal(n), H_E)
+        t = timed(lambda: L.call("pfnCompress", m, v))
+    elif c == "group":
+        n = args.rows or 8_662_796
+        f = dev(rng.integers(0, 3, n).astype(np.int8), H_C)
+        s_ = dev(rng.integers(0, 2, n).astype(np.int8), H_C)
+        lst = L.list([f, s_])
+        t = timed(lambda: L.call("pfnGroup", lst))
+    elif c == "groupkey":
+        from horsepower_gb300 import serve as S
+        o = S.order_table(L, args.rows or 150_000_000, seed=2)
+        t = timed(lambda: L.call("pfnGroup", o["key"]))
+    elif c == "order":
+        n = args.rows or 20_000_000
+        key = dev(np.minimum(rng.zipf(1.1, n), 10_000_000).astype(np.int64), H_L)
+        sec = dev(rng.integers(0, 2 ** 20 + 1, n).astype(np.int32), H_I)
+        lst = L.list([key, sec])
+        d = L.vec(np.array([1, 1], bool), H_B)
+        t = timed(lambda: L.call("pfnOrderBy", lst, d))
+    elif c == "gather":
+        n = args.rows or 59_986_052
+        x = dev(rng.standard_normal(n), H_E)
+        idx = dev(np.flatnonzero(rng.random(n) < 0.1445).astype(np.int64), H_L)
+        t = timed(lambda: L.call("pfnIndex", x, idx))
+    elif c == "sum":
+        n = args.rows or 60_000_000
+        x = dev(rng.uniform(0, 1e5, n), H_E)
+        t = timed(lambda: (L.call("pfnSum", x), L.call("pfnMax", x)))
+    elif c == "elementwise":
+        n = args.rows or 60_000_000
+        a = dev(rng.standard_normal(n), H_E)
+        b = dev(rng.standard_normal(n), H_E)
+        m1, m2 = dev(rng.random(n) < 0.5, H_B), dev(rng.random(n) < 0.5, H_B)
+        sc = L.scalar(0.25, H_E)
+        t = timed(lambda: (L.call("pfnGt", a, sc), L.call("pfnMul", a, b), L.call("pfnAnd", m1, m2)))
+    elif c == "groupsum":
+        n = args.rows or 8_662_796
+        f = dev(rng.integers(0, 3, n).astype(np.int8), H_C)
+        s_ = dev(rng.integers(0, 2, n).astype(np.int8), H_C)
+        g = L.call("pfnGroup", L.list([f, s_]))
+        vals = L.call("pfnValues", g)
+        cols = [dev(rng.uniform(0, 1e5, n), H_E) for _ in range(3)]
+        t = timed(lambda: [L.call("hgpuGroupSum", col, vals) for col in cols])
+    elif c == "shared":
+        from horsepower_gb300 import batch as B
+        n = args.rows or 59_986_052
+        dim, fact = B.synth_tables(L, 1, n, n // 4)
+        plans = [B.make_plan(dim, fact, D.DAYS0 + 100 * k, D.DAYS0 + 100 * k + 365) for k in range(16)]
+        t = timed(lambda: B.run_batch(L, plans))
+    elif c in ("csv", "like"):
+        import tempfile
+        text, _ = D.lineitem_csv(args.rows or 1_000_000, seed=9)
+        fd, path = tempfile.mkstemp(suffix=".tbl")
+        os.write(fd, text)
+        os.close(fd)
+        ty = (C.c_longlong * 16)(*D.LINEITEM_TYPES)
+        sy = (C.c_longlong * 16)(*[Lb.getSymbol(nm.encode()) for nm in D.LINEITEM_NAMES])
+        Lb.hgpuReadCSV.argtypes = [C.c_void_p, C.c_char_p, C.c_longlong, C.c_void_p, C.c_void_p]
+
+        def load_table():
+            z = V0()
+            assert Lb.hgpuReadCSV(C.addressof(z), path.encode(), 16, ty, sy) == 0
+            return z
+        if c == "csv":
+            t = timed(load_table)
+        else:
+            tab = load_table()
+            keep_alive.append(tab)
+            vals = V0.from_address(tab.g + 32)
+            comment = V0.from_address(vals.g + 32 * 15)
+            pat = L.strs([b"%special%requests%"])
+            t = timed(lambda: L.call("pfnLike", comment, pat))
+        os.remove(path)
+    elif c == "quicksort":
+        n = args.rows or 2_000_000
+        x = dev(np.round(rng.standard_normal(n), 2), H_E)
+        d = L.vec(np.array([1], bool), H_B)
+        t = timed(lambda: L.call("pfnOrderBy", x, d))
+    else:
+        tb = D.filter_table(args.rows or 6_001_215)
+        nodes = {k: dev(v, P.FILTER_TYPES[k]) for k, v in tb.items()}
+        ch = P.Chain(L, P.Q6_CHAIN.format(lo=D.WIN_LO, hi=D.WIN_HI))
+        t = timed(lambda: ch.run([nodes["shipdate"], nodes["qty"], nodes["disc"], nodes["price"]]))
+    print(f"{c}: ms per call {[round(v, 4) for v in t]}")
+
+
+def cpu_full(args, dim, fact, reps, warmup=0):
+    """The oracle port (the reference's builtins restated in C, OpenMP like
+    the reference) running the same query on the same full-size tables, on
+    all host cores.  Returns (the cpu_baseline record, the result vectors)."""
     ora = Builtins(os.path.join(ROOT, "oracle", "_build", "liboracle.so"), "oracle")
-    F, Dn = args.fact // args.cpu_scale, args.dim // args.cpu_scale
-    dim, fact = D.join_tables(F, Dn, seed=101)
     hd, hf = P.host_nodes(ora, dim, P.DIM_TYPES), P.host_nodes(ora, fact, P.FACT_TYPES)
-    times = []
-    for _ in range(args.cpu_reps):
+    times, res = [], None
+    for k in range(warmup + reps):
         mark = ora.lib.getHeapOffset()
         t0 = time.perf_counter()
-        P.join_group(ora, hd, hf)
-        times.append(time.perf_counter() - t0)
+        out = P.join_group(ora, hd, hf)
+        dt = time.perf_counter() - t0
+        if k >= warmup:
+            times.append(dt)
+        if res is None:
+            res = [ora.to_py(v) for v in out]
         ora.lib.setHeapOffset(mark)
     t = statistics.median(times)
-    return dict(value=F / t, unit="rows/s", cores=os.cpu_count(), kind="port",
-                sample=f"fact {F:,} x dim {Dn:,} rows (1/{args.cpu_scale} of the workload), median of {len(times)}")
+    F, Dn = len(fact["fk"]), len(dim["pk"])
+    rec = dict(value=F / t, unit="rows/s", cores=int(os.environ.get("OMP_NUM_THREADS", os.cpu_count())),
+               kind="port", ms_per_step=1000 * t,
+               sample=f"the full workload: fact {F:,} x dim {Dn:,} rows (the same seeded tables), "
+                      f"median of {len(times)} steps after {warmup} warm-up")
+    return rec, res
+
+
+def check_result(gpu_res, cpu_res, rtol=1e-12):
+    """The query's six result vectors: group keys (flag, status) and counts
+    bit-exact, the f64 aggregates within rtol of the oracle (whose OpenMP sum
+    order depends on the thread count, like the reference's)."""
+    g = [np.asarray(v) for v in gpu_res]
+    c = [np.asarray(v) for v in cpu_res]
+    exact = all(np.array_equal(g[k], c[k].astype(g[k].dtype)) for k in (0, 1, 5))
+    close = all(g[k].shape == c[k].shape and np.allclose(g[k], c[k], rtol=rtol, atol=0) for k in (2, 3, 4))
+    err = max(float(np.max(np.abs(g[k] - c[k]) / np.maximum(np.abs(c[k]), 1e-300))) if g[k].size else 0.0
+              for k in (2, 3, 4))
+    return {"keys_counts_bit_exact": bool(exact), "aggregates_within_1e-12": bool(close),
+            "max_rel_err": err, "ok": bool(exact and close)}
 
 
 def main():
@@ -824,10 +1014,14 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fact", type=int, default=59_986_052)
     ap.add_argument("--dim", type=int, default=15_000_000)
-    ap.add_argument("--cpu-scale", type=int, default=10)
+    ap.add_argument("--cpu-scale", type=int, default=10, help="ingest workload: CPU sample = rows / this")
     ap.add_argument("--cpu-reps", type=int, default=3)
     ap.add_argument("--workload", default="join_group",
-                    choices=["join_group", "batched", "served", "builtins", "ingest"])
+                    choices=["join_group", "batched", "served", "builtins", "ingest", "case"])
+    ap.add_argument("--case", choices=CASES, default="join", help="with --workload case: the builtin to run")
+    ap.add_argument("--rows", type=int, default=0, help="with --workload case: rows (0 = the case's default)")
+    ap.add_argument("--reps", type=int, default=3, help="with --workload case: calls to time")
+    ap.add_argument("--tune", action="append", default=[], help="with --workload case: knob=value")
     ap.add_argument("--ingest-rows", type=int, default=6_001_215)
     ap.add_argument("--rates", default="200,1000,5000")
     ap.add_argument("--serve-seconds", type=float, default=1.5)
@@ -836,6 +1030,9 @@ def main():
     ap.add_argument("--plans", type=int, default=256)
     ap.add_argument("--max-fact", type=int, default=20_000_000)
     args = ap.parse_args()
+    if args.workload == "case":
+        run_case(args)
+        return
     rank, ws, dist = dist_init(args.gpus)
     if args.workload in ("batched", "served", "builtins", "ingest") and args.impl == "gb300":
         line = {"batched": run_batched, "served": run_served, "builtins": run_builtins,
@@ -849,17 +1046,20 @@ def main():
         if rank != 0:
             return
         subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
-        cb = cpu_sample(args)
+        dim, fact = D.join_tables(args.fact, args.dim, seed=1)
+        cb, _ = cpu_full(args, dim, fact, reps=args.steps, warmup=args.warmup)
         print(json.dumps({"metric": METRIC, "value": cb["value"], "unit": "rows/s", "n_gpus": args.gpus,
-                          "steps": args.cpu_reps, "warmup": 0, "ms_per_step": 1000 * (args.fact // args.cpu_scale) / cb["value"],
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["ms_per_step"],
                           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
-                          "data": "synthetic (seeded)", "impl": "reference",
-                          "config": {"workload": WORKLOAD, "sample": cb["sample"]},
+                          "data": "synthetic (seeded, reference-shaped)", "impl": "reference",
+                          "config": {"workload": WORKLOAD, "fact_rows": args.fact, "dim_rows": args.dim,
+                                     "sample": cb["sample"]},
                           "cpu_baseline": cb,
                           "e2e": {"value": cb["value"], "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return
 
-    r = run_gb300(args, rank, ws, dist)
+    dim, fact = D.join_tables(args.fact, args.dim, seed=1 + rank)
+    r = run_gb300(args, rank, ws, dist, dim, fact)
     if rank != 0:
         return
     hbm, src = peaks()
@@ -878,7 +1078,11 @@ def main():
         b = alg.get(k)
         builtins[k] = {"ms_per_step": round(t / args.steps, 4), "launches_per_step": n / args.steps,
                        "gbs": round(b / (t / args.steps / 1000) / 1e9, 1) if b else None}
-    cpu = cpu_sample(args)
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+    cpu, cpu_res = cpu_full(args, dim, fact, reps=args.cpu_reps)
+    parity = check_result(r["result"], cpu_res)
+    if not parity["ok"]:
+        raise SystemExit(f"the GPU result differs from the oracle's: {parity}")
     value = ws * sh["F"] / (r["step_ms"] / 1000)
     line = {
         "metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": ws, "steps": args.steps,
@@ -896,6 +1100,7 @@ def main():
                      "traffic_gbs": (traffic / (top[1] / args.steps / 1000) / 1e9) if traffic else None,
                      "traffic_frac": (traffic / (top[1] / args.steps / 1000) / 1e9 / hbm) if traffic else None},
         "cpu_baseline": cpu,
+        "parity_vs_oracle": parity,
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
         "kernels_ms_per_step": {k: round(v, 4) for k, v in per_step_ms.items()},

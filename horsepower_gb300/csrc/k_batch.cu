@@ -1186,11 +1186,8 @@ extern "C" I hgpuBatchJoinGroup(const hgpuJoinGroupPlan* plans, L nplans, hgpuJo
     if (nt_probe > 0) {
         const unsigned nt = (unsigned)nt_probe;
         const size_t sm = (size_t)2 * R * 256 * 4;
-        static bool attr = false;
-        if (!attr) {
-            HG_CU(cudaFuncSetAttribute(k_b_probe<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 32 * 256 * 4));
-            attr = true;
-        }
+        // per context: set on every call (a host-side write)
+        HG_CU(cudaFuncSetAttribute(k_b_probe<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 32 * 256 * 4));
         if (R == 8) HG_LAUNCH("b_probe", nt, 256, sm, k_b_probe<8>, dP, fT, np, mbits, tcount);
         else if (R == 32) HG_LAUNCH("b_probe", nt, 256, sm, k_b_probe<32>, dP, fT, np, mbits, tcount);
         else HG_LAUNCH("b_probe", nt, 256, sm, k_b_probe<16>, dP, fT, np, mbits, tcount);

@@ -592,10 +592,10 @@ I pfnLen(V z, V x) {
 // Allocation-free f64 sum.
 //
 // Some callers cannot allocate device memory at the point where they need a
-// sum: code running while a CUDA graph is being captured (cudaMalloc is not
-// allowed there), callers with a fixed, pre-reserved memory budget, and
-// latency-critical paths that cannot afford the device-wide synchronisation
-// an allocation may cause.  hgpuSumF64Static serves them: it computes the same
+// sum: a query engine that reserved a fixed device-memory budget up front and
+// must not grow it, and latency-critical paths that cannot afford the
+// device-wide synchronisation an allocation (or an arena's first chunk) may
+// cause.  hgpuSumF64Static serves them: it computes the same
 // fixed-point tile sum as pfnSum on f64 data, but keeps the tile
 // partials in the file-scope array below instead of the scratch arena, and
 // touches no arena, no cudaMalloc/cudaFree and no allocating library call.
@@ -611,7 +611,10 @@ I pfnLen(V z, V x) {
 //     them on one stream or serialise them.
 //   * The first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (the host-side name is only a stand-in).  Make
-//     that first call before any stream capture begins.
+//     that first call before any stream capture begins.  The address is kept
+//     for the life of the process: after cudaDeviceReset on that device it
+//     would be stale, so a device reset is not supported (the library's
+//     arenas and stream do not survive one either).
 // ---------------------------------------------------------------------------
 #define HGPU_STATIC_SUM_MAX_TILES 65536LL
 #define HGPU_STATIC_SUM_MAX_ROWS (HGPU_STATIC_SUM_MAX_TILES * 4096LL)
@@ -636,9 +639,5 @@ extern "C" I hgpuSumF64Static(const double* x, L n, double* result, void* stream
     }
     double* level0 = (double*)g_static_sum_ptr[dev];                  // up to 65,536 tile partials
     double* const levels[2] = {level0, level0 + HGPU_STATIC_SUM_MAX_TILES};  // then up to 16 partials of those
-    I rc = fx_sum_f64(x, n, result, s, levels);
-    if (rc) return rc;
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "hgpuSumF64Static launch", __FILE__, __LINE__);
-    return 0;
+    return fx_sum_f64(x, n, result, s, levels);  // checks each launch
 }

@@ -256,18 +256,17 @@ I radix_sort(const K* keys, long long n, const K** kres, const unsigned** vres, 
     if (!kb[0] || !kb[1] || !vb[1] || !st) return E_DEVICE_OOM;
     const K* kin = keys;
     const unsigned* vin = init_vals;
+    {  // the attribute belongs to the current device's context: set it on every call (a host-side write)
+        const int dsm = (int)((size_t)RS_TILE * (sizeof(K) + 4));
+        HG_CU(cudaFuncSetAttribute(k_onesweep<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
+        HG_CU(cudaFuncSetAttribute(k_onesweep<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
+    }
     for (int p = 0; p < npass; p++) {
         HG_CU(cudaMemsetAsync(st, 0, (size_t)ntiles * 256 * 8 + 64, g_stream));
         K* ko = kb[p & 1];
         unsigned* vo = vb[p & 1];
         unsigned* ticket = (unsigned*)(st + (size_t)ntiles * 256 * 8);
         const size_t dsm = (size_t)RS_TILE * (sizeof(K) + 4);
-        static bool attr_set = false;
-        if (!attr_set) {
-            cudaFuncSetAttribute(k_onesweep<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
-            cudaFuncSetAttribute(k_onesweep<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
-            attr_set = true;
-        }
         if (p == 0 && !init_vals)
             HG_LAUNCH("onesweep", (unsigned)ntiles, RS_THREADS, dsm, (k_onesweep<K, true>), kin, vin, ko, vo, n,
                       lo + p * bits, bits, bucket + p * 256, (unsigned long long*)st, ticket, g_derr);
@@ -721,9 +720,9 @@ static I group_finish(V z, long long* starts, long long G, long long* perm, long
         HG_CU(cudaMemcpyAsync(host_nodes(&kv[1]), stage, (size_t)G * sizeof(V0), cudaMemcpyDeviceToHost, g_stream));
     }
     HG_CHECK(last_launch_error());
+    HG_CHECK(check_device_errors());  // synchronises: the node array is written by the kernel
     HG_CHECK(finish_out(&kv[0], dkeys));
     register_bound(kv[0].g, kv[0].len, n);
-    HG_CHECK(sync());  // the node array is written by the kernel
     if (G > 0) register_list({host_nodes(&kv[1]), G, LIST_SEGMENTS, H_L, starts, n, perm, 1, 0, 0, 0, nullptr, nullptr, nullptr});
     return apply_residency(z);
 }
@@ -733,6 +732,9 @@ static I order_output(V z, const SortResult& r, long long n, bool reverse) {
     HG_CHECK(alloc_out(z, H_L, n, &d));
     if (n > 0) HG_LAUNCH("widen", gcap(n), 256, 0, k_widen, r.perm, n, (long long*)d, reverse ? 1 : 0);
     HG_CHECK(last_launch_error());
+    // a radix pass whose look-back gave up leaves a wrong permutation: read
+    // the device error word before the result is marked as in range
+    HG_CHECK(check_device_errors());
     register_bound(d, n, n);
     return finish_out(z, d);
 }

@@ -361,16 +361,17 @@ I    hgpuSetTuning(I knob, E value);
 E    hgpuGetTuning(I knob);
 
 /* Allocation-free f64 sum (no counterpart in the reference).  For callers that
- * cannot allocate device memory where they need a sum: code running during a
- * CUDA stream capture, under a fixed pre-reserved memory budget, or on a path
- * that cannot take the synchronisation an allocation may cause.  Same
+ * cannot allocate device memory where they need a sum: an engine that works in
+ * a fixed device-memory budget reserved up front, or a path that cannot take
+ * the synchronisation an allocation may cause.  Same
  * fixed-point tile sum as pfnSum on f64 data (the same bits).  x and result are
  * device pointers the caller owns; the tile partials live in a static device
  * array (~512 KiB, held by every GPU that loads the library), so the call
  * makes no cudaMalloc/cudaFree and uses no arena.  n is limited to
  * 268,435,456 (E_LENGTH beyond).  Calls share the array: calls overlapping
  * on the GPU race, so issue them on one stream.  The first call on a device
- * looks up the array's address; make it before any stream capture. */
+ * looks up the array's address; make it before any stream capture.  A device
+ * reset (cudaDeviceReset) is not supported afterwards. */
 I    hgpuSumF64Static(const double *x, L n, double *result, void *stream);
 
 /* ---------------- ingest: binary tables and CSV (h_io.cc) ----------------

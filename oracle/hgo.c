@@ -1211,3 +1211,23 @@ E hgoTreeSumF64(const E *x, L n) {
     free(p);
     return r;
 }
+
+/* hgoTreeSumF64 per group: out[g] = the fixed-order tile-tree sum of
+ * x[perm[starts[g]]], ..., x[perm[starts[g+1] - 1]] (starts[ng] = n), the
+ * order every segmented sum of the GPU library follows.  Groups are
+ * independent, so they run as OpenMP iterations. */
+void hgoSegTreeSumF64(const E *x, const L *perm, const L *starts, L ng, L n, E *out) {
+#pragma omp parallel
+    {
+        L cap = 4096;
+        E *buf = malloc(sizeof(E) * cap);
+#pragma omp for schedule(dynamic, 1024)
+        for (L g = 0; g < ng; g++) {
+            L a = starts[g], b = g + 1 < ng ? starts[g + 1] : n;
+            if (b - a > cap) { cap = b - a; buf = realloc(buf, sizeof(E) * cap); }
+            for (L k = a; k < b; k++) buf[k - a] = x[perm[k]];
+            out[g] = hgoTreeSumF64(buf, b - a);
+        }
+        free(buf);
+    }
+}

@@ -166,7 +166,11 @@ static void quicksort_dispatch(L *rtn, V val, L low, L high, B *isUp, CmpFn cmp)
 }
 
 /* lib_mergesort: h_libs.cc:490-536 (stable top-down merge; the two-element
- * case swaps only on a strict inversion). */
+ * case swaps only on a strict inversion).  The merge of [low, high) uses
+ * merge_buf[low, high) (the reference uses LARGE_BUFF from 0; the output is the
+ * same), so the two halves of a large range can sort as parallel OpenMP tasks
+ * with the same result.  merge_buf holds one slot per row of the column and is
+ * allocated once per @order (the reference mallocs LARGE_BUFF per range). */
 static L *merge_buf;
 static void mergesort_rec(L *rtn, V val, L low, L high, B *isUp, CmpFn cmp) {
     if (low < high - 1) {
@@ -174,20 +178,34 @@ static void mergesort_rec(L *rtn, V val, L low, L high, B *isUp, CmpFn cmp) {
             if (cmp(val, rtn[low], rtn[high - 1], isUp) > 0) { L t = rtn[low]; rtn[low] = rtn[high - 1]; rtn[high - 1] = t; }
         } else {
             L mid = (low + high) >> 1, len = high - low;
-            mergesort_rec(rtn, val, low, mid, isUp, cmp);
-            mergesort_rec(rtn, val, mid, high, isUp, cmp);
+            if (len > (1 << 16)) {
+#pragma omp task default(shared) firstprivate(low, mid)
+                mergesort_rec(rtn, val, low, mid, isUp, cmp);
+                mergesort_rec(rtn, val, mid, high, isUp, cmp);
+#pragma omp taskwait
+            } else {
+                mergesort_rec(rtn, val, low, mid, isUp, cmp);
+                mergesort_rec(rtn, val, mid, high, isUp, cmp);
+            }
             if (cmp(val, rtn[mid - 1], rtn[mid], isUp) > 0) {
-                L cl = low, cr = mid;
+                L cl = low, cr = mid, *buf = merge_buf + low;
                 for (L i = 0; i < len; i++) {
-                    if (cl == mid) merge_buf[i] = rtn[cr++];
-                    else if (cr == high) merge_buf[i] = rtn[cl++];
-                    else if (cmp(val, rtn[cl], rtn[cr], isUp) > 0) merge_buf[i] = rtn[cr++];
-                    else merge_buf[i] = rtn[cl++];
+                    if (cl == mid) buf[i] = rtn[cr++];
+                    else if (cr == high) buf[i] = rtn[cl++];
+                    else if (cmp(val, rtn[cl], rtn[cr], isUp) > 0) buf[i] = rtn[cr++];
+                    else buf[i] = rtn[cl++];
                 }
-                memcpy(rtn + low, merge_buf, sizeof(L) * len);
+                memcpy(rtn + low, buf, sizeof(L) * len);
             }
         }
     }
+}
+static void mergesort_top(L *rtn, V val, L low, L high, B *isUp, CmpFn cmp) {
+    if (high - low > (1 << 16)) {
+#pragma omp parallel
+#pragma omp single
+        mergesort_rec(rtn, val, low, high, isUp, cmp);
+    } else mergesort_rec(rtn, val, low, high, isUp, cmp);
 }
 
 /* lib_order_by_sorted: h_libs.cc:604-617 — an already ordered range is kept;
@@ -216,11 +234,8 @@ static void quicksort_list(L *targ, V val, B *isUp, L low, L high, L colId) {
     V curV = vV(val, colId);
     B *curB = isUp + colId;
     if (!order_by_sorted(targ, curV, curB, low, high, hgo_cmp_item)) {
-        if (vp(curV) == H_I || vp(curV) == H_L) {
-            merge_buf = malloc(sizeof(L) * (vn(curV) > 0 ? vn(curV) : 1));
-            mergesort_rec(targ, curV, low, high, curB, hgo_cmp_item);
-            free(merge_buf);
-        } else quicksort_dispatch(targ, curV, low, high, curB, hgo_cmp_item);
+        if (vp(curV) == H_I || vp(curV) == H_L) mergesort_top(targ, curV, low, high, curB, hgo_cmp_item);
+        else quicksort_dispatch(targ, curV, low, high, curB, hgo_cmp_item);
     }
     L pos = low;
     while (pos < high) {
@@ -363,7 +378,10 @@ I pfnOrderBy(V z, V x, V y) {
         initV(z, H_L, lenZ);
         hgo_sort_err = 0;
         for (L i = 0; i < lenZ; i++) sL(z)[i] = i;
+        merge_buf = malloc(sizeof(L) * (lenZ > 0 ? lenZ : 1));
         quicksort_list(sL(z), x, sB(y), 0, lenZ, 0);
+        free(merge_buf);
+        merge_buf = NULL;
         R hgo_sort_err;
     }
     R order_basic(z, x, y);
