@@ -108,6 +108,24 @@ struct Arena {
         if (chunks.empty()) return 0;
         return ((long long)cur_chunk << 40) | (long long)chunks[cur_chunk].cur;
     }
+    // bytes in use: the capacity of every chunk before the current one plus
+    // the current chunk's cursor (chunks before the cursor are never dropped,
+    // so a value taken earlier maps back to the same chunk and offset)
+    size_t used() const {
+        if (chunks.empty()) return 0;
+        size_t u = 0;
+        for (size_t k = 0; k < cur_chunk; k++) u += chunks[k].cap;
+        return u + chunks[cur_chunk].cur;
+    }
+    // rewinds to a used() value no larger than the current one
+    void rewind_used(size_t u) {
+        if (chunks.empty() || u > used()) return;
+        size_t k = 0;
+        while (k < cur_chunk && u >= chunks[k].cap) u -= chunks[k++].cap;
+        cur_chunk = k;
+        chunks[k].cur = u;
+        last_chunk = -1;
+    }
     void rewind(long long m) {
         size_t c = (size_t)(m >> 40), off = (size_t)(m & ((1LL << 40) - 1));
         if (chunks.empty()) return;
@@ -168,7 +186,6 @@ static Arena* g_scratch = nullptr;  // scratch arena (device)
 static Arena* g_host = nullptr;     // pinned host arena
 
 // heap-offset tokens: token -> (output mark, host mark)
-static std::vector<std::pair<long long, long long>> g_marks;
 
 I ensure_init() {
     if (g_inited) return 0;
@@ -190,8 +207,6 @@ I ensure_init() {
     if (!g_out) g_out = new Arena(env_mb("HGPU_DEVICE_CHUNK_MB", 4096), false);
     if (!g_scratch) g_scratch = new Arena(env_mb("HGPU_SCRATCH_CHUNK_MB", 4096), false);
     if (!g_host) g_host = new Arena(env_mb("HGPU_HOST_CHUNK_MB", 256), true);
-    g_marks.clear();
-    g_marks.push_back({0, 0});
     g_inited = true;
     return 0;
 }
@@ -589,22 +604,26 @@ V initV(V x, I typ, L len) {
     return x;
 }
 
+// The heap offset (h_memory.cc:155-161 returns the arena's byte cursor) covers
+// both arenas that outputs come from, in their 256-byte allocation units:
+// bits 62..32 = device output arena bytes in use / 256 (up to 512 GiB),
+// bits 31..0 = pinned host arena bytes in use / 256 (up to 1 TiB).  It grows
+// as outputs are allocated, reading it allocates nothing, and
+// setHeapOffset(v) rewinds both arenas to where they were when v was read.
 L getHeapOffset(void) {
     if (ensure_init()) return 0;
-    g_marks.push_back({g_out->mark(), g_host->mark()});
-    return (L)(g_marks.size() - 1);
+    return (L)(((unsigned long long)(g_out->used() >> 8) << 32) | (unsigned long long)(g_host->used() >> 8));
 }
 
 L setHeapOffset(L cur) {
     if (ensure_init()) return cur;
-    if (cur < 0 || (size_t)cur >= g_marks.size()) return cur;
+    if (cur < 0) return cur;
     // work already queued (and uploads in flight) may still use the region being released
     wait_all_pending();
     cudaStreamSynchronize(g_stream);
-    g_out->rewind(g_marks[(size_t)cur].first);
-    g_host->rewind(g_marks[(size_t)cur].second);
+    g_out->rewind_used((size_t)((unsigned long long)cur >> 32) << 8);
+    g_host->rewind_used((size_t)((unsigned long long)cur & 0xffffffffull) << 8);
     prune_registries();
-    g_marks.resize((size_t)cur + 1);
     return cur;
 }
 

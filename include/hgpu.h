@@ -132,7 +132,7 @@ typedef struct NodeValue {
 void initBackend(void);
 V    allocNode(void);                       /* h_memory.cc:160-162 */
 V    initV(V x, I typ, L len);              /* h_memory.cc:182-196 (payload in the output arena) */
-L    getHeapOffset(void);                   /* h_memory.cc:155-157 */
+L    getHeapOffset(void);                   /* h_memory.cc:155-157 (both output arenas, in 256-byte units) */
 L    setHeapOffset(L cur);                  /* h_memory.cc:159-161 (rewinds device + host arenas) */
 L    getTypeSize(I typ, L len);             /* h_memory.cc:124-153 */
 /* Symbols: src/horseir/v3/backend/h_symbol.h:38-56 (interning used by @join_index's op list) */

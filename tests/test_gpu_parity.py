@@ -491,3 +491,23 @@ def test_index_many_errors(libs):
     rc, zs = index_many(gpu, [gpu.vec(a, H_E), gpu.vec(b, H_I)], gpu.vec(np.array([3, 499], np.int64), H_L))
     assert rc == 0 and gpu.to_py(zs[0]).tolist() == [a[3], a[499]] and gpu.to_py(zs[1]).tolist() == [b[3], b[499]]
     gpu.free_inputs()
+
+
+def test_heap_offset_is_a_position(libs):
+    """getHeapOffset (h_memory.cc:155-157) reads the arenas' position without
+    allocating: repeated reads give the same value, an output moves it
+    forward, and setHeapOffset returns both arenas to a value read earlier."""
+    gpu = libs[0]
+    Lb = gpu.lib
+    a = Lb.getHeapOffset()
+    assert all(Lb.getHeapOffset() == a for _ in range(100))
+    z = gpu.call("pfnPlus", gpu.vec(np.arange(100_000, dtype=np.int64), H_L), gpu.vec(np.ones(100_000, np.int64), H_L))
+    lst = gpu.call("pfnGroup", gpu.vec(np.arange(1000, dtype=np.int32) % 7, H_I))  # host nodes too
+    b = Lb.getHeapOffset()
+    assert b > a and Lb.getHeapOffset() == b
+    Lb.setHeapOffset(a)
+    assert Lb.getHeapOffset() == a
+    z2 = gpu.call("pfnPlus", gpu.vec(np.arange(100_000, dtype=np.int64), H_L), gpu.vec(np.ones(100_000, np.int64), H_L))
+    assert z2.g == z.g  # the rewound region is reused
+    del lst
+    gpu.free_inputs()
