@@ -283,6 +283,14 @@ I radix_sort(const K* keys, long long n, const K** kres, const unsigned** vres, 
 }
 
 
+template I radix_sort<unsigned>(const unsigned*, long long, const unsigned**, const unsigned**, const unsigned*);
+template I radix_sort<unsigned long long>(const unsigned long long*, long long, const unsigned long long**,
+                                          const unsigned**, const unsigned*);
+
+// the reference's comparison sorts (k_qsort.cu)
+I qs_sort_vector(const void* col, I typ, long long n, bool asc, const unsigned** perm_out);
+I qs_sort_list(int nc, const void* const* cols, const I* typs, const B* asc, long long n, const unsigned** perm_out);
+
 // ---------------------------------------------------------------- sort keys
 enum KeyXf : int {
     XF_RAW32 = 0,   // (u32)(i32)v: the reference's 32-bit pattern
@@ -967,6 +975,8 @@ I pfnGroupBasic(V z, V x) {
         if (nc == 0) return group_dict(z, r, 0, nullptr);
         if (nc > KMAXC) return set_error(E_NOT_IMPL, "group by more than %d columns", KMAXC);
         V0* c = host_nodes(x);
+        // one column: pfnOrderBy -> lib_order_basic sorts it as a vector (h_primitive.cc:1776-1778)
+        if (nc == 1) return pfnGroupBasic(z, &c[0]);
         long long n = c[0].len;
         V cols[KMAXC];
         const void* ptrs[KMAXC];
@@ -995,7 +1005,18 @@ I pfnGroupBasic(V z, V x) {
             HG_CHECK(sort_int_column(&tmp, k, n, &r));
             return group_dict(z, r, n, &cs);
         }
-        HG_CHECK(sort_columns(nc, cols, ptrs, nullptr, n, &r));
+        bool all_int = true;  // i32/i64 columns only: lib_quicksort_list merge sorts each = stable lexicographic
+        for (int i = 0; i < nc; i++) all_int = all_int && (c[i].typ == H_I || c[i].typ == H_L);
+        if (all_int) HG_CHECK(sort_columns(nc, cols, ptrs, nullptr, n, &r));
+        else {
+            I typs[KMAXC];
+            B up[KMAXC];
+            for (int i = 0; i < nc; i++) { typs[i] = c[i].typ; up[i] = 1; }
+            HG_CHECK(qs_sort_list(nc, ptrs, typs, up, n, &r.perm));
+            r.keys = nullptr;
+            r.key64 = 0;
+            r.key_injective = false;
+        }
         return group_dict(z, r, n, &cs);
     }
     if (x->typ == H_C) {
@@ -1006,12 +1027,13 @@ I pfnGroupBasic(V z, V x) {
         cs.ncol = 1; cs.col[0] = p; cs.typ[0] = H_C;
         return group_dict(z, r, x->len, &cs);
     }
-    if (is_real(x->typ) || is_dtime(x->typ)) {  // the reference uses its quicksort here: same partition
+    if (is_real(x->typ) || is_dtime(x->typ)) {  // pfnOrderBy -> lib_order_by_vector: the reference's quicksort
         const void* p;
         HG_CHECK(in_ptr(x, &p));
-        V cols[1] = {x};
-        const void* ptrs[1] = {p};
-        HG_CHECK(sort_columns(1, cols, ptrs, nullptr, x->len, &r));
+        HG_CHECK(qs_sort_vector(p, x->typ, x->len, true, &r.perm));
+        r.keys = nullptr;
+        r.key64 = 0;
+        r.key_injective = false;
         ColSet cs{};
         cs.ncol = 1; cs.col[0] = p; cs.typ[0] = x->typ;
         return group_dict(z, r, x->len, &cs);
@@ -1045,11 +1067,8 @@ static I order_basic(V z, V x, V y) {
         HG_CHECK(sort_char(p, n, &r));
         return order_output(z, r, n, false);
     }
-    if (is_real(x->typ) || is_dtime(x->typ)) {
-        V cols[1] = {x};
-        const void* ptrs[1] = {p};
-        B d[1] = {asc};
-        HG_CHECK(sort_columns(1, cols, ptrs, d, n, &r));
+    if (is_real(x->typ) || is_dtime(x->typ)) {  // lib_order_by_vector: the reference's quicksort
+        HG_CHECK(qs_sort_vector(p, x->typ, n, asc, &r.perm));
         return order_output(z, r, n, false);
     }
     return set_error(E_NOT_IMPL, "order on this type is outside the path");
@@ -1091,12 +1110,20 @@ I pfnOrderBy(V z, V x, V y) {
         if (nc == 1) return order_basic(z, &c[0], y);
         V cols[KMAXC];
         const void* ptrs[KMAXC];
+        bool all_int = true;
         for (int i = 0; i < nc; i++) {
             if (c[i].len != n) return E_LENGTH;
-            if (!(is_int(c[i].typ) || is_dtime(c[i].typ)))
-                return set_error(E_NOT_IMPL, "multi-column order on non-integer columns (the reference uses its quicksort)");
+            if (!(is_real(c[i].typ) || is_dtime(c[i].typ) || c[i].typ == H_C))
+                return set_error(E_NOT_IMPL, "order on symbol or string columns is outside the path");
             cols[i] = &c[i];
             HG_CHECK(in_ptr(&c[i], &ptrs[i]));
+            all_int = all_int && (c[i].typ == H_I || c[i].typ == H_L);
+        }
+        if (!all_int) {  // lib_quicksort_list with the quicksort or the char sort on some column
+            I typs[KMAXC];
+            for (int i = 0; i < nc; i++) typs[i] = c[i].typ;
+            HG_CHECK(qs_sort_list(nc, ptrs, typs, dir, n, &r.perm));
+            return order_output(z, r, n, false);
         }
         bool all_asc = true;
         for (int i = 0; i < nc; i++) all_asc = all_asc && dir[i];

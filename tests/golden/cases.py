@@ -209,8 +209,8 @@ def build_cases():
     add("group_trie", "pfnGroup", Ls(V(rng.integers(0, 3, 12000).astype(np.int8), H_C), V(rng.integers(0, 2, 12000).astype(np.int8), H_C)))
     add("group_list_ii", "pfnGroup", Ls(V(rng.integers(0, 20, 5000).astype(np.int32), H_I), V(rng.integers(0, 20, 5000).astype(np.int32), H_I)))
     add("group_list_li", "pfnGroup", Ls(V(rng.integers(-30, 30, 5000).astype(np.int64), H_L), V(rng.integers(-5, 5, 5000).astype(np.int32), H_I)))
-    add("group_list_jj", "pfnGroup", Ls(V(rng.integers(0, 3, 5000).astype(np.int8), H_J), V(rng.integers(0, 2, 5000).astype(np.int8), H_J)), canonical=True)
-    add("group_f64", "pfnGroup", V(np.round(rng.standard_normal(3000), 1), H_E), canonical=True)
+    add("group_list_jj", "pfnGroup", Ls(V(rng.integers(0, 3, 5000).astype(np.int8), H_J), V(rng.integers(0, 2, 5000).astype(np.int8), H_J)))
+    add("group_f64", "pfnGroup", V(np.round(rng.standard_normal(3000), 1), H_E))
     add("group_char", "pfnGroup", V(rng.integers(0, 60, 3000).astype(np.int8), H_C))
     add("group_empty", "pfnGroup", V(np.zeros(0, np.int32), H_I))
 
@@ -231,7 +231,7 @@ def build_cases():
     add("order_list_sorted_desc", "pfnOrderBy", Ls(V(np.sort(k2), H_L), V(s2, H_I)), V([0, 1], H_B))
     add("order_list_3col", "pfnOrderBy", Ls(V(rng.integers(0, 5, 3000).astype(np.int32), H_I), V(rng.integers(0, 5, 3000).astype(np.int64), H_L),
                                             V(rng.integers(0, 50, 3000).astype(np.int32), H_I)), V([1, 0, 1], H_B))
-    add("order_f64", "pfnOrderBy", V(np.round(rng.standard_normal(3000), 1), H_E), V([1], H_B), canonical=True)
+    add("order_f64", "pfnOrderBy", V(np.round(rng.standard_normal(3000), 1), H_E), V([1], H_B))
     add("order_char", "pfnOrderBy", V(rng.integers(0, 100, 3000).astype(np.int8), H_C), V([1], H_B))
     add("order_char_small", "pfnOrderBy", V([5, 3, 9, 3, 1], H_C), V([1], H_B))
 
@@ -358,4 +358,49 @@ def build_cases():
     add("like_domain", "pfnLike", V([1, 2], H_I), ("strs", [b"%"]), error=1)
     add("like_length", "pfnLike", ("strs", [b"a", b"b", b"c"]), ("strs", [b"a", b"b"]), error=5)
     add("enum_list_len", "pfnEnum", Ls(V(pk[:10], H_I), V(pk[:10], H_I)), Ls(V(fk[:10], H_I)), error=1)
+
+    # ---- the reference's quicksort paths (lib_quicksort_other h_libs.cc:409-442, lib_quicksort_list
+    #      :637-697, lib_order_by_sorted :604-617): keys other than i32/i64/char, alone and in lists,
+    #      with many ties, at 100K+ rows (own generator, so the cases above keep their inputs)
+    q = np.random.default_rng(20261204)
+    N = 120_000
+    f_ties = np.round(q.standard_normal(N), 1)                            # ~80 distinct values
+    f_ties[q.random(N) < 0.05] = -0.0                                     # -0.0 ties +0.0
+    add("qs_order_f64_asc_120k", "pfnOrderBy", V(f_ties, H_E), V([1], H_B))
+    add("qs_order_f64_desc_120k", "pfnOrderBy", V(f_ties, H_E), V([0], H_B))
+    add("qs_group_f64_120k", "pfnGroup", V(f_ties, H_E))
+    add("qs_order_f32_120k", "pfnOrderBy", V(f_ties.astype(np.float32), H_F), V([1], H_B))
+    j3 = q.integers(-1, 2, N).astype(np.int8)
+    add("qs_order_i8_120k", "pfnOrderBy", V(j3, H_J), V([1], H_B))
+    add("qs_order_i16_desc_120k", "pfnOrderBy", V(q.integers(-300, 300, N).astype(np.int16), H_H), V([0], H_B))
+    add("qs_order_bool_120k", "pfnOrderBy", V(q.random(N) < 0.5, H_B), V([1], H_B))
+    add("qs_group_bool_120k", "pfnGroup", V(q.random(N) < 0.3, H_B))
+    add("qs_group_i16_120k", "pfnGroup", V(q.integers(0, 40, N).astype(np.int16), H_H))
+    add("qs_order_date_120k", "pfnOrderBy", V(q.integers(8000, 8400, N).astype(np.int32), H_D), V([1], H_B))
+    add("qs_group_date_120k", "pfnGroup", V(q.integers(8000, 8100, N).astype(np.int32), H_D))
+    add("qs_group_list_jj_120k", "pfnGroup", Ls(V(q.integers(0, 3, N).astype(np.int8), H_J), V(q.integers(0, 2, N).astype(np.int8), H_J)))
+    add("qs_group_list_ej_120k", "pfnGroup", Ls(V(np.round(q.standard_normal(N), 0), H_E), V(q.integers(0, 4, N).astype(np.int8), H_J)))
+    add("qs_group_list_il_e", "pfnGroup", Ls(V(q.integers(0, 30, N).astype(np.int32), H_I), V(np.round(q.standard_normal(N), 0), H_E)))
+    add("qs_group_list_one_neg_i32", "pfnGroup", Ls(V(q.integers(-50, 50, 20000).astype(np.int32), H_I)))
+    add("qs_group_list_one_f64", "pfnGroup", Ls(V(np.round(q.standard_normal(20000), 1), H_E)))
+    ek, ik = np.round(q.standard_normal(N), 0), q.integers(0, 50, N).astype(np.int32)
+    add("qs_order_list_ei_asc", "pfnOrderBy", Ls(V(ek, H_E), V(ik, H_I)), V([1, 1], H_B))
+    add("qs_order_list_ei_mixed", "pfnOrderBy", Ls(V(ek, H_E), V(ik, H_I)), V([0, 1], H_B))
+    add("qs_order_list_ie_mixed", "pfnOrderBy", Ls(V(ik, H_I), V(ek, H_E)), V([1, 0], H_B))
+    add("qs_order_list_jel", "pfnOrderBy", Ls(V(j3, H_J), V(ek, H_E), V(q.integers(0, 9, N).astype(np.int64), H_L)), V([1, 0, 1], H_B))
+    add("qs_order_list_ci", "pfnOrderBy", Ls(V(q.integers(65, 70, N).astype(np.int8), H_C), V(ik, H_I)), V([1, 1], H_B))
+    add("qs_order_list_ic_small_runs", "pfnOrderBy", Ls(V(q.integers(0, 20000, 60000).astype(np.int32), H_I),
+                                                     V(q.integers(65, 90, 60000).astype(np.int8), H_C)), V([1, 1], H_B))
+    add("qs_order_list_dd", "pfnOrderBy", Ls(V(q.integers(8000, 8050, N).astype(np.int32), H_D), V(q.integers(0, 7, N).astype(np.int16), H_H)), V([0, 0], H_B))
+    # ranges already in order: kept (ascending) or reversed (descending key whose values ascend)
+    srt = np.sort(np.round(q.standard_normal(50000), 2))
+    add("qs_order_list_sorted_e_desc", "pfnOrderBy", Ls(V(srt, H_E), V(q.integers(0, 3, 50000).astype(np.int8), H_J)), V([0, 1], H_B))
+    add("qs_order_list_runs_sorted", "pfnOrderBy", Ls(V(np.repeat(np.arange(500), 100).astype(np.int32), H_I),
+                                                   V(np.tile(np.round(np.linspace(-3, 3, 100), 1), 500), H_E)), V([1, 0], H_B))
+    # deep recursion: the first-element pivot on ordered keys peels one element per level
+    add("qs_order_f64_sorted_3k", "pfnOrderBy", V(np.sort(q.standard_normal(3000)), H_E), V([1], H_B))
+    add("qs_order_f64_reverse_3k", "pfnOrderBy", V(np.sort(q.standard_normal(3000))[::-1].copy(), H_E), V([1], H_B))
+    add("qs_group_f64_tiny", "pfnGroup", V([2.0, -0.0, 0.0, 2.0, 1.5], H_E))
+    add("qs_order_f64_one", "pfnOrderBy", V([3.5], H_E), V([0], H_B))
+    add("qs_order_f64_empty", "pfnOrderBy", V(np.zeros(0), H_E), V([1], H_B))
     return cases

@@ -511,3 +511,67 @@ def test_heap_offset_is_a_position(libs):
     assert z2.g == z.g  # the rewound region is reused
     del lst
     gpu.free_inputs()
+
+
+QS_CASES = {
+    # the reference's quicksort on keys other than i32/i64/char (lib_quicksort_other h_libs.cc:409-442)
+    "order_f64_ties": ("pfnOrderBy", lambda r, n: [("vec", np.round(r.standard_normal(n), 1), H_E)], [1]),
+    "order_f64_desc": ("pfnOrderBy", lambda r, n: [("vec", np.round(r.standard_normal(n), 2), H_E)], [0]),
+    "order_f32": ("pfnOrderBy", lambda r, n: [("vec", np.round(r.standard_normal(n), 1).astype(np.float32), 5)], [1]),
+    "order_i8": ("pfnOrderBy", lambda r, n: [("vec", r.integers(-3, 3, n).astype(np.int8), 1)], [1]),
+    "order_i16": ("pfnOrderBy", lambda r, n: [("vec", r.integers(-500, 500, n).astype(np.int16), 2)], [0]),
+    "order_bool": ("pfnOrderBy", lambda r, n: [("vec", r.random(n) < 0.4, H_B)], [1]),
+    "group_f64": ("pfnGroup", lambda r, n: [("vec", np.round(r.standard_normal(n), 1), H_E)], None),
+    "group_i16": ("pfnGroup", lambda r, n: [("vec", r.integers(0, 1000, n).astype(np.int16), 2)], None),
+    # lib_quicksort_list over lists holding them (h_libs.cc:637-697)
+    "group_list_jj": ("pfnGroup", lambda r, n: [("list", [(r.integers(0, 3, n).astype(np.int8), 1),
+                                                          (r.integers(0, 2, n).astype(np.int8), 1)])], None),
+    "group_list_ei": ("pfnGroup", lambda r, n: [("list", [(np.round(r.standard_normal(n), 0), H_E),
+                                                          (r.integers(0, 100, n).astype(np.int32), H_I)])], None),
+    "order_list_ei": ("pfnOrderBy", lambda r, n: [("list", [(np.round(r.standard_normal(n), 1), H_E),
+                                                            (r.integers(0, 1000, n).astype(np.int32), H_I)])], [0, 1]),
+    "order_list_jel": ("pfnOrderBy", lambda r, n: [("list", [(r.integers(0, 4, n).astype(np.int8), 1),
+                                                             (np.round(r.standard_normal(n), 1), H_E),
+                                                             (r.integers(0, 50, n).astype(np.int64), H_L)])], [1, 0, 1]),
+    "order_list_ci": ("pfnOrderBy", lambda r, n: [("list", [(r.integers(65, 91, n).astype(np.int8), H_C),
+                                                            (r.integers(0, 300, n).astype(np.int32), H_I)])], [1, 1]),
+}
+
+
+@pytest.mark.parametrize("kind", sorted(QS_CASES))
+def test_quicksort_paths_large(libs, kind):
+    """The reference's quicksort (and the list sort around it) reproduced
+    step for step: the permutation, or the groups with their keys and row
+    order, bit-exact against the oracle's restatement at 1.5M rows."""
+    fn, mk, dirs = QS_CASES[kind]
+    import zlib
+    rng = np.random.default_rng(zlib.crc32(kind.encode()))
+    spec = mk(rng, 1_500_000)
+
+    def args(L):
+        out = []
+        for a in spec:
+            if a[0] == "vec":
+                out.append(L.vec(a[1], a[2]))
+            else:
+                out.append(L.list([L.vec(v, t) for v, t in a[1]]))
+        if dirs is not None:
+            out.append(L.vec(np.array(dirs, bool), H_B))
+        return tuple(out)
+    a, b = both(libs, fn, args)
+    assert same(a, b)
+
+
+def test_quicksort_nan_key_refused(libs):
+    """A NaN key sends the reference's quicksort outside its range
+    (undefined): the library refuses it with E_NOT_IMPL and stays usable."""
+    gpu = libs[0]
+    x = np.round(np.random.default_rng(3).standard_normal(5000), 1)
+    x[1234] = np.nan
+    rc = gpu.rc("pfnOrderBy", gpu.vec(x, H_E), gpu.vec(np.array([1], bool), H_B))
+    assert rc == 99
+    rc = gpu.rc("pfnGroup", gpu.vec(x, H_E))
+    assert rc == 99
+    ok = gpu.to_py(gpu.call("pfnOrderBy", gpu.vec(np.nan_to_num(x), H_E), gpu.vec(np.array([1], bool), H_B)))
+    assert ok.size == x.size
+    gpu.free_inputs()
