@@ -465,7 +465,8 @@ def run_served(args):
     clocks.start()
     l0 = Lb.hgpuLaunchCount()
     for rate in rates:
-        n = max(50, int(rate * args.serve_seconds))
+        secs = args.serve_seconds if rate <= 5000 else min(args.serve_seconds, 5000 * args.serve_seconds / rate * 2)
+        n = max(50, int(rate * secs))
         reqs = S.request_stream(n, rate, seed=7 + rate)
         row = {"rate": rate, "requests": n}
         for name, mode in (("served", S.BATCHED), ("plain", S.PLAIN)):
@@ -648,6 +649,56 @@ def run_builtins(args):
                                "larger than L2 (except the 6M-row table)", "peak_gbs": hbm, "peak_source": src},
         "builtins": rows,
     }
+
+
+def run_extras(args):
+    """The rest of the metric, measured in the same process after the
+    headline: each builtin alone (the configurations' shapes, C0's plain and
+    fused q6 chain, C2's group / group-sum / order at 150M rows), the batched
+    256-plan form against the same plans one at a time (C3), and the served
+    loop against one request per launch sequence at 1,000 and 5,000 req/s and
+    at an offered rate above its capacity (C4).  Each part has its own timed
+    regions and clock samples; a part that fails is reported, not fatal."""
+    import horsepower_gb300
+    Lb = horsepower_gb300.load().lib
+    Lb.getHeapOffset.restype = C.c_longlong
+    Lb.setHeapOffset.argtypes = [C.c_longlong]
+    out = {}
+    sub = argparse.Namespace(**vars(args))
+    sub.steps = min(args.steps, 10)
+    sub.warmup = min(args.warmup, 3)
+    sub.rates = "1000,5000,20000"
+    sub.serve_seconds = 1.0
+    for name, fn in (("builtins", run_builtins), ("batched", run_batched), ("served", run_served)):
+        mark = Lb.getHeapOffset()
+        t0 = time.perf_counter()
+        try:
+            r = fn(sub)
+            if name == "builtins":
+                r = {"peak_gbs": r["config"]["peak_gbs"], "peak_source": r["config"]["peak_source"],
+                     "note": "algorithmic bytes (inputs read once + outputs written once) / summed CUDA-event time "
+                             "of the call's kernels; call_ms includes host work and result-size reads",
+                     "table": {k: {"rows": v["rows"], "call_ms": v["call_ms"], "kernel_ms": v["kernel_ms"],
+                                   "rows_per_s": round(v["rows_per_s"]), "gbs": v["gbs_kernels"],
+                                   "frac_of_peak": v["frac_kernels"]} for k, v in r["builtins"].items()}}
+            elif name == "batched":
+                r = {k: r[k] for k in ("metric", "value", "unit", "ms_per_step", "plain_one_at_a_time",
+                                        "speedup_vs_plain", "bit_exact_vs_plain", "fact_rows_per_s", "gpu_launches",
+                                        "clocks", "config")} | {"autotune_chosen": r["autotune"]["chosen"]}
+            else:
+                r = {"metric": r["metric"], "clocks": r["clocks"], "gpu_launches": r["gpu_launches"],
+                     "rates": [{"offered_req_s": row["rate"], "requests": row["requests"],
+                                "served": {k: row["served"][k] for k in ("qps", "p50_ms", "p99_ms", "max_step_requests")},
+                                "plain": {k: row["plain"][k] for k in ("qps", "p50_ms", "p99_ms")},
+                                "qps_vs_plain": round(row["served"]["qps"] / max(row["plain"]["qps"], 1e-9), 2)}
+                               for row in r["rates"]]}
+        except Exception as e:  # reported in the line; the headline stands
+            r = {"error": f"{type(e).__name__}: {e}"}
+        r["wall_s"] = round(time.perf_counter() - t0, 1)
+        out[name] = r
+        Lb.hgpuSync()
+        Lb.setHeapOffset(mark)
+    return out
 
 
 def run_ingest(args):
@@ -1023,6 +1074,8 @@ def main():
     ap.add_argument("--reps", type=int, default=3, help="with --workload case: calls to time")
     ap.add_argument("--tune", action="append", default=[], help="with --workload case: knob=value")
     ap.add_argument("--ingest-rows", type=int, default=6_001_215)
+    ap.add_argument("--headline-only", action="store_true",
+                    help="default workload: skip the per-builtin, batched and served parts after the headline")
     ap.add_argument("--rates", default="200,1000,5000")
     ap.add_argument("--serve-seconds", type=float, default=1.5)
     ap.add_argument("--order-rows", type=int, default=150_000_000)
@@ -1109,6 +1162,8 @@ def main():
                          "without them)"),
         "builtins": builtins,
     }
+    if not args.headline_only:
+        line["configs"] = run_extras(args)
     print(json.dumps(line))
 
 

@@ -71,7 +71,8 @@ constexpr unsigned long long LB_AGG = 1ull << 62, LB_INC = 2ull << 62, LB_MASK =
 // Called by one full warp (warp 0) of the tile.  Publishes `agg` and returns
 // the exclusive prefix of tile `t` (valid in all lanes).
 __device__ __forceinline__ unsigned long long lookback_exclusive(unsigned long long* status, long long t,
-                                                                 unsigned long long agg, unsigned* derr) {
+                                                                 unsigned long long agg, unsigned* derr,
+                                                                 long long limit = SPIN_LIMIT) {
     const unsigned lane = lane_id();
     if (t == 0) {
         if (lane == 0) st_release(&status[0], LB_INC | agg);
@@ -91,7 +92,7 @@ __device__ __forceinline__ unsigned long long lookback_exclusive(unsigned long l
         int stop = inc ? __ffs(inc) - 1 : 31;
         unsigned upto = stop == 31 ? 0xffffffffu : ((1u << (stop + 1)) - 1u);
         if (notready & upto) {
-            if (++spins > SPIN_LIMIT) {
+            if (++spins > limit) {
                 if (lane == 0) flag_error(derr, DERR_TIMEOUT);
                 break;
             }
@@ -146,7 +147,8 @@ __device__ __forceinline__ unsigned long long lookback_seg(unsigned long long* s
 // in [first, t)), one thread per chain: the per-digit prefixes of the radix
 // passes.
 __device__ __forceinline__ unsigned long long chain_lookback(unsigned long long* status, size_t stride, long long t,
-                                                             long long first, unsigned long long c, unsigned* derr) {
+                                                             long long first, unsigned long long c, unsigned* derr,
+                                                             long long limit = SPIN_LIMIT) {
     unsigned long long* st = status + (size_t)t * stride;
     if (t == first) {
         st_release(st, LB_INC | c);
@@ -159,7 +161,7 @@ __device__ __forceinline__ unsigned long long chain_lookback(unsigned long long*
         unsigned long long sv = ld_acquire(status + (size_t)j * stride);
         unsigned long long f = sv >> 62;
         if (f == 0) {
-            if (++spins > SPIN_LIMIT) { flag_error(derr, DERR_TIMEOUT); break; }
+            if (++spins > limit) { flag_error(derr, DERR_TIMEOUT); break; }
             continue;
         }
         excl += sv & LB_MASK;

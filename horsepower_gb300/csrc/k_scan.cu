@@ -65,4 +65,36 @@ I scan_exclusive(const unsigned* in, long long n, unsigned long long* out, unsig
     return 0;
 }
 
+// Self-test of the bounded device waits: a look-back over four tiles in
+// which tile 0 never publishes its status (a flag nothing sets).  The waits
+// of the later tiles give up after `limit` polls each, record DERR_TIMEOUT
+// and return, so the kernel ends and the context stays usable.  mode 0: the
+// block-wide look-back of the scans and compactions; mode 1: the per-digit
+// chain look-back of the radix passes.
+__global__ void k_selftest_wait(unsigned long long* status, unsigned* ticket, int mode, long long limit, unsigned* derr) {
+    __shared__ long long tile;
+    if (threadIdx.x == 0) tile = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const long long t = tile;
+    if (t == 0) return;  // withholds its status
+    if (mode == 0) lookback_exclusive(status, t, 1, derr, limit);  // one full warp per tile
+    else if (threadIdx.x == 0) chain_lookback(status, 1, t, 0, 1, derr, limit);
+}
+
 }  // namespace hg
+
+using namespace hg;
+
+extern "C" I hgpuSelfTestWait(I mode, L limit) {
+    HG_CHECK(ensure_init());
+    ScratchScope ss;
+    if (mode < 0 || mode > 1) return set_error(E_DOMAIN, "hgpuSelfTestWait: mode %d is not 0 or 1", mode);
+    if (limit < 1 || limit > (1LL << 20)) return set_error(E_DOMAIN, "hgpuSelfTestWait: limit %lld outside [1, 2^20]", limit);
+    char* s = (char*)salloc(256);
+    if (!s) return E_DEVICE_OOM;
+    HG_CU(cudaMemsetAsync(s, 0, 256, g_stream));
+    HG_LAUNCH("selftest_wait", 4, 32, 0, k_selftest_wait, (unsigned long long*)s, (unsigned*)(s + 128), (int)mode,
+              (long long)limit, g_derr);
+    HG_CHECK(last_launch_error());
+    return check_device_errors();
+}

@@ -5,6 +5,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <dlfcn.h>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -22,7 +23,7 @@ static cudaStream_t g_copy_stream = nullptr;  // asynchronous uploads (hgpuToDev
 int g_sms = 0;
 unsigned* g_derr = nullptr;
 int g_reduce_mode = 1;
-static int g_residency = HGPU_RESIDENT_DEVICE;
+static int g_residency = -1;  // decided at first use (residency())
 static bool g_inited = false;
 static std::mutex g_init_mu;
 static long long g_launches = 0;
@@ -61,10 +62,16 @@ struct Arena {
     size_t cur_chunk = 0;
     size_t chunk_bytes;
     bool host;
+    size_t limit;                          // most bytes of chunks held at once (0: no limit)
     size_t last_off = 0, last_bytes = 0;  // last allocation (for shrinking)
     long long last_chunk = -1;
 
-    Arena(size_t cb, bool h) : chunk_bytes(cb), host(h) {}
+    Arena(size_t cb, bool h, size_t lim = 0) : chunk_bytes(cb), host(h), limit(lim) {}
+    size_t held() const {
+        size_t t = 0;
+        for (const Chunk& c : chunks) t += c.cap;
+        return t;
+    }
 
     void* alloc(size_t bytes) {
         size_t need = (bytes + 255) & ~(size_t)255;
@@ -87,6 +94,15 @@ struct Arena {
                 }
             }
             size_t cap = need > chunk_bytes ? need : chunk_bytes;
+            if (limit) {  // a capped arena grows only up to its limit
+                const size_t h = held();
+                if (h + need > limit) {
+                    set_error(E_DEVICE_OOM, "%s arena: %zu more bytes would pass its limit of %zu bytes",
+                              host ? "host" : "device", need, limit);
+                    return nullptr;
+                }
+                if (h + cap > limit) cap = limit - h;
+            }
             char* base = nullptr;
             cudaError_t e = host ? cudaHostAlloc((void**)&base, cap, cudaHostAllocPortable | cudaHostAllocMapped)
                                  : cudaMalloc((void**)&base, cap);
@@ -204,9 +220,11 @@ I ensure_init() {
     HG_CU(cudaMalloc((void**)&g_derr, 256));
     HG_CU(cudaMemset(g_derr, 0, 256));
     HG_CU(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t)g_l2_fetch));
-    if (!g_out) g_out = new Arena(env_mb("HGPU_DEVICE_CHUNK_MB", 4096), false);
-    if (!g_scratch) g_scratch = new Arena(env_mb("HGPU_SCRATCH_CHUNK_MB", 4096), false);
-    if (!g_host) g_host = new Arena(env_mb("HGPU_HOST_CHUNK_MB", 256), true);
+    // HGPU_*_LIMIT_MB caps an arena's total size (0 or unset: no cap); a call
+    // that needs more returns E_DEVICE_OOM
+    if (!g_out) g_out = new Arena(env_mb("HGPU_DEVICE_CHUNK_MB", 4096), false, env_mb("HGPU_DEVICE_LIMIT_MB", 0));
+    if (!g_scratch) g_scratch = new Arena(env_mb("HGPU_SCRATCH_CHUNK_MB", 4096), false, env_mb("HGPU_SCRATCH_LIMIT_MB", 0));
+    if (!g_host) g_host = new Arena(env_mb("HGPU_HOST_CHUNK_MB", 256), true, env_mb("HGPU_HOST_LIMIT_MB", 0));
     g_inited = true;
     return 0;
 }
@@ -264,7 +282,27 @@ bool host_readable(const void* p) {
     }
     return a.type != cudaMemoryTypeDevice;
 }
-int residency() { return g_residency; }
+// Default residency.  When the process also holds another builtin library
+// (the reference's libcore linked after libhgpu supplies every builtin
+// libhgpu does not export, h_primitive.h:72-211), that library's builtins
+// dereference payloads on the host, so outputs are copied to pinned host
+// memory by default; alone, outputs stay in HBM.  HGPU_RESIDENCY=host|device
+// in the environment, or hgpuSetResidency, decides instead.
+static const char* const k_foreign_builtins[] = {"pfnUnique", "pfnVector", "pfnAppend", "pfnDateYear"};
+bool foreign_builtins_linked() {
+    for (const char* name : k_foreign_builtins)
+        if (dlsym(RTLD_DEFAULT, name)) return true;
+    return false;
+}
+int residency() {
+    if (g_residency < 0) {
+        const char* e = getenv("HGPU_RESIDENCY");
+        if (e && !strcmp(e, "host")) g_residency = HGPU_RESIDENT_HOST;
+        else if (e && !strcmp(e, "device")) g_residency = HGPU_RESIDENT_DEVICE;
+        else g_residency = foreign_builtins_linked() ? HGPU_RESIDENT_HOST : HGPU_RESIDENT_DEVICE;
+    }
+    return g_residency;
+}
 
 int esize(I t) {
     switch (t) {
@@ -435,7 +473,7 @@ static I to_host_rec(V z, V x, bool in_place) {
 }
 
 I apply_residency(V z) {
-    if (g_residency != HGPU_RESIDENT_HOST) return 0;
+    if (residency() != HGPU_RESIDENT_HOST) return 0;
     return to_host_rec(z, z, true);
 }
 
@@ -651,7 +689,7 @@ I hgpuSetResidency(I mode) {
     g_residency = mode;
     return 0;
 }
-I hgpuGetResidency(void) { return g_residency; }
+I hgpuGetResidency(void) { return residency(); }
 
 I hgpuToHost(V z, V x) {
     HG_CHECK(ensure_init());

@@ -360,6 +360,16 @@ double hgpuTimerStop(void);
 I    hgpuSetTuning(I knob, E value);
 E    hgpuGetTuning(I knob);
 
+/* Self-test of the bounded device waits (no counterpart in the reference):
+ * runs a four-tile look-back whose first tile never publishes, so the other
+ * tiles' waits give up after `limit` polls (1 .. 2^20).  Returns
+ * E_DEVICE_TIMEOUT, as any builtin whose wait gave up does, and leaves the
+ * library usable.  mode 0: the scans' look-back; 1: the radix passes' chain
+ * look-back.  Arena caps for out-of-memory handling come from the
+ * environment at first use: HGPU_DEVICE_LIMIT_MB, HGPU_SCRATCH_LIMIT_MB,
+ * HGPU_HOST_LIMIT_MB (a call that needs more returns E_DEVICE_OOM). */
+I    hgpuSelfTestWait(I mode, L limit);
+
 /* Allocation-free f64 sum (no counterpart in the reference).  For callers that
  * cannot allocate device memory where they need a sum: an engine that works in
  * a fixed device-memory budget reserved up front, or a path that cannot take
