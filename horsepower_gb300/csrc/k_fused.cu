@@ -317,11 +317,17 @@ static I compile_chain(hgpu_chain_s* c, const std::vector<int>& types, std::shar
                 while (!st.empty()) { Node* q = st.back(); st.pop_back(); if (q->op == "x") in_val[q->col] = true; for (auto& k : q->kids) st.push_back(k.get()); }
             }
         }
-        std::string vloads;
-        for (int k = 0; k < nin; k++)
-            if (in_val[k] && !in_mask[k])
-                vloads += std::string("            ") + ctype(types[k]) + " v" + std::to_string(k) + " = ((const " + ctype(types[k]) +
-                          "*)cols[" + std::to_string(k) + "])[i];\n";
+        std::string vloads, hoist, preload, unpack;
+        for (int k = 0; k < nin; k++) {
+            const std::string K = std::to_string(k), T = ctype(types[k]);
+            if (in_mask[k] || in_val[k]) hoist += "    const " + T + "* __restrict__ c" + K + " = (const " + T + "*)cols[" + K + "];\n";
+            if (in_val[k] && !in_mask[k]) vloads += "                " + T + " v" + K + " = c" + K + "[i];\n";
+            if (in_mask[k]) {
+                preload += "        a" + K + "[k] = in ? c" + K + "[i] : (" + T + ")0;\n";
+                hoist += "    " + T + " a" + K + "[16];\n";
+                unpack += "            " + T + " v" + K + " = a" + K + "[k];\n";
+            }
+        }
         int vt = r->op == "count" ? H_L : arith_rank(r->kids[0]->typ);
         int at = r->op == "count" ? H_L : (r->op == "sum" ? (vt == H_F ? H_F : vt == H_E ? H_E : H_L) : vt);
         cm->acc_typ = at;
@@ -329,25 +335,54 @@ static I compile_chain(hgpu_chain_s* c, const std::vector<int>& types, std::shar
         std::string opf = r->op == "min" ? "(a < b ? a : b)" : r->op == "max" ? "(a > b ? a : b)"
                         : (at == H_E ? "__dadd_rn(a, b)" : at == H_F ? "__fadd_rn(a, b)" : "(long long)((unsigned long long)a + (unsigned long long)b)");
         std::string ident = r->op == "min" ? "ident" : r->op == "max" ? "ident" : std::string("(") + A + ")0";
-        for (int k = 0; k < nin; k++) g.used[k] = in_mask[k];
-        gen_loads();
+        // Each block reduces one 4096-row tile in the tile-tree order: lane t
+        // takes rows t, t+256, ..., t+3840 (the mask columns of all 16 rows
+        // are loaded before the first is used, so the loads overlap), then a
+        // xor butterfly and the pairwise combine of the 8 warps.  With
+        // `result` set, the block that finishes last reduces the tile
+        // partials by the same tree (one tile of partials: at most 4096
+        // blocks) and writes the result, so the chain is one launch.
+        std::string tree =
+            "    for (int o = 16; o > 0; o >>= 1) acc = hg_op(acc, __shfl_xor_sync(0xffffffffu, acc, o));\n"
+            "    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;\n"
+            "    __syncthreads();\n"
+            "    const " + std::string(A) + " blk = hg_op(hg_op(hg_op(ws[0], ws[1]), hg_op(ws[2], ws[3])),"
+            " hg_op(hg_op(ws[4], ws[5]), hg_op(ws[6], ws[7])));\n";
         src += std::string("__device__ __forceinline__ ") + A + " hg_op(" + A + " a, " + A + " b) { return " + opf + "; }\n";
         src += std::string("extern \"C\" __global__ void __launch_bounds__(256) chain_kernel(const void* const* cols, long long n, ") + A +
-               "* part, " + A + " ident, unsigned* derr) {\n"
+               "* part, " + A + " ident, unsigned* derr, unsigned* done, " + A + "* result) {\n"
                "    __shared__ " + A + " ws[8];\n"
-               "    long long base = (long long)blockIdx.x * 4096;\n"
-               "    " + A + " acc = " + ident + ";\n    bool dz = false;\n"
+               "    __shared__ bool last;\n"
+               "    const long long base = (long long)blockIdx.x * 4096;\n" + hoist +
+               "    #pragma unroll\n"
                "    for (int k = 0; k < 16; k++) {\n"
-               "        long long i = base + k * 256 + threadIdx.x;\n"
-               "        if (i >= n) break;\n" + loads +
-               "        if (" + mask + ") {\n" + vloads + "            acc = hg_op(acc, (" + A + ")(" + val + "));\n        }\n"
+               "        const long long i = base + k * 256 + threadIdx.x;\n"
+               "        const bool in = i < n;\n" + preload +
                "    }\n"
-               "    for (int o = 16; o > 0; o >>= 1) acc = hg_op(acc, __shfl_xor_sync(0xffffffffu, acc, o));\n"
-               "    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;\n"
+               "    " + A + " acc = " + ident + ";\n    bool dz = false;\n"
+               "    #pragma unroll\n"
+               "    for (int k = 0; k < 16; k++) {\n"
+               "        const long long i = base + k * 256 + threadIdx.x;\n"
+               "        if (i < n) {\n" + unpack +
+               "            if (" + mask + ") {\n" + vloads + "                acc = hg_op(acc, (" + A + ")(" + val + "));\n            }\n"
+               "        }\n"
+               "    }\n" + tree +
+               "    if (threadIdx.x == 0) part[blockIdx.x] = blk;\n"
+               "    if (dz) atomicOr(derr, 4u);\n"
+               "    if (!result) return;\n"
+               "    __threadfence();\n"
                "    __syncthreads();\n"
-               "    if (threadIdx.x == 0) part[blockIdx.x] = hg_op(hg_op(hg_op(ws[0], ws[1]), hg_op(ws[2], ws[3])),"
-               " hg_op(hg_op(ws[4], ws[5]), hg_op(ws[6], ws[7])));\n"
-               "    if (dz) atomicOr(derr, 4u);\n}\n";
+               "    if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;\n"
+               "    __syncthreads();\n"
+               "    if (!last) return;\n"
+               "    __threadfence();\n"
+               "    acc = " + ident + ";\n"
+               "    for (int k = 0; k < 16; k++) {\n"
+               "        const long long i = k * 256 + threadIdx.x;\n"
+               "        acc = hg_op(acc, i < gridDim.x ? ((volatile " + A + "*)part)[i] : ident);\n"
+               "    }\n"
+               "    __syncthreads();\n" + tree +
+               "    if (threadIdx.x == 0) *result = blk;\n}\n";
     } else if (r->op == "compress" || r->op == "map") {
         if (r->kids.empty()) return set_error(E_DOMAIN, "chain: %s needs operands", r->op.c_str());
         bool isc = r->op == "compress";
@@ -499,13 +534,22 @@ static I run_chain(hgpu_chain_s* c, V z, V* zs_many, V* x) {
         default: ident.b = mn; break;
         }
     }
-    void* args[] = {&dcols, &nn, &part, &ident, &g_derr};
+    // up to one tile of tile partials: the last block reduces them in the
+    // same launch; more: a separate tree over the partials
+    const bool one_launch = tiles <= TILE_SUM;
+    unsigned* done = (unsigned*)salloc(16);
+    if (!done) return E_DEVICE_OOM;
+    void* rptr = one_launch ? res : nullptr;
+    if (one_launch) HG_CU(cudaMemsetAsync(done, 0, 4, g_stream));
+    void* args[] = {&dcols, &nn, &part, &ident, &g_derr, &done, &rptr};
     {
         LaunchScope ls("chain");
         HG_CU(cudaLaunchKernel((const void*)cm->kern, dim3((unsigned)tiles), dim3(256), args, 0, g_stream));
     }
-    int op = cm->sink == "min" ? 1 : cm->sink == "max" ? 2 : 0;
-    HG_CHECK(tree_reduce_any(cm->acc_typ, op, part, tiles, res));
+    if (!one_launch) {
+        int op = cm->sink == "min" ? 1 : cm->sink == "max" ? 2 : 0;
+        HG_CHECK(tree_reduce_any(cm->acc_typ, op, part, tiles, res));
+    }
     HG_CHECK(check_device_errors());
     z->typ = cm->acc_typ;
     z->len = 1;

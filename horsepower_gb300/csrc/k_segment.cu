@@ -320,6 +320,73 @@ static unsigned gcap(long long n, int per = 256) {
     return g > (unsigned)g_sms * 32 ? (unsigned)g_sms * 32 : g;
 }
 
+// Segment ids by size class (kept with the list when there is one, with a
+// host copy of the class counts so that empty classes launch nothing).
+static I seg_classes(const long long* starts, long long ng, long long total, ListInfo* li, const unsigned** ids,
+                     const unsigned** ccnt) {
+    if (li && li->cls_ids) {
+        *ids = li->cls_ids;
+        *ccnt = li->cls_cnt;
+        return 0;
+    }
+    unsigned* cc = (unsigned*)(li ? dalloc(2 * SEG_CLASSES * 4) : salloc(2 * SEG_CLASSES * 4));
+    unsigned* id = (unsigned*)(li ? dalloc((size_t)ng * 4) : salloc((size_t)ng * 4));
+    if (!cc || !id) return E_DEVICE_OOM;
+    HG_CU(cudaMemsetAsync(cc, 0, 2 * SEG_CLASSES * 4, g_stream));
+    const unsigned gb = (unsigned)((ng + 255) / 256);
+    HG_LAUNCH("seg_class", gb, 256, 0, k_seg_class_count, starts, ng, total, cc);
+    HG_LAUNCH("seg_class_ids", gb, 256, 0, k_seg_class_ids, starts, ng, total, (const unsigned*)cc,
+              cc + SEG_CLASSES, id);
+    *ids = id;
+    *ccnt = cc;
+    if (li) {
+        li->cls_ids = id;
+        li->cls_cnt = cc;
+        // a list's segments are reduced several times (one aggregate per
+        // column): read the class counts once, so empty classes are skipped
+        HG_CU(cudaMemcpyAsync(li->cls_host, cc, sizeof(li->cls_host), cudaMemcpyDeviceToHost, g_stream));
+        HG_CU(cudaStreamSynchronize(g_stream));
+        li->cls_known = 1;
+    }
+    return last_launch_error();
+}
+
+// The split of the segments longer than one tile into 4096-element chunks:
+// big[k] = the k-th long segment, chunk0[k] its first chunk, pstarts[k] the
+// same as i64, nchunks in all (kept with the list when there is one).
+struct LongPlan {
+    long long nbig = 0;
+    unsigned long long nchunks = 0;
+    const long long* big = nullptr;
+    const unsigned long long* c0 = nullptr;
+    const long long* pstarts = nullptr;
+};
+static I seg_plan_long(const long long* starts, long long ng, long long total, ListInfo* li, LongPlan* pl) {
+    if (li && li->planned) {
+        pl->nbig = li->nbig; pl->nchunks = li->nchunks; pl->big = li->big; pl->c0 = li->chunk0; pl->pstarts = li->pstarts;
+        return 0;
+    }
+    uint8_t* f = (uint8_t*)salloc((size_t)ng);
+    long long* bigs = (long long*)(li ? dalloc((size_t)ng * 8) : salloc((size_t)ng * 8));
+    if (!f || !bigs) return E_DEVICE_OOM;
+    HG_LAUNCH("seg_flags", gcap(ng), 256, 0, k_big_flags, starts, ng, total, f, (unsigned*)nullptr);
+    long long nbig = 0;
+    unsigned long long nchunks = 0;
+    HG_CHECK(compact_rows(f, ng, bigs, &nbig));
+    unsigned* nch = (unsigned*)salloc((size_t)(nbig > 0 ? nbig : 1) * 4);
+    unsigned long long* c0s = (unsigned long long*)(li ? dalloc((size_t)(nbig > 0 ? nbig : 1) * 8) : salloc((size_t)(nbig > 0 ? nbig : 1) * 8));
+    long long* ps = (long long*)(li ? dalloc((size_t)(nbig > 0 ? nbig : 1) * 8) : salloc((size_t)(nbig > 0 ? nbig : 1) * 8));
+    if (!nch || !c0s || !ps) return E_DEVICE_OOM;
+    if (nbig > 0) {
+        HG_LAUNCH("seg_chunks", gcap(nbig), 256, 0, k_big_chunks, starts, ng, total, bigs, nbig, nch);
+        HG_CHECK(scan_exclusive(nch, nbig, c0s, &nchunks));
+        HG_LAUNCH("u64_to_i64", gcap(nbig), 256, 0, k_u64_to_i64, c0s, nbig, ps);
+    }
+    pl->nbig = nbig; pl->nchunks = nchunks; pl->big = bigs; pl->c0 = c0s; pl->pstarts = ps;
+    if (li) { li->planned = 1; li->nbig = nbig; li->nchunks = nchunks; li->big = bigs; li->chunk0 = c0s; li->pstarts = ps; }
+    return last_launch_error();
+}
+
 // Reduces every segment of (src via rows | src) into out[ng] (device).  When
 // `li` is given, the split of the long segments is computed once per list
 // and kept with it.
@@ -327,32 +394,8 @@ template <typename T, typename A, int OP, bool GATHER>
 static I seg_reduce(const T* src, const long long* rows, long long nx, const long long* starts, long long ng,
                     long long total, A ident, A* out, ListInfo* li = nullptr) {
     if (ng == 0) return 0;
-    // segment ids by size class (kept with the list when there is one)
     const unsigned *ids, *ccnt;
-    if (li && li->cls_ids) {
-        ids = li->cls_ids;
-        ccnt = li->cls_cnt;
-    } else {
-        unsigned* cc = (unsigned*)(li ? dalloc(2 * SEG_CLASSES * 4) : salloc(2 * SEG_CLASSES * 4));
-        unsigned* id = (unsigned*)(li ? dalloc((size_t)ng * 4) : salloc((size_t)ng * 4));
-        if (!cc || !id) return E_DEVICE_OOM;
-        HG_CU(cudaMemsetAsync(cc, 0, 2 * SEG_CLASSES * 4, g_stream));
-        const unsigned gb = (unsigned)((ng + 255) / 256);
-        HG_LAUNCH("seg_class", gb, 256, 0, k_seg_class_count, starts, ng, total, cc);
-        HG_LAUNCH("seg_class_ids", gb, 256, 0, k_seg_class_ids, starts, ng, total, (const unsigned*)cc,
-                  cc + SEG_CLASSES, id);
-        ids = id;
-        ccnt = cc;
-        if (li) {
-            li->cls_ids = id;
-            li->cls_cnt = cc;
-            // a list's segments are reduced several times (one aggregate per
-            // column): read the class counts once, so empty classes are skipped
-            HG_CU(cudaMemcpyAsync(li->cls_host, cc, sizeof(li->cls_host), cudaMemcpyDeviceToHost, g_stream));
-            HG_CU(cudaStreamSynchronize(g_stream));
-            li->cls_known = 1;
-        }
-    }
+    HG_CHECK(seg_classes(starts, ng, total, li, &ids, &ccnt));
     const bool known = li && li->cls_known;
     bool small = true, mid = true;
     if (known) {
@@ -367,46 +410,117 @@ static I seg_reduce(const T* src, const long long* rows, long long nx, const lon
         HG_LAUNCH("seg_mid", gcap(ng), 256, 0, (k_seg_mid<T, A, OP, GATHER>), src, rows, nx, starts, ng, total, ids,
                   ccnt, ident, out, g_derr);
     if (known && li->cls_host[7] == 0) return last_launch_error();
-    long long nbig = 0;
-    unsigned long long nchunks = 0;
-    const long long *big, *pstarts;
-    const unsigned long long* c0;
-    if (li && li->planned) {
-        nbig = li->nbig; nchunks = li->nchunks; big = li->big; c0 = li->chunk0; pstarts = li->pstarts;
-    } else {
-        uint8_t* f = (uint8_t*)salloc((size_t)ng);
-        long long* bigs = (long long*)(li ? dalloc((size_t)ng * 8) : salloc((size_t)ng * 8));
-        if (!f || !bigs) return E_DEVICE_OOM;
-        HG_LAUNCH("seg_flags", gcap(ng), 256, 0, k_big_flags, starts, ng, total, f, (unsigned*)nullptr);
-        HG_CHECK(compact_rows(f, ng, bigs, &nbig));
-        unsigned* nch = (unsigned*)salloc((size_t)(nbig > 0 ? nbig : 1) * 4);
-        unsigned long long* c0s = (unsigned long long*)(li ? dalloc((size_t)(nbig > 0 ? nbig : 1) * 8) : salloc((size_t)(nbig > 0 ? nbig : 1) * 8));
-        long long* ps = (long long*)(li ? dalloc((size_t)(nbig > 0 ? nbig : 1) * 8) : salloc((size_t)(nbig > 0 ? nbig : 1) * 8));
-        if (!nch || !c0s || !ps) return E_DEVICE_OOM;
-        if (nbig > 0) {
-            HG_LAUNCH("seg_chunks", gcap(nbig), 256, 0, k_big_chunks, starts, ng, total, bigs, nbig, nch);
-            HG_CHECK(scan_exclusive(nch, nbig, c0s, &nchunks));
-            HG_LAUNCH("u64_to_i64", gcap(nbig), 256, 0, k_u64_to_i64, c0s, nbig, ps);
-        }
-        big = bigs; c0 = c0s; pstarts = ps;
-        if (li) { li->planned = 1; li->nbig = nbig; li->nchunks = nchunks; li->big = bigs; li->chunk0 = c0s; li->pstarts = ps; }
-    }
+    LongPlan pl;
+    HG_CHECK(seg_plan_long(starts, ng, total, li, &pl));
+    const long long nbig = pl.nbig;
+    const unsigned long long nchunks = pl.nchunks;
     if (nbig == 0) return last_launch_error();
     A* part = (A*)salloc((size_t)nchunks * sizeof(A));
     A* res = (A*)salloc((size_t)nbig * sizeof(A));
     if (!part || !res) return E_DEVICE_OOM;
     HG_LAUNCH("seg_chunk", (unsigned)nchunks, 256, 0, (k_seg_chunk<T, A, OP, GATHER>), src, rows, nx, starts, ng,
-              total, big, c0, nbig, ident, part, g_derr);
+              total, pl.big, pl.c0, nbig, ident, part, g_derr);
     // partials of each long segment are reduced by the same procedure: at
     // most 4096 of them per segment (certain when there are at most 4096 in
     // all) in one launch straight into out, else as segments of their own
     if (nchunks <= (unsigned long long)TILE_SUM) {
-        HG_LAUNCH("seg_partials", (unsigned)nbig, 256, 0, (k_seg_partials<A, OP>), part, pstarts, big, nbig,
+        HG_LAUNCH("seg_partials", (unsigned)nbig, 256, 0, (k_seg_partials<A, OP>), part, pl.pstarts, pl.big, nbig,
                   (long long)nchunks, ident, out);
         return last_launch_error();
     }
-    HG_CHECK((seg_reduce<A, A, OP, false>(part, nullptr, 0, pstarts, nbig, (long long)nchunks, ident, res)));
-    HG_LAUNCH("scatter_big", gcap(nbig), 256, 0, k_scatter_big<A>, res, big, nbig, out);
+    HG_CHECK((seg_reduce<A, A, OP, false>(part, nullptr, 0, pl.pstarts, nbig, (long long)nchunks, ident, res)));
+    HG_LAUNCH("scatter_big", gcap(nbig), 256, 0, k_scatter_big<A>, res, pl.big, nbig, out);
+    return last_launch_error();
+}
+
+// ---- several f64 sums over the long segments of one grouping at once.
+// One CTA per 4096-element chunk, as k_seg_chunk, but the chunk's row ids
+// are read once and each of the ncol columns is gathered through them (all
+// 16 x ncol gathers of a lane issued before the first add); each column's
+// chunk partial follows the tile tree, so part[col * nchunks + c] is
+// bit-identical to k_seg_chunk's for that column.
+constexpr int SEG_MANY = 4;
+struct SegCols { const double* src[SEG_MANY]; };
+template <int NCOL>
+__global__ void __launch_bounds__(256, NCOL <= 2 ? 3 : 2) k_seg_chunk_many(SegCols cols, int ncol, const long long* __restrict__ rows,
+                                                        long long nx, const long long* __restrict__ starts, long long ng,
+                                                        long long total, const long long* __restrict__ big,
+                                                        const unsigned long long* __restrict__ chunk0, long long nbig,
+                                                        unsigned long long nchunks, double* __restrict__ part,
+                                                        unsigned* derr) {
+    __shared__ double ws[SEG_MANY][8];
+    const long long c = blockIdx.x;
+    long long lo = 0, hi = nbig - 1;  // the long segment owning chunk c
+    while (lo < hi) {
+        long long mid = (lo + hi + 1) >> 1;
+        if ((long long)chunk0[mid] <= c) lo = mid; else hi = mid - 1;
+    }
+    const long long g = big[lo];
+    const long long s = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total;
+    const long long first = s + (c - (long long)chunk0[lo]) * TILE_SUM + threadIdx.x;
+    long long r[16];
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        const long long j = first + (long long)k * 256;
+        r[k] = j < e ? rows[j] : -1;
+        bad |= j < e && (r[k] < 0 || r[k] >= nx);
+    }
+    double v[NCOL][16];
+#pragma unroll
+    for (int q = 0; q < NCOL; q++)
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+            v[q][k] = (r[k] >= 0 && r[k] < nx) ? cols.src[q][r[k]] : 0.0;
+#pragma unroll
+    for (int q = 0; q < NCOL; q++) {
+        double acc = 0.0;
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+            if (first + (long long)k * 256 < e) acc = __dadd_rn(acc, v[q][k]);
+        acc = swarp<double, OP_SUM>(acc);
+        if ((threadIdx.x & 31) == 0) ws[q][threadIdx.x >> 5] = acc;
+    }
+    __syncthreads();
+    if (threadIdx.x < (unsigned)NCOL) {
+        const double* w = ws[threadIdx.x];
+        const double w01 = __dadd_rn(w[0], w[1]), w23 = __dadd_rn(w[2], w[3]);
+        const double w45 = __dadd_rn(w[4], w[5]), w67 = __dadd_rn(w[6], w[7]);
+        part[(unsigned long long)threadIdx.x * nchunks + c] = __dadd_rn(__dadd_rn(w01, w23), __dadd_rn(w45, w67));
+    }
+    if (bad) flag_error(derr, DERR_INDEX);
+}
+
+// f64 sums of several columns over the segments of one grouping whose
+// segments are all longer than one tile, with at most 4096 chunks in all;
+// sums[q] receives column q's ng sums.  Returns 1 (nothing done) when the
+// grouping is of another shape.
+I seg_sum_f64_many(const double* const* srcs, int ncol, const long long* rows, long long nx, const long long* starts,
+                   long long ng, long long total, ListInfo* li, double* const* sums) {
+    if (ncol < 1 || ncol > SEG_MANY || ng == 0 || !li) return 1;
+    const unsigned *ids, *ccnt;
+    HG_CHECK(seg_classes(starts, ng, total, li, &ids, &ccnt));
+    if (!li->cls_known) return 1;
+    for (int c = 0; c < 7; c++)
+        if (li->cls_host[c]) return 1;
+    LongPlan pl;
+    HG_CHECK(seg_plan_long(starts, ng, total, li, &pl));
+    if (pl.nbig == 0 || pl.nchunks > (unsigned long long)TILE_SUM) return 1;
+    double* part = (double*)salloc((size_t)pl.nchunks * ncol * sizeof(double));
+    if (!part) return E_DEVICE_OOM;
+    SegCols sc{};
+    for (int q = 0; q < ncol; q++) sc.src[q] = srcs[q];
+#define SEG_MANY_LAUNCH(NC)                                                                                          \
+    HG_LAUNCH("seg_chunk_many", (unsigned)pl.nchunks, 256, 0, k_seg_chunk_many<NC>, sc, ncol, rows, nx, starts, ng, total, \
+              pl.big, pl.c0, pl.nbig, pl.nchunks, part, g_derr)
+    if (ncol == 1) SEG_MANY_LAUNCH(1);
+    else if (ncol == 2) SEG_MANY_LAUNCH(2);
+    else if (ncol == 3) SEG_MANY_LAUNCH(3);
+    else SEG_MANY_LAUNCH(4);
+#undef SEG_MANY_LAUNCH
+    for (int q = 0; q < ncol; q++)
+        HG_LAUNCH("seg_partials", (unsigned)pl.nbig, 256, 0, (k_seg_partials<double, OP_SUM>), part + (size_t)q * pl.nchunks,
+                  pl.pstarts, pl.big, pl.nbig, (long long)pl.nchunks, 0.0, sums[q]);
     return last_launch_error();
 }
 
@@ -674,6 +788,67 @@ I hgpuGroupAvg(V z, V x, V y) { return group_agg(z, x, y, AG_AVG); }
 I hgpuGroupMin(V z, V x, V y) { return group_agg(z, x, y, AG_MIN); }
 I hgpuGroupMax(V z, V x, V y) { return group_agg(z, x, y, AG_MAX); }
 I hgpuGroupLen(V z, V x, V y) { return group_agg(z, x, y, AG_LEN); }
+
+// z[k] = the aggregate aggs[k] (0 sum, 1 avg, 2 min, 3 max, 4 len) of x[k]
+// over the grouping y, each bit for bit what hgpuGroupSum/Avg/Min/Max/Len
+// returns.  The f64 sums and averages over a @group whose groups are all
+// longer than one 4096-row tile share one pass that reads each group's row
+// ids once (the common-index pattern applied to the segmented reductions).
+I hgpuGroupAggMany(V* z, V* x, V y, const I* aggs, L n) {
+    HG_CHECK(ensure_init());
+    if (n < 0) return E_LENGTH;
+    if (y->typ != H_G) return E_DOMAIN;
+    int fused[SEG_MANY];
+    int nf = 0;
+    for (L k = 0; k < n; k++) {
+        if (aggs[k] < AG_SUM || aggs[k] > AG_LEN || !is_real(x[k]->typ)) return E_DOMAIN;
+        if ((aggs[k] == AG_SUM || aggs[k] == AG_AVG) && x[k]->typ == H_E && nf < SEG_MANY) fused[nf++] = (int)k;
+    }
+    bool done[64] = {false};
+    if (nf >= 2 && n <= 64) {
+        ScratchScope ss;
+        const long long* starts;
+        long long total;
+        const void* rows;
+        ListInfo* li;
+        HG_CHECK(list_segments(y, H_L, &starts, &total, &rows, &li));
+        const long long ng = y->len;
+        const double* srcs[SEG_MANY];
+        double* sums[SEG_MANY];
+        bool in_range = li && li->group_rows;
+        long long nx = -1;
+        for (int q = 0; q < nf; q++) {
+            const void* px;
+            HG_CHECK(in_ptr(x[fused[q]], &px));
+            srcs[q] = (const double*)px;
+            sums[q] = (double*)salloc((size_t)(ng > 0 ? ng : 1) * 8);
+            if (!sums[q]) return E_DEVICE_OOM;
+            nx = nx < 0 ? x[fused[q]]->len : (x[fused[q]]->len < nx ? x[fused[q]]->len : nx);
+        }
+        in_range = in_range && nx >= total;
+        I rc = seg_sum_f64_many(srcs, nf, (const long long*)rows, nx, starts, ng, total, li, sums);
+        if (rc > 1) return rc;
+        if (rc == 0) {
+            if (!in_range) HG_CHECK(check_device_errors());
+            for (int q = 0; q < nf; q++) {
+                const int k = fused[q];
+                void* dz;
+                HG_CHECK(alloc_out(z[k], H_E, ng, &dz));
+                if (aggs[k] == AG_AVG) {
+                    if (ng > 0) HG_LAUNCH("avg_seg", gcap(ng), 256, 0, k_avg_seg<double>, sums[q], starts, ng, total, dz);
+                    HG_CHECK(last_launch_error());
+                } else if (ng > 0) {
+                    HG_CU(cudaMemcpyAsync(dz, sums[q], (size_t)ng * 8, cudaMemcpyDeviceToDevice, g_stream));
+                }
+                HG_CHECK(finish_out(z[k], dz));
+                done[k] = true;
+            }
+        }
+    }
+    for (L k = 0; k < n; k++)
+        if (!(k < 64 && done[k])) HG_CHECK(group_agg(z[k], x[k], y, aggs[k]));
+    return 0;
+}
 
 // pfnEachRight: h_primitive.cc:1882-1904.  With @index over a list of i64 row
 // vectors all groups are gathered in one kernel into one contiguous payload.

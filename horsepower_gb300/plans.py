@@ -45,6 +45,29 @@ def group_agg(L, agg, x, vals):
     return L.call("pfnRaze", e)
 
 
+_AGG_CODE = {"pfnSum": 0, "pfnAvg": 1, "pfnMin": 2, "pfnMax": 3, "pfnLen": 4}
+
+
+def group_agg_many(L, pairs, vals):
+    """Several (aggregate, column) pairs over one grouping: hgpuGroupAggMany
+    where the library has it (the same bits as one call each), else one
+    group_agg per pair."""
+    import ctypes as C
+    from .abi import BuiltinError
+    fn = getattr(L.lib, "hgpuGroupAggMany", None)
+    if fn is None or len(pairs) < 2:
+        return [group_agg(L, a, x, vals) for a, x in pairs]
+    fn.restype = C.c_int32
+    fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong]
+    zs = [L.node() for _ in pairs]
+    aggs = (C.c_int32 * len(pairs))(*[_AGG_CODE[a] for a, _ in pairs])
+    L._keep.append(aggs)
+    rc = fn(L.node_array(zs), L.node_array([x for _, x in pairs]), C.byref(vals), aggs, len(pairs))
+    if rc:
+        raise BuiltinError("hgpuGroupAggMany", rc, L.lib.hgpuLastError().decode() if L.has_device else "")
+    return zs
+
+
 def index_many(L, cols, idx):
     """@index of several columns by one index vector: the reference's common
     index pattern (pattern.cc:558-672) through hgpuIndexMany where the library
@@ -84,10 +107,8 @@ def join_group(L, dim, fact, lo=D.WIN_LO, hi=D.WIN_HI):
     qty, price, disc = index_many(L, [fact["qty"], fact["price"], fact["disc"]], fi)
     out_flag = L.call("pfnIndex", flag, keys)
     out_status = L.call("pfnIndex", status, keys)
-    sum_qty = group_agg(L, "pfnSum", qty, vals)
-    avg_price = group_agg(L, "pfnAvg", price, vals)
-    sum_disc = group_agg(L, "pfnSum", disc, vals)
-    count = group_agg(L, "pfnLen", qty, vals)
+    sum_qty, avg_price, sum_disc, count = group_agg_many(
+        L, [("pfnSum", qty), ("pfnAvg", price), ("pfnSum", disc), ("pfnLen", qty)], vals)
     return out_flag, out_status, sum_qty, avg_price, sum_disc, count
 
 

@@ -3,7 +3,7 @@
  * generator turns a query into C: one builtin call per statement over the
  * library's C ABI (include/hgpu.h), with the common-index pattern
  * (optimizer/pattern.cc:558-672) applied to the five gathers by the join's
- * fact rows.  Statement for statement the same as plans.join_group in
+ * fact rows and to the four aggregates over the groups.  Statement for statement the same as plans.join_group in
  * horsepower_gb300/plans.py.  This is a caller of libhgpu, built into its own
  * libhgpu_queries.so, not part of the library.
  */
@@ -73,9 +73,10 @@ I hgpuQueryJoinGroup(V *in, I lo, I hi, V *out) {
     }
     CK(pfnIndex(out[0], &flag, &keys));
     CK(pfnIndex(out[1], &status, &keys));
-    CK(hgpuGroupSum(out[2], &qty, &vals));
-    CK(hgpuGroupAvg(out[3], &price, &vals));
-    CK(hgpuGroupSum(out[4], &disc, &vals));
-    CK(hgpuGroupLen(out[5], &qty, &vals));
+    {  /* the four aggregates over the same groups in one call */
+        V z[4] = {out[2], out[3], out[4], out[5]}, x[4] = {&qty, &price, &disc, &qty};
+        const I aggs[4] = {HGPU_AGG_SUM, HGPU_AGG_AVG, HGPU_AGG_SUM, HGPU_AGG_LEN};
+        CK(hgpuGroupAggMany(z, x, &vals, aggs, 4));
+    }
     return 0;
 }

@@ -213,6 +213,18 @@ I hgpuGroupAvg(V z, V x, V y);
 I hgpuGroupMin(V z, V x, V y);
 I hgpuGroupMax(V z, V x, V y);
 I hgpuGroupLen(V z, V x, V y);
+/* Several aggregates over one grouping (no counterpart in the reference: the
+ * common-index pattern, pattern.cc:558-672, applied to the segmented
+ * reductions of pattern.cc:63-105).  z[k] = hgpuGroupSum / Avg / Min / Max /
+ * Len (x[k], y) for aggs[k] = HGPU_AGG_SUM .. HGPU_AGG_LEN, bit for bit; f64
+ * sums and averages over a @group whose groups are all longer than 4096 rows
+ * read the groups' row ids once for all of them. */
+#define HGPU_AGG_SUM 0
+#define HGPU_AGG_AVG 1
+#define HGPU_AGG_MIN 2
+#define HGPU_AGG_MAX 3
+#define HGPU_AGG_LEN 4
+I hgpuGroupAggMany(V *z, V *x, V y, const I *aggs, L n);
 
 /* ---------------- fused chains ----------------
  * GB300 counterpart of the fused loops emitted by the loop-fusion passes

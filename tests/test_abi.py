@@ -44,7 +44,7 @@ def test_compiled_queries_link_against_the_library(lib):
     out = subprocess.run(["nm", "-D", path], capture_output=True, text=True, check=True).stdout
     assert any(ln.split()[-1] == "hgpuQueryJoinGroup" and " T " in ln for ln in out.splitlines())
     undefined = {ln.split()[-1] for ln in out.splitlines() if " U " in ln}
-    assert {"pfnJoinIndex", "hgpuIndexMany", "hgpuGroupSum"} <= undefined
+    assert {"pfnJoinIndex", "hgpuIndexMany", "hgpuGroupAggMany"} <= undefined
     assert C.CDLL(path).hgpuQueryJoinGroup
 
 

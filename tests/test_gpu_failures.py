@@ -51,7 +51,7 @@ probe = rng.integers(0, 40_000_000, 30_000_000).astype(np.int32)
 rc = L.rc("pfnJoinIndex", L.vec(build, H_I), L.vec(probe, H_I), L.sym("eq"))
 print("join_rc", rc, L.lib.hgpuLastError().decode())
 small = L.call("pfnJoinIndex", L.vec(np.array([3, 1, 2], np.int32), H_I), L.vec(np.array([1, 2, 3, 3], np.int32), H_I), L.sym("eq"))
-print("small", sorted(zip(*[L.to_py(v).tolist() for v in L.to_py(small)])))
+print("small", sorted(zip(*[v.tolist() for v in L.to_py(small)])))
 """
 
 

@@ -575,3 +575,33 @@ def test_quicksort_nan_key_refused(libs):
     ok = gpu.to_py(gpu.call("pfnOrderBy", gpu.vec(np.nan_to_num(x), H_E), gpu.vec(np.array([1], bool), H_B)))
     assert ok.size == x.size
     gpu.free_inputs()
+
+
+@pytest.mark.parametrize("shape", ["long_groups", "mixed_sizes", "types"])
+def test_group_agg_many_matches_single_calls(libs, shape):
+    """hgpuGroupAggMany returns, bit for bit, what one hgpuGroupSum / Avg /
+    Min / Max / Len call per column returns: the shared pass over long groups
+    (shape long_groups), the per-column path for groups of every size class,
+    and non-f64 columns."""
+    from horsepower_gb300 import plans as P
+    gpu = libs[0]
+    rng = np.random.default_rng(47)
+    n = 6_000_000
+    if shape == "long_groups":
+        key = rng.integers(0, 6, n).astype(np.int8)
+        g = gpu.call("pfnGroup", gpu.list([gpu.vec(key, H_C), gpu.vec(rng.integers(0, 2, n).astype(np.int8), H_C)]))
+    else:
+        key = np.minimum(rng.zipf(1.3, n), 100_000).astype(np.int64)
+        g = gpu.call("pfnGroup", gpu.vec(key, H_L))
+    vals = gpu.call("pfnValues", g)
+    cols = [gpu.vec(rng.uniform(0, 1e5, n), H_E) for _ in range(3)]
+    if shape == "types":
+        cols = [gpu.vec(rng.integers(-9, 9, n).astype(np.int32), H_I), gpu.vec(rng.standard_normal(n).astype(np.float32), 5),
+                gpu.vec(rng.uniform(0, 1e5, n), H_E)]
+    pairs = [("pfnSum", cols[0]), ("pfnAvg", cols[1]), ("pfnSum", cols[2]), ("pfnLen", cols[0]),
+             ("pfnMax", cols[2]), ("pfnAvg", cols[2])]
+    many = [gpu.to_py(z) for z in P.group_agg_many(gpu, pairs, vals)]
+    single = [gpu.to_py(P.group_agg(gpu, a, x, vals)) for a, x in pairs]
+    for a, b in zip(many, single):
+        assert a.dtype == b.dtype and a.tobytes() == b.tobytes()
+    gpu.free_inputs()
