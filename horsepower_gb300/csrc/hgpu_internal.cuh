@@ -58,6 +58,7 @@ bool dshrink(void* p, size_t new_bytes);       // shrink the LAST output allocat
 
 // autotuner knobs (hgpuSetTuning)
 extern int g_tile_rows;                         // rows per lane of the tiled probe kernels: 8, 16, 32
+extern int g_join_filter;                       // join presence bitmap: 0 through L2, 1 in a cluster's shared memory
 void set_hash_load_factor(double f);
 double get_hash_load_factor();
 void set_radix_digit_bits(int b);

@@ -342,12 +342,15 @@ static I compile_chain(hgpu_chain_s* c, const std::vector<int>& types, std::shar
         // `result` set, the block that finishes last reduces the tile
         // partials by the same tree (one tile of partials: at most 4096
         // blocks) and writes the result, so the chain is one launch.
-        std::string tree =
-            "    for (int o = 16; o > 0; o >>= 1) acc = hg_op(acc, __shfl_xor_sync(0xffffffffu, acc, o));\n"
-            "    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;\n"
-            "    __syncthreads();\n"
-            "    const " + std::string(A) + " blk = hg_op(hg_op(hg_op(ws[0], ws[1]), hg_op(ws[2], ws[3])),"
-            " hg_op(hg_op(ws[4], ws[5]), hg_op(ws[6], ws[7])));\n";
+        auto tree = [&](const std::string& dest) {
+            return std::string("    {\n") +
+                   "    for (int o = 16; o > 0; o >>= 1) acc = hg_op(acc, __shfl_xor_sync(0xffffffffu, acc, o));\n"
+                   "    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;\n"
+                   "    __syncthreads();\n"
+                   "    if (threadIdx.x == 0) " + dest + " = hg_op(hg_op(hg_op(ws[0], ws[1]), hg_op(ws[2], ws[3])),"
+                   " hg_op(hg_op(ws[4], ws[5]), hg_op(ws[6], ws[7])));\n"
+                   "    }\n";
+        };
         src += std::string("__device__ __forceinline__ ") + A + " hg_op(" + A + " a, " + A + " b) { return " + opf + "; }\n";
         src += std::string("extern \"C\" __global__ void __launch_bounds__(256) chain_kernel(const void* const* cols, long long n, ") + A +
                "* part, " + A + " ident, unsigned* derr, unsigned* done, " + A + "* result) {\n"
@@ -366,8 +369,7 @@ static I compile_chain(hgpu_chain_s* c, const std::vector<int>& types, std::shar
                "        if (i < n) {\n" + unpack +
                "            if (" + mask + ") {\n" + vloads + "                acc = hg_op(acc, (" + A + ")(" + val + "));\n            }\n"
                "        }\n"
-               "    }\n" + tree +
-               "    if (threadIdx.x == 0) part[blockIdx.x] = blk;\n"
+               "    }\n" + tree("part[blockIdx.x]") +
                "    if (dz) atomicOr(derr, 4u);\n"
                "    if (!result) return;\n"
                "    __threadfence();\n"
@@ -381,8 +383,7 @@ static I compile_chain(hgpu_chain_s* c, const std::vector<int>& types, std::shar
                "        const long long i = k * 256 + threadIdx.x;\n"
                "        acc = hg_op(acc, i < gridDim.x ? ((volatile " + A + "*)part)[i] : ident);\n"
                "    }\n"
-               "    __syncthreads();\n" + tree +
-               "    if (threadIdx.x == 0) *result = blk;\n}\n";
+               "    __syncthreads();\n" + tree("*result") + "}\n";
     } else if (r->op == "compress" || r->op == "map") {
         if (r->kids.empty()) return set_error(E_DOMAIN, "chain: %s needs operands", r->op.c_str());
         bool isc = r->op == "compress";

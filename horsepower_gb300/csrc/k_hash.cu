@@ -28,6 +28,8 @@
 #include <cstring>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "dev_common.cuh"
 
 namespace hg {
@@ -868,6 +870,134 @@ __global__ void __launch_bounds__(JT_THREADS) k_jp_stage(Table<unsigned> t, cons
     }
 }
 
+// The same pass 1 with the presence bitmap held in the shared memory of a
+// thread-block cluster: CTA r of a cluster of QC keeps bitmap words
+// [r * per, (r + 1) * per), and a probe reads its key's word from the owning
+// CTA's shared memory (distributed shared memory) instead of L1/L2.  The
+// grid is persistent (tiles strided by gridDim.x); every CTA waits at the
+// cluster barrier before it exits, so no CTA's shared memory goes away while
+// another may still read it.  Outputs are those of k_jp_stage, tile for tile.
+constexpr int QC = 16;
+template <int R>
+__global__ void __launch_bounds__(JT_THREADS) k_jp_stage_dsmem(Table<unsigned> t, const int* __restrict__ y, long long n,
+                                                               long long ntiles, unsigned nwords, int shift,
+                                                               uint2* __restrict__ stage, unsigned* __restrict__ wcounts,
+                                                               unsigned* __restrict__ wpre, unsigned* __restrict__ tcounts) {
+    namespace cg = cooperative_groups;
+    extern __shared__ __align__(16) unsigned qs_bits[];
+    __shared__ const unsigned* peer[QC];
+    __shared__ unsigned wc[JT_THREADS / 32];
+    cg::cluster_group cl = cg::this_cluster();
+    const unsigned rank = cl.block_rank();
+    const unsigned per = 1u << shift;
+    {  // this CTA's slice of the bitmap
+        const unsigned w0 = rank * per;
+        for (unsigned i = threadIdx.x; i < per; i += JT_THREADS) qs_bits[i] = w0 + i < nwords ? t.filter[w0 + i] : 0u;
+        if (threadIdx.x < QC) peer[threadIdx.x] = cl.map_shared_rank(qs_bits, threadIdx.x);
+    }
+    cl.sync();
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    const unsigned long long range = (unsigned long long)(t.kmax - t.kmin);
+    const unsigned* rows = (const unsigned*)t.slots;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long long wid = tile * (JT_THREADS / 32) + warp;
+        const long long base = wid * (32 * R);
+        unsigned off[R];
+#pragma unroll
+        for (int k = 0; k < R; k++) {
+            long long i = base + k * 32 + lane;
+            long long v = i < n ? (long long)__ldcs(y + i) - t.kmin : -1;
+            off[k] = (unsigned long long)v <= range ? (unsigned)v : 0xffffffffu;
+        }
+        unsigned word[R];
+#pragma unroll
+        for (int k = 0; k < R; k++) {
+            const unsigned wi = off[k] >> 5;
+            word[k] = off[k] != 0xffffffffu ? peer[wi >> shift][wi & (per - 1)] : 0u;
+        }
+        unsigned r[R];
+        bool hit[R];
+#pragma unroll
+        for (int k = 0; k < R; k++) {
+            hit[k] = off[k] != 0xffffffffu && ((word[k] >> (off[k] & 31)) & 1u);
+            r[k] = hit[k] ? __ldg(rows + off[k]) : 0u;
+        }
+        uint2* out = stage + base;
+        unsigned pos = 0;
+#pragma unroll
+        for (int k = 0; k < R; k++) {
+            const unsigned bal = __ballot_sync(0xffffffffu, hit[k]);
+            if (hit[k]) out[pos + __popc(bal & lanemask_lt())] = make_uint2(r[k], (unsigned)(k * 32 + lane));
+            pos += __popc(bal);
+        }
+        if (lane == 0) wc[warp] = pos;
+        __syncthreads();
+        if (threadIdx.x < JT_THREADS / 32) {
+            unsigned before = 0, tot = 0;
+            for (int v = 0; v < JT_THREADS / 32; v++) {
+                before += v < (int)threadIdx.x ? wc[v] : 0u;
+                tot += wc[v];
+            }
+            const long long w2 = tile * (JT_THREADS / 32) + threadIdx.x;
+            wcounts[w2] = wc[threadIdx.x];
+            wpre[w2] = before;
+            if (threadIdx.x == 0) tcounts[tile] = tot;
+        }
+        __syncthreads();
+    }
+    cl.sync();
+}
+
+int g_join_filter = 0;  // 0: presence bitmap read through L2; 1: held in a cluster's shared memory
+
+// Launches k_jp_stage_dsmem when the bitmap fits the shared memory of a
+// cluster of QC CTAs and such clusters can be resident; *ok = false otherwise.
+template <int R>
+static I launch_stage_dsmem(const Table<unsigned>& t, const int* y, long long ny, long long ntiles, uint2* stage,
+                            unsigned* wcounts, unsigned* wpre, unsigned* tcounts, bool* ok) {
+    *ok = false;
+    const unsigned long long range = (unsigned long long)(t.kmax - t.kmin) + 1;
+    const unsigned long long nwords = (range + 31) / 32;
+    int shift = 0;  // words per CTA: the power of two covering a QC-th of the bitmap
+    while ((unsigned long long)QC << shift < nwords) shift++;
+    const size_t smem = (size_t)4 << shift;
+    if (smem > 128 * 1024) return 0;
+    auto kern = k_jp_stage_dsmem<R>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    cudaLaunchConfig_t cfg{};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = QC;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(JT_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = g_stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3(QC * 256);
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, (void*)kern, &cfg) != cudaSuccess || nclusters < 1) {
+        cudaGetLastError();
+        return 0;
+    }
+    cfg.gridDim = dim3((unsigned)(QC * nclusters));
+    {
+        LaunchScope ls("join_probe");
+        if (cudaLaunchKernelEx(&cfg, kern, t, y, ny, ntiles, (unsigned)nwords, shift, stage, wcounts, wpre, tcounts) !=
+            cudaSuccess) {
+            cudaGetLastError();  // not launched: the caller takes the L2 kernel
+            return 0;
+        }
+    }
+    *ok = true;
+    return 0;
+}
+
 // Pass 2: one warp per four staged warps.  Lanes 0-3 read the four counts
 // and offsets; the first 32 pairs of all four regions are loaded before any
 // is stored (a region rarely holds more), so four loads are in flight per lane.
@@ -919,7 +1049,9 @@ static I probe_direct_staged(const Table<unsigned>& t, const int* y, long long n
     unsigned* tcounts = (unsigned*)salloc((size_t)ntiles * 4);
     unsigned long long* toffs = (unsigned long long*)salloc((size_t)(ntiles + 1) * 8);
     if (!stage || !wcounts || !wpre || !tcounts || !toffs) return E_DEVICE_OOM;
-    HG_LAUNCH("join_probe", (unsigned)ntiles, JT_THREADS, 0, k_jp_stage<R>, t, y, ny, stage, wcounts, wpre, tcounts);
+    bool done = false;
+    if (g_join_filter == 1) HG_CHECK(launch_stage_dsmem<R>(t, y, ny, ntiles, stage, wcounts, wpre, tcounts, &done));
+    if (!done) HG_LAUNCH("join_probe", (unsigned)ntiles, JT_THREADS, 0, k_jp_stage<R>, t, y, ny, stage, wcounts, wpre, tcounts);
     HG_CHECK(scan_counts(tcounts, ntiles, toffs));
     HG_LAUNCH("join_emit", (unsigned)((nwarps + 8 * JU_GROUP - 1) / (8 * JU_GROUP)), 256, 0, k_jp_unstage, (const uint2*)stage,
               (const unsigned*)wcounts, (const unsigned*)wpre, (const unsigned long long*)toffs, nwarps, 32 * R, zb, zp);

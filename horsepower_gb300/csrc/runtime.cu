@@ -831,6 +831,7 @@ I hgpuSetTuning(I knob, E value) {
     case HGPU_TUNE_HASH_LOAD: set_hash_load_factor(value); return 0;
     case HGPU_TUNE_RADIX_BITS: set_radix_digit_bits((int)value); return 0;
     case HGPU_TUNE_TILE_ROWS: g_tile_rows = value <= 8 ? 8 : (value <= 16 ? 16 : 32); return 0;
+    case HGPU_TUNE_JOIN_FILTER: g_join_filter = value >= 0.5 ? 1 : 0; return 0;
     case HGPU_TUNE_L2_FETCH:
         g_l2_fetch = value <= 32 ? 32 : (value <= 64 ? 64 : 128);
         if (g_inited) {
@@ -848,6 +849,7 @@ E hgpuGetTuning(I knob) {
     case HGPU_TUNE_RADIX_BITS: return (E)get_radix_digit_bits();
     case HGPU_TUNE_TILE_ROWS: return (E)g_tile_rows;
     case HGPU_TUNE_L2_FETCH: return (E)g_l2_fetch;
+    case HGPU_TUNE_JOIN_FILTER: return (E)g_join_filter;
     default: return -1.0;
     }
 }

@@ -369,6 +369,8 @@ double hgpuTimerStop(void);
                                     (tile = 256 x that; default 8) */
 #define HGPU_TUNE_L2_FETCH   3   /* largest L2 fetch from DRAM, bytes: 32, 64 or 128 (default 64;
                                     32 suits sparse sorted gathers, 64 random probes and scatters) */
+#define HGPU_TUNE_JOIN_FILTER 4 /* @join_index presence bitmap on dense i32 keys: 0 read through L2
+                                    (default), 1 held in the shared memory of a 16-CTA cluster */
 I    hgpuSetTuning(I knob, E value);
 E    hgpuGetTuning(I knob);
 

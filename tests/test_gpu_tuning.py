@@ -49,9 +49,28 @@ def test_join_knobs(L, wide):
     assert ref[0].size > 0
     for tr in (8, 16, 32):
         for hl in (0.5, 0.65, 0.8):
-            T.apply(L, {"tile_rows": tr, "hash_load": hl})
-            assert same(outputs(L, lambda: L.call("pfnJoinIndex", x, y, f)), ref), (tr, hl)
-    T.apply(L, {"tile_rows": 8, "hash_load": 0.5})
+            for jf in (0, 1):
+                T.apply(L, {"tile_rows": tr, "hash_load": hl, "join_filter": jf})
+                assert same(outputs(L, lambda: L.call("pfnJoinIndex", x, y, f)), ref), (tr, hl, jf)
+    T.apply(L, {"tile_rows": 8, "hash_load": 0.5, "join_filter": 0})
+
+
+def test_join_filter_in_cluster_shared_memory(L):
+    """The join + group-by shape (60M probe keys over a 15M-key dimension,
+    2.17M selected): the probe with the presence bitmap in a 16-CTA
+    cluster's shared memory returns exactly the L2 probe's pairs."""
+    rng = np.random.default_rng(22)
+    nd, nf = 15_000_000, 20_000_000
+    pk = rng.permutation(nd).astype(np.int32)
+    build = pk[rng.random(nd) < 0.1445]
+    x, y = L.vec(build, H_I), L.vec(rng.integers(0, nd, nf).astype(np.int32), H_I)
+    f = L.sym("eq")
+    T.apply(L, {"join_filter": 0})
+    ref = outputs(L, lambda: L.call("pfnJoinIndex", x, y, f))
+    T.apply(L, {"join_filter": 1})
+    got = outputs(L, lambda: L.call("pfnJoinIndex", x, y, f))
+    T.apply(L, {"join_filter": 0})
+    assert ref[0].size > 2_000_000 and same(got, ref)
 
 
 def test_radix_bits(L):
@@ -89,7 +108,7 @@ def test_batched_tile_rows(L):
 def test_tune_and_clamp(L):
     T.apply(L, {"hash_load": 0.95, "radix_bits": 2, "tile_rows": 100, "l2_fetch": 1000})
     c = T.current(L)
-    assert c == {"tile_rows": 32, "hash_load": 0.8, "radix_bits": 4, "l2_fetch": 128}
+    assert c == {"tile_rows": 32, "hash_load": 0.8, "radix_bits": 4, "l2_fetch": 128, "join_filter": 0}
     T.apply(L, {"l2_fetch": 10})
     assert T.current(L)["l2_fetch"] == 32
     tabs = [B.synth_tables(L, 900 + i, n, n // 4) for i, n in enumerate([20_000, 200_000])]
