@@ -442,7 +442,7 @@ static I seg_reduce(const T* src, const long long* rows, long long nx, const lon
 constexpr int SEG_MANY = 4;
 struct SegCols { const double* src[SEG_MANY]; };
 template <int NCOL>
-__global__ void __launch_bounds__(256, NCOL <= 2 ? 3 : 2) k_seg_chunk_many(SegCols cols, int ncol, const long long* __restrict__ rows,
+__global__ void __launch_bounds__(256) k_seg_chunk_many(SegCols cols, int ncol, const long long* __restrict__ rows,
                                                         long long nx, const long long* __restrict__ starts, long long ng,
                                                         long long total, const long long* __restrict__ big,
                                                         const unsigned long long* __restrict__ chunk0, long long nbig,
@@ -466,18 +466,15 @@ __global__ void __launch_bounds__(256, NCOL <= 2 ? 3 : 2) k_seg_chunk_many(SegCo
         r[k] = j < e ? rows[j] : -1;
         bad |= j < e && (r[k] < 0 || r[k] >= nx);
     }
-    double v[NCOL][16];
+#pragma unroll 1
+    for (int q = 0; q < NCOL; q++) {  // one column at a time: 16 gathers in flight, few registers
+        double v[16];
 #pragma unroll
-    for (int q = 0; q < NCOL; q++)
-#pragma unroll
-        for (int k = 0; k < 16; k++)
-            v[q][k] = (r[k] >= 0 && r[k] < nx) ? cols.src[q][r[k]] : 0.0;
-#pragma unroll
-    for (int q = 0; q < NCOL; q++) {
+        for (int k = 0; k < 16; k++) v[k] = (r[k] >= 0 && r[k] < nx) ? cols.src[q][r[k]] : 0.0;
         double acc = 0.0;
 #pragma unroll
         for (int k = 0; k < 16; k++)
-            if (first + (long long)k * 256 < e) acc = __dadd_rn(acc, v[q][k]);
+            if (first + (long long)k * 256 < e) acc = __dadd_rn(acc, v[k]);
         acc = swarp<double, OP_SUM>(acc);
         if ((threadIdx.x & 31) == 0) ws[q][threadIdx.x >> 5] = acc;
     }

@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(RS_THREADS, (sizeof(K) == 4 ? 4 : 3)) k_oneswe
     extern __shared__ __align__(16) unsigned char os_smem[];
     K* skey = reinterpret_cast<K*>(os_smem);
     unsigned* sval = reinterpret_cast<unsigned*>(os_smem + RS_TILE * sizeof(K));
-    __shared__ unsigned whist[8][256];
+    __shared__ unsigned short whist[8][256];  // per-warp digit counts, then offsets (at most 4096)
     __shared__ unsigned dstart[256];
     __shared__ unsigned long long dbase[256];
     __shared__ unsigned wscan[8];
@@ -112,13 +112,11 @@ __global__ void __launch_bounds__(RS_THREADS, (sizeof(K) == 4 ? 4 : 3)) k_oneswe
     const long long wbase = t * RS_TILE + (long long)w * (32 * RS_ITEMS);
     const unsigned dmask = (1u << bits) - 1;
     K key[RS_ITEMS];
-    unsigned val[RS_ITEMS], rd[RS_ITEMS];  // rd = digit << 16 | rank within the warp's items
+    unsigned rd[RS_ITEMS];  // rd = digit << 16 | rank within the warp's items
 #pragma unroll
     for (int k = 0; k < RS_ITEMS; k++) {
         long long i = wbase + k * 32 + lane;
-        bool valid = i < n;
-        key[k] = valid ? kin[i] : K(0);
-        val[k] = FIRST ? (unsigned)i : (valid ? vin[i] : 0u);
+        key[k] = i < n ? kin[i] : K(0);
     }
 #pragma unroll
     for (int k = 0; k < RS_ITEMS; k++) {
@@ -137,32 +135,48 @@ __global__ void __launch_bounds__(RS_THREADS, (sizeof(K) == 4 ? 4 : 3)) k_oneswe
         __syncwarp();
     }
     __syncthreads();
+    const int dd = threadIdx.x;  // one thread per digit
+    unsigned dcount = 0;
     {
-        const int d = threadIdx.x;  // one thread per digit
-        unsigned c = 0;
-        for (int ww = 0; ww < 8; ww++) { unsigned h = whist[ww][d]; whist[ww][d] = c; c += h; }
-        // tile-local start of digit d: exclusive scan of the 256 digit counts
-        unsigned inc = warp_incl_scan(c);
+        for (int ww = 0; ww < 8; ww++) { unsigned h = whist[ww][dd]; whist[ww][dd] = dcount; dcount += h; }
+        // tile-local start of digit dd: exclusive scan of the 256 digit counts
+        unsigned inc = warp_incl_scan(dcount);
         if (lane == 31) wscan[w] = inc;
         __syncthreads();
         unsigned before = 0;
         for (unsigned ww = 0; ww < w; ww++) before += wscan[ww];
-        dstart[d] = before + inc - c;
-        unsigned long long excl = 0;
-        if (d <= (int)dmask) excl = chain_lookback(status + d, 256, t, 0, c, derr);
-        dbase[d] = bucket[d] + excl;
+        dstart[dd] = before + inc - dcount;
     }
     __syncthreads();
-    // place the tile in digit order in shared memory ...
+    // place the tile in digit order in shared memory (tile-local positions
+    // only, so the keys leave registers before the look-back); the row ids
+    // are read only now, which keeps them out of registers while ranking ...
 #pragma unroll
     for (int k = 0; k < RS_ITEMS; k++) {
         long long i = wbase + k * 32 + lane;
         if (i < n) {
             unsigned d = rd[k] >> 16;
-            unsigned local = dstart[d] + whist[w][d] + (rd[k] & 0xffffu);
-            skey[local] = key[k];
-            sval[local] = val[k];
+            skey[dstart[d] + whist[w][d] + (rd[k] & 0xffffu)] = key[k];
         }
+    }
+    unsigned val[RS_ITEMS];
+#pragma unroll
+    for (int k = 0; k < RS_ITEMS; k++) {
+        long long i = wbase + k * 32 + lane;
+        val[k] = FIRST ? (unsigned)i : (i < n ? vin[i] : 0u);
+    }
+#pragma unroll
+    for (int k = 0; k < RS_ITEMS; k++) {
+        long long i = wbase + k * 32 + lane;
+        if (i < n) {
+            unsigned d = rd[k] >> 16;
+            sval[dstart[d] + whist[w][d] + (rd[k] & 0xffffu)] = val[k];
+        }
+    }
+    {  // ... then each digit's global base from the preceding tiles
+        unsigned long long excl = 0;
+        if (dd <= (int)dmask) excl = chain_lookback(status + dd, 256, t, 0, dcount, derr);
+        dbase[dd] = bucket[dd] + excl;
     }
     __syncthreads();
     // ... and write each digit's run contiguously (consecutive threads, consecutive addresses)
