@@ -227,6 +227,9 @@ def run_gb300(args, rank, ws, dist, dim, fact):
     Lb.setHeapOffset.argtypes = [C.c_longlong]
 
     F, Dn = args.fact, args.dim
+    if args.l2_fetch:
+        Lb.hgpuSetTuning.argtypes = [C.c_int32, C.c_double]
+        assert Lb.hgpuSetTuning(3, float(args.l2_fetch)) == 0  # HGPU_TUNE_L2_FETCH
     # device-resident copies of the tables
     host = {}
     dev = {}
@@ -271,6 +274,17 @@ def run_gb300(args, rank, ws, dist, dim, fact):
     sel = ((dim["date"] >= D.WIN_LO) & (dim["date"] < D.WIN_HI))
     Dp = int(sel.sum())
     G = len(res_np[0])
+    # the gathers' sector-level floor: the matched fact rows (ascending, as
+    # the join emits them) touch these 32-byte sectors of each column; DRAM
+    # cannot deliver less than whole sectors
+    present = np.zeros(Dn, bool)
+    present[dim["pk"][sel]] = True
+    fi = np.flatnonzero(present[fact["fk"]])
+    assert fi.size == M
+
+    def sectors(es):
+        return int(np.unique(fi * es // 32).size) * 32
+    gather_floor = 2 * 8 * M + 2 * sectors(1) + 3 * sectors(8) + (2 * 1 + 3 * 8) * M
 
     # ---- timed region (device resident), no per-launch instrumentation
     clocks = Clocks()
@@ -350,7 +364,8 @@ def run_gb300(args, rank, ws, dist, dim, fact):
                driver="compiled C query (queries/join_group.c)" if query is not P.join_group else "python statements",
                profiled_step_ms=ms_profiled / args.steps,
                clocks=clk, e2e_rows_s=ws * F * args.steps / e2e_s, e2e_ms=1000 * e2e_s / args.steps,
-               h2d=h2d, d2h=d2h, shapes=dict(F=F, D=Dn, Dp=Dp, M=M, G=G), result=[v.tolist() for v in res_np])
+               h2d=h2d, d2h=d2h, shapes=dict(F=F, D=Dn, Dp=Dp, M=M, G=G), result=[v.tolist() for v in res_np],
+               gather_floor=gather_floor)
     return out
 
 
@@ -1074,6 +1089,8 @@ def main():
     ap.add_argument("--reps", type=int, default=3, help="with --workload case: calls to time")
     ap.add_argument("--tune", action="append", default=[], help="with --workload case: knob=value")
     ap.add_argument("--ingest-rows", type=int, default=6_001_215)
+    ap.add_argument("--l2-fetch", type=int, default=0,
+                    help="default workload: the library's L2 fetch granularity knob (32, 64, 128; 0 = library default)")
     ap.add_argument("--headline-only", action="store_true",
                     help="default workload: skip the per-builtin, batched and served parts after the headline")
     ap.add_argument("--rates", default="200,1000,5000")
@@ -1151,7 +1168,10 @@ def main():
                      "frac": (achieved / hbm) if achieved else None, "peak_source": src,
                      "traffic": traffic, "algorithmic_bytes_per_step": tb,
                      "traffic_gbs": (traffic / (top[1] / args.steps / 1000) / 1e9) if traffic else None,
-                     "traffic_frac": (traffic / (top[1] / args.steps / 1000) / 1e9 / hbm) if traffic else None},
+                     "traffic_frac": (traffic / (top[1] / args.steps / 1000) / 1e9 / hbm) if traffic else None,
+                     "sector_floor_bytes_per_step": r["gather_floor"] if top[0] == "gather_many" else None,
+                     "frac_vs_sector_floor": (r["gather_floor"] / (top[1] / args.steps / 1000) / 1e9 / hbm)
+                     if top[0] == "gather_many" else None},
         "cpu_baseline": cpu,
         "parity_vs_oracle": parity,
         "gpu_launches": r["launches"],
