@@ -27,12 +27,6 @@ __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long lon
 __device__ __forceinline__ void st_release(unsigned long long* p, unsigned long long v) {
     asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
-// a coherent (L2) read with no ordering: several can be in flight at once
-__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long* p) {
-    unsigned long long v;
-    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
 __device__ __forceinline__ unsigned ld_acquire32(const unsigned* p) {
     unsigned v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -151,13 +145,7 @@ __device__ __forceinline__ unsigned long long lookback_seg(unsigned long long* s
 
 // Look-back along one chain of status words (status[j * stride] for tiles j
 // in [first, t)), one thread per chain: the per-digit prefixes of the radix
-// passes.  The thread reads its next LB_WINDOW predecessors at once (relaxed
-// loads: the status word itself carries the value, so nothing else needs
-// ordering) and adds them in order up to the first inclusive prefix; a
-// predecessor that has not published yet is polled again, at most `limit`
-// times in all.  The sum is the same as one predecessor at a time, with one
-// memory latency per window instead of per tile.
-constexpr int LB_WINDOW = 8;
+// passes.
 __device__ __forceinline__ unsigned long long chain_lookback(unsigned long long* status, size_t stride, long long t,
                                                              long long first, unsigned long long c, unsigned* derr,
                                                              long long limit = SPIN_LIMIT) {
@@ -170,27 +158,15 @@ __device__ __forceinline__ unsigned long long chain_lookback(unsigned long long*
     unsigned long long excl = 0;
     long long j = t - 1, spins = 0;
     while (j >= first) {
-        unsigned long long sv[LB_WINDOW];
-#pragma unroll
-        for (int w = 0; w < LB_WINDOW; w++)  // before tile `first`: an inclusive prefix of 0
-            sv[w] = (j - w >= first) ? ld_relaxed(status + (size_t)(j - w) * stride) : LB_INC;
-        int w = 0;
-        bool inc = false;
-#pragma unroll
-        for (int q = 0; q < LB_WINDOW; q++) {
-            const unsigned long long f = sv[q] >> 62;
-            if (f == 0) break;
-            excl += sv[q] & LB_MASK;
-            w = q + 1;
-            if (f == 2) { inc = true; break; }
-        }
-        if (inc) break;
-        if (w < LB_WINDOW) {  // predecessor j - w has not published: poll from it again
-            j -= w;
+        unsigned long long sv = ld_acquire(status + (size_t)j * stride);
+        unsigned long long f = sv >> 62;
+        if (f == 0) {
             if (++spins > limit) { flag_error(derr, DERR_TIMEOUT); break; }
             continue;
         }
-        j -= LB_WINDOW;
+        excl += sv & LB_MASK;
+        if (f == 2) break;
+        j--;
     }
     st_release(st, LB_INC | (excl + c));
     return excl;

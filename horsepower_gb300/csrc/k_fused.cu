@@ -317,15 +317,11 @@ static I compile_chain(hgpu_chain_s* c, const std::vector<int>& types, std::shar
                 while (!st.empty()) { Node* q = st.back(); st.pop_back(); if (q->op == "x") in_val[q->col] = true; for (auto& k : q->kids) st.push_back(k.get()); }
             }
         }
-        std::string vpre, hoist, preload, unpack, vunpack;
+        std::string vloads, hoist, preload, unpack;
         for (int k = 0; k < nin; k++) {
             const std::string K = std::to_string(k), T = ctype(types[k]);
             if (in_mask[k] || in_val[k]) hoist += "    const " + T + "* __restrict__ c" + K + " = (const " + T + "*)cols[" + K + "];\n";
-            if (in_val[k] && !in_mask[k]) {  // read for the selected rows only, all 16 issued together
-                hoist += "    " + T + " b" + K + "[16];\n";
-                vpre += "        b" + K + "[k] = sel[k] ? c" + K + "[base + k * 256 + threadIdx.x] : (" + T + ")0;\n";
-                vunpack += "            " + T + " v" + K + " = b" + K + "[k];\n";
-            }
+            if (in_val[k] && !in_mask[k]) vloads += "                " + T + " v" + K + " = c" + K + "[i];\n";
             if (in_mask[k]) {
                 preload += "        a" + K + "[k] = in ? c" + K + "[i] : (" + T + ")0;\n";
                 hoist += "    " + T + " a" + K + "[16];\n";
@@ -367,21 +363,11 @@ static I compile_chain(hgpu_chain_s* c, const std::vector<int>& types, std::shar
                "        const bool in = i < n;\n" + preload +
                "    }\n"
                "    " + A + " acc = " + ident + ";\n    bool dz = false;\n"
-               "    bool sel[16];\n"
                "    #pragma unroll\n"
                "    for (int k = 0; k < 16; k++) {\n"
                "        const long long i = base + k * 256 + threadIdx.x;\n"
-               "        sel[k] = false;\n"
                "        if (i < n) {\n" + unpack +
-               "            sel[k] = " + mask + ";\n"
-               "        }\n"
-               "    }\n"
-               "    #pragma unroll\n"
-               "    for (int k = 0; k < 16; k++) {\n" + vpre + "    }\n"
-               "    #pragma unroll\n"
-               "    for (int k = 0; k < 16; k++) {\n"
-               "        if (sel[k]) {\n" + unpack + vunpack +
-               "            acc = hg_op(acc, (" + A + ")(" + val + "));\n"
+               "            if (" + mask + ") {\n" + vloads + "                acc = hg_op(acc, (" + A + ")(" + val + "));\n            }\n"
                "        }\n"
                "    }\n" + tree("part[blockIdx.x]") +
                "    if (dz) atomicOr(derr, 4u);\n"

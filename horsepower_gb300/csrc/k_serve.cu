@@ -50,22 +50,24 @@ __global__ void __launch_bounds__(256) k_s_q6(const int* __restrict__ ship, cons
         s_lo[w] = lohi[2 * w];
         s_hi[w] = lohi[2 * w + 1];
     }
-    const long long base = (long long)blockIdx.x * TILE_SUM;
-    int d[16];
-    double v[16];
+    const long long base = (long long)blockIdx.x * TILE_SUM, last = n > 0 ? n - 1 : 0;
+    int d[16], q[16];
+    double v[16], dc[16];
     unsigned live = 0;  // bit k: row k exists and passes the request-independent predicate
 #pragma unroll
+    for (int k = 0; k < 16; k++) {  // unconditional loads (past the end: the last row), all issued up front
+        const long long i = base + k * 256 + threadIdx.x, j = i < n ? i : last;
+        dc[k] = disc[j];
+        q[k] = qty[j];
+        d[k] = ship[j];
+        v[k] = price[j];
+    }
+#pragma unroll
     for (int k = 0; k < 16; k++) {
-        long long i = base + k * 256 + threadIdx.x;
-        d[k] = 0;
-        v[k] = 0.0;
-        if (i < n) {
-            double dc = disc[i];
-            bool c = qty[i] < 24 && f64_cmp_fixed(dc, d_lo) >= 0 && f64_cmp_fixed(dc, d_hi) <= 0;
-            d[k] = ship[i];
-            v[k] = __dmul_rn(price[i], dc);
-            live |= (unsigned)c << k;
-        }
+        const long long i = base + k * 256 + threadIdx.x;
+        const bool c = i < n && q[k] < 24 && f64_cmp_fixed(dc[k], d_lo) >= 0 && f64_cmp_fixed(dc[k], d_hi) <= 0;
+        v[k] = c ? __dmul_rn(v[k], dc[k]) : 0.0;
+        live |= (unsigned)c << k;
     }
     __syncthreads();
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;

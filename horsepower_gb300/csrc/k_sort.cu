@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(RS_THREADS, (sizeof(K) == 4 ? 4 : 3)) k_oneswe
     extern __shared__ __align__(16) unsigned char os_smem[];
     K* skey = reinterpret_cast<K*>(os_smem);
     unsigned* sval = reinterpret_cast<unsigned*>(os_smem + RS_TILE * sizeof(K));
-    __shared__ unsigned short whist[8][256];  // per-warp digit counts, then offsets (at most 4096)
+    __shared__ unsigned whist[8][256];
     __shared__ unsigned dstart[256];
     __shared__ unsigned long long dbase[256];
     __shared__ unsigned wscan[8];
@@ -112,11 +112,13 @@ __global__ void __launch_bounds__(RS_THREADS, (sizeof(K) == 4 ? 4 : 3)) k_oneswe
     const long long wbase = t * RS_TILE + (long long)w * (32 * RS_ITEMS);
     const unsigned dmask = (1u << bits) - 1;
     K key[RS_ITEMS];
-    unsigned rd[RS_ITEMS];  // rd = digit << 16 | rank within the warp's items
+    unsigned val[RS_ITEMS], rd[RS_ITEMS];  // rd = digit << 16 | rank within the warp's items
 #pragma unroll
     for (int k = 0; k < RS_ITEMS; k++) {
         long long i = wbase + k * 32 + lane;
-        key[k] = i < n ? kin[i] : K(0);
+        bool valid = i < n;
+        key[k] = valid ? kin[i] : K(0);
+        val[k] = FIRST ? (unsigned)i : (valid ? vin[i] : 0u);
     }
 #pragma unroll
     for (int k = 0; k < RS_ITEMS; k++) {
@@ -135,48 +137,32 @@ __global__ void __launch_bounds__(RS_THREADS, (sizeof(K) == 4 ? 4 : 3)) k_oneswe
         __syncwarp();
     }
     __syncthreads();
-    const int dd = threadIdx.x;  // one thread per digit
-    unsigned dcount = 0;
     {
-        for (int ww = 0; ww < 8; ww++) { unsigned h = whist[ww][dd]; whist[ww][dd] = dcount; dcount += h; }
-        // tile-local start of digit dd: exclusive scan of the 256 digit counts
-        unsigned inc = warp_incl_scan(dcount);
+        const int d = threadIdx.x;  // one thread per digit
+        unsigned c = 0;
+        for (int ww = 0; ww < 8; ww++) { unsigned h = whist[ww][d]; whist[ww][d] = c; c += h; }
+        // tile-local start of digit d: exclusive scan of the 256 digit counts
+        unsigned inc = warp_incl_scan(c);
         if (lane == 31) wscan[w] = inc;
         __syncthreads();
         unsigned before = 0;
         for (unsigned ww = 0; ww < w; ww++) before += wscan[ww];
-        dstart[dd] = before + inc - dcount;
+        dstart[d] = before + inc - c;
+        unsigned long long excl = 0;
+        if (d <= (int)dmask) excl = chain_lookback(status + d, 256, t, 0, c, derr);
+        dbase[d] = bucket[d] + excl;
     }
     __syncthreads();
-    // place the tile in digit order in shared memory (tile-local positions
-    // only, so the keys leave registers before the look-back); the row ids
-    // are read only now, which keeps them out of registers while ranking ...
+    // place the tile in digit order in shared memory ...
 #pragma unroll
     for (int k = 0; k < RS_ITEMS; k++) {
         long long i = wbase + k * 32 + lane;
         if (i < n) {
             unsigned d = rd[k] >> 16;
-            skey[dstart[d] + whist[w][d] + (rd[k] & 0xffffu)] = key[k];
+            unsigned local = dstart[d] + whist[w][d] + (rd[k] & 0xffffu);
+            skey[local] = key[k];
+            sval[local] = val[k];
         }
-    }
-    unsigned val[RS_ITEMS];
-#pragma unroll
-    for (int k = 0; k < RS_ITEMS; k++) {
-        long long i = wbase + k * 32 + lane;
-        val[k] = FIRST ? (unsigned)i : (i < n ? vin[i] : 0u);
-    }
-#pragma unroll
-    for (int k = 0; k < RS_ITEMS; k++) {
-        long long i = wbase + k * 32 + lane;
-        if (i < n) {
-            unsigned d = rd[k] >> 16;
-            sval[dstart[d] + whist[w][d] + (rd[k] & 0xffffu)] = val[k];
-        }
-    }
-    {  // ... then each digit's global base from the preceding tiles
-        unsigned long long excl = 0;
-        if (dd <= (int)dmask) excl = chain_lookback(status + dd, 256, t, 0, dcount, derr);
-        dbase[dd] = bucket[dd] + excl;
     }
     __syncthreads();
     // ... and write each digit's run contiguously (consecutive threads, consecutive addresses)
@@ -853,20 +839,22 @@ __global__ void __launch_bounds__(256) k_trie_scatter(Code code_of, long long n,
                                                       long long* __restrict__ perm) {
     __shared__ TrieRank r;
     __shared__ unsigned wcnt[8][TS_MAXG];  // per warp: rows of each bucket, then the warp's base
+    __shared__ unsigned long long toff[TS_MAXG];  // the tile's first position in each bucket
     load_rank(r, rk);  // once per block: each block walks several tiles
     const unsigned lane = lane_id(), w = threadIdx.x >> 5;
     for (long long t = blockIdx.x; t < T; t += gridDim.x) {
     for (int b = lane; b < G; b += 32) wcnt[w][b] = 0;
+    for (int b = threadIdx.x; b < G; b += blockDim.x) toff[b] = offs[(long long)b * T + t];
     __syncthreads();
     const long long base = t * TS_TILE + (long long)w * (TS_TILE / 8);
-    unsigned bk[16];
+    unsigned bk[16], pr[16];  // bucket, and the lanes sharing it in that round
 #pragma unroll
     for (int k = 0; k < 16; k++) {  // warp w owns rows base .. base + 511, in order
         const long long i = base + k * 32 + lane;
         const bool in = i < n;
         bk[k] = in ? trie_bucket(r, code_of(i)) : 0xffffffffu;
-        const unsigned peers = __match_any_sync(0xffffffffu, bk[k]);
-        if (in && (int)lane == __ffs(peers) - 1) wcnt[w][bk[k]] += __popc(peers);
+        pr[k] = __match_any_sync(0xffffffffu, bk[k]);
+        if (in && (int)lane == __ffs(pr[k]) - 1) wcnt[w][bk[k]] += __popc(pr[k]);
         __syncwarp();
     }
     __syncthreads();
@@ -879,12 +867,11 @@ __global__ void __launch_bounds__(256) k_trie_scatter(Code code_of, long long n,
     for (int k = 0; k < 16; k++) {
         const long long i = base + k * 32 + lane;
         const bool in = i < n;
-        const unsigned peers = __match_any_sync(0xffffffffu, bk[k]);
-        const int leader = __ffs(peers) - 1;
+        const int leader = __ffs(pr[k]) - 1;
         unsigned pre = 0;
-        if (in && (int)lane == leader) { pre = wcnt[w][bk[k]]; wcnt[w][bk[k]] = pre + __popc(peers); }
+        if (in && (int)lane == leader) { pre = wcnt[w][bk[k]]; wcnt[w][bk[k]] = pre + __popc(pr[k]); }
         pre = __shfl_sync(0xffffffffu, pre, leader);
-        if (in) perm[offs[(long long)bk[k] * T + t] + pre + __popc(peers & lanemask_lt())] = i;
+        if (in) perm[toff[bk[k]] + pre + __popc(pr[k] & lanemask_lt())] = i;
         __syncwarp();
     }
     __syncthreads();
