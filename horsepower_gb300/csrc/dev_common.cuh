@@ -197,142 +197,6 @@ __device__ __forceinline__ int f64_cmp_fixed(double v, const F64Cmp& t) {
 }
 F64Cmp f64_cmp_thresholds(double s, bool scalar_first);  // host (k_elementwise.cu)
 
-// ---- exact f64 tile sums in 128-bit fixed point (see k_reduce.cu for the
-// method): the element accumulation, the rounding, and the handling of NaN
-// and infinities shared by @sum / @avg and the segmented f64 sums.
-struct Fx128 {
-    unsigned long long lo, hi;
-};
-
-__device__ __forceinline__ void fx_add(Fx128& a, unsigned long long lo, unsigned long long hi) {
-    asm("add.cc.u64 %0, %0, %2;\n\taddc.u64 %1, %1, %3;" : "+l"(a.lo), "+l"(a.hi) : "l"(lo), "l"(hi));
-}
-
-// The element with bits b in units of 2^(E - 1075 - F), signed, added to a.
-__device__ __forceinline__ void fx_accumulate(Fx128& a, unsigned long long b, int E, int F) {
-    const int e = (int)((b >> 52) & 0x7ff);
-    const unsigned long long m = (b & 0xfffffffffffffull) | ((unsigned long long)(e != 0) << 52);
-    const int k = F - E + (e > 1 ? e : 1);
-    unsigned long long lo, hi;
-    if (k >= 0) {
-        lo = m << k;
-        hi = k ? m >> (64 - k) : 0ull;
-    } else {
-        lo = k > -64 ? m >> (-k) : 0ull;
-        hi = 0;
-    }
-    const unsigned long long s = (unsigned long long)((long long)b >> 63);  // all ones when negative
-    fx_add(a, lo ^ s, hi ^ s);
-    fx_add(a, s & 1ull, 0ull);
-}
-
-// Round a (signed, |a| < 2^127) times 2^sexp to the nearest double (ties to
-// even).  sexp >= -1074, so a result below 2^-1022 is exact.
-__device__ __forceinline__ unsigned long long fx_round(Fx128 a, int sexp) {
-    const unsigned long long sign = a.hi >> 63;
-    unsigned long long lo = a.lo, hi = a.hi;
-    if (sign) {
-        lo = ~lo + 1ull;
-        hi = ~hi + (lo == 0 ? 1ull : 0ull);
-    }
-    if (!hi && !lo) return 0ull;
-    const int p = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);
-    int biased = p + sexp + 1023;
-    if (biased <= 0) return (sign << 63) | (lo << (sexp + 1074));  // subnormal: p <= 51, exact
-    const int sh = p - 52;
-    unsigned long long M;
-    bool up;
-    if (sh <= 0) {
-        M = lo << (-sh);
-        up = false;
-    } else if (sh < 64) {
-        M = (lo >> sh) | (hi << (64 - sh));
-        const unsigned long long rem = lo & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
-        up = rem > half || (rem == half && (M & 1ull));
-    } else {
-        const int r = sh - 64;
-        M = hi >> r;
-        if (r == 0) {
-            up = lo > (1ull << 63) || (lo == (1ull << 63) && (M & 1ull));
-        } else {
-            const unsigned long long remhi = hi & ((1ull << r) - 1ull), halfhi = 1ull << (r - 1);
-            up = remhi > halfhi || (remhi == halfhi && (lo != 0 || (M & 1ull)));
-        }
-    }
-    if (up && ++M == (1ull << 53)) {
-        M >>= 1;
-        biased++;
-    }
-    if (biased >= 2047) return (sign << 63) | 0x7ff0000000000000ull;
-    return (sign << 63) | ((unsigned long long)biased << 52) | (M & 0xfffffffffffffull);
-}
-
-// NaN / infinity bookkeeping of a tile: bit 0 a NaN, bit 1 +inf, bit 2 -inf;
-// the largest biased exponent among the finite elements (at least 1).
-__device__ __forceinline__ void fx_scan(unsigned long long b, unsigned& emax, unsigned& flags) {
-    const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
-    if (e == 0x7ffu) flags |= (b & 0xfffffffffffffull) ? 1u : ((b >> 63) ? 4u : 2u);
-    else emax = emax > e ? emax : e;
-}
-// The sum of a tile holding a NaN, or +inf and -inf: the quiet NaN; one kind
-// of infinity: itself.
-__device__ __forceinline__ unsigned long long fx_special(unsigned flags) {
-    return ((flags & 1u) || (flags & 6u) == 6u) ? 0x7ff8000000000000ull
-           : (flags & 2u)                       ? 0x7ff0000000000000ull
-                                                : 0xfff0000000000000ull;
-}
-// Exact sum of up to 4096 doubles held 16 per thread by a block of 256
-// threads (absent elements as +0.0), rounded once: the fixed-point tile of
-// @sum.  The result (bits) is valid in thread 0; every thread must call.
-struct FxShared {
-    unsigned e[8], f[8];
-    Fx128 acc[8];
-};
-__device__ __forceinline__ unsigned long long fx_block_sum16(const unsigned long long v[16], FxShared& sh) {
-    unsigned emax = 1, flags = 0;
-#pragma unroll
-    for (int k = 0; k < 16; k++) fx_scan(v[k], emax, flags);
-    const unsigned w = threadIdx.x >> 5;
-    emax = __reduce_max_sync(0xffffffffu, emax);
-    flags = __reduce_or_sync(0xffffffffu, flags);
-    if ((threadIdx.x & 31) == 0) {
-        sh.e[w] = emax;
-        sh.f[w] = flags;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-        emax = emax > sh.e[j] ? emax : sh.e[j];
-        flags |= sh.f[j];
-    }
-    const int E = (int)emax, F = E - 1 < 62 ? E - 1 : 62;
-    if (!flags) {  // uniform over the block
-        Fx128 acc = {0ull, 0ull};
-#pragma unroll
-        for (int k = 0; k < 16; k++) fx_accumulate(acc, v[k], E, F);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const unsigned long long l2 = __shfl_xor_sync(0xffffffffu, acc.lo, o);
-            const unsigned long long h2 = __shfl_xor_sync(0xffffffffu, acc.hi, o);
-            fx_add(acc, l2, h2);
-        }
-        if ((threadIdx.x & 31) == 0) sh.acc[w] = acc;
-    }
-    __syncthreads();
-    unsigned long long r = 0;
-    if (threadIdx.x == 0) {
-        if (flags) r = fx_special(flags);
-        else {
-            Fx128 t = sh.acc[0];
-#pragma unroll
-            for (int j = 1; j < 8; j++) fx_add(t, sh.acc[j].lo, sh.acc[j].hi);
-            r = fx_round(t, E - 1075 - F);
-        }
-    }
-    __syncthreads();  // sh may be reused
-    return r;
-}
-
 // ---- fixed-order deterministic tile sum (used by @sum/@avg and every
 // segmented sum).  A chunk of up to TILE_SUM = 4096 elements is summed as:
 //   lane t (0..255) accumulates e[t], e[t+256], ..., e[t+3840] in order

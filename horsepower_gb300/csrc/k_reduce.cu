@@ -89,7 +89,72 @@ __global__ void __launch_bounds__(256) k_tile_reduce(const T* __restrict__ x, lo
 // infinity otherwise gives itself.  Longer vectors sum their tile partials
 // the same way until one value is left.  Within a tile the result does not
 // depend on the order of the elements; the oracle restates it bit for bit.
-// (Fx128, fx_add, fx_accumulate and fx_round live in dev_common.cuh.)
+struct Fx128 {
+    unsigned long long lo, hi;
+};
+
+__device__ __forceinline__ void fx_add(Fx128& a, unsigned long long lo, unsigned long long hi) {
+    asm("add.cc.u64 %0, %0, %2;\n\taddc.u64 %1, %1, %3;" : "+l"(a.lo), "+l"(a.hi) : "l"(lo), "l"(hi));
+}
+
+// The element with bits b in units of 2^(E - 1075 - F), signed, added to a.
+__device__ __forceinline__ void fx_accumulate(Fx128& a, unsigned long long b, int E, int F) {
+    const int e = (int)((b >> 52) & 0x7ff);
+    const unsigned long long m = (b & 0xfffffffffffffull) | ((unsigned long long)(e != 0) << 52);
+    const int k = F - E + (e > 1 ? e : 1);
+    unsigned long long lo, hi;
+    if (k >= 0) {
+        lo = m << k;
+        hi = k ? m >> (64 - k) : 0ull;
+    } else {
+        lo = k > -64 ? m >> (-k) : 0ull;
+        hi = 0;
+    }
+    const unsigned long long s = (unsigned long long)((long long)b >> 63);  // all ones when negative
+    fx_add(a, lo ^ s, hi ^ s);
+    fx_add(a, s & 1ull, 0ull);
+}
+
+// Round a (signed, |a| < 2^127) times 2^sexp to the nearest double (ties to
+// even).  sexp >= -1074, so a result below 2^-1022 is exact.
+__device__ __forceinline__ unsigned long long fx_round(Fx128 a, int sexp) {
+    const unsigned long long sign = a.hi >> 63;
+    unsigned long long lo = a.lo, hi = a.hi;
+    if (sign) {
+        lo = ~lo + 1ull;
+        hi = ~hi + (lo == 0 ? 1ull : 0ull);
+    }
+    if (!hi && !lo) return 0ull;
+    const int p = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);
+    int biased = p + sexp + 1023;
+    if (biased <= 0) return (sign << 63) | (lo << (sexp + 1074));  // subnormal: p <= 51, exact
+    const int sh = p - 52;
+    unsigned long long M;
+    bool up;
+    if (sh <= 0) {
+        M = lo << (-sh);
+        up = false;
+    } else if (sh < 64) {
+        M = (lo >> sh) | (hi << (64 - sh));
+        const unsigned long long rem = lo & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        up = rem > half || (rem == half && (M & 1ull));
+    } else {
+        const int r = sh - 64;
+        M = hi >> r;
+        if (r == 0) {
+            up = lo > (1ull << 63) || (lo == (1ull << 63) && (M & 1ull));
+        } else {
+            const unsigned long long remhi = hi & ((1ull << r) - 1ull), halfhi = 1ull << (r - 1);
+            up = remhi > halfhi || (remhi == halfhi && (lo != 0 || (M & 1ull)));
+        }
+    }
+    if (up && ++M == (1ull << 53)) {
+        M >>= 1;
+        biased++;
+    }
+    if (biased >= 2047) return (sign << 63) | 0x7ff0000000000000ull;
+    return (sign << 63) | ((unsigned long long)biased << 52) | (M & 0xfffffffffffffull);
+}
 
 // Block = 256 threads, one 4096-element tile per block.
 __global__ void __launch_bounds__(256) k_tile_sum_fx(const unsigned long long* __restrict__ x, long long n,

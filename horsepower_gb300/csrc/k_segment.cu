@@ -315,173 +315,6 @@ __global__ void k_u64_to_i64(const unsigned long long* __restrict__ a, long long
         b[i] = (long long)a[i];
 }
 
-// ---- f64 sums of segments in fixed point.  Each segment is summed as @sum
-// sums a vector (k_reduce.cu): tiles of 4096 consecutive elements, each tile
-// exact in 128-bit fixed point and rounded once, then the tile sums the same
-// way until one value is left.  So a group's f64 sum is, bit for bit, pfnSum
-// of the group's rows gathered into one vector, whatever kernel reduces it.
-// Within a tile the exact sum does not depend on the order of the elements,
-// so each size class takes the cheapest split.
-__device__ __forceinline__ unsigned long long dbits(double v) { return (unsigned long long)__double_as_longlong(v); }
-
-// Classes 0-5 (at most 32 elements): a sub-warp of P lanes per segment, one
-// element per lane.
-template <bool GATHER>
-__global__ void __launch_bounds__(256) k_segfx_small(const double* __restrict__ src, const long long* __restrict__ rows,
-                                                     long long nx, const long long* __restrict__ starts, long long ng,
-                                                     long long total, const unsigned* __restrict__ ids,
-                                                     const unsigned* __restrict__ cnt, double* __restrict__ out,
-                                                     unsigned* derr) {
-    __shared__ long long wfirst[7];
-    __shared__ unsigned cfirst[6];
-    if (threadIdx.x == 0) {
-        long long w = 0;
-        unsigned o = 0;
-        for (int c = 0; c < 6; c++) {
-            wfirst[c] = w;
-            cfirst[c] = o;
-            const long long per = 32 >> c;
-            w += ((long long)cnt[c] + per - 1) / per;
-            o += cnt[c];
-        }
-        wfirst[6] = w;
-    }
-    __syncthreads();
-    const unsigned lane = lane_id();
-    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-    bool bad = false;
-    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < wfirst[6]; w += warps) {
-        int c = 0;
-        while (c < 5 && w >= wfirst[c + 1]) c++;
-        const int P = 1 << c;
-        const unsigned q = lane >> c, j = lane & (P - 1);
-        const long long k = (w - wfirst[c]) * (32 >> c) + q;
-        unsigned long long b = 0;
-        long long g = -1;
-        if (k < (long long)cnt[c]) {
-            g = ids[cfirst[c] + k];
-            const long long st = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total;
-            if ((long long)j < e - st) b = dbits(seg_elem<double, GATHER>(src, rows, nx, st + j, bad));
-        }
-        unsigned emax = 1, flags = 0;
-        fx_scan(b, emax, flags);
-        for (int o = P >> 1; o > 0; o >>= 1) {
-            const unsigned e2 = __shfl_xor_sync(0xffffffffu, emax, o);
-            emax = emax > e2 ? emax : e2;
-            flags |= __shfl_xor_sync(0xffffffffu, flags, o);
-        }
-        const int E = (int)emax, F = E - 1 < 62 ? E - 1 : 62;
-        Fx128 acc = {0ull, 0ull};
-        if (!flags) fx_accumulate(acc, b, E, F);
-        for (int o = P >> 1; o > 0; o >>= 1) {
-            const unsigned long long l2 = __shfl_xor_sync(0xffffffffu, acc.lo, o);
-            const unsigned long long h2 = __shfl_xor_sync(0xffffffffu, acc.hi, o);
-            fx_add(acc, l2, h2);
-        }
-        if (j == 0 && g >= 0) out[g] = __longlong_as_double((long long)(flags ? fx_special(flags) : fx_round(acc, E - 1075 - F)));
-    }
-    if (bad) flag_error(derr, DERR_INDEX);
-}
-
-// Class 6 (33 to 4096 elements, one tile): one warp per segment, in two
-// passes over its elements (the largest exponent first, then the sum).
-template <bool GATHER>
-__global__ void __launch_bounds__(256) k_segfx_mid(const double* __restrict__ src, const long long* __restrict__ rows,
-                                                   long long nx, const long long* __restrict__ starts, long long ng,
-                                                   long long total, const unsigned* __restrict__ ids,
-                                                   const unsigned* __restrict__ cnt, double* __restrict__ out,
-                                                   unsigned* derr) {
-    __shared__ unsigned first;
-    if (threadIdx.x == 0) {
-        unsigned o = 0;
-        for (int c = 0; c < 6; c++) o += cnt[c];
-        first = o;
-    }
-    __syncthreads();
-    const long long n6 = cnt[6];
-    const unsigned lane = lane_id();
-    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-    bool bad = false;
-    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n6; w += warps) {
-        const long long g = ids[first + w];
-        const long long st = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total;
-        const long long m = e - st;  // at most 4096: the virtual warps v of one 256-lane tile cover it
-        unsigned emax = 1, flags = 0;
-        for (int v = 0; v < 8 && v * 32 < m; v++) {
-            double x[16];
-            seg_load16<double, GATHER>(src, rows, nx, st + v * 32 + lane, e, x, bad);
-#pragma unroll
-            for (int k = 0; k < 16; k++) fx_scan(dbits(x[k]), emax, flags);
-        }
-        emax = __reduce_max_sync(0xffffffffu, emax);
-        flags = __reduce_or_sync(0xffffffffu, flags);
-        const int E = (int)emax, F = E - 1 < 62 ? E - 1 : 62;
-        Fx128 acc = {0ull, 0ull};
-        if (!flags) {
-            for (int v = 0; v < 8 && v * 32 < m; v++) {
-                double x[16];
-                seg_load16<double, GATHER>(src, rows, nx, st + v * 32 + lane, e, x, bad);
-#pragma unroll
-                for (int k = 0; k < 16; k++) fx_accumulate(acc, dbits(x[k]), E, F);
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const unsigned long long l2 = __shfl_xor_sync(0xffffffffu, acc.lo, o);
-                const unsigned long long h2 = __shfl_xor_sync(0xffffffffu, acc.hi, o);
-                fx_add(acc, l2, h2);
-            }
-        }
-        if (lane == 0) out[g] = __longlong_as_double((long long)(flags ? fx_special(flags) : fx_round(acc, E - 1075 - F)));
-    }
-    if (bad) flag_error(derr, DERR_INDEX);
-}
-
-// One CTA per 4096-element chunk of the long segments: the chunk's exact sum.
-template <bool GATHER>
-__global__ void __launch_bounds__(256) k_segfx_chunk(const double* __restrict__ src, const long long* __restrict__ rows,
-                                                     long long nx, const long long* __restrict__ starts, long long ng,
-                                                     long long total, const long long* __restrict__ big,
-                                                     const unsigned long long* __restrict__ chunk0, long long nbig,
-                                                     double* __restrict__ part, unsigned* derr) {
-    __shared__ FxShared sh;
-    const long long c = blockIdx.x;
-    long long lo = 0, hi = nbig - 1;
-    while (lo < hi) {
-        long long mid = (lo + hi + 1) >> 1;
-        if ((long long)chunk0[mid] <= c) lo = mid; else hi = mid - 1;
-    }
-    const long long g = big[lo];
-    const long long st = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total;
-    const long long base = st + (c - (long long)chunk0[lo]) * TILE_SUM;
-    bool bad = false;
-    double x[16];
-    seg_load16<double, GATHER>(src, rows, nx, base + threadIdx.x, e, x, bad);
-    unsigned long long v[16];
-#pragma unroll
-    for (int k = 0; k < 16; k++) v[k] = dbits(x[k]);
-    const unsigned long long r = fx_block_sum16(v, sh);
-    if (threadIdx.x == 0) part[c] = __longlong_as_double((long long)r);
-    if (bad) flag_error(derr, DERR_INDEX);
-}
-
-// The chunk sums of each long segment (at most 4096 of them: the caller
-// checks), one CTA per segment, summed as one more tile into out.
-__global__ void __launch_bounds__(256) k_segfx_partials(const double* __restrict__ part, const long long* __restrict__ pstarts,
-                                                        const long long* __restrict__ big, long long nbig,
-                                                        long long nchunks, double* __restrict__ out) {
-    __shared__ FxShared sh;
-    const long long g = blockIdx.x;
-    const long long st = pstarts[g], e = (g + 1 < nbig) ? pstarts[g + 1] : nchunks;
-    unsigned long long v[16];
-#pragma unroll
-    for (int k = 0; k < 16; k++) {
-        const long long j = st + k * 256 + threadIdx.x;
-        v[k] = j < e ? dbits(part[j]) : 0ull;
-    }
-    const unsigned long long r = fx_block_sum16(v, sh);
-    if (threadIdx.x == 0) out[big[g]] = __longlong_as_double((long long)r);
-}
-
 static unsigned gcap(long long n, int per = 256) {
     unsigned g = grid_for(n, per);
     return g > (unsigned)g_sms * 32 ? (unsigned)g_sms * 32 : g;
@@ -570,22 +403,12 @@ static I seg_reduce(const T* src, const long long* rows, long long nx, const lon
         for (int c = 0; c < 6; c++) small = small || li->cls_host[c] != 0;
         mid = li->cls_host[6] != 0;
     }
-    constexpr bool FX = std::is_same<T, double>::value && std::is_same<A, double>::value && OP == OP_SUM;
-    if constexpr (FX) {
-        if (small)
-            HG_LAUNCH("seg_warps", gcap(ng * 4), 256, 0, (k_segfx_small<GATHER>), src, rows, nx, starts, ng, total, ids,
-                      ccnt, out, g_derr);
-        if (mid)
-            HG_LAUNCH("seg_mid", gcap(ng), 256, 0, (k_segfx_mid<GATHER>), src, rows, nx, starts, ng, total, ids, ccnt,
-                      out, g_derr);
-    } else {
-        if (small)
-            HG_LAUNCH("seg_warps", gcap(ng * 4), 256, 0, (k_seg_warps<T, A, OP, GATHER>), src, rows, nx, starts, ng,
-                      total, ids, ccnt, ident, out, g_derr);
-        if (mid)
-            HG_LAUNCH("seg_mid", gcap(ng), 256, 0, (k_seg_mid<T, A, OP, GATHER>), src, rows, nx, starts, ng, total,
-                      ids, ccnt, ident, out, g_derr);
-    }
+    if (small)
+        HG_LAUNCH("seg_warps", gcap(ng * 4), 256, 0, (k_seg_warps<T, A, OP, GATHER>), src, rows, nx, starts, ng, total,
+                  ids, ccnt, ident, out, g_derr);
+    if (mid)
+        HG_LAUNCH("seg_mid", gcap(ng), 256, 0, (k_seg_mid<T, A, OP, GATHER>), src, rows, nx, starts, ng, total, ids,
+                  ccnt, ident, out, g_derr);
     if (known && li->cls_host[7] == 0) return last_launch_error();
     LongPlan pl;
     HG_CHECK(seg_plan_long(starts, ng, total, li, &pl));
@@ -595,22 +418,14 @@ static I seg_reduce(const T* src, const long long* rows, long long nx, const lon
     A* part = (A*)salloc((size_t)nchunks * sizeof(A));
     A* res = (A*)salloc((size_t)nbig * sizeof(A));
     if (!part || !res) return E_DEVICE_OOM;
-    if constexpr (FX)
-        HG_LAUNCH("seg_chunk", (unsigned)nchunks, 256, 0, (k_segfx_chunk<GATHER>), src, rows, nx, starts, ng, total,
-                  pl.big, pl.c0, nbig, part, g_derr);
-    else
-        HG_LAUNCH("seg_chunk", (unsigned)nchunks, 256, 0, (k_seg_chunk<T, A, OP, GATHER>), src, rows, nx, starts, ng,
-                  total, pl.big, pl.c0, nbig, ident, part, g_derr);
+    HG_LAUNCH("seg_chunk", (unsigned)nchunks, 256, 0, (k_seg_chunk<T, A, OP, GATHER>), src, rows, nx, starts, ng,
+              total, pl.big, pl.c0, nbig, ident, part, g_derr);
     // partials of each long segment are reduced by the same procedure: at
     // most 4096 of them per segment (certain when there are at most 4096 in
     // all) in one launch straight into out, else as segments of their own
     if (nchunks <= (unsigned long long)TILE_SUM) {
-        if constexpr (FX)
-            HG_LAUNCH("seg_partials", (unsigned)nbig, 256, 0, k_segfx_partials, part, pl.pstarts, pl.big, nbig,
-                      (long long)nchunks, out);
-        else
-            HG_LAUNCH("seg_partials", (unsigned)nbig, 256, 0, (k_seg_partials<A, OP>), part, pl.pstarts, pl.big, nbig,
-                      (long long)nchunks, ident, out);
+        HG_LAUNCH("seg_partials", (unsigned)nbig, 256, 0, (k_seg_partials<A, OP>), part, pl.pstarts, pl.big, nbig,
+                  (long long)nchunks, ident, out);
         return last_launch_error();
     }
     HG_CHECK((seg_reduce<A, A, OP, false>(part, nullptr, 0, pl.pstarts, nbig, (long long)nchunks, ident, res)));
@@ -619,11 +434,11 @@ static I seg_reduce(const T* src, const long long* rows, long long nx, const lon
 }
 
 // ---- several f64 sums over the long segments of one grouping at once.
-// One CTA per 4096-element chunk, as k_segfx_chunk, but the chunk's row ids
-// are read once and each of the ncol columns is gathered through them, one
-// column at a time (16 gathers in flight per lane); each column's chunk sum
-// is the same exact fixed-point tile, so part[col * nchunks + c] is
-// bit-identical to k_segfx_chunk's for that column.
+// One CTA per 4096-element chunk, as k_seg_chunk, but the chunk's row ids
+// are read once and each of the ncol columns is gathered through them (all
+// 16 x ncol gathers of a lane issued before the first add); each column's
+// chunk partial follows the tile tree, so part[col * nchunks + c] is
+// bit-identical to k_seg_chunk's for that column.
 constexpr int SEG_MANY = 4;
 struct SegCols { const double* src[SEG_MANY]; };
 template <int NCOL>
@@ -633,7 +448,7 @@ __global__ void __launch_bounds__(256) k_seg_chunk_many(SegCols cols, int ncol, 
                                                         const unsigned long long* __restrict__ chunk0, long long nbig,
                                                         unsigned long long nchunks, double* __restrict__ part,
                                                         unsigned* derr) {
-    __shared__ FxShared sh;
+    __shared__ double ws[SEG_MANY][8];
     const long long c = blockIdx.x;
     long long lo = 0, hi = nbig - 1;  // the long segment owning chunk c
     while (lo < hi) {
@@ -652,12 +467,23 @@ __global__ void __launch_bounds__(256) k_seg_chunk_many(SegCols cols, int ncol, 
         bad |= j < e && (r[k] < 0 || r[k] >= nx);
     }
 #pragma unroll 1
-    for (int q = 0; q < NCOL; q++) {
-        unsigned long long v[16];
+    for (int q = 0; q < NCOL; q++) {  // one column at a time: 16 gathers in flight, few registers
+        double v[16];
 #pragma unroll
-        for (int k = 0; k < 16; k++) v[k] = (r[k] >= 0 && r[k] < nx) ? dbits(cols.src[q][r[k]]) : 0ull;
-        const unsigned long long sum = fx_block_sum16(v, sh);
-        if (threadIdx.x == 0) part[(unsigned long long)q * nchunks + c] = __longlong_as_double((long long)sum);
+        for (int k = 0; k < 16; k++) v[k] = (r[k] >= 0 && r[k] < nx) ? cols.src[q][r[k]] : 0.0;
+        double acc = 0.0;
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+            if (first + (long long)k * 256 < e) acc = __dadd_rn(acc, v[k]);
+        acc = swarp<double, OP_SUM>(acc);
+        if ((threadIdx.x & 31) == 0) ws[q][threadIdx.x >> 5] = acc;
+    }
+    __syncthreads();
+    if (threadIdx.x < (unsigned)NCOL) {
+        const double* w = ws[threadIdx.x];
+        const double w01 = __dadd_rn(w[0], w[1]), w23 = __dadd_rn(w[2], w[3]);
+        const double w45 = __dadd_rn(w[4], w[5]), w67 = __dadd_rn(w[6], w[7]);
+        part[(unsigned long long)threadIdx.x * nchunks + c] = __dadd_rn(__dadd_rn(w01, w23), __dadd_rn(w45, w67));
     }
     if (bad) flag_error(derr, DERR_INDEX);
 }
@@ -690,8 +516,8 @@ I seg_sum_f64_many(const double* const* srcs, int ncol, const long long* rows, l
     else SEG_MANY_LAUNCH(4);
 #undef SEG_MANY_LAUNCH
     for (int q = 0; q < ncol; q++)
-        HG_LAUNCH("seg_partials", (unsigned)pl.nbig, 256, 0, k_segfx_partials, part + (size_t)q * pl.nchunks,
-                  pl.pstarts, pl.big, pl.nbig, (long long)pl.nchunks, sums[q]);
+        HG_LAUNCH("seg_partials", (unsigned)pl.nbig, 256, 0, (k_seg_partials<double, OP_SUM>), part + (size_t)q * pl.nchunks,
+                  pl.pstarts, pl.big, pl.nbig, (long long)pl.nchunks, 0.0, sums[q]);
     return last_launch_error();
 }
 

@@ -1212,12 +1212,11 @@ E hgoTreeSumF64(const E *x, L n) {
     return r;
 }
 
-/* hgoFixedSumF64 per group: out[g] = the fixed-point sum (tiles of 4096
- * exact sums, each rounded once, then the tile sums the same way) of
- * x[perm[starts[g]]], ..., x[perm[starts[g+1] - 1]] (starts[ng] = n): the
- * library's per-group f64 sums, which equal @sum of each group's rows.
- * Groups are independent, so they run as OpenMP iterations. */
-void hgoSegFixedSumF64(const E *x, const L *perm, const L *starts, L ng, L n, E *out) {
+/* hgoTreeSumF64 per group: out[g] = the fixed-order tile-tree sum of
+ * x[perm[starts[g]]], ..., x[perm[starts[g+1] - 1]] (starts[ng] = n), the
+ * order every segmented sum of the GPU library follows.  Groups are
+ * independent, so they run as OpenMP iterations. */
+void hgoSegTreeSumF64(const E *x, const L *perm, const L *starts, L ng, L n, E *out) {
 #pragma omp parallel
     {
         L cap = 4096;
@@ -1227,7 +1226,7 @@ void hgoSegFixedSumF64(const E *x, const L *perm, const L *starts, L ng, L n, E 
             L a = starts[g], b = g + 1 < ng ? starts[g + 1] : n;
             if (b - a > cap) { cap = b - a; buf = realloc(buf, sizeof(E) * cap); }
             for (L k = a; k < b; k++) buf[k - a] = x[perm[k]];
-            out[g] = hgoFixedSumF64(buf, b - a);
+            out[g] = hgoTreeSumF64(buf, b - a);
         }
         free(buf);
     }

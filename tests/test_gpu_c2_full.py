@@ -10,9 +10,9 @@ f64 payload uniform over [0, 1e5).  Checked:
   values) and the group lengths are bit-exact against the oracle's
   restatement of lib_group_by_normal_long (h_libs.cc:1369-1403);
 * per-group sums (hgpuGroupSum) are bit-exact against the oracle's
-  restatement of the library's fixed-point @sum over each group's rows, and
-  within 1e-12 relative of the oracle's per-group pfnSum (the reference's
-  OpenMP order, h_primitive.cc:764-786);
+  restatement of the library's fixed tile-tree order over each group's rows,
+  and within 1e-12 relative of the oracle's per-group pfnSum (the
+  reference's OpenMP order, h_primitive.cc:764-786);
 * @order((key, sec), (1, 1)): the permutation is bit-exact against the
   oracle's lib_quicksort_list (h_libs.cc:637-697: merge sort on key, then on
   sec within each run of equal keys).
@@ -41,8 +41,8 @@ def c2():
     from horsepower_gb300 import serve as S
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
     ora = Builtins(os.path.join(ROOT, "oracle", "_build", "liboracle.so"), "oracle")
-    ora.lib.hgoSegFixedSumF64.restype = None
-    ora.lib.hgoSegFixedSumF64.argtypes = [C.c_void_p] * 3 + [C.c_longlong, C.c_longlong, C.c_void_p]
+    ora.lib.hgoSegTreeSumF64.restype = None
+    ora.lib.hgoSegTreeSumF64.argtypes = [C.c_void_p] * 3 + [C.c_longlong, C.c_longlong, C.c_void_p]
     gpu = horsepower_gb300.load()
     o = S.order_table(gpu, N, seed=2)
     key, sec = gpu.to_py(o["key"]), gpu.to_py(o["sec"])
@@ -83,13 +83,13 @@ def test_c2_group_full(c2):
     assert gkeys.dtype == okeys.dtype and np.array_equal(gkeys, okeys)
     assert np.array_equal(glens, olens)
     assert np.array_equal(grows, orows)
-    # per-group sums: @sum of each group's rows (fixed-point tiles), over the (now known equal) row lists
+    # per-group sums: the fixed tile-tree order exactly, over the (now known equal) row lists
     starts = np.zeros(len(glens), np.int64)
     np.cumsum(glens[:-1], out=starts[1:])
     want = np.empty(len(glens))
     t0 = time.perf_counter()
-    ora.lib.hgoSegFixedSumF64(pay.ctypes.data, orows.ctypes.data, starts.ctypes.data, len(glens), N, want.ctypes.data)
-    _log("oracle fixed-point sums", t0)
+    ora.lib.hgoSegTreeSumF64(pay.ctypes.data, orows.ctypes.data, starts.ctypes.data, len(glens), N, want.ctypes.data)
+    _log("oracle tree sums", t0)
     assert gsums.tobytes() == want.tobytes()
     # and the reference's own per-group sums (pfnSum, OpenMP order) within the tolerance
     t0 = time.perf_counter()
