@@ -219,6 +219,7 @@ def run_gb300(args, rank, ws, dist, dim, fact):
     Lb = gpu.lib
     Lb.hgpuTimerStop.restype = C.c_double
     Lb.hgpuLaunchCount.restype = C.c_longlong
+    Lb.hgpuSyncCount.restype = C.c_longlong
     Lb.hgpuProfileRead.restype = C.c_int32
     Lb.hgpuProfileRead.argtypes = [C.c_int32, C.POINTER(C.c_char_p), C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
     Lb.initV.restype = C.c_void_p
@@ -292,6 +293,7 @@ def run_gb300(args, rank, ws, dist, dim, fact):
         dist.barrier()
     Lb.hgpuSync()
     launches0 = Lb.hgpuLaunchCount()
+    syncs0 = Lb.hgpuSyncCount()
     clocks.start()
     Lb.hgpuTimerStart()
     t0 = time.perf_counter()
@@ -301,6 +303,7 @@ def run_gb300(args, rank, ws, dist, dim, fact):
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     launches = Lb.hgpuLaunchCount() - launches0
+    syncs = Lb.hgpuSyncCount() - syncs0
 
     # ---- the same K steps again with a CUDA event pair around every launch,
     # for the per-kernel durations (roofline, breakdown); the event records
@@ -360,7 +363,7 @@ def run_gb300(args, rank, ws, dist, dim, fact):
     e2e_s = barrier_max(dist, time.perf_counter() - t0)
     d2h = sum(v.nbytes for v in vals)
 
-    out = dict(rows_per_step=F, step_ms=step_ms, wall_s=wall, launches=launches, kernels=kernels,
+    out = dict(rows_per_step=F, step_ms=step_ms, wall_s=wall, launches=launches, syncs=syncs, kernels=kernels,
                driver="compiled C query (queries/join_group.c)" if query is not P.join_group else "python statements",
                profiled_step_ms=ms_profiled / args.steps,
                clocks=clk, e2e_rows_s=ws * F * args.steps / e2e_s, e2e_ms=1000 * e2e_s / args.steps,
@@ -1175,6 +1178,7 @@ def main():
         "cpu_baseline": cpu,
         "parity_vs_oracle": parity,
         "gpu_launches": r["launches"],
+        "host_syncs_per_step": r["syncs"] / args.steps,
         "clocks": r["clocks"],
         "kernels_ms_per_step": {k: round(v, 4) for k, v in per_step_ms.items()},
         "kernel_times": ("a second pass of the same K steps with a CUDA event pair around every launch "

@@ -48,6 +48,15 @@ constexpr long long SPIN_LIMIT = 1LL << 24;
 
 // ---------------------------------------------------------------- runtime
 extern cudaStream_t g_stream;
+// waits for the library stream, counts the wait (hgpuSyncCount) and
+// delivers the reads queued by rb_queue
+cudaError_t stream_sync();
+// queues a read of `bytes` of device memory into host_dst, performed by the
+// next stream_sync (or check_device_errors) in the same round trip
+constexpr int RB_ITEMS = 8;
+constexpr unsigned RB_BYTES = 16384;
+I rb_queue(void* host_dst, const void* dev, size_t bytes);
+cudaError_t rb_init();
 extern int g_sms;
 I ensure_init();
 I sync();
@@ -151,6 +160,7 @@ struct ListInfo {
     const long long* big;
     const unsigned long long* chunk0;
     const long long* pstarts;
+    const unsigned* corder;   // chunk launch order (nullptr: in segment order)
     // cached segment ids by size class and the class counts (output arena)
     const unsigned* cls_ids;
     const unsigned* cls_cnt;
@@ -159,6 +169,26 @@ struct ListInfo {
     unsigned cls_host[8];
 };
 void register_list(const ListInfo& g);
+// The size classes and the long-segment plan of a list of at most
+// SEG_PLAN_SMALL segments, made by one launch queued on the library stream;
+// the caller queues the read of hdr_dev into hdr (rb_queue) with its own
+// next wait and then hands the plan to seg_plan_adopt, which puts it into
+// the list's ListInfo, so that aggregations over the list need no round
+// trip of their own.  Lists with more segments get nothing (hdr == nullptr).
+constexpr long long SEG_PLAN_SMALL = 4096;
+constexpr size_t SEG_PLAN_HDR_BYTES = 10 * 8;  // 8 class counts, nbig, nchunks
+struct SmallPlan {
+    unsigned* cc = nullptr;
+    unsigned* ids = nullptr;
+    long long* big = nullptr;
+    unsigned long long* c0 = nullptr;
+    long long* ps = nullptr;
+    unsigned* order = nullptr;
+    unsigned long long* hdr = nullptr;      // host: 8 class counts, nbig, nchunks (after the wait)
+    const unsigned long long* hdr_dev = nullptr;  // the same on the device, for the caller to queue
+};
+I seg_plan_small(const long long* starts, long long ng, long long total, SmallPlan* p);
+void seg_plan_adopt(ListInfo& li, const SmallPlan& p);
 ListInfo* find_list(const V0* nodes, long long ng);
 
 // Index vectors produced by this library carry a known value range: every

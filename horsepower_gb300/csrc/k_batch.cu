@@ -839,7 +839,7 @@ I plan_through_builtins(const hgpuJoinGroupPlan& q, hgpuJoinGroupResult* r) {
                 goto done;
             }
         }
-        if (cudaStreamSynchronize(g_stream) != cudaSuccess) rc = set_error(E_DEVICE, "copying a plan result");
+        if (stream_sync() != cudaSuccess) rc = set_error(E_DEVICE, "copying a plan result");
     }
 #undef STEP
 done:
@@ -989,7 +989,7 @@ static I shared_probe(const hgpuJoinGroupPlan* plans, int np, std::vector<char>*
     }
     std::vector<long long> hmm(4 * ng);
     HG_CU(cudaMemcpyAsync(hmm.data(), mm, (size_t)ng * 32, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CU(stream_sync());
     struct Built { int g; long long kmin; unsigned long long kspan; int dmin, drange; unsigned* dimhist; unsigned* facthist;
                    unsigned* dup; unsigned short* dd; };
     std::vector<Built> built;
@@ -1123,7 +1123,7 @@ extern "C" I hgpuBatchJoinGroup(const hgpuJoinGroupPlan* plans, L nplans, hgpuJo
     if (dtiles[np] > 0) HG_LAUNCH("b_minmax", (unsigned)dtiles[np], 256, 0, k_b_minmax, dP, dT, np, mm);
     std::vector<long long> hmm(2 * np);
     HG_CU(cudaMemcpyAsync(hmm.data(), mm, np * 16, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CU(stream_sync());
     // presence bitmaps and code tables
     long long bm_words = 0;
     for (int p = 0; p < np; p++) {

@@ -234,7 +234,7 @@ static I compact(const uint8_t* mask, long long n, CompactCols& cols, long long*
     }
     HG_CHECK(last_launch_error());
     unsigned long long h = 0;
-    HG_CU(cudaMemcpyAsync(&h, offs + ntiles, 8, cudaMemcpyDeviceToHost, g_stream));
+    HG_CHECK(rb_queue(&h, offs + ntiles, 8));
     HG_CHECK(check_device_errors());  // synchronises
     *count = (long long)h;
     return 0;
@@ -289,8 +289,8 @@ static I compress_one(V z, V x, V y) {
         void* tmp = d;
         z->g = (G)&z->b;
         z->i64 = 0;
-        if (cnt == 1) HG_CU(cudaMemcpyAsync(&z->b, tmp, es, cudaMemcpyDeviceToHost, g_stream));
-        HG_CU(cudaStreamSynchronize(g_stream));
+        if (cnt == 1) HG_CHECK(rb_queue(&z->b, tmp, es));
+        HG_CU(stream_sync());
         out_rewind(mark);
         return apply_residency(z);
     }
@@ -338,8 +338,8 @@ I pfnWhere(V z, V x) {
     if (cnt <= 1) {
         z->g = (G)&z->b;
         z->i64 = 0;
-        if (cnt == 1) HG_CU(cudaMemcpyAsync(&z->b, d, 8, cudaMemcpyDeviceToHost, g_stream));
-        HG_CU(cudaStreamSynchronize(g_stream));
+        if (cnt == 1) HG_CHECK(rb_queue(&z->b, d, 8));
+        HG_CU(stream_sync());
         out_rewind(mark);
         return apply_residency(z);
     }

@@ -345,8 +345,8 @@ static I table_build(Table<K>* t, const void* x, int typ, long long n, bool with
         if (g > (unsigned)g_sms * 8) g = g_sms * 8;
         HG_LAUNCH("key_minmax", g, 256, 0, k_key_minmax, x, typ, n, mm);
         long long h[2];
-        HG_CU(cudaMemcpyAsync(h, mm, 16, cudaMemcpyDeviceToHost, g_stream));
-        HG_CU(cudaStreamSynchronize(g_stream));
+        HG_CHECK(rb_queue(h, mm, 16));
+        HG_CU(stream_sync());
         unsigned long long range = (unsigned long long)h[1] - (unsigned long long)h[0] + 1ull;
         unsigned long long lim = 8ull * (unsigned long long)n;
         if (lim < (1ull << 16)) lim = 1ull << 16;
@@ -1056,8 +1056,7 @@ static I probe_direct_staged(const Table<unsigned>& t, const int* y, long long n
     HG_LAUNCH("join_emit", (unsigned)((nwarps + 8 * JU_GROUP - 1) / (8 * JU_GROUP)), 256, 0, k_jp_unstage, (const uint2*)stage,
               (const unsigned*)wcounts, (const unsigned*)wpre, (const unsigned long long*)toffs, nwarps, 32 * R, zb, zp);
     HG_CHECK(last_launch_error());
-    HG_CU(cudaMemcpyAsync(m, toffs + ntiles, 8, cudaMemcpyDeviceToHost, g_stream));
-    return 0;
+    return rb_queue(m, toffs + ntiles, 8);  // read by the caller's check_device_errors
 }
 
 // s: one status word per warp sub-tile, then the tile ticket and the total
@@ -1075,14 +1074,18 @@ static I launch_probe(const Table<K>& t, const LinearBuild& lin, int mode, const
 // vectors: both are allocated for ny rows, the second (the last allocation)
 // shrinks to the m matches afterwards, the first keeps its unused tail until
 // the arena is rewound.  No copy of the pairs is made.
+// With `repeat_flag` (the build's repeated-key word) the probe runs before
+// the build is known to be unique and the flag comes back with the match
+// count: when it is set, *repeated is set and nothing is returned in z.
 template <typename K>
 static I join_probe_unique(V z, const Table<K>& t, const LinearBuild& lin, int mode, const void* py, I ytyp,
-                           long long ny, long long nbuild) {
+                           long long ny, long long nbuild, const unsigned* repeat_flag = nullptr,
+                           bool* repeated = nullptr) {
     const int R = g_tile_rows;
     const long long tile = (long long)JT_THREADS * R;
     long long ntiles = (ny + tile - 1) / tile;
-    HG_CHECK(init_list(z, H_G, 2));
-    V0* e = host_nodes(z);
+    const long long mark = out_mark();
+    unsigned rep = 0;
     const size_t cap = (size_t)(ny > 1 ? ny : 2) * 8;
     long long* zb = (long long*)dalloc(cap);
     long long* zp = (long long*)dalloc(cap);
@@ -1099,15 +1102,27 @@ static I join_probe_unique(V z, const Table<K>& t, const LinearBuild& lin, int m
             else if (R == 32) HG_CHECK(probe_direct_staged<32>(t, y, ny, ntiles, zb, zp, &m));
             else HG_CHECK(probe_direct_staged<16>(t, y, ny, ntiles, zb, zp, &m));
         }
+        if (repeat_flag) HG_CHECK(rb_queue(&rep, repeat_flag, 4));
         HG_CHECK(check_device_errors());
     } else if (ntiles > 0) {
         HG_CU(cudaMemsetAsync(s, 0, sbytes, g_stream));
         if (R == 8) HG_CHECK((launch_probe<K, 8>(t, lin, mode, py, ytyp, ny, zb, zp, s, ntiles)));
         else if (R == 32) HG_CHECK((launch_probe<K, 32>(t, lin, mode, py, ytyp, ny, zb, zp, s, ntiles)));
         else HG_CHECK((launch_probe<K, 16>(t, lin, mode, py, ytyp, ny, zb, zp, s, ntiles)));
-        HG_CU(cudaMemcpyAsync(&m, s + sbytes - 56, 8, cudaMemcpyDeviceToHost, g_stream));
+        HG_CHECK(rb_queue(&m, s + sbytes - 56, 8));
+        if (repeat_flag) HG_CHECK(rb_queue(&rep, repeat_flag, 4));
+        HG_CHECK(check_device_errors());
+    } else if (repeat_flag) {
+        HG_CHECK(rb_queue(&rep, repeat_flag, 4));
         HG_CHECK(check_device_errors());
     }
+    if (rep) {  // repeated build keys: the caller takes the other path
+        *repeated = true;
+        out_rewind(mark);
+        return 0;
+    }
+    HG_CHECK(init_list(z, H_G, 2));
+    V0* e = host_nodes(z);
     dshrink(zp, (size_t)(m > 1 ? m : 1) * 8);
     long long* outs[2] = {zb, zp};
     for (int i = 0; i < 2; i++) {
@@ -1130,12 +1145,21 @@ static I join_hash(V z, const void* px, I typ, long long nx, const void* py, lon
     // 15M-key range would otherwise clear 60 MB per join for nothing)
     HG_CHECK(table_build<K>(&t, px, typ, nx, false));
     unsigned long long nslots = t.cap + 1;  // + the side slot of 64-bit keys
-    unsigned dup = 0;
-    HG_CU(cudaMemcpyAsync(&dup, t.flags, 4, cudaMemcpyDeviceToHost, g_stream));
-    HG_CHECK(check_device_errors());
-    if (!dup) {
+    if (t.direct) {
+        // a direct table: probe as if the build keys were unique and read
+        // the repeated-key flag with the match count, in one round trip
         LinearBuild lin{};
-        return join_probe_unique<K>(z, t, lin, 0, py, typ, ny, nx);
+        bool repeated = false;
+        HG_CHECK(join_probe_unique<K>(z, t, lin, 0, py, typ, ny, nx, t.flags, &repeated));
+        if (!repeated) return 0;
+    } else {
+        unsigned dup = 0;
+        HG_CHECK(rb_queue(&dup, t.flags, 4));
+        HG_CHECK(check_device_errors());
+        if (!dup) {
+            LinearBuild lin{};
+            return join_probe_unique<K>(z, t, lin, 0, py, typ, ny, nx);
+        }
     }
     t.cnt = (unsigned*)salloc(t.cap * 4);
     if (!t.cnt) return E_DEVICE_OOM;
@@ -1218,7 +1242,7 @@ static I join_single(V z, V x, V y, V f) {
         const void* pxd;
         HG_CHECK(promote_to(x, typ, &pxd));
         HG_CU(cudaMemcpyAsync(lin.k, pxd, nx * 8 / (typ == H_I ? 2 : 1), cudaMemcpyDefault, g_stream));
-        HG_CU(cudaStreamSynchronize(g_stream));
+        HG_CU(stream_sync());
         if (typ == H_I) {
             int tmp[10];
             memcpy(tmp, lin.k, nx * 4);
@@ -1238,9 +1262,9 @@ static I join_single(V z, V x, V y, V f) {
 template <typename T>
 static I search_bucketed_t(const T* x, long long lenX, const void* py, I ytyp, long long n, long long* z, unsigned* miss) {
     T ends[2];
-    HG_CU(cudaMemcpyAsync(&ends[0], x, sizeof(T), cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaMemcpyAsync(&ends[1], x + lenX - 1, sizeof(T), cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CHECK(rb_queue(&ends[0], x, sizeof(T)));
+    HG_CHECK(rb_queue(&ends[1], x + lenX - 1, sizeof(T)));
+    HG_CU(stream_sync());
     const long long x0 = (long long)ends[0], xl = (long long)ends[1];
     const unsigned long long range = (unsigned long long)xl - (unsigned long long)x0;
     const bool rank = range < 8ull * (unsigned long long)lenX;  // rank table of <= 2 bytes per key
@@ -1304,8 +1328,8 @@ static I index_of(V z, V x, V y, unsigned* miss, bool force_hash = false) {
             else HG_LAUNCH("order_flags", grid_cap(lenX), 256, 0, k_order_flags<long long>, (const long long*)px, lenX, flags);
         }
         unsigned fl = 0;
-        HG_CU(cudaMemcpyAsync(&fl, flags, 4, cudaMemcpyDeviceToHost, g_stream));
-        HG_CU(cudaStreamSynchronize(g_stream));
+        HG_CHECK(rb_queue(&fl, flags, 4));
+        HG_CU(stream_sync());
         if ((fl & 3) != 3) {  // monotone or constant: searchOrdered
             // The reference reads y through x's element type (vI(y,i) / vL(y,i),
             // h_system.cc:735-742): a y at least as wide is read as its first
@@ -1438,8 +1462,8 @@ static I index_of_list(V z, V x, V y, unsigned* miss) {
         long long init[2] = {LLONG_MAX, LLONG_MIN}, h[2];
         HG_CU(cudaMemcpyAsync(mm, init, 16, cudaMemcpyHostToDevice, g_stream));
         HG_LAUNCH("key_minmax", grid_cap(lenX), 256, 0, k_key_minmax, px, (int)xc[c].typ, lenX, mm);
-        HG_CU(cudaMemcpyAsync(h, mm, 16, cudaMemcpyDeviceToHost, g_stream));
-        HG_CU(cudaStreamSynchronize(g_stream));
+        HG_CHECK(rb_queue(h, mm, 16));
+        HG_CU(stream_sync());
         const unsigned long long span = (unsigned long long)h[1] - (unsigned long long)h[0];
         const int bits = span == 0 ? 0 : 64 - __builtin_clzll(span);
         xs.col[c] = px; ys.col[c] = py;
@@ -1502,8 +1526,8 @@ I pfnEnum(V z, V x, V y) {
     I e = lists ? index_of_list(&ind, x, y, miss) : index_of(&ind, x, y, miss);
     if (e) { out_rewind(mark); return e; }
     unsigned h = 0;
-    HG_CU(cudaMemcpyAsync(&h, miss, 4, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CHECK(rb_queue(&h, miss, 4));
+    HG_CU(stream_sync());
     if (h) { out_rewind(mark); return E_ENUM_INDEX; }
     Y hdr = (Y)halloc(sizeof(Y0));
     if (!hdr) { out_rewind(mark); return E_DEVICE_OOM; }
@@ -1515,7 +1539,7 @@ I pfnEnum(V z, V x, V y) {
         void* d = dalloc(16);
         if (!d) { out_rewind(mark); return E_DEVICE_OOM; }
         HG_CU(cudaMemcpyAsync(d, &ind.b, 8, cudaMemcpyHostToDevice, g_stream));
-        HG_CU(cudaStreamSynchronize(g_stream));
+        HG_CU(stream_sync());
         payload = (G)d;
     }
     z->typ = H_Y;
@@ -1557,7 +1581,7 @@ I pfnMember(V z, V y, V x) {
             uint64_t a = 0, b = 0;
             if (nx >= 1) HG_CU(cudaMemcpyAsync(&a, px, esize(typ), cudaMemcpyDefault, g_stream));
             if (nx >= 2) HG_CU(cudaMemcpyAsync(&b, (const char*)px + esize(typ), esize(typ), cudaMemcpyDefault, g_stream));
-            HG_CU(cudaStreamSynchronize(g_stream));
+            HG_CU(stream_sync());
             int m = (int)nx;
             if (n > 0) switch (typ) {
             case H_H: HG_LAUNCH("member_small", grid_cap(n), 256, 0, k_member_small<int16_t>, (const int16_t*)py, n, *(int16_t*)&a, *(int16_t*)&b, m, (bool*)dz); break;

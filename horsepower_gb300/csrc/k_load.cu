@@ -79,7 +79,7 @@ I stream_in(FILE* fp, void* dst, size_t bytes) {
         const size_t c = bytes - done < STAGE_BYTES ? bytes - done : STAGE_BYTES;
         HG_CU(cudaEventSynchronize(g_stage.ev[k]));  // the copy out of this buffer has finished
         if (fread(g_stage.buf[k], 1, c, fp) != c) {
-            cudaStreamSynchronize(g_stream);
+            stream_sync();
             return io_fail("fread: unexpected end of file");
         }
         HG_CU(cudaMemcpyAsync((char*)dst + done, g_stage.buf[k], c, cudaMemcpyHostToDevice, g_stream));
@@ -87,7 +87,7 @@ I stream_in(FILE* fp, void* dst, size_t bytes) {
         done += c;
         k ^= 1;
     }
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CU(stream_sync());
     return 0;
 }
 
@@ -212,7 +212,7 @@ I stream_out(FILE* fp, const void* src, size_t bytes) {
         HG_CU(cudaEventSynchronize(g_stage.ev[j & 1]));
         const size_t off = j * STAGE_BYTES, c = bytes - off < STAGE_BYTES ? bytes - off : STAGE_BYTES;
         if (fwrite(g_stage.buf[j & 1], 1, c, fp) != c) {
-            cudaStreamSynchronize(g_stream);
+            stream_sync();
             return io_fail("fwrite failed");
         }
     }
@@ -242,7 +242,7 @@ I put_words(V x, I typ, const std::vector<L>& w) {
     void* d = dalloc(w.size() * 8);
     if (!d) return E_DEVICE_OOM;
     HG_CU(cudaMemcpyAsync(d, w.data(), w.size() * 8, cudaMemcpyHostToDevice, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CU(stream_sync());
     x->g = (G)d;
     return 0;
 }
@@ -329,8 +329,8 @@ I read_node(V x, FILE* fp) {
         HG_CHECK(scan_exclusive(lens, len, offs, nullptr));
         HG_LAUNCH("text_spans", grid_of(len), 256, 0, k_text_spans, dblob, dsz, offs, len, dspans, bad);
         unsigned hb = 0;
-        HG_CU(cudaMemcpyAsync(&hb, bad, 4, cudaMemcpyDeviceToHost, g_stream));
-        HG_CU(cudaStreamSynchronize(g_stream));
+        HG_CHECK(rb_queue(&hb, bad, 4));
+        HG_CU(stream_sync());
         if (hb) return set_error(E_GENERAL, "serialized text without its NUL");
         HG_CHECK(csv_symbols(dblob, dspans, len, ids));
         x->typ = H_Q;
@@ -397,7 +397,7 @@ I host_words(V x, std::vector<L>* w) {  // an 8-byte payload as host words
         return 0;
     }
     HG_CU(cudaMemcpyAsync(w->data(), x->g, (size_t)x->len * 8, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CU(stream_sync());
     return 0;
 }
 
@@ -1241,7 +1241,7 @@ I csv_symbols(const char* dbuf, const unsigned long long* spans, long long rows,
     if (nd > 0) HG_LAUNCH("sym_pack", grid_of(nd), 256, 0, k_sym_pack, dbuf, spans, drows, nd, offs, blob, dpos);
     std::vector<unsigned long long> hoffs((size_t)nd);
     if (nd > 0) HG_CU(cudaMemcpyAsync(hoffs.data(), offs, (size_t)nd * 8, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CU(stream_sync());
     HG_CHECK(last_launch_error());
     // interning in first-occurrence order, as loadItem's getSymbol calls meet the texts
     std::vector<L> ids((size_t)nd);
@@ -1251,7 +1251,7 @@ I csv_symbols(const char* dbuf, const unsigned long long* spans, long long rows,
     if (nd > 0) HG_CU(cudaMemcpyAsync(dids, ids.data(), (size_t)nd * 8, cudaMemcpyHostToDevice, g_stream));
     HG_LAUNCH("sym_ids", grid_of(rows), 256, 0, k_sym_ids, dbuf, spans, rows, rep, dpos, dids, out, bad);
     unsigned hb = 0;
-    HG_CU(cudaMemcpyAsync(&hb, bad, 4, cudaMemcpyDeviceToHost, g_stream));
+    HG_CHECK(rb_queue(&hb, bad, 4));
     HG_CHECK(check_device_errors());
     if (hb) return set_error(E_GENERAL, "readCSV: two symbol texts share a 64-bit hash");
     return 0;
@@ -1275,7 +1275,7 @@ I csv_strings(const char* dbuf, const unsigned long long* spans, long long rows,
               (unsigned long long)(uintptr_t)blob, dptrs, bspans);
     HG_CU(cudaMemcpyAsync(blob, dblob, total, cudaMemcpyDeviceToHost, g_stream));
     HG_CU(cudaMemcpyAsync(ptrs, dptrs, (size_t)rows * 8, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CU(stream_sync());
     HG_CHECK(last_launch_error());
     if (rows > 1) register_strings(ptrs, rows, dblob, bspans);
     *ptrs_out = ptrs;
@@ -1314,8 +1314,8 @@ I read_csv(V z, S fileName, L numCols, L* types, Q* symList) {
         HG_LAUNCH("csv_nl_count", (unsigned)ntiles, NL_THREADS, 0, k_nl_count, dbuf, size, counts);
         HG_CHECK(scan_counts(counts, ntiles, toffs));
         unsigned long long h = 0;
-        HG_CU(cudaMemcpyAsync(&h, toffs + ntiles, 8, cudaMemcpyDeviceToHost, g_stream));
-        HG_CU(cudaStreamSynchronize(g_stream));
+        HG_CHECK(rb_queue(&h, toffs + ntiles, 8));
+        HG_CU(stream_sync());
         nnl = (long long)h;
         nl = (long long*)salloc((size_t)(nnl > 0 ? nnl : 1) * 8);
         if (!nl) return E_DEVICE_OOM;
@@ -1364,9 +1364,9 @@ I read_csv(V z, S fileName, L numCols, L* types, Q* symList) {
         HG_CHECK(last_launch_error());
     }
     unsigned herr[2], hslow = 0;
-    HG_CU(cudaMemcpyAsync(herr, err, 8, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaMemcpyAsync(&hslow, nslow, 4, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CHECK(rb_queue(herr, err, 8));
+    HG_CHECK(rb_queue(&hslow, nslow, 4));
+    HG_CU(stream_sync());
     if (herr[0]) {
         const long long line = (long long)herr[1] + first_line + 1;
         const char* why = (herr[0] & CSV_FIELDS)   ? "a line whose field count differs from the column count"

@@ -396,8 +396,8 @@ static I qs_run(long long n, unsigned* perm, unsigned long long* img, unsigned* 
         }
         HG_CHECK(last_launch_error());
         unsigned h = 0;
-        HG_CU(cudaMemcpyAsync(&h, act + QS_SPLIT_LEVELS - 1, 4, cudaMemcpyDeviceToHost, g_stream));
-        HG_CU(cudaStreamSynchronize(g_stream));
+        HG_CHECK(rb_queue(&h, act + QS_SPLIT_LEVELS - 1, 4));
+        HG_CU(stream_sync());
         if (h == 0) break;
     }
     return check_device_errors();
@@ -412,8 +412,8 @@ static I qs_image_of(const void* col, I typ, const unsigned* perm, long long n, 
 
 static I qs_nan_check(unsigned* nanflag) {
     unsigned h = 0;
-    HG_CU(cudaMemcpyAsync(&h, nanflag, 4, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CHECK(rb_queue(&h, nanflag, 4));
+    HG_CU(stream_sync());
     if (h) return set_error(E_NOT_IMPL, "NaN sort key: the reference's quicksort compares NaN as greater than "
                             "itself and scans outside the range");
     return 0;
@@ -483,8 +483,8 @@ I qs_sort_list(int nc, const void* const* cols, const I* typs, const B* asc, lon
         HG_LAUNCH("qs_updown", g, 256, 0, k_qs_updown, img, seg, n, up, down);
         HG_LAUNCH("qs_mode", qs_grid(ns), 256, 0, k_qs_mode, up, down, ns, desc ? 1 : 0, mode, nrev);
         unsigned hrev = 0;
-        HG_CU(cudaMemcpyAsync(&hrev, nrev, 4, cudaMemcpyDeviceToHost, g_stream));
-        HG_CU(cudaStreamSynchronize(g_stream));
+        HG_CHECK(rb_queue(&hrev, nrev, 4));
+        HG_CU(stream_sync());
         HG_CHECK(qs_nan_check(nanflag));
         if (hrev) {
             HG_LAUNCH("qs_reverse", g, 256, 0, k_qs_reverse, perm, seg, starts, ns, n, mode, tmp);

@@ -59,7 +59,7 @@ I scan_exclusive(const unsigned* in, long long n, unsigned long long* out, unsig
               (unsigned*)(s + ntiles * 8), total, g_derr);
     HG_CHECK(last_launch_error());
     if (total_h) {
-        HG_CU(cudaMemcpyAsync(total_h, total, 8, cudaMemcpyDeviceToHost, g_stream));
+        HG_CHECK(rb_queue(total_h, total, 8));
         HG_CHECK(check_device_errors());
     }
     return 0;

@@ -91,6 +91,7 @@ __device__ __forceinline__ void seg_load16(const T* __restrict__ src, const long
 // reproduces the tile tree exactly: sizes 0-1, 2, 3-4, 5-8, 9-16, 17-32
 // (classes 0-5), 33-4096 (6) and longer (7).
 constexpr int SEG_CLASSES = 8;
+static_assert(SEG_PLAN_HDR_BYTES == (SEG_CLASSES + 2) * 8, "plan header layout");
 __device__ __forceinline__ int seg_class(long long m) {
     if (m <= 1) return 0;
     if (m > TILE_SUM) return 7;
@@ -260,9 +261,10 @@ __global__ void __launch_bounds__(256) k_seg_chunk(const T* __restrict__ src, co
                                                    long long nx, const long long* __restrict__ starts, long long ng,
                                                    long long total, const long long* __restrict__ big,
                                                    const unsigned long long* __restrict__ chunk0, long long nbig,
-                                                   A ident, A* __restrict__ part, unsigned* derr) {
+                                                   const unsigned* __restrict__ order, A ident, A* __restrict__ part,
+                                                   unsigned* derr) {
     __shared__ A ws[8];
-    const long long c = blockIdx.x;
+    const long long c = order ? (long long)order[blockIdx.x] : (long long)blockIdx.x;
     long long lo = 0, hi = nbig - 1;  // the long segment owning chunk c
     while (lo < hi) {
         long long mid = (lo + hi + 1) >> 1;
@@ -310,9 +312,135 @@ __global__ void k_scatter_big(const A* __restrict__ r, const long long* __restri
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nbig; k += (long long)gridDim.x * blockDim.x)
         out[big[k]] = r[k];
 }
-__global__ void k_u64_to_i64(const unsigned long long* __restrict__ a, long long n, long long* __restrict__ b) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        b[i] = (long long)a[i];
+// The chunk starts as i64 and, for a few long segments, the order in which
+// the chunk CTAs run.  A segment's rows are spread over the whole source
+// column, so running one segment's chunks after another's would sweep the
+// column once per segment.  Instead chunk (k, c) of long segment k (n_k
+// chunks) runs at the rank of its relative position (2c + 1) / (2 n_k), ties
+// to the lower k: the CTAs resident together then cover the same region of
+// the column in every segment, and a sector fetched for one segment is
+// still in L2 when the others reach it.  Only the schedule changes; each
+// chunk's partial lands at its own index as before.
+constexpr long long CHUNK_ORDER_MAX_SEGS = 64;
+// order[rank of chunk t] = t, for chunk t of nchunks (c0: the long segments' first chunks)
+__device__ __forceinline__ void chunk_rank(const unsigned long long* c0, long long nbig,
+                                           unsigned long long nchunks, long long t, unsigned* __restrict__ order) {
+    long long lo = 0, hi = nbig - 1;  // the long segment owning chunk t
+    while (lo < hi) {
+        long long mid = (lo + hi + 1) >> 1;
+        if ((long long)c0[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    const long long k = lo, c = t - (long long)c0[k];
+    const long long nk = (long long)((k + 1 < nbig ? c0[k + 1] : nchunks) - c0[k]);
+    long long rank = c;
+    for (long long k2 = 0; k2 < nbig; k2++) {
+        if (k2 == k) continue;
+        const long long n2 = (long long)((k2 + 1 < nbig ? c0[k2 + 1] : nchunks) - c0[k2]);
+        // chunks c2 of segment k2 placed before (k, c): (2 c2 + 1) n_k < (2c + 1) n2, or equal and k2 < k
+        const long long x = (2 * c + 1) * n2 + (k2 < k ? 1 : 0);
+        const long long q = x <= 0xffffffffll ? (long long)((unsigned)(x - 1) / (unsigned)nk) : (x - 1) / nk;
+        const long long cnt = (q + 1) / 2;
+        rank += cnt < n2 ? cnt : n2;
+    }
+    order[rank] = (unsigned)t;
+}
+__global__ void k_chunk_plan(const unsigned long long* __restrict__ c0, long long nbig, unsigned long long nchunks,
+                             long long* __restrict__ ps, unsigned* __restrict__ order) {
+    const long long n = nbig > (long long)nchunks ? nbig : (long long)nchunks;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        if (t < nbig) ps[t] = (long long)c0[t];
+        if (order && t < (long long)nchunks) chunk_rank(c0, nbig, nchunks, t, order);
+    }
+}
+
+// The whole plan of a list of at most SEG_PLAN_SMALL segments in one CTA of
+// 1024 threads (four consecutive segments each): the class counts and ids
+// of seg_classes, then the long segments in ascending order with their
+// first chunks (an exclusive scan over the threads) and the chunk order.
+// hdr = {the 8 class counts, nbig, nchunks}.
+__global__ void __launch_bounds__(1024) k_seg_plan_small(const long long* __restrict__ starts, long long ng,
+                                                         long long total, unsigned* __restrict__ cc,
+                                                         unsigned* __restrict__ ids, long long* __restrict__ big,
+                                                         unsigned long long* __restrict__ c0, long long* __restrict__ ps,
+                                                         unsigned* __restrict__ order, unsigned long long* __restrict__ hdr) {
+    __shared__ unsigned sc[SEG_CLASSES], soff[SEG_CLASSES], scur[SEG_CLASSES];
+    __shared__ unsigned wb[32];
+    __shared__ unsigned long long wc[32];
+    __shared__ unsigned long long s_nbig, s_nch;
+    __shared__ unsigned long long sc0[CHUNK_ORDER_MAX_SEGS];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    if (t < SEG_CLASSES) { sc[t] = 0; scur[t] = 0; }
+    __syncthreads();
+    int cls[4];
+    long long len[4];
+    unsigned nb = 0;
+    unsigned long long nc = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const long long g = (long long)t * 4 + k;
+        cls[k] = -1;
+        len[k] = 0;
+        if (g < ng) {
+            len[k] = ((g + 1 < ng) ? starts[g + 1] : total) - starts[g];
+            cls[k] = seg_class(len[k]);
+            atomicAdd(&sc[cls[k]], 1u);
+            if (len[k] > TILE_SUM) { nb++; nc += (unsigned long long)((len[k] + TILE_SUM - 1) / TILE_SUM); }
+        }
+    }
+    // exclusive scan of (nb, nc) over the threads
+    unsigned ib = nb;
+    unsigned long long ic = nc;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned ob = __shfl_up_sync(0xffffffffu, ib, d);
+        const unsigned long long oc = __shfl_up_sync(0xffffffffu, ic, d);
+        if (lane >= d) { ib += ob; ic += oc; }
+    }
+    if (lane == 31) { wb[w] = ib; wc[w] = ic; }
+    __syncthreads();
+    if (t == 0) {
+        unsigned ab = 0;
+        unsigned long long ac = 0;
+        for (int k = 0; k < 32; k++) {
+            const unsigned b = wb[k];
+            const unsigned long long c = wc[k];
+            wb[k] = ab; wc[k] = ac;
+            ab += b; ac += c;
+        }
+        s_nbig = ab;
+        s_nch = ac;
+        unsigned off = 0;
+        for (int c = 0; c < SEG_CLASSES; c++) {
+            soff[c] = off;
+            off += sc[c];
+            cc[c] = sc[c];
+            cc[SEG_CLASSES + c] = sc[c];
+            hdr[c] = sc[c];
+        }
+    }
+    __syncthreads();
+    unsigned pb = wb[w] + ib - nb;
+    unsigned long long pc = wc[w] + ic - nc;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (cls[k] < 0) continue;
+        const long long g = (long long)t * 4 + k;
+        ids[soff[cls[k]] + atomicAdd(&scur[cls[k]], 1u)] = (unsigned)g;
+        if (len[k] > TILE_SUM) {
+            big[pb] = g;
+            c0[pb] = pc;
+            ps[pb] = (long long)pc;
+            if (pb < CHUNK_ORDER_MAX_SEGS) sc0[pb] = pc;
+            pb++;
+            pc += (unsigned long long)((len[k] + TILE_SUM - 1) / TILE_SUM);
+        }
+    }
+    __syncthreads();
+    const long long nbig = (long long)s_nbig;
+    const unsigned long long nchunks = s_nch;
+    if (t == 0) { hdr[SEG_CLASSES] = nbig; hdr[SEG_CLASSES + 1] = nchunks; }
+    if (order && nbig > 1 && nbig <= CHUNK_ORDER_MAX_SEGS)  // first chunks from shared memory
+        for (long long q = t; q < (long long)nchunks; q += 1024) chunk_rank(sc0, nbig, nchunks, q, order);
 }
 
 static unsigned gcap(long long n, int per = 256) {
@@ -344,8 +472,8 @@ static I seg_classes(const long long* starts, long long ng, long long total, Lis
         li->cls_cnt = cc;
         // a list's segments are reduced several times (one aggregate per
         // column): read the class counts once, so empty classes are skipped
-        HG_CU(cudaMemcpyAsync(li->cls_host, cc, sizeof(li->cls_host), cudaMemcpyDeviceToHost, g_stream));
-        HG_CU(cudaStreamSynchronize(g_stream));
+        HG_CHECK(rb_queue(li->cls_host, cc, sizeof(li->cls_host)));
+        HG_CU(stream_sync());
         li->cls_known = 1;
     }
     return last_launch_error();
@@ -360,10 +488,12 @@ struct LongPlan {
     const long long* big = nullptr;
     const unsigned long long* c0 = nullptr;
     const long long* pstarts = nullptr;
+    const unsigned* order = nullptr;
 };
 static I seg_plan_long(const long long* starts, long long ng, long long total, ListInfo* li, LongPlan* pl) {
     if (li && li->planned) {
         pl->nbig = li->nbig; pl->nchunks = li->nchunks; pl->big = li->big; pl->c0 = li->chunk0; pl->pstarts = li->pstarts;
+        pl->order = li->corder;
         return 0;
     }
     uint8_t* f = (uint8_t*)salloc((size_t)ng);
@@ -377,14 +507,61 @@ static I seg_plan_long(const long long* starts, long long ng, long long total, L
     unsigned long long* c0s = (unsigned long long*)(li ? dalloc((size_t)(nbig > 0 ? nbig : 1) * 8) : salloc((size_t)(nbig > 0 ? nbig : 1) * 8));
     long long* ps = (long long*)(li ? dalloc((size_t)(nbig > 0 ? nbig : 1) * 8) : salloc((size_t)(nbig > 0 ? nbig : 1) * 8));
     if (!nch || !c0s || !ps) return E_DEVICE_OOM;
+    unsigned* order = nullptr;
     if (nbig > 0) {
         HG_LAUNCH("seg_chunks", gcap(nbig), 256, 0, k_big_chunks, starts, ng, total, bigs, nbig, nch);
         HG_CHECK(scan_exclusive(nch, nbig, c0s, &nchunks));
-        HG_LAUNCH("u64_to_i64", gcap(nbig), 256, 0, k_u64_to_i64, c0s, nbig, ps);
+        if (nbig > 1 && nbig <= CHUNK_ORDER_MAX_SEGS) {
+            order = (unsigned*)(li ? dalloc((size_t)nchunks * 4) : salloc((size_t)nchunks * 4));
+            if (!order) return E_DEVICE_OOM;
+        }
+        const long long nt = nbig > (long long)nchunks ? nbig : (long long)nchunks;
+        HG_LAUNCH("chunk_plan", gcap(nt), 256, 0, k_chunk_plan, c0s, nbig, nchunks, ps, order);
     }
-    pl->nbig = nbig; pl->nchunks = nchunks; pl->big = bigs; pl->c0 = c0s; pl->pstarts = ps;
-    if (li) { li->planned = 1; li->nbig = nbig; li->nchunks = nchunks; li->big = bigs; li->chunk0 = c0s; li->pstarts = ps; }
+    pl->nbig = nbig; pl->nchunks = nchunks; pl->big = bigs; pl->c0 = c0s; pl->pstarts = ps; pl->order = order;
+    if (li) {
+        li->planned = 1; li->nbig = nbig; li->nchunks = nchunks; li->big = bigs; li->chunk0 = c0s; li->pstarts = ps;
+        li->corder = order;
+    }
     return last_launch_error();
+}
+
+I seg_plan_small(const long long* starts, long long ng, long long total, SmallPlan* p) {
+    *p = SmallPlan{};
+    if (ng <= 0 || ng > SEG_PLAN_SMALL) return 0;
+    const size_t maxch = (size_t)(total / TILE_SUM) + (size_t)ng + 1;
+    p->cc = (unsigned*)dalloc(2 * SEG_CLASSES * 4);
+    p->ids = (unsigned*)dalloc((size_t)ng * 4);
+    p->big = (long long*)dalloc((size_t)ng * 8);
+    p->c0 = (unsigned long long*)dalloc((size_t)ng * 8);
+    p->ps = (long long*)dalloc((size_t)ng * 8);
+    p->order = ng > 1 ? (unsigned*)dalloc(maxch * 4) : nullptr;
+    unsigned long long* hd = (unsigned long long*)salloc(16 * 8);
+    p->hdr = (unsigned long long*)halloc(16 * 8);
+    if (p->hdr) memset(p->hdr, 0, 16 * 8);
+    if (!p->cc || !p->ids || !p->big || !p->c0 || !p->ps || (ng > 1 && !p->order) || !hd || !p->hdr) {
+        *p = SmallPlan{};
+        return E_DEVICE_OOM;
+    }
+    HG_LAUNCH("seg_plan_small", 1, 1024, 0, k_seg_plan_small, starts, ng, total, p->cc, p->ids, p->big, p->c0, p->ps,
+              p->order, hd);
+    p->hdr_dev = hd;
+    return last_launch_error();
+}
+
+void seg_plan_adopt(ListInfo& li, const SmallPlan& p) {
+    if (!p.hdr) return;
+    li.cls_ids = p.ids;
+    li.cls_cnt = p.cc;
+    for (int c = 0; c < SEG_CLASSES; c++) li.cls_host[c] = (unsigned)p.hdr[c];
+    li.cls_known = 1;
+    li.planned = 1;
+    li.nbig = (long long)p.hdr[SEG_CLASSES];
+    li.nchunks = p.hdr[SEG_CLASSES + 1];
+    li.big = p.big;
+    li.chunk0 = p.c0;
+    li.pstarts = p.ps;
+    li.corder = (li.nbig > 1 && li.nbig <= CHUNK_ORDER_MAX_SEGS) ? p.order : nullptr;
 }
 
 // Reduces every segment of (src via rows | src) into out[ng] (device).  When
@@ -419,7 +596,7 @@ static I seg_reduce(const T* src, const long long* rows, long long nx, const lon
     A* res = (A*)salloc((size_t)nbig * sizeof(A));
     if (!part || !res) return E_DEVICE_OOM;
     HG_LAUNCH("seg_chunk", (unsigned)nchunks, 256, 0, (k_seg_chunk<T, A, OP, GATHER>), src, rows, nx, starts, ng,
-              total, pl.big, pl.c0, nbig, ident, part, g_derr);
+              total, pl.big, pl.c0, nbig, pl.order, ident, part, g_derr);
     // partials of each long segment are reduced by the same procedure: at
     // most 4096 of them per segment (certain when there are at most 4096 in
     // all) in one launch straight into out, else as segments of their own
@@ -446,10 +623,10 @@ __global__ void __launch_bounds__(256) k_seg_chunk_many(SegCols cols, int ncol, 
                                                         long long nx, const long long* __restrict__ starts, long long ng,
                                                         long long total, const long long* __restrict__ big,
                                                         const unsigned long long* __restrict__ chunk0, long long nbig,
-                                                        unsigned long long nchunks, double* __restrict__ part,
-                                                        unsigned* derr) {
+                                                        unsigned long long nchunks, const unsigned* __restrict__ order,
+                                                        double* __restrict__ part, unsigned* derr) {
     __shared__ double ws[SEG_MANY][8];
-    const long long c = blockIdx.x;
+    const long long c = order ? (long long)order[blockIdx.x] : (long long)blockIdx.x;
     long long lo = 0, hi = nbig - 1;  // the long segment owning chunk c
     while (lo < hi) {
         long long mid = (lo + hi + 1) >> 1;
@@ -509,7 +686,7 @@ I seg_sum_f64_many(const double* const* srcs, int ncol, const long long* rows, l
     for (int q = 0; q < ncol; q++) sc.src[q] = srcs[q];
 #define SEG_MANY_LAUNCH(NC)                                                                                          \
     HG_LAUNCH("seg_chunk_many", (unsigned)pl.nchunks, 256, 0, k_seg_chunk_many<NC>, sc, ncol, rows, nx, starts, ng, total, \
-              pl.big, pl.c0, pl.nbig, pl.nchunks, part, g_derr)
+              pl.big, pl.c0, pl.nbig, pl.nchunks, pl.order, part, g_derr)
     if (ncol == 1) SEG_MANY_LAUNCH(1);
     else if (ncol == 2) SEG_MANY_LAUNCH(2);
     else if (ncol == 3) SEG_MANY_LAUNCH(3);
@@ -607,8 +784,8 @@ static I agg_typed(int ag, I xt, const T* src, const long long* rows, long long 
         if (!fl) return E_DEVICE_OOM;
         HG_CU(cudaMemsetAsync(fl, 0, 4, g_stream));
         if (ng > 0) HG_LAUNCH("any_empty", gcap(ng), 256, 0, k_any_empty, starts, ng, total, fl);
-        HG_CU(cudaMemcpyAsync(&h, fl, 4, cudaMemcpyDeviceToHost, g_stream));
-        HG_CU(cudaStreamSynchronize(g_stream));
+        HG_CHECK(rb_queue(&h, fl, 4));
+        HG_CU(stream_sync());
     }
     bool to_long = h && is_int(xt);
     *typ = to_long ? H_L : xt;
@@ -688,7 +865,7 @@ static I list_segments(V y, I typ, const long long** starts, long long* total, c
     V0* dn = (V0*)salloc((size_t)(ng > 0 ? ng : 1) * sizeof(V0));
     if (!dn) return E_DEVICE_OOM;
     if (ng > 0) HG_CU(cudaMemcpyAsync(dn, nodes, (size_t)ng * sizeof(V0), cudaMemcpyDefault, g_stream));
-    if (!is_device_ptr(nodes)) HG_CU(cudaStreamSynchronize(g_stream));  // pageable source: finish before returning
+    if (!is_device_ptr(nodes)) HG_CU(stream_sync());  // pageable source: finish before returning
     nodes = dn;
     unsigned* lens = (unsigned*)salloc((size_t)(ng > 0 ? ng : 1) * 4);
     unsigned long long* off = (unsigned long long*)salloc((size_t)(ng > 0 ? ng : 1) * 8);

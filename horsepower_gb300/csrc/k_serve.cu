@@ -203,8 +203,8 @@ static I build_cum(const void* col, int is64, long long n, long long max_range, 
     unsigned g = grid_for(n, 256);
     if (g > (unsigned)g_sms * 8) g = g_sms * 8;
     HG_LAUNCH("serve_minmax", g, 256, 0, k_s_minmax, col, is64, n, mm);
-    HG_CU(cudaMemcpyAsync(h, mm, 16, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CHECK(rb_queue(h, mm, 16));
+    HG_CU(stream_sync());
     const unsigned long long range = (unsigned long long)(h[1] - h[0]) + 1;
     if (range > (unsigned long long)max_range) return 0;  // too wide: admission uses the upper bound
     unsigned* hist = (unsigned*)salloc(range * 4);
@@ -263,7 +263,7 @@ static I read_i64(const V0& v, L k, L* dst) {
         return 0;
     }
     HG_CU(cudaMemcpyAsync(dst, v.g, (size_t)k * 8, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CU(stream_sync());
     return 0;
 }
 

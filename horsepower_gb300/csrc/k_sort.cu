@@ -209,8 +209,8 @@ I radix_sort(const K* keys, long long n, const K** kres, const unsigned** vres, 
     if (grid > (unsigned)g_sms * 8) grid = g_sms * 8;
     HG_LAUNCH("key_bits", grid, 256, 0, k_key_bits<K>, keys, n, red, red + 1);
     unsigned long long hb[2];
-    HG_CU(cudaMemcpyAsync(hb, red, 16, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CHECK(rb_queue(hb, red, 16));
+    HG_CU(stream_sync());
     unsigned long long vary = hb[0] ^ hb[1];
     unsigned* vid = (unsigned*)salloc((size_t)(n > 0 ? n : 1) * 4);
     if (!vid) return E_DEVICE_OOM;
@@ -540,8 +540,8 @@ static I col_minmax(const void* p, I typ, long long n, long long* mn, long long*
     HG_CU(cudaMemcpyAsync(d, init, 16, cudaMemcpyHostToDevice, g_stream));
     if (n > 0) HG_LAUNCH("minmax", gcap(n), 256, 0, k_minmax_i64, p, (int)typ, n, d, d + 1);
     long long h[2];
-    HG_CU(cudaMemcpyAsync(h, d, 16, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CHECK(rb_queue(h, d, 16));
+    HG_CU(stream_sync());
     *mn = h[0];
     *mx = h[1];
     return 0;
@@ -622,8 +622,8 @@ static I final_order(const KeySpec& s, long long n, const uint8_t* dirbit, SortR
     HG_CU(cudaMemsetAsync(any, 0, 4, g_stream));
     HG_LAUNCH("tiebreak", gcap(n), 256, 0, k_tiebreak, dirbit, n, tb, any);
     unsigned h = 0;
-    HG_CU(cudaMemcpyAsync(&h, any, 4, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CHECK(rb_queue(&h, any, 4));
+    HG_CU(stream_sync());
     const K* ks;
     if (!h) {  // no range was reversed: ties stay in row order
         HG_CHECK(radix_sort<K>(k, n, &ks, &r->perm));
@@ -727,11 +727,19 @@ static I group_finish(V z, long long* starts, long long G, long long* perm, long
                   (unsigned long long)(uintptr_t)host_nodes(&kv[1]));
         HG_CU(cudaMemcpyAsync(host_nodes(&kv[1]), stage, (size_t)G * sizeof(V0), cudaMemcpyDeviceToHost, g_stream));
     }
+    // few groups: plan the aggregations over them now, inside this call's own round trip
+    SmallPlan plan;
+    HG_CHECK(seg_plan_small(starts, G, n, &plan));
     HG_CHECK(last_launch_error());
+    if (plan.hdr) HG_CHECK(rb_queue(plan.hdr, plan.hdr_dev, SEG_PLAN_HDR_BYTES));
     HG_CHECK(check_device_errors());  // synchronises: the node array is written by the kernel
     HG_CHECK(finish_out(&kv[0], dkeys));
     register_bound(kv[0].g, kv[0].len, n);
-    if (G > 0) register_list({host_nodes(&kv[1]), G, LIST_SEGMENTS, H_L, starts, n, perm, 1, 0, 0, 0, nullptr, nullptr, nullptr});
+    if (G > 0) {
+        ListInfo li{host_nodes(&kv[1]), G, LIST_SEGMENTS, H_L, starts, n, perm, 1, 0, 0, 0, nullptr, nullptr, nullptr};
+        seg_plan_adopt(li, plan);
+        register_list(li);
+    }
     return apply_residency(z);
 }
 
@@ -893,8 +901,8 @@ static I small_group(V z, Code code_of, long long n, int* done) {
     if (grid > (unsigned)g_sms * 4) grid = g_sms * 4;
     HG_LAUNCH("trie_present", grid, 256, 0, k_trie_present<Code>, code_of, n, bitmap);
     TrieRank hr;
-    HG_CU(cudaMemcpyAsync(hr.bits, bitmap, 2048 * 4, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CHECK(rb_queue(hr.bits, bitmap, 2048 * 4));
+    HG_CU(stream_sync());
     unsigned G = 0;
     for (int i = 0; i < 2048; i++) { hr.wpre[i] = (unsigned short)G; G += (unsigned)__builtin_popcount(hr.bits[i]); }
     if (G == 0 || G > (unsigned)TS_MAXG) return 0;
@@ -1088,7 +1096,7 @@ I pfnOrderBy(V z, V x, V y) {
         if (nc > KMAXC) return set_error(E_NOT_IMPL, "order by more than %d columns", KMAXC);
         if (nc > 0) {
             HG_CU(cudaMemcpyAsync(dir, pb, nc, cudaMemcpyDefault, g_stream));
-            HG_CU(cudaStreamSynchronize(g_stream));
+            HG_CU(stream_sync());
         }
         long long n = nc ? c[0].len : 0;
         SortResult r{};

@@ -43,7 +43,7 @@ I grow(void** p, size_t old_bytes, size_t new_bytes) {
     void* q = nullptr;
     HG_CU(cudaMalloc(&q, new_bytes));
     if (*p && old_bytes) HG_CU(cudaMemcpyAsync(q, *p, old_bytes, cudaMemcpyDeviceToDevice, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CU(stream_sync());
     if (*p) cudaFree(*p);
     *p = q;
     return 0;
@@ -78,7 +78,7 @@ I sym_texts(SymTable** out) {
         }
         HG_CU(cudaMemcpyAsync(t.blob + t.blob_len, add.data(), add.size(), cudaMemcpyHostToDevice, g_stream));
         HG_CU(cudaMemcpyAsync(t.spans + t.n, sp.data(), sp.size() * 8, cudaMemcpyHostToDevice, g_stream));
-        HG_CU(cudaStreamSynchronize(g_stream));
+        HG_CU(stream_sync());
         t.blob_len += add.size();
         t.n = n;
     }
@@ -100,7 +100,7 @@ I sym_ranks(const long long** rank, L* n_out) {
         t.rank = nullptr;
         HG_CU(cudaMalloc((void**)&t.rank, r.size() * 8));
         HG_CU(cudaMemcpyAsync(t.rank, r.data(), r.size() * 8, cudaMemcpyHostToDevice, g_stream));
-        HG_CU(cudaStreamSynchronize(g_stream));
+        HG_CU(stream_sync());
         t.rank_n = n;
     }
     *rank = t.rank;
@@ -216,7 +216,7 @@ I string_spans(V x, const char** blob, const unsigned long long** spans) {
         if (host_readable(x->g)) memcpy(ptrs.data(), x->g, (size_t)n * sizeof(S));
         else {
             HG_CU(cudaMemcpyAsync(ptrs.data(), x->g, (size_t)n * sizeof(S), cudaMemcpyDeviceToHost, g_stream));
-            HG_CU(cudaStreamSynchronize(g_stream));
+            HG_CU(stream_sync());
         }
     }
     std::vector<unsigned long long> sp((size_t)n);

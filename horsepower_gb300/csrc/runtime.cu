@@ -27,11 +27,14 @@ static int g_residency = -1;  // decided at first use (residency())
 static bool g_inited = false;
 static std::mutex g_init_mu;
 static long long g_launches = 0;
+static long long g_syncs = 0;
 
 // ------------------------------------------------------------------ errors
 static thread_local char t_err[512];
 
+static void rb_drop();
 I set_error(I code, const char* fmt, ...) {
+    rb_drop();
     va_list ap;
     va_start(ap, fmt);
     vsnprintf(t_err, sizeof t_err, fmt, ap);
@@ -40,6 +43,7 @@ I set_error(I code, const char* fmt, ...) {
 }
 
 I cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+    rb_drop();
     const char* base = strrchr(file, '/');
     set_error(e == cudaErrorMemoryAllocation ? E_DEVICE_OOM : E_DEVICE, "%s failed: %s (%s:%d)", what,
               cudaGetErrorString(e), base ? base + 1 : file, line);
@@ -117,7 +121,7 @@ struct Arena {
         }
     }
     void free_chunk(Chunk& c) {
-        cudaStreamSynchronize(g_stream);  // queued work may still use the chunk
+        stream_sync();  // queued work may still use the chunk
         if (host) cudaFreeHost(c.base); else cudaFree(c.base);
     }
     long long mark() const {
@@ -219,6 +223,7 @@ I ensure_init() {
     HG_CU(cudaStreamCreateWithFlags(&g_copy_stream, cudaStreamNonBlocking));
     HG_CU(cudaMalloc((void**)&g_derr, 256));
     HG_CU(cudaMemset(g_derr, 0, 256));
+    HG_CU(rb_init());
     HG_CU(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t)g_l2_fetch));
     // HGPU_*_LIMIT_MB caps an arena's total size (0 or unset: no cap); a call
     // that needs more returns E_DEVICE_OOM
@@ -230,7 +235,7 @@ I ensure_init() {
 }
 
 I sync() {
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CU(stream_sync());
     return 0;
 }
 
@@ -380,8 +385,8 @@ I read_elem0(V x, uint64_t* bits) {
         return 0;
     }
     cudaGetLastError();
-    HG_CU(cudaMemcpyAsync(bits, x->g, es, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CHECK(rb_queue(bits, x->g, es));
+    HG_CU(stream_sync());
     return 0;
 }
 
@@ -405,8 +410,8 @@ I alloc_out(V z, I typ, L len, void** dptr) {
 
 I finish_out(V z, void* dptr) {
     if (z->len == 1 && is_basic(z->typ)) {
-        HG_CU(cudaMemcpyAsync(&z->b, dptr, esize(z->typ), cudaMemcpyDeviceToHost, g_stream));
-        HG_CU(cudaStreamSynchronize(g_stream));
+        HG_CHECK(rb_queue(&z->b, dptr, esize(z->typ)));
+        HG_CU(stream_sync());
         z->g = (G)&z->b;
     }
     return apply_residency(z);
@@ -443,7 +448,7 @@ static I to_host_rec(V z, V x, bool in_place) {
         void* h = g_host->alloc(nb);
         if (!h) return E_DEVICE_OOM;
         if (hdr.len > 0) HG_CU(cudaMemcpyAsync(h, hdr.g, (size_t)hdr.len * 8, cudaMemcpyDefault, g_stream));
-        HG_CU(cudaStreamSynchronize(g_stream));
+        HG_CU(stream_sync());
         z->g = (G)h;
         return 0;
     }
@@ -467,7 +472,7 @@ static I to_host_rec(V z, V x, bool in_place) {
     void* h = g_host->alloc(nb);
     if (!h) return E_DEVICE_OOM;
     HG_CU(cudaMemcpyAsync(h, hdr.g, nb, cudaMemcpyDefault, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CU(stream_sync());
     z->g = (G)h;
     return 0;
 }
@@ -502,11 +507,91 @@ bool known_in_range(const void* data, long long len, long long limit) {
     return false;
 }
 
+// --------------------------------------------------------------- read-back
+// Small values a call needs on the host before it returns (counts, flags,
+// the device error word) come back through one one-block kernel that copies
+// them into mapped pinned memory, launched just before the host waits: a
+// copy into pageable memory blocks by itself, and a copy operation costs
+// more than such a launch (GB300: two pageable 8-byte reads and the wait
+// 33 us per round trip, the copy kernel and the wait 18 us, the wait alone
+// 15 us).  rb_queue records a read; the next stream_sync performs every
+// recorded read and copies each value to its host destination, which must
+// stay valid until then (the callers queue right before they wait).
+struct RbList {
+    const unsigned char* src[RB_ITEMS];
+    unsigned bytes[RB_ITEMS];
+    unsigned off[RB_ITEMS];
+    int n;
+};
+static RbList g_rbl{};
+static void* g_rbdst[RB_ITEMS];
+static unsigned char* g_rbhost = nullptr;  // mapped pinned host memory
+static unsigned char* g_rbmap = nullptr;   // its device address
+static unsigned g_rbused = 0;
+
+__global__ void k_read_back(RbList l, unsigned char* dst) {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (w >= l.n) return;
+    const unsigned char* src = l.src[w];
+    const unsigned nb = l.bytes[w];
+    if ((((uintptr_t)src) & 3) == 0 && (nb & 3) == 0) {  // destinations are 16-byte aligned
+        const unsigned* s4 = (const unsigned*)src;
+        volatile unsigned* d4 = (volatile unsigned*)(dst + l.off[w]);
+        for (unsigned k = lane; k < nb / 4; k += 32) d4[k] = s4[k];
+    } else {
+        for (unsigned b = lane; b < nb; b += 32) ((volatile unsigned char*)dst)[l.off[w] + b] = src[b];
+    }
+}
+
+// an error return abandons the reads queued by the failing call
+static void rb_drop() {
+    g_rbl.n = 0;
+    g_rbused = 0;
+}
+
+cudaError_t rb_init() {
+    if (g_rbhost) return cudaSuccess;
+    cudaError_t e = cudaHostAlloc((void**)&g_rbhost, RB_BYTES, cudaHostAllocMapped | cudaHostAllocPortable);
+    if (e != cudaSuccess) return e;
+    return cudaHostGetDevicePointer((void**)&g_rbmap, g_rbhost, 0);
+}
+
+I rb_queue(void* host_dst, const void* dev, size_t bytes) {
+    const unsigned off = (g_rbused + 15u) & ~15u;
+    if (g_rbl.n == RB_ITEMS || bytes > RB_BYTES || off + bytes > RB_BYTES)
+        return set_error(E_DEVICE, "read-back: more than %d values or %u bytes queued before a wait", RB_ITEMS,
+                         RB_BYTES);
+    g_rbl.src[g_rbl.n] = (const unsigned char*)dev;
+    g_rbl.bytes[g_rbl.n] = (unsigned)bytes;
+    g_rbl.off[g_rbl.n] = off;
+    g_rbdst[g_rbl.n] = host_dst;
+    g_rbl.n++;
+    g_rbused = off + (unsigned)bytes;
+    return 0;
+}
+
+cudaError_t stream_sync() {
+    g_syncs++;
+    const int n = g_rbl.n;
+    if (n > 0) {
+        ::hg::LaunchScope ls_("read_back");
+        k_read_back<<<1, 32 * RB_ITEMS, 0, g_stream>>>(g_rbl, g_rbmap);
+    }
+    g_rbl.n = 0;
+    g_rbused = 0;
+    cudaError_t e = n > 0 ? cudaGetLastError() : cudaSuccess;
+    const cudaError_t w = cudaStreamSynchronize(g_stream);
+    if (e == cudaSuccess) e = w;
+    if (e != cudaSuccess) return e;
+    for (int i = 0; i < n; i++) memcpy(g_rbdst[i], g_rbhost + g_rbl.off[i], g_rbl.bytes[i]);
+    return cudaSuccess;
+}
+
 // ------------------------------------------------------------ device errors
 I check_device_errors() {
     unsigned h = 0;
-    HG_CU(cudaMemcpyAsync(&h, g_derr, sizeof h, cudaMemcpyDeviceToHost, g_stream));
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CHECK(rb_queue(&h, g_derr, sizeof h));
+    HG_CU(stream_sync());
     if (!h) return 0;
     HG_CU(cudaMemsetAsync(g_derr, 0, sizeof h, g_stream));
     if (h & DERR_TIMEOUT) return set_error(E_DEVICE_TIMEOUT, "a device-side wait exceeded its iteration limit");
@@ -590,7 +675,8 @@ static void prune_registries() {
     std::vector<ListInfo> keep;
     for (ListInfo& li : g_lists) {
         if (!live(li.nodes) || !live(li.starts) || !live(li.data)) continue;
-        if (li.planned && (!live(li.big) || !live(li.chunk0) || !live(li.pstarts))) li.planned = 0;
+        if (li.planned && (!live(li.big) || !live(li.chunk0) || !live(li.pstarts) || (li.corder && !live(li.corder))))
+            li.planned = 0;
         if (li.cls_ids && (!live(li.cls_ids) || !live(li.cls_cnt))) li.cls_ids = li.cls_cnt = nullptr;
         keep.push_back(li);
     }
@@ -658,7 +744,7 @@ L setHeapOffset(L cur) {
     if (cur < 0) return cur;
     // work already queued (and uploads in flight) may still use the region being released
     wait_all_pending();
-    cudaStreamSynchronize(g_stream);
+    stream_sync();
     g_out->rewind_used((size_t)((unsigned long long)cur >> 32) << 8);
     g_host->rewind_used((size_t)((unsigned long long)cur & 0xffffffffull) << 8);
     prune_registries();
@@ -774,7 +860,7 @@ I hgpuIsDevice(V x) {
 I hgpuSync(void) {
     HG_CHECK(ensure_init());
     wait_all_pending();
-    HG_CU(cudaStreamSynchronize(g_stream));
+    HG_CU(stream_sync());
     return check_device_errors();
 }
 
@@ -797,14 +883,14 @@ I hgpuProfile(I enable) {
 }
 
 I hgpuProfileReset(void) {
-    if (g_stream) cudaStreamSynchronize(g_stream);
+    if (g_stream) stream_sync();
     for (auto& r : g_recs) { g_event_pool.push_back(r.e0); g_event_pool.push_back(r.e1); }
     g_recs.clear();
     return 0;
 }
 
 I hgpuProfileRead(I cap, const char** names, double* total_ms, L* launches) {
-    if (g_stream) cudaStreamSynchronize(g_stream);
+    if (g_stream) stream_sync();
     std::vector<std::pair<const char*, std::pair<double, L>>> acc;
     for (auto& r : g_recs) {
         float ms = 0.f;
@@ -825,6 +911,7 @@ I hgpuProfileRead(I cap, const char** names, double* total_ms, L* launches) {
 }
 
 L hgpuLaunchCount(void) { return g_launches; }
+L hgpuSyncCount(void) { return g_syncs; }
 
 I hgpuSetTuning(I knob, E value) {
     switch (knob) {
@@ -835,7 +922,7 @@ I hgpuSetTuning(I knob, E value) {
     case HGPU_TUNE_L2_FETCH:
         g_l2_fetch = value <= 32 ? 32 : (value <= 64 ? 64 : 128);
         if (g_inited) {
-            HG_CU(cudaStreamSynchronize(g_stream));
+            HG_CU(stream_sync());
             HG_CU(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t)g_l2_fetch));
         }
         return 0;

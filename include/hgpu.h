@@ -356,6 +356,7 @@ I    hgpuProfileReset(void);
 /* Returns the number of distinct kernels recorded; fills names/ms/launches up to cap. */
 I    hgpuProfileRead(I cap, const char **names, double *total_ms, L *launches);
 L    hgpuLaunchCount(void);           /* kernels launched by this library since load */
+L    hgpuSyncCount(void);             /* waits of the host on the library stream since load */
 /* Event timer on the library stream */
 I    hgpuTimerStart(void);
 double hgpuTimerStop(void);

@@ -407,6 +407,45 @@ def test_group_sum_tree_order(libs):
     gpu.free_inputs()
 
 
+@pytest.mark.parametrize("shape", ["two_long", "many_long", "groups_over_4096"])
+def test_group_sum_plans(libs, shape):
+    """The long groups' chunks run in an interleaved order when there are 2
+    to 64 of them, in group order otherwise, and a grouping of at most 4096
+    groups is planned inside @group: every shape gives each group the tile
+    tree's sum of its rows, bit for bit, and hgpuGroupAggMany agrees with
+    the single calls."""
+    from horsepower_gb300 import plans as P
+    gpu, ora = libs
+    rng = np.random.default_rng(48)
+    if shape == "two_long":
+        sizes = [9_000, 300_001]
+    elif shape == "many_long":
+        sizes = list(rng.integers(4_097, 30_000, 100)) + list(rng.integers(1, 300, 200))
+    else:
+        sizes = list(rng.integers(4_097, 200_000, 10)) + list(rng.integers(1, 40, 5_000))
+    key = np.repeat(rng.permutation(len(sizes)).astype(np.int64) * 7 - 3, sizes)
+    rng.shuffle(key)
+    pay = rng.standard_normal(key.size) * 10.0 ** rng.integers(-6, 6, key.size)
+    g = gpu.call("pfnGroup", gpu.vec(key, H_L))
+    vals = gpu.call("pfnValues", g)
+    keys = gpu.to_py(gpu.call("pfnKeys", g))
+    sums = gpu.to_py(gpu.call("hgpuGroupSum", gpu.vec(pay, H_E), vals))
+    order = np.argsort(key, kind="stable")
+    bounds = np.flatnonzero(np.diff(key[order])) + 1
+    by_key = {int(key[r[0]]): r for r in np.split(order, bounds)}
+    for gi, first in enumerate(keys):
+        x = np.ascontiguousarray(pay[by_key[int(key[first])]])
+        want = ora.lib.hgoTreeSumF64(x.ctypes.data, x.size)
+        assert sums[gi].tobytes() == np.float64(want).tobytes(), (gi, x.size)
+    cols = [gpu.vec(rng.uniform(0, 1e5, key.size), H_E) for _ in range(3)]
+    pairs = [("pfnSum", cols[0]), ("pfnAvg", cols[1]), ("pfnSum", cols[2]), ("pfnLen", cols[0])]
+    many = [gpu.to_py(z) for z in P.group_agg_many(gpu, pairs, vals)]
+    single = [gpu.to_py(P.group_agg(gpu, a, x, vals)) for a, x in pairs]
+    for a, b in zip(many, single):
+        assert a.dtype == b.dtype and a.tobytes() == b.tobytes()
+    gpu.free_inputs()
+
+
 @pytest.mark.parametrize("ops", [["eq", "lt"], ["geq", "eq", "neq"], ["eq", "eq"]])
 def test_join_multi_large(libs, ops):
     """Multi-column @join_index at 1M x 3M rows with repeated keys: GPU vs oracle."""
