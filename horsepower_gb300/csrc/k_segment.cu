@@ -665,6 +665,33 @@ __global__ void __launch_bounds__(256) k_seg_chunk_many(SegCols cols, int ncol, 
     if (bad) flag_error(derr, DERR_INDEX);
 }
 
+// the chunk partials of column blockIdx.y, as k_seg_partials does for one
+struct SegOut { double* dst[SEG_MANY]; };
+__global__ void __launch_bounds__(256) k_seg_partials_many(const double* __restrict__ part,
+                                                           const long long* __restrict__ pstarts,
+                                                           const long long* __restrict__ big, long long nbig,
+                                                           long long nchunks, SegOut so) {
+    __shared__ double ws[8];
+    const long long g = blockIdx.x;
+    const double* p = part + (size_t)blockIdx.y * (size_t)nchunks;
+    const long long s = pstarts[g], e = (g + 1 < nbig) ? pstarts[g + 1] : nchunks;
+    bool bad = false;
+    double v[16];
+    seg_load16<double, false>(p, nullptr, 0, s + threadIdx.x, e, v, bad);
+    double acc = 0.0;
+#pragma unroll
+    for (int k = 0; k < 16; k++)
+        if (s + k * 256 + threadIdx.x < e) acc = __dadd_rn(acc, v[k]);
+    acc = swarp<double, OP_SUM>(acc);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const double w01 = __dadd_rn(ws[0], ws[1]), w23 = __dadd_rn(ws[2], ws[3]);
+        const double w45 = __dadd_rn(ws[4], ws[5]), w67 = __dadd_rn(ws[6], ws[7]);
+        so.dst[blockIdx.y][big[g]] = __dadd_rn(__dadd_rn(w01, w23), __dadd_rn(w45, w67));
+    }
+}
+
 // f64 sums of several columns over the segments of one grouping whose
 // segments are all longer than one tile, with at most 4096 chunks in all;
 // sums[q] receives column q's ng sums.  Returns 1 (nothing done) when the
@@ -692,9 +719,10 @@ I seg_sum_f64_many(const double* const* srcs, int ncol, const long long* rows, l
     else if (ncol == 3) SEG_MANY_LAUNCH(3);
     else SEG_MANY_LAUNCH(4);
 #undef SEG_MANY_LAUNCH
-    for (int q = 0; q < ncol; q++)
-        HG_LAUNCH("seg_partials", (unsigned)pl.nbig, 256, 0, (k_seg_partials<double, OP_SUM>), part + (size_t)q * pl.nchunks,
-                  pl.pstarts, pl.big, pl.nbig, (long long)pl.nchunks, 0.0, sums[q]);
+    SegOut so{};
+    for (int q = 0; q < ncol; q++) so.dst[q] = sums[q];
+    HG_LAUNCH("seg_partials", dim3((unsigned)pl.nbig, (unsigned)ncol), 256, 0, k_seg_partials_many, part, pl.pstarts,
+              pl.big, pl.nbig, (long long)pl.nchunks, so);
     return last_launch_error();
 }
 
