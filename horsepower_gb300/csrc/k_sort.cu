@@ -90,9 +90,17 @@ __global__ void k_bucket_base(const unsigned long long* __restrict__ hist, unsig
 // decoupled look-back over the per-digit counts of the preceding tiles,
 // stages the tile in shared memory in digit order and writes each digit's
 // run contiguously.
-template <typename K, bool FIRST>
+//
+// OUT selects what a pass writes: RS_OUT_KV the keys and u32 row ids (every
+// pass but the last), RS_OUT_KV64 the keys and the row ids as the i64
+// result (the last pass of a @group, whose boundaries are read from the
+// keys), RS_OUT_V64 the i64 row ids alone (the last pass of an @order), at
+// position n - 1 - pos when `reverse`.
+enum { RS_OUT_KV = 0, RS_OUT_KV64 = 1, RS_OUT_V64 = 2 };
+template <typename K, bool FIRST, int OUT>
 __global__ void __launch_bounds__(RS_THREADS, (sizeof(K) == 4 ? 4 : 3)) k_onesweep(const K* __restrict__ kin, const unsigned* __restrict__ vin,
-                                                         K* __restrict__ kout, unsigned* __restrict__ vout, long long n,
+                                                         K* __restrict__ kout, unsigned* __restrict__ vout,
+                                                         long long* __restrict__ vout64, int reverse, long long n,
                                                          int shift, int bits, const unsigned long long* __restrict__ bucket,
                                                          unsigned long long* status, unsigned* ticket, unsigned* derr) {
     // dynamic shared memory: the tile's keys and row ids in digit order
@@ -171,8 +179,9 @@ __global__ void __launch_bounds__(RS_THREADS, (sizeof(K) == 4 ? 4 : 3)) k_oneswe
         K kk = skey[i];
         unsigned d = (unsigned)((unsigned long long)kk >> shift) & dmask;
         unsigned long long pos = dbase[d] + (unsigned long long)(i - (int)dstart[d]);
-        kout[pos] = kk;
-        vout[pos] = sval[i];
+        if constexpr (OUT != RS_OUT_V64) kout[pos] = kk;
+        if constexpr (OUT == RS_OUT_KV) vout[pos] = sval[i];
+        else vout64[reverse ? (unsigned long long)(n - 1) - pos : pos] = (long long)sval[i];
     }
 }
 
@@ -196,22 +205,57 @@ __global__ void k_iota(unsigned* v, long long n) {
         v[i] = (unsigned)i;
 }
 
+__global__ void k_widen(const unsigned* __restrict__ v, long long n, long long* __restrict__ out, int reverse);
+
+// The digit plan of a sort over the key bits `vary`: passes of `bits`
+// bits from bit lo up to bit hi.
+struct RadixPlan {
+    int lo, hi, bits, npass;
+};
+static RadixPlan radix_plan(unsigned long long vary) {
+    RadixPlan p;
+    p.lo = __builtin_ctzll(vary);
+    p.hi = 64 - __builtin_clzll(vary);
+    p.bits = g_digit_bits;
+    p.npass = (p.hi - p.lo + p.bits - 1) / p.bits;
+    if (p.npass > 8) { p.bits = 8; p.npass = (p.hi - p.lo + 7) / 8; }
+    return p;
+}
+
+// Where the last pass puts the permutation: as i64 row ids in perm64 (at
+// n - 1 - pos when `reverse`), with the sorted keys too when `keys`.
+struct RadixOut {
+    long long* perm64 = nullptr;
+    bool reverse = false;
+    bool keys = true;
+};
+
 // Stable sort of keys[0..n) (row ids travel along).  On return *kres/*vres
 // point to the sorted keys and row ids (scratch).  When no key bit varies
 // the result is the identity permutation.
+//   vary_hint: a superset of the key bits that vary, from bit 0, known to
+//              the caller (0: found with one OR/AND reduction);
+//   hist:      the digit histograms of the plan of vary_hint, already counted
+//              (k_make_keys_hist), or null;
+//   out:       the last pass writes the i64 permutation there instead of
+//              u32 row ids (*vres is then null; *kres too unless out->keys).
 template <typename K>
-I radix_sort(const K* keys, long long n, const K** kres, const unsigned** vres, const unsigned* init_vals = nullptr) {
-    unsigned long long* red = (unsigned long long*)salloc(16);
-    if (!red) return E_DEVICE_OOM;
-    unsigned long long init[2] = {0, ~0ull};
-    HG_CU(cudaMemcpyAsync(red, init, 16, cudaMemcpyHostToDevice, g_stream));
+I radix_sort_ex(const K* keys, long long n, const K** kres, const unsigned** vres, const unsigned* init_vals,
+                unsigned long long vary_hint, unsigned long long* hist_ready, const RadixOut* out) {
     unsigned grid = grid_for(n, 256);
     if (grid > (unsigned)g_sms * 8) grid = g_sms * 8;
-    HG_LAUNCH("key_bits", grid, 256, 0, k_key_bits<K>, keys, n, red, red + 1);
-    unsigned long long hb[2];
-    HG_CHECK(rb_queue(hb, red, 16));
-    HG_CU(stream_sync());
-    unsigned long long vary = hb[0] ^ hb[1];
+    unsigned long long vary = vary_hint;
+    if (!vary_hint && n > 1) {
+        unsigned long long* red = (unsigned long long*)salloc(16);
+        if (!red) return E_DEVICE_OOM;
+        unsigned long long init[2] = {0, ~0ull};
+        HG_CU(cudaMemcpyAsync(red, init, 16, cudaMemcpyHostToDevice, g_stream));
+        HG_LAUNCH("key_bits", grid, 256, 0, k_key_bits<K>, keys, n, red, red + 1);
+        unsigned long long hb[2];
+        HG_CHECK(rb_queue(hb, red, 16));
+        HG_CU(stream_sync());
+        vary = hb[0] ^ hb[1];
+    }
     unsigned* vid = (unsigned*)salloc((size_t)(n > 0 ? n : 1) * 4);
     if (!vid) return E_DEVICE_OOM;
     if (vary == 0 || n <= 1) {
@@ -222,32 +266,33 @@ I radix_sort(const K* keys, long long n, const K** kres, const unsigned** vres, 
         if (n > 0) {
             if (init_vals) HG_CU(cudaMemcpyAsync(vid, init_vals, n * 4, cudaMemcpyDeviceToDevice, g_stream));
             else HG_LAUNCH("iota", grid, 256, 0, k_iota, vid, n);
+            if (out && out->perm64)
+                HG_LAUNCH("widen", grid, 256, 0, k_widen, vid, n, out->perm64, out->reverse ? 1 : 0);
         }
         *kres = kcopy;
         *vres = vid;
         return last_launch_error();
     }
-    int lo = __builtin_ctzll(vary), hi = 64 - __builtin_clzll(vary);
-    int bits = g_digit_bits;
-    int npass = (hi - lo + bits - 1) / bits;
+    RadixPlan pl = radix_plan(vary);
     int nvar = __builtin_popcountll(vary);
-    if ((nvar + bits - 1) / bits < npass) {
+    if (!hist_ready && (nvar + pl.bits - 1) / pl.bits < pl.npass) {
         // bits that never change inside the range: squeeze them out (order
         // preserving, injective) and sort the shorter keys
         K* sq = (K*)salloc((size_t)n * sizeof(K));
         if (!sq) return E_DEVICE_OOM;
         HG_LAUNCH("squeeze_keys", grid, 256, 0, k_squeeze<K>, keys, n, vary, sq);
         keys = sq;
-        lo = 0;
-        hi = nvar;
-        npass = (nvar + bits - 1) / bits;
+        pl = radix_plan(nvar >= 64 ? ~0ull : (1ull << nvar) - 1);
     }
-    if (npass > 8) { bits = 8; npass = (hi - lo + 7) / 8; }
-    unsigned long long* hist = (unsigned long long*)salloc((size_t)npass * 256 * 8 * 2);
-    if (!hist) return E_DEVICE_OOM;
+    const int lo = pl.lo, bits = pl.bits, npass = pl.npass;
+    unsigned long long* hist = hist_ready;
+    if (!hist) {
+        hist = (unsigned long long*)salloc((size_t)npass * 256 * 8 * 2);
+        if (!hist) return E_DEVICE_OOM;
+        HG_CU(cudaMemsetAsync(hist, 0, (size_t)npass * 256 * 8, g_stream));
+        HG_LAUNCH("radix_hist", grid, 256, 0, k_radix_hist<K>, keys, n, lo, bits, npass, hist);
+    }
     unsigned long long* bucket = hist + npass * 256;
-    HG_CU(cudaMemsetAsync(hist, 0, (size_t)npass * 256 * 8, g_stream));
-    HG_LAUNCH("radix_hist", grid, 256, 0, k_radix_hist<K>, keys, n, lo, bits, npass, hist);
     HG_LAUNCH("bucket_base", npass, 256, 0, k_bucket_base, hist, bucket);
     long long ntiles = (n + RS_TILE - 1) / RS_TILE;
     K* kb[2] = {(K*)salloc(n * sizeof(K)), (K*)salloc(n * sizeof(K))};
@@ -256,25 +301,37 @@ I radix_sort(const K* keys, long long n, const K** kres, const unsigned** vres, 
     if (!kb[0] || !kb[1] || !vb[1] || !st) return E_DEVICE_OOM;
     const K* kin = keys;
     const unsigned* vin = init_vals;
-    {  // the attribute belongs to the current device's context: set it on every call (a host-side write)
-        const int dsm = (int)((size_t)RS_TILE * (sizeof(K) + 4));
-        HG_CU(cudaFuncSetAttribute(k_onesweep<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
-        HG_CU(cudaFuncSetAttribute(k_onesweep<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
-    }
+    const int dsm = (int)((size_t)RS_TILE * (sizeof(K) + 4));
     for (int p = 0; p < npass; p++) {
         HG_CU(cudaMemsetAsync(st, 0, (size_t)ntiles * 256 * 8 + 64, g_stream));
         K* ko = kb[p & 1];
         unsigned* vo = vb[p & 1];
         unsigned* ticket = (unsigned*)(st + (size_t)ntiles * 256 * 8);
-        const size_t dsm = (size_t)RS_TILE * (sizeof(K) + 4);
-        if (p == 0 && !init_vals)
-            HG_LAUNCH("onesweep", (unsigned)ntiles, RS_THREADS, dsm, (k_onesweep<K, true>), kin, vin, ko, vo, n,
-                      lo + p * bits, bits, bucket + p * 256, (unsigned long long*)st, ticket, g_derr);
-        else
-            HG_LAUNCH("onesweep", (unsigned)ntiles, RS_THREADS, dsm, (k_onesweep<K, false>), kin, vin, ko, vo, n,
-                      lo + p * bits, bits, bucket + p * 256, (unsigned long long*)st, ticket, g_derr);
+        const bool first = p == 0 && !init_vals;
+        const int mode = (p == npass - 1 && out && out->perm64) ? (out->keys ? RS_OUT_KV64 : RS_OUT_V64) : RS_OUT_KV;
+        long long* v64 = mode == RS_OUT_KV ? nullptr : out->perm64;
+        const int rev = (mode != RS_OUT_KV && out->reverse) ? 1 : 0;
+#define RS_PASS(F, M)                                                                                                \
+    do {                                                                                                             \
+        /* the attribute belongs to the current device's context: set it on every call (a host-side write) */      \
+        HG_CU(cudaFuncSetAttribute(k_onesweep<K, F, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));          \
+        HG_LAUNCH("onesweep", (unsigned)ntiles, RS_THREADS, (size_t)dsm, (k_onesweep<K, F, M>), kin, vin, ko, vo, v64, \
+                  rev, n, lo + p * bits, bits, bucket + p * 256, (unsigned long long*)st, ticket, g_derr);           \
+    } while (0)
+        if (first) {
+            if (mode == RS_OUT_KV) RS_PASS(true, RS_OUT_KV);
+            else if (mode == RS_OUT_KV64) RS_PASS(true, RS_OUT_KV64);
+            else RS_PASS(true, RS_OUT_V64);
+        } else {
+            if (mode == RS_OUT_KV) RS_PASS(false, RS_OUT_KV);
+            else if (mode == RS_OUT_KV64) RS_PASS(false, RS_OUT_KV64);
+            else RS_PASS(false, RS_OUT_V64);
+        }
+#undef RS_PASS
         kin = ko;
         vin = vo;
+        if (mode == RS_OUT_V64) kin = nullptr;
+        if (mode != RS_OUT_KV) vin = nullptr;
     }
     HG_CHECK(last_launch_error());
     *kres = kin;
@@ -282,6 +339,10 @@ I radix_sort(const K* keys, long long n, const K** kres, const unsigned** vres, 
     return 0;
 }
 
+template <typename K>
+I radix_sort(const K* keys, long long n, const K** kres, const unsigned** vres, const unsigned* init_vals = nullptr) {
+    return radix_sort_ex<K>(keys, n, kres, vres, init_vals, 0, nullptr, nullptr);
+}
 
 template I radix_sort<unsigned>(const unsigned*, long long, const unsigned**, const unsigned**, const unsigned*);
 template I radix_sort<unsigned long long>(const unsigned long long*, long long, const unsigned long long**,
@@ -325,9 +386,34 @@ __device__ __forceinline__ double fval(const void* p, int typ, long long i) {
     return typ == H_F ? (double)((const float*)p)[i] : ((const double*)p)[i];
 }
 
+__device__ __forceinline__ unsigned long long spec_key(const KeySpec& s, long long i);
 template <typename K>
 __global__ void k_make_keys(KeySpec s, long long n, K* __restrict__ out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (K)spec_key(s, i);
+}
+// k_make_keys and k_radix_hist in one pass over the columns: the keys are
+// written and the digit histograms of all npass passes counted as they are
+// made (when the varying key bits are known before the keys exist)
+template <typename K>
+__global__ void k_make_keys_hist(KeySpec s, long long n, K* __restrict__ out, int lo, int bits, int npass,
+                                 unsigned long long* __restrict__ hist) {
+    __shared__ unsigned sh[8][256];
+    for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) (&sh[0][0])[i] = 0;
+    __syncthreads();
+    const unsigned dmask = (1u << bits) - 1;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const K k = (K)spec_key(s, i);
+        out[i] = k;
+        const unsigned long long v = (unsigned long long)k;
+        for (int p = 0; p < npass; p++) atomicAdd(&sh[p][(unsigned)(v >> (lo + p * bits)) & dmask], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < npass * 256; i += blockDim.x)
+        if ((&sh[0][0])[i]) atomicAdd(&hist[i], (unsigned long long)(&sh[0][0])[i]);
+}
+__device__ __forceinline__ unsigned long long spec_key(const KeySpec& s, long long i) {
+    {
         unsigned long long key = 0;
         for (int c = 0; c < s.ncol; c++) {
             unsigned long long u;
@@ -355,7 +441,7 @@ __global__ void k_make_keys(KeySpec s, long long n, K* __restrict__ out) {
             }
             key |= u << s.shift[c < KMAXC ? c : 0];
         }
-        out[i] = (K)key;
+        return key;
     }
 }
 
@@ -509,26 +595,41 @@ struct SortResult {
     const void* keys;       // sorted keys (scratch), null for the small-char path
     int key64;
     bool key_injective;     // equal keys <=> equal rows (boundary test on keys)
+    const long long* perm64;  // the permutation as i64, written by the last pass (RadixOut), else null
 };
 
-static I sort_by_spec(const KeySpec& s, long long n, int total_bits, SortResult* r) {
-    r->key64 = total_bits > 32;
-    if (r->key64) {
-        unsigned long long* k = (unsigned long long*)salloc((size_t)(n > 0 ? n : 1) * 8);
-        if (!k) return E_DEVICE_OOM;
-        if (n > 0) HG_LAUNCH("make_keys", gcap(n), 256, 0, k_make_keys<unsigned long long>, s, n, k);
-        const unsigned long long* ks;
-        HG_CHECK(radix_sort<unsigned long long>(k, n, &ks, &r->perm));
-        r->keys = ks;
-    } else {
-        unsigned* k = (unsigned*)salloc((size_t)(n > 0 ? n : 1) * 4);
-        if (!k) return E_DEVICE_OOM;
-        if (n > 0) HG_LAUNCH("make_keys", gcap(n), 256, 0, k_make_keys<unsigned>, s, n, k);
-        const unsigned* ks;
-        HG_CHECK(radix_sort<unsigned>(k, n, &ks, &r->perm));
-        r->keys = ks;
+template <typename K>
+static I sort_keys_spec(const KeySpec& s, long long n, unsigned long long vary_hint, const RadixOut* ro,
+                        SortResult* r) {
+    K* k = (K*)salloc((size_t)(n > 0 ? n : 1) * sizeof(K));
+    if (!k) return E_DEVICE_OOM;
+    unsigned long long* hist = nullptr;
+    if (n > 1 && vary_hint) {  // the digit plan is known: count the histograms while making the keys
+        const RadixPlan pl = radix_plan(vary_hint);
+        hist = (unsigned long long*)salloc((size_t)pl.npass * 256 * 8 * 2);
+        if (!hist) return E_DEVICE_OOM;
+        HG_CU(cudaMemsetAsync(hist, 0, (size_t)pl.npass * 256 * 8, g_stream));
+        unsigned grid = grid_for(n, 256);
+        if (grid > (unsigned)g_sms * 8) grid = g_sms * 8;
+        HG_LAUNCH("make_keys", grid, 256, 0, k_make_keys_hist<K>, s, n, k, pl.lo, pl.bits, pl.npass, hist);
+    } else if (n > 0) {
+        HG_LAUNCH("make_keys", gcap(n), 256, 0, k_make_keys<K>, s, n, k);
     }
+    const K* ks;
+    HG_CHECK(radix_sort_ex<K>(k, n, &ks, &r->perm, nullptr, n > 1 ? vary_hint : 0, hist, ro));
+    r->keys = ks;
+    r->perm64 = ro ? ro->perm64 : nullptr;
     return last_launch_error();
+}
+
+// vary_hint: the key bits that can vary, when the caller knows them (0: found
+// by the sort); ro: where the permutation goes as i64 (null: u32 in r->perm)
+static I sort_by_spec(const KeySpec& s, long long n, int total_bits, SortResult* r, unsigned long long vary_hint = 0,
+                      const RadixOut* ro = nullptr) {
+    r->key64 = total_bits > 32;
+    r->perm64 = nullptr;
+    if (r->key64) return sort_keys_spec<unsigned long long>(s, n, vary_hint, ro, r);
+    return sort_keys_spec<unsigned>(s, n, vary_hint, ro, r);
 }
 
 static int bits_for(unsigned long long range) { return range == 0 ? 1 : 64 - __builtin_clzll(range); }
@@ -548,7 +649,10 @@ static I col_minmax(const void* p, I typ, long long n, long long* mn, long long*
 }
 
 // Single-column keys following the reference's radix rules (i32 / i64).
-static I sort_int_column(V x, const void* p, long long n, SortResult* r, const long long* known_mm = nullptr) {
+// With `ro` the permutation is written as i64 there (for a @group only when
+// the keys are injective, since the boundaries are then read from them).
+static I sort_int_column(V x, const void* p, long long n, SortResult* r, const long long* known_mm = nullptr,
+                         const RadixOut* ro = nullptr) {
     KeySpec s{};
     s.ncol = 1;
     s.col[0] = p;
@@ -557,7 +661,7 @@ static I sort_int_column(V x, const void* p, long long n, SortResult* r, const l
     if (x->typ == H_I) {
         s.xf[0] = XF_RAW32;
         r->key_injective = true;
-        return sort_by_spec(s, n, 32, r);
+        return sort_by_spec(s, n, 32, r, 0, ro);
     }
     // some value has (x >> 32) > 0 exactly when the maximum is >= 2^32; the
     // low 32 bits are injective when every value lies in one 2^32-wide range
@@ -567,7 +671,12 @@ static I sort_int_column(V x, const void* p, long long n, SortResult* r, const l
     const bool f = n > 0 && mx >= (1LL << 32);
     s.xf[0] = f ? XF_RAW64 : XF_LOW32;
     r->key_injective = f || n == 0 || ((unsigned long long)mx - (unsigned long long)mn) < (1ull << 32);
-    return sort_by_spec(s, n, f ? 64 : 32, r);
+    if (ro && ro->keys && !r->key_injective) ro = nullptr;
+    // non-negative values in [mn, mx] agree on every bit above the highest
+    // one in which mn and mx differ: only the bits below it can vary
+    unsigned long long hint = 0;
+    if (n > 1 && mn >= 0 && mx > mn) hint = (1ull << bits_for((unsigned long long)(mn ^ mx))) - 1;
+    return sort_by_spec(s, n, f ? 64 : 32, r, hint, ro);
 }
 
 // Key spec for the stable lexicographic order of integer / float columns
@@ -602,12 +711,18 @@ static I column_spec(int ncol, V* cols, const void** ptrs, const B* asc, long lo
     return 0;
 }
 
-static I sort_columns(int ncol, V* cols, const void** ptrs, const B* asc, long long n, SortResult* r) {
+static I sort_columns(int ncol, V* cols, const void** ptrs, const B* asc, long long n, SortResult* r,
+                      const RadixOut* ro = nullptr) {
     KeySpec s;
     int bits;
     HG_CHECK(column_spec(ncol, cols, ptrs, asc, n, &s, &bits));
     r->key_injective = true;
-    return sort_by_spec(s, n, bits, r);
+    // range-compressed integer columns: the packed key's top bit is the top
+    // column's (hi - lo), so bits 0 .. bits-1 are the ones that can vary
+    bool ranged = true;
+    for (int c = 0; c < ncol; c++) ranged = ranged && s.xf[c] == XF_RANGE;
+    const unsigned long long hint = (ranged && n > 1) ? (bits >= 64 ? ~0ull : (1ull << bits) - 1) : 0;
+    return sort_by_spec(s, n, bits, r, hint, ro);
 }
 
 // Multi-column @order with descending columns, as lib_quicksort_list does it
@@ -685,7 +800,9 @@ static I order_columns_exact(int nc, V* cols, const void** ptrs, const B* asc, l
 // Builds the @group dict from a sorted permutation.
 static I group_finish(V z, long long* starts, long long G, long long* perm, long long n);
 
-static I group_dict(V z, const SortResult& r, long long n, const ColSet* cols) {
+// perm_pre: the output-arena buffer for the i64 permutation, allocated by
+// the caller before the sort (r.perm64 is set when the sort wrote it)
+static I group_dict(V z, const SortResult& r, long long n, const ColSet* cols, long long* perm_pre = nullptr) {
     uint8_t* flags = (uint8_t*)salloc((size_t)(n > 0 ? n : 1));
     long long* starts = (long long*)salloc((size_t)(n > 0 ? n : 1) * 8);
     if (!flags || !starts) return E_DEVICE_OOM;
@@ -703,9 +820,9 @@ static I group_dict(V z, const SortResult& r, long long n, const ColSet* cols) {
         starts = keep;
     }
     // permutation as i64 (the rows of every group, concatenated)
-    long long* perm = nullptr;
-    if (n > 0) {
-        perm = (long long*)dalloc((size_t)n * 8);
+    long long* perm = r.perm64 ? (long long*)r.perm64 : perm_pre;
+    if (n > 0 && !r.perm64) {
+        if (!perm) perm = (long long*)dalloc((size_t)n * 8);
         if (!perm) return E_DEVICE_OOM;
         HG_LAUNCH("widen", gcap(n), 256, 0, k_widen, r.perm, n, perm, 0);
     }
@@ -743,10 +860,22 @@ static I group_finish(V z, long long* starts, long long G, long long* perm, long
     return apply_residency(z);
 }
 
-static I order_output(V z, const SortResult& r, long long n, bool reverse) {
-    void* d;
-    HG_CHECK(alloc_out(z, H_L, n, &d));
-    if (n > 0) HG_LAUNCH("widen", gcap(n), 256, 0, k_widen, r.perm, n, (long long*)d, reverse ? 1 : 0);
+// The @order result allocated before the sort, so that the last radix pass
+// writes it (outputs of one row stay on the ordinary path).
+static I order_prealloc(V z, long long n, bool reverse, RadixOut* ro, void** d) {
+    *d = nullptr;
+    if (n <= 1) return 0;
+    HG_CHECK(alloc_out(z, H_L, n, d));
+    ro->perm64 = (long long*)*d;
+    ro->reverse = reverse;
+    ro->keys = false;
+    return 0;
+}
+
+static I order_output(V z, const SortResult& r, long long n, bool reverse, void* d_pre = nullptr) {
+    void* d = d_pre;
+    if (!d) HG_CHECK(alloc_out(z, H_L, n, &d));
+    if (n > 0 && !r.perm64) HG_LAUNCH("widen", gcap(n), 256, 0, k_widen, r.perm, n, (long long*)d, reverse ? 1 : 0);
     HG_CHECK(last_launch_error());
     // a radix pass whose look-back gave up leaves a wrong permutation: read
     // the device error word before the result is marked as in range
@@ -972,11 +1101,16 @@ I pfnGroupBasic(V z, V x) {
                 if (done) return 0;
             }
         }
-        HG_CHECK(sort_int_column(x, p, x->len, &r, have_mm && x->typ == H_L ? mm : nullptr));
-        if (r.key_injective) return group_dict(z, r, x->len, nullptr);
+        // the permutation is allocated first, so that the last radix pass writes it
+        long long* pre = x->len > 1 ? (long long*)dalloc((size_t)x->len * 8) : nullptr;
+        if (x->len > 1 && !pre) return E_DEVICE_OOM;
+        RadixOut ro;
+        ro.perm64 = pre;
+        HG_CHECK(sort_int_column(x, p, x->len, &r, have_mm && x->typ == H_L ? mm : nullptr, pre ? &ro : nullptr));
+        if (r.key_injective) return group_dict(z, r, x->len, nullptr, pre);
         ColSet cs{};
         cs.ncol = 1; cs.col[0] = p; cs.typ[0] = x->typ;
-        return group_dict(z, r, x->len, &cs);
+        return group_dict(z, r, x->len, &cs, pre);
     }
     if (x->typ == H_G) {
         if (!list_of_basic(x)) return E_DOMAIN;
@@ -1068,8 +1202,11 @@ static I order_basic(V z, V x, V y) {
     HG_CHECK(in_ptr(x, &p));
     SortResult r{};
     if (x->typ == H_I || x->typ == H_L) {
-        HG_CHECK(sort_int_column(x, p, n, &r));
-        return order_output(z, r, n, !asc);
+        RadixOut ro;
+        void* d;
+        HG_CHECK(order_prealloc(z, n, !asc, &ro, &d));
+        HG_CHECK(sort_int_column(x, p, n, &r, nullptr, d ? &ro : nullptr));
+        return order_output(z, r, n, !asc, d);
     }
     if (x->typ == H_C) {
         if (!asc) return set_error(E_NOT_IMPL, "descending char order (the reference indexes past the range)");
@@ -1113,8 +1250,11 @@ I pfnOrderBy(V z, V x, V y) {
             if (n > 0) HG_LAUNCH("make_keys", gcap(n), 256, 0, k_make_keys<unsigned long long>, s, n, k);
             V0 tmp{};
             tmp.typ = H_L; tmp.len = n; tmp.g = (G)k;
-            HG_CHECK(sort_int_column(&tmp, k, n, &r));
-            return order_output(z, r, n, !dir[0]);
+            RadixOut ro;
+            void* d;
+            HG_CHECK(order_prealloc(z, n, !dir[0], &ro, &d));
+            HG_CHECK(sort_int_column(&tmp, k, n, &r, nullptr, d ? &ro : nullptr));
+            return order_output(z, r, n, !dir[0], d);
         }
         if (nc == 1) return order_basic(z, &c[0], y);
         V cols[KMAXC];
@@ -1136,8 +1276,14 @@ I pfnOrderBy(V z, V x, V y) {
         }
         bool all_asc = true;
         for (int i = 0; i < nc; i++) all_asc = all_asc && dir[i];
-        if (all_asc) HG_CHECK(sort_columns(nc, cols, ptrs, dir, n, &r));
-        else HG_CHECK(order_columns_exact(nc, cols, ptrs, dir, n, &r));
+        if (all_asc) {
+            RadixOut ro;
+            void* d;
+            HG_CHECK(order_prealloc(z, n, false, &ro, &d));
+            HG_CHECK(sort_columns(nc, cols, ptrs, dir, n, &r, d ? &ro : nullptr));
+            return order_output(z, r, n, false, d);
+        }
+        HG_CHECK(order_columns_exact(nc, cols, ptrs, dir, n, &r));
         return order_output(z, r, n, false);
     }
     I rc = order_basic(z, x, y);
