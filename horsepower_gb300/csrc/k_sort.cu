@@ -838,11 +838,22 @@ static I group_finish(V z, long long* starts, long long G, long long* perm, long
     HG_CHECK(alloc_out(&kv[0], H_L, G, &dkeys));
     HG_CHECK(init_list(&kv[1], H_G, G));
     if (G > 0) {
-        V0* stage = (V0*)salloc((size_t)G * sizeof(V0));
+        // the node array lives in mapped pinned host memory: a few nodes are
+        // written there by the kernel directly (no copy operation); many go
+        // through a device staging copy, since kernel stores to host memory
+        // are slow in bulk (GB300: 8.6M nodes, 276 MB, 5.0 ms against 1.1 ms
+        // for the staged kernel and the copy)
+        V0* hn = host_nodes(&kv[1]);
+        V0* dn = nullptr;
+        if (G <= SEG_PLAN_SMALL && cudaHostGetDevicePointer((void**)&dn, hn, 0) != cudaSuccess) {
+            cudaGetLastError();  // clears the failed look-up's own error
+            dn = nullptr;
+        }
+        V0* stage = dn ? dn : (V0*)salloc((size_t)G * sizeof(V0));
         if (!stage) return E_DEVICE_OOM;
         HG_LAUNCH("group_nodes", gcap(G), 256, 0, k_group_nodes, starts, G, n, perm, (long long*)dkeys, stage,
-                  (unsigned long long)(uintptr_t)host_nodes(&kv[1]));
-        HG_CU(cudaMemcpyAsync(host_nodes(&kv[1]), stage, (size_t)G * sizeof(V0), cudaMemcpyDeviceToHost, g_stream));
+                  (unsigned long long)(uintptr_t)hn);
+        if (!dn) HG_CU(cudaMemcpyAsync(hn, stage, (size_t)G * sizeof(V0), cudaMemcpyDeviceToHost, g_stream));
     }
     // few groups: plan the aggregations over them now, inside this call's own round trip
     SmallPlan plan;
