@@ -60,45 +60,57 @@ __global__ void __launch_bounds__(CT_THREADS) k_compact_count(const uint8_t* __r
 // even 2^31 rows make only 2^19 counts); out[ntiles] = total
 __global__ void __launch_bounds__(1024) k_scan_counts(const unsigned* __restrict__ in, long long n,
                                                       unsigned long long* __restrict__ out) {
-    __shared__ unsigned long long wsum[32];
+    // Rounds of 8192 counts, element k * 1024 + t of a round held by thread
+    // t, so that every load and store of a warp covers 32 consecutive
+    // counts.  The round's order is k-major: the exclusive prefix of element
+    // (k, warp, lane) = the totals of all (k', warp') before it + the warp's
+    // own inclusive scan.
+    constexpr int PER = 8;
+    __shared__ unsigned long long part[PER * 32];  // total of each (k, warp), then its exclusive prefix
+    __shared__ unsigned long long wtot[PER];
     __shared__ unsigned long long carry;
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
-    constexpr int PER = 16;  // 16384 counts per round
     for (long long c0 = 0; c0 < n; c0 += 1024 * PER) {
-        const long long b = c0 + (long long)threadIdx.x * PER;
-        unsigned v[PER];
-        unsigned long long s = 0;
-        if (b + PER <= n && (reinterpret_cast<uintptr_t>(in + b) & 15) == 0) {
-#pragma unroll
-            for (int q = 0; q < PER / 4; q++) {
-                const uint4 t = __ldg(reinterpret_cast<const uint4*>(in + b) + q);
-                v[4 * q] = t.x; v[4 * q + 1] = t.y; v[4 * q + 2] = t.z; v[4 * q + 3] = t.w;
-            }
-        } else {
-#pragma unroll
-            for (int k = 0; k < PER; k++) v[k] = b + k < n ? in[b + k] : 0u;
-        }
-#pragma unroll
-        for (int k = 0; k < PER; k++) s += v[k];
-        unsigned long long incl = warp_incl_scan64(s);
-        if (lane == 31) wsum[warp] = incl;
-        __syncthreads();
-        if (warp == 0) {
-            unsigned long long x = wsum[lane];
-            unsigned long long xi = warp_incl_scan64(x);
-            wsum[lane] = xi - x;
-        }
-        __syncthreads();
-        unsigned long long off = carry + wsum[warp] + (incl - s);
+        unsigned long long v[PER], incl[PER];
 #pragma unroll
         for (int k = 0; k < PER; k++) {
-            if (b + k < n) out[b + k] = off;
-            off += v[k];
+            const long long i = c0 + (long long)k * 1024 + threadIdx.x;
+            v[k] = i < n ? in[i] : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < PER; k++) {
+            incl[k] = warp_incl_scan64(v[k]);
+            if (lane == 31) part[k * 32 + warp] = incl[k];
         }
         __syncthreads();
-        if (threadIdx.x == 1023) carry = off;
+        // scan of the 256 (k, warp) totals in k-major order by the first 8 warps
+        unsigned long long x = 0, xi = 0;
+        if (threadIdx.x < PER * 32) {
+            x = part[threadIdx.x];
+            xi = warp_incl_scan64(x);
+            if (lane == 31) wtot[warp] = xi;
+        }
+        __syncthreads();
+        if (threadIdx.x < PER * 32) {
+            unsigned long long before = 0;
+            for (unsigned w = 0; w < warp; w++) before += wtot[w];
+            part[threadIdx.x] = before + xi - x;
+        }
+        __syncthreads();
+        const unsigned long long base = carry;
+#pragma unroll
+        for (int k = 0; k < PER; k++) {
+            const long long i = c0 + (long long)k * 1024 + threadIdx.x;
+            if (i < n) out[i] = base + part[k * 32 + warp] + incl[k] - v[k];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long t = 0;
+            for (int w = 0; w < PER; w++) t += wtot[w];
+            carry = base + t;
+        }
         __syncthreads();
     }
     if (threadIdx.x == 0) out[n] = carry;
