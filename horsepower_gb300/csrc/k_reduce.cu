@@ -610,10 +610,9 @@ I pfnLen(V z, V x) {
 //     GPU (different streams, or different host threads) race on it: issue
 //     them on one stream or serialise them.
 //   * The first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (the host-side name is only a stand-in).  Make
-//     that first call before any stream capture begins.  The address is kept
-//     for the life of the process: after cudaDeviceReset on that device it
-//     would be stale, so a device reset is not supported (the library's
+//     cudaGetSymbolAddress (the host-side name is only a stand-in).  The
+//     address is kept for the life of the process: after cudaDeviceReset on
+//     that device it would be stale, so a device reset is not supported (the library's
 //     arenas and stream do not survive one either).
 // ---------------------------------------------------------------------------
 #define HGPU_STATIC_SUM_MAX_TILES 65536LL

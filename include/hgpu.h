@@ -395,8 +395,8 @@ I    hgpuSelfTestWait(I mode, L limit);
  * makes no cudaMalloc/cudaFree and uses no arena.  n is limited to
  * 268,435,456 (E_LENGTH beyond).  Calls share the array: calls overlapping
  * on the GPU race, so issue them on one stream.  The first call on a device
- * looks up the array's address; make it before any stream capture.  A device
- * reset (cudaDeviceReset) is not supported afterwards. */
+ * looks up the array's address.  A device reset (cudaDeviceReset) is not
+ * supported afterwards. */
 I    hgpuSumF64Static(const double *x, L n, double *result, void *stream);
 
 /* ---------------- ingest: binary tables and CSV (h_io.cc) ----------------
