@@ -144,6 +144,14 @@ inline unsigned grid_for(long long n, int per_block) {
 //                  e.g. @group's row lists or each_right(@index)'s gathered vectors
 //   LIST_SCALARS : element g = the one value data[g] (each(@sum) and friends)
 enum { LIST_SEGMENTS = 0, LIST_SCALARS = 1 };
+// One 4096-element chunk of a long segment as a reduction CTA takes it: its
+// first element, its length and its index among the chunks (where its
+// partial goes), in launch order.
+struct ChunkDesc {
+    long long first;
+    unsigned len;
+    unsigned chunk;
+};
 struct ListInfo {
     const V0* nodes;          // host node array of the list
     long long ng;             // number of elements
@@ -160,7 +168,7 @@ struct ListInfo {
     const long long* big;
     const unsigned long long* chunk0;
     const long long* pstarts;
-    const unsigned* corder;   // chunk launch order (nullptr: in segment order)
+    const struct ChunkDesc* corder;  // chunk launch order (nullptr: in segment order)
     // cached segment ids by size class and the class counts (output arena)
     const unsigned* cls_ids;
     const unsigned* cls_cnt;
@@ -183,7 +191,7 @@ struct SmallPlan {
     long long* big = nullptr;
     unsigned long long* c0 = nullptr;
     long long* ps = nullptr;
-    unsigned* order = nullptr;
+    ChunkDesc* order = nullptr;
     unsigned long long* hdr = nullptr;      // host: 8 class counts, nbig, nchunks (after the wait)
     const unsigned long long* hdr_dev = nullptr;  // the same on the device, for the caller to queue
 };

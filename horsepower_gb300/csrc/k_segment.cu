@@ -255,24 +255,45 @@ __global__ void __launch_bounds__(256) k_seg_partials(const A* __restrict__ part
     }
 }
 
-// one CTA per 4096-element chunk of the long segments
-template <typename T, typename A, int OP, bool GATHER>
-__global__ void __launch_bounds__(256) k_seg_chunk(const T* __restrict__ src, const long long* __restrict__ rows,
-                                                   long long nx, const long long* __restrict__ starts, long long ng,
-                                                   long long total, const long long* __restrict__ big,
-                                                   const unsigned long long* __restrict__ chunk0, long long nbig,
-                                                   const unsigned* __restrict__ order, A ident, A* __restrict__ part,
-                                                   unsigned* derr) {
-    __shared__ A ws[8];
-    const long long c = order ? (long long)order[blockIdx.x] : (long long)blockIdx.x;
+// The chunk a reduction CTA takes: from its descriptor (one 16-byte load)
+// when the chunks run in a planned order, else chunk blockIdx.x, found
+// among the long segments by a binary search over their first chunks.
+// base = its first element, e = one past its last (at most base + 4096).
+__device__ __forceinline__ void chunk_of_block(const ChunkDesc* __restrict__ order, const long long* __restrict__ starts,
+                                               long long ng, long long total, const long long* __restrict__ big,
+                                               const unsigned long long* __restrict__ chunk0, long long nbig,
+                                               long long& c, long long& base, long long& e) {
+    if (order) {
+        const ChunkDesc d = order[blockIdx.x];
+        c = d.chunk;
+        base = d.first;
+        e = d.first + d.len;
+        return;
+    }
+    c = blockIdx.x;
     long long lo = 0, hi = nbig - 1;  // the long segment owning chunk c
     while (lo < hi) {
         long long mid = (lo + hi + 1) >> 1;
         if ((long long)chunk0[mid] <= c) lo = mid; else hi = mid - 1;
     }
     const long long g = big[lo];
-    const long long s = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total;
-    const long long base = s + (c - (long long)chunk0[lo]) * TILE_SUM;
+    const long long s = starts[g];
+    const long long se = (g + 1 < ng) ? starts[g + 1] : total;
+    base = s + (c - (long long)chunk0[lo]) * TILE_SUM;
+    e = se < base + TILE_SUM ? se : base + TILE_SUM;
+}
+
+// one CTA per 4096-element chunk of the long segments
+template <typename T, typename A, int OP, bool GATHER>
+__global__ void __launch_bounds__(256) k_seg_chunk(const T* __restrict__ src, const long long* __restrict__ rows,
+                                                   long long nx, const long long* __restrict__ starts, long long ng,
+                                                   long long total, const long long* __restrict__ big,
+                                                   const unsigned long long* __restrict__ chunk0, long long nbig,
+                                                   const ChunkDesc* __restrict__ order, A ident, A* __restrict__ part,
+                                                   unsigned* derr) {
+    __shared__ A ws[8];
+    long long c, base, e;
+    chunk_of_block(order, starts, ng, total, big, chunk0, nbig, c, base, e);
     bool bad = false;
     T v[16];
     seg_load16<T, GATHER>(src, rows, nx, base + threadIdx.x, e, v, bad);
@@ -322,9 +343,12 @@ __global__ void k_scatter_big(const A* __restrict__ r, const long long* __restri
 // still in L2 when the others reach it.  Only the schedule changes; each
 // chunk's partial lands at its own index as before.
 constexpr long long CHUNK_ORDER_MAX_SEGS = 64;
-// order[rank of chunk t] = t, for chunk t of nchunks (c0: the long segments' first chunks)
-__device__ __forceinline__ void chunk_rank(const unsigned long long* c0, long long nbig,
-                                           unsigned long long nchunks, long long t, unsigned* __restrict__ order) {
+// order[rank of chunk t] = chunk t's descriptor, for chunk t of nchunks (c0:
+// the long segments' first chunks; seg_first/seg_end(k): long segment k's
+// element range)
+template <typename SegRange>
+__device__ __forceinline__ void chunk_rank(const unsigned long long* c0, long long nbig, unsigned long long nchunks,
+                                           long long t, ChunkDesc* __restrict__ order, SegRange range) {
     long long lo = 0, hi = nbig - 1;  // the long segment owning chunk t
     while (lo < hi) {
         long long mid = (lo + hi + 1) >> 1;
@@ -342,14 +366,25 @@ __device__ __forceinline__ void chunk_rank(const unsigned long long* c0, long lo
         const long long cnt = (q + 1) / 2;
         rank += cnt < n2 ? cnt : n2;
     }
-    order[rank] = (unsigned)t;
+    long long sf, se;
+    range(k, sf, se);
+    const long long first = sf + c * TILE_SUM;
+    const long long len = se - first < TILE_SUM ? se - first : TILE_SUM;
+    order[rank] = ChunkDesc{first, (unsigned)len, (unsigned)t};
 }
 __global__ void k_chunk_plan(const unsigned long long* __restrict__ c0, long long nbig, unsigned long long nchunks,
-                             long long* __restrict__ ps, unsigned* __restrict__ order) {
+                             const long long* __restrict__ starts, long long ng, long long total,
+                             const long long* __restrict__ big, long long* __restrict__ ps,
+                             ChunkDesc* __restrict__ order) {
     const long long n = nbig > (long long)nchunks ? nbig : (long long)nchunks;
+    auto range = [&](long long k, long long& f, long long& e) {
+        const long long g = big[k];
+        f = starts[g];
+        e = (g + 1 < ng) ? starts[g + 1] : total;
+    };
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         if (t < nbig) ps[t] = (long long)c0[t];
-        if (order && t < (long long)nchunks) chunk_rank(c0, nbig, nchunks, t, order);
+        if (order && t < (long long)nchunks) chunk_rank(c0, nbig, nchunks, t, order, range);
     }
 }
 
@@ -362,12 +397,13 @@ __global__ void __launch_bounds__(1024) k_seg_plan_small(const long long* __rest
                                                          long long total, unsigned* __restrict__ cc,
                                                          unsigned* __restrict__ ids, long long* __restrict__ big,
                                                          unsigned long long* __restrict__ c0, long long* __restrict__ ps,
-                                                         unsigned* __restrict__ order, unsigned long long* __restrict__ hdr) {
+                                                         ChunkDesc* __restrict__ order, unsigned long long* __restrict__ hdr) {
     __shared__ unsigned sc[SEG_CLASSES], soff[SEG_CLASSES], scur[SEG_CLASSES];
     __shared__ unsigned wb[32];
     __shared__ unsigned long long wc[32];
     __shared__ unsigned long long s_nbig, s_nch;
     __shared__ unsigned long long sc0[CHUNK_ORDER_MAX_SEGS];
+    __shared__ long long sfirst[CHUNK_ORDER_MAX_SEGS], send[CHUNK_ORDER_MAX_SEGS];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     if (t < SEG_CLASSES) { sc[t] = 0; scur[t] = 0; }
     __syncthreads();
@@ -430,7 +466,11 @@ __global__ void __launch_bounds__(1024) k_seg_plan_small(const long long* __rest
             big[pb] = g;
             c0[pb] = pc;
             ps[pb] = (long long)pc;
-            if (pb < CHUNK_ORDER_MAX_SEGS) sc0[pb] = pc;
+            if (pb < CHUNK_ORDER_MAX_SEGS) {
+                sc0[pb] = pc;
+                sfirst[pb] = starts[g];
+                send[pb] = starts[g] + len[k];
+            }
             pb++;
             pc += (unsigned long long)((len[k] + TILE_SUM - 1) / TILE_SUM);
         }
@@ -439,8 +479,12 @@ __global__ void __launch_bounds__(1024) k_seg_plan_small(const long long* __rest
     const long long nbig = (long long)s_nbig;
     const unsigned long long nchunks = s_nch;
     if (t == 0) { hdr[SEG_CLASSES] = nbig; hdr[SEG_CLASSES + 1] = nchunks; }
-    if (order && nbig > 1 && nbig <= CHUNK_ORDER_MAX_SEGS)  // first chunks from shared memory
-        for (long long q = t; q < (long long)nchunks; q += 1024) chunk_rank(sc0, nbig, nchunks, q, order);
+    auto range = [&](long long k, long long& f, long long& e) {
+        f = sfirst[k];
+        e = send[k];
+    };
+    if (order && nbig > 1 && nbig <= CHUNK_ORDER_MAX_SEGS)  // the long segments from shared memory
+        for (long long q = t; q < (long long)nchunks; q += 1024) chunk_rank(sc0, nbig, nchunks, q, order, range);
 }
 
 static unsigned gcap(long long n, int per = 256) {
@@ -488,7 +532,7 @@ struct LongPlan {
     const long long* big = nullptr;
     const unsigned long long* c0 = nullptr;
     const long long* pstarts = nullptr;
-    const unsigned* order = nullptr;
+    const ChunkDesc* order = nullptr;
 };
 static I seg_plan_long(const long long* starts, long long ng, long long total, ListInfo* li, LongPlan* pl) {
     if (li && li->planned) {
@@ -507,16 +551,17 @@ static I seg_plan_long(const long long* starts, long long ng, long long total, L
     unsigned long long* c0s = (unsigned long long*)(li ? dalloc((size_t)(nbig > 0 ? nbig : 1) * 8) : salloc((size_t)(nbig > 0 ? nbig : 1) * 8));
     long long* ps = (long long*)(li ? dalloc((size_t)(nbig > 0 ? nbig : 1) * 8) : salloc((size_t)(nbig > 0 ? nbig : 1) * 8));
     if (!nch || !c0s || !ps) return E_DEVICE_OOM;
-    unsigned* order = nullptr;
+    ChunkDesc* order = nullptr;
     if (nbig > 0) {
         HG_LAUNCH("seg_chunks", gcap(nbig), 256, 0, k_big_chunks, starts, ng, total, bigs, nbig, nch);
         HG_CHECK(scan_exclusive(nch, nbig, c0s, &nchunks));
         if (nbig > 1 && nbig <= CHUNK_ORDER_MAX_SEGS) {
-            order = (unsigned*)(li ? dalloc((size_t)nchunks * 4) : salloc((size_t)nchunks * 4));
+            const size_t ob = (size_t)nchunks * sizeof(ChunkDesc);
+            order = (ChunkDesc*)(li ? dalloc(ob) : salloc(ob));
             if (!order) return E_DEVICE_OOM;
         }
         const long long nt = nbig > (long long)nchunks ? nbig : (long long)nchunks;
-        HG_LAUNCH("chunk_plan", gcap(nt), 256, 0, k_chunk_plan, c0s, nbig, nchunks, ps, order);
+        HG_LAUNCH("chunk_plan", gcap(nt), 256, 0, k_chunk_plan, c0s, nbig, nchunks, starts, ng, total, bigs, ps, order);
     }
     pl->nbig = nbig; pl->nchunks = nchunks; pl->big = bigs; pl->c0 = c0s; pl->pstarts = ps; pl->order = order;
     if (li) {
@@ -535,7 +580,7 @@ I seg_plan_small(const long long* starts, long long ng, long long total, SmallPl
     p->big = (long long*)dalloc((size_t)ng * 8);
     p->c0 = (unsigned long long*)dalloc((size_t)ng * 8);
     p->ps = (long long*)dalloc((size_t)ng * 8);
-    p->order = ng > 1 ? (unsigned*)dalloc(maxch * 4) : nullptr;
+    p->order = ng > 1 ? (ChunkDesc*)dalloc(maxch * sizeof(ChunkDesc)) : nullptr;
     unsigned long long* hd = (unsigned long long*)salloc(16 * 8);
     p->hdr = (unsigned long long*)halloc(16 * 8);
     if (p->hdr) memset(p->hdr, 0, 16 * 8);
@@ -623,18 +668,12 @@ __global__ void __launch_bounds__(256) k_seg_chunk_many(SegCols cols, int ncol, 
                                                         long long nx, const long long* __restrict__ starts, long long ng,
                                                         long long total, const long long* __restrict__ big,
                                                         const unsigned long long* __restrict__ chunk0, long long nbig,
-                                                        unsigned long long nchunks, const unsigned* __restrict__ order,
+                                                        unsigned long long nchunks, const ChunkDesc* __restrict__ order,
                                                         double* __restrict__ part, unsigned* derr) {
     __shared__ double ws[SEG_MANY][8];
-    const long long c = order ? (long long)order[blockIdx.x] : (long long)blockIdx.x;
-    long long lo = 0, hi = nbig - 1;  // the long segment owning chunk c
-    while (lo < hi) {
-        long long mid = (lo + hi + 1) >> 1;
-        if ((long long)chunk0[mid] <= c) lo = mid; else hi = mid - 1;
-    }
-    const long long g = big[lo];
-    const long long s = starts[g], e = (g + 1 < ng) ? starts[g + 1] : total;
-    const long long first = s + (c - (long long)chunk0[lo]) * TILE_SUM + threadIdx.x;
+    long long c, base, e;
+    chunk_of_block(order, starts, ng, total, big, chunk0, nbig, c, base, e);
+    const long long first = base + threadIdx.x;
     long long r[16];
     bool bad = false;
 #pragma unroll
