@@ -342,7 +342,14 @@ __global__ void k_scatter_big(const A* __restrict__ r, const long long* __restri
 // the column in every segment, and a sector fetched for one segment is
 // still in L2 when the others reach it.  Only the schedule changes; each
 // chunk's partial lands at its own index as before.
-constexpr long long CHUNK_ORDER_MAX_SEGS = 64;
+// Chunk orders are built for 2..CHUNK_ORDER_MAX_SEGS long segments (each
+// chunk's rank costs one step per long segment), by one CTA from shared
+// memory for the lists @group plans (at most CHUNK_ORDER_SMALL_SEGS).
+constexpr long long CHUNK_ORDER_MAX_SEGS = 2048;
+constexpr long long CHUNK_ORDER_SMALL_SEGS = 64;
+// below this many elements the values of a list fit in L2 whatever the
+// order, and the general plan builds none (it costs a launch's worth of work)
+constexpr long long CHUNK_ORDER_MIN_TOTAL = 4ll << 20;
 // order[rank of chunk t] = chunk t's descriptor, for chunk t of nchunks (c0:
 // the long segments' first chunks; seg_first/seg_end(k): long segment k's
 // element range)
@@ -372,19 +379,48 @@ __device__ __forceinline__ void chunk_rank(const unsigned long long* c0, long lo
     const long long len = se - first < TILE_SUM ? se - first : TILE_SUM;
     order[rank] = ChunkDesc{first, (unsigned)len, (unsigned)t};
 }
+// The general plan: ps = the first chunks as i64 and, with `order`, the
+// chunk order of up to CHUNK_ORDER_MAX_SEGS long segments, one warp per chunk
+// (the lanes share the walk over the other segments).
 __global__ void k_chunk_plan(const unsigned long long* __restrict__ c0, long long nbig, unsigned long long nchunks,
                              const long long* __restrict__ starts, long long ng, long long total,
                              const long long* __restrict__ big, long long* __restrict__ ps,
                              ChunkDesc* __restrict__ order) {
-    const long long n = nbig > (long long)nchunks ? nbig : (long long)nchunks;
-    auto range = [&](long long k, long long& f, long long& e) {
-        const long long g = big[k];
-        f = starts[g];
-        e = (g + 1 < ng) ? starts[g + 1] : total;
-    };
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        if (t < nbig) ps[t] = (long long)c0[t];
-        if (order && t < (long long)nchunks) chunk_rank(c0, nbig, nchunks, t, order, range);
+    extern __shared__ unsigned long long sc0[];  // the first chunks, when there is an order to build
+    const long long nth = (long long)gridDim.x * blockDim.x;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nbig; t += nth) ps[t] = (long long)c0[t];
+    if (!order) return;
+    for (long long k = threadIdx.x; k < nbig; k += blockDim.x) sc0[k] = c0[k];
+    __syncthreads();
+    const unsigned lane = lane_id();
+    const long long nwarps = nth >> 5;
+    for (long long t = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; t < (long long)nchunks; t += nwarps) {
+        long long lo = 0, hi = nbig - 1;  // the long segment owning chunk t
+        while (lo < hi) {
+            const long long mid = (lo + hi + 1) >> 1;
+            if ((long long)sc0[mid] <= t) lo = mid; else hi = mid - 1;
+        }
+        const long long k = lo, c = t - (long long)sc0[k];
+        const long long nk = (long long)((k + 1 < nbig ? sc0[k + 1] : nchunks) - sc0[k]);
+        long long part = 0;
+        for (long long k2 = lane; k2 < nbig; k2 += 32) {
+            if (k2 == k) continue;
+            const long long n2 = (long long)((k2 + 1 < nbig ? sc0[k2 + 1] : nchunks) - sc0[k2]);
+            // chunks c2 of segment k2 placed before (k, c): (2 c2 + 1) n_k < (2c + 1) n2, or equal and k2 < k
+            const long long x = (2 * c + 1) * n2 + (k2 < k ? 1 : 0);
+            const long long q = x <= 0xffffffffll ? (long long)((unsigned)(x - 1) / (unsigned)nk) : (x - 1) / nk;
+            const long long cnt = (q + 1) / 2;
+            part += cnt < n2 ? cnt : n2;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+        if (lane == 0) {
+            const long long g = big[k];
+            const long long sf = starts[g], se = (g + 1 < ng) ? starts[g + 1] : total;
+            const long long first = sf + c * TILE_SUM;
+            const long long len = se - first < TILE_SUM ? se - first : TILE_SUM;
+            order[c + part] = ChunkDesc{first, (unsigned)len, (unsigned)t};
+        }
     }
 }
 
@@ -402,8 +438,8 @@ __global__ void __launch_bounds__(1024) k_seg_plan_small(const long long* __rest
     __shared__ unsigned wb[32];
     __shared__ unsigned long long wc[32];
     __shared__ unsigned long long s_nbig, s_nch;
-    __shared__ unsigned long long sc0[CHUNK_ORDER_MAX_SEGS];
-    __shared__ long long sfirst[CHUNK_ORDER_MAX_SEGS], send[CHUNK_ORDER_MAX_SEGS];
+    __shared__ unsigned long long sc0[CHUNK_ORDER_SMALL_SEGS];
+    __shared__ long long sfirst[CHUNK_ORDER_SMALL_SEGS], send[CHUNK_ORDER_SMALL_SEGS];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     if (t < SEG_CLASSES) { sc[t] = 0; scur[t] = 0; }
     __syncthreads();
@@ -466,7 +502,7 @@ __global__ void __launch_bounds__(1024) k_seg_plan_small(const long long* __rest
             big[pb] = g;
             c0[pb] = pc;
             ps[pb] = (long long)pc;
-            if (pb < CHUNK_ORDER_MAX_SEGS) {
+            if (pb < CHUNK_ORDER_SMALL_SEGS) {
                 sc0[pb] = pc;
                 sfirst[pb] = starts[g];
                 send[pb] = starts[g] + len[k];
@@ -483,7 +519,7 @@ __global__ void __launch_bounds__(1024) k_seg_plan_small(const long long* __rest
         f = sfirst[k];
         e = send[k];
     };
-    if (order && nbig > 1 && nbig <= CHUNK_ORDER_MAX_SEGS)  // the long segments from shared memory
+    if (order && nbig > 1 && nbig <= CHUNK_ORDER_SMALL_SEGS)  // the long segments from shared memory
         for (long long q = t; q < (long long)nchunks; q += 1024) chunk_rank(sc0, nbig, nchunks, q, order, range);
 }
 
@@ -555,13 +591,16 @@ static I seg_plan_long(const long long* starts, long long ng, long long total, L
     if (nbig > 0) {
         HG_LAUNCH("seg_chunks", gcap(nbig), 256, 0, k_big_chunks, starts, ng, total, bigs, nbig, nch);
         HG_CHECK(scan_exclusive(nch, nbig, c0s, &nchunks));
-        if (nbig > 1 && nbig <= CHUNK_ORDER_MAX_SEGS) {
+        if (nbig > 1 && nbig <= CHUNK_ORDER_MAX_SEGS && total >= CHUNK_ORDER_MIN_TOTAL) {
             const size_t ob = (size_t)nchunks * sizeof(ChunkDesc);
             order = (ChunkDesc*)(li ? dalloc(ob) : salloc(ob));
             if (!order) return E_DEVICE_OOM;
         }
         const long long nt = nbig > (long long)nchunks ? nbig : (long long)nchunks;
-        HG_LAUNCH("chunk_plan", gcap(nt), 256, 0, k_chunk_plan, c0s, nbig, nchunks, starts, ng, total, bigs, ps, order);
+        const size_t csm = order ? (size_t)nbig * 8 : 0;  // at most 16 KB
+        const long long nthreads = order ? (long long)nchunks * 32 : nt;  // a warp per chunk for the order
+        HG_LAUNCH("chunk_plan", gcap(nthreads), 256, csm, k_chunk_plan, c0s, nbig, nchunks, starts, ng, total, bigs, ps,
+                  order);
     }
     pl->nbig = nbig; pl->nchunks = nchunks; pl->big = bigs; pl->c0 = c0s; pl->pstarts = ps; pl->order = order;
     if (li) {
@@ -606,7 +645,7 @@ void seg_plan_adopt(ListInfo& li, const SmallPlan& p) {
     li.big = p.big;
     li.chunk0 = p.c0;
     li.pstarts = p.ps;
-    li.corder = (li.nbig > 1 && li.nbig <= CHUNK_ORDER_MAX_SEGS) ? p.order : nullptr;
+    li.corder = (li.nbig > 1 && li.nbig <= CHUNK_ORDER_SMALL_SEGS) ? p.order : nullptr;
 }
 
 // Reduces every segment of (src via rows | src) into out[ng] (device).  When

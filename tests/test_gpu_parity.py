@@ -409,11 +409,11 @@ def test_group_sum_tree_order(libs):
 
 @pytest.mark.parametrize("shape", ["two_long", "many_long", "groups_over_4096"])
 def test_group_sum_plans(libs, shape):
-    """The long groups' chunks run in an interleaved order when there are 2
-    to 64 of them, in group order otherwise, and a grouping of at most 4096
-    groups is planned inside @group: every shape gives each group the tile
-    tree's sum of its rows, bit for bit, and hgpuGroupAggMany agrees with
-    the single calls."""
+    """The long groups' chunks run in an interleaved order (planned inside
+    @group for 2 to 64 long groups among at most 4096 groups, by the general
+    plan for up to 2048 long groups over at least 4M rows) or in group order:
+    every shape gives each group the tile tree's sum of its rows, bit for
+    bit, and hgpuGroupAggMany agrees with the single calls."""
     from horsepower_gb300 import plans as P
     gpu, ora = libs
     rng = np.random.default_rng(48)
@@ -421,8 +421,8 @@ def test_group_sum_plans(libs, shape):
         sizes = [9_000, 300_001]
     elif shape == "many_long":
         sizes = list(rng.integers(4_097, 30_000, 100)) + list(rng.integers(1, 300, 200))
-    else:
-        sizes = list(rng.integers(4_097, 200_000, 10)) + list(rng.integers(1, 40, 5_000))
+    else:  # more than 4096 groups and over 4M rows: the general plan builds the chunk order
+        sizes = list(rng.integers(400_000, 600_000, 10)) + list(rng.integers(1, 40, 5_000))
     key = np.repeat(rng.permutation(len(sizes)).astype(np.int64) * 7 - 3, sizes)
     rng.shuffle(key)
     pay = rng.standard_normal(key.size) * 10.0 ** rng.integers(-6, 6, key.size)
