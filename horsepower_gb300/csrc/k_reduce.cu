@@ -345,14 +345,42 @@ __global__ void __launch_bounds__(256) k_tile_minmax_f(const T* __restrict__ x, 
     lastnan = __reduce_max_sync(0xffffffffu, lastnan);
     const long long J = block_max_i64(lastnan);
     long long bk = 0, bp = -1;
+    if (J < 0 && lim == TILE_SUM) {
+        // a full tile without NaN (the common case): the best key in 32-bit
+        // halves, first the signed high words, then among the elements that
+        // share the best high word the low words, the later element winning
+        // ties as in the fold below
+        int hi[16];
+        unsigned lo[16];
 #pragma unroll
-    for (int k = 0; k < 16; k++) {
-        const int off = k * 256 + (int)threadIdx.x;
-        if (off < lim && off > J) {
+        for (int k = 0; k < 16; k++) {
             const long long key = fkey(v[k]);
-            if (bp < 0 || (OP == RED_MAX ? key >= bk : key <= bk)) {
-                bk = key;
-                bp = off;
+            hi[k] = (int)(key >> 32);
+            lo[k] = (unsigned)key;
+        }
+        int hb = hi[0];
+#pragma unroll
+        for (int k = 1; k < 16; k++) hb = OP == RED_MAX ? max(hb, hi[k]) : min(hb, hi[k]);
+        unsigned lb = 0;
+        int kb = -1;
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+            if (hi[k] == hb && (kb < 0 || (OP == RED_MAX ? lo[k] >= lb : lo[k] <= lb))) {
+                lb = lo[k];
+                kb = k;
+            }
+        bk = (long long)(((unsigned long long)(unsigned)hb << 32) | lb);
+        bp = kb * 256 + (int)threadIdx.x;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            const int off = k * 256 + (int)threadIdx.x;
+            if (off < lim && off > J) {
+                const long long key = fkey(v[k]);
+                if (bp < 0 || (OP == RED_MAX ? key >= bk : key <= bk)) {
+                    bk = key;
+                    bp = off;
+                }
             }
         }
     }
