@@ -259,6 +259,7 @@ struct Compiled {
     std::string sink;       // sum|min|max|count|compress|map
     int acc_typ = H_E;      // accumulator / result type
     std::vector<int> out_typ;
+    bool may_fail = false;  // some operation can flag an error (division by zero)
 };
 
 }  // namespace hg
@@ -409,6 +410,7 @@ static I compile_chain(hgpu_chain_s* c, const std::vector<int>& types, std::shar
     } else {
         return set_error(E_DOMAIN, "chain: unknown sink %s (sum|min|max|count|compress|map)", r->op.c_str());
     }
+    cm->may_fail = g.uses_div;
     Nvrtc* nv = nvrtc();
     if (!nv) return set_error(E_NOT_IMPL, "chain compilation needs libnvrtc, which could not be opened");
     nvrtcProgram_t prog;
@@ -471,8 +473,33 @@ static I run_chain(hgpu_chain_s* c, V z, V* zs_many, V* x) {
     const void** dcols = (const void**)salloc(16 + nin * sizeof(void*));
     if (!dcols) return E_DEVICE_OOM;
     if (nin) HG_CU(cudaMemcpyAsync(dcols, ptrs.data(), nin * sizeof(void*), cudaMemcpyHostToDevice, g_stream));
-    if (cm->sink == "compress" || cm->sink == "map") {
-        bool isc = cm->sink == "compress";
+    if (cm->sink == "map") {
+        // the values go straight into the outputs; with no operation that
+        // can fail there is nothing to read back, so no wait
+        V single[1] = {z};
+        V* zs = zs_many ? zs_many : single;
+        const size_t no = cm->out_typ.size();
+        if (no > 1 && !zs_many) return set_error(E_DOMAIN, "chain: map writes several outputs; use hgpuChainRunMany");
+        std::vector<void*> outs(no);
+        for (size_t k = 0; k < no; k++) HG_CHECK(alloc_out(zs[k], cm->out_typ[k], n, &outs[k]));
+        void** douts = (void**)salloc(16 + no * sizeof(void*));
+        if (!douts) return E_DEVICE_OOM;
+        HG_CU(cudaMemcpyAsync(douts, outs.data(), no * sizeof(void*), cudaMemcpyHostToDevice, g_stream));
+        long long nn = n;
+        unsigned char* nomask = nullptr;
+        void* args[] = {&dcols, &nn, &nomask, &douts, &g_derr};
+        unsigned grid = grid_for(n, 256);
+        if (grid > (unsigned)g_sms * 16) grid = g_sms * 16;
+        {
+            LaunchScope ls("chain");
+            HG_CU(cudaLaunchKernel((const void*)cm->kern, dim3(grid), dim3(256), args, 0, g_stream));
+        }
+        HG_CHECK(last_launch_error());
+        if (cm->may_fail) HG_CHECK(check_device_errors());
+        for (size_t k = 0; k < no; k++) HG_CHECK(finish_out(zs[k], outs[k]));
+        return 0;
+    }
+    if (cm->sink == "compress") {
         size_t no = cm->out_typ.size();
         std::vector<void*> outs(no);
         for (size_t k = 0; k < no; k++) {
@@ -492,15 +519,8 @@ static I run_chain(hgpu_chain_s* c, V z, V* zs_many, V* x) {
             HG_CU(cudaLaunchKernel((const void*)cm->kern, dim3(grid), dim3(256), args, 0, g_stream));
         }
         HG_CHECK(check_device_errors());
-        V single[1] = {z};
-        V* zs = zs_many ? zs_many : single;
-        if (isc && !zs_many) return set_error(E_DOMAIN, "chain: compress writes several outputs; use hgpuChainRunMany");
-        if (!isc) {
-            void* d;
-            HG_CHECK(alloc_out(zs[0], cm->out_typ[0], n, &d));
-            HG_CU(cudaMemcpyAsync(d, outs[0], (size_t)n * esize(cm->out_typ[0]), cudaMemcpyDeviceToDevice, g_stream));
-            return finish_out(zs[0], d);
-        }
+        if (!zs_many) return set_error(E_DOMAIN, "chain: compress writes several outputs; use hgpuChainRunMany");
+        V* zs = zs_many;
         long long* rows = (long long*)salloc((size_t)(n > 0 ? n : 1) * 8);
         long long cnt = 0;
         if (!rows) return E_DEVICE_OOM;
