@@ -132,6 +132,7 @@ struct Gen {
     std::vector<int> in_typ;   // input column types
     std::vector<bool> used;
     std::string err;
+    std::string vsuffix;       // appended to the input variables (v0, v1, ...) of the expressions made
 
     // returns a C++ expression; sets n->typ
     std::string expr(Node* n) {
@@ -139,7 +140,7 @@ struct Gen {
             if (n->col < 0 || n->col >= (int)in_typ.size()) { err = "input x" + std::to_string(n->col) + " not given"; return ""; }
             used[n->col] = true;
             n->typ = in_typ[n->col];
-            return "v" + std::to_string(n->col);
+            return "v" + std::to_string(n->col) + vsuffix;
         }
         if (n->op == "lit") {
             size_t c = n->lit.find(':');
@@ -388,25 +389,47 @@ static I compile_chain(hgpu_chain_s* c, const std::vector<int>& types, std::shar
     } else if (r->op == "compress" || r->op == "map") {
         if (r->kids.empty()) return set_error(E_DOMAIN, "chain: %s needs operands", r->op.c_str());
         bool isc = r->op == "compress";
-        std::string mask = isc ? g.expr(r->kids[0].get()) : "true";
-        std::vector<std::string> outs;
-        for (size_t k = isc ? 1 : 0; k < r->kids.size(); k++) {
-            outs.push_back(g.expr(r->kids[k].get()));
-            cm->out_typ.push_back(arith_rank(r->kids[k]->typ) == r->kids[k]->typ ? r->kids[k]->typ : r->kids[k]->typ);
+        // mask (compress) or values (map) are produced row by row, CH_UNROLL
+        // rows per thread and round with all their loads issued before the
+        // first store (the outputs are fresh buffers, never the inputs);
+        // compress writes the mask and the values into scratch and compacts
+        // afterwards
+        constexpr int CH_UNROLL = 4;
+        std::string body;
+        for (int u = 0; u < CH_UNROLL; u++) {
+            g.vsuffix = "_" + std::to_string(u);
+            const std::string iu = "i" + std::to_string(u);
+            const std::string mask = isc ? g.expr(r->kids[0].get()) : "";
+            std::vector<std::string> outs;
+            for (size_t k = isc ? 1 : 0; k < r->kids.size(); k++) {
+                outs.push_back(g.expr(r->kids[k].get()));
+                if (u == 0) cm->out_typ.push_back(r->kids[k]->typ);
+            }
+            body += "        if (" + iu + " < n) {\n" +
+                    (isc ? "            const bool m = " + mask + ";\n            mask[" + iu + "] = m;\n" : "");
+            for (size_t k = 0; k < outs.size(); k++)
+                body += std::string("            ") + (isc ? "if (m) " : "") + "((" + ctype(cm->out_typ[k]) + "*)outs[" +
+                        std::to_string(k) + "])[" + iu + "] = " + outs[k] + ";\n";
+            body += "        }\n";
         }
+        g.vsuffix.clear();
         if (!g.err.empty()) return set_error(E_DOMAIN, "chain: %s", g.err.c_str());
         if (isc && r->kids[0]->typ != H_B) return set_error(E_DOMAIN, "chain: compress mask must be bool");
-        gen_loads();
-        // mask (compress) or values (map) are produced row by row; compress
-        // writes the mask and the values into scratch and compacts afterwards
+        std::string ld;
+        for (int u = 0; u < CH_UNROLL; u++) {
+            const std::string iu = "i" + std::to_string(u);
+            ld += "        const long long " + iu + " = i + " + std::to_string(u) + " * stride;\n";
+            for (int k = 0; k < nin; k++)
+                if (g.used[k])
+                    ld += std::string("        const ") + ctype(types[k]) + " v" + std::to_string(k) + "_" + std::to_string(u) +
+                          " = " + iu + " < n ? ((const " + ctype(types[k]) + "*)cols[" + std::to_string(k) + "])[" + iu +
+                          "] : (" + ctype(types[k]) + ")0;\n";
+        }
         src += "extern \"C\" __global__ void __launch_bounds__(256) chain_kernel(const void* const* cols, long long n, "
                "unsigned char* mask, void* const* outs, unsigned* derr) {\n    bool dz = false;\n"
-               "    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {\n" +
-               loads + "        bool m = " + mask + ";\n" + (isc ? "        mask[i] = m;\n" : "");
-        for (size_t k = 0; k < outs.size(); k++)
-            src += std::string("        ") + (isc ? "if (m) " : "") + "((" + ctype(cm->out_typ[k]) + "*)outs[" + std::to_string(k) +
-                   "])[i] = " + outs[k] + ";\n";
-        src += "    }\n    if (dz) atomicOr(derr, 4u);\n}\n";
+               "    const long long stride = (long long)gridDim.x * blockDim.x;\n"
+               "    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += " +
+               std::to_string(CH_UNROLL) + " * stride) {\n" + ld + body + "    }\n    if (dz) atomicOr(derr, 4u);\n}\n";
     } else {
         return set_error(E_DOMAIN, "chain: unknown sink %s (sum|min|max|count|compress|map)", r->op.c_str());
     }
@@ -481,6 +504,7 @@ static I run_chain(hgpu_chain_s* c, V z, V* zs_many, V* x) {
         const size_t no = cm->out_typ.size();
         if (no > 1 && !zs_many) return set_error(E_DOMAIN, "chain: map writes several outputs; use hgpuChainRunMany");
         std::vector<void*> outs(no);
+        const long long mark = out_mark();
         for (size_t k = 0; k < no; k++) HG_CHECK(alloc_out(zs[k], cm->out_typ[k], n, &outs[k]));
         void** douts = (void**)salloc(16 + no * sizeof(void*));
         if (!douts) return E_DEVICE_OOM;
@@ -495,7 +519,13 @@ static I run_chain(hgpu_chain_s* c, V z, V* zs_many, V* x) {
             HG_CU(cudaLaunchKernel((const void*)cm->kern, dim3(grid), dim3(256), args, 0, g_stream));
         }
         HG_CHECK(last_launch_error());
-        if (cm->may_fail) HG_CHECK(check_device_errors());
+        if (cm->may_fail) {  // a division by zero fails the call, as the builtin's checkZero does
+            const I e = check_device_errors();
+            if (e) {
+                out_rewind(mark);
+                return e;
+            }
+        }
         for (size_t k = 0; k < no; k++) HG_CHECK(finish_out(zs[k], outs[k]));
         return 0;
     }

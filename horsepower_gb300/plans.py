@@ -199,6 +199,18 @@ class Chain:
             raise BuiltinError("hgpuChainRun", rc, self.L.lib.hgpuLastError().decode())
         return z
 
+    def run_many(self, inputs, nout):
+        """A chain with several outputs ((compress M E1 E2 ...), (map E1 E2 ...))."""
+        import ctypes as C
+        from .abi import V0, BuiltinError
+        arr = (C.POINTER(V0) * len(inputs))(*[C.pointer(v) for v in inputs])
+        zs = [self.L.node() for _ in range(nout)]
+        zarr = (C.POINTER(V0) * nout)(*[C.pointer(z) for z in zs])
+        rc = self.L.lib.hgpuChainRunMany(self.h, zarr, arr)
+        if rc:
+            raise BuiltinError("hgpuChainRunMany", rc, self.L.lib.hgpuLastError().decode())
+        return zs
+
 
 def filter_aggregate_fused(L, t, chain=None, lo=D.WIN_LO, hi=D.WIN_HI):
     chain = chain or Chain(L, Q6_CHAIN.format(lo=lo, hi=hi))
