@@ -9,6 +9,8 @@ Knobs and their search ranges:
               32, random probes and scattered writes 64)
   join_filter where the join's presence bitmap is read: 0 through L2, 1 from
               the shared memory of a 16-CTA cluster (dense i32 keys)
+  radix_pass  how a radix pass of @group / @order finds each tile's offsets:
+              0 a decoupled look-back, 1 a counting pass and one scan
 
 No knob changes a result (stable sorts, order-preserving compaction,
 fixed-order sums), so tuning is a pure search over time: coordinate descent
@@ -23,12 +25,13 @@ import json
 import os
 import statistics
 
-TILE_ROWS, HASH_LOAD, RADIX_BITS, L2_FETCH, JOIN_FILTER = 2, 0, 1, 3, 4
+TILE_ROWS, HASH_LOAD, RADIX_BITS, L2_FETCH, JOIN_FILTER, RADIX_PASS = 2, 0, 1, 3, 4, 5
 KNOBS = {"tile_rows": (TILE_ROWS, [8, 16, 32]),
          "hash_load": (HASH_LOAD, [0.5, 0.6, 0.7, 0.8]),
          "radix_bits": (RADIX_BITS, [4, 5, 6, 7, 8]),
          "l2_fetch": (L2_FETCH, [32, 64, 128]),
-         "join_filter": (JOIN_FILTER, [0, 1])}
+         "join_filter": (JOIN_FILTER, [0, 1]),
+         "radix_pass": (RADIX_PASS, [0, 1])}
 
 
 def _bind(L):

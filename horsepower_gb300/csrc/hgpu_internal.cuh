@@ -72,6 +72,8 @@ void set_hash_load_factor(double f);
 double get_hash_load_factor();
 void set_radix_digit_bits(int b);
 int get_radix_digit_bits();
+void set_radix_pass_mode(int m);
+int get_radix_pass_mode();
 long long out_mark();                          // output-arena cursor (for undoing a failed call)
 void out_rewind(long long m);
 void* salloc(size_t bytes);                    // scratch arena

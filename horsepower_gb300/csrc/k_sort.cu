@@ -39,6 +39,12 @@ constexpr int RS_THREADS = 256, RS_ITEMS = 16, RS_TILE = RS_THREADS * RS_ITEMS;
 static int g_digit_bits = 8;  // LSD digit width, 4 - 8 bits (autotuner knob)
 void set_radix_digit_bits(int b) { g_digit_bits = b < 4 ? 4 : (b > 8 ? 8 : b); }
 int get_radix_digit_bits() { return g_digit_bits; }
+// how a pass finds each tile's offset per digit (autotuner knob): 0 a
+// decoupled look-back over the preceding tiles, 1 a counting pass over the
+// keys and one scan of the (digit, tile) counts before the scatter
+static int g_radix_pass = 0;
+void set_radix_pass_mode(int m) { g_radix_pass = m ? 1 : 0; }
+int get_radix_pass_mode() { return g_radix_pass; }
 
 template <typename K>
 __global__ void k_key_bits(const K* __restrict__ k, long long n, unsigned long long* orv, unsigned long long* andv) {
@@ -96,8 +102,12 @@ __global__ void k_bucket_base(const unsigned long long* __restrict__ hist, unsig
 // result (the last pass of a @group, whose boundaries are read from the
 // keys), RS_OUT_V64 the i64 row ids alone (the last pass of an @order), at
 // position n - 1 - pos when `reverse`.
+//
+// PRE: the offsets are counted beforehand (k_rs_count, one scan): `bucket`
+// then holds every (digit, tile)'s first position, digit-major, tile t =
+// blockIdx.x, and there is no look-back.
 enum { RS_OUT_KV = 0, RS_OUT_KV64 = 1, RS_OUT_V64 = 2 };
-template <typename K, bool FIRST, int OUT>
+template <typename K, bool FIRST, int OUT, bool PRE>
 __global__ void __launch_bounds__(RS_THREADS, (sizeof(K) == 4 ? 4 : 3)) k_onesweep(const K* __restrict__ kin, const unsigned* __restrict__ vin,
                                                          K* __restrict__ kout, unsigned* __restrict__ vout,
                                                          long long* __restrict__ vout64, int reverse, long long n,
@@ -113,7 +123,7 @@ __global__ void __launch_bounds__(RS_THREADS, (sizeof(K) == 4 ? 4 : 3)) k_oneswe
     __shared__ unsigned wscan[8];
     __shared__ long long tile_id;
     for (int i = threadIdx.x; i < 8 * 256; i += RS_THREADS) (&whist[0][0])[i] = 0;
-    if (threadIdx.x == 0) tile_id = atomicAdd(ticket, 1u);
+    if (threadIdx.x == 0) tile_id = PRE ? (long long)blockIdx.x : (long long)atomicAdd(ticket, 1u);
     __syncthreads();
     const long long t = tile_id;
     const unsigned lane = lane_id(), w = threadIdx.x >> 5;
@@ -156,9 +166,13 @@ __global__ void __launch_bounds__(RS_THREADS, (sizeof(K) == 4 ? 4 : 3)) k_oneswe
         unsigned before = 0;
         for (unsigned ww = 0; ww < w; ww++) before += wscan[ww];
         dstart[d] = before + inc - c;
-        unsigned long long excl = 0;
-        if (d <= (int)dmask) excl = chain_lookback(status + d, 256, t, 0, c, derr);
-        dbase[d] = bucket[d] + excl;
+        if constexpr (PRE) {
+            dbase[d] = d <= (int)dmask ? bucket[(size_t)d * gridDim.x + (size_t)t] : 0ull;
+        } else {
+            unsigned long long excl = 0;
+            if (d <= (int)dmask) excl = chain_lookback(status + d, 256, t, 0, c, derr);
+            dbase[d] = bucket[d] + excl;
+        }
     }
     __syncthreads();
     // place the tile in digit order in shared memory ...
@@ -179,9 +193,45 @@ __global__ void __launch_bounds__(RS_THREADS, (sizeof(K) == 4 ? 4 : 3)) k_oneswe
         K kk = skey[i];
         unsigned d = (unsigned)((unsigned long long)kk >> shift) & dmask;
         unsigned long long pos = dbase[d] + (unsigned long long)(i - (int)dstart[d]);
+        if constexpr (PRE) {  // counted offsets: a position outside the output is an error, not a store
+            if (pos >= (unsigned long long)n) {
+                flag_error(derr, DERR_INDEX);
+                continue;
+            }
+        }
         if constexpr (OUT != RS_OUT_V64) kout[pos] = kk;
         if constexpr (OUT == RS_OUT_KV) vout[pos] = sval[i];
         else vout64[reverse ? (unsigned long long)(n - 1) - pos : pos] = (long long)sval[i];
+    }
+}
+
+// The digit counts of every 4096-key tile of one pass, digit-major:
+// counts[d * ntiles + t] (per-warp histograms in shared memory)
+template <typename K>
+__global__ void __launch_bounds__(RS_THREADS) k_rs_count(const K* __restrict__ kin, long long n, int shift, int bits,
+                                                         unsigned* __restrict__ counts) {
+    __shared__ unsigned wh[8][256];
+    for (int i = threadIdx.x; i < 8 * 256; i += RS_THREADS) (&wh[0][0])[i] = 0;
+    __syncthreads();
+    const unsigned dmask = (1u << bits) - 1, w = threadIdx.x >> 5;
+    const long long base = (long long)blockIdx.x * RS_TILE + threadIdx.x;
+    K key[RS_ITEMS];
+#pragma unroll
+    for (int k = 0; k < RS_ITEMS; k++) {
+        const long long i = base + (long long)k * RS_THREADS;
+        key[k] = i < n ? kin[i] : K(0);
+    }
+#pragma unroll
+    for (int k = 0; k < RS_ITEMS; k++)
+        if (base + (long long)k * RS_THREADS < n)
+            atomicAdd(&wh[w][(unsigned)((unsigned long long)key[k] >> shift) & dmask], 1u);
+    __syncthreads();
+    const unsigned d = threadIdx.x;
+    if (d <= dmask) {
+        unsigned c = 0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) c += wh[q][d];
+        counts[(size_t)d * gridDim.x + blockIdx.x] = c;
     }
 }
 
@@ -302,8 +352,21 @@ I radix_sort_ex(const K* keys, long long n, const K** kres, const unsigned** vre
     const K* kin = keys;
     const unsigned* vin = init_vals;
     const int dsm = (int)((size_t)RS_TILE * (sizeof(K) + 4));
+    const bool counted = g_radix_pass == 1;
+    unsigned* cnts = nullptr;
+    unsigned long long* offs = nullptr;
+    if (counted) {
+        cnts = (unsigned*)salloc((size_t)ntiles * 256 * 4);
+        offs = (unsigned long long*)salloc(((size_t)ntiles * 256 + 1) * 8);
+        if (!cnts || !offs) return E_DEVICE_OOM;
+    }
     for (int p = 0; p < npass; p++) {
-        HG_CU(cudaMemsetAsync(st, 0, (size_t)ntiles * 256 * 8 + 64, g_stream));
+        if (counted) {  // the (digit, tile) offsets of this pass, from the keys it reads
+            HG_LAUNCH("radix_count", (unsigned)ntiles, RS_THREADS, 0, k_rs_count<K>, kin, n, lo + p * bits, bits, cnts);
+            HG_CHECK(scan_exclusive(cnts, (long long)ntiles << bits, offs, nullptr));
+        } else {
+            HG_CU(cudaMemsetAsync(st, 0, (size_t)ntiles * 256 * 8 + 64, g_stream));
+        }
         K* ko = kb[p & 1];
         unsigned* vo = vb[p & 1];
         unsigned* ticket = (unsigned*)(st + (size_t)ntiles * 256 * 8);
@@ -311,12 +374,17 @@ I radix_sort_ex(const K* keys, long long n, const K** kres, const unsigned** vre
         const int mode = (p == npass - 1 && out && out->perm64) ? (out->keys ? RS_OUT_KV64 : RS_OUT_V64) : RS_OUT_KV;
         long long* v64 = mode == RS_OUT_KV ? nullptr : out->perm64;
         const int rev = (mode != RS_OUT_KV && out->reverse) ? 1 : 0;
-#define RS_PASS(F, M)                                                                                                \
+#define RS_PASS1(F, M, PR, BASE)                                                                                     \
     do {                                                                                                             \
         /* the attribute belongs to the current device's context: set it on every call (a host-side write) */      \
-        HG_CU(cudaFuncSetAttribute(k_onesweep<K, F, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));          \
-        HG_LAUNCH("onesweep", (unsigned)ntiles, RS_THREADS, (size_t)dsm, (k_onesweep<K, F, M>), kin, vin, ko, vo, v64, \
-                  rev, n, lo + p * bits, bits, bucket + p * 256, (unsigned long long*)st, ticket, g_derr);           \
+        HG_CU(cudaFuncSetAttribute(k_onesweep<K, F, M, PR>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));      \
+        HG_LAUNCH("onesweep", (unsigned)ntiles, RS_THREADS, (size_t)dsm, (k_onesweep<K, F, M, PR>), kin, vin, ko, vo, \
+                  v64, rev, n, lo + p * bits, bits, BASE, (unsigned long long*)st, ticket, g_derr);                  \
+    } while (0)
+#define RS_PASS(F, M)                                            \
+    do {                                                         \
+        if (counted) RS_PASS1(F, M, true, offs);                 \
+        else RS_PASS1(F, M, false, bucket + p * 256);            \
     } while (0)
         if (first) {
             if (mode == RS_OUT_KV) RS_PASS(true, RS_OUT_KV);
@@ -328,6 +396,7 @@ I radix_sort_ex(const K* keys, long long n, const K** kres, const unsigned** vre
             else RS_PASS(false, RS_OUT_V64);
         }
 #undef RS_PASS
+#undef RS_PASS1
         kin = ko;
         vin = vo;
         if (mode == RS_OUT_V64) kin = nullptr;

@@ -73,7 +73,9 @@ def test_join_filter_in_cluster_shared_memory(L):
     assert ref[0].size > 2_000_000 and same(got, ref)
 
 
-def test_radix_bits(L):
+def test_radix_knobs(L):
+    """@order and @group give the same permutation for every digit width and
+    both ways of finding a pass's tile offsets."""
     rng = np.random.default_rng(22)
     n = 1_500_000
     key = np.minimum(rng.zipf(1.1, n), 1_000_000).astype(np.int64)
@@ -81,14 +83,20 @@ def test_radix_bits(L):
     k, s = L.vec(key, H_L), L.vec(sec, H_I)
     d = L.vec(np.array([1, 1], bool), H_B)
     T.apply(L, {"radix_bits": 8})
+    T.apply(L, {"radix_pass": 0})
     ref_o = outputs(L, lambda: L.call("pfnOrderBy", L.list([k, s]), d))
     ref_g = outputs(L, lambda: L.call("pfnGroup", k))
-    for b in (4, 5, 6, 7):
-        T.apply(L, {"radix_bits": b})
-        assert T.current(L)["radix_bits"] == b
-        assert same(outputs(L, lambda: L.call("pfnOrderBy", L.list([k, s]), d)), ref_o), b
-        assert same(outputs(L, lambda: L.call("pfnGroup", k)), ref_g), b
-    T.apply(L, {"radix_bits": 8})
+    ref_d = outputs(L, lambda: L.call("pfnOrderBy", s, L.vec(np.array([0], bool), H_B)))
+    assert np.array_equal(ref_d, np.argsort(sec, kind="stable")[::-1])  # descending = ascending reversed
+    for pm in (0, 1):
+        for b in (4, 5, 6, 7, 8):
+            T.apply(L, {"radix_bits": b, "radix_pass": pm})
+            assert T.current(L)["radix_bits"] == b and T.current(L)["radix_pass"] == pm
+            assert same(outputs(L, lambda: L.call("pfnOrderBy", L.list([k, s]), d)), ref_o), (b, pm)
+            assert same(outputs(L, lambda: L.call("pfnGroup", k)), ref_g), (b, pm)
+            # descending (the last pass writes the permutation in reverse) and a 32-bit key
+            assert same(outputs(L, lambda: L.call("pfnOrderBy", s, L.vec(np.array([0], bool), H_B))), ref_d), (b, pm)
+    T.apply(L, {"radix_bits": 8, "radix_pass": 0})
 
 
 def test_batched_tile_rows(L):
