@@ -10,7 +10,8 @@ Knobs and their search ranges:
   join_filter where the join's presence bitmap is read: 0 through L2, 1 from
               the shared memory of a 16-CTA cluster (dense i32 keys)
   radix_pass  how a radix pass of @group / @order finds each tile's offsets:
-              0 a decoupled look-back, 1 a counting pass and one scan
+              0 a decoupled look-back, 1 a counting pass and one scan, 2 the
+              counting pass for 32-bit keys only (default)
 
 No knob changes a result (stable sorts, order-preserving compaction,
 fixed-order sums), so tuning is a pure search over time: coordinate descent
@@ -31,7 +32,7 @@ KNOBS = {"tile_rows": (TILE_ROWS, [8, 16, 32]),
          "radix_bits": (RADIX_BITS, [4, 5, 6, 7, 8]),
          "l2_fetch": (L2_FETCH, [32, 64, 128]),
          "join_filter": (JOIN_FILTER, [0, 1]),
-         "radix_pass": (RADIX_PASS, [0, 1])}
+         "radix_pass": (RADIX_PASS, [0, 1, 2])}
 
 
 def _bind(L):

@@ -41,9 +41,13 @@ void set_radix_digit_bits(int b) { g_digit_bits = b < 4 ? 4 : (b > 8 ? 8 : b); }
 int get_radix_digit_bits() { return g_digit_bits; }
 // how a pass finds each tile's offset per digit (autotuner knob): 0 a
 // decoupled look-back over the preceding tiles, 1 a counting pass over the
-// keys and one scan of the (digit, tile) counts before the scatter
-static int g_radix_pass = 0;
-void set_radix_pass_mode(int m) { g_radix_pass = m ? 1 : 0; }
+// keys and one scan of the (digit, tile) counts before the scatter, 2 (the
+// default) the counting pass for 32-bit keys and the look-back for 64-bit
+// ones.  150M rows: the scatter runs 17-23% faster without the look-back;
+// the counting pass reads the keys once more, which leaves @group's 32-bit
+// keys 3% ahead (6.14 -> 5.96 ms) and @order's 64-bit keys even.
+static int g_radix_pass = 2;
+void set_radix_pass_mode(int m) { g_radix_pass = m < 0 ? 0 : (m > 2 ? 2 : m); }
 int get_radix_pass_mode() { return g_radix_pass; }
 
 template <typename K>
@@ -352,7 +356,7 @@ I radix_sort_ex(const K* keys, long long n, const K** kres, const unsigned** vre
     const K* kin = keys;
     const unsigned* vin = init_vals;
     const int dsm = (int)((size_t)RS_TILE * (sizeof(K) + 4));
-    const bool counted = g_radix_pass == 1;
+    const bool counted = g_radix_pass == 1 || (g_radix_pass == 2 && sizeof(K) == 4);
     unsigned* cnts = nullptr;
     unsigned long long* offs = nullptr;
     if (counted) {

@@ -225,7 +225,7 @@ I ensure_init() {
     HG_CU(cudaMemset(g_derr, 0, 256));
     HG_CU(rb_init());
     HG_CU(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t)g_l2_fetch));
-    // HGPU_RADIX_PASS=1 starts the process with the counted radix passes (the knob's other setting)
+    // HGPU_RADIX_PASS=0/1/2 starts the process with that radix pass mode (HGPU_TUNE_RADIX_PASS)
     if (const char* rp = getenv("HGPU_RADIX_PASS")) set_radix_pass_mode(atoi(rp));
     // HGPU_*_LIMIT_MB caps an arena's total size (0 or unset: no cap); a call
     // that needs more returns E_DEVICE_OOM
@@ -921,7 +921,7 @@ I hgpuSetTuning(I knob, E value) {
     case HGPU_TUNE_RADIX_BITS: set_radix_digit_bits((int)value); return 0;
     case HGPU_TUNE_TILE_ROWS: g_tile_rows = value <= 8 ? 8 : (value <= 16 ? 16 : 32); return 0;
     case HGPU_TUNE_JOIN_FILTER: g_join_filter = value >= 0.5 ? 1 : 0; return 0;
-    case HGPU_TUNE_RADIX_PASS: set_radix_pass_mode(value >= 0.5 ? 1 : 0); return 0;
+    case HGPU_TUNE_RADIX_PASS: set_radix_pass_mode((int)(value + 0.5)); return 0;
     case HGPU_TUNE_L2_FETCH:
         g_l2_fetch = value <= 32 ? 32 : (value <= 64 ? 64 : 128);
         if (g_inited) {

@@ -372,8 +372,9 @@ double hgpuTimerStop(void);
                                     32 suits sparse sorted gathers, 64 random probes and scatters) */
 #define HGPU_TUNE_JOIN_FILTER 4 /* @join_index presence bitmap on dense i32 keys: 0 read through L2
                                     (default), 1 held in the shared memory of a 16-CTA cluster */
-#define HGPU_TUNE_RADIX_PASS 5  /* radix pass of @group/@order: 0 tile offsets by a decoupled look-back
-                                    (default), 1 by a counting pass and one scan before the scatter */
+#define HGPU_TUNE_RADIX_PASS 5  /* radix pass of @group/@order: 0 tile offsets by a decoupled look-back,
+                                    1 by a counting pass and one scan before the scatter, 2 (default)
+                                    1 for 32-bit keys and 0 for 64-bit ones */
 I    hgpuSetTuning(I knob, E value);
 E    hgpuGetTuning(I knob);
 
