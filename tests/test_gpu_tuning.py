@@ -114,9 +114,13 @@ def test_batched_tile_rows(L):
 
 
 def test_tune_and_clamp(L):
-    T.apply(L, {"hash_load": 0.95, "radix_bits": 2, "tile_rows": 100, "l2_fetch": 1000})
+    T.apply(L, {"hash_load": 0.95, "radix_bits": 2, "tile_rows": 100, "l2_fetch": 1000, "radix_pass": 7})
     c = T.current(L)
-    assert c == {"tile_rows": 32, "hash_load": 0.8, "radix_bits": 4, "l2_fetch": 128, "join_filter": 0}
+    assert c == {"tile_rows": 32, "hash_load": 0.8, "radix_bits": 4, "l2_fetch": 128, "join_filter": 0,
+                 "radix_pass": 2}
+    T.apply(L, {"radix_pass": -3})
+    assert T.current(L)["radix_pass"] == 0
+    T.apply(L, {"radix_pass": 2})
     T.apply(L, {"l2_fetch": 10})
     assert T.current(L)["l2_fetch"] == 32
     tabs = [B.synth_tables(L, 900 + i, n, n // 4) for i, n in enumerate([20_000, 200_000])]
