@@ -16,15 +16,17 @@
 //   pfnGroupTrie            h_primitive.cc:2656-2681  counting on (c0<<8)+c1
 //
 // Any stable sort by the same key yields the same permutation, so the GPU
-// sorts only the key bits that vary (found with one OR/AND reduction) and
-// packs multi-column integer keys into one u64 after range compression.
+// sorts only the key bits that vary (found with one OR/AND reduction, or
+// known from the value range) and packs multi-column integer keys into one
+// u64 after range compression.
 //
 // Radix kernel: onesweep-style LSD (Adinets & Merrill 2022).  One histogram
 // pass gives every digit's global bucket base for all passes; each pass
 // then ranks a 4096-key tile with warp-level __match_any_sync (warps own
 // contiguous sub-ranges, so ranks are stable), resolves per-digit tile
-// offsets with a decoupled look-back (one thread per digit, bounded spin),
-// and scatters keys and row ids.
+// offsets with a decoupled look-back (one thread per digit, bounded spin) or
+// from counts taken by a separate pass and one scan, and scatters keys and
+// row ids.
 #include <cstring>
 #include <vector>
 
