@@ -72,3 +72,12 @@ def test_value_node_layout():
     from horsepower_gb300.abi import V0
     assert C.sizeof(V0) == 32
     assert V0.len.offset == 0 and V0.g.offset == 8 and V0.typ.offset == 16 and V0.u.offset == 24
+
+
+def test_tuning_knob_ids_match_the_header():
+    """The autotuner's knob ids are the HGPU_TUNE_* values include/hgpu.h
+    defines, one for one."""
+    from horsepower_gb300 import autotune as T
+    src = open(HEADER).read()
+    ids = {m.group(1).lower(): int(m.group(2)) for m in re.finditer(r"#define\s+HGPU_TUNE_(\w+)\s+(\d+)", src)}
+    assert ids and {k: v for k, (v, _) in T.KNOBS.items()} == ids
