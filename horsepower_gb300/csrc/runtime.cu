@@ -559,6 +559,7 @@ cudaError_t rb_init() {
 }
 
 I rb_queue(void* host_dst, const void* dev, size_t bytes) {
+    if (!g_rbmap) return set_error(E_DEVICE, "read-back: no mapped host area");
     const unsigned off = (g_rbused + 15u) & ~15u;
     if (g_rbl.n == RB_ITEMS || bytes > RB_BYTES || off + bytes > RB_BYTES)
         return set_error(E_DEVICE, "read-back: more than %d values or %u bytes queued before a wait", RB_ITEMS,
